@@ -1,0 +1,200 @@
+"""Seeded synthetic scenes for the benchmark workloads and parity cases.
+
+Each generator drives a *builder* with the flat creation calls that forge2d's
+RawBox2D seam exposes (createBody / createBoxShape / createCircleShape /
+createCapsuleShape / createPolygonShape / createRevoluteJoint,
+packages/forge2d/lib/src/backend/raw_box2d.dart:71-91, :320-385, :~700).
+The same generator therefore builds bit-identical scenes in the GPU world
+and in any CPU world that offers the same calls: every number is drawn once
+as a Python float and rounded to float32 by the callee, as forge2d's FFI
+backend does when it fills b2BodyDef / b2ShapeDef.
+
+Scenes:
+
+* ``pyramid``      -- 40-row pyramid of 820 unit boxes on a 100x2 static box.
+* ``pile``         -- mixed circles / capsules / convex polygons dropped into a
+                      static U-shaped container (the 100k-body pile and its
+                      scaled-down parity variants).
+* ``pyramids_chains`` -- side-by-side pyramids plus revolute-joint capsule
+                      chains hanging from static anchors.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+WORLD_DEFAULTS = dict(
+    gravityX=0.0, gravityY=-10.0, restitutionThreshold=1.0, hitEventThreshold=1.0,
+    contactHertz=30.0, contactDampingRatio=10.0, maxContactPushSpeed=3.0,
+    maximumLinearSpeed=400.0, enableSleep=1, enableContinuous=1,
+)
+
+BODY_DEFAULTS = dict(
+    type=0, positionX=0.0, positionY=0.0, rotationCos=1.0, rotationSin=0.0,
+    linearVelocityX=0.0, linearVelocityY=0.0, angularVelocity=0.0,
+    linearDamping=0.0, angularDamping=0.0, gravityScale=1.0, sleepThreshold=0.05,
+    enableSleep=1, isAwake=1, fixedRotation=0, isBullet=0, isEnabled=1,
+    allowFastRotation=0,
+)
+
+SHAPE_DEFAULTS = dict(
+    friction=0.6, restitution=0.0, rollingResistance=0.0, tangentSpeed=0.0,
+    density=1.0, categoryBits=1, maskBits=-1, groupIndex=0, userMaterialId=0,
+    isSensor=0, enableSensorEvents=0, enableContactEvents=0, enableHitEvents=0,
+    enablePreSolveEvents=0, invokeContactCreation=1, updateBodyMass=1,
+)
+
+REVOLUTE_DEFAULTS = dict(
+    bodyA=0, bodyB=0, localAnchorAX=0.0, localAnchorAY=0.0, localAnchorBX=0.0,
+    localAnchorBY=0.0, referenceAngle=0.0, targetAngle=0.0, enableSpring=0,
+    hertz=0.0, dampingRatio=0.0, enableLimit=0, lowerAngle=0.0, upperAngle=0.0,
+    enableMotor=0, maxMotorTorque=0.0, motorSpeed=0.0, drawSize=0.25,
+    collideConnected=0,
+)
+
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+
+
+def world_def(**kw):
+    d = dict(WORLD_DEFAULTS)
+    d.update(kw)
+    return d
+
+
+def body_def(**kw):
+    d = dict(BODY_DEFAULTS)
+    d.update(kw)
+    return d
+
+
+def shape_def(**kw):
+    d = dict(SHAPE_DEFAULTS)
+    d.update(kw)
+    return d
+
+
+def revolute_def(**kw):
+    d = dict(REVOLUTE_DEFAULTS)
+    d.update(kw)
+    return d
+
+
+def pyramid(b, rows=40, x0=None, y0=0.0, ground=True, half=0.5, friction=0.6,
+            density=1.0, restitution=0.0, **shape_kw):
+    """BASELINE config 1 layout: row r has rows-r boxes, spacing 1.0, offset
+    0.5 per row, resting on a static box 100x2 centred at y=-1."""
+    ids = []
+    if ground:
+        g = b.create_body(body_def(type=STATIC, positionX=0.0 if x0 is None else x0 + rows / 2 - 0.5,
+                                   positionY=y0 - 1.0))
+        b.create_box(g, shape_def(), 50.0, 1.0)
+    if x0 is None:
+        x0 = -(rows - 1) * 0.5
+    sd = shape_def(friction=friction, density=density, restitution=restitution, **shape_kw)
+    for r in range(rows):
+        for i in range(rows - r):
+            body = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 0.5 * r + i,
+                                          positionY=y0 + 0.5 + r))
+            b.create_box(body, sd, half, half)
+            ids.append(body)
+    return ids
+
+
+def _polygon_points(rng, n, radius):
+    """n vertices on a jittered circle (angles perturbed, CCW)."""
+    base = np.linspace(0.0, 2.0 * math.pi, n, endpoint=False)
+    jitter = rng.uniform(-0.3, 0.3, n) * (2.0 * math.pi / n)
+    ang = np.sort(base + jitter)
+    rad = radius * rng.uniform(0.85, 1.0, n)
+    return [(float(rad[k] * math.cos(ang[k])), float(rad[k] * math.sin(ang[k]))) for k in range(n)]
+
+
+def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
+         frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False):
+    """BASELINE config 2: ``count`` bodies drawn from ``seed`` -- 40% circles
+    r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
+    30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
+    uniform spawn in a width x height region above a static U-shaped
+    container of three boxes; density 1, friction 0.6, restitution U[0,0.3]."""
+    rng = np.random.default_rng(seed)
+    hw = 0.5 * width
+    if wall_height is None:
+        wall_height = 0.5 * height
+    if with_container:
+        c = b.create_body(body_def(type=STATIC))
+        sd = shape_def()
+        b.create_box(c, sd, hw + 5.0, 1.0, 0.0, -1.0, 1.0, 0.0, 0.0)          # floor
+        b.create_box(c, sd, 1.0, wall_height, -hw - 1.0, wall_height, 1.0, 0.0, 0.0)  # left wall
+        b.create_box(c, sd, 1.0, wall_height, hw + 1.0, wall_height, 1.0, 0.0, 0.0)   # right wall
+    kinds = rng.random(count)
+    xs = rng.uniform(-hw + 1.0, hw - 1.0, count)
+    ys = rng.uniform(1.0, 1.0 + height, count)
+    angles = rng.uniform(-math.pi, math.pi, count)
+    rest = rng.uniform(0.0, 0.3, count)
+    ids = []
+    for k in range(count):
+        a = float(angles[k])
+        body = b.create_body(body_def(type=DYNAMIC, positionX=float(xs[k]), positionY=float(ys[k]),
+                                      rotationCos=math.cos(a), rotationSin=math.sin(a)))
+        sd = shape_def(restitution=float(rest[k]), enableHitEvents=int(enable_hit_events))
+        u = kinds[k]
+        if u < frac_circle:
+            b.create_circle(body, sd, 0.0, 0.0, float(rng.uniform(0.25, 0.75)))
+        elif u < frac_circle + frac_capsule:
+            hl = float(rng.uniform(0.2, 0.8))
+            r = float(rng.uniform(0.15, 0.4))
+            b.create_capsule(body, sd, -hl, 0.0, hl, 0.0, r)
+        else:
+            n = int(rng.integers(3, 9))
+            pts = _polygon_points(rng, n, float(rng.uniform(0.3, 0.8)))
+            if b.create_polygon(body, sd, pts, 0.0) < 0:
+                b.create_circle(body, sd, 0.0, 0.0, 0.5)
+        ids.append(body)
+    return ids
+
+
+def chain(b, anchor_x, anchor_y, links=50, half_length=0.25, radius=0.1, density=1.0):
+    """A chain of capsule links hanging from a static anchor by revolute
+    joints; the first joint pins link 0 to the anchor body."""
+    anchor = b.create_body(body_def(type=STATIC, positionX=anchor_x, positionY=anchor_y))
+    sd = shape_def(density=density)
+    prev = anchor
+    prev_anchor = (0.0, 0.0)
+    pitch = 2.0 * half_length
+    for k in range(links):
+        x = anchor_x + half_length + k * pitch
+        body = b.create_body(body_def(type=DYNAMIC, positionX=x, positionY=anchor_y))
+        b.create_capsule(body, sd, -half_length, 0.0, half_length, 0.0, radius)
+        b.create_revolute(revolute_def(bodyA=prev, bodyB=body, localAnchorAX=prev_anchor[0],
+                                       localAnchorAY=prev_anchor[1], localAnchorBX=-half_length,
+                                       localAnchorBY=0.0))
+        prev = body
+        prev_anchor = (half_length, 0.0)
+    return anchor
+
+
+def pyramids_chains(b, pyramids=64, rows=40, chains=200, links=50, gap=2.0):
+    """BASELINE config 3: ``pyramids`` copies of the 40-row pyramid side by
+    side ``gap`` units apart plus ``chains`` revolute chains of ``links``
+    capsule links (half-length 0.25, r 0.1) fixed to static anchors."""
+    pitch = rows + gap
+    g = b.create_body(body_def(type=STATIC, positionX=0.0, positionY=-1.0))
+    total = pyramids * pitch
+    b.create_box(g, shape_def(), 0.5 * total + 10.0, 1.0)
+    left = -0.5 * total
+    for p in range(pyramids):
+        pyramid(b, rows=rows, x0=left + p * pitch + 0.5, ground=False)
+    span = total / max(chains, 1)
+    for c in range(chains):
+        chain(b, left + (c + 0.25) * span, rows + 20.0 + 1.0 * (c % 2), links=links)
+
+
+def build(b, name, **kw):
+    if name == "pyramid":
+        return pyramid(b, **kw)
+    if name == "pile":
+        return pile(b, **kw)
+    if name == "pyramids_chains":
+        return pyramids_chains(b, **kw)
+    raise ValueError(name)

@@ -1,0 +1,341 @@
+"""ctypes front end of the two CPU oracles. TEST INFRASTRUCTURE ONLY.
+
+* ``RefWorld`` drives the unmodified Box2D v3.1.1 C library that forge2d
+  vendors (packages/forge2d/third_party/box2d), compiled into
+  ``oracle/_ref/libbox2d_ref.so`` together with ``oracle/ref_harness.c``.
+  It exists only where the reference checkout exists (this build container).
+* ``PortWorld`` drives ``oracle/_build/libf2d_port.so``, the plain-C
+  restatement in ``oracle/port/`` that travels with the repository and is the
+  parity checker and CPU baseline on machines without the reference.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline arm may
+import this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SO = os.path.join(HERE, "_ref", "libbox2d_ref.so")
+PORT_SO = os.path.join(HERE, "_build", "libf2d_port.so")
+REF_B2 = "/root/reference/packages/forge2d/third_party/box2d"
+
+BODY_STRIDE = 12
+CONTACT_INTS = 9
+CONTACT_FLOATS = 25
+
+
+class WorldDef(C.Structure):
+    _fields_ = [
+        ("gravityX", C.c_double), ("gravityY", C.c_double),
+        ("restitutionThreshold", C.c_double), ("hitEventThreshold", C.c_double),
+        ("contactHertz", C.c_double), ("contactDampingRatio", C.c_double),
+        ("maxContactPushSpeed", C.c_double), ("maximumLinearSpeed", C.c_double),
+        ("enableSleep", C.c_int32), ("enableContinuous", C.c_int32),
+    ]
+
+
+class BodyDef(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("pad0", C.c_int32),
+        ("positionX", C.c_double), ("positionY", C.c_double),
+        ("rotationCos", C.c_double), ("rotationSin", C.c_double),
+        ("linearVelocityX", C.c_double), ("linearVelocityY", C.c_double),
+        ("angularVelocity", C.c_double), ("linearDamping", C.c_double),
+        ("angularDamping", C.c_double), ("gravityScale", C.c_double),
+        ("sleepThreshold", C.c_double),
+        ("enableSleep", C.c_int32), ("isAwake", C.c_int32),
+        ("fixedRotation", C.c_int32), ("isBullet", C.c_int32),
+        ("isEnabled", C.c_int32), ("allowFastRotation", C.c_int32),
+    ]
+
+
+class ShapeDef(C.Structure):
+    _fields_ = [
+        ("friction", C.c_double), ("restitution", C.c_double),
+        ("rollingResistance", C.c_double), ("tangentSpeed", C.c_double),
+        ("density", C.c_double),
+        ("categoryBits", C.c_int64), ("maskBits", C.c_int64),
+        ("groupIndex", C.c_int32), ("userMaterialId", C.c_int32),
+        ("isSensor", C.c_int32), ("enableSensorEvents", C.c_int32),
+        ("enableContactEvents", C.c_int32), ("enableHitEvents", C.c_int32),
+        ("enablePreSolveEvents", C.c_int32), ("invokeContactCreation", C.c_int32),
+        ("updateBodyMass", C.c_int32), ("pad0", C.c_int32),
+    ]
+
+
+class RevoluteDef(C.Structure):
+    _fields_ = [
+        ("bodyA", C.c_int32), ("bodyB", C.c_int32),
+        ("localAnchorAX", C.c_double), ("localAnchorAY", C.c_double),
+        ("localAnchorBX", C.c_double), ("localAnchorBY", C.c_double),
+        ("referenceAngle", C.c_double), ("targetAngle", C.c_double),
+        ("enableSpring", C.c_int32), ("pad0", C.c_int32),
+        ("hertz", C.c_double), ("dampingRatio", C.c_double),
+        ("enableLimit", C.c_int32), ("pad1", C.c_int32),
+        ("lowerAngle", C.c_double), ("upperAngle", C.c_double),
+        ("enableMotor", C.c_int32), ("pad2", C.c_int32),
+        ("maxMotorTorque", C.c_double), ("motorSpeed", C.c_double),
+        ("drawSize", C.c_double),
+        ("collideConnected", C.c_int32), ("pad3", C.c_int32),
+    ]
+
+
+def _fill(struct, values: dict):
+    for k, v in values.items():
+        setattr(struct, k, v)
+    return struct
+
+
+def build_ref(quiet=True) -> bool:
+    """Compile the reference library in place (needs the reference tree)."""
+    if not os.path.isdir(REF_B2):
+        return os.path.exists(REF_SO)
+    r = subprocess.run(["make", "-C", HERE, "ref", "-j8"], capture_output=quiet)
+    return r.returncode == 0 and os.path.exists(REF_SO)
+
+
+def build_port(quiet=True) -> bool:
+    r = subprocess.run(["make", "-C", HERE, "port", "-j8"], capture_output=quiet)
+    return r.returncode == 0 and os.path.exists(PORT_SO)
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO) or os.path.isdir(REF_B2)
+
+
+_P = C.POINTER
+
+
+def _bind(lib, prefix):
+    d = C.c_double
+    i = C.c_int
+    sig = {
+        "create_world": (i, [_P(WorldDef), i]),
+        "destroy_world": (None, [i]),
+        "world_step": (None, [i, d, i]),
+        "world_step_timed": (d, [i, d, i, i]),
+        "create_body": (i, [i, _P(BodyDef)]),
+        "create_circle_shape": (i, [i, i, _P(ShapeDef), d, d, d]),
+        "create_capsule_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d]),
+        "create_segment_shape": (i, [i, i, _P(ShapeDef), d, d, d, d]),
+        "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
+        "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
+        "create_revolute_joint": (i, [i, _P(RevoluteDef)]),
+        "body_capacity": (i, [i]),
+        "get_bodies": (i, [i, _P(C.c_float), i]),
+        "contact_capacity": (i, [i]),
+        "get_contacts": (i, [i, _P(i), _P(C.c_float), i]),
+        "shape_capacity": (i, [i]),
+        "get_shapes": (i, [i, _P(C.c_float), _P(i), i]),
+        "get_mass": (i, [i, _P(C.c_float), i]),
+        "get_polygon": (i, [i, i, _P(C.c_float)]),
+        "get_color_counts": (None, [i, _P(i)]),
+        "awake_body_count": (i, [i]),
+        "event_counts": (None, [i, _P(i)]),
+        "get_begin_events": (i, [i, _P(i), i]),
+        "get_end_events": (i, [i, _P(i), i]),
+        "get_hit_events": (i, [i, _P(i), _P(C.c_float), i]),
+        "get_move_events": (i, [i, _P(i), _P(C.c_float), i]),
+        "cast_ray_closest": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), _P(C.c_float)]),
+        "overlap_aabb": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), i]),
+        "joint_color": (i, [i, i]),
+    }
+    out = {}
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, prefix + name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+        out[name] = fn
+    return out
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_P(C.c_float))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(_P(C.c_int))
+
+
+class _CpuWorld:
+    """Common driver for ref_* and orc_* libraries (same flat signatures)."""
+
+    _lib = None
+    _fns = None
+    prefix = ""
+
+    def __init__(self, world_def: dict, workers: int = 1):
+        wd = _fill(WorldDef(), world_def)
+        self.w = self._fns["create_world"](C.byref(wd), int(workers))
+        if self.w < 0:
+            raise RuntimeError("world table full")
+
+    def close(self):
+        if self.w is not None and self.w >= 0:
+            self._fns["destroy_world"](self.w)
+            self.w = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # creation ---------------------------------------------------------
+    def create_body(self, body_def: dict) -> int:
+        return self._fns["create_body"](self.w, C.byref(_fill(BodyDef(), body_def)))
+
+    def create_circle(self, body, sd, cx, cy, r):
+        return self._fns["create_circle_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), cx, cy, r)
+
+    def create_capsule(self, body, sd, x1, y1, x2, y2, r):
+        return self._fns["create_capsule_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), x1, y1, x2, y2, r)
+
+    def create_segment(self, body, sd, x1, y1, x2, y2):
+        return self._fns["create_segment_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), x1, y1, x2, y2)
+
+    def create_box(self, body, sd, hx, hy, cx=0.0, cy=0.0, c=1.0, s=0.0, radius=0.0):
+        return self._fns["create_box_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), hx, hy, cx, cy, c, s, radius)
+
+    def create_polygon(self, body, sd, points, radius=0.0):
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1))
+        return self._fns["create_polygon_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)),
+                                                 pts.ctypes.data_as(_P(C.c_double)), len(pts) // 2, radius)
+
+    def create_revolute(self, jd: dict) -> int:
+        return self._fns["create_revolute_joint"](self.w, C.byref(_fill(RevoluteDef(), jd)))
+
+    # stepping ---------------------------------------------------------
+    def step(self, dt=1.0 / 60.0, substeps=4):
+        self._fns["world_step"](self.w, dt, substeps)
+
+    def step_timed(self, dt, substeps, steps) -> float:
+        return self._fns["world_step_timed"](self.w, dt, substeps, steps)
+
+    # dumps ------------------------------------------------------------
+    def bodies(self) -> np.ndarray:
+        n = self._fns["body_capacity"](self.w)
+        out = np.zeros((max(n, 1), BODY_STRIDE), np.float32)
+        self._fns["get_bodies"](self.w, _fptr(out), n)
+        return out[:n]
+
+    def contacts(self):
+        n = self._fns["contact_capacity"](self.w)
+        ints = np.zeros((max(n, 1), CONTACT_INTS), np.int32)
+        fl = np.zeros((max(n, 1), CONTACT_FLOATS), np.float32)
+        m = self._fns["get_contacts"](self.w, _iptr(ints), _fptr(fl), n)
+        return ints[:m], fl[:m]
+
+    def shapes(self):
+        n = self._fns["shape_capacity"](self.w)
+        fl = np.zeros((max(n, 1), 8), np.float32)
+        ints = np.zeros((max(n, 1), 4), np.int32)
+        self._fns["get_shapes"](self.w, _fptr(fl), _iptr(ints), n)
+        return fl[:n], ints[:n]
+
+    def mass(self) -> np.ndarray:
+        n = self._fns["body_capacity"](self.w)
+        out = np.zeros((max(n, 1), 8), np.float32)
+        self._fns["get_mass"](self.w, _fptr(out), n)
+        return out[:n]
+
+    def polygon(self, shape) -> np.ndarray:
+        out = np.zeros(36, np.float32)
+        self._fns["get_polygon"](self.w, shape, _fptr(out))
+        return out
+
+    def color_counts(self) -> np.ndarray:
+        out = np.zeros(24, np.int32)
+        self._fns["get_color_counts"](self.w, _iptr(out))
+        return out[:12]
+
+    def event_counts(self):
+        out = np.zeros(4, np.int32)
+        self._fns["event_counts"](self.w, _iptr(out))
+        return out
+
+    def begin_events(self):
+        n = int(self.event_counts()[0])
+        out = np.zeros((max(n, 1), 2), np.int32)
+        m = self._fns["get_begin_events"](self.w, _iptr(out), n)
+        return out[:m]
+
+    def end_events(self):
+        n = int(self.event_counts()[1])
+        out = np.zeros((max(n, 1), 2), np.int32)
+        m = self._fns["get_end_events"](self.w, _iptr(out), n)
+        return out[:m]
+
+    def hit_events(self):
+        n = int(self.event_counts()[2])
+        ints = np.zeros((max(n, 1), 2), np.int32)
+        fl = np.zeros((max(n, 1), 5), np.float32)
+        m = self._fns["get_hit_events"](self.w, _iptr(ints), _fptr(fl), n)
+        return ints[:m], fl[:m]
+
+    def move_events(self):
+        n = int(self.event_counts()[3])
+        ints = np.zeros((max(n, 1), 2), np.int32)
+        fl = np.zeros((max(n, 1), 4), np.float32)
+        m = self._fns["get_move_events"](self.w, _iptr(ints), _fptr(fl), n)
+        return ints[:m], fl[:m]
+
+    def cast_ray_closest(self, ox, oy, tx, ty, cat=1, mask=-1):
+        shape = C.c_int(-1)
+        out = np.zeros(5, np.float32)
+        hit = self._fns["cast_ray_closest"](self.w, ox, oy, tx, ty, cat, mask, C.byref(shape), _fptr(out))
+        if not hit:
+            return None
+        return shape.value, out
+
+    def overlap_aabb(self, lx, ly, ux, uy, cat=1, mask=-1):
+        cap = 4096
+        out = np.zeros(cap, np.int32)
+        n = self._fns["overlap_aabb"](self.w, lx, ly, ux, uy, cat, mask, _iptr(out), cap)
+        return out[:min(n, cap)]
+
+    def joint_color(self, j):
+        return self._fns["joint_color"](self.w, j)
+
+    def awake_body_count(self):
+        return self._fns["awake_body_count"](self.w)
+
+
+class RefWorld(_CpuWorld):
+    prefix = "ref_"
+
+    def __init__(self, world_def, workers=1):
+        if RefWorld._lib is None:
+            if not os.path.exists(REF_SO) and not build_ref():
+                raise RuntimeError("reference library unavailable")
+            RefWorld._lib = C.CDLL(REF_SO)
+            RefWorld._fns = _bind(RefWorld._lib, "ref_")
+        super().__init__(world_def, workers)
+
+
+class PortWorld(_CpuWorld):
+    prefix = "orc_"
+
+    def __init__(self, world_def, workers=1):
+        if PortWorld._lib is None:
+            if not os.path.exists(PORT_SO) and not build_port():
+                raise RuntimeError("port library failed to build")
+            PortWorld._lib = C.CDLL(PORT_SO)
+            PortWorld._fns = _bind(PortWorld._lib, "orc_")
+            lib = PortWorld._lib
+            lib.orc_set_contact_plan.restype = None
+            lib.orc_set_contact_plan.argtypes = [C.c_int, _P(C.c_int), C.c_int]
+        super().__init__(world_def, workers)
+
+    def set_contact_plan(self, plan: np.ndarray):
+        """Parity mode: contacts created during the next step take the given
+        ids. ``plan`` rows are (contactId, shapeIdA, shapeIdB)."""
+        plan = np.ascontiguousarray(plan, dtype=np.int32).reshape(-1, 3)
+        PortWorld._lib.orc_set_contact_plan(self.w, _iptr(plan), len(plan))

@@ -1,0 +1,94 @@
+// Flattened definition records shared by the two CPU oracles (the reference
+// harness oracle/ref_harness.c and the restatement oracle/port/). TEST
+// INFRASTRUCTURE ONLY. The product's C-ABI (include/forge2d_gb300.h) declares
+// records with the same field order so one Python scene builder can drive all
+// three; this header is never included by product code.
+//
+// Field meaning follows forge2d's RawBox2D seam: RawBox2D.createWorld
+// (packages/forge2d/lib/src/backend/raw_box2d.dart:18-29), createBody (:71-91)
+// and RawShapeDef (raw_box2d_ffi.dart:564-584 shows the b2ShapeDef mapping).
+#pragma once
+
+#include <stdint.h>
+
+typedef struct f2d_world_def
+{
+	double gravityX, gravityY;
+	double restitutionThreshold;
+	double hitEventThreshold;
+	double contactHertz;
+	double contactDampingRatio;
+	double maxContactPushSpeed;
+	double maximumLinearSpeed;
+	int32_t enableSleep;
+	int32_t enableContinuous;
+} f2d_world_def;
+
+typedef struct f2d_body_def
+{
+	int32_t type; // 0 static, 1 kinematic, 2 dynamic (b2BodyType)
+	int32_t pad0;
+	double positionX, positionY;
+	double rotationCos, rotationSin;
+	double linearVelocityX, linearVelocityY;
+	double angularVelocity;
+	double linearDamping;
+	double angularDamping;
+	double gravityScale;
+	double sleepThreshold;
+	int32_t enableSleep;
+	int32_t isAwake;
+	int32_t fixedRotation;
+	int32_t isBullet;
+	int32_t isEnabled;
+	int32_t allowFastRotation;
+} f2d_body_def;
+
+typedef struct f2d_shape_def
+{
+	double friction;
+	double restitution;
+	double rollingResistance;
+	double tangentSpeed;
+	double density;
+	int64_t categoryBits;
+	int64_t maskBits;
+	int32_t groupIndex;
+	int32_t userMaterialId;
+	int32_t isSensor;
+	int32_t enableSensorEvents;
+	int32_t enableContactEvents;
+	int32_t enableHitEvents;
+	int32_t enablePreSolveEvents;
+	int32_t invokeContactCreation;
+	int32_t updateBodyMass;
+	int32_t pad0;
+} f2d_shape_def;
+
+typedef struct f2d_revolute_def
+{
+	int32_t bodyA, bodyB; // 0-based body ids
+	double localAnchorAX, localAnchorAY;
+	double localAnchorBX, localAnchorBY;
+	double referenceAngle;
+	double targetAngle;
+	int32_t enableSpring;
+	int32_t pad0;
+	double hertz;
+	double dampingRatio;
+	int32_t enableLimit;
+	int32_t pad1;
+	double lowerAngle, upperAngle;
+	int32_t enableMotor;
+	int32_t pad2;
+	double maxMotorTorque;
+	double motorSpeed;
+	double drawSize;
+	int32_t collideConnected;
+	int32_t pad3;
+} f2d_revolute_def;
+
+// Dump strides used by the ref_get_* / orc_get_* state readers.
+#define F2D_BODY_DUMP_STRIDE 12
+#define F2D_CONTACT_DUMP_INTS 9
+#define F2D_CONTACT_DUMP_FLOATS 25

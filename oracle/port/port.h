@@ -1,0 +1,332 @@
+// Internal types of the CPU restatement of Box2D v3.1.1's world step.
+// TEST INFRASTRUCTURE (oracle): the parity checker for the CUDA path and the
+// CPU baseline on machines without the reference checkout. Each function in
+// the .c files cites the reference file:line it restates
+// (packages/forge2d/third_party/box2d/src/...).
+#pragma once
+
+#include "f2d_defs.h"
+#include "pmath.h"
+
+enum
+{
+	SHAPE_CIRCLE = 0,
+	SHAPE_CAPSULE = 1,
+	SHAPE_SEGMENT = 2,
+	SHAPE_POLYGON = 3,
+	SHAPE_CHAIN_SEGMENT = 4,
+};
+
+enum
+{
+	BODY_STATIC = 0,
+	BODY_KINEMATIC = 1,
+	BODY_DYNAMIC = 2,
+};
+
+typedef struct Polygon
+{
+	v2 vertices[P_MAX_POLY];
+	v2 normals[P_MAX_POLY];
+	v2 centroid;
+	float radius;
+	int count;
+} Polygon;
+
+typedef struct Geometry
+{
+	int type;
+	// circle: c1 = center; capsule: c1, c2, radius; segment: c1, c2
+	v2 c1, c2;
+	float radius;
+	Polygon poly;
+} Geometry;
+
+typedef struct MassData
+{
+	float mass;
+	v2 center;
+	float rotationalInertia;
+} MassData;
+
+typedef struct ManifoldPoint
+{
+	v2 point;
+	v2 anchorA, anchorB;
+	float separation;
+	float normalImpulse;
+	float tangentImpulse;
+	float totalNormalImpulse;
+	float normalVelocity;
+	uint16_t id;
+	bool persisted;
+} ManifoldPoint;
+
+typedef struct Manifold
+{
+	v2 normal;
+	float rollingImpulse;
+	ManifoldPoint points[2];
+	int pointCount;
+} Manifold;
+
+typedef struct Body
+{
+	int used;
+	int generation;
+	int type;
+	int enabled;
+	// sim (body.h:120-159)
+	xform xf;
+	v2 center;
+	rot rotation0;
+	v2 center0;
+	v2 localCenter;
+	v2 force;
+	float torque;
+	float invMass, invInertia;
+	float minExtent, maxExtent;
+	float linearDamping, angularDamping, gravityScale;
+	float mass, inertia;
+	int isBullet, isSpeedCapped, allowFastRotation, isFast, enlargeAABB, fixedRotation;
+	// state (body.h:101-113)
+	v2 v;
+	float w;
+	v2 dp;
+	rot dq;
+	// topology
+	int headShape;
+	int shapeCount;
+	int headJoint; // joint key list: (jointId << 1) | edge
+	int jointCount;
+	float sleepThreshold, sleepTime;
+	int enableSleep;
+	// constraint-graph membership: bit c set when the body holds a
+	// constraint in colour c < P_OVERFLOW (constraint_graph.c bodySet bitsets)
+	uint16_t colorMask;
+} Body;
+
+typedef struct Shape
+{
+	int used;
+	int generation;
+	int bodyId;
+	Geometry g;
+	float density, friction, restitution, rollingResistance, tangentSpeed;
+	int userMaterialId;
+	uint64_t categoryBits, maskBits;
+	int groupIndex;
+	int isSensor, enableContactEvents, enableHitEvents, enableSensorEvents, enablePreSolveEvents;
+	box2 aabb, fatAABB;
+	int enlarged;
+	int moved; // in the move buffer (broad_phase.h:74-82)
+	int proxyKey;
+	v2 localCentroid;
+	int nextShape, prevShape;
+} Shape;
+
+enum
+{
+	SIM_TOUCHING = 0x00010000,
+	SIM_DISJOINT = 0x00020000,
+	SIM_STARTED = 0x00040000,
+	SIM_STOPPED = 0x00080000,
+	SIM_HIT_EVENT = 0x00100000,
+	SIM_PRESOLVE = 0x00200000,
+};
+
+typedef struct Contact
+{
+	int used;
+	int shapeA, shapeB;
+	int bodyA, bodyB;
+	int touchingFlag;	  // b2_contactTouchingFlag on b2Contact
+	int enableContactEvents; // b2_contactEnableContactEvents
+	uint32_t simFlags;
+	int color;		   // -1 when not touching
+	int overflowIndex; // position in the overflow array when color == P_OVERFLOW
+	float friction, restitution, rollingResistance, tangentSpeed;
+	float invMassA, invIA, invMassB, invIB;
+	Manifold m;
+} Contact;
+
+// Per-constraint solver data (contact_solver.c:1034-1064 lanes / contact_solver.h)
+typedef struct ConstraintPoint
+{
+	v2 anchorA, anchorB;
+	float baseSeparation;
+	float relativeVelocity;
+	float normalImpulse;
+	float tangentImpulse;
+	float totalNormalImpulse;
+	float normalMass;
+	float tangentMass;
+} ConstraintPoint;
+
+typedef struct Constraint
+{
+	int contactId;
+	int indexA, indexB; // body ids, -1 for static
+	float invMassA, invIA, invMassB, invIB;
+	v2 normal;
+	float friction, restitution, tangentSpeed, rollingResistance, rollingMass, rollingImpulse;
+	float biasRate, massScale, impulseScale; // softness
+	ConstraintPoint points[2];
+	int pointCount;
+} Constraint;
+
+typedef struct Softness
+{
+	float biasRate, massScale, impulseScale;
+} Softness;
+
+typedef struct Joint
+{
+	int used;
+	int generation;
+	int type; // revolute only here
+	int bodyA, bodyB;
+	int color;
+	int overflowIndex;
+	int collideConnected;
+	int nextA, prevA, nextB, prevB; // body joint lists (joint keys)
+	// revolute definition (revolute_joint.c / joint.h:247-278)
+	v2 localOriginAnchorA, localOriginAnchorB;
+	float referenceAngle, targetAngle;
+	float hertz, dampingRatio;
+	float lowerAngle, upperAngle;
+	float maxMotorTorque, motorSpeed;
+	int enableSpring, enableLimit, enableMotor;
+	float drawSize;
+	float constraintHertz, constraintDampingRatio;
+	// solver state
+	v2 linearImpulse;
+	float springImpulse, motorImpulse, lowerImpulse, upperImpulse;
+	// prepared
+	int indexA, indexB;
+	v2 anchorA, anchorB;
+	v2 deltaCenter;
+	float deltaAngle;
+	float axialMass;
+	Softness springSoftness, constraintSoftness;
+	float invMassA, invMassB, invIA, invIB;
+} Joint;
+
+typedef struct TreeIds
+{
+	int* freeStack;
+	int freeCount;
+	int freeCap;
+	int nodeCount;
+	int proxyCount;
+} TreeIds;
+
+typedef struct PairSet
+{
+	uint64_t* keys; // 0 = empty, key+1 stored
+	int cap;
+	int count;
+} PairSet;
+
+typedef struct World
+{
+	int used;
+	f2d_world_def def;
+	v2 gravity;
+	float contactHertz, contactDampingRatio, maxContactPushSpeed, maximumLinearSpeed;
+	float restitutionThreshold, hitEventThreshold;
+	float contactSpeed, inv_h;
+	int enableSleep, enableContinuous, enableWarmStarting;
+
+	Body* bodies;
+	int bodyCount, bodyCap;
+	int* bodyFree;
+	int bodyFreeCount;
+
+	Shape* shapes;
+	int shapeCount, shapeCap;
+	int* shapeFree;
+	int shapeFreeCount;
+
+	Contact* contacts;
+	int contactCount, contactCap; // count = id capacity used
+	int* contactFree;
+	int contactFreeCount;
+
+	Joint* joints;
+	int jointCount, jointCap;
+	int* jointFree;
+	int jointFreeCount;
+
+	TreeIds trees[3];
+	PairSet pairs;
+
+	// move buffer in deterministic order (shape ids)
+	int* moveArray;
+	int moveCount, moveCap;
+
+	// overflow colour order (contact ids / joint ids) as the reference's
+	// colour-11 arrays keep them: append on add, swap-remove on remove
+	int* overflowContacts;
+	int overflowCount, overflowCap;
+	int* overflowJoints;
+	int overflowJointCount, overflowJointCap;
+
+	// parity plan: contact ids to use for pairs created in the next step
+	int* plan;
+	int planCount, planCap;
+
+	// scratch
+	Constraint* constraints;
+	int constraintCap;
+
+	// events of the last step
+	int* beginEvents; // pairs shapeA shapeB
+	int beginCount, beginCap;
+	int* endEvents;
+	int endCount, endCap;
+	int* hitShapes;
+	float* hitData;
+	int hitCount, hitCap;
+	int* moveEventBodies;
+	float* moveEventXf;
+	int moveEventCount, moveEventCap;
+
+	int stepIndex;
+} World;
+
+// geometry (pgeom.c)
+int p_compute_hull( const v2* points, int count, v2* hull );
+Polygon p_make_polygon( const v2* hull, int count, float radius );
+Polygon p_make_offset_rounded_box( float hx, float hy, v2 center, rot q, float radius );
+MassData p_shape_mass( const Shape* s );
+box2 p_shape_aabb( const Geometry* g, xform xf );
+v2 p_shape_centroid( const Geometry* g );
+void p_shape_extent( const Shape* s, v2 localCenter, float* minExtent, float* maxExtent );
+float p_shape_radius( const Geometry* g );
+
+// manifolds (pmanifold.c)
+Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB );
+int p_manifold_registered( int typeA, int typeB, int* primary );
+
+// distance / time of impact (pdistance.c)
+typedef struct ShapeProxy
+{
+	v2 points[P_MAX_POLY];
+	int count;
+	float radius;
+} ShapeProxy;
+typedef struct Sweep
+{
+	v2 localCenter;
+	v2 c1, c2;
+	rot q1, q2;
+} Sweep;
+ShapeProxy p_make_proxy( const v2* pts, int count, float radius );
+ShapeProxy p_shape_proxy( const Geometry* g );
+float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sweep sb, float maxFraction, int* state );
+
+// joints (pjoint.c)
+void p_prepare_joint( World* w, Joint* j, float h, float inv_h, Softness jointSoftness );
+void p_warm_start_joint( World* w, Joint* j );
+void p_solve_joint( World* w, Joint* j, float h, float inv_h, int useBias );

@@ -1,0 +1,1299 @@
+// World, creation path, broadphase pairs, narrowphase update, contact state
+// changes and constraint-graph colouring of the restatement. TEST
+// INFRASTRUCTURE (oracle). Reference files (packages/forge2d/third_party/
+// box2d/src/): world.c, body.c, shape.c, broad_phase.c, contact.c,
+// constraint_graph.c, id_pool.c.
+//
+// Contact creation order. The reference creates new contacts in broadphase
+// move-array order x dynamic-tree traversal order (broad_phase.c:376-474),
+// which only its incremental tree can reproduce. This port orders the pairs
+// found in a step by their 64-bit shape-pair key instead ("native order", the
+// same rule the CUDA path uses), and offers a parity mode (orc_set_contact_plan)
+// in which the caller dictates the contact id of each pair created in the next
+// step, e.g. the ids the reference itself assigned. Everything downstream of
+// the ids -- colour assignment, overflow order, events -- then follows the
+// reference's own rules.
+#include "port.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+#define MAX_WORLDS 64
+static World s_worlds[MAX_WORLDS];
+
+void p_solve( World* w, float dt, int subSteps ); // psolver.c
+
+static void* grow( void* p, int* cap, int need, size_t elem )
+{
+	if ( need <= *cap )
+		return p;
+	int nc = *cap < 16 ? 16 : *cap;
+	while ( nc < need )
+		nc *= 2;
+	void* q = realloc( p, (size_t)nc * elem );
+	memset( (char*)q + (size_t)( *cap ) * elem, 0, (size_t)( nc - *cap ) * elem );
+	*cap = nc;
+	return q;
+}
+
+World* p_world( int w )
+{
+	if ( w < 0 || w >= MAX_WORLDS || s_worlds[w].used == 0 )
+		return NULL;
+	return s_worlds + w;
+}
+
+// ---------------------------------------------------------------------------
+// pair set (table.c: open addressing keyed by B2_SHAPE_PAIR_KEY)
+// ---------------------------------------------------------------------------
+static uint64_t pair_key( int a, int b )
+{
+	return a < b ? ( (uint64_t)a << 32 ) | (uint64_t)b : ( (uint64_t)b << 32 ) | (uint64_t)a;
+}
+
+static uint32_t hash64( uint64_t k )
+{
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdULL;
+	k ^= k >> 33;
+	k *= 0xc4ceb9fe1a85ec53ULL;
+	k ^= k >> 33;
+	return (uint32_t)k;
+}
+
+static void pairset_rehash( PairSet* s, int ncap );
+
+static void pairset_add( PairSet* s, uint64_t key )
+{
+	if ( ( s->count + 1 ) * 2 > s->cap )
+		pairset_rehash( s, s->cap < 64 ? 128 : s->cap * 2 );
+	uint32_t m = (uint32_t)s->cap - 1;
+	uint32_t i = hash64( key ) & m;
+	while ( s->keys[i] != 0 )
+	{
+		if ( s->keys[i] == key + 1 )
+			return;
+		i = ( i + 1 ) & m;
+	}
+	s->keys[i] = key + 1;
+	s->count += 1;
+}
+
+static int pairset_contains( const PairSet* s, uint64_t key )
+{
+	if ( s->cap == 0 )
+		return 0;
+	uint32_t m = (uint32_t)s->cap - 1;
+	uint32_t i = hash64( key ) & m;
+	while ( s->keys[i] != 0 )
+	{
+		if ( s->keys[i] == key + 1 )
+			return 1;
+		i = ( i + 1 ) & m;
+	}
+	return 0;
+}
+
+static void pairset_remove( PairSet* s, uint64_t key )
+{
+	if ( s->cap == 0 )
+		return;
+	uint32_t m = (uint32_t)s->cap - 1;
+	uint32_t i = hash64( key ) & m;
+	while ( s->keys[i] != 0 )
+	{
+		if ( s->keys[i] == key + 1 )
+			break;
+		i = ( i + 1 ) & m;
+	}
+	if ( s->keys[i] == 0 )
+		return;
+	s->keys[i] = 0;
+	s->count -= 1;
+	// backward-shift deletion
+	uint32_t j = i;
+	while ( 1 )
+	{
+		j = ( j + 1 ) & m;
+		if ( s->keys[j] == 0 )
+			break;
+		uint32_t home = hash64( s->keys[j] - 1 ) & m;
+		int moveIt = ( i <= j ) ? ( home <= i || home > j ) : ( home <= i && home > j );
+		if ( moveIt )
+		{
+			s->keys[i] = s->keys[j];
+			s->keys[j] = 0;
+			i = j;
+		}
+	}
+}
+
+static void pairset_rehash( PairSet* s, int ncap )
+{
+	uint64_t* old = s->keys;
+	int oc = s->cap;
+	s->keys = calloc( (size_t)ncap, sizeof( uint64_t ) );
+	s->cap = ncap;
+	s->count = 0;
+	for ( int i = 0; i < oc; ++i )
+		if ( old[i] )
+			pairset_add( s, old[i] - 1 );
+	free( old );
+}
+
+// ---------------------------------------------------------------------------
+// dynamic-tree node ids (dynamic_tree.c:122-167, :625-800): a proxy takes a
+// leaf node, and a parent node when the tree already holds a proxy. Tree
+// rebuilds free and re-allocate the same number of internal nodes LIFO, so
+// they leave the free list unchanged and need no emulation.
+// ---------------------------------------------------------------------------
+static int tree_alloc( TreeIds* t )
+{
+	if ( t->freeCount > 0 )
+		return t->freeStack[--t->freeCount];
+	return t->nodeCount++;
+}
+
+static int tree_create_proxy( TreeIds* t )
+{
+	int leaf = tree_alloc( t );
+	if ( t->proxyCount > 0 )
+		(void)tree_alloc( t );
+	t->proxyCount += 1;
+	return leaf;
+}
+
+// ---------------------------------------------------------------------------
+// world lifecycle (world.c:100-340)
+// ---------------------------------------------------------------------------
+int orc_create_world( const f2d_world_def* d, int workerCount )
+{
+	(void)workerCount;
+	int slot = -1;
+	for ( int i = 0; i < MAX_WORLDS; ++i )
+		if ( s_worlds[i].used == 0 )
+		{
+			slot = i;
+			break;
+		}
+	if ( slot < 0 )
+		return -1;
+	World* w = s_worlds + slot;
+	memset( w, 0, sizeof( *w ) );
+	w->used = 1;
+	w->def = *d;
+	w->gravity = V( (float)d->gravityX, (float)d->gravityY );
+	w->restitutionThreshold = (float)d->restitutionThreshold;
+	w->hitEventThreshold = (float)d->hitEventThreshold;
+	w->contactHertz = (float)d->contactHertz;
+	w->contactDampingRatio = (float)d->contactDampingRatio;
+	w->maxContactPushSpeed = (float)d->maxContactPushSpeed;
+	w->maximumLinearSpeed = (float)d->maximumLinearSpeed;
+	w->enableSleep = d->enableSleep != 0;
+	w->enableContinuous = d->enableContinuous != 0;
+	w->enableWarmStarting = 1;
+	return slot;
+}
+
+void orc_destroy_world( int wi )
+{
+	World* w = p_world( wi );
+	if ( w == NULL )
+		return;
+	free( w->bodies );
+	free( w->bodyFree );
+	free( w->shapes );
+	free( w->shapeFree );
+	free( w->contacts );
+	free( w->contactFree );
+	free( w->joints );
+	free( w->jointFree );
+	for ( int i = 0; i < 3; ++i )
+		free( w->trees[i].freeStack );
+	free( w->pairs.keys );
+	free( w->moveArray );
+	free( w->overflowContacts );
+	free( w->overflowJoints );
+	free( w->plan );
+	free( w->constraints );
+	free( w->beginEvents );
+	free( w->endEvents );
+	free( w->hitShapes );
+	free( w->hitData );
+	free( w->moveEventBodies );
+	free( w->moveEventXf );
+	memset( w, 0, sizeof( *w ) );
+}
+
+// id_pool.c:19-38: LIFO free list
+static int alloc_id( int** freeList, int* freeCount, int* count )
+{
+	if ( *freeCount > 0 )
+	{
+		*freeCount -= 1;
+		return ( *freeList )[*freeCount];
+	}
+	int id = *count;
+	*count += 1;
+	return id;
+}
+
+// ---------------------------------------------------------------------------
+// bodies (body.c:177-330, :528-632)
+// ---------------------------------------------------------------------------
+int orc_create_body( int wi, const f2d_body_def* d )
+{
+	World* w = p_world( wi );
+	int cap = w->bodyCap;
+	int id = alloc_id( &w->bodyFree, &w->bodyFreeCount, &w->bodyCount );
+	w->bodies = grow( w->bodies, &cap, w->bodyCount, sizeof( Body ) );
+	w->bodyCap = cap;
+	Body* b = w->bodies + id;
+	int gen = b->generation;
+	memset( b, 0, sizeof( *b ) );
+	b->generation = gen + 1;
+	b->used = 1;
+	b->type = d->type;
+	b->enabled = d->isEnabled != 0;
+	b->xf.p = V( (float)d->positionX, (float)d->positionY );
+	b->xf.q.c = (float)d->rotationCos;
+	b->xf.q.s = (float)d->rotationSin;
+	b->center = b->xf.p;
+	b->rotation0 = b->xf.q;
+	b->center0 = b->center;
+	b->minExtent = P_HUGE;
+	b->maxExtent = 0.0f;
+	b->linearDamping = (float)d->linearDamping;
+	b->angularDamping = (float)d->angularDamping;
+	b->gravityScale = (float)d->gravityScale;
+	b->isBullet = d->isBullet != 0;
+	b->allowFastRotation = d->allowFastRotation != 0;
+	b->fixedRotation = d->fixedRotation != 0;
+	if ( b->type != BODY_STATIC )
+	{
+		b->v = V( (float)d->linearVelocityX, (float)d->linearVelocityY );
+		b->w = (float)d->angularVelocity;
+	}
+	b->dq.c = 1.0f;
+	b->dq.s = 0.0f;
+	b->headShape = P_NULL;
+	b->headJoint = P_NULL;
+	b->sleepThreshold = (float)d->sleepThreshold;
+	b->enableSleep = d->enableSleep != 0;
+	return id;
+}
+
+static void update_mass( World* w, Body* b )
+{
+	b->mass = 0.0f;
+	b->inertia = 0.0f;
+	b->invMass = 0.0f;
+	b->invInertia = 0.0f;
+	b->localCenter = V( 0.0f, 0.0f );
+	b->minExtent = P_HUGE;
+	b->maxExtent = 0.0f;
+	if ( b->type != BODY_DYNAMIC )
+	{
+		b->center = b->xf.p;
+		if ( b->type == BODY_KINEMATIC )
+		{
+			for ( int s = b->headShape; s != P_NULL; s = w->shapes[s].nextShape )
+			{
+				float mn, mx;
+				p_shape_extent( w->shapes + s, V( 0.0f, 0.0f ), &mn, &mx );
+				b->minExtent = fminp( b->minExtent, mn );
+				b->maxExtent = fmaxp( b->maxExtent, mx );
+			}
+		}
+		return;
+	}
+	v2 localCenter = V( 0.0f, 0.0f );
+	for ( int s = b->headShape; s != P_NULL; s = w->shapes[s].nextShape )
+	{
+		const Shape* sh = w->shapes + s;
+		if ( sh->density == 0.0f )
+			continue;
+		MassData md = p_shape_mass( sh );
+		b->mass += md.mass;
+		localCenter = mulAdd( localCenter, md.mass, md.center );
+		b->inertia += md.rotationalInertia;
+	}
+	if ( b->mass > 0.0f )
+	{
+		b->invMass = 1.0f / b->mass;
+		localCenter = mulSV( b->invMass, localCenter );
+	}
+	if ( b->inertia > 0.0f && b->fixedRotation == 0 )
+	{
+		b->inertia -= b->mass * dot( localCenter, localCenter );
+		b->invInertia = 1.0f / b->inertia;
+	}
+	else
+	{
+		b->inertia = 0.0f;
+		b->invInertia = 0.0f;
+	}
+	v2 oldCenter = b->center;
+	b->localCenter = localCenter;
+	b->center = xfPoint( b->xf, b->localCenter );
+	b->center0 = b->center;
+	// body.c:600-606: awake bodies carry velocity at the new centre
+	v2 deltaLinear = crossSV( b->w, sub( b->center, oldCenter ) );
+	b->v = add( b->v, deltaLinear );
+	for ( int s = b->headShape; s != P_NULL; s = w->shapes[s].nextShape )
+	{
+		float mn, mx;
+		p_shape_extent( w->shapes + s, localCenter, &mn, &mx );
+		b->minExtent = fminp( b->minExtent, mn );
+		b->maxExtent = fmaxp( b->maxExtent, mx );
+	}
+}
+
+// ---------------------------------------------------------------------------
+// shapes (shape.c:36-180, :901-925)
+// ---------------------------------------------------------------------------
+static void push_move( World* w, int shapeId )
+{
+	Shape* s = w->shapes + shapeId;
+	if ( s->moved )
+		return;
+	s->moved = 1;
+	w->moveArray = grow( w->moveArray, &w->moveCap, w->moveCount + 1, sizeof( int ) );
+	w->moveArray[w->moveCount++] = shapeId;
+}
+
+static int create_shape( World* w, int bodyId, const f2d_shape_def* d, const Geometry* g )
+{
+	int cap = w->shapeCap;
+	int id = alloc_id( &w->shapeFree, &w->shapeFreeCount, &w->shapeCount );
+	w->shapes = grow( w->shapes, &cap, w->shapeCount, sizeof( Shape ) );
+	w->shapeCap = cap;
+	Body* b = w->bodies + bodyId;
+	Shape* s = w->shapes + id;
+	int gen = s->generation;
+	memset( s, 0, sizeof( *s ) );
+	s->generation = gen + 1;
+	s->used = 1;
+	s->bodyId = bodyId;
+	s->g = *g;
+	s->density = (float)d->density;
+	s->friction = (float)d->friction;
+	s->restitution = (float)d->restitution;
+	s->rollingResistance = (float)d->rollingResistance;
+	s->tangentSpeed = (float)d->tangentSpeed;
+	s->userMaterialId = d->userMaterialId;
+	s->categoryBits = (uint64_t)d->categoryBits;
+	s->maskBits = (uint64_t)d->maskBits;
+	s->groupIndex = d->groupIndex;
+	s->isSensor = d->isSensor != 0;
+	s->enableContactEvents = d->enableContactEvents != 0;
+	s->enableHitEvents = d->enableHitEvents != 0;
+	s->enableSensorEvents = d->enableSensorEvents != 0;
+	s->enablePreSolveEvents = d->enablePreSolveEvents != 0;
+	s->localCentroid = p_shape_centroid( g );
+	s->proxyKey = P_NULL;
+	if ( b->enabled )
+	{
+		int proxyType = b->type;
+		box2 aabb = p_shape_aabb( &s->g, b->xf );
+		aabb.lo.x -= P_SPECULATIVE;
+		aabb.lo.y -= P_SPECULATIVE;
+		aabb.hi.x += P_SPECULATIVE;
+		aabb.hi.y += P_SPECULATIVE;
+		s->aabb = aabb;
+		float margin = proxyType == BODY_STATIC ? P_SPECULATIVE : P_AABB_MARGIN;
+		s->fatAABB.lo.x = aabb.lo.x - margin;
+		s->fatAABB.lo.y = aabb.lo.y - margin;
+		s->fatAABB.hi.x = aabb.hi.x + margin;
+		s->fatAABB.hi.y = aabb.hi.y + margin;
+		int proxyId = tree_create_proxy( w->trees + proxyType );
+		s->proxyKey = ( proxyId << 2 ) | proxyType;
+		int force = d->invokeContactCreation != 0 || d->isSensor != 0;
+		if ( proxyType != BODY_STATIC || force )
+			push_move( w, id );
+	}
+	if ( b->headShape != P_NULL )
+		w->shapes[b->headShape].prevShape = id;
+	s->prevShape = P_NULL;
+	s->nextShape = b->headShape;
+	b->headShape = id;
+	b->shapeCount += 1;
+	if ( d->updateBodyMass )
+		update_mass( w, b );
+	return id;
+}
+
+int orc_create_circle_shape( int wi, int body, const f2d_shape_def* d, double cx, double cy, double radius )
+{
+	Geometry g = { 0 };
+	g.type = SHAPE_CIRCLE;
+	g.c1 = V( (float)cx, (float)cy );
+	g.radius = (float)radius;
+	return create_shape( p_world( wi ), body, d, &g );
+}
+
+int orc_create_capsule_shape( int wi, int body, const f2d_shape_def* d, double x1, double y1, double x2, double y2,
+							  double radius )
+{
+	Geometry g = { 0 };
+	g.type = SHAPE_CAPSULE;
+	g.c1 = V( (float)x1, (float)y1 );
+	g.c2 = V( (float)x2, (float)y2 );
+	g.radius = (float)radius;
+	return create_shape( p_world( wi ), body, d, &g );
+}
+
+int orc_create_segment_shape( int wi, int body, const f2d_shape_def* d, double x1, double y1, double x2, double y2 )
+{
+	Geometry g = { 0 };
+	g.type = SHAPE_SEGMENT;
+	g.c1 = V( (float)x1, (float)y1 );
+	g.c2 = V( (float)x2, (float)y2 );
+	return create_shape( p_world( wi ), body, d, &g );
+}
+
+int orc_create_box_shape( int wi, int body, const f2d_shape_def* d, double hx, double hy, double cx, double cy,
+						  double c, double s, double radius )
+{
+	Geometry g = { 0 };
+	g.type = SHAPE_POLYGON;
+	rot q = { (float)c, (float)s };
+	g.poly = p_make_offset_rounded_box( (float)hx, (float)hy, V( (float)cx, (float)cy ), q, (float)radius );
+	return create_shape( p_world( wi ), body, d, &g );
+}
+
+int orc_create_polygon_shape( int wi, int body, const f2d_shape_def* d, const double* points, int count, double radius )
+{
+	if ( count > P_MAX_POLY )
+		return -1;
+	v2 pts[P_MAX_POLY], hull[P_MAX_POLY];
+	for ( int i = 0; i < count; ++i )
+		pts[i] = V( (float)points[2 * i], (float)points[2 * i + 1] );
+	int hc = p_compute_hull( pts, count, hull );
+	if ( hc == 0 )
+		return -1;
+	Geometry g = { 0 };
+	g.type = SHAPE_POLYGON;
+	g.poly = p_make_polygon( hull, hc, (float)radius );
+	return create_shape( p_world( wi ), body, d, &g );
+}
+
+// ---------------------------------------------------------------------------
+// joint exclusion (body.c:1861-1897 b2ShouldBodiesCollide)
+// ---------------------------------------------------------------------------
+static int should_bodies_collide( World* w, int ia, int ib )
+{
+	Body* a = w->bodies + ia;
+	Body* b = w->bodies + ib;
+	if ( a->type != BODY_DYNAMIC && b->type != BODY_DYNAMIC )
+		return 0;
+	int key, other;
+	if ( a->jointCount < b->jointCount )
+	{
+		key = a->headJoint;
+		other = ib;
+	}
+	else
+	{
+		key = b->headJoint;
+		other = ia;
+	}
+	while ( key != P_NULL )
+	{
+		int jid = key >> 1;
+		int edge = key & 1;
+		Joint* j = w->joints + jid;
+		int otherBody = edge == 0 ? j->bodyB : j->bodyA;
+		if ( j->collideConnected == 0 && otherBody == other )
+			return 0;
+		key = edge == 0 ? j->nextA : j->nextB;
+	}
+	return 1;
+}
+
+// shape.h:122-130
+static int should_shapes_collide( const Shape* a, const Shape* b )
+{
+	if ( a->groupIndex == b->groupIndex && a->groupIndex != 0 )
+		return a->groupIndex > 0;
+	return ( a->maskBits & b->categoryBits ) != 0 && ( a->categoryBits & b->maskBits ) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// contact creation (contact.c:186-330)
+// ---------------------------------------------------------------------------
+static int create_contact_with_id( World* w, int shapeIdA, int shapeIdB, int id )
+{
+	Shape* sa = w->shapes + shapeIdA;
+	Shape* sb = w->shapes + shapeIdB;
+	int primary;
+	if ( p_manifold_registered( sa->g.type, sb->g.type, &primary ) == 0 )
+		return -1;
+	if ( primary == 0 )
+	{
+		int t = shapeIdA;
+		shapeIdA = shapeIdB;
+		shapeIdB = t;
+		sa = w->shapes + shapeIdA;
+		sb = w->shapes + shapeIdB;
+	}
+	w->contacts = grow( w->contacts, &w->contactCap, id + 1, sizeof( Contact ) );
+	if ( id >= w->contactCount )
+	{
+		// ids between the old count and id become free (parity plans may skip)
+		for ( int k = w->contactCount; k < id; ++k )
+		{
+			w->contactFree = realloc( w->contactFree, sizeof( int ) * ( w->contactFreeCount + 1 ) );
+			w->contactFree[w->contactFreeCount++] = k;
+		}
+		w->contactCount = id + 1;
+	}
+	Contact* c = w->contacts + id;
+	memset( c, 0, sizeof( *c ) );
+	c->used = 1;
+	c->shapeA = shapeIdA;
+	c->shapeB = shapeIdB;
+	c->bodyA = sa->bodyId;
+	c->bodyB = sb->bodyId;
+	c->color = P_NULL;
+	c->overflowIndex = P_NULL;
+	c->enableContactEvents = ( sa->enableContactEvents || sb->enableContactEvents ) ? 1 : 0;
+	// world.c:88-98 default mixing: sqrt(fA*fB), max(rA, rB)
+	c->friction = sqrtf( sa->friction * sb->friction );
+	c->restitution = sa->restitution > sb->restitution ? sa->restitution : sb->restitution;
+	c->simFlags = 0;
+	if ( sa->enablePreSolveEvents || sb->enablePreSolveEvents )
+		c->simFlags |= SIM_PRESOLVE;
+	pairset_add( &w->pairs, pair_key( shapeIdA, shapeIdB ) );
+	return id;
+}
+
+static void free_contact_id( World* w, int id )
+{
+	w->contactFree = realloc( w->contactFree, sizeof( int ) * ( w->contactFreeCount + 1 ) );
+	w->contactFree[w->contactFreeCount++] = id;
+}
+
+static int take_contact_id( World* w, int id )
+{
+	// remove a specific id from the free list (parity mode)
+	for ( int k = w->contactFreeCount - 1; k >= 0; --k )
+	{
+		if ( w->contactFree[k] == id )
+		{
+			memmove( w->contactFree + k, w->contactFree + k + 1, sizeof( int ) * ( w->contactFreeCount - k - 1 ) );
+			w->contactFreeCount -= 1;
+			return 1;
+		}
+	}
+	return id >= w->contactCount;
+}
+
+void orc_set_contact_plan( int wi, const int* rows, int count )
+{
+	World* w = p_world( wi );
+	w->plan = grow( w->plan, &w->planCap, 3 * count, sizeof( int ) );
+	memcpy( w->plan, rows, sizeof( int ) * 3 * (size_t)count );
+	w->planCount = count;
+}
+
+// ---------------------------------------------------------------------------
+// broadphase pair finding (broad_phase.c:160-474). The reference queries its
+// dynamic trees with each moved proxy; the pair SET it produces is every
+// filter-passing pair with overlapping fat AABBs, at least one dynamic
+// proxy and at least one moved proxy, that has no contact yet. This port
+// finds the same set with a uniform grid (small proxies) plus a brute-force
+// list (large proxies).
+// ---------------------------------------------------------------------------
+typedef struct Cand
+{
+	uint64_t key;
+	int a, b; // ordered by proxy key: a has the smaller proxy key
+} Cand;
+
+static int cmp_cand( const void* x, const void* y )
+{
+	const Cand* a = x;
+	const Cand* b = y;
+	return a->key < b->key ? -1 : ( a->key > b->key ? 1 : 0 );
+}
+
+typedef struct GridEntry
+{
+	int64_t cell;
+	int shape;
+} GridEntry;
+
+static int cmp_grid( const void* x, const void* y )
+{
+	const GridEntry* a = x;
+	const GridEntry* b = y;
+	if ( a->cell != b->cell )
+		return a->cell < b->cell ? -1 : 1;
+	return a->shape - b->shape;
+}
+
+static int shape_active( World* w, int s )
+{
+	Shape* sh = w->shapes + s;
+	return sh->used && sh->proxyKey != P_NULL;
+}
+
+static void consider_pair( World* w, int s1, int s2, Cand** cands, int* n, int* cap )
+{
+	Shape* a = w->shapes + s1;
+	Shape* b = w->shapes + s2;
+	if ( a->moved == 0 && b->moved == 0 )
+		return;
+	int ta = a->proxyKey & 3, tb = b->proxyKey & 3;
+	if ( ta != BODY_DYNAMIC && tb != BODY_DYNAMIC )
+		return;
+	if ( boxOverlaps( a->fatAABB, b->fatAABB ) == 0 )
+		return;
+	uint64_t key = pair_key( s1, s2 );
+	if ( pairset_contains( &w->pairs, key ) )
+		return;
+	if ( a->bodyId == b->bodyId )
+		return;
+	if ( a->isSensor || b->isSensor )
+		return;
+	if ( should_shapes_collide( a, b ) == 0 )
+		return;
+	if ( should_bodies_collide( w, a->bodyId, b->bodyId ) == 0 )
+		return;
+	*cands = grow( *cands, cap, *n + 1, sizeof( Cand ) );
+	Cand* c = *cands + *n;
+	c->key = key;
+	if ( a->proxyKey < b->proxyKey )
+	{
+		c->a = s1;
+		c->b = s2;
+	}
+	else
+	{
+		c->a = s2;
+		c->b = s1;
+	}
+	*n += 1;
+}
+
+static void update_pairs( World* w )
+{
+	if ( w->moveCount == 0 )
+	{
+		w->planCount = 0;
+		return;
+	}
+	int ns = w->shapeCount;
+	// cell size: largest fat extent of non-static proxies, clamped
+	float cell = 0.0f;
+	for ( int s = 0; s < ns; ++s )
+	{
+		if ( !shape_active( w, s ) || ( w->shapes[s].proxyKey & 3 ) == BODY_STATIC )
+			continue;
+		box2 f = w->shapes[s].fatAABB;
+		cell = fmaxp( cell, fmaxp( f.hi.x - f.lo.x, f.hi.y - f.lo.y ) );
+	}
+	if ( cell < 0.5f )
+		cell = 0.5f;
+	float inv = 1.0f / cell;
+	int* large = NULL;
+	int nl = 0, capl = 0;
+	GridEntry* grid = NULL;
+	int ng = 0, capg = 0;
+	for ( int s = 0; s < ns; ++s )
+	{
+		if ( !shape_active( w, s ) )
+			continue;
+		box2 f = w->shapes[s].fatAABB;
+		if ( f.hi.x - f.lo.x > cell || f.hi.y - f.lo.y > cell )
+		{
+			large = grow( large, &capl, nl + 1, sizeof( int ) );
+			large[nl++] = s;
+			continue;
+		}
+		int64_t x0 = (int64_t)floorf( f.lo.x * inv ), x1 = (int64_t)floorf( f.hi.x * inv );
+		int64_t y0 = (int64_t)floorf( f.lo.y * inv ), y1 = (int64_t)floorf( f.hi.y * inv );
+		for ( int64_t x = x0; x <= x1; ++x )
+			for ( int64_t y = y0; y <= y1; ++y )
+			{
+				grid = grow( grid, &capg, ng + 1, sizeof( GridEntry ) );
+				grid[ng].cell = (int64_t)( ( (uint64_t)(uint32_t)x << 32 ) | (uint64_t)(uint32_t)y );
+				grid[ng].shape = s;
+				ng += 1;
+			}
+	}
+	qsort( grid, (size_t)ng, sizeof( GridEntry ), cmp_grid );
+	Cand* cands = NULL;
+	int nc = 0, capc = 0;
+	for ( int i = 0; i < ng; )
+	{
+		int j = i;
+		while ( j < ng && grid[j].cell == grid[i].cell )
+			++j;
+		for ( int p = i; p < j; ++p )
+			for ( int q = p + 1; q < j; ++q )
+				consider_pair( w, grid[p].shape, grid[q].shape, &cands, &nc, &capc );
+		i = j;
+	}
+	for ( int i = 0; i < nl; ++i )
+	{
+		for ( int s = 0; s < ns; ++s )
+		{
+			if ( s == large[i] || !shape_active( w, s ) )
+				continue;
+			// large-large pairs are visited twice; the sort+unique below drops repeats
+			consider_pair( w, large[i], s, &cands, &nc, &capc );
+		}
+	}
+	qsort( cands, (size_t)nc, sizeof( Cand ), cmp_cand );
+	int u = 0;
+	for ( int i = 0; i < nc; ++i )
+		if ( u == 0 || cands[u - 1].key != cands[i].key )
+			cands[u++] = cands[i];
+	nc = u;
+
+	// create contacts in native order (ascending pair key) or per plan
+	for ( int i = 0; i < nc; ++i )
+	{
+		int id = -1;
+		if ( w->planCount > 0 )
+		{
+			for ( int k = 0; k < w->planCount; ++k )
+			{
+				const int* row = w->plan + 3 * k;
+				if ( pair_key( row[1], row[2] ) == cands[i].key )
+				{
+					id = row[0];
+					break;
+				}
+			}
+		}
+		if ( id >= 0 )
+		{
+			take_contact_id( w, id );
+		}
+		else
+		{
+			id = alloc_id( &w->contactFree, &w->contactFreeCount, &w->contactCount );
+		}
+		create_contact_with_id( w, cands[i].a, cands[i].b, id );
+	}
+	// reset move buffer
+	for ( int i = 0; i < w->moveCount; ++i )
+		w->shapes[w->moveArray[i]].moved = 0;
+	w->moveCount = 0;
+	w->planCount = 0;
+	free( cands );
+	free( grid );
+	free( large );
+}
+
+// ---------------------------------------------------------------------------
+// narrowphase update (world.c:357-445 b2CollideTask, contact.c:472-600)
+// ---------------------------------------------------------------------------
+static void update_contact( World* w, Contact* c )
+{
+	Shape* sa = w->shapes + c->shapeA;
+	Shape* sb = w->shapes + c->shapeB;
+	if ( boxOverlaps( sa->fatAABB, sb->fatAABB ) == 0 )
+	{
+		c->simFlags |= SIM_DISJOINT;
+		c->simFlags &= ~SIM_TOUCHING;
+		return;
+	}
+	int wasTouching = ( c->simFlags & SIM_TOUCHING ) != 0;
+	Body* ba = w->bodies + sa->bodyId;
+	Body* bb = w->bodies + sb->bodyId;
+	c->invMassA = ba->invMass;
+	c->invIA = ba->invInertia;
+	c->invMassB = bb->invMass;
+	c->invIB = bb->invInertia;
+	xform xfA = ba->xf;
+	xform xfB = bb->xf;
+	v2 centerOffsetA = rotate( xfA.q, ba->localCenter );
+	v2 centerOffsetB = rotate( xfB.q, bb->localCenter );
+
+	Manifold old = c->m;
+	c->m = p_collide( &sa->g, xfA, &sb->g, xfB );
+	c->friction = sqrtf( sa->friction * sb->friction );
+	c->restitution = sa->restitution > sb->restitution ? sa->restitution : sb->restitution;
+	if ( sa->rollingResistance > 0.0f || sb->rollingResistance > 0.0f )
+	{
+		float ra = p_shape_radius( &sa->g );
+		float rb = p_shape_radius( &sb->g );
+		float mr = fmaxp( ra, rb );
+		c->rollingResistance = fmaxp( sa->rollingResistance, sb->rollingResistance ) * mr;
+	}
+	else
+		c->rollingResistance = 0.0f;
+	c->tangentSpeed = sa->tangentSpeed + sb->tangentSpeed;
+	int pointCount = c->m.pointCount;
+	int touching = pointCount > 0;
+	if ( touching && ( sa->enableHitEvents || sb->enableHitEvents ) )
+		c->simFlags |= SIM_HIT_EVENT;
+	else
+		c->simFlags &= ~SIM_HIT_EVENT;
+	if ( pointCount > 0 )
+		c->m.rollingImpulse = old.rollingImpulse;
+	for ( int i = 0; i < pointCount; ++i )
+	{
+		ManifoldPoint* mp2 = c->m.points + i;
+		mp2->anchorA = sub( mp2->anchorA, centerOffsetA );
+		mp2->anchorB = sub( mp2->anchorB, centerOffsetB );
+		mp2->normalImpulse = 0.0f;
+		mp2->tangentImpulse = 0.0f;
+		mp2->totalNormalImpulse = 0.0f;
+		mp2->normalVelocity = 0.0f;
+		mp2->persisted = false;
+		uint16_t id2 = mp2->id;
+		for ( int j = 0; j < old.pointCount; ++j )
+		{
+			ManifoldPoint* mp1 = old.points + j;
+			if ( mp1->id == id2 )
+			{
+				mp2->normalImpulse = mp1->normalImpulse;
+				mp2->tangentImpulse = mp1->tangentImpulse;
+				mp2->persisted = true;
+				mp1->normalImpulse = 0.0f;
+				mp1->tangentImpulse = 0.0f;
+				break;
+			}
+		}
+	}
+	if ( touching )
+		c->simFlags |= SIM_TOUCHING;
+	else
+		c->simFlags &= ~SIM_TOUCHING;
+	if ( touching && !wasTouching )
+		c->simFlags |= SIM_STARTED;
+	else if ( !touching && wasTouching )
+		c->simFlags |= SIM_STOPPED;
+}
+
+// ---------------------------------------------------------------------------
+// constraint graph (constraint_graph.c:68-212)
+// ---------------------------------------------------------------------------
+static void overflow_add( World* w, int cid )
+{
+	w->overflowContacts = grow( w->overflowContacts, &w->overflowCap, w->overflowCount + 1, sizeof( int ) );
+	w->contacts[cid].overflowIndex = w->overflowCount;
+	w->overflowContacts[w->overflowCount++] = cid;
+}
+
+static void overflow_remove( World* w, int cid )
+{
+	int idx = w->contacts[cid].overflowIndex;
+	int last = w->overflowCount - 1;
+	if ( idx != last )
+	{
+		int moved = w->overflowContacts[last];
+		w->overflowContacts[idx] = moved;
+		w->contacts[moved].overflowIndex = idx;
+	}
+	w->overflowCount -= 1;
+	w->contacts[cid].overflowIndex = P_NULL;
+}
+
+static void add_contact_to_graph( World* w, int cid )
+{
+	Contact* c = w->contacts + cid;
+	Body* a = w->bodies + c->bodyA;
+	Body* b = w->bodies + c->bodyB;
+	int staticA = a->type == BODY_STATIC;
+	int staticB = b->type == BODY_STATIC;
+	int color = P_OVERFLOW;
+	if ( staticA == 0 && staticB == 0 )
+	{
+		for ( int i = 0; i < P_OVERFLOW; ++i )
+		{
+			uint16_t bit = (uint16_t)( 1u << i );
+			if ( ( a->colorMask & bit ) || ( b->colorMask & bit ) )
+				continue;
+			a->colorMask |= bit;
+			b->colorMask |= bit;
+			color = i;
+			break;
+		}
+	}
+	else if ( staticA == 0 )
+	{
+		for ( int i = 1; i < P_OVERFLOW; ++i )
+		{
+			uint16_t bit = (uint16_t)( 1u << i );
+			if ( a->colorMask & bit )
+				continue;
+			a->colorMask |= bit;
+			color = i;
+			break;
+		}
+	}
+	else if ( staticB == 0 )
+	{
+		for ( int i = 1; i < P_OVERFLOW; ++i )
+		{
+			uint16_t bit = (uint16_t)( 1u << i );
+			if ( b->colorMask & bit )
+				continue;
+			b->colorMask |= bit;
+			color = i;
+			break;
+		}
+	}
+	c->color = color;
+	if ( color == P_OVERFLOW )
+		overflow_add( w, cid );
+	// constraint_graph.c:139-181: static bodies contribute zero mass
+	if ( staticA )
+	{
+		c->invMassA = 0.0f;
+		c->invIA = 0.0f;
+	}
+	else
+	{
+		c->invMassA = a->invMass;
+		c->invIA = a->invInertia;
+	}
+	if ( staticB )
+	{
+		c->invMassB = 0.0f;
+		c->invIB = 0.0f;
+	}
+	else
+	{
+		c->invMassB = b->invMass;
+		c->invIB = b->invInertia;
+	}
+}
+
+static void remove_contact_from_graph( World* w, int cid )
+{
+	Contact* c = w->contacts + cid;
+	int color = c->color;
+	if ( color != P_OVERFLOW )
+	{
+		uint16_t bit = (uint16_t)( 1u << color );
+		w->bodies[c->bodyA].colorMask &= (uint16_t)~bit;
+		w->bodies[c->bodyB].colorMask &= (uint16_t)~bit;
+	}
+	else
+		overflow_remove( w, cid );
+	c->color = P_NULL;
+}
+
+static void push_pair( int** arr, int* count, int* cap, int a, int b )
+{
+	*arr = grow( *arr, cap, 2 * ( *count + 1 ), sizeof( int ) );
+	( *arr )[2 * *count] = a;
+	( *arr )[2 * *count + 1] = b;
+	*count += 1;
+}
+
+static void destroy_contact( World* w, int cid )
+{
+	Contact* c = w->contacts + cid;
+	pairset_remove( &w->pairs, pair_key( c->shapeA, c->shapeB ) );
+	if ( c->touchingFlag && c->enableContactEvents )
+		push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
+	if ( c->color != P_NULL )
+		remove_contact_from_graph( w, cid );
+	c->used = 0;
+	free_contact_id( w, cid );
+}
+
+// world.c:586-686: serial state changes in contact-id order
+static void process_state_changes( World* w )
+{
+	for ( int id = 0; id < w->contactCount; ++id )
+	{
+		Contact* c = w->contacts + id;
+		if ( c->used == 0 )
+			continue;
+		uint32_t f = c->simFlags;
+		if ( f & SIM_DISJOINT )
+		{
+			destroy_contact( w, id );
+		}
+		else if ( f & SIM_STARTED )
+		{
+			if ( c->enableContactEvents )
+				push_pair( &w->beginEvents, &w->beginCount, &w->beginCap, c->shapeA, c->shapeB );
+			c->touchingFlag = 1;
+			c->simFlags &= ~SIM_STARTED;
+			add_contact_to_graph( w, id );
+		}
+		else if ( f & SIM_STOPPED )
+		{
+			c->simFlags &= ~SIM_STOPPED;
+			c->touchingFlag = 0;
+			if ( c->enableContactEvents )
+				push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
+			remove_contact_from_graph( w, id );
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// step (world.c:695-812)
+// ---------------------------------------------------------------------------
+void orc_world_step( int wi, double timeStep, int subStepCount )
+{
+	World* w = p_world( wi );
+	w->beginCount = 0;
+	w->hitCount = 0;
+	w->moveEventCount = 0;
+	// end events are double-buffered in the reference and reported for the
+	// step that produced them; this port clears them at step start
+	w->endCount = 0;
+	float dt = (float)timeStep;
+	if ( dt == 0.0f )
+		return;
+	update_pairs( w );
+	for ( int id = 0; id < w->contactCount; ++id )
+		if ( w->contacts[id].used )
+			update_contact( w, w->contacts + id );
+	process_state_changes( w );
+	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
+}
+
+double orc_world_step_timed( int wi, double dt, int subSteps, int steps );
+
+// ---------------------------------------------------------------------------
+// dumps (same layouts as ref_harness.c)
+// ---------------------------------------------------------------------------
+int orc_body_capacity( int wi )
+{
+	return p_world( wi )->bodyCount;
+}
+
+int orc_get_bodies( int wi, float* out, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->bodyCount < cap ? w->bodyCount : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		float* o = out + F2D_BODY_DUMP_STRIDE * i;
+		memset( o, 0, sizeof( float ) * F2D_BODY_DUMP_STRIDE );
+		Body* b = w->bodies + i;
+		if ( b->used == 0 )
+			continue;
+		o[0] = b->xf.p.x;
+		o[1] = b->xf.p.y;
+		o[2] = b->xf.q.c;
+		o[3] = b->xf.q.s;
+		o[4] = b->v.x;
+		o[5] = b->v.y;
+		o[6] = b->w;
+		o[7] = b->center.x;
+		o[8] = b->center.y;
+		o[9] = 1.0f;
+		o[10] = b->type == BODY_STATIC ? 0.0f : 2.0f;
+		o[11] = b->sleepTime;
+	}
+	return n;
+}
+
+int orc_contact_capacity( int wi )
+{
+	return p_world( wi )->contactCount;
+}
+
+int orc_get_contacts( int wi, int* ints, float* floats, int cap )
+{
+	World* w = p_world( wi );
+	int n = 0;
+	for ( int id = 0; id < w->contactCount && n < cap; ++id )
+	{
+		Contact* c = w->contacts + id;
+		if ( c->used == 0 )
+			continue;
+		int* oi = ints + F2D_CONTACT_DUMP_INTS * n;
+		float* of = floats + F2D_CONTACT_DUMP_FLOATS * n;
+		oi[0] = id;
+		oi[1] = c->shapeA;
+		oi[2] = c->shapeB;
+		oi[3] = c->color;
+		oi[4] = c->m.pointCount;
+		oi[5] = ( c->touchingFlag ? 1 : 0 ) | ( c->enableContactEvents ? 2 : 0 );
+		oi[6] = (int)c->simFlags;
+		oi[7] = c->m.points[0].id;
+		oi[8] = c->m.points[1].id;
+		of[0] = c->m.normal.x;
+		of[1] = c->m.normal.y;
+		of[2] = c->m.rollingImpulse;
+		for ( int k = 0; k < 2; ++k )
+		{
+			ManifoldPoint* mp = c->m.points + k;
+			float* p = of + 3 + 11 * k;
+			p[0] = mp->anchorA.x;
+			p[1] = mp->anchorA.y;
+			p[2] = mp->anchorB.x;
+			p[3] = mp->anchorB.y;
+			p[4] = mp->point.x;
+			p[5] = mp->point.y;
+			p[6] = mp->separation;
+			p[7] = mp->normalImpulse;
+			p[8] = mp->tangentImpulse;
+			p[9] = mp->totalNormalImpulse;
+			p[10] = mp->normalVelocity;
+		}
+		n += 1;
+	}
+	return n;
+}
+
+int orc_shape_capacity( int wi )
+{
+	return p_world( wi )->shapeCount;
+}
+
+int orc_get_shapes( int wi, float* floats, int* ints, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->shapeCount < cap ? w->shapeCount : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		Shape* s = w->shapes + i;
+		float* f = floats + 8 * i;
+		int* k = ints + 4 * i;
+		f[0] = s->aabb.lo.x;
+		f[1] = s->aabb.lo.y;
+		f[2] = s->aabb.hi.x;
+		f[3] = s->aabb.hi.y;
+		f[4] = s->fatAABB.lo.x;
+		f[5] = s->fatAABB.lo.y;
+		f[6] = s->fatAABB.hi.x;
+		f[7] = s->fatAABB.hi.y;
+		k[0] = s->proxyKey;
+		k[1] = s->bodyId;
+		k[2] = s->g.type;
+		k[3] = s->enlarged;
+	}
+	return n;
+}
+
+int orc_get_mass( int wi, float* out, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->bodyCount < cap ? w->bodyCount : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		float* o = out + 8 * i;
+		memset( o, 0, 8 * sizeof( float ) );
+		Body* b = w->bodies + i;
+		if ( b->used == 0 )
+			continue;
+		o[0] = b->mass;
+		o[1] = b->inertia;
+		o[2] = b->invMass;
+		o[3] = b->invInertia;
+		o[4] = b->localCenter.x;
+		o[5] = b->localCenter.y;
+		o[6] = b->minExtent;
+		o[7] = b->maxExtent;
+	}
+	return n;
+}
+
+int orc_get_polygon( int wi, int shape, float* out )
+{
+	World* w = p_world( wi );
+	Shape* s = w->shapes + shape;
+	if ( s->g.type != SHAPE_POLYGON )
+		return 0;
+	const Polygon* p = &s->g.poly;
+	out[0] = (float)p->count;
+	out[1] = p->radius;
+	out[2] = p->centroid.x;
+	out[3] = p->centroid.y;
+	for ( int i = 0; i < 8; ++i )
+	{
+		out[4 + 2 * i] = p->vertices[i].x;
+		out[5 + 2 * i] = p->vertices[i].y;
+		out[20 + 2 * i] = p->normals[i].x;
+		out[21 + 2 * i] = p->normals[i].y;
+	}
+	return p->count;
+}
+
+void orc_get_color_counts( int wi, int* out )
+{
+	World* w = p_world( wi );
+	for ( int i = 0; i < P_COLORS; ++i )
+		out[i] = 0;
+	for ( int id = 0; id < w->contactCount; ++id )
+	{
+		Contact* c = w->contacts + id;
+		if ( c->used && c->color >= 0 )
+			out[c->color] += 1;
+	}
+	for ( int j = 0; j < w->jointCount; ++j )
+	{
+		Joint* jt = w->joints + j;
+		if ( jt->used && jt->color >= 0 )
+			out[jt->color] += 1;
+	}
+}
+
+int orc_awake_body_count( int wi )
+{
+	World* w = p_world( wi );
+	int n = 0;
+	for ( int i = 0; i < w->bodyCount; ++i )
+		if ( w->bodies[i].used && w->bodies[i].type != BODY_STATIC && w->bodies[i].enabled )
+			n += 1;
+	return n;
+}
+
+void orc_event_counts( int wi, int* out )
+{
+	World* w = p_world( wi );
+	out[0] = w->beginCount;
+	out[1] = w->endCount;
+	out[2] = w->hitCount;
+	out[3] = w->moveEventCount;
+}
+
+int orc_get_begin_events( int wi, int* pairs, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->beginCount < cap ? w->beginCount : cap;
+	memcpy( pairs, w->beginEvents, sizeof( int ) * 2 * (size_t)n );
+	return n;
+}
+
+int orc_get_end_events( int wi, int* pairs, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->endCount < cap ? w->endCount : cap;
+	memcpy( pairs, w->endEvents, sizeof( int ) * 2 * (size_t)n );
+	return n;
+}
+
+int orc_get_hit_events( int wi, int* ints, float* floats, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->hitCount < cap ? w->hitCount : cap;
+	memcpy( ints, w->hitShapes, sizeof( int ) * 2 * (size_t)n );
+	memcpy( floats, w->hitData, sizeof( float ) * 5 * (size_t)n );
+	return n;
+}
+
+int orc_get_move_events( int wi, int* ints, float* floats, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->moveEventCount < cap ? w->moveEventCount : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		ints[2 * i] = w->moveEventBodies[i];
+		ints[2 * i + 1] = 0;
+	}
+	memcpy( floats, w->moveEventXf, sizeof( float ) * 4 * (size_t)n );
+	return n;
+}
+
+// world-internal helpers used by psolver.c
+void p_push_move( World* w, int shapeId )
+{
+	push_move( w, shapeId );
+}
