@@ -1,0 +1,594 @@
+// Broadphase of the world step: the set of new contact pairs.
+//
+// Box2D v3.1.1 keeps three incremental dynamic trees and queries them with
+// every proxy whose fat AABB grew last step (broad_phase.c:160-474,
+// dynamic_tree.c:1114). The pair set that produces is: every pair of shapes
+// with overlapping fat AABBs, at least one of them a dynamic proxy and at
+// least one of them moved, that passes the filters and has no contact yet.
+// This file computes the same set GPU-first:
+//   1. a linear BVH (Karras 2012) over all proxies' fat AABBs, rebuilt each
+//      step from 30-bit Morton codes sorted with the stable radix sort;
+//   2. one thread per moved proxy traverses it (leaves in Morton order, so
+//      neighbouring threads walk neighbouring subtrees);
+//   3. new pairs are sorted by their 64-bit shape-pair key, the order in
+//      which contact ids are then drawn from the LIFO id pool.
+#include "dscan.cuh"
+#include "dworld.cuh"
+#include "kernels.cuh"
+
+#define BP_THREADS 256
+#define TRAVERSE_STACK 64
+
+__device__ __forceinline__ unsigned long long pair_key( int a, int b )
+{
+	return a < b ? ( ( (unsigned long long)a << 32 ) | (unsigned)b ) : ( ( (unsigned long long)b << 32 ) | (unsigned)a );
+}
+
+__device__ __forceinline__ unsigned hash64( unsigned long long k )
+{
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdULL;
+	k ^= k >> 33;
+	k *= 0xc4ceb9fe1a85ec53ULL;
+	k ^= k >> 33;
+	return (unsigned)k;
+}
+
+// ---------------------------------------------------------------------------
+// pair set: rebuilt every step from the live contacts (no deletions needed)
+// ---------------------------------------------------------------------------
+__global__ void k_hash_clear( DWorld w )
+{
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.hashCap; i += gridDim.x * blockDim.x )
+		w.pairHash[i] = 0ull;
+}
+
+__global__ void k_hash_insert( DWorld w )
+{
+	int n = w.sc->contactIdCount;
+	unsigned m = (unsigned)w.hashCap - 1u;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		if ( ( w.cflags[c] & CF_USED ) == 0 )
+			continue;
+		int2 s = w.cshape[c];
+		unsigned long long key = pair_key( s.x, s.y ) + 1ull;
+		unsigned h = hash64( key - 1ull ) & m;
+		for ( int probe = 0; probe < w.hashCap; ++probe )
+		{
+			unsigned long long prev = atomicCAS( w.pairHash + h, 0ull, key );
+			if ( prev == 0ull || prev == key )
+				break;
+			h = ( h + 1u ) & m;
+		}
+	}
+}
+
+__device__ __forceinline__ bool hash_contains( const DWorld& w, unsigned long long key )
+{
+	unsigned m = (unsigned)w.hashCap - 1u;
+	unsigned h = hash64( key ) & m;
+	unsigned long long k1 = key + 1ull;
+	for ( int probe = 0; probe < w.hashCap; ++probe )
+	{
+		unsigned long long v = w.pairHash[h];
+		if ( v == 0ull )
+			return false;
+		if ( v == k1 )
+			return true;
+		h = ( h + 1u ) & m;
+	}
+	return false;
+}
+
+// ---------------------------------------------------------------------------
+// LBVH build
+// ---------------------------------------------------------------------------
+__global__ void k_leaf_flags( DWorld w, int* flags )
+{
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+		flags[s] = ( w.sflags[s] & ( SF_USED | SF_PROXY ) ) == ( SF_USED | SF_PROXY ) ? 1 : 0;
+}
+
+__global__ void k_leaf_compact( DWorld w, const int* flags, const int* offs )
+{
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+		if ( flags[s] )
+			w.leafShape[offs[s]] = s;
+}
+
+// block min/max of fat-box centres, then a single-block final reduction
+__global__ void k_bounds_partial( DWorld w, float4* partial )
+{
+	__shared__ float4 red[BP_THREADS];
+	int n = w.sc->treeLeafCount;
+	float4 b = make_float4( FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX );
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		float4 f = w.fat[w.leafShape[i]];
+		float cx = 0.5f * ( f.x + f.z ), cy = 0.5f * ( f.y + f.w );
+		b.x = fminf( b.x, cx );
+		b.y = fminf( b.y, cy );
+		b.z = fmaxf( b.z, cx );
+		b.w = fmaxf( b.w, cy );
+	}
+	red[threadIdx.x] = b;
+	__syncthreads();
+	for ( int o = blockDim.x / 2; o > 0; o >>= 1 )
+	{
+		if ( threadIdx.x < o )
+		{
+			float4 a = red[threadIdx.x], c = red[threadIdx.x + o];
+			red[threadIdx.x] = make_float4( fminf( a.x, c.x ), fminf( a.y, c.y ), fmaxf( a.z, c.z ), fmaxf( a.w, c.w ) );
+		}
+		__syncthreads();
+	}
+	if ( threadIdx.x == 0 )
+		partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_bounds_final( float4* partial, int count )
+{
+	__shared__ float4 red[BP_THREADS];
+	float4 b = make_float4( FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX );
+	for ( int i = threadIdx.x; i < count; i += blockDim.x )
+	{
+		float4 a = partial[i];
+		b = make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fmaxf( a.z, b.z ), fmaxf( a.w, b.w ) );
+	}
+	red[threadIdx.x] = b;
+	__syncthreads();
+	for ( int o = blockDim.x / 2; o > 0; o >>= 1 )
+	{
+		if ( threadIdx.x < o )
+		{
+			float4 a = red[threadIdx.x], c = red[threadIdx.x + o];
+			red[threadIdx.x] = make_float4( fminf( a.x, c.x ), fminf( a.y, c.y ), fmaxf( a.z, c.z ), fmaxf( a.w, c.w ) );
+		}
+		__syncthreads();
+	}
+	if ( threadIdx.x == 0 )
+		partial[0] = red[0];
+}
+
+__device__ __forceinline__ unsigned expand_bits15( unsigned v )
+{
+	v &= 0x7fffu;
+	v = ( v | ( v << 8 ) ) & 0x00ff00ffu;
+	v = ( v | ( v << 4 ) ) & 0x0f0f0f0fu;
+	v = ( v | ( v << 2 ) ) & 0x33333333u;
+	v = ( v | ( v << 1 ) ) & 0x55555555u;
+	return v;
+}
+
+__global__ void k_morton( DWorld w, const float4* bounds )
+{
+	int n = w.sc->treeLeafCount;
+	float4 b = bounds[0];
+	float sx = b.z - b.x, sy = b.w - b.y;
+	float inx = sx > 0.0f ? 32767.0f / sx : 0.0f;
+	float iny = sy > 0.0f ? 32767.0f / sy : 0.0f;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		float4 f = w.fat[w.leafShape[i]];
+		float cx = 0.5f * ( f.x + f.z ), cy = 0.5f * ( f.y + f.w );
+		unsigned qx = (unsigned)fminf( fmaxf( ( cx - b.x ) * inx, 0.0f ), 32767.0f );
+		unsigned qy = (unsigned)fminf( fmaxf( ( cy - b.y ) * iny, 0.0f ), 32767.0f );
+		w.mortonKeys[i] = ( expand_bits15( qx ) << 1 ) | expand_bits15( qy );
+	}
+}
+
+// Karras 2012 common-prefix length with index tie-break
+__device__ __forceinline__ int delta_fn( const unsigned* keys, int n, int i, int j )
+{
+	if ( j < 0 || j >= n )
+		return -1;
+	unsigned a = keys[i], b = keys[j];
+	if ( a == b )
+		return 32 + __clz( (unsigned)( i ^ j ) );
+	return __clz( a ^ b );
+}
+
+// Internal node i spans a key range; children are internal nodes or leaves
+// (~leaf). nodeParent holds internal parents at [0, n-1) and leaf parents at
+// [n-1, 2n-1).
+__global__ void k_build_tree( DWorld w )
+{
+	int n = w.sc->treeLeafCount;
+	const unsigned* keys = w.mortonKeys;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x )
+	{
+		int d = ( delta_fn( keys, n, i, i + 1 ) - delta_fn( keys, n, i, i - 1 ) ) >= 0 ? 1 : -1;
+		int dmin = delta_fn( keys, n, i, i - d );
+		int lmax = 2;
+		while ( delta_fn( keys, n, i, i + lmax * d ) > dmin )
+			lmax <<= 1;
+		int l = 0;
+		for ( int t = lmax >> 1; t >= 1; t >>= 1 )
+			if ( delta_fn( keys, n, i, i + ( l + t ) * d ) > dmin )
+				l += t;
+		int j = i + l * d;
+		int dnode = delta_fn( keys, n, i, j );
+		int s = 0;
+		int len = l;
+		int t = ( len + 1 ) >> 1;
+		while ( true )
+		{
+			if ( delta_fn( keys, n, i, i + ( s + t ) * d ) > dnode )
+				s += t;
+			if ( t == 1 )
+				break;
+			t = ( t + 1 ) >> 1;
+		}
+		int gamma = i + s * d + ( d < 0 ? d : 0 );
+		int lo = i < j ? i : j;
+		int hi = i < j ? j : i;
+		int left = ( lo == gamma ) ? ~gamma : gamma;
+		int right = ( hi == gamma + 1 ) ? ~( gamma + 1 ) : gamma + 1;
+		w.nodeLeft[i] = left;
+		w.nodeRight[i] = right;
+		if ( left < 0 )
+			w.nodeParent[n - 1 + ~left] = i;
+		else
+			w.nodeParent[left] = i;
+		if ( right < 0 )
+			w.nodeParent[n - 1 + ~right] = i;
+		else
+			w.nodeParent[right] = i;
+		w.nodeVisit[i] = 0;
+	}
+	if ( blockIdx.x == 0 && threadIdx.x == 0 && n > 0 )
+		w.nodeParent[0] = -1;
+}
+
+// leaf boxes live at nodeBox[n-1+leaf]; walk up, second arrival merges
+__global__ void k_tree_boxes( DWorld w )
+{
+	int n = w.sc->treeLeafCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		int s = w.leafShape[i];
+		w.nodeBox[n - 1 + i] = w.fat[s];
+		if ( n == 1 )
+			continue;
+		__threadfence();
+		int node = w.nodeParent[n - 1 + i];
+		for ( int guard = 0; node >= 0; ++guard )
+		{
+			if ( guard > 4096 || node >= n - 1 )
+			{
+				atomicOr( &w.sc->error, ERR_TREE );
+				break;
+			}
+			int prev = atomicAdd( w.nodeVisit + node, 1 );
+			if ( prev == 0 )
+				break;
+			__threadfence();
+			int l = w.nodeLeft[node], r = w.nodeRight[node];
+			float4 a = __ldcg( w.nodeBox + ( l < 0 ? n - 1 + ~l : l ) );
+			float4 b = __ldcg( w.nodeBox + ( r < 0 ? n - 1 + ~r : r ) );
+			w.nodeBox[node] = make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fmaxf( a.z, b.z ), fmaxf( a.w, b.w ) );
+			__threadfence();
+			node = w.nodeParent[node];
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// pair filters (shape.h:122-130, body.c:1861-1897)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool shapes_collide( const DWorld& w, int a, int b )
+{
+	int ga = w.group[a], gb = w.group[b];
+	if ( ga == gb && ga != 0 )
+		return ga > 0;
+	return ( w.mask[a] & w.cat[b] ) != 0ull && ( w.cat[a] & w.mask[b] ) != 0ull;
+}
+
+__device__ __forceinline__ bool bodies_collide( const DWorld& w, int ia, int ib )
+{
+	int fa = w.bflags[ia], fb = w.bflags[ib];
+	if ( body_type( fa ) != 2 && body_type( fb ) != 2 )
+		return false;
+	int key, other;
+	if ( w.jointCountB[ia] < w.jointCountB[ib] )
+	{
+		key = w.headJoint[ia];
+		other = ib;
+	}
+	else
+	{
+		key = w.headJoint[ib];
+		other = ia;
+	}
+	for ( int guard = 0; key != F2D_NULL && guard < ( 1 << 20 ); ++guard )
+	{
+		int jid = key >> 1;
+		int edge = key & 1;
+		int2 jb = w.jbody[jid];
+		int otherBody = edge == 0 ? jb.y : jb.x;
+		if ( ( w.jflags[jid] & 0x10 ) == 0 && otherBody == other )
+			return false;
+		key = w.jnext[2 * jid + edge];
+	}
+	return true;
+}
+
+__device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
+{
+	// contact.c:151-175 registry: (first, second) has a manifold function
+	// circle-circle, capsule-circle, capsule-capsule, polygon-circle,
+	// polygon-capsule, polygon-polygon, segment-circle, segment-capsule,
+	// segment-polygon
+	const unsigned reg = ( 1u << ( 0 * 4 + 0 ) ) | ( 1u << ( 1 * 4 + 0 ) ) | ( 1u << ( 1 * 4 + 1 ) ) |
+						 ( 1u << ( 3 * 4 + 0 ) ) | ( 1u << ( 3 * 4 + 1 ) ) | ( 1u << ( 3 * 4 + 3 ) ) |
+						 ( 1u << ( 2 * 4 + 0 ) ) | ( 1u << ( 2 * 4 + 1 ) ) | ( 1u << ( 2 * 4 + 3 ) );
+	if ( reg & ( 1u << ( ta * 4 + tb ) ) )
+	{
+		*primary = true;
+		return true;
+	}
+	if ( reg & ( 1u << ( tb * 4 + ta ) ) )
+	{
+		*primary = false;
+		return true;
+	}
+	*primary = true;
+	return false;
+}
+
+// One thread per moved proxy. A pair found by both of its moved proxies is
+// reported by the one with the smaller shape id.
+__global__ void k_find_pairs( DWorld w )
+{
+	int n = w.sc->treeLeafCount;
+	for ( int li = blockIdx.x * blockDim.x + threadIdx.x; li < n; li += gridDim.x * blockDim.x )
+	{
+		int si = w.leafShape[li];
+		int fi = w.sflags[si];
+		if ( ( fi & SF_MOVED ) == 0 )
+			continue;
+		int typeI = w.proxyKey[si] & 3;
+		fbox q = box_from4( w.fat[si] );
+		int bi = w.shapeBody[si];
+		int stack[TRAVERSE_STACK];
+		int sp = 0;
+		int node = n == 1 ? ~0 : 0;
+		for ( int guard = 0;; ++guard )
+		{
+			if ( guard > 4 * n + 64 || node >= n - 1 + ( n == 1 ) || ~node >= n )
+			{
+				atomicOr( &w.sc->error, ERR_TREE );
+				break;
+			}
+			if ( node < 0 )
+			{
+				int leaf = ~node;
+				int sj = w.leafShape[leaf];
+				if ( sj != si )
+				{
+					fbox bj = box_from4( w.nodeBox[n - 1 + leaf] );
+					if ( box_overlaps( q, bj ) )
+					{
+						int fj = w.sflags[sj];
+						int typeJ = w.proxyKey[sj] & 3;
+						bool movedJ = ( fj & SF_MOVED ) != 0;
+						bool ok = true;
+						if ( movedJ && sj < si )
+							ok = false; // reported by sj
+						if ( typeI != 2 && typeJ != 2 )
+							ok = false;
+						bool primaryUnused;
+						if ( ok && !registered( shape_type( fi ), shape_type( fj ), &primaryUnused ) )
+							ok = false; // no manifold function: b2CreateContact makes no contact
+						if ( ok )
+						{
+							int bj2 = w.shapeBody[sj];
+							if ( bj2 == bi || ( fi & SF_SENSOR ) || ( fj & SF_SENSOR ) )
+								ok = false;
+							else if ( !shapes_collide( w, si, sj ) )
+								ok = false;
+							else if ( !bodies_collide( w, bi, bj2 ) )
+								ok = false;
+							else if ( hash_contains( w, pair_key( si, sj ) ) )
+								ok = false;
+						}
+						if ( ok )
+						{
+							int slot = atomicAdd( &w.sc->newPairCount, 1 );
+							if ( slot < w.pairCap )
+							{
+								int lo = si < sj ? si : sj, hi = si < sj ? sj : si;
+								w.pairKeys[slot] = ( (unsigned long long)lo << w.pairKeyBits ) | (unsigned)hi;
+								w.pairVal[slot] = slot;
+							}
+							else
+								atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
+						}
+					}
+				}
+				if ( sp == 0 )
+					break;
+				node = stack[--sp];
+				continue;
+			}
+			// internal node: test children
+			int l = w.nodeLeft[node], r = w.nodeRight[node];
+			fbox bl = box_from4( w.nodeBox[l < 0 ? n - 1 + ~l : l] );
+			fbox br = box_from4( w.nodeBox[r < 0 ? n - 1 + ~r : r] );
+			bool ol = box_overlaps( q, bl );
+			bool orr = box_overlaps( q, br );
+			if ( ol && orr )
+			{
+				if ( sp < TRAVERSE_STACK )
+					stack[sp++] = r;
+				else
+					atomicOr( &w.sc->error, ERR_TREE );
+				node = l;
+			}
+			else if ( ol )
+				node = l;
+			else if ( orr )
+				node = r;
+			else
+			{
+				if ( sp == 0 )
+					break;
+				node = stack[--sp];
+			}
+		}
+	}
+}
+
+__global__ void k_clamp_pairs( DWorld w )
+{
+	if ( w.sc->newPairCount > w.pairCap )
+		w.sc->newPairCount = w.pairCap;
+}
+
+// ---------------------------------------------------------------------------
+// contact creation (contact.c:186-330) in pair-key order
+// ---------------------------------------------------------------------------
+__global__ void k_create_contacts( DWorld w, int planMode )
+{
+	int n = w.sc->newPairCount;
+	int F = w.sc->contactFreeCount;
+	int base = w.sc->contactIdCount;
+	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
+	{
+		unsigned long long sortKey = w.pairKeys[r];
+		int s1 = (int)( sortKey >> w.pairKeyBits );
+		int s2 = (int)( sortKey & ( ( 1ull << w.pairKeyBits ) - 1ull ) );
+		unsigned long long key = pair_key( s1, s2 );
+		// A is the shape with the smaller proxy key (broad_phase.c:258-267)
+		int a = s1, b = s2;
+		if ( w.proxyKey[s2] < w.proxyKey[s1] )
+		{
+			a = s2;
+			b = s1;
+		}
+		int ta = shape_type( w.sflags[a] ), tb = shape_type( w.sflags[b] );
+		bool primary;
+		int id;
+		if ( planMode )
+		{
+			id = r < w.sc->planCount && w.planKeys[r] == key ? w.planIds[r] : -1;
+			if ( id < 0 )
+			{
+				atomicOr( &w.sc->error, ERR_PLAN_MISMATCH );
+				continue;
+			}
+		}
+		else
+			id = r < F ? w.contactFree[F - 1 - r] : base + ( r - F );
+		if ( id >= w.contactCap )
+		{
+			atomicOr( &w.sc->error, ERR_CONTACT_CAPACITY );
+			continue;
+		}
+		if ( !registered( ta, tb, &primary ) )
+			continue; // no manifold function (e.g. segment-segment): no contact
+		if ( !primary )
+		{
+			int t = a;
+			a = b;
+			b = t;
+		}
+		int fa = w.sflags[a], fb = w.sflags[b];
+		w.cshape[id] = make_int2( a, b );
+		w.cbody[id] = make_int2( w.shapeBody[a], w.shapeBody[b] );
+		int flags = CF_USED;
+		if ( ( fa | fb ) & SF_CONTACT_EVENTS )
+			flags |= CF_EVENTS;
+		if ( ( fa | fb ) & SF_PRESOLVE )
+			flags |= CF_PRESOLVE;
+		w.cflags[id] = flags;
+		w.ccolor[id] = F2D_NULL;
+		w.coverflowIndex[id] = F2D_NULL;
+		float4 ma = w.mat[a], mb = w.mat[b];
+		// world.c:88-98 default mixing
+		w.cmat[id] = make_float4( sqrtf( ma.x * mb.x ), ma.y > mb.y ? ma.y : mb.y, 0.0f, 0.0f );
+		w.cmass[id] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+		w.mnorm[id] = make_float4( 0.0f, 0.0f, 0.0f, __int_as_float( 0 ) );
+		for ( int k = 0; k < 2; ++k )
+		{
+			w.mpA[2 * id + k] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			w.mpB[2 * id + k] = make_float4( 0.0f, 0.0f, 0.0f, __int_as_float( 0 ) );
+			w.mpI[2 * id + k] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+		}
+	}
+}
+
+// advance the id pool after creation and clear the move flags
+__global__ void k_after_create( DWorld w, int planMode )
+{
+	if ( blockIdx.x == 0 && threadIdx.x == 0 )
+	{
+		int n = w.sc->newPairCount;
+		if ( planMode )
+		{
+			// plan ids are explicit; raise the high-water mark and drop used
+			// ids from the free stack (order of the remaining ids is kept)
+			int hi = w.sc->contactIdCount;
+			for ( int r = 0; r < n && r < w.sc->planCount; ++r )
+				hi = max( hi, w.planIds[r] + 1 );
+			int F = w.sc->contactFreeCount;
+			int keep = 0;
+			for ( int k = 0; k < F; ++k )
+			{
+				int id = w.contactFree[k];
+				bool used = ( w.cflags[id] & CF_USED ) != 0;
+				if ( !used )
+					w.contactFree[keep++] = id;
+			}
+			// ids skipped between the old and the new high-water mark are free
+			for ( int id = w.sc->contactIdCount; id < hi; ++id )
+				if ( ( w.cflags[id] & CF_USED ) == 0 && keep < w.contactCap )
+					w.contactFree[keep++] = id;
+			w.sc->contactFreeCount = keep;
+			w.sc->contactIdCount = min( hi, w.contactCap );
+		}
+		else
+		{
+			int F = w.sc->contactFreeCount;
+			if ( n <= F )
+				w.sc->contactFreeCount = F - n;
+			else
+			{
+				w.sc->contactFreeCount = 0;
+				w.sc->contactIdCount = min( w.sc->contactIdCount + ( n - F ), w.contactCap );
+			}
+		}
+		w.sc->newPairCount = 0;
+		w.sc->planCount = 0;
+	}
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+		w.sflags[s] &= ~SF_MOVED;
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode )
+{
+	int gridS = grid_for( w.shapeCount );
+	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, st>>>( w );
+	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, st>>>( w );
+	k_leaf_flags<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA );
+	scan_exclusive( s.tmpA, s.tmpB, s.scanTmp, nullptr, w.shapeCount, w.shapeCap, &w.sc->treeLeafCount, st );
+	k_leaf_compact<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA, s.tmpB );
+	k_bounds_partial<<<s.boundsBlocks, BP_THREADS, 0, st>>>( w, s.bounds );
+	k_bounds_final<<<1, BP_THREADS, 0, st>>>( s.bounds, s.boundsBlocks );
+	k_morton<<<gridS, BP_THREADS, 0, st>>>( w, s.bounds );
+	radix_sort<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount,
+						  w.shapeCap, 30, w.sortHist, s.scanTmp, st );
+	k_build_tree<<<gridS, BP_THREADS, 0, st>>>( w );
+	k_tree_boxes<<<gridS, BP_THREADS, 0, st>>>( w );
+	k_find_pairs<<<gridS, BP_THREADS, 0, st>>>( w );
+	k_clamp_pairs<<<1, 1, 0, st>>>( w );
+	int bits = 2 * w.pairKeyBits;
+	radix_sort<unsigned long long>( w.pairKeys, w.pairVal, w.pairKeysAlt, w.pairValAlt, &w.sc->newPairCount,
+									w.pairCap, bits, w.sortHist, s.scanTmp, st );
+	k_create_contacts<<<grid_for( w.pairCap ), BP_THREADS, 0, st>>>( w, planMode );
+	k_after_create<<<gridS, BP_THREADS, 0, st>>>( w, planMode );
+}

@@ -1,0 +1,243 @@
+// Device-resident world state: structure-of-arrays body, shape, contact,
+// joint and constraint records in HBM, plus the step's scratch buffers.
+//
+// Indexing follows the reference's stable ids: bodies by body id, shapes by
+// shape id, contacts by contact id (b2Contact array indexed by the contact id
+// pool, packages/forge2d/third_party/box2d/src/contact.c:186-240). Static
+// bodies keep rows too; the solver treats them as the identity state
+// (contact_solver.c:1195-1201 dummy body).
+#pragma once
+
+#include "dmath.cuh"
+
+#include <cuda_runtime.h>
+
+// body flags
+#define BF_USED 0x1
+#define BF_ENABLED 0x2
+#define BF_BULLET 0x4
+#define BF_FAST_ROT 0x8
+#define BF_FIXED_ROT 0x10
+#define BF_ENABLE_SLEEP 0x20
+#define BF_SPEED_CAPPED 0x40
+#define BF_IS_FAST 0x80
+#define BF_ENLARGE 0x100
+#define BF_TYPE_SHIFT 16 // 2 bits: 0 static 1 kinematic 2 dynamic
+
+// shape flags
+#define SF_USED 0x1
+#define SF_SENSOR 0x2
+#define SF_CONTACT_EVENTS 0x4
+#define SF_HIT_EVENTS 0x8
+#define SF_PRESOLVE 0x10
+#define SF_ENLARGED 0x20
+#define SF_MOVED 0x40
+#define SF_PROXY 0x80 // has a broadphase proxy
+#define SF_TYPE_SHIFT 16
+
+// shape types (b2ShapeType)
+#define ST_CIRCLE 0
+#define ST_CAPSULE 1
+#define ST_SEGMENT 2
+#define ST_POLYGON 3
+
+// contact flags (contact.h:74-93 sim flags plus the b2Contact flags)
+#define CF_USED 0x1
+#define CF_TOUCHING 0x2 // b2_contactTouchingFlag (graph membership)
+#define CF_EVENTS 0x4	// b2_contactEnableContactEvents
+#define CF_SIM_TOUCHING 0x10000
+#define CF_DISJOINT 0x20000
+#define CF_STARTED 0x40000
+#define CF_STOPPED 0x80000
+#define CF_HIT_EVENT 0x100000
+#define CF_PRESOLVE 0x200000
+
+// error bits in DScalars::error
+#define ERR_CONTACT_CAPACITY 0x1
+#define ERR_PAIR_CAPACITY 0x2
+#define ERR_BARRIER_TIMEOUT 0x4
+#define ERR_PLAN_MISMATCH 0x8
+#define ERR_OP_CAPACITY 0x10
+#define ERR_COLOR_ROUNDS 0x20
+#define ERR_EVENT_CAPACITY 0x40
+#define ERR_TREE 0x80
+
+// Shape geometry record: 10 float4 per shape.
+//   g[0] = c1.x c1.y c2.x c2.y   (circle centre; capsule/segment ends; polygon centroid)
+//   g[1] = radius, count (int bits), localCentroid.x, localCentroid.y
+//   g[2..5] polygon vertices, g[6..9] polygon normals
+#define GEOM_F4 10
+
+// Per-step scalars kept in device memory so that no launch needs a host
+// round trip.
+struct DScalars
+{
+	int contactIdCount; // high-water mark of the contact id pool
+	int contactFreeCount;
+	int newPairCount;
+	int opCount;
+	int touchingCount;
+	int colorCount[F2D_COLORS];
+	int colorStart[F2D_COLORS + 1];
+	int overflowCount;
+	int overflowJointCount;
+	int fastCount;
+	int beginCount, endCount, hitCount, moveCount;
+	int error;
+	int colorRounds;
+	unsigned barrierCount;
+	unsigned barrierGen;
+	int planCount;
+	int awakeCount;
+	int treeLeafCount;
+	float contactSpeed;
+	int stepIndex;
+	int pad[8];
+};
+
+struct DWorld
+{
+	// capacities
+	int bodyCap, shapeCap, contactCap, jointCap;
+	int pairCap;  // new-pair buffer capacity per step
+	int pairKeyBits; // sort key of a new pair: (min shape id << pairKeyBits) | max shape id
+	int opCap;	  // state-change op capacity per step
+	int hashCap;  // pair-set hash capacity (power of two)
+	int eventCap; // per-step event buffer capacity
+
+	// host-known counts (creation path)
+	int bodyCount, shapeCount, jointCount;
+
+	// world constants
+	fv2 gravity;
+	float restitutionThreshold, hitEventThreshold;
+	float contactHertz, contactDampingRatio, maxContactPushSpeed, maxLinearSpeed;
+	float jointHertz, jointDampingRatio;
+	int enableSleep, enableContinuous, enableWarmStarting;
+
+	// ---------------- bodies (by body id) ----------------
+	float4* xf;			// p.x p.y q.c q.s
+	float4* vel;		// v.x v.y w flags-pad      (b2BodyState bytes 0..15)
+	float4* delta;		// dp.x dp.y dq.c dq.s      (b2BodyState bytes 16..31)
+	float2* center;		// world centre of mass
+	float4* sweep0;		// center0.x center0.y rotation0.c rotation0.s
+	float2* localCenter;
+	float4* massv;		// invMass invInertia minExtent maxExtent
+	float4* damp;		// linearDamping angularDamping gravityScale sleepThreshold
+	float4* force;		// force.x force.y torque sleepTime
+	int* bflags;
+	int* headShape;
+	int* headJoint; // joint key list: (jointId << 1) | edge
+	int* jointCountB;
+	unsigned* colorMask; // bit c: body holds a graph constraint of colour c < 11
+	int* colorLock;		 // scratch for the colouring rounds
+
+	// ---------------- shapes (by shape id) ----------------
+	float4* geom; // GEOM_F4 per shape
+	float4* aabb;
+	float4* fat;
+	float4* mat; // friction restitution rollingResistance tangentSpeed
+	unsigned long long* cat;
+	unsigned long long* mask;
+	int* group;
+	int* shapeBody;
+	int* sflags;
+	int* proxyKey;
+	int* nextShape;
+
+	// ---------------- contacts (by contact id) ----------------
+	int2* cshape; // shapeA shapeB
+	int2* cbody;  // bodyA bodyB
+	int* cflags;
+	int* ccolor;
+	int* coverflowIndex;
+	float4* cmat;  // friction restitution rollingResistance tangentSpeed
+	float4* cmass; // invMassA invIA invMassB invIB
+	float4* mnorm; // normal.x normal.y rollingImpulse pointCount(bits)
+	float4* mpA;   // [2*id+k] anchorA.xy anchorB.xy
+	float4* mpB;   // [2*id+k] point.xy separation id(bits, bit16 = persisted)
+	float4* mpI;   // [2*id+k] normalImpulse tangentImpulse totalNormalImpulse normalVelocity
+	int* contactFree; // LIFO free id stack (id_pool.c:19-38)
+	unsigned long long* pairHash; // open-addressing set of live pair keys (key+1)
+
+	// ---------------- broadphase scratch ----------------
+	unsigned* mortonKeys;
+	unsigned* mortonKeysAlt;
+	int* leafShape;
+	int* leafShapeAlt;
+	int* nodeLeft;	 // internal node children; leaves encoded as ~leafIndex
+	int* nodeRight;
+	int* nodeParent; // [internal nodes, then leaves]
+	float4* nodeBox;
+	int* nodeVisit;
+	unsigned* sortHist; // radix sort histograms
+	unsigned long long* pairKeys;
+	unsigned long long* pairKeysAlt;
+	int* pairVal;
+	int* pairValAlt;
+	int* planIds; // parity plan: contact id for the k-th new pair in key order
+	unsigned long long* planKeys;
+
+	// ---------------- state-change ops ----------------
+	int* opContact; // contact id
+	int* opKind;	// 0 destroy, 1 begin, 2 end
+	int* opColor;	// colour result / colour removed
+	int* opDone;
+
+	// ---------------- constraints (by slot, grouped by colour) ----------------
+	int* slotContact;
+	int* overflowList; // contact ids in overflow-array order
+	int2* kIndex;	   // indexA indexB (-1 static)
+	float4* kMass;	   // invMassA invIA invMassB invIB
+	float4* kNormal;   // normal.x normal.y friction tangentSpeed
+	float4* kMisc;	   // restitution rollingResistance rollingMass rollingImpulse
+	float4* kSoft;	   // biasRate massScale impulseScale pointCount(bits)
+	float4* kAnch1;	   // anchorA1.xy anchorB1.xy
+	float4* kAnch2;	   // anchorA2.xy anchorB2.xy
+	float4* kP1;	   // baseSeparation normalMass tangentMass relativeVelocity (point 1)
+	float4* kP2;	   // same, point 2
+	float4* kImp;	   // normalImpulse1 normalImpulse2 tangentImpulse1 tangentImpulse2
+	float2* kTot;	   // totalNormalImpulse1 totalNormalImpulse2
+
+	// ---------------- joints (by joint id) ----------------
+	int2* jbody;
+	int* jflags; // used, enableSpring, enableLimit, enableMotor, collideConnected
+	int* jcolor;
+	int* jnext;	 // [2*id+edge] next joint key in the body list
+	float4* jdef0; // localOriginAnchorA.xy localOriginAnchorB.xy
+	float4* jdef1; // referenceAngle targetAngle hertz dampingRatio
+	float4* jdef2; // lowerAngle upperAngle maxMotorTorque motorSpeed
+	float4* jimp;  // linearImpulse.xy springImpulse motorImpulse
+	float2* jimp2; // lowerImpulse upperImpulse
+	float4* jprep0; // anchorA.xy anchorB.xy
+	float4* jprep1; // deltaCenter.xy deltaAngle axialMass
+	float4* jprep2; // springSoftness biasRate massScale impulseScale, pad
+	float4* jprepM; // invMassA invIA invMassB invIB
+	int2* jindex;	// solver body indices
+	int* overflowJoints;
+	int* pendingJointOps; // joint ids whose colour must be assigned at next step
+	int pendingJointCount;
+
+	// ---------------- finalize / events ----------------
+	int* fastBodies;
+	int* beginEv; // [2*i] shapeA shapeB
+	int* endEv;
+	int* hitEvI;
+	float* hitEvF; // [5*i] point normal approachSpeed
+	int* moveEvBody;
+	float4* moveEvXf;
+	int* staticShapes; // compact list of static proxies (CCD candidates)
+	int staticCount;
+
+	DScalars* sc;
+	int* sortTemp;
+};
+
+__host__ __device__ __forceinline__ int body_type( int f )
+{
+	return ( f >> BF_TYPE_SHIFT ) & 3;
+}
+__host__ __device__ __forceinline__ int shape_type( int f )
+{
+	return ( f >> SF_TYPE_SHIFT ) & 7;
+}

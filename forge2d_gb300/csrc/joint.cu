@@ -1,0 +1,105 @@
+// Joint preparation and the per-colour joint slot lists of the solver.
+// Reference: packages/forge2d/third_party/box2d/src/joint.c:1346-1352
+// (softness clamp), revolute_joint.c:195-259 (b2PrepareRevoluteJoint).
+#include "joint.cuh"
+
+__global__ void k_prepare_joints( DWorld w, float h, float inv_h, Soft jointSoft )
+{
+	int n = w.jointCount;
+	for ( int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x )
+	{
+		if ( ( w.jflags[j] & JF_USED ) == 0 )
+			continue;
+		int2 jb = w.jbody[j];
+		int a = jb.x, b = jb.y;
+		int fa = w.bflags[a], fb = w.bflags[b];
+		float4 ma = w.massv[a], mb = w.massv[b];
+		float mA = ma.x, iA = ma.y, mB = mb.x, iB = mb.y;
+		w.jprepM[j] = make_float4( mA, iA, mB, iB );
+		w.jindex[j] = make_int2( body_type( fa ) == 0 ? -1 : a, body_type( fb ) == 0 ? -1 : b );
+		float4 xa = w.xf[a], xb = w.xf[b];
+		frot qA, qB;
+		qA.c = xa.z;
+		qA.s = xa.w;
+		qB.c = xb.z;
+		qB.s = xb.w;
+		float4 d0 = w.jdef0[j];
+		float2 lca = w.localCenter[a], lcb = w.localCenter[b];
+		fv2 anchorA = rrot( qA, vsub( mk( d0.x, d0.y ), mk( lca.x, lca.y ) ) );
+		fv2 anchorB = rrot( qB, vsub( mk( d0.z, d0.w ), mk( lcb.x, lcb.y ) ) );
+		float2 ca = w.center[a], cb = w.center[b];
+		fv2 deltaCenter = vsub( mk( cb.x, cb.y ), mk( ca.x, ca.y ) );
+		float deltaAngle = relative_angle( qB, qA );
+		float k = iA + iB;
+		float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+		float4 d1 = w.jdef1[j];
+		Soft spring = make_soft( d1.z, d1.w, h );
+		w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+		w.jprep1[j] = make_float4( deltaCenter.x, deltaCenter.y, deltaAngle, axialMass );
+		w.jprep2[j] = make_float4( spring.biasRate, spring.massScale, spring.impulseScale, 0.0f );
+		w.jprep2[w.jointCap + j] = make_float4( jointSoft.biasRate, jointSoft.massScale, jointSoft.impulseScale, 0.0f );
+		if ( w.enableWarmStarting == 0 )
+		{
+			w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			w.jimp2[j] = make_float2( 0.0f, 0.0f );
+		}
+	}
+}
+
+__global__ void k_joint_count( DWorld w, int* cnt )
+{
+	int n = w.jointCount;
+	for ( int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x )
+	{
+		int c = w.jcolor[j];
+		if ( ( w.jflags[j] & JF_USED ) && c >= 0 && c < F2D_OVERFLOW )
+			atomicAdd( cnt + c, 1 );
+	}
+}
+
+__global__ void k_joint_offsets( int* cnt, int* start )
+{
+	if ( threadIdx.x != 0 || blockIdx.x != 0 )
+		return;
+	int s = 0;
+	for ( int c = 0; c < F2D_OVERFLOW; ++c )
+	{
+		start[c] = s;
+		s += cnt[c];
+		cnt[c] = 0;
+	}
+	start[F2D_OVERFLOW] = s;
+}
+
+__global__ void k_joint_fill( DWorld w, int* cnt, const int* start, int* slots )
+{
+	int n = w.jointCount;
+	for ( int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x )
+	{
+		int c = w.jcolor[j];
+		if ( ( w.jflags[j] & JF_USED ) && c >= 0 && c < F2D_OVERFLOW )
+			slots[start[c] + atomicAdd( cnt + c, 1 )] = j;
+	}
+}
+
+__global__ void k_zero_small( int* p, int n )
+{
+	if ( threadIdx.x < n )
+		p[threadIdx.x] = 0;
+}
+
+void launch_prepare_joints( DWorld& w, StepScratch& s, cudaStream_t st, float h, float inv_h, Soft jointSoft )
+{
+	int* slots = s.tmpB;
+	int* start = s.tmpB + w.jointCap;
+	int* cnt = start + F2D_COLORS + 4;
+	k_zero_small<<<1, 32, 0, st>>>( cnt, F2D_COLORS );
+	if ( w.jointCount > 0 )
+	{
+		k_prepare_joints<<<grid_for( w.jointCount ), 256, 0, st>>>( w, h, inv_h, jointSoft );
+		k_joint_count<<<grid_for( w.jointCount ), 256, 0, st>>>( w, cnt );
+	}
+	k_joint_offsets<<<1, 1, 0, st>>>( cnt, start );
+	if ( w.jointCount > 0 )
+		k_joint_fill<<<grid_for( w.jointCount ), 256, 0, st>>>( w, cnt, start, slots );
+}

@@ -1,0 +1,42 @@
+// Shared launch helpers and the per-phase launch entry points of the step.
+#pragma once
+
+#include "dworld.cuh"
+
+#include <cuda_runtime.h>
+
+#define F2D_SMS 152 // GB300: 2 dies x 76 SMs
+
+// Grid for a grid-stride kernel over `cap` items: whole waves of the
+// 152 SMs, at most 8 resident 256-thread blocks per SM.
+static inline int grid_for( int cap )
+{
+	int blocks = ( cap + 255 ) / 256;
+	if ( blocks < 1 )
+		blocks = 1;
+	int maxBlocks = F2D_SMS * 8;
+	if ( blocks > maxBlocks )
+		blocks = maxBlocks;
+	return blocks;
+}
+
+// Step scratch owned by the host world; device pointers only.
+struct StepScratch
+{
+	int* tmpA;	  // >= max(shapeCap, contactCap, bodyCap) ints
+	int* tmpB;
+	int* scanTmp; // scan tile sums
+	float4* bounds;
+	int boundsBlocks;
+	int shapeIdBits;
+	int solverBlocks;  // persistent solver grid (co-resident)
+	int solverThreads;
+};
+
+void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode );
+void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st );
+void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st );
+void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps );
+void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
+void launch_joint_ops( DWorld& w, cudaStream_t st );
+int solver_max_blocks( int threads );

@@ -1,0 +1,186 @@
+// Narrowphase of the world step: one thread per live contact refreshes its
+// manifold, carries warm-start impulses over by point id and raises the
+// state-change flags, as b2CollideTask + b2UpdateContact do
+// (packages/forge2d/third_party/box2d/src/world.c:357-445,
+// contact.c:472-600). The contacts that changed state are then compacted in
+// contact-id order, the order in which the reference applies them serially
+// (world.c:586-686).
+#include "dnarrow.cuh"
+#include "dscan.cuh"
+#include "dworld.cuh"
+#include "kernels.cuh"
+
+#define NP_THREADS 128
+
+__device__ __forceinline__ float shape_radius( int type, const float4* g )
+{
+	return ( type == ST_CIRCLE || type == ST_CAPSULE || type == ST_POLYGON ) ? g[1].x : 0.0f;
+}
+
+__global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
+{
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int flags = w.cflags[c];
+		if ( ( flags & CF_USED ) == 0 )
+			continue;
+		int2 sh = w.cshape[c];
+		fbox fa = box_from4( w.fat[sh.x] );
+		fbox fb = box_from4( w.fat[sh.y] );
+		if ( !box_overlaps( fa, fb ) )
+		{
+			flags |= CF_DISJOINT;
+			flags &= ~CF_SIM_TOUCHING;
+			w.cflags[c] = flags;
+			continue;
+		}
+		bool wasTouching = ( flags & CF_SIM_TOUCHING ) != 0;
+		int2 bd = w.cbody[c];
+		float4 ma = w.massv[bd.x], mb = w.massv[bd.y];
+		w.cmass[c] = make_float4( ma.x, ma.y, mb.x, mb.y );
+		float4 xa4 = w.xf[bd.x], xb4 = w.xf[bd.y];
+		fxf xfA, xfB;
+		xfA.p = mk( xa4.x, xa4.y );
+		xfA.q.c = xa4.z;
+		xfA.q.s = xa4.w;
+		xfB.p = mk( xb4.x, xb4.y );
+		xfB.q.c = xb4.z;
+		xfB.q.s = xb4.w;
+		float2 lca = w.localCenter[bd.x], lcb = w.localCenter[bd.y];
+		fv2 offA = rrot( xfA.q, mk( lca.x, lca.y ) );
+		fv2 offB = rrot( xfB.q, mk( lcb.x, lcb.y ) );
+		int sfa = w.sflags[sh.x], sfb = w.sflags[sh.y];
+		int ta = shape_type( sfa ), tb = shape_type( sfb );
+		const float4* ga = w.geom + (size_t)sh.x * GEOM_F4;
+		const float4* gb = w.geom + (size_t)sh.y * GEOM_F4;
+		DGeom A = load_geom( ga, ta );
+		DGeom B = load_geom( gb, tb );
+		DManifold m = compute_manifold( A, xfA, B, xfB );
+
+		float4 mta = w.mat[sh.x], mtb = w.mat[sh.y];
+		float friction = sqrtf( mta.x * mtb.x );
+		float restitution = mta.y > mtb.y ? mta.y : mtb.y;
+		float rolling = 0.0f;
+		if ( mta.z > 0.0f || mtb.z > 0.0f )
+		{
+			float ra = shape_radius( ta, ga ), rb = shape_radius( tb, gb );
+			float mr = fmax_s( ra, rb );
+			rolling = fmax_s( mta.z, mtb.z ) * mr;
+		}
+		float tangentSpeed = mta.w + mtb.w;
+		w.cmat[c] = make_float4( friction, restitution, rolling, tangentSpeed );
+
+		int pointCount = m.count;
+		bool touching = pointCount > 0;
+		if ( touching && ( ( sfa | sfb ) & SF_HIT_EVENTS ) )
+			flags |= CF_HIT_EVENT;
+		else
+			flags &= ~CF_HIT_EVENT;
+
+		// old manifold (ids and impulses)
+		float4 oldN = w.mnorm[c];
+		int oldCount = __float_as_int( oldN.w );
+		unsigned oldId[2];
+		float oldNI[2], oldTI[2];
+		for ( int k = 0; k < 2; ++k )
+		{
+			oldId[k] = (unsigned)__float_as_int( w.mpB[2 * c + k].w ) & 0xffffu;
+			float4 im = w.mpI[2 * c + k];
+			oldNI[k] = im.x;
+			oldTI[k] = im.y;
+		}
+		float rollingImpulse = pointCount > 0 ? oldN.z : 0.0f;
+		fv2 normal = pointCount > 0 ? m.normal : mk( 0.0f, 0.0f );
+		w.mnorm[c] = make_float4( normal.x, normal.y, rollingImpulse, __int_as_float( pointCount ) );
+		for ( int i = 0; i < 2; ++i )
+		{
+			if ( i < pointCount )
+			{
+				DPoint p = m.p[i];
+				fv2 anchorA = vsub( p.anchorA, offA );
+				fv2 anchorB = vsub( p.anchorB, offB );
+				float ni = 0.0f, ti = 0.0f;
+				int persisted = 0;
+				for ( int j = 0; j < oldCount; ++j )
+				{
+					if ( oldId[j] == p.id )
+					{
+						ni = oldNI[j];
+						ti = oldTI[j];
+						persisted = 1;
+						oldNI[j] = 0.0f;
+						oldTI[j] = 0.0f;
+						break;
+					}
+				}
+				w.mpA[2 * c + i] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+				w.mpB[2 * c + i] = make_float4( p.point.x, p.point.y, p.separation,
+												__int_as_float( (int)( p.id | ( persisted << 16 ) ) ) );
+				w.mpI[2 * c + i] = make_float4( ni, ti, 0.0f, 0.0f );
+			}
+			else
+			{
+				w.mpA[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+				w.mpB[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, __int_as_float( 0 ) );
+				w.mpI[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			}
+		}
+		if ( touching )
+			flags |= CF_SIM_TOUCHING;
+		else
+			flags &= ~CF_SIM_TOUCHING;
+		if ( touching && !wasTouching )
+			flags |= CF_STARTED;
+		else if ( !touching && wasTouching )
+			flags |= CF_STOPPED;
+		w.cflags[c] = flags;
+	}
+}
+
+__global__ void k_op_flags( DWorld w, int* flags )
+{
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int f = w.cflags[c];
+		flags[c] = ( ( f & CF_USED ) && ( f & ( CF_DISJOINT | CF_STARTED | CF_STOPPED ) ) ) ? 1 : 0;
+	}
+}
+
+__global__ void k_op_compact( DWorld w, const int* flags, const int* offs )
+{
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		if ( flags[c] == 0 )
+			continue;
+		int o = offs[c];
+		if ( o >= w.opCap )
+		{
+			atomicOr( &w.sc->error, ERR_OP_CAPACITY );
+			continue;
+		}
+		int f = w.cflags[c];
+		w.opContact[o] = c;
+		w.opKind[o] = ( f & CF_DISJOINT ) ? 0 : ( ( f & CF_STARTED ) ? 1 : 2 );
+	}
+}
+
+__global__ void k_op_clamp( DWorld w )
+{
+	if ( w.sc->opCount > w.opCap )
+		w.sc->opCount = w.opCap;
+}
+
+void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st )
+{
+	int g = ( w.contactCap + NP_THREADS - 1 ) / NP_THREADS;
+	if ( g > F2D_SMS * 16 )
+		g = F2D_SMS * 16;
+	k_narrowphase<<<g, NP_THREADS, 0, st>>>( w );
+	k_op_flags<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA );
+	scan_exclusive( s.tmpA, s.tmpB, s.scanTmp, &w.sc->contactIdCount, 0, w.contactCap, &w.sc->opCount, st );
+	k_op_compact<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA, s.tmpB );
+	k_op_clamp<<<1, 1, 0, st>>>( w );
+}

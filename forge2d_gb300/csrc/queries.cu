@@ -1,0 +1,438 @@
+// World queries: closest ray hit and AABB overlap.
+//
+// Box2D v3.1.1 walks its three dynamic trees for these (world.c:2071-2098
+// b2World_OverlapAABB tests tree boxes, i.e. fat AABBs, plus
+// b2ShouldQueryCollide; world.c:2222-2300 b2World_CastRayClosest clips the
+// ray with each hit, ignoring hits at fraction 0). A query here is one thread
+// per shape over the device rows: every candidate is tested against the full
+// ray and the closest hit is picked with one 64-bit atomicMin on
+// (fraction bits, shape id), so ties resolve to the lower shape id.
+// Shape ray casts follow geometry.c:506-760 (circle, capsule, segment,
+// polygon with zero radius).
+#include "dmath.cuh"
+#include "dworld.cuh"
+#include "kernels.cuh"
+
+#include "../../include/forge2d_gb300.h"
+
+#include <algorithm>
+#include <vector>
+
+struct RayHit
+{
+	bool hit;
+	fv2 point, normal;
+	float fraction;
+};
+
+__device__ RayHit ray_circle( fv2 origin, fv2 translation, float maxFraction, fv2 p, float r )
+{
+	RayHit out;
+	out.hit = false;
+	out.fraction = 0.0f;
+	out.point = out.normal = mk( 0.0f, 0.0f );
+	fv2 s = vsub( origin, p );
+	float rr = r * r;
+	float length;
+	fv2 d = vlen_norm( &length, translation );
+	if ( length == 0.0f )
+	{
+		if ( vlen2( s ) < rr )
+		{
+			out.point = origin;
+			out.hit = true;
+		}
+		return out;
+	}
+	float t = -vdot( s, d );
+	fv2 c = vmuladd( s, t, d );
+	float cc = vdot( c, c );
+	if ( cc > rr )
+		return out;
+	float h = sqrtf( rr - cc );
+	float fraction = t - h;
+	if ( fraction < 0.0f || maxFraction * length < fraction )
+	{
+		if ( vlen2( s ) < rr )
+		{
+			out.point = origin;
+			out.hit = true;
+		}
+		return out;
+	}
+	fv2 hitPoint = vmuladd( s, fraction, d );
+	out.fraction = fraction / length;
+	out.normal = vnormalize( hitPoint );
+	out.point = vmuladd( p, r, out.normal );
+	out.hit = true;
+	return out;
+}
+
+__device__ RayHit ray_capsule( fv2 origin, fv2 translation, float maxFraction, fv2 v1, fv2 v2, float radius )
+{
+	RayHit out;
+	out.hit = false;
+	out.fraction = 0.0f;
+	out.point = out.normal = mk( 0.0f, 0.0f );
+	fv2 e = vsub( v2, v1 );
+	float capsuleLength;
+	fv2 a = vlen_norm( &capsuleLength, e );
+	if ( capsuleLength < FLT_EPSILON )
+		return ray_circle( origin, translation, maxFraction, v1, radius );
+	fv2 p1 = origin;
+	fv2 d = translation;
+	fv2 q = vsub( p1, v1 );
+	float qa = vdot( q, a );
+	fv2 qp = vmuladd( q, -qa, a );
+	if ( vdot( qp, qp ) < radius * radius )
+	{
+		if ( qa < 0.0f )
+			return ray_circle( origin, translation, maxFraction, v1, radius );
+		if ( qa > capsuleLength )
+			return ray_circle( origin, translation, maxFraction, v2, radius );
+		out.point = origin;
+		out.hit = true;
+		return out;
+	}
+	fv2 n = mk( a.y, -a.x );
+	float rayLength;
+	fv2 u = vlen_norm( &rayLength, d );
+	float den = -a.x * u.y + u.x * a.y;
+	if ( -FLT_EPSILON < den && den < FLT_EPSILON )
+		return out;
+	fv2 b1 = vmulsub( q, radius, n );
+	fv2 b2 = vmuladd( q, radius, n );
+	float invDen = 1.0f / den;
+	float s21 = ( a.x * b1.y - b1.x * a.y ) * invDen;
+	float s22 = ( a.x * b2.y - b2.x * a.y ) * invDen;
+	float s2;
+	fv2 b;
+	if ( s21 < s22 )
+	{
+		s2 = s21;
+		b = b1;
+	}
+	else
+	{
+		s2 = s22;
+		b = b2;
+		n = vneg( n );
+	}
+	if ( s2 < 0.0f || maxFraction * rayLength < s2 )
+		return out;
+	float s1 = ( -b.x * u.y + u.x * b.y ) * invDen;
+	if ( s1 < 0.0f )
+		return ray_circle( origin, translation, maxFraction, v1, radius );
+	if ( capsuleLength < s1 )
+		return ray_circle( origin, translation, maxFraction, v2, radius );
+	out.fraction = s2 / rayLength;
+	out.point = vadd( vlerp( v1, v2, s1 / capsuleLength ), vscale( radius, n ) );
+	out.normal = n;
+	out.hit = true;
+	return out;
+}
+
+__device__ RayHit ray_segment( fv2 origin, fv2 translation, float maxFraction, fv2 v1, fv2 v2 )
+{
+	RayHit out;
+	out.hit = false;
+	out.fraction = 0.0f;
+	out.point = out.normal = mk( 0.0f, 0.0f );
+	fv2 e = vsub( v2, v1 );
+	float length;
+	fv2 eUnit = vlen_norm( &length, e );
+	if ( length == 0.0f )
+		return out;
+	fv2 normal = vright( eUnit );
+	float numerator = vdot( normal, vsub( v1, origin ) );
+	float denominator = vdot( normal, translation );
+	if ( denominator == 0.0f )
+		return out;
+	float t = numerator / denominator;
+	if ( t < 0.0f || maxFraction < t )
+		return out;
+	fv2 p = vmuladd( origin, t, translation );
+	float s = vdot( vsub( p, v1 ), eUnit );
+	if ( s < 0.0f || length < s )
+		return out;
+	if ( numerator > 0.0f )
+		normal = vneg( normal );
+	out.fraction = t;
+	out.point = p;
+	out.normal = normal;
+	out.hit = true;
+	return out;
+}
+
+__device__ RayHit ray_polygon( fv2 origin, fv2 d, float maxFraction, const float4* g )
+{
+	RayHit out;
+	out.hit = false;
+	out.fraction = 0.0f;
+	out.point = out.normal = mk( 0.0f, 0.0f );
+	int count = __float_as_int( g[1].y );
+	fv2 v[F2D_MAX_POLY], n[F2D_MAX_POLY];
+	for ( int i = 0; i < 4; ++i )
+	{
+		float4 a = g[2 + i], b = g[6 + i];
+		v[2 * i] = mk( a.x, a.y );
+		v[2 * i + 1] = mk( a.z, a.w );
+		n[2 * i] = mk( b.x, b.y );
+		n[2 * i + 1] = mk( b.z, b.w );
+	}
+	fv2 base = v[0];
+	fv2 p1 = vsub( origin, base );
+	float lower = 0.0f, upper = maxFraction;
+	int index = -1;
+	for ( int i = 0; i < count; ++i )
+	{
+		fv2 vertex = vsub( v[i], base );
+		float numerator = vdot( n[i], vsub( vertex, p1 ) );
+		float denominator = vdot( n[i], d );
+		if ( denominator == 0.0f )
+		{
+			if ( numerator < 0.0f )
+				return out;
+		}
+		else
+		{
+			if ( denominator < 0.0f && numerator < lower * denominator )
+			{
+				lower = numerator / denominator;
+				index = i;
+			}
+			else if ( denominator > 0.0f && numerator < upper * denominator )
+				upper = numerator / denominator;
+		}
+		if ( upper < lower )
+			return out;
+	}
+	if ( index >= 0 )
+	{
+		out.fraction = lower;
+		out.normal = n[index];
+		out.point = vmuladd( origin, lower, d );
+		out.hit = true;
+	}
+	else
+	{
+		out.point = origin;
+		out.hit = true;
+	}
+	return out;
+}
+
+__device__ __forceinline__ bool query_collide( const DWorld& w, int s, unsigned long long cat,
+											   unsigned long long msk )
+{
+	return ( w.cat[s] & msk ) != 0ull && ( w.mask[s] & cat ) != 0ull;
+}
+
+__device__ __forceinline__ float ray_box_enter( fbox b, fv2 o, fv2 t )
+{
+	// slab test of the ray segment o + s t, s in [0,1]; returns entry or 2 (miss)
+	float tmin = 0.0f, tmax = 1.0f;
+	float lo[2] = { b.lo.x, b.lo.y }, hi[2] = { b.hi.x, b.hi.y }, oo[2] = { o.x, o.y }, tt[2] = { t.x, t.y };
+	for ( int k = 0; k < 2; ++k )
+	{
+		if ( fabsf( tt[k] ) < FLT_EPSILON )
+		{
+			if ( oo[k] < lo[k] || hi[k] < oo[k] )
+				return 2.0f;
+		}
+		else
+		{
+			float inv = 1.0f / tt[k];
+			float t1 = ( lo[k] - oo[k] ) * inv, t2 = ( hi[k] - oo[k] ) * inv;
+			if ( t1 > t2 )
+			{
+				float x = t1;
+				t1 = t2;
+				t2 = x;
+			}
+			tmin = fmaxf( tmin, t1 );
+			tmax = fminf( tmax, t2 );
+			if ( tmin > tmax )
+				return 2.0f;
+		}
+	}
+	return tmin;
+}
+
+__global__ void k_ray_closest( DWorld w, fv2 origin, fv2 translation, unsigned long long cat, unsigned long long msk,
+							   unsigned long long* best )
+{
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+	{
+		int f = w.sflags[s];
+		if ( ( f & ( SF_USED | SF_PROXY ) ) != ( SF_USED | SF_PROXY ) )
+			continue;
+		if ( ( w.cat[s] & msk ) == 0ull || !query_collide( w, s, cat, msk ) )
+			continue;
+		if ( ray_box_enter( box_from4( w.fat[s] ), origin, translation ) > 1.0f )
+			continue;
+		int b = w.shapeBody[s];
+		float4 x4 = w.xf[b];
+		fxf xf;
+		xf.p = mk( x4.x, x4.y );
+		xf.q.c = x4.z;
+		xf.q.s = x4.w;
+		// shape.c:792-832: cast in the shape's local frame
+		fv2 lo = rinvrot( xf.q, vsub( origin, xf.p ) );
+		fv2 lt = rinvrot( xf.q, translation );
+		const float4* g = w.geom + (size_t)s * GEOM_F4;
+		float4 g0 = g[0], g1 = g[1];
+		int type = shape_type( f );
+		RayHit h;
+		if ( type == ST_CIRCLE )
+			h = ray_circle( lo, lt, 1.0f, mk( g0.x, g0.y ), g1.x );
+		else if ( type == ST_CAPSULE )
+			h = ray_capsule( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ), g1.x );
+		else if ( type == ST_SEGMENT )
+			h = ray_segment( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ) );
+		else
+			h = ray_polygon( lo, lt, 1.0f, g );
+		if ( !h.hit || h.fraction == 0.0f )
+			continue;
+		unsigned long long key = ( (unsigned long long)__float_as_uint( h.fraction ) << 32 ) | (unsigned)s;
+		atomicMin( best, key );
+	}
+}
+
+__global__ void k_ray_result( DWorld w, fv2 origin, fv2 translation, const unsigned long long* best, float* out )
+{
+	unsigned long long key = *best;
+	if ( key == ~0ull )
+	{
+		out[5] = -1.0f;
+		return;
+	}
+	int s = (int)( key & 0xffffffffull );
+	int b = w.shapeBody[s];
+	float4 x4 = w.xf[b];
+	fxf xf;
+	xf.p = mk( x4.x, x4.y );
+	xf.q.c = x4.z;
+	xf.q.s = x4.w;
+	fv2 lo = rinvrot( xf.q, vsub( origin, xf.p ) );
+	fv2 lt = rinvrot( xf.q, translation );
+	const float4* g = w.geom + (size_t)s * GEOM_F4;
+	float4 g0 = g[0], g1 = g[1];
+	int type = shape_type( w.sflags[s] );
+	RayHit h;
+	if ( type == ST_CIRCLE )
+		h = ray_circle( lo, lt, 1.0f, mk( g0.x, g0.y ), g1.x );
+	else if ( type == ST_CAPSULE )
+		h = ray_capsule( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ), g1.x );
+	else if ( type == ST_SEGMENT )
+		h = ray_segment( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ) );
+	else
+		h = ray_polygon( lo, lt, 1.0f, g );
+	fv2 p = xpoint( xf, h.point );
+	fv2 n = rrot( xf.q, h.normal );
+	out[0] = p.x;
+	out[1] = p.y;
+	out[2] = n.x;
+	out[3] = n.y;
+	out[4] = h.fraction;
+	out[5] = __int_as_float( s );
+}
+
+__global__ void k_overlap( DWorld w, fbox box, unsigned long long cat, unsigned long long msk, int* out, int* count,
+						   int cap )
+{
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+	{
+		int f = w.sflags[s];
+		if ( ( f & ( SF_USED | SF_PROXY ) ) != ( SF_USED | SF_PROXY ) )
+			continue;
+		if ( ( w.cat[s] & msk ) == 0ull || !query_collide( w, s, cat, msk ) )
+			continue;
+		if ( !box_overlaps( box_from4( w.fat[s] ), box ) )
+			continue;
+		int k = atomicAdd( count, 1 );
+		if ( k < cap )
+			out[k] = s;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// host entry points (world.cu owns the world table)
+// ---------------------------------------------------------------------------
+DWorld* f2d_internal_world( int32_t worldId, cudaStream_t* st, int* gens, int genCap );
+uint16_t f2d_internal_shape_gen( int32_t worldId, int shape );
+int32_t f2d_internal_world0( int32_t worldId );
+
+extern "C" F2D_API int32_t f2d_world_cast_ray_closest( int32_t worldId, double ox, double oy, double tx, double ty,
+													   int64_t categoryBits, int64_t maskBits, int32_t* shape2,
+													   float* out5 )
+{
+	cudaStream_t st;
+	DWorld* w = f2d_internal_world( worldId, &st, nullptr, 0 );
+	if ( w == nullptr )
+		return 0;
+	unsigned long long* best = nullptr;
+	float* res = nullptr;
+	cudaMalloc( (void**)&best, sizeof( unsigned long long ) );
+	cudaMalloc( (void**)&res, 6 * sizeof( float ) );
+	cudaMemsetAsync( best, 0xff, sizeof( unsigned long long ), st );
+	fv2 o = mk( (float)ox, (float)oy ), t = mk( (float)tx, (float)ty );
+	k_ray_closest<<<grid_for( w->shapeCount ), 256, 0, st>>>( *w, o, t, (unsigned long long)categoryBits,
+															   (unsigned long long)maskBits, best );
+	k_ray_result<<<1, 1, 0, st>>>( *w, o, t, best, res );
+	float h[6];
+	cudaMemcpyAsync( h, res, sizeof( h ), cudaMemcpyDeviceToHost, st );
+	cudaStreamSynchronize( st );
+	cudaFree( best );
+	cudaFree( res );
+	if ( h[5] == -1.0f )
+		return 0;
+	int s;
+	memcpy( &s, &h[5], sizeof( int ) );
+	if ( shape2 )
+	{
+		shape2[0] = s + 1;
+		shape2[1] = f2d_internal_world0( worldId ) | ( (int)f2d_internal_shape_gen( worldId, s ) << 16 );
+	}
+	if ( out5 )
+		for ( int k = 0; k < 5; ++k )
+			out5[k] = h[k];
+	return 1;
+}
+
+extern "C" F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lx, double ly, double ux, double uy,
+												   int64_t categoryBits, int64_t maskBits, int32_t* shapes2,
+												   int32_t capacity )
+{
+	cudaStream_t st;
+	DWorld* w = f2d_internal_world( worldId, &st, nullptr, 0 );
+	if ( w == nullptr )
+		return 0;
+	int cap = w->shapeCount > 0 ? w->shapeCount : 1;
+	int* out = nullptr;
+	int* count = nullptr;
+	cudaMalloc( (void**)&out, sizeof( int ) * cap );
+	cudaMalloc( (void**)&count, sizeof( int ) );
+	cudaMemsetAsync( count, 0, sizeof( int ), st );
+	fbox box;
+	box.lo = mk( (float)lx, (float)ly );
+	box.hi = mk( (float)ux, (float)uy );
+	k_overlap<<<grid_for( w->shapeCount ), 256, 0, st>>>( *w, box, (unsigned long long)categoryBits,
+														   (unsigned long long)maskBits, out, count, cap );
+	int n = 0;
+	cudaMemcpyAsync( &n, count, sizeof( int ), cudaMemcpyDeviceToHost, st );
+	cudaStreamSynchronize( st );
+	std::vector<int> ids( std::min( n, cap ) );
+	if ( !ids.empty() )
+		cudaMemcpy( ids.data(), out, sizeof( int ) * ids.size(), cudaMemcpyDeviceToHost );
+	cudaFree( out );
+	cudaFree( count );
+	std::sort( ids.begin(), ids.end() );
+	int world0 = f2d_internal_world0( worldId );
+	for ( int i = 0; i < (int)ids.size() && i < capacity; ++i )
+	{
+		shapes2[2 * i] = ids[i] + 1;
+		shapes2[2 * i + 1] = world0 | ( (int)f2d_internal_shape_gen( worldId, ids[i] ) << 16 );
+	}
+	return n;
+}

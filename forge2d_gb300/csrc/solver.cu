@@ -1,0 +1,900 @@
+// Soft-step solver of the world step, GPU-first.
+//
+// Stage order is that of b2SolverTask (packages/forge2d/third_party/box2d/
+// src/solver.c:929-1160): prepare joints and contacts; per substep integrate
+// velocities, warm start (overflow joints, overflow contacts, then graph
+// colours 0..10), solve, integrate positions, relax; then restitution and
+// impulse storage. All of it runs in one persistent cooperative kernel: the
+// colour stages are separated by grid barriers (bounded spins that raise an
+// error bit instead of hanging), the serial overflow constraints run on one
+// thread between two barriers, and within a colour one thread solves one
+// constraint (bodies within a colour are disjoint, so the slot order inside
+// a colour does not change any result).
+//
+// Constraint arithmetic: graph-colour constraints follow the operand order of
+// the reference's SIMD lanes (contact_solver.c:1438-2120, separate mul and
+// add, SSE2 min/max/blend semantics); overflow constraints follow its scalar
+// functions (contact_solver.c:24-510). Built with -fmad=false the results
+// are bit-identical to the reference C code.
+#include "dscan.cuh"
+#include "dworld.cuh"
+#include "joint.cuh"
+#include "kernels.cuh"
+
+#define SOLVER_THREADS 256
+#define BARRIER_SPIN_LIMIT ( 1ll << 25 )
+
+struct SolveParams
+{
+	float h, inv_h, dt, inv_dt;
+	Soft contactSoft, staticSoft, jointSoft;
+	float minBiasVel; // -contactSpeed (world.c:767)
+	float pushout;	  // maxContactPushSpeed (overflow path)
+	float restitutionThreshold;
+	float maxLinearSpeed, maxAngularSpeed;
+	fv2 gravity;
+	int subSteps;
+	int enableWarmStarting;
+};
+
+// ---------------------------------------------------------------------------
+// constraint slots: overflow first (overflow-array order), then colours
+// ---------------------------------------------------------------------------
+__global__ void k_count_colors( DWorld w, int* fill )
+{
+	if ( blockIdx.x == 0 && threadIdx.x < F2D_COLORS )
+	{
+		// counts are produced by the previous kernel; fill is cleared here
+	}
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int col = w.ccolor[c];
+		if ( col >= 0 && col < F2D_OVERFLOW && ( w.cflags[c] & CF_USED ) )
+			atomicAdd( fill + col, 1 );
+	}
+}
+
+__global__ void k_zero_ints( int* p, int n )
+{
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+		p[i] = 0;
+}
+
+__global__ void k_color_offsets( DWorld w, int* fill )
+{
+	if ( blockIdx.x != 0 || threadIdx.x != 0 )
+		return;
+	int start = w.sc->overflowCount;
+	for ( int c = 0; c < F2D_OVERFLOW; ++c )
+	{
+		w.sc->colorStart[c] = start;
+		w.sc->colorCount[c] = fill[c];
+		start += fill[c];
+		fill[c] = 0;
+	}
+	w.sc->colorStart[F2D_OVERFLOW] = start;
+	w.sc->colorCount[F2D_OVERFLOW] = w.sc->overflowCount;
+	w.sc->touchingCount = start;
+}
+
+__global__ void k_fill_slots( DWorld w, int* fill )
+{
+	int n = w.sc->contactIdCount;
+	int nov = w.sc->overflowCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < nov; i += gridDim.x * blockDim.x )
+		w.slotContact[i] = w.overflowList[i];
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int col = w.ccolor[c];
+		if ( col >= 0 && col < F2D_OVERFLOW && ( w.cflags[c] & CF_USED ) )
+		{
+			int slot = w.sc->colorStart[col] + atomicAdd( fill + col, 1 );
+			w.slotContact[slot] = c;
+		}
+	}
+}
+
+// contact_solver.c:1438-1669 / :24-156 (identical expressions in both)
+__global__ void k_prepare_contacts( DWorld w, SolveParams p )
+{
+	int n = w.sc->touchingCount;
+	float warmStartScale = p.enableWarmStarting ? 1.0f : 0.0f;
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x )
+	{
+		int c = w.slotContact[k];
+		int2 bd = w.cbody[c];
+		int ia = body_type( w.bflags[bd.x] ) == 0 ? -1 : bd.x;
+		int ib = body_type( w.bflags[bd.y] ) == 0 ? -1 : bd.y;
+		float4 cm = w.cmass[c];
+		float mA = cm.x, iA = cm.y, mB = cm.z, iB = cm.w;
+		// constraint_graph.c:139-181: a static side carries zero mass
+		if ( ia < 0 )
+		{
+			mA = 0.0f;
+			iA = 0.0f;
+		}
+		if ( ib < 0 )
+		{
+			mB = 0.0f;
+			iB = 0.0f;
+		}
+		fv2 vA = mk( 0.0f, 0.0f ), vB = mk( 0.0f, 0.0f );
+		float wA = 0.0f, wB = 0.0f;
+		if ( ia >= 0 )
+		{
+			float4 v = w.vel[ia];
+			vA = mk( v.x, v.y );
+			wA = v.z;
+		}
+		if ( ib >= 0 )
+		{
+			float4 v = w.vel[ib];
+			vB = mk( v.x, v.y );
+			wB = v.z;
+		}
+		float kk = iA + iB;
+		float rollingMass = kk > 0.0f ? 1.0f / kk : 0.0f;
+		Soft soft = ( ia < 0 || ib < 0 ) ? p.staticSoft : p.contactSoft;
+		float4 mn = w.mnorm[c];
+		fv2 normal = mk( mn.x, mn.y );
+		int pointCount = __float_as_int( mn.w );
+		float4 cmat = w.cmat[c];
+		w.kIndex[k] = make_int2( ia, ib );
+		w.kMass[k] = make_float4( mA, iA, mB, iB );
+		w.kNormal[k] = make_float4( normal.x, normal.y, cmat.x, cmat.w );
+		w.kMisc[k] = make_float4( cmat.y, cmat.z, rollingMass, warmStartScale * mn.z );
+		w.kSoft[k] = make_float4( soft.biasRate, soft.massScale, soft.impulseScale, __int_as_float( pointCount ) );
+		fv2 tangent = vright( normal );
+		float4 anch[2], pp[2];
+		float ni[2], ti[2];
+		for ( int j = 0; j < 2; ++j )
+		{
+			if ( j >= pointCount )
+			{
+				anch[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+				pp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+				ni[j] = 0.0f;
+				ti[j] = 0.0f;
+				continue;
+			}
+			float4 a = w.mpA[2 * c + j];
+			float4 b = w.mpB[2 * c + j];
+			float4 im = w.mpI[2 * c + j];
+			fv2 rA = mk( a.x, a.y ), rB = mk( a.z, a.w );
+			anch[j] = a;
+			float baseSeparation = b.z - vdot( vsub( rB, rA ), normal );
+			ni[j] = warmStartScale * im.x;
+			ti[j] = warmStartScale * im.y;
+			float rnA = vcross( rA, normal );
+			float rnB = vcross( rB, normal );
+			float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+			float normalMass = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+			float rtA = vcross( rA, tangent );
+			float rtB = vcross( rB, tangent );
+			float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+			float tangentMass = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+			fv2 vrA = vadd( vA, vcrossSV( wA, rA ) );
+			fv2 vrB = vadd( vB, vcrossSV( wB, rB ) );
+			float relVel = vdot( normal, vsub( vrB, vrA ) );
+			pp[j] = make_float4( baseSeparation, normalMass, tangentMass, relVel );
+		}
+		w.kAnch1[k] = anch[0];
+		w.kAnch2[k] = anch[1];
+		w.kP1[k] = pp[0];
+		w.kP2[k] = pp[1];
+		w.kImp[k] = make_float4( ni[0], ni[1], ti[0], ti[1] );
+		w.kTot[k] = make_float2( 0.0f, 0.0f );
+	}
+}
+
+// ---------------------------------------------------------------------------
+// body state access: static bodies read as the identity state and are never
+// written (contact_solver.c:1184-1222)
+// ---------------------------------------------------------------------------
+struct BState
+{
+	float vx, vy, w;
+	float dpx, dpy, dqc, dqs;
+};
+
+__device__ __forceinline__ BState load_state( const DWorld& w, int i )
+{
+	BState s;
+	if ( i < 0 )
+	{
+		s.vx = s.vy = s.w = 0.0f;
+		s.dpx = s.dpy = 0.0f;
+		s.dqc = 1.0f;
+		s.dqs = 0.0f;
+		return s;
+	}
+	float4 v = __ldcg( w.vel + i );
+	float4 d = __ldcg( w.delta + i );
+	s.vx = v.x;
+	s.vy = v.y;
+	s.w = v.z;
+	s.dpx = d.x;
+	s.dpy = d.y;
+	s.dqc = d.z;
+	s.dqs = d.w;
+	return s;
+}
+
+__device__ __forceinline__ void store_vel( const DWorld& w, int i, const BState& s )
+{
+	if ( i < 0 )
+		return;
+	__stcg( w.vel + i, make_float4( s.vx, s.vy, s.w, 0.0f ) );
+}
+
+__device__ __forceinline__ float lmax( float a, float b )
+{
+	return a > b ? a : b;
+}
+__device__ __forceinline__ float lmin( float a, float b )
+{
+	return a < b ? a : b;
+}
+
+// contact_solver.c:1671-1727
+static __device__ void warm_lane( const DWorld& w, int k )
+{
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float4 nm = w.kNormal[k];
+	float4 imp = __ldcg( w.kImp + k );
+	float4 misc = __ldcg( w.kMisc + k );
+	float tx = nm.y;
+	float ty = 0.0f - nm.x;
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tis[2] = { imp.z, imp.w };
+	for ( int j = 0; j < 2; ++j )
+	{
+		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float Px = nis[j] * nm.x + tis[j] * tx;
+		float Py = nis[j] * nm.y + tis[j] * ty;
+		A.w = A.w - ms.y * ( rAx * Py - rAy * Px );
+		A.vx = A.vx - ms.x * Px;
+		A.vy = A.vy - ms.x * Py;
+		B.w = B.w + ms.w * ( rBx * Py - rBy * Px );
+		B.vx = B.vx + ms.z * Px;
+		B.vy = B.vy + ms.z * Py;
+	}
+	A.w = A.w - ms.y * misc.w;
+	B.w = B.w + ms.w * misc.w;
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// contact_solver.c:1729-1967
+static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float minBiasVel, bool useBias )
+{
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float4 nm = w.kNormal[k];
+	float4 sf = w.kSoft[k];
+	float4 misc = __ldcg( w.kMisc + k );
+	float4 imp = __ldcg( w.kImp + k );
+	float2 tot = __ldcg( w.kTot + k );
+	float biasRate, massScale, impulseScale;
+	if ( useBias )
+	{
+		biasRate = sf.x;
+		massScale = sf.y;
+		impulseScale = sf.z;
+	}
+	else
+	{
+		biasRate = 0.0f;
+		massScale = 1.0f;
+		impulseScale = 0.0f;
+	}
+	float totalNormalImpulse = 0.0f;
+	float dpx = B.dpx - A.dpx;
+	float dpy = B.dpy - A.dpy;
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float4 pt[2] = { w.kP1[k], w.kP2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tis[2] = { imp.z, imp.w };
+	float tots[2] = { tot.x, tot.y };
+	for ( int j = 0; j < 2; ++j )
+	{
+		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float rsAx = A.dqc * rAx - A.dqs * rAy;
+		float rsAy = A.dqs * rAx + A.dqc * rAy;
+		float rsBx = B.dqc * rBx - B.dqs * rBy;
+		float rsBy = B.dqs * rBx + B.dqc * rBy;
+		float dsx = dpx + ( rsBx - rsAx );
+		float dsy = dpy + ( rsBy - rsAy );
+		float s = ( nm.x * dsx + nm.y * dsy ) + pt[j].x;
+		bool mask = s > 0.0f;
+		float specBias = s * inv_h;
+		float softBias = lmax( biasRate * s, minBiasVel );
+		float bias = mask ? specBias : softBias;
+		float pointMassScale = mask ? 1.0f : massScale;
+		float pointImpulseScale = mask ? 0.0f : impulseScale;
+		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
+		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
+		float vn = dvx * nm.x + dvy * nm.y;
+		float negImpulse = pt[j].y * ( pointMassScale * ( vn + bias ) ) + pointImpulseScale * nis[j];
+		float newImpulse = lmax( nis[j] - negImpulse, 0.0f );
+		float impulse = newImpulse - nis[j];
+		nis[j] = newImpulse;
+		tots[j] = tots[j] + newImpulse;
+		totalNormalImpulse = totalNormalImpulse + newImpulse;
+		float Px = impulse * nm.x;
+		float Py = impulse * nm.y;
+		A.vx = A.vx - ms.x * Px;
+		A.vy = A.vy - ms.x * Py;
+		A.w = A.w - ms.y * ( rAx * Py - rAy * Px );
+		B.vx = B.vx + ms.z * Px;
+		B.vy = B.vy + ms.z * Py;
+		B.w = B.w + ms.w * ( rBx * Py - rBy * Px );
+	}
+	float tx = nm.y;
+	float ty = 0.0f - nm.x;
+	for ( int j = 0; j < 2; ++j )
+	{
+		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
+		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
+		float vt = dvx * tx + dvy * ty;
+		vt = vt - nm.w;
+		float negImpulse = pt[j].z * vt;
+		float maxFriction = nm.z * nis[j];
+		float newImpulse = tis[j] - negImpulse;
+		newImpulse = lmax( 0.0f - maxFriction, lmin( newImpulse, maxFriction ) );
+		float impulse = newImpulse - tis[j];
+		tis[j] = newImpulse;
+		float Px = impulse * tx;
+		float Py = impulse * ty;
+		A.vx = A.vx - ms.x * Px;
+		A.vy = A.vy - ms.x * Py;
+		A.w = A.w - ms.y * ( rAx * Py - rAy * Px );
+		B.vx = B.vx + ms.z * Px;
+		B.vy = B.vy + ms.z * Py;
+		B.w = B.w + ms.w * ( rBx * Py - rBy * Px );
+	}
+	{
+		float deltaLambda = misc.z * ( A.w - B.w );
+		float lambda = misc.w;
+		float maxLambda = misc.y * totalNormalImpulse;
+		float nb = -maxLambda;
+		float r = lmax( nb, lmin( lambda + deltaLambda, maxLambda ) );
+		misc.w = r;
+		deltaLambda = r - lambda;
+		A.w = A.w - ms.y * deltaLambda;
+		B.w = B.w + ms.w * deltaLambda;
+	}
+	__stcg( w.kImp + k, make_float4( nis[0], nis[1], tis[0], tis[1] ) );
+	__stcg( w.kTot + k, make_float2( tots[0], tots[1] ) );
+	__stcg( w.kMisc + k, misc );
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// contact_solver.c:1969-2076 (lanes with restitution 0 are unchanged)
+static __device__ void restitution_lane( const DWorld& w, int k, float threshold )
+{
+	float4 misc = __ldcg( w.kMisc + k );
+	float restitution = misc.x;
+	if ( restitution == 0.0f )
+		return;
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float4 nm = w.kNormal[k];
+	float4 imp = __ldcg( w.kImp + k );
+	float2 tot = __ldcg( w.kTot + k );
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float4 pt[2] = { w.kP1[k], w.kP2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tots[2] = { tot.x, tot.y };
+	for ( int j = 0; j < 2; ++j )
+	{
+		bool mask1 = ( pt[j].w + threshold ) > 0.0f;
+		bool mask2 = tots[j] == 0.0f;
+		float mass = ( mask1 || mask2 ) ? 0.0f : pt[j].y;
+		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
+		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
+		float vn = dvx * nm.x + dvy * nm.y;
+		float negImpulse = mass * ( vn + restitution * pt[j].w );
+		float newImpulse = lmax( nis[j] - negImpulse, 0.0f );
+		float impulse = newImpulse - nis[j];
+		nis[j] = newImpulse;
+		float Px = impulse * nm.x;
+		float Py = impulse * nm.y;
+		A.vx = A.vx - ms.x * Px;
+		A.vy = A.vy - ms.x * Py;
+		A.w = A.w - ms.y * ( rAx * Py - rAy * Px );
+		B.vx = B.vx + ms.z * Px;
+		B.vy = B.vy + ms.z * Py;
+		B.w = B.w + ms.w * ( rBx * Py - rBy * Px );
+	}
+	__stcg( w.kImp + k, make_float4( nis[0], nis[1], imp.z, imp.w ) );
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// contact_solver.c:160-225
+static __device__ void warm_overflow( const DWorld& w, int k )
+{
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float4 nm = w.kNormal[k];
+	float4 imp = __ldcg( w.kImp + k );
+	float4 misc = __ldcg( w.kMisc + k );
+	int count = __float_as_int( w.kSoft[k].w );
+	fv2 normal = mk( nm.x, nm.y );
+	fv2 tangent = vright( normal );
+	fv2 vA = mk( A.vx, A.vy ), vB = mk( B.vx, B.vy );
+	float wA = A.w, wB = B.w;
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tis[2] = { imp.z, imp.w };
+	for ( int j = 0; j < count; ++j )
+	{
+		fv2 rA = mk( an[j].x, an[j].y ), rB = mk( an[j].z, an[j].w );
+		fv2 P = vadd( vscale( nis[j], normal ), vscale( tis[j], tangent ) );
+		wA -= ms.y * vcross( rA, P );
+		vA = vmuladd( vA, -ms.x, P );
+		wB += ms.w * vcross( rB, P );
+		vB = vmuladd( vB, ms.z, P );
+	}
+	wA -= ms.y * misc.w;
+	wB += ms.w * misc.w;
+	A.vx = vA.x;
+	A.vy = vA.y;
+	A.w = wA;
+	B.vx = vB.x;
+	B.vy = vB.y;
+	B.w = wB;
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// contact_solver.c:227-380
+static __device__ void solve_overflow( const DWorld& w, int k, float inv_h, float pushout, bool useBias )
+{
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float mA = ms.x, iA = ms.y, mB = ms.z, iB = ms.w;
+	float4 nm = w.kNormal[k];
+	float4 sf = w.kSoft[k];
+	float4 misc = __ldcg( w.kMisc + k );
+	float4 imp = __ldcg( w.kImp + k );
+	float2 tot = __ldcg( w.kTot + k );
+	int count = __float_as_int( sf.w );
+	fv2 vA = mk( A.vx, A.vy ), vB = mk( B.vx, B.vy );
+	float wA = A.w, wB = B.w;
+	frot dqA, dqB;
+	dqA.c = A.dqc;
+	dqA.s = A.dqs;
+	dqB.c = B.dqc;
+	dqB.s = B.dqs;
+	fv2 dp = vsub( mk( B.dpx, B.dpy ), mk( A.dpx, A.dpy ) );
+	fv2 normal = mk( nm.x, nm.y );
+	fv2 tangent = vright( normal );
+	float friction = nm.z;
+	float totalNormalImpulse = 0.0f;
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float4 pt[2] = { w.kP1[k], w.kP2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tis[2] = { imp.z, imp.w };
+	float tots[2] = { tot.x, tot.y };
+	for ( int j = 0; j < count; ++j )
+	{
+		fv2 rA = mk( an[j].x, an[j].y ), rB = mk( an[j].z, an[j].w );
+		fv2 ds = vadd( dp, vsub( rrot( dqB, rB ), rrot( dqA, rA ) ) );
+		float s = pt[j].x + vdot( ds, normal );
+		float velocityBias = 0.0f;
+		float massScale = 1.0f;
+		float impulseScale = 0.0f;
+		if ( s > 0.0f )
+			velocityBias = s * inv_h;
+		else if ( useBias )
+		{
+			velocityBias = fmax_s( sf.x * s, -pushout );
+			massScale = sf.y;
+			impulseScale = sf.z;
+		}
+		fv2 vrA = vadd( vA, vcrossSV( wA, rA ) );
+		fv2 vrB = vadd( vB, vcrossSV( wB, rB ) );
+		float vn = vdot( vsub( vrB, vrA ), normal );
+		float impulse = -pt[j].y * massScale * ( vn + velocityBias ) - impulseScale * nis[j];
+		float newImpulse = fmax_s( nis[j] + impulse, 0.0f );
+		impulse = newImpulse - nis[j];
+		nis[j] = newImpulse;
+		tots[j] += newImpulse;
+		totalNormalImpulse += newImpulse;
+		fv2 P = vscale( impulse, normal );
+		vA = vmulsub( vA, mA, P );
+		wA -= iA * vcross( rA, P );
+		vB = vmuladd( vB, mB, P );
+		wB += iB * vcross( rB, P );
+	}
+	for ( int j = 0; j < count; ++j )
+	{
+		fv2 rA = mk( an[j].x, an[j].y ), rB = mk( an[j].z, an[j].w );
+		fv2 vrB = vadd( vB, vcrossSV( wB, rB ) );
+		fv2 vrA = vadd( vA, vcrossSV( wA, rA ) );
+		float vt = vdot( vsub( vrB, vrA ), tangent ) - nm.w;
+		float impulse = pt[j].z * ( -vt );
+		float maxFriction = friction * nis[j];
+		float newImpulse = fclamp_s( tis[j] + impulse, -maxFriction, maxFriction );
+		impulse = newImpulse - tis[j];
+		tis[j] = newImpulse;
+		fv2 P = vscale( impulse, tangent );
+		vA = vmulsub( vA, mA, P );
+		wA -= iA * vcross( rA, P );
+		vB = vmuladd( vB, mB, P );
+		wB += iB * vcross( rB, P );
+	}
+	{
+		float deltaLambda = -misc.z * ( wB - wA );
+		float lambda = misc.w;
+		float maxLambda = misc.y * totalNormalImpulse;
+		misc.w = fclamp_s( lambda + deltaLambda, -maxLambda, maxLambda );
+		deltaLambda = misc.w - lambda;
+		wA -= iA * deltaLambda;
+		wB += iB * deltaLambda;
+	}
+	__stcg( w.kImp + k, make_float4( nis[0], nis[1], tis[0], tis[1] ) );
+	__stcg( w.kTot + k, make_float2( tots[0], tots[1] ) );
+	__stcg( w.kMisc + k, misc );
+	A.vx = vA.x;
+	A.vy = vA.y;
+	A.w = wA;
+	B.vx = vB.x;
+	B.vy = vB.y;
+	B.w = wB;
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// contact_solver.c:382-478
+static __device__ void restitution_overflow( const DWorld& w, int k, float threshold )
+{
+	float4 misc = __ldcg( w.kMisc + k );
+	float restitution = misc.x;
+	if ( restitution == 0.0f )
+		return;
+	int2 idx = w.kIndex[k];
+	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
+	float4 ms = w.kMass[k];
+	float mA = ms.x, iA = ms.y, mB = ms.z, iB = ms.w;
+	float4 nm = w.kNormal[k];
+	int count = __float_as_int( w.kSoft[k].w );
+	float4 imp = __ldcg( w.kImp + k );
+	float2 tot = __ldcg( w.kTot + k );
+	fv2 vA = mk( A.vx, A.vy ), vB = mk( B.vx, B.vy );
+	float wA = A.w, wB = B.w;
+	fv2 normal = mk( nm.x, nm.y );
+	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
+	float4 pt[2] = { w.kP1[k], w.kP2[k] };
+	float nis[2] = { imp.x, imp.y };
+	float tots[2] = { tot.x, tot.y };
+	for ( int j = 0; j < count; ++j )
+	{
+		if ( pt[j].w > -threshold || tots[j] == 0.0f )
+			continue;
+		fv2 rA = mk( an[j].x, an[j].y ), rB = mk( an[j].z, an[j].w );
+		fv2 vrB = vadd( vB, vcrossSV( wB, rB ) );
+		fv2 vrA = vadd( vA, vcrossSV( wA, rA ) );
+		float vn = vdot( vsub( vrB, vrA ), normal );
+		float impulse = -pt[j].y * ( vn + restitution * pt[j].w );
+		float newImpulse = fmax_s( nis[j] + impulse, 0.0f );
+		impulse = newImpulse - nis[j];
+		nis[j] = newImpulse;
+		tots[j] += impulse;
+		fv2 P = vscale( impulse, normal );
+		vA = vmulsub( vA, mA, P );
+		wA -= iA * vcross( rA, P );
+		vB = vmuladd( vB, mB, P );
+		wB += iB * vcross( rB, P );
+	}
+	__stcg( w.kImp + k, make_float4( nis[0], nis[1], imp.z, imp.w ) );
+	__stcg( w.kTot + k, make_float2( tots[0], tots[1] ) );
+	A.vx = vA.x;
+	A.vy = vA.y;
+	A.w = wA;
+	B.vx = vB.x;
+	B.vy = vB.y;
+	B.w = wB;
+	store_vel( w, idx.x, A );
+	store_vel( w, idx.y, B );
+}
+
+// ---------------------------------------------------------------------------
+// bounded grid barrier (co-residency guaranteed by the cooperative launch)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool grid_barrier( DScalars* sc )
+{
+	__syncthreads();
+	if ( threadIdx.x == 0 )
+	{
+		volatile unsigned* genp = &sc->barrierGen;
+		volatile int* errp = &sc->error;
+		unsigned gen = *genp;
+		__threadfence();
+		unsigned arrived = atomicAdd( &sc->barrierCount, 1u );
+		if ( arrived == gridDim.x - 1 )
+		{
+			sc->barrierCount = 0;
+			__threadfence();
+			atomicAdd( &sc->barrierGen, 1u );
+		}
+		else
+		{
+			long long spins = 0;
+			while ( *genp == gen )
+			{
+				if ( ( *errp & ERR_BARRIER_TIMEOUT ) || ++spins > BARRIER_SPIN_LIMIT )
+				{
+					atomicOr( &sc->error, ERR_BARRIER_TIMEOUT );
+					break;
+				}
+				__nanosleep( 32 );
+			}
+		}
+		__threadfence();
+	}
+	__syncthreads();
+	return ( *(volatile int*)&sc->error & ERR_BARRIER_TIMEOUT ) == 0;
+}
+
+__device__ __forceinline__ void integrate_velocity( const DWorld& w, int b, const SolveParams& p )
+{
+	float4 v4 = w.vel[b];
+	float4 m = w.massv[b];
+	float4 dmp = w.damp[b];
+	float4 f = w.force[b];
+	float h = p.h;
+	float maxLinearSpeedSq = p.maxLinearSpeed * p.maxLinearSpeed;
+	float maxAngularSpeedSq = p.maxAngularSpeed * p.maxAngularSpeed;
+	fv2 v = mk( v4.x, v4.y );
+	float wv = v4.z;
+	float linearDamping = 1.0f / ( 1.0f + h * dmp.x );
+	float angularDamping = 1.0f / ( 1.0f + h * dmp.y );
+	float gravityScale = m.x > 0.0f ? dmp.z : 0.0f;
+	fv2 lvd = vadd( vscale( h * m.x, mk( f.x, f.y ) ), vscale( h * gravityScale, p.gravity ) );
+	float avd = h * m.y * f.z;
+	v = vmuladd( lvd, linearDamping, v );
+	wv = avd + angularDamping * wv;
+	int flags = w.bflags[b];
+	bool capped = false;
+	if ( vdot( v, v ) > maxLinearSpeedSq )
+	{
+		float ratio = p.maxLinearSpeed / vlen( v );
+		v = vscale( ratio, v );
+		capped = true;
+	}
+	if ( wv * wv > maxAngularSpeedSq && ( flags & BF_FAST_ROT ) == 0 )
+	{
+		float ratio = p.maxAngularSpeed / fabs_s( wv );
+		wv *= ratio;
+		capped = true;
+	}
+	if ( capped )
+		w.bflags[b] = flags | BF_SPEED_CAPPED;
+	w.vel[b] = make_float4( v.x, v.y, wv, 0.0f );
+}
+
+__device__ __forceinline__ bool body_awake( int f )
+{
+	return ( f & ( BF_USED | BF_ENABLED ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
+}
+
+// One colour stage: joints of colour c then contacts of colour c, spread over
+// the grid. kind 0 warm start, 1 solve (bias), 2 relax, 3 restitution.
+__device__ __forceinline__ void colour_stage( const DWorld& w, int c, int kind, const SolveParams& p, int gtid,
+											  int gstride )
+{
+	int start = w.sc->colorStart[c];
+	int count = w.sc->colorCount[c];
+	for ( int k = gtid; k < count; k += gstride )
+	{
+		int slot = start + k;
+		if ( kind == 0 )
+			warm_lane( w, slot );
+		else if ( kind == 1 )
+			solve_lane( w, slot, p.inv_h, p.minBiasVel, true );
+		else if ( kind == 2 )
+			solve_lane( w, slot, p.inv_h, p.minBiasVel, false );
+		else
+			restitution_lane( w, slot, p.restitutionThreshold );
+	}
+}
+
+__device__ __forceinline__ void joint_colour_stage( const DWorld& w, int c, int kind, const SolveParams& p, int gtid,
+													int gstride, const int* jointSlots, const int* jointStart )
+{
+	int start = jointStart[c];
+	int count = jointStart[c + 1] - start;
+	for ( int k = gtid; k < count; k += gstride )
+	{
+		int j = jointSlots[start + k];
+		if ( kind == 0 )
+			joint_warm_start( w, j );
+		else if ( kind == 1 )
+			joint_solve( w, j, p.h, p.inv_h, true );
+		else if ( kind == 2 )
+			joint_solve( w, j, p.h, p.inv_h, false );
+	}
+}
+
+__global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolveParams p, const int* jointSlots,
+															 const int* jointStart )
+{
+	int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+	int gstride = gridDim.x * blockDim.x;
+	int nb = w.bodyCount;
+	int novf = w.sc->overflowCount;
+	int novfJ = w.sc->overflowJointCount;
+	bool serialStage = novf > 0 || novfJ > 0;
+	// active colours: any contact or joint
+	int active[F2D_OVERFLOW];
+	int nActive = 0;
+	for ( int c = 0; c < F2D_OVERFLOW; ++c )
+		if ( w.sc->colorCount[c] > 0 || jointStart[c + 1] > jointStart[c] )
+			active[nActive++] = c;
+
+	for ( int sub = 0; sub < p.subSteps; ++sub )
+	{
+		for ( int b = gtid; b < nb; b += gstride )
+			if ( body_awake( w.bflags[b] ) )
+				integrate_velocity( w, b, p );
+		if ( !grid_barrier( w.sc ) )
+			return;
+		for ( int kind = 0; kind < 3; ++kind )
+		{
+			if ( kind == 2 )
+			{
+				// integrate positions (solver.c:182-200)
+				for ( int b = gtid; b < nb; b += gstride )
+				{
+					if ( !body_awake( w.bflags[b] ) )
+						continue;
+					float4 v = __ldcg( w.vel + b );
+					float4 d = __ldcg( w.delta + b );
+					frot dq;
+					dq.c = d.z;
+					dq.s = d.w;
+					dq = rintegrate( dq, p.h * v.z );
+					fv2 dp = vmuladd( mk( d.x, d.y ), p.h, mk( v.x, v.y ) );
+					__stcg( w.delta + b, make_float4( dp.x, dp.y, dq.c, dq.s ) );
+				}
+				if ( !grid_barrier( w.sc ) )
+					return;
+			}
+			if ( serialStage )
+			{
+				if ( gtid == 0 )
+				{
+					for ( int k = 0; k < novfJ; ++k )
+					{
+						int j = w.overflowJoints[k];
+						if ( kind == 0 )
+							joint_warm_start( w, j );
+						else
+							joint_solve( w, j, p.h, p.inv_h, kind == 1 );
+					}
+					for ( int k = 0; k < novf; ++k )
+					{
+						if ( kind == 0 )
+							warm_overflow( w, k );
+						else
+							solve_overflow( w, k, p.inv_h, p.pushout, kind == 1 );
+					}
+				}
+				if ( !grid_barrier( w.sc ) )
+					return;
+			}
+			for ( int a = 0; a < nActive; ++a )
+			{
+				int c = active[a];
+				joint_colour_stage( w, c, kind, p, gtid, gstride, jointSlots, jointStart );
+				colour_stage( w, c, kind, p, gtid, gstride );
+				if ( !grid_barrier( w.sc ) )
+					return;
+			}
+		}
+	}
+	// restitution: overflow then colours (solver.c:1103-1117)
+	if ( novf > 0 )
+	{
+		if ( gtid == 0 )
+			for ( int k = 0; k < novf; ++k )
+				restitution_overflow( w, k, p.restitutionThreshold );
+		if ( !grid_barrier( w.sc ) )
+			return;
+	}
+	for ( int a = 0; a < nActive; ++a )
+	{
+		int c = active[a];
+		if ( w.sc->colorCount[c] == 0 )
+			continue;
+		colour_stage( w, c, 3, p, gtid, gstride );
+		if ( !grid_barrier( w.sc ) )
+			return;
+	}
+	// store impulses (contact_solver.c:480-509, :2078-2120)
+	int n = w.sc->touchingCount;
+	for ( int k = gtid; k < n; k += gstride )
+	{
+		int c = w.slotContact[k];
+		float4 imp = w.kImp[k];
+		float2 tot = w.kTot[k];
+		float4 misc = w.kMisc[k];
+		float4 p1 = w.kP1[k], p2 = w.kP2[k];
+		int count = __float_as_int( w.kSoft[k].w );
+		bool lane = k >= novf; // graph lanes store both points (zeros for a 1-point manifold)
+		w.mpI[2 * c + 0] = make_float4( imp.x, imp.z, tot.x, p1.w );
+		if ( lane || count > 1 )
+			w.mpI[2 * c + 1] = make_float4( imp.y, imp.w, tot.y, p2.w );
+		float4 mn = w.mnorm[c];
+		mn.z = misc.w;
+		w.mnorm[c] = mn;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+int solver_max_blocks( int threads )
+{
+	int perSM = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_solve, threads, 0 );
+	int dev = 0;
+	cudaGetDevice( &dev );
+	int sms = 0;
+	cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
+	if ( perSM < 1 )
+		perSM = 1;
+	if ( perSM > 2 )
+		perSM = 2;
+	return perSM * sms;
+}
+
+void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps )
+{
+	SolveParams p;
+	p.dt = dt;
+	p.inv_dt = 1.0f / dt;
+	p.h = dt / (float)subSteps;
+	p.inv_h = (float)subSteps * p.inv_dt;
+	float contactHertz = fmin_s( w.contactHertz, 0.125f * p.inv_h );
+	p.contactSoft = make_soft( contactHertz, w.contactDampingRatio, p.h );
+	p.staticSoft = make_soft( 2.0f * contactHertz, w.contactDampingRatio, p.h );
+	float contactSpeed = w.maxContactPushSpeed / p.staticSoft.massScale;
+	p.minBiasVel = -contactSpeed;
+	p.pushout = w.maxContactPushSpeed;
+	float jointHertz = fmin_s( w.jointHertz, 0.25f * p.inv_h );
+	p.jointSoft = make_soft( jointHertz, w.jointDampingRatio, p.h );
+	p.restitutionThreshold = w.restitutionThreshold;
+	p.maxLinearSpeed = w.maxLinearSpeed;
+	p.maxAngularSpeed = F2D_MAX_ROTATION * p.inv_dt;
+	p.gravity = w.gravity;
+	p.subSteps = subSteps;
+	p.enableWarmStarting = w.enableWarmStarting;
+
+	int* fill = s.tmpA; // F2D_COLORS ints
+	k_zero_ints<<<1, 32, 0, st>>>( fill, F2D_COLORS );
+	k_count_colors<<<grid_for( w.contactCap ), 256, 0, st>>>( w, fill );
+	k_color_offsets<<<1, 1, 0, st>>>( w, fill );
+	k_fill_slots<<<grid_for( w.contactCap ), 256, 0, st>>>( w, fill );
+	k_prepare_contacts<<<grid_for( w.contactCap ), 256, 0, st>>>( w, p );
+	launch_prepare_joints( w, s, st, p.h, p.inv_h, p.jointSoft );
+
+	int* jointSlots = s.tmpB;
+	int* jointStart = s.tmpB + w.jointCap;
+	void* args[] = { &w, &p, &jointSlots, &jointStart };
+	cudaLaunchCooperativeKernel( (void*)k_solve, dim3( s.solverBlocks ), dim3( SOLVER_THREADS ), args, 0, st );
+}

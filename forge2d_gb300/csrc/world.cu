@@ -1,0 +1,1894 @@
+// Host side of the GPU world: the C ABI of include/forge2d_gb300.h, the
+// creation path, device allocation and uploads, and the step driver.
+//
+// Creation follows Box2D v3.1.1 (packages/forge2d/third_party/box2d/src/
+// body.c:177-330, shape.c:36-180, joint.c:146-330, id_pool.c:19-38) on host
+// mirrors of the device rows; rows created since the last step are uploaded
+// as one contiguous range per array before the step. The step itself is a
+// fixed sequence of launches whose sizes come from device-resident counts,
+// captured once into a CUDA graph and replayed while the world's capacities
+// and step parameters stay the same.
+#include "../../include/forge2d_gb300.h"
+#include "dscan.cuh"
+#include "dworld.cuh"
+#include "hgeom.h"
+#include "kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+void launch_reset_counters( DWorld& w, cudaStream_t st );
+
+
+#define MAX_WORLDS 128
+
+struct TreeIds
+{
+	std::vector<int> freeStack;
+	int nodeCount = 0;
+	int proxyCount = 0;
+};
+
+struct HostWorld
+{
+	bool used = false;
+	uint16_t generation = 0;
+	int index = 0;
+	DWorld d;
+	StepScratch s;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t evStart = nullptr, evStop = nullptr;
+	int* hostError = nullptr; // pinned
+	int statusAccum = 0;
+	bool stepped = false;
+	float lastStepMs = 0.0f;
+	int lastLaunches = 0;
+
+	// graph replay
+	cudaGraphExec_t graphExec = nullptr;
+	float graphDt = 0.0f;
+	int graphSubSteps = 0;
+	int graphKernelNodes = 0;
+	bool graphDirty = true;
+
+	// ---- host mirrors (same layout as the device rows) ----
+	std::vector<float4> xf, vel, delta, sweep0, massv, damp, force;
+	std::vector<float2> center, localCenter;
+	std::vector<int> bflags, headShape, headJoint, jointCountB;
+	std::vector<uint16_t> bgen;
+	std::vector<float> bmass, binertia;
+	std::vector<int> bodyFree;
+	int bodyCount = 0, bodyUploaded = 0;
+	std::vector<int> bodyDirty;
+
+	std::vector<float4> geom, aabb, fat, mat;
+	std::vector<unsigned long long> cat, mask;
+	std::vector<int> group, shapeBody, sflags, proxyKey, nextShape;
+	std::vector<float> density;
+	std::vector<uint16_t> sgen;
+	std::vector<HShapeGeom> hgeomv;
+	std::vector<int> shapeFree;
+	int shapeCount = 0, shapeUploaded = 0;
+	std::vector<int> shapeDirty;
+	TreeIds trees[3];
+	std::vector<int> staticShapes;
+	bool staticDirty = false;
+
+	std::vector<int2> jbody;
+	std::vector<int> jflags, jcolor, jnext;
+	std::vector<float4> jdef0, jdef1, jdef2;
+	std::vector<uint16_t> jgen;
+	int jointCount = 0, jointUploaded = 0;
+	std::vector<int> pendingJoints;
+
+	// plan (parity mode)
+	std::vector<unsigned long long> planKeys;
+	std::vector<int> planIds;
+	bool planPending = false;
+};
+
+static HostWorld* s_worlds[MAX_WORLDS];
+
+static int ceil_pow2( int v )
+{
+	int p = 1;
+	while ( p < v )
+		p <<= 1;
+	return p;
+}
+
+template <typename T> static void dgrow( T*& p, size_t oldN, size_t newN )
+{
+	T* q = nullptr;
+	cudaMalloc( (void**)&q, sizeof( T ) * ( newN > 0 ? newN : 1 ) );
+	cudaMemset( q, 0, sizeof( T ) * ( newN > 0 ? newN : 1 ) );
+	if ( p && oldN > 0 )
+		cudaMemcpy( q, p, sizeof( T ) * std::min( oldN, newN ), cudaMemcpyDeviceToDevice );
+	if ( p )
+		cudaFree( p );
+	p = q;
+}
+
+template <typename T> static void dfree( T*& p )
+{
+	if ( p )
+		cudaFree( p );
+	p = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// capacities
+// ---------------------------------------------------------------------------
+static void alloc_scratch( HostWorld* W )
+{
+	DWorld& d = W->d;
+	StepScratch& s = W->s;
+	dfree( s.tmpA );
+	dfree( s.tmpB );
+	dfree( s.scanTmp );
+	dfree( s.bounds );
+	int m = std::max( std::max( d.shapeCap, d.contactCap ), std::max( d.bodyCap, d.pairCap ) );
+	size_t tmpN = 2 * (size_t)m + 64;
+	dgrow( s.tmpA, 0, tmpN );
+	dgrow( s.tmpB, 0, tmpN + d.jointCap + 64 );
+	int sortBlocks = ( std::max( d.pairCap, d.shapeCap ) + SORT_TILE - 1 ) / SORT_TILE + 1;
+	int scanN = std::max( 256 * sortBlocks, m );
+	dgrow( s.scanTmp, 0, (size_t)( scanN + SCAN_TILE - 1 ) / SCAN_TILE + 64 );
+	dfree( d.sortHist );
+	dgrow( d.sortHist, 0, (size_t)256 * sortBlocks + 256 );
+	s.boundsBlocks = 64;
+	dgrow( s.bounds, 0, (size_t)s.boundsBlocks );
+	int bits = 1;
+	while ( ( 1 << bits ) < d.shapeCap )
+		bits += 1;
+	s.shapeIdBits = bits;
+	d.pairKeyBits = bits;
+	s.solverThreads = 256;
+	s.solverBlocks = solver_max_blocks( 256 );
+}
+
+static void grow_bodies( HostWorld* W, int cap )
+{
+	DWorld& d = W->d;
+	size_t o = d.bodyCap;
+	dgrow( d.xf, o, cap );
+	dgrow( d.vel, o, cap );
+	dgrow( d.delta, o, cap );
+	dgrow( d.center, o, cap );
+	dgrow( d.sweep0, o, cap );
+	dgrow( d.localCenter, o, cap );
+	dgrow( d.massv, o, cap );
+	dgrow( d.damp, o, cap );
+	dgrow( d.force, o, cap );
+	dgrow( d.bflags, o, cap );
+	dgrow( d.headShape, o, cap );
+	dgrow( d.headJoint, o, cap );
+	dgrow( d.jointCountB, o, cap );
+	dgrow( d.colorMask, o, cap );
+	dgrow( d.colorLock, o, cap );
+	dgrow( d.fastBodies, o, cap );
+	dgrow( d.moveEvXf, o, cap );
+	d.bodyCap = cap;
+}
+
+static void grow_contacts( HostWorld* W, int cap )
+{
+	DWorld& d = W->d;
+	size_t o = d.contactCap;
+	dgrow( d.cshape, o, cap );
+	dgrow( d.cbody, o, cap );
+	dgrow( d.cflags, o, cap );
+	dgrow( d.ccolor, o, cap );
+	dgrow( d.coverflowIndex, o, cap );
+	dgrow( d.cmat, o, cap );
+	dgrow( d.cmass, o, cap );
+	dgrow( d.mnorm, o, cap );
+	dgrow( d.mpA, 2 * o, 2 * (size_t)cap );
+	dgrow( d.mpB, 2 * o, 2 * (size_t)cap );
+	dgrow( d.mpI, 2 * o, 2 * (size_t)cap );
+	dgrow( d.contactFree, o, cap );
+	// step scratch sized by contacts (content not preserved)
+	dgrow( d.opContact, 0, cap );
+	dgrow( d.opKind, 0, cap );
+	dgrow( d.opColor, 0, cap );
+	dgrow( d.opDone, 0, cap );
+	dgrow( d.slotContact, 0, cap );
+	dgrow( d.overflowList, o, cap );
+	dgrow( d.kIndex, 0, cap );
+	dgrow( d.kMass, 0, cap );
+	dgrow( d.kNormal, 0, cap );
+	dgrow( d.kMisc, 0, cap );
+	dgrow( d.kSoft, 0, cap );
+	dgrow( d.kAnch1, 0, cap );
+	dgrow( d.kAnch2, 0, cap );
+	dgrow( d.kP1, 0, cap );
+	dgrow( d.kP2, 0, cap );
+	dgrow( d.kImp, 0, cap );
+	dgrow( d.kTot, 0, cap );
+	dgrow( d.beginEv, 0, 2 * (size_t)cap );
+	dgrow( d.endEv, 0, 2 * (size_t)cap );
+	dgrow( d.hitEvI, 0, 2 * (size_t)cap );
+	dgrow( d.hitEvF, 0, 5 * (size_t)cap );
+	d.contactCap = cap;
+	d.opCap = cap;
+	d.eventCap = cap;
+	int hcap = ceil_pow2( 2 * cap );
+	dfree( d.pairHash );
+	dgrow( d.pairHash, 0, hcap );
+	d.hashCap = hcap;
+}
+
+static void grow_shapes( HostWorld* W, int cap )
+{
+	DWorld& d = W->d;
+	size_t o = d.shapeCap;
+	dgrow( d.geom, o * GEOM_F4, (size_t)cap * GEOM_F4 );
+	dgrow( d.aabb, o, cap );
+	dgrow( d.fat, o, cap );
+	dgrow( d.mat, o, cap );
+	dgrow( d.cat, o, cap );
+	dgrow( d.mask, o, cap );
+	dgrow( d.group, o, cap );
+	dgrow( d.shapeBody, o, cap );
+	dgrow( d.sflags, o, cap );
+	dgrow( d.proxyKey, o, cap );
+	dgrow( d.nextShape, o, cap );
+	dgrow( d.staticShapes, 0, cap );
+	// broadphase scratch
+	dgrow( d.mortonKeys, 0, cap );
+	dgrow( d.mortonKeysAlt, 0, cap );
+	dgrow( d.leafShape, 0, cap );
+	dgrow( d.leafShapeAlt, 0, cap );
+	dgrow( d.nodeLeft, 0, cap );
+	dgrow( d.nodeRight, 0, cap );
+	dgrow( d.nodeParent, 0, 2 * (size_t)cap );
+	dgrow( d.nodeBox, 0, 2 * (size_t)cap );
+	dgrow( d.nodeVisit, 0, cap );
+	d.shapeCap = cap;
+	int pc = std::max( 65536, 4 * cap );
+	dgrow( d.pairKeys, 0, pc );
+	dgrow( d.pairKeysAlt, 0, pc );
+	dgrow( d.pairVal, 0, pc );
+	dgrow( d.pairValAlt, 0, pc );
+	dgrow( d.planKeys, 0, pc );
+	dgrow( d.planIds, 0, pc );
+	d.pairCap = pc;
+	if ( d.contactCap < 8 * cap )
+		grow_contacts( W, 8 * cap );
+}
+
+static void grow_joints( HostWorld* W, int cap )
+{
+	DWorld& d = W->d;
+	size_t o = d.jointCap;
+	dgrow( d.jbody, o, cap );
+	dgrow( d.jflags, o, cap );
+	dgrow( d.jcolor, o, cap );
+	dgrow( d.jnext, 2 * o, 2 * (size_t)cap );
+	dgrow( d.jdef0, o, cap );
+	dgrow( d.jdef1, o, cap );
+	dgrow( d.jdef2, o, cap );
+	dgrow( d.jimp, o, cap );
+	dgrow( d.jimp2, o, cap );
+	dgrow( d.jprep0, 0, cap );
+	dgrow( d.jprep1, 0, cap );
+	dgrow( d.jprep2, 0, 2 * (size_t)cap );
+	dgrow( d.jprepM, 0, cap );
+	dgrow( d.jindex, 0, cap );
+	dgrow( d.overflowJoints, o, cap );
+	dgrow( d.pendingJointOps, 0, cap );
+	d.jointCap = cap;
+}
+
+static void ensure_capacity( HostWorld* W )
+{
+	bool changed = false;
+	DWorld& d = W->d;
+	if ( W->bodyCount > d.bodyCap )
+	{
+		int c = d.bodyCap;
+		while ( c < W->bodyCount )
+			c *= 2;
+		grow_bodies( W, c );
+		changed = true;
+	}
+	if ( W->shapeCount > d.shapeCap )
+	{
+		int c = d.shapeCap;
+		while ( c < W->shapeCount )
+			c *= 2;
+		grow_shapes( W, c );
+		changed = true;
+	}
+	if ( W->jointCount > d.jointCap )
+	{
+		int c = d.jointCap;
+		while ( c < W->jointCount )
+			c *= 2;
+		grow_joints( W, c );
+		changed = true;
+	}
+	if ( changed )
+	{
+		alloc_scratch( W );
+		W->graphDirty = true;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// ids
+// ---------------------------------------------------------------------------
+static HostWorld* world_from_id( int32_t worldId )
+{
+	int index1 = worldId & 0xffff;
+	int gen = ( worldId >> 16 ) & 0xffff;
+	if ( index1 < 1 || index1 > MAX_WORLDS )
+		return nullptr;
+	HostWorld* W = s_worlds[index1 - 1];
+	if ( W == nullptr || W->used == false || W->generation != gen )
+		return nullptr;
+	return W;
+}
+
+static HostWorld* world_from_wg( int32_t wg )
+{
+	int world0 = wg & 0xffff;
+	if ( world0 < 0 || world0 >= MAX_WORLDS )
+		return nullptr;
+	HostWorld* W = s_worlds[world0];
+	if ( W == nullptr || W->used == false )
+		return nullptr;
+	return W;
+}
+
+static int body_from( int32_t index1, int32_t wg, HostWorld** out )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return -1;
+	int id = index1 - 1;
+	int gen = ( wg >> 16 ) & 0xffff;
+	if ( id < 0 || id >= W->bodyCount || ( W->bflags[id] & BF_USED ) == 0 || W->bgen[id] != gen )
+		return -1;
+	*out = W;
+	return id;
+}
+
+static int shape_from( int32_t index1, int32_t wg, HostWorld** out )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return -1;
+	int id = index1 - 1;
+	int gen = ( wg >> 16 ) & 0xffff;
+	if ( id < 0 || id >= W->shapeCount || ( W->sflags[id] & SF_USED ) == 0 || W->sgen[id] != gen )
+		return -1;
+	*out = W;
+	return id;
+}
+
+static int32_t pack_wg( HostWorld* W, int gen )
+{
+	return ( W->index & 0xffff ) | ( ( gen & 0xffff ) << 16 );
+}
+
+// ---------------------------------------------------------------------------
+// device row sync
+// ---------------------------------------------------------------------------
+template <typename T> static void up( T* dptr, const std::vector<T>& h, int lo, int hi, cudaStream_t st, int stride = 1 )
+{
+	if ( hi <= lo )
+		return;
+	cudaMemcpyAsync( dptr + (size_t)lo * stride, h.data() + (size_t)lo * stride, sizeof( T ) * (size_t)( hi - lo ) * stride,
+					 cudaMemcpyHostToDevice, st );
+}
+
+template <typename T> static void down( std::vector<T>& h, const T* dptr, int lo, int hi, int stride = 1 )
+{
+	if ( hi <= lo )
+		return;
+	cudaMemcpy( h.data() + (size_t)lo * stride, dptr + (size_t)lo * stride, sizeof( T ) * (size_t)( hi - lo ) * stride,
+				cudaMemcpyDeviceToHost );
+}
+
+static void upload_body_rows( HostWorld* W, int lo, int hi )
+{
+	DWorld& d = W->d;
+	cudaStream_t st = W->stream;
+	up( d.xf, W->xf, lo, hi, st );
+	up( d.vel, W->vel, lo, hi, st );
+	up( d.delta, W->delta, lo, hi, st );
+	up( d.center, W->center, lo, hi, st );
+	up( d.sweep0, W->sweep0, lo, hi, st );
+	up( d.localCenter, W->localCenter, lo, hi, st );
+	up( d.massv, W->massv, lo, hi, st );
+	up( d.damp, W->damp, lo, hi, st );
+	up( d.force, W->force, lo, hi, st );
+	up( d.bflags, W->bflags, lo, hi, st );
+	up( d.headShape, W->headShape, lo, hi, st );
+	up( d.headJoint, W->headJoint, lo, hi, st );
+	up( d.jointCountB, W->jointCountB, lo, hi, st );
+}
+
+static void upload_shape_rows( HostWorld* W, int lo, int hi )
+{
+	DWorld& d = W->d;
+	cudaStream_t st = W->stream;
+	up( d.geom, W->geom, lo, hi, st, GEOM_F4 );
+	up( d.aabb, W->aabb, lo, hi, st );
+	up( d.fat, W->fat, lo, hi, st );
+	up( d.mat, W->mat, lo, hi, st );
+	up( d.cat, W->cat, lo, hi, st );
+	up( d.mask, W->mask, lo, hi, st );
+	up( d.group, W->group, lo, hi, st );
+	up( d.shapeBody, W->shapeBody, lo, hi, st );
+	up( d.sflags, W->sflags, lo, hi, st );
+	up( d.proxyKey, W->proxyKey, lo, hi, st );
+	up( d.nextShape, W->nextShape, lo, hi, st );
+}
+
+static void upload_joint_rows( HostWorld* W, int lo, int hi )
+{
+	DWorld& d = W->d;
+	cudaStream_t st = W->stream;
+	up( d.jbody, W->jbody, lo, hi, st );
+	up( d.jflags, W->jflags, lo, hi, st );
+	up( d.jcolor, W->jcolor, lo, hi, st );
+	up( d.jnext, W->jnext, lo, hi, st, 2 );
+	up( d.jdef0, W->jdef0, lo, hi, st );
+	up( d.jdef1, W->jdef1, lo, hi, st );
+	up( d.jdef2, W->jdef2, lo, hi, st );
+}
+
+// bring one existing body's device-updated fields into the host mirror
+static void pull_body( HostWorld* W, int b )
+{
+	if ( b >= W->bodyUploaded )
+		return;
+	cudaStreamSynchronize( W->stream );
+	DWorld& d = W->d;
+	down( W->xf, d.xf, b, b + 1 );
+	down( W->vel, d.vel, b, b + 1 );
+	down( W->delta, d.delta, b, b + 1 );
+	down( W->center, d.center, b, b + 1 );
+	down( W->sweep0, d.sweep0, b, b + 1 );
+	down( W->force, d.force, b, b + 1 );
+	down( W->bflags, d.bflags, b, b + 1 );
+}
+
+static void mark_body( HostWorld* W, int b )
+{
+	if ( b < W->bodyUploaded )
+		W->bodyDirty.push_back( b );
+}
+
+static void mark_shape( HostWorld* W, int s )
+{
+	if ( s < W->shapeUploaded )
+		W->shapeDirty.push_back( s );
+}
+
+static void flush_uploads( HostWorld* W )
+{
+	ensure_capacity( W );
+	if ( W->bodyUploaded < W->bodyCount )
+	{
+		upload_body_rows( W, W->bodyUploaded, W->bodyCount );
+		W->bodyUploaded = W->bodyCount;
+	}
+	for ( int b : W->bodyDirty )
+		upload_body_rows( W, b, b + 1 );
+	W->bodyDirty.clear();
+	if ( W->shapeUploaded < W->shapeCount )
+	{
+		upload_shape_rows( W, W->shapeUploaded, W->shapeCount );
+		W->shapeUploaded = W->shapeCount;
+	}
+	for ( int s : W->shapeDirty )
+		upload_shape_rows( W, s, s + 1 );
+	W->shapeDirty.clear();
+	if ( W->jointUploaded < W->jointCount )
+	{
+		upload_joint_rows( W, W->jointUploaded, W->jointCount );
+		W->jointUploaded = W->jointCount;
+	}
+	if ( W->staticDirty )
+	{
+		if ( !W->staticShapes.empty() )
+			cudaMemcpyAsync( W->d.staticShapes, W->staticShapes.data(), sizeof( int ) * W->staticShapes.size(),
+							 cudaMemcpyHostToDevice, W->stream );
+		W->d.staticCount = (int)W->staticShapes.size();
+		W->staticDirty = false;
+		W->graphDirty = true;
+	}
+	if ( !W->pendingJoints.empty() )
+	{
+		cudaMemcpyAsync( W->d.pendingJointOps, W->pendingJoints.data(), sizeof( int ) * W->pendingJoints.size(),
+						 cudaMemcpyHostToDevice, W->stream );
+		W->d.pendingJointCount = (int)W->pendingJoints.size();
+		launch_joint_ops( W->d, W->stream );
+		W->d.pendingJointCount = 0;
+		W->pendingJoints.clear();
+		W->graphDirty = true;
+	}
+	W->d.bodyCount = W->bodyCount;
+	W->d.shapeCount = W->shapeCount;
+	W->d.jointCount = W->jointCount;
+}
+
+// ---------------------------------------------------------------------------
+// world lifecycle
+// ---------------------------------------------------------------------------
+extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
+{
+	int count = 0;
+	if ( cudaGetDeviceCount( &count ) != cudaSuccess || count == 0 )
+		return 0;
+	int slot = -1;
+	for ( int i = 0; i < MAX_WORLDS; ++i )
+		if ( s_worlds[i] == nullptr || s_worlds[i]->used == false )
+		{
+			slot = i;
+			break;
+		}
+	if ( slot < 0 )
+		return 0;
+	uint16_t gen = s_worlds[slot] ? s_worlds[slot]->generation : 0;
+	delete s_worlds[slot];
+	HostWorld* W = new HostWorld();
+	s_worlds[slot] = W;
+	W->used = true;
+	W->generation = (uint16_t)( gen + 1 );
+	W->index = slot;
+	DWorld& d = W->d;
+	memset( &d, 0, sizeof( d ) );
+	d.gravity = mk( (float)def->gravityX, (float)def->gravityY );
+	d.restitutionThreshold = (float)def->restitutionThreshold;
+	d.hitEventThreshold = (float)def->hitEventThreshold;
+	d.contactHertz = (float)def->contactHertz;
+	d.contactDampingRatio = (float)def->contactDampingRatio;
+	d.maxContactPushSpeed = (float)def->maxContactPushSpeed;
+	d.maxLinearSpeed = (float)def->maximumLinearSpeed;
+	d.jointHertz = 60.0f;
+	d.jointDampingRatio = 2.0f;
+	d.enableSleep = def->enableSleep != 0;
+	d.enableContinuous = def->enableContinuous != 0;
+	d.enableWarmStarting = 1;
+	cudaStreamCreateWithFlags( &W->stream, cudaStreamNonBlocking );
+	cudaEventCreate( &W->evStart );
+	cudaEventCreate( &W->evStop );
+	cudaMallocHost( (void**)&W->hostError, sizeof( int ) );
+	*W->hostError = 0;
+	cudaMalloc( (void**)&d.sc, sizeof( DScalars ) );
+	cudaMemset( d.sc, 0, sizeof( DScalars ) );
+	grow_bodies( W, 1024 );
+	grow_shapes( W, 1024 );
+	grow_joints( W, 256 );
+	alloc_scratch( W );
+	return ( slot + 1 ) | ( (int)W->generation << 16 );
+}
+
+static void free_world( HostWorld* W )
+{
+	cudaStreamSynchronize( W->stream );
+	if ( W->graphExec )
+		cudaGraphExecDestroy( W->graphExec );
+	DWorld& d = W->d;
+	void** ptrs = (void**)&d;
+	(void)ptrs;
+	// free every device array
+#define F( p ) dfree( d.p )
+	F( xf ); F( vel ); F( delta ); F( center ); F( sweep0 ); F( localCenter ); F( massv ); F( damp ); F( force );
+	F( bflags ); F( headShape ); F( headJoint ); F( jointCountB ); F( colorMask ); F( colorLock );
+	F( geom ); F( aabb ); F( fat ); F( mat ); F( cat ); F( mask ); F( group ); F( shapeBody ); F( sflags );
+	F( proxyKey ); F( nextShape ); F( cshape ); F( cbody ); F( cflags ); F( ccolor ); F( coverflowIndex ); F( cmat );
+	F( cmass ); F( mnorm ); F( mpA ); F( mpB ); F( mpI ); F( contactFree ); F( pairHash ); F( mortonKeys );
+	F( mortonKeysAlt ); F( leafShape ); F( leafShapeAlt ); F( nodeLeft ); F( nodeRight ); F( nodeParent ); F( nodeBox );
+	F( nodeVisit ); F( sortHist ); F( pairKeys ); F( pairKeysAlt ); F( pairVal ); F( pairValAlt ); F( planIds );
+	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( slotContact ); F( overflowList );
+	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
+	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 );
+	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints );
+	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
+	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp );
+#undef F
+	dfree( W->s.tmpA );
+	dfree( W->s.tmpB );
+	dfree( W->s.scanTmp );
+	dfree( W->s.bounds );
+	cudaFreeHost( W->hostError );
+	cudaEventDestroy( W->evStart );
+	cudaEventDestroy( W->evStop );
+	cudaStreamDestroy( W->stream );
+}
+
+extern "C" F2D_API void f2d_destroy_world( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	free_world( W );
+	uint16_t gen = W->generation;
+	int idx = W->index;
+	delete W;
+	s_worlds[idx] = new HostWorld();
+	s_worlds[idx]->generation = gen;
+	s_worlds[idx]->used = false;
+}
+
+extern "C" F2D_API int32_t f2d_world_is_valid( int32_t worldId )
+{
+	return world_from_id( worldId ) != nullptr;
+}
+
+extern "C" F2D_API void f2d_world_reserve( int32_t worldId, int32_t bodies, int32_t shapes, int32_t contacts,
+										   int32_t joints )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	if ( bodies > W->d.bodyCap )
+		grow_bodies( W, bodies );
+	if ( shapes > W->d.shapeCap )
+		grow_shapes( W, shapes );
+	if ( contacts > W->d.contactCap )
+		grow_contacts( W, contacts );
+	if ( joints > W->d.jointCap )
+		grow_joints( W, joints );
+	alloc_scratch( W );
+	W->graphDirty = true;
+}
+
+// ---------------------------------------------------------------------------
+// bodies
+// ---------------------------------------------------------------------------
+template <typename T> static void vset( std::vector<T>& v, int i, const T& x )
+{
+	if ( (int)v.size() <= i )
+		v.resize( (size_t)i + 1 );
+	v[i] = x;
+}
+
+extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def* def, int32_t* index1,
+											int32_t* worldAndGeneration )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( worldAndGeneration )
+		*worldAndGeneration = 0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || def == nullptr )
+		return 0;
+	int id;
+	if ( !W->bodyFree.empty() )
+	{
+		id = W->bodyFree.back();
+		W->bodyFree.pop_back();
+		pull_body( W, id );
+	}
+	else
+		id = W->bodyCount++;
+	uint16_t gen = (uint16_t)( ( id < (int)W->bgen.size() ? W->bgen[id] : 0 ) + 1 );
+	vset( W->bgen, id, gen );
+	fv2 p = mk( (float)def->positionX, (float)def->positionY );
+	frot q;
+	q.c = (float)def->rotationCos;
+	q.s = (float)def->rotationSin;
+	int type = def->type;
+	vset( W->xf, id, make_float4( p.x, p.y, q.c, q.s ) );
+	float vx = type == 0 ? 0.0f : (float)def->linearVelocityX;
+	float vy = type == 0 ? 0.0f : (float)def->linearVelocityY;
+	float av = type == 0 ? 0.0f : (float)def->angularVelocity;
+	vset( W->vel, id, make_float4( vx, vy, av, 0.0f ) );
+	vset( W->delta, id, make_float4( 0.0f, 0.0f, 1.0f, 0.0f ) );
+	vset( W->center, id, make_float2( p.x, p.y ) );
+	vset( W->sweep0, id, make_float4( p.x, p.y, q.c, q.s ) );
+	vset( W->localCenter, id, make_float2( 0.0f, 0.0f ) );
+	vset( W->massv, id, make_float4( 0.0f, 0.0f, F2D_HUGE, 0.0f ) );
+	vset( W->damp, id,
+		  make_float4( (float)def->linearDamping, (float)def->angularDamping, (float)def->gravityScale,
+					   (float)def->sleepThreshold ) );
+	vset( W->force, id, make_float4( 0.0f, 0.0f, 0.0f, 0.0f ) );
+	int flags = BF_USED | ( type << BF_TYPE_SHIFT );
+	if ( def->isEnabled )
+		flags |= BF_ENABLED;
+	if ( def->isBullet )
+		flags |= BF_BULLET;
+	if ( def->allowFastRotation )
+		flags |= BF_FAST_ROT;
+	if ( def->fixedRotation )
+		flags |= BF_FIXED_ROT;
+	if ( def->enableSleep )
+		flags |= BF_ENABLE_SLEEP;
+	vset( W->bflags, id, flags );
+	vset( W->headShape, id, F2D_NULL );
+	vset( W->headJoint, id, F2D_NULL );
+	vset( W->jointCountB, id, 0 );
+	vset( W->bmass, id, 0.0f );
+	vset( W->binertia, id, 0.0f );
+	mark_body( W, id );
+	if ( index1 )
+		*index1 = id + 1;
+	if ( worldAndGeneration )
+		*worldAndGeneration = pack_wg( W, gen );
+	return 1;
+}
+
+// body.c:528-632 (b2UpdateBodyMassData) on the host mirror
+static void update_mass( HostWorld* W, int b )
+{
+	int type = body_type( W->bflags[b] );
+	float mass = 0.0f, inertia = 0.0f, invMass = 0.0f, invInertia = 0.0f;
+	fv2 localCenter = mk( 0.0f, 0.0f );
+	float minExtent = F2D_HUGE, maxExtent = 0.0f;
+	float4 x4 = W->xf[b];
+	fxf xf;
+	xf.p = mk( x4.x, x4.y );
+	xf.q.c = x4.z;
+	xf.q.s = x4.w;
+	if ( type != 2 )
+	{
+		W->center[b] = make_float2( xf.p.x, xf.p.y );
+		if ( type == 1 )
+		{
+			for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+			{
+				float mn, mx;
+				h_shape_extent( W->hgeomv[s], mk( 0.0f, 0.0f ), &mn, &mx );
+				minExtent = fmin_s( minExtent, mn );
+				maxExtent = fmax_s( maxExtent, mx );
+			}
+		}
+		W->bmass[b] = 0.0f;
+		W->binertia[b] = 0.0f;
+		W->localCenter[b] = make_float2( 0.0f, 0.0f );
+		W->massv[b] = make_float4( 0.0f, 0.0f, minExtent, maxExtent );
+		return;
+	}
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		if ( W->density[s] == 0.0f )
+			continue;
+		HMass md = h_shape_mass( W->hgeomv[s], W->density[s] );
+		mass += md.mass;
+		localCenter = vmuladd( localCenter, md.mass, md.center );
+		inertia += md.rotationalInertia;
+	}
+	if ( mass > 0.0f )
+	{
+		invMass = 1.0f / mass;
+		localCenter = vscale( invMass, localCenter );
+	}
+	if ( inertia > 0.0f && ( W->bflags[b] & BF_FIXED_ROT ) == 0 )
+	{
+		inertia -= mass * vdot( localCenter, localCenter );
+		invInertia = 1.0f / inertia;
+	}
+	else
+	{
+		inertia = 0.0f;
+		invInertia = 0.0f;
+	}
+	float2 oc = W->center[b];
+	fv2 oldCenter = mk( oc.x, oc.y );
+	fv2 c = xpoint( xf, localCenter );
+	W->localCenter[b] = make_float2( localCenter.x, localCenter.y );
+	W->center[b] = make_float2( c.x, c.y );
+	float4 s0 = W->sweep0[b];
+	W->sweep0[b] = make_float4( c.x, c.y, s0.z, s0.w );
+	float4 v = W->vel[b];
+	fv2 deltaLinear = vcrossSV( v.z, vsub( c, oldCenter ) );
+	W->vel[b] = make_float4( v.x + deltaLinear.x, v.y + deltaLinear.y, v.z, v.w );
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		float mn, mx;
+		h_shape_extent( W->hgeomv[s], localCenter, &mn, &mx );
+		minExtent = fmin_s( minExtent, mn );
+		maxExtent = fmax_s( maxExtent, mx );
+	}
+	W->bmass[b] = mass;
+	W->binertia[b] = inertia;
+	W->massv[b] = make_float4( invMass, invInertia, minExtent, maxExtent );
+}
+
+static int tree_create_proxy( TreeIds& t )
+{
+	auto alloc = [&]() {
+		if ( !t.freeStack.empty() )
+		{
+			int v = t.freeStack.back();
+			t.freeStack.pop_back();
+			return v;
+		}
+		return t.nodeCount++;
+	};
+	int leaf = alloc();
+	if ( t.proxyCount > 0 )
+		(void)alloc();
+	t.proxyCount += 1;
+	return leaf;
+}
+
+static void pack_geom( const HShapeGeom& g, float4* out )
+{
+	for ( int i = 0; i < GEOM_F4; ++i )
+		out[i] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	fv2 centroid = h_shape_centroid( g );
+	if ( g.type == ST_POLYGON )
+	{
+		out[0] = make_float4( g.poly.centroid.x, g.poly.centroid.y, 0.0f, 0.0f );
+		out[1] = make_float4( g.poly.radius, bits_to_float( g.poly.count ), centroid.x, centroid.y );
+		for ( int i = 0; i < 4; ++i )
+		{
+			out[2 + i] = make_float4( g.poly.v[2 * i].x, g.poly.v[2 * i].y, g.poly.v[2 * i + 1].x, g.poly.v[2 * i + 1].y );
+			out[6 + i] = make_float4( g.poly.n[2 * i].x, g.poly.n[2 * i].y, g.poly.n[2 * i + 1].x, g.poly.n[2 * i + 1].y );
+		}
+	}
+	else
+	{
+		out[0] = make_float4( g.c1.x, g.c1.y, g.c2.x, g.c2.y );
+		out[1] = make_float4( g.radius, bits_to_float( 0 ), centroid.x, centroid.y );
+	}
+}
+
+// shape.c:59-180 (b2CreateShapeInternal) + shape.c:36-57 (AABBs)
+static int create_shape( HostWorld* W, int b, const f2d_shape_def* def, const HShapeGeom& g, int32_t* index1,
+						 int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	pull_body( W, b );
+	int id;
+	if ( !W->shapeFree.empty() )
+	{
+		id = W->shapeFree.back();
+		W->shapeFree.pop_back();
+	}
+	else
+		id = W->shapeCount++;
+	uint16_t gen = (uint16_t)( ( id < (int)W->sgen.size() ? W->sgen[id] : 0 ) + 1 );
+	vset( W->sgen, id, gen );
+	vset( W->hgeomv, id, g );
+	if ( (int)W->geom.size() < ( id + 1 ) * GEOM_F4 )
+		W->geom.resize( (size_t)( id + 1 ) * GEOM_F4 );
+	pack_geom( g, W->geom.data() + (size_t)id * GEOM_F4 );
+	vset( W->mat, id,
+		  make_float4( (float)def->friction, (float)def->restitution, (float)def->rollingResistance,
+					   (float)def->tangentSpeed ) );
+	vset( W->density, id, (float)def->density );
+	vset( W->cat, id, (unsigned long long)def->categoryBits );
+	vset( W->mask, id, (unsigned long long)def->maskBits );
+	vset( W->group, id, def->groupIndex );
+	vset( W->shapeBody, id, b );
+	int flags = SF_USED | ( g.type << SF_TYPE_SHIFT );
+	if ( def->isSensor )
+		flags |= SF_SENSOR;
+	if ( def->enableContactEvents )
+		flags |= SF_CONTACT_EVENTS;
+	if ( def->enableHitEvents )
+		flags |= SF_HIT_EVENTS;
+	if ( def->enablePreSolveEvents )
+		flags |= SF_PRESOLVE;
+	int pkey = F2D_NULL;
+	fbox aabb, fat;
+	aabb.lo = aabb.hi = mk( 0.0f, 0.0f );
+	fat = aabb;
+	int bflags = W->bflags[b];
+	if ( bflags & BF_ENABLED )
+	{
+		int proxyType = body_type( bflags );
+		float4 x4 = W->xf[b];
+		fxf xf;
+		xf.p = mk( x4.x, x4.y );
+		xf.q.c = x4.z;
+		xf.q.s = x4.w;
+		aabb = box_grow( h_shape_aabb( g, xf ), F2D_SPECULATIVE );
+		float margin = proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN;
+		fat = box_grow( aabb, margin );
+		int proxyId = tree_create_proxy( W->trees[proxyType] );
+		pkey = ( proxyId << 2 ) | proxyType;
+		flags |= SF_PROXY;
+		bool force = def->invokeContactCreation != 0 || def->isSensor != 0;
+		if ( proxyType != 0 || force )
+			flags |= SF_MOVED;
+		if ( proxyType == 0 && !def->isSensor )
+		{
+			W->staticShapes.push_back( id );
+			W->staticDirty = true;
+		}
+	}
+	vset( W->sflags, id, flags );
+	vset( W->proxyKey, id, pkey );
+	vset( W->aabb, id, box_to4( aabb ) );
+	vset( W->fat, id, box_to4( fat ) );
+	vset( W->nextShape, id, W->headShape[b] );
+	W->headShape[b] = id;
+	if ( def->updateBodyMass )
+		update_mass( W, b );
+	mark_body( W, b );
+	mark_shape( W, id );
+	if ( index1 )
+		*index1 = id + 1;
+	if ( wg )
+		*wg = pack_wg( W, gen );
+	return 1;
+}
+
+extern "C" F2D_API int32_t f2d_create_circle_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def, double cx,
+													double cy, double radius, int32_t* index1, int32_t* wg )
+{
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || def == nullptr )
+		return 0;
+	HShapeGeom g = {};
+	g.type = ST_CIRCLE;
+	g.c1 = mk( (float)cx, (float)cy );
+	g.radius = (float)radius;
+	return create_shape( W, b, def, g, index1, wg );
+}
+
+extern "C" F2D_API int32_t f2d_create_capsule_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def, double x1,
+													 double y1, double x2, double y2, double radius, int32_t* index1,
+													 int32_t* wg )
+{
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || def == nullptr )
+		return 0;
+	HShapeGeom g = {};
+	g.type = ST_CAPSULE;
+	g.c1 = mk( (float)x1, (float)y1 );
+	g.c2 = mk( (float)x2, (float)y2 );
+	g.radius = (float)radius;
+	return create_shape( W, b, def, g, index1, wg );
+}
+
+extern "C" F2D_API int32_t f2d_create_segment_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def, double x1,
+													 double y1, double x2, double y2, int32_t* index1, int32_t* wg )
+{
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || def == nullptr )
+		return 0;
+	HShapeGeom g = {};
+	g.type = ST_SEGMENT;
+	g.c1 = mk( (float)x1, (float)y1 );
+	g.c2 = mk( (float)x2, (float)y2 );
+	return create_shape( W, b, def, g, index1, wg );
+}
+
+extern "C" F2D_API int32_t f2d_create_box_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def, double hx,
+												 double hy, double cx, double cy, double c, double s, double radius,
+												 int32_t* index1, int32_t* wg )
+{
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || def == nullptr )
+		return 0;
+	HShapeGeom g = {};
+	g.type = ST_POLYGON;
+	frot q;
+	q.c = (float)c;
+	q.s = (float)s;
+	g.poly = h_make_offset_rounded_box( (float)hx, (float)hy, mk( (float)cx, (float)cy ), q, (float)radius );
+	return create_shape( W, b, def, g, index1, wg );
+}
+
+extern "C" F2D_API int32_t f2d_create_polygon_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def,
+													 const double* points, int32_t count, double radius,
+													 int32_t* index1, int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || def == nullptr || points == nullptr || count < 3 || count > F2D_MAX_POLY )
+		return 0;
+	fv2 pts[F2D_MAX_POLY], hull[F2D_MAX_POLY];
+	for ( int i = 0; i < count; ++i )
+		pts[i] = mk( (float)points[2 * i], (float)points[2 * i + 1] );
+	int hc = h_compute_hull( pts, count, hull );
+	if ( hc == 0 )
+		return 0;
+	HShapeGeom g = {};
+	g.type = ST_POLYGON;
+	g.poly = h_make_polygon( hull, hc, (float)radius );
+	return create_shape( W, b, def, g, index1, wg );
+}
+
+extern "C" F2D_API int32_t f2d_shape_is_valid( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	return shape_from( index1, wg, &W ) >= 0;
+}
+
+extern "C" F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return -1;
+	return shape_type( W->sflags[s] );
+}
+
+// ---------------------------------------------------------------------------
+// joints (joint.c:146-330, :507-560)
+// ---------------------------------------------------------------------------
+extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
+													  int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || def == nullptr )
+		return 0;
+	HostWorld* WA;
+	HostWorld* WB;
+	int a = body_from( def->bodyAIndex1, def->bodyAWorldAndGeneration, &WA );
+	int b = body_from( def->bodyBIndex1, def->bodyBWorldAndGeneration, &WB );
+	if ( a < 0 || b < 0 || WA != W || WB != W )
+		return 0;
+	int j = W->jointCount++;
+	uint16_t gen = (uint16_t)( ( j < (int)W->jgen.size() ? W->jgen[j] : 0 ) + 1 );
+	vset( W->jgen, j, gen );
+	vset( W->jbody, j, make_int2( a, b ) );
+	int flags = 0x1;
+	if ( def->enableSpring )
+		flags |= 0x2;
+	if ( def->enableLimit )
+		flags |= 0x4;
+	if ( def->enableMotor )
+		flags |= 0x8;
+	if ( def->collideConnected )
+		flags |= 0x10;
+	vset( W->jflags, j, flags );
+	vset( W->jcolor, j, F2D_NULL );
+	if ( (int)W->jnext.size() < 2 * ( j + 1 ) )
+		W->jnext.resize( 2 * ( (size_t)j + 1 ) );
+	pull_body( W, a );
+	pull_body( W, b );
+	W->jnext[2 * j + 0] = W->headJoint[a];
+	W->headJoint[a] = ( j << 1 ) | 0;
+	W->jointCountB[a] += 1;
+	W->jnext[2 * j + 1] = W->headJoint[b];
+	W->headJoint[b] = ( j << 1 ) | 1;
+	W->jointCountB[b] += 1;
+	mark_body( W, a );
+	mark_body( W, b );
+	float ref = fclamp_s( (float)def->referenceAngle, -F2D_PI, F2D_PI );
+	float target = fclamp_s( (float)def->targetAngle, -F2D_PI, F2D_PI );
+	vset( W->jdef0, j,
+		  make_float4( (float)def->localAnchorAX, (float)def->localAnchorAY, (float)def->localAnchorBX,
+					   (float)def->localAnchorBY ) );
+	vset( W->jdef1, j, make_float4( ref, target, (float)def->hertz, (float)def->dampingRatio ) );
+	vset( W->jdef2, j,
+		  make_float4( (float)def->lowerAngle, (float)def->upperAngle, (float)def->maxMotorTorque,
+					   (float)def->motorSpeed ) );
+	// joints between two static bodies never enter the graph
+	bool staticA = body_type( W->bflags[a] ) == 0, staticB = body_type( W->bflags[b] ) == 0;
+	if ( !( staticA && staticB ) )
+		W->pendingJoints.push_back( j );
+	if ( index1 )
+		*index1 = j + 1;
+	if ( wg )
+		*wg = pack_wg( W, gen );
+	return 1;
+}
+
+extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return 0;
+	int j = index1 - 1;
+	return j >= 0 && j < W->jointCount && W->jgen[j] == ( ( wg >> 16 ) & 0xffff );
+}
+
+// ---------------------------------------------------------------------------
+// step
+// ---------------------------------------------------------------------------
+static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
+{
+	DWorld& d = W->d;
+	launch_reset_counters( d, W->stream );
+	launch_broadphase( d, W->s, W->stream, planMode );
+	launch_narrowphase( d, W->s, W->stream );
+	launch_graph( d, W->s, W->stream );
+	launch_solver( d, W->s, W->stream, dt, subSteps );
+	launch_finalize( d, W->s, W->stream, dt );
+}
+
+static int count_kernel_nodes( cudaGraph_t g )
+{
+	size_t n = 0;
+	cudaGraphGetNodes( g, nullptr, &n );
+	std::vector<cudaGraphNode_t> nodes( n );
+	cudaGraphGetNodes( g, nodes.data(), &n );
+	int k = 0;
+	for ( size_t i = 0; i < n; ++i )
+	{
+		cudaGraphNodeType t;
+		cudaGraphNodeGetType( nodes[i], &t );
+		if ( t == cudaGraphNodeTypeKernel )
+			k += 1;
+	}
+	return k;
+}
+
+extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int32_t subStepCount )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return F2D_STATUS_INVALID;
+	float dt = (float)timeStep;
+	if ( dt == 0.0f )
+		return 0;
+	int subSteps = subStepCount < 1 ? 1 : subStepCount;
+	// collect the status of earlier steps without blocking
+	if ( W->stepped && cudaEventQuery( W->evStop ) == cudaSuccess )
+		W->statusAccum |= *W->hostError;
+	flush_uploads( W );
+	int planMode = 0;
+	if ( W->planPending )
+	{
+		int n = (int)W->planKeys.size();
+		if ( n > W->d.pairCap )
+			n = W->d.pairCap;
+		cudaMemcpyAsync( W->d.planKeys, W->planKeys.data(), sizeof( unsigned long long ) * n, cudaMemcpyHostToDevice,
+						 W->stream );
+		cudaMemcpyAsync( W->d.planIds, W->planIds.data(), sizeof( int ) * n, cudaMemcpyHostToDevice, W->stream );
+		cudaMemcpyAsync( &W->d.sc->planCount, &n, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+		cudaStreamSynchronize( W->stream );
+		W->planPending = false;
+		planMode = 1;
+	}
+	cudaMemsetAsync( &W->d.sc->error, 0, sizeof( int ), W->stream );
+	cudaEventRecord( W->evStart, W->stream );
+	bool useGraph = planMode == 0;
+	if ( useGraph && ( W->graphDirty || W->graphExec == nullptr || W->graphDt != dt || W->graphSubSteps != subSteps ) )
+	{
+		if ( W->graphExec )
+		{
+			cudaGraphExecDestroy( W->graphExec );
+			W->graphExec = nullptr;
+		}
+		cudaGraph_t g;
+		if ( cudaStreamBeginCapture( W->stream, cudaStreamCaptureModeThreadLocal ) == cudaSuccess )
+		{
+			enqueue_step( W, dt, subSteps, 0 );
+			if ( cudaStreamEndCapture( W->stream, &g ) == cudaSuccess )
+			{
+				if ( cudaGraphInstantiate( &W->graphExec, g, 0 ) != cudaSuccess )
+					W->graphExec = nullptr;
+				W->graphKernelNodes = count_kernel_nodes( g );
+				cudaGraphDestroy( g );
+			}
+		}
+		cudaGetLastError();
+		W->graphDt = dt;
+		W->graphSubSteps = subSteps;
+		W->graphDirty = false;
+	}
+	if ( useGraph && W->graphExec )
+	{
+		cudaGraphLaunch( W->graphExec, W->stream );
+		W->lastLaunches = W->graphKernelNodes;
+	}
+	else
+	{
+		enqueue_step( W, dt, subSteps, planMode );
+		W->lastLaunches = W->graphKernelNodes;
+	}
+	cudaEventRecord( W->evStop, W->stream );
+	cudaMemcpyAsync( W->hostError, &W->d.sc->error, sizeof( int ), cudaMemcpyDeviceToHost, W->stream );
+	W->stepped = true;
+	cudaError_t e = cudaGetLastError();
+	if ( e != cudaSuccess )
+		W->statusAccum |= F2D_STATUS_CUDA;
+	int st = W->statusAccum;
+	W->statusAccum = 0;
+	return st;
+}
+
+extern "C" F2D_API int32_t f2d_world_sync( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return F2D_STATUS_INVALID;
+	cudaError_t e = cudaStreamSynchronize( W->stream );
+	int st = W->statusAccum | ( W->stepped ? *W->hostError : 0 );
+	if ( e != cudaSuccess )
+		st |= F2D_STATUS_CUDA;
+	if ( W->stepped )
+	{
+		float ms = 0.0f;
+		cudaEventElapsedTime( &ms, W->evStart, W->evStop );
+		W->lastStepMs = ms;
+	}
+	W->statusAccum = 0;
+	*W->hostError = 0;
+	return st;
+}
+
+extern "C" F2D_API double f2d_world_last_step_ms( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0.0;
+	cudaEventSynchronize( W->evStop );
+	float ms = 0.0f;
+	cudaEventElapsedTime( &ms, W->evStart, W->evStop );
+	return ms;
+}
+
+extern "C" F2D_API int32_t f2d_world_last_step_launches( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->lastLaunches : 0;
+}
+
+extern "C" F2D_API void f2d_world_set_contact_plan( int32_t worldId, const int32_t* rows, int32_t count )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	std::vector<std::pair<unsigned long long, int>> v;
+	for ( int i = 0; i < count; ++i )
+	{
+		int id = rows[3 * i], a = rows[3 * i + 1], b = rows[3 * i + 2];
+		unsigned long long key = a < b ? ( ( (unsigned long long)a << 32 ) | (unsigned)b )
+									   : ( ( (unsigned long long)b << 32 ) | (unsigned)a );
+		v.push_back( std::make_pair( key, id ) );
+	}
+	std::sort( v.begin(), v.end() );
+	W->planKeys.resize( v.size() );
+	W->planIds.resize( v.size() );
+	for ( size_t i = 0; i < v.size(); ++i )
+	{
+		W->planKeys[i] = v[i].first;
+		W->planIds[i] = v[i].second;
+	}
+	W->planPending = true;
+}
+
+// ---------------------------------------------------------------------------
+// world settings
+// ---------------------------------------------------------------------------
+extern "C" F2D_API void f2d_world_set_gravity( int32_t worldId, double x, double y )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->d.gravity = mk( (float)x, (float)y );
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API void f2d_world_get_gravity( int32_t worldId, double* x, double* y )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	*x = W->d.gravity.x;
+	*y = W->d.gravity.y;
+}
+
+extern "C" F2D_API void f2d_world_enable_sleeping( int32_t worldId, int32_t enabled )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->d.enableSleep = enabled != 0;
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API int32_t f2d_world_is_sleeping_enabled( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->d.enableSleep : 0;
+}
+
+extern "C" F2D_API void f2d_world_enable_continuous( int32_t worldId, int32_t enabled )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->d.enableContinuous = enabled != 0;
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API int32_t f2d_world_is_continuous_enabled( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->d.enableContinuous : 0;
+}
+
+// ---------------------------------------------------------------------------
+// body accessors
+// ---------------------------------------------------------------------------
+extern "C" F2D_API int32_t f2d_body_is_valid( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	return body_from( index1, wg, &W ) >= 0;
+}
+
+extern "C" F2D_API void f2d_body_get_position( int32_t index1, int32_t wg, double* x, double* y )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	*x = W->xf[b].x;
+	*y = W->xf[b].y;
+}
+
+extern "C" F2D_API void f2d_body_get_rotation( int32_t index1, int32_t wg, double* c, double* s )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	*c = W->xf[b].z;
+	*s = W->xf[b].w;
+}
+
+extern "C" F2D_API void f2d_body_set_transform( int32_t index1, int32_t wg, double px, double py, double c, double s )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	frot q;
+	q.c = (float)c;
+	q.s = (float)s;
+	fv2 p = mk( (float)px, (float)py );
+	W->xf[b] = make_float4( p.x, p.y, q.c, q.s );
+	float2 lc = W->localCenter[b];
+	fv2 cc = vadd( rrot( q, mk( lc.x, lc.y ) ), p );
+	W->center[b] = make_float2( cc.x, cc.y );
+	W->sweep0[b] = make_float4( cc.x, cc.y, q.c, q.s );
+	// refresh shape boxes and re-enter the move buffer (body.c:720-780)
+	fxf xf;
+	xf.p = p;
+	xf.q = q;
+	int proxyType = body_type( W->bflags[b] );
+	for ( int sh = W->headShape[b]; sh != F2D_NULL; sh = W->nextShape[sh] )
+	{
+		if ( sh < W->shapeUploaded )
+		{
+			cudaStreamSynchronize( W->stream );
+			down( W->sflags, W->d.sflags, sh, sh + 1 );
+		}
+		fbox aabb = box_grow( h_shape_aabb( W->hgeomv[sh], xf ), F2D_SPECULATIVE );
+		float margin = proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN;
+		W->aabb[sh] = box_to4( aabb );
+		W->fat[sh] = box_to4( box_grow( aabb, margin ) );
+		W->sflags[sh] |= SF_MOVED;
+		mark_shape( W, sh );
+	}
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_get_linear_velocity( int32_t index1, int32_t wg, double* x, double* y )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	*x = W->vel[b].x;
+	*y = W->vel[b].y;
+}
+
+extern "C" F2D_API void f2d_body_set_linear_velocity( int32_t index1, int32_t wg, double x, double y )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) == 0 )
+		return;
+	pull_body( W, b );
+	W->vel[b].x = (float)x;
+	W->vel[b].y = (float)y;
+	mark_body( W, b );
+}
+
+extern "C" F2D_API double f2d_body_get_angular_velocity( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return 0.0;
+	pull_body( W, b );
+	return W->vel[b].z;
+}
+
+extern "C" F2D_API void f2d_body_set_angular_velocity( int32_t index1, int32_t wg, double w )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) == 0 )
+		return;
+	pull_body( W, b );
+	W->vel[b].z = (float)w;
+	mark_body( W, b );
+}
+
+// body.c:1000-1110 (b2Body_ApplyForce ... ApplyAngularImpulse)
+extern "C" F2D_API void f2d_body_apply_force( int32_t index1, int32_t wg, double fx, double fy, double px, double py,
+											  int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	fv2 f = mk( (float)fx, (float)fy );
+	fv2 c = mk( W->center[b].x, W->center[b].y );
+	float4 fo = W->force[b];
+	fo.x += f.x;
+	fo.y += f.y;
+	fo.z += vcross( vsub( mk( (float)px, (float)py ), c ), f );
+	W->force[b] = fo;
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_force_to_center( int32_t index1, int32_t wg, double fx, double fy, int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	W->force[b].x += (float)fx;
+	W->force[b].y += (float)fy;
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_torque( int32_t index1, int32_t wg, double torque, int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	W->force[b].z += (float)torque;
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_linear_impulse( int32_t index1, int32_t wg, double ix, double iy, double px,
+													   double py, int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	fv2 impulse = mk( (float)ix, (float)iy );
+	fv2 c = mk( W->center[b].x, W->center[b].y );
+	float4 v = W->vel[b];
+	float invMass = W->massv[b].x, invI = W->massv[b].y;
+	fv2 nv = vmuladd( mk( v.x, v.y ), invMass, impulse );
+	float nw = v.z + invI * vcross( vsub( mk( (float)px, (float)py ), c ), impulse );
+	W->vel[b] = make_float4( nv.x, nv.y, nw, v.w );
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_linear_impulse_to_center( int32_t index1, int32_t wg, double ix, double iy,
+																 int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	float4 v = W->vel[b];
+	float invMass = W->massv[b].x;
+	fv2 nv = vmuladd( mk( v.x, v.y ), invMass, mk( (float)ix, (float)iy ) );
+	W->vel[b] = make_float4( nv.x, nv.y, v.z, v.w );
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_angular_impulse( int32_t index1, int32_t wg, double impulse, int32_t wake )
+{
+	(void)wake;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	pull_body( W, b );
+	W->vel[b].z += W->massv[b].y * (float)impulse;
+	mark_body( W, b );
+}
+
+extern "C" F2D_API double f2d_body_get_mass( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	return b < 0 ? 0.0 : W->bmass[b];
+}
+
+extern "C" F2D_API double f2d_body_get_rotational_inertia( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	return b < 0 ? 0.0 : W->binertia[b];
+}
+
+extern "C" F2D_API int32_t f2d_body_get_type( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	return b < 0 ? -1 : body_type( W->bflags[b] );
+}
+
+extern "C" F2D_API int32_t f2d_body_is_awake( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return 0;
+	return body_type( W->bflags[b] ) != 0 && ( W->bflags[b] & BF_ENABLED );
+}
+
+// ---------------------------------------------------------------------------
+// bulk readers
+// ---------------------------------------------------------------------------
+extern "C" F2D_API int32_t f2d_world_body_capacity( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->bodyCount : 0;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_bodies( int32_t worldId, float* out, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	int n = std::min( W->bodyCount, cap );
+	int up = std::min( n, W->bodyUploaded );
+	std::vector<float4> xf( W->xf.begin(), W->xf.begin() + n ), vel( W->vel.begin(), W->vel.begin() + n ),
+		force( W->force.begin(), W->force.begin() + n );
+	std::vector<float2> center( W->center.begin(), W->center.begin() + n );
+	if ( up > 0 )
+	{
+		cudaMemcpy( xf.data(), W->d.xf, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
+		cudaMemcpy( vel.data(), W->d.vel, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
+		cudaMemcpy( force.data(), W->d.force, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
+		cudaMemcpy( center.data(), W->d.center, sizeof( float2 ) * up, cudaMemcpyDeviceToHost );
+	}
+	for ( int i = 0; i < n; ++i )
+	{
+		float* o = out + 12 * i;
+		memset( o, 0, sizeof( float ) * 12 );
+		if ( ( W->bflags[i] & BF_USED ) == 0 )
+			continue;
+		o[0] = xf[i].x;
+		o[1] = xf[i].y;
+		o[2] = xf[i].z;
+		o[3] = xf[i].w;
+		o[4] = vel[i].x;
+		o[5] = vel[i].y;
+		o[6] = vel[i].z;
+		o[7] = center[i].x;
+		o[8] = center[i].y;
+		o[9] = 1.0f;
+		o[10] = body_type( W->bflags[i] ) == 0 ? 0.0f : 2.0f;
+		o[11] = force[i].w;
+	}
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_world_contact_capacity( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	return sc.contactIdCount;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_contacts( int32_t worldId, int32_t* ints, float* floats, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	int n = sc.contactIdCount;
+	std::vector<int2> cs( n );
+	std::vector<int> cf( n ), cc( n );
+	std::vector<float4> mn( n ), pa( 2 * (size_t)n ), pb( 2 * (size_t)n ), pi( 2 * (size_t)n );
+	if ( n > 0 )
+	{
+		cudaMemcpy( cs.data(), W->d.cshape, sizeof( int2 ) * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( cf.data(), W->d.cflags, sizeof( int ) * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( cc.data(), W->d.ccolor, sizeof( int ) * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( mn.data(), W->d.mnorm, sizeof( float4 ) * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( pa.data(), W->d.mpA, sizeof( float4 ) * 2 * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( pb.data(), W->d.mpB, sizeof( float4 ) * 2 * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( pi.data(), W->d.mpI, sizeof( float4 ) * 2 * n, cudaMemcpyDeviceToHost );
+	}
+	int m = 0;
+	for ( int id = 0; id < n && m < cap; ++id )
+	{
+		if ( ( cf[id] & CF_USED ) == 0 )
+			continue;
+		int* oi = ints + 9 * m;
+		float* of = floats + 25 * m;
+		int count = float_to_bits( mn[id].w );
+		oi[0] = id;
+		oi[1] = cs[id].x;
+		oi[2] = cs[id].y;
+		oi[3] = cc[id];
+		oi[4] = count;
+		oi[5] = ( ( cf[id] & CF_TOUCHING ) ? 1 : 0 ) | ( ( cf[id] & CF_EVENTS ) ? 2 : 0 );
+		oi[6] = cf[id] & 0xffff0000;
+		oi[7] = float_to_bits( pb[2 * id].w ) & 0xffff;
+		oi[8] = float_to_bits( pb[2 * id + 1].w ) & 0xffff;
+		of[0] = mn[id].x;
+		of[1] = mn[id].y;
+		of[2] = mn[id].z;
+		for ( int k = 0; k < 2; ++k )
+		{
+			float* p = of + 3 + 11 * k;
+			float4 a = pa[2 * id + k], b = pb[2 * id + k], im = pi[2 * id + k];
+			p[0] = a.x;
+			p[1] = a.y;
+			p[2] = a.z;
+			p[3] = a.w;
+			p[4] = b.x;
+			p[5] = b.y;
+			p[6] = b.z;
+			p[7] = im.x;
+			p[8] = im.y;
+			p[9] = im.z;
+			p[10] = im.w;
+		}
+		m += 1;
+	}
+	return m;
+}
+
+extern "C" F2D_API int32_t f2d_world_shape_capacity( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->shapeCount : 0;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_shapes( int32_t worldId, float* floats, int32_t* ints, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	int n = std::min( W->shapeCount, cap );
+	int up = std::min( n, W->shapeUploaded );
+	std::vector<float4> aabb( W->aabb.begin(), W->aabb.begin() + n ), fat( W->fat.begin(), W->fat.begin() + n );
+	std::vector<int> fl( W->sflags.begin(), W->sflags.begin() + n );
+	if ( up > 0 )
+	{
+		cudaMemcpy( aabb.data(), W->d.aabb, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
+		cudaMemcpy( fat.data(), W->d.fat, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
+		cudaMemcpy( fl.data(), W->d.sflags, sizeof( int ) * up, cudaMemcpyDeviceToHost );
+	}
+	for ( int i = 0; i < n; ++i )
+	{
+		float* f = floats + 8 * i;
+		f[0] = aabb[i].x;
+		f[1] = aabb[i].y;
+		f[2] = aabb[i].z;
+		f[3] = aabb[i].w;
+		f[4] = fat[i].x;
+		f[5] = fat[i].y;
+		f[6] = fat[i].z;
+		f[7] = fat[i].w;
+		int* k = ints + 4 * i;
+		k[0] = W->proxyKey[i];
+		k[1] = W->shapeBody[i];
+		k[2] = shape_type( W->sflags[i] );
+		k[3] = fl[i];
+	}
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_mass( int32_t worldId, float* out, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	int n = std::min( W->bodyCount, cap );
+	for ( int i = 0; i < n; ++i )
+	{
+		float* o = out + 8 * i;
+		o[0] = W->bmass[i];
+		o[1] = W->binertia[i];
+		o[2] = W->massv[i].x;
+		o[3] = W->massv[i].y;
+		o[4] = W->localCenter[i].x;
+		o[5] = W->localCenter[i].y;
+		o[6] = W->massv[i].z;
+		o[7] = W->massv[i].w;
+	}
+	return n;
+}
+
+extern "C" F2D_API void f2d_world_get_color_counts( int32_t worldId, int32_t* out12 )
+{
+	HostWorld* W = world_from_id( worldId );
+	for ( int i = 0; i < 12; ++i )
+		out12[i] = 0;
+	if ( W == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	for ( int i = 0; i < 11; ++i )
+		out12[i] = sc.colorCount[i];
+	out12[11] = sc.overflowCount;
+	if ( W->jointCount > 0 )
+	{
+		std::vector<int> jc( W->jointCount );
+		cudaMemcpy( jc.data(), W->d.jcolor, sizeof( int ) * W->jointCount, cudaMemcpyDeviceToHost );
+		for ( int c : jc )
+			if ( c >= 0 && c < 12 )
+				out12[c] += 1;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// events
+// ---------------------------------------------------------------------------
+extern "C" F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* counts4 )
+{
+	HostWorld* W = world_from_id( worldId );
+	for ( int i = 0; i < 4; ++i )
+		counts4[i] = 0;
+	if ( W == nullptr || !W->stepped )
+		return;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	counts4[0] = sc.beginCount;
+	counts4[1] = sc.endCount;
+	counts4[2] = std::min( sc.hitCount, W->d.eventCap );
+	int moved = 0;
+	for ( int b = 0; b < W->bodyCount; ++b )
+	{
+		int f = W->bflags[b];
+		if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
+			moved += 1;
+	}
+	counts4[3] = moved;
+}
+
+static int read_pairs( HostWorld* W, const int* dptr, int count, int32_t* out4, int cap )
+{
+	int n = std::min( count, cap );
+	std::vector<int> tmp( 2 * (size_t)n );
+	if ( n > 0 )
+		cudaMemcpy( tmp.data(), dptr, sizeof( int ) * 2 * n, cudaMemcpyDeviceToHost );
+	for ( int i = 0; i < n; ++i )
+	{
+		int a = tmp[2 * i], b = tmp[2 * i + 1];
+		out4[4 * i + 0] = a + 1;
+		out4[4 * i + 1] = pack_wg( W, W->sgen[a] );
+		out4[4 * i + 2] = b + 1;
+		out4[4 * i + 3] = pack_wg( W, W->sgen[b] );
+	}
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	int c[4];
+	f2d_world_get_event_counts( worldId, c );
+	return read_pairs( W, W->d.beginEv, c[0], out4, cap );
+}
+
+extern "C" F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* out4, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	int c[4];
+	f2d_world_get_event_counts( worldId, c );
+	return read_pairs( W, W->d.endEv, c[1], out4, cap );
+}
+
+extern "C" F2D_API int32_t f2d_world_get_hit_events( int32_t worldId, int32_t* ints4, float* floats5, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	int c[4];
+	f2d_world_get_event_counts( worldId, c );
+	int n = read_pairs( W, W->d.hitEvI, c[2], ints4, cap );
+	if ( n > 0 )
+		cudaMemcpy( floats5, W->d.hitEvF, sizeof( float ) * 5 * n, cudaMemcpyDeviceToHost );
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* ints3, float* floats4, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	int n = W->bodyCount;
+	std::vector<float4> ev( n );
+	if ( n > 0 )
+		cudaMemcpy( ev.data(), W->d.moveEvXf, sizeof( float4 ) * n, cudaMemcpyDeviceToHost );
+	int m = 0;
+	for ( int b = 0; b < n && m < cap; ++b )
+	{
+		int f = W->bflags[b];
+		if ( !( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 ) )
+			continue;
+		ints3[3 * m + 0] = b + 1;
+		ints3[3 * m + 1] = pack_wg( W, W->bgen[b] );
+		ints3[3 * m + 2] = 0;
+		floats4[4 * m + 0] = ev[b].x;
+		floats4[4 * m + 1] = ev[b].y;
+		floats4[4 * m + 2] = ev[b].z;
+		floats4[4 * m + 3] = ev[b].w;
+		m += 1;
+	}
+	return m;
+}
+
+// ---------------------------------------------------------------------------
+// accessors for queries.cu
+// ---------------------------------------------------------------------------
+DWorld* f2d_internal_world( int32_t worldId, cudaStream_t* st, int* gens, int genCap )
+{
+	(void)gens;
+	(void)genCap;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return nullptr;
+	flush_uploads( W );
+	cudaStreamSynchronize( W->stream );
+	*st = W->stream;
+	return &W->d;
+}
+
+uint16_t f2d_internal_shape_gen( int32_t worldId, int shape )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || shape < 0 || shape >= (int)W->sgen.size() )
+		return 0;
+	return W->sgen[shape];
+}
+
+int32_t f2d_internal_world0( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->index : 0;
+}

@@ -148,7 +148,7 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
         else:
             n = int(rng.integers(3, 9))
             pts = _polygon_points(rng, n, float(rng.uniform(0.3, 0.8)))
-            if b.create_polygon(body, sd, pts, 0.0) < 0:
+            if b.create_polygon(body, sd, pts, 0.0) == -1:
                 b.create_circle(body, sd, 0.0, 0.0, 0.5)
         ids.append(body)
     return ids

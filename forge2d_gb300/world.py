@@ -1,0 +1,395 @@
+"""Host-side mirror of forge2d's world API over the GPU C ABI.
+
+``World`` / ``Body`` / ``Shape`` / ``Joint`` follow the names and argument
+meaning of forge2d's public Dart API (packages/forge2d/lib/src/api/world.dart,
+body.dart; the defs of defs.dart) and of the RawBox2D seam it sits on
+(packages/forge2d/lib/src/backend/raw_box2d.dart). Ids are the seam's packed
+pairs (index1, worldAndGeneration).
+
+``GpuWorld`` is the flat builder the seeded scenes in ``scenes.py`` and the
+parity tests drive; the oracle worlds expose the same methods.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native
+from .scenes import BODY_DEFAULTS, SHAPE_DEFAULTS, WORLD_DEFAULTS, REVOLUTE_DEFAULTS
+
+BODY_STRIDE = 12
+CONTACT_INTS = 9
+CONTACT_FLOATS = 25
+
+
+def _fill(struct, values: dict):
+    for k, v in values.items():
+        if hasattr(struct, k):
+            setattr(struct, k, v)
+    return struct
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class GpuWorld:
+    """Flat builder over the C ABI (one GPU world)."""
+
+    def __init__(self, world_def: dict | None = None, workers: int = 1):
+        self.lib = native.lib()
+        wd = dict(WORLD_DEFAULTS)
+        if world_def:
+            wd.update(world_def)
+        self.id = self.lib.f2d_create_world(C.byref(_fill(native.WorldDef(), wd)))
+        if self.id == 0:
+            raise RuntimeError("f2d_create_world failed (no CUDA device?)")
+        self._closed = False
+
+    def close(self):
+        if not self._closed:
+            self.lib.f2d_destroy_world(self.id)
+            self._closed = True
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, bodies=0, shapes=0, contacts=0, joints=0):
+        self.lib.f2d_world_reserve(self.id, bodies, shapes, contacts, joints)
+
+    # creation ---------------------------------------------------------
+    def create_body(self, body_def: dict):
+        bd = dict(BODY_DEFAULTS)
+        bd.update(body_def)
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        if not self.lib.f2d_create_body(self.id, C.byref(_fill(native.BodyDef(), bd)), C.byref(i1), C.byref(wg)):
+            raise RuntimeError("createBody failed")
+        return (i1.value, wg.value)
+
+    def _sd(self, sd):
+        d = dict(SHAPE_DEFAULTS)
+        d.update(sd)
+        return C.byref(_fill(native.ShapeDef(), d))
+
+    def _ret(self, ok, i1, wg):
+        return (i1.value, wg.value) if ok else -1
+
+    def create_circle(self, body, sd, cx, cy, r):
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_circle_shape(body[0], body[1], self._sd(sd), cx, cy, r, C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_capsule(self, body, sd, x1, y1, x2, y2, r):
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_capsule_shape(body[0], body[1], self._sd(sd), x1, y1, x2, y2, r, C.byref(i1),
+                                               C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_segment(self, body, sd, x1, y1, x2, y2):
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_segment_shape(body[0], body[1], self._sd(sd), x1, y1, x2, y2, C.byref(i1),
+                                               C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_box(self, body, sd, hx, hy, cx=0.0, cy=0.0, c=1.0, s=0.0, radius=0.0):
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_box_shape(body[0], body[1], self._sd(sd), hx, hy, cx, cy, c, s, radius,
+                                           C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_polygon(self, body, sd, points, radius=0.0):
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1))
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_polygon_shape(body[0], body[1], self._sd(sd),
+                                               pts.ctypes.data_as(C.POINTER(C.c_double)), len(pts) // 2, radius,
+                                               C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_revolute(self, jd: dict):
+        d = dict(REVOLUTE_DEFAULTS)
+        d.update(jd)
+        a, b = d.pop("bodyA"), d.pop("bodyB")
+        rd = _fill(native.RevoluteDef(), d)
+        rd.bodyAIndex1, rd.bodyAWorldAndGeneration = a
+        rd.bodyBIndex1, rd.bodyBWorldAndGeneration = b
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    # stepping ---------------------------------------------------------
+    def step(self, dt=1.0 / 60.0, substeps=4):
+        return self.lib.f2d_world_step(self.id, dt, substeps)
+
+    def sync(self) -> int:
+        return self.lib.f2d_world_sync(self.id)
+
+    def last_step_ms(self) -> float:
+        return self.lib.f2d_world_last_step_ms(self.id)
+
+    def last_step_launches(self) -> int:
+        return self.lib.f2d_world_last_step_launches(self.id)
+
+    def set_contact_plan(self, plan):
+        plan = np.ascontiguousarray(np.asarray(plan, dtype=np.int32).reshape(-1, 3))
+        self.lib.f2d_world_set_contact_plan(self.id, _iptr(plan), len(plan))
+
+    # dumps ------------------------------------------------------------
+    def bodies(self) -> np.ndarray:
+        n = self.lib.f2d_world_body_capacity(self.id)
+        out = np.zeros((max(n, 1), BODY_STRIDE), np.float32)
+        self.lib.f2d_world_get_bodies(self.id, _fptr(out), n)
+        return out[:n]
+
+    def contacts(self):
+        n = self.lib.f2d_world_contact_capacity(self.id)
+        ints = np.zeros((max(n, 1), CONTACT_INTS), np.int32)
+        fl = np.zeros((max(n, 1), CONTACT_FLOATS), np.float32)
+        m = self.lib.f2d_world_get_contacts(self.id, _iptr(ints), _fptr(fl), n)
+        return ints[:m], fl[:m]
+
+    def shapes(self):
+        n = self.lib.f2d_world_shape_capacity(self.id)
+        fl = np.zeros((max(n, 1), 8), np.float32)
+        ints = np.zeros((max(n, 1), 4), np.int32)
+        self.lib.f2d_world_get_shapes(self.id, _fptr(fl), _iptr(ints), n)
+        return fl[:n], ints[:n]
+
+    def mass(self) -> np.ndarray:
+        n = self.lib.f2d_world_body_capacity(self.id)
+        out = np.zeros((max(n, 1), 8), np.float32)
+        self.lib.f2d_world_get_mass(self.id, _fptr(out), n)
+        return out[:n]
+
+    def color_counts(self) -> np.ndarray:
+        out = np.zeros(12, np.int32)
+        self.lib.f2d_world_get_color_counts(self.id, _iptr(out))
+        return out
+
+    def event_counts(self):
+        out = np.zeros(4, np.int32)
+        self.lib.f2d_world_get_event_counts(self.id, _iptr(out))
+        return out
+
+    def begin_events(self):
+        n = int(self.event_counts()[0])
+        out = np.zeros((max(n, 1), 4), np.int32)
+        m = self.lib.f2d_world_get_begin_events(self.id, _iptr(out), n)
+        return out[:m][:, [0, 2]] - 1
+
+    def end_events(self):
+        n = int(self.event_counts()[1])
+        out = np.zeros((max(n, 1), 4), np.int32)
+        m = self.lib.f2d_world_get_end_events(self.id, _iptr(out), n)
+        return out[:m][:, [0, 2]] - 1
+
+    def hit_events(self):
+        n = int(self.event_counts()[2])
+        ints = np.zeros((max(n, 1), 4), np.int32)
+        fl = np.zeros((max(n, 1), 5), np.float32)
+        m = self.lib.f2d_world_get_hit_events(self.id, _iptr(ints), _fptr(fl), n)
+        return ints[:m][:, [0, 2]] - 1, fl[:m]
+
+    def move_events(self):
+        n = int(self.event_counts()[3])
+        ints = np.zeros((max(n, 1), 3), np.int32)
+        fl = np.zeros((max(n, 1), 4), np.float32)
+        m = self.lib.f2d_world_get_body_events(self.id, _iptr(ints), _fptr(fl), n)
+        return ints[:m], fl[:m]
+
+    def cast_ray_closest(self, ox, oy, tx, ty, cat=1, mask=-1):
+        shape = np.zeros(2, np.int32)
+        out = np.zeros(5, np.float32)
+        hit = self.lib.f2d_world_cast_ray_closest(self.id, ox, oy, tx, ty, cat, mask, _iptr(shape), _fptr(out))
+        if not hit:
+            return None
+        return int(shape[0]) - 1, out
+
+    def overlap_aabb(self, lx, ly, ux, uy, cat=1, mask=-1):
+        cap = 1 << 16
+        out = np.zeros((cap, 2), np.int32)
+        n = self.lib.f2d_world_overlap_aabb(self.id, lx, ly, ux, uy, cat, mask, _iptr(out), cap)
+        return out[:min(n, cap), 0] - 1
+
+
+# ---------------------------------------------------------------------------
+# forge2d-style object API
+# ---------------------------------------------------------------------------
+class Shape:
+    def __init__(self, world, sid):
+        self.world, self.id = world, sid
+
+    @property
+    def is_valid(self):
+        return bool(self.world.lib.f2d_shape_is_valid(*self.id))
+
+    @property
+    def type(self):
+        return self.world.lib.f2d_shape_get_type(*self.id)
+
+
+class Body:
+    def __init__(self, world, bid):
+        self.world, self.id = world, bid
+
+    @property
+    def lib(self):
+        return self.world.lib
+
+    def create_box(self, half_width, half_height, center=(0.0, 0.0), rotation=(1.0, 0.0), radius=0.0, **sd):
+        return Shape(self.world, self.world._w.create_box(self.id, sd, half_width, half_height, center[0], center[1],
+                                                          rotation[0], rotation[1], radius))
+
+    def create_circle(self, radius, center=(0.0, 0.0), **sd):
+        return Shape(self.world, self.world._w.create_circle(self.id, sd, center[0], center[1], radius))
+
+    def create_capsule(self, center1, center2, radius, **sd):
+        return Shape(self.world, self.world._w.create_capsule(self.id, sd, center1[0], center1[1], center2[0],
+                                                              center2[1], radius))
+
+    def create_segment(self, point1, point2, **sd):
+        return Shape(self.world, self.world._w.create_segment(self.id, sd, point1[0], point1[1], point2[0],
+                                                              point2[1]))
+
+    def create_polygon(self, points, radius=0.0, **sd):
+        sid = self.world._w.create_polygon(self.id, sd, points, radius)
+        if sid == -1:
+            raise ValueError("The points do not form a valid convex hull: at least three distinct, "
+                             "non-collinear points are required")
+        return Shape(self.world, sid)
+
+    @property
+    def position(self):
+        x, y = C.c_double(), C.c_double()
+        self.lib.f2d_body_get_position(self.id[0], self.id[1], C.byref(x), C.byref(y))
+        return (x.value, y.value)
+
+    @property
+    def rotation(self):
+        c, s = C.c_double(), C.c_double()
+        self.lib.f2d_body_get_rotation(self.id[0], self.id[1], C.byref(c), C.byref(s))
+        return (c.value, s.value)
+
+    @property
+    def linear_velocity(self):
+        x, y = C.c_double(), C.c_double()
+        self.lib.f2d_body_get_linear_velocity(self.id[0], self.id[1], C.byref(x), C.byref(y))
+        return (x.value, y.value)
+
+    @linear_velocity.setter
+    def linear_velocity(self, v):
+        self.lib.f2d_body_set_linear_velocity(self.id[0], self.id[1], v[0], v[1])
+
+    @property
+    def angular_velocity(self):
+        return self.lib.f2d_body_get_angular_velocity(self.id[0], self.id[1])
+
+    @angular_velocity.setter
+    def angular_velocity(self, w):
+        self.lib.f2d_body_set_angular_velocity(self.id[0], self.id[1], w)
+
+    def set_transform(self, position, rotation=(1.0, 0.0)):
+        self.lib.f2d_body_set_transform(self.id[0], self.id[1], position[0], position[1], rotation[0], rotation[1])
+
+    def apply_force(self, force, point, wake=True):
+        self.lib.f2d_body_apply_force(self.id[0], self.id[1], force[0], force[1], point[0], point[1], int(wake))
+
+    def apply_force_to_center(self, force, wake=True):
+        self.lib.f2d_body_apply_force_to_center(self.id[0], self.id[1], force[0], force[1], int(wake))
+
+    def apply_torque(self, torque, wake=True):
+        self.lib.f2d_body_apply_torque(self.id[0], self.id[1], torque, int(wake))
+
+    def apply_linear_impulse(self, impulse, point, wake=True):
+        self.lib.f2d_body_apply_linear_impulse(self.id[0], self.id[1], impulse[0], impulse[1], point[0], point[1],
+                                               int(wake))
+
+    def apply_linear_impulse_to_center(self, impulse, wake=True):
+        self.lib.f2d_body_apply_linear_impulse_to_center(self.id[0], self.id[1], impulse[0], impulse[1], int(wake))
+
+    def apply_angular_impulse(self, impulse, wake=True):
+        self.lib.f2d_body_apply_angular_impulse(self.id[0], self.id[1], impulse, int(wake))
+
+    @property
+    def mass(self):
+        return self.lib.f2d_body_get_mass(*self.id)
+
+    @property
+    def rotational_inertia(self):
+        return self.lib.f2d_body_get_rotational_inertia(*self.id)
+
+    @property
+    def type(self):
+        return self.lib.f2d_body_get_type(*self.id)
+
+    @property
+    def is_valid(self):
+        return bool(self.lib.f2d_body_is_valid(*self.id))
+
+
+class Joint:
+    def __init__(self, world, jid):
+        self.world, self.id = world, jid
+
+    @property
+    def is_valid(self):
+        return bool(self.world.lib.f2d_joint_is_valid(*self.id))
+
+
+class World:
+    """forge2d ``World``: step, createBody, createRevoluteJoint, events, queries."""
+
+    def __init__(self, gravity=(0.0, -10.0), **world_def):
+        wd = dict(gravityX=gravity[0], gravityY=gravity[1])
+        wd.update(world_def)
+        self._w = GpuWorld(wd)
+        self.lib = self._w.lib
+
+    @property
+    def id(self):
+        return self._w.id
+
+    def destroy(self):
+        self._w.close()
+
+    def step(self, dt, sub_step_count=4):
+        return self._w.step(dt, sub_step_count)
+
+    def create_body(self, **body_def):
+        return Body(self, self._w.create_body(body_def))
+
+    def create_revolute_joint(self, body_a, body_b, **jd):
+        jd = dict(jd)
+        jd["bodyA"] = body_a.id
+        jd["bodyB"] = body_b.id
+        return Joint(self, self._w.create_revolute(jd))
+
+    @property
+    def gravity(self):
+        x, y = C.c_double(), C.c_double()
+        self.lib.f2d_world_get_gravity(self.id, C.byref(x), C.byref(y))
+        return (x.value, y.value)
+
+    @gravity.setter
+    def gravity(self, g):
+        self.lib.f2d_world_set_gravity(self.id, g[0], g[1])
+
+    def cast_ray_closest(self, origin, translation, category_bits=1, mask_bits=-1):
+        return self._w.cast_ray_closest(origin[0], origin[1], translation[0], translation[1], category_bits,
+                                        mask_bits)
+
+    def overlap_aabb(self, lower, upper, category_bits=1, mask_bits=-1):
+        return self._w.overlap_aabb(lower[0], lower[1], upper[0], upper[1], category_bits, mask_bits)
+
+    def contact_events(self):
+        return {"begin": self._w.begin_events(), "end": self._w.end_events(), "hit": self._w.hit_events()}
+
+    def body_move_events(self):
+        return self._w.move_events()

@@ -1,0 +1,299 @@
+/*
+ * forge2d_gb300 -- C ABI of the GPU world step.
+ *
+ * A drop-in for the part of forge2d's backend seam that drives the Box2D v3
+ * world step: `abstract interface class RawBox2D`
+ * (packages/forge2d/lib/src/backend/raw_box2d.dart:10). Each entry point
+ * below names the RawBox2D method it replaces and the native Box2D call that
+ * method makes today through dart:ffi (raw_box2d_ffi.dart). The seam's rules
+ * hold (packages/forge2d/lib/src/backend/README.md:21-39): primitives only,
+ * ids packed into 32-bit ints -- world id = index1 | generation << 16; body,
+ * shape and joint ids are (index1, worldAndGeneration = world0 |
+ * generation << 16) pairs -- no callbacks, definition structs flattened,
+ * results written into caller-provided buffers.
+ *
+ * Errors: functions never trap. Invalid ids are ignored (getters return 0),
+ * creation returns 0 and leaves the id outputs at 0, f2d_world_step returns
+ * a nonzero F2D_STATUS_* bit set when a device capacity or wait limit was
+ * hit (the step's results are then incomplete and the world should be
+ * recreated with larger capacities).
+ *
+ * Threading: a world belongs to one host thread; every call is synchronous
+ * with respect to the caller except f2d_world_step, which enqueues the step
+ * on the world's CUDA stream (getters and event readers synchronise).
+ */
+#ifndef FORGE2D_GB300_H
+#define FORGE2D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined( _WIN32 )
+#define F2D_API __declspec( dllexport )
+#else
+#define F2D_API __attribute__( ( visibility( "default" ) ) )
+#endif
+
+/* Mirrors RawBox2D.createWorld's named parameters (raw_box2d.dart:18-29). */
+typedef struct f2d_world_def
+{
+	double gravityX, gravityY;
+	double restitutionThreshold;
+	double hitEventThreshold;
+	double contactHertz;
+	double contactDampingRatio;
+	double maxContactPushSpeed;
+	double maximumLinearSpeed;
+	int32_t enableSleep;
+	int32_t enableContinuous;
+} f2d_world_def;
+
+/* Mirrors RawBox2D.createBody's named parameters (raw_box2d.dart:71-91);
+ * type is the BodyType index (0 static, 1 kinematic, 2 dynamic). */
+typedef struct f2d_body_def
+{
+	int32_t type;
+	int32_t pad0;
+	double positionX, positionY;
+	double rotationCos, rotationSin;
+	double linearVelocityX, linearVelocityY;
+	double angularVelocity;
+	double linearDamping;
+	double angularDamping;
+	double gravityScale;
+	double sleepThreshold;
+	int32_t enableSleep;
+	int32_t isAwake;
+	int32_t fixedRotation;
+	int32_t isBullet;
+	int32_t isEnabled;
+	int32_t allowFastRotation;
+} f2d_body_def;
+
+/* Mirrors RawShapeDef (raw_box2d_ffi.dart:564-584 maps it to b2ShapeDef).
+ * 64-bit filter masks follow the seam's sign-extension rule: -1 = all bits. */
+typedef struct f2d_shape_def
+{
+	double friction;
+	double restitution;
+	double rollingResistance;
+	double tangentSpeed;
+	double density;
+	int64_t categoryBits;
+	int64_t maskBits;
+	int32_t groupIndex;
+	int32_t userMaterialId;
+	int32_t isSensor;
+	int32_t enableSensorEvents;
+	int32_t enableContactEvents;
+	int32_t enableHitEvents;
+	int32_t enablePreSolveEvents;
+	int32_t invokeContactCreation;
+	int32_t updateBodyMass;
+	int32_t pad0;
+} f2d_shape_def;
+
+/* Mirrors World.createRevoluteJoint / RawBox2D.createRevoluteJoint
+ * (packages/forge2d/lib/src/api/world.dart:297-321). */
+typedef struct f2d_revolute_def
+{
+	int32_t bodyAIndex1, bodyAWorldAndGeneration;
+	int32_t bodyBIndex1, bodyBWorldAndGeneration;
+	double localAnchorAX, localAnchorAY;
+	double localAnchorBX, localAnchorBY;
+	double referenceAngle;
+	double targetAngle;
+	int32_t enableSpring;
+	int32_t pad0;
+	double hertz;
+	double dampingRatio;
+	int32_t enableLimit;
+	int32_t pad1;
+	double lowerAngle, upperAngle;
+	int32_t enableMotor;
+	int32_t pad2;
+	double maxMotorTorque;
+	double motorSpeed;
+	double drawSize;
+	int32_t collideConnected;
+	int32_t pad3;
+} f2d_revolute_def;
+
+#define F2D_STATUS_OK 0
+#define F2D_STATUS_CONTACT_CAPACITY 0x1
+#define F2D_STATUS_PAIR_CAPACITY 0x2
+#define F2D_STATUS_BARRIER_TIMEOUT 0x4
+#define F2D_STATUS_PLAN_MISMATCH 0x8
+#define F2D_STATUS_OP_CAPACITY 0x10
+#define F2D_STATUS_COLOR_ROUNDS 0x20
+#define F2D_STATUS_EVENT_CAPACITY 0x40
+#define F2D_STATUS_TREE 0x80
+#define F2D_STATUS_INVALID 0x100
+#define F2D_STATUS_CUDA 0x200
+
+/* ---- world lifecycle ---------------------------------------------------- */
+
+/* RawBox2D.createWorld (raw_box2d.dart:18; raw_box2d_ffi.dart:67 -> b2CreateWorld).
+ * Returns the packed world id, 0 on failure (no CUDA device, table full). */
+F2D_API int32_t f2d_create_world( const f2d_world_def* def );
+/* RawBox2D.destroyWorld (raw_box2d.dart:32 -> b2DestroyWorld). */
+F2D_API void f2d_destroy_world( int32_t worldId );
+/* RawBox2D.worldIsValid (raw_box2d.dart:35 -> b2World_IsValid). */
+F2D_API int32_t f2d_world_is_valid( int32_t worldId );
+/* RawBox2D.worldStep (raw_box2d.dart:39; raw_box2d_ffi.dart:103 -> b2World_Step).
+ * Returns F2D_STATUS_* bits of the previous device step (checked lazily so
+ * that consecutive steps do not synchronise). */
+F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int32_t subStepCount );
+/* Blocks until the world's enqueued work is done; returns the status bits. */
+F2D_API int32_t f2d_world_sync( int32_t worldId );
+/* RawBox2D.worldSetGravity / worldGetGravity (raw_box2d.dart:42-45). */
+F2D_API void f2d_world_set_gravity( int32_t worldId, double x, double y );
+F2D_API void f2d_world_get_gravity( int32_t worldId, double* x, double* y );
+/* RawBox2D.worldEnableSleeping / worldIsSleepingEnabled (raw_box2d.dart:49-52). */
+F2D_API void f2d_world_enable_sleeping( int32_t worldId, int32_t enabled );
+F2D_API int32_t f2d_world_is_sleeping_enabled( int32_t worldId );
+/* RawBox2D.worldEnableContinuous / worldIsContinuousEnabled (raw_box2d.dart:55-58). */
+F2D_API void f2d_world_enable_continuous( int32_t worldId, int32_t enabled );
+F2D_API int32_t f2d_world_is_continuous_enabled( int32_t worldId );
+
+/* ---- bodies ------------------------------------------------------------- */
+
+/* RawBox2D.createBody (raw_box2d.dart:71; raw_box2d_ffi.dart:135 -> b2CreateBody). */
+F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def* def, int32_t* index1,
+								 int32_t* worldAndGeneration );
+/* RawBox2D.bodyIsValid (raw_box2d.dart:99 -> b2Body_IsValid). */
+F2D_API int32_t f2d_body_is_valid( int32_t index1, int32_t worldAndGeneration );
+/* RawBox2D.bodyGetPosition / bodyGetRotation (raw_box2d.dart:102-106). */
+F2D_API void f2d_body_get_position( int32_t index1, int32_t worldAndGeneration, double* x, double* y );
+F2D_API void f2d_body_get_rotation( int32_t index1, int32_t worldAndGeneration, double* c, double* s );
+/* RawBox2D.bodySetTransform (raw_box2d.dart:109 -> b2Body_SetTransform). */
+F2D_API void f2d_body_set_transform( int32_t index1, int32_t worldAndGeneration, double px, double py, double c,
+									 double s );
+/* RawBox2D.bodyGet/SetLinearVelocity, bodyGet/SetAngularVelocity (raw_box2d.dart:119-133). */
+F2D_API void f2d_body_get_linear_velocity( int32_t index1, int32_t worldAndGeneration, double* x, double* y );
+F2D_API void f2d_body_set_linear_velocity( int32_t index1, int32_t worldAndGeneration, double x, double y );
+F2D_API double f2d_body_get_angular_velocity( int32_t index1, int32_t worldAndGeneration );
+F2D_API void f2d_body_set_angular_velocity( int32_t index1, int32_t worldAndGeneration, double w );
+/* RawBox2D.bodyApplyForce / bodyApplyForceToCenter / bodyApplyTorque /
+ * bodyApplyLinearImpulse / bodyApplyLinearImpulseToCenter /
+ * bodyApplyAngularImpulse (raw_box2d.dart:136-190). wake is accepted and,
+ * with sleeping handled per world, has no further effect. */
+F2D_API void f2d_body_apply_force( int32_t index1, int32_t worldAndGeneration, double fx, double fy, double px,
+								   double py, int32_t wake );
+F2D_API void f2d_body_apply_force_to_center( int32_t index1, int32_t worldAndGeneration, double fx, double fy,
+											 int32_t wake );
+F2D_API void f2d_body_apply_torque( int32_t index1, int32_t worldAndGeneration, double torque, int32_t wake );
+F2D_API void f2d_body_apply_linear_impulse( int32_t index1, int32_t worldAndGeneration, double ix, double iy,
+											double px, double py, int32_t wake );
+F2D_API void f2d_body_apply_linear_impulse_to_center( int32_t index1, int32_t worldAndGeneration, double ix,
+													  double iy, int32_t wake );
+F2D_API void f2d_body_apply_angular_impulse( int32_t index1, int32_t worldAndGeneration, double impulse,
+											 int32_t wake );
+/* RawBox2D.bodyGetMass / bodyGetRotationalInertia / bodyGetType (raw_box2d.dart:192-217). */
+F2D_API double f2d_body_get_mass( int32_t index1, int32_t worldAndGeneration );
+F2D_API double f2d_body_get_rotational_inertia( int32_t index1, int32_t worldAndGeneration );
+F2D_API int32_t f2d_body_get_type( int32_t index1, int32_t worldAndGeneration );
+F2D_API int32_t f2d_body_is_awake( int32_t index1, int32_t worldAndGeneration );
+
+/* ---- shapes ------------------------------------------------------------- */
+
+/* RawBox2D.createCircleShape (raw_box2d.dart:327; raw_box2d_ffi.dart:588 -> b2CreateCircleShape). */
+F2D_API int32_t f2d_create_circle_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration, const f2d_shape_def* def,
+										 double centerX, double centerY, double radius, int32_t* index1,
+										 int32_t* worldAndGeneration );
+/* RawBox2D.createCapsuleShape (raw_box2d.dart:336; raw_box2d_ffi.dart:612 -> b2CreateCapsuleShape). */
+F2D_API int32_t f2d_create_capsule_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration,
+										  const f2d_shape_def* def, double center1X, double center1Y,
+										  double center2X, double center2Y, double radius, int32_t* index1,
+										  int32_t* worldAndGeneration );
+/* RawBox2D.createSegmentShape (raw_box2d.dart:348; raw_box2d_ffi.dart:640 -> b2CreateSegmentShape). */
+F2D_API int32_t f2d_create_segment_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration,
+										  const f2d_shape_def* def, double point1X, double point1Y,
+										  double point2X, double point2Y, int32_t* index1,
+										  int32_t* worldAndGeneration );
+/* RawBox2D.createBoxShape (raw_box2d.dart:363; raw_box2d_ffi.dart:666 ->
+ * b2MakeOffsetRoundedBox + b2CreatePolygonShape). */
+F2D_API int32_t f2d_create_box_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration, const f2d_shape_def* def,
+									  double halfWidth, double halfHeight, double centerX, double centerY,
+									  double rotationCos, double rotationSin, double radius, int32_t* index1,
+									  int32_t* worldAndGeneration );
+/* RawBox2D.createPolygonShape (raw_box2d.dart:380; raw_box2d_ffi.dart:696 ->
+ * b2ComputeHull + b2MakePolygon + b2CreatePolygonShape). points packed
+ * x0,y0,x1,y1,...; returns 0 for a degenerate hull (forge2d throws
+ * ArgumentError there, raw_box2d_ffi.dart:717-721). */
+F2D_API int32_t f2d_create_polygon_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration,
+										  const f2d_shape_def* def, const double* points, int32_t count,
+										  double radius, int32_t* index1, int32_t* worldAndGeneration );
+/* RawBox2D.shapeIsValid / shapeGetType (raw_box2d.dart:397-400). */
+F2D_API int32_t f2d_shape_is_valid( int32_t index1, int32_t worldAndGeneration );
+F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t worldAndGeneration );
+
+/* ---- joints ------------------------------------------------------------- */
+
+/* RawBox2D.createRevoluteJoint (world.dart:297-321 -> b2CreateRevoluteJoint, joint.c:507). */
+F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
+										   int32_t* worldAndGeneration );
+F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );
+
+/* ---- events (RawBox2D.worldGetContactEvents / worldGetBodyEvents,
+ *      raw_box2d_ffi.dart:2172 and :2259) ----------------------------------
+ * Counts of the last step's events: begin, end, hit, body move. */
+F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* counts4 );
+/* Begin / end touch events as shape id pairs (index1, worldAndGeneration) x 2
+ * = 4 ints per event. Return the number written. */
+F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int32_t capacity );
+F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* out4, int32_t capacity );
+/* Hit events: 4 ints (shape ids) and 5 floats (point.xy normal.xy approachSpeed). */
+F2D_API int32_t f2d_world_get_hit_events( int32_t worldId, int32_t* ints4, float* floats5, int32_t capacity );
+/* Body move events: 2 ints (body index1, worldAndGeneration) + 1 int fellAsleep,
+ * and 4 floats (transform p.xy q.cs) per moved body. */
+F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* ints3, float* floats4, int32_t capacity );
+
+/* ---- queries (RawBox2D.worldCastRayClosest / worldOverlapAabb,
+ *      raw_box2d_ffi.dart:2285 and :2388) --------------------------------- */
+/* Returns 1 on hit; writes shape id (2 ints) and point.xy normal.xy fraction. */
+F2D_API int32_t f2d_world_cast_ray_closest( int32_t worldId, double originX, double originY, double translationX,
+											double translationY, int64_t categoryBits, int64_t maskBits,
+											int32_t* shape2, float* out5 );
+/* Shapes whose fat AABB overlaps the box (b2World_OverlapAABB tests tree
+ * boxes only, dynamic_tree.c:1114). Writes shape id pairs; returns the total
+ * count (may exceed capacity). */
+F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lowerX, double lowerY, double upperX, double upperY,
+										int64_t categoryBits, int64_t maskBits, int32_t* shapes2, int32_t capacity );
+
+/* ---- bulk state access (for batch readers and parity checks) ------------ */
+/* Per body id, 12 floats: p.xy q.cs v.xy w centre.xy valid type sleepTime. */
+F2D_API int32_t f2d_world_body_capacity( int32_t worldId );
+F2D_API int32_t f2d_world_get_bodies( int32_t worldId, float* out12, int32_t capacity );
+/* Per live contact: 9 ints (id shapeA shapeB colour pointCount flags simFlags
+ * id0 id1) and 25 floats (normal.xy rollingImpulse, then per point anchorA.xy
+ * anchorB.xy point.xy separation normalImpulse tangentImpulse
+ * totalNormalImpulse normalVelocity). */
+F2D_API int32_t f2d_world_contact_capacity( int32_t worldId );
+F2D_API int32_t f2d_world_get_contacts( int32_t worldId, int32_t* ints9, float* floats25, int32_t capacity );
+/* Per shape id: aabb(4) fat aabb(4) floats; proxyKey bodyId type flags ints. */
+F2D_API int32_t f2d_world_shape_capacity( int32_t worldId );
+F2D_API int32_t f2d_world_get_shapes( int32_t worldId, float* floats8, int32_t* ints4, int32_t capacity );
+/* Per body id: mass inertia invMass invInertia localCenter.xy minExtent maxExtent. */
+F2D_API int32_t f2d_world_get_mass( int32_t worldId, float* out8, int32_t capacity );
+/* Colour occupancy (contacts + joints per graph colour, 12 ints; b2Counters.colorCounts). */
+F2D_API void f2d_world_get_color_counts( int32_t worldId, int32_t* out12 );
+/* Contact ids for the pairs the next step creates (parity with an external
+ * Box2D run): rows of (contactId, shapeIdA, shapeIdB), 0-based ids. */
+F2D_API void f2d_world_set_contact_plan( int32_t worldId, const int32_t* rows3, int32_t count );
+/* Device timing of the last step in milliseconds (CUDA events around the
+ * step's launches); 0 before the first step. */
+F2D_API double f2d_world_last_step_ms( int32_t worldId );
+/* Number of kernel launches the last step enqueued. */
+F2D_API int32_t f2d_world_last_step_launches( int32_t worldId );
+/* Capacities chosen at creation can be raised before the first step. */
+F2D_API void f2d_world_reserve( int32_t worldId, int32_t bodies, int32_t shapes, int32_t contacts, int32_t joints );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
