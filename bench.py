@@ -1,0 +1,366 @@
+"""Benchmark of the GPU world step: body-steps/s on one GB300.
+
+Workload (default): the 100k-body mixed pile -- 40% circles, 30% capsules,
+30% convex polygons from seed 1234, uniform spawn in a 400x800 region above a
+static U-shaped container, density 1, friction 0.6, restitution U[0,0.3],
+dt=1/60, 4 substeps, sleep off, continuous collision on (synthetic scene
+generated by forge2d_gb300/scenes.py; no dataset exists for this metric).
+
+A step is one world step (b2World_Step). Timing: W warm-up steps, then K
+steps bracketed by a barrier and torch.cuda.synchronize(); each timed step is
+preceded by an untimed 512 MB write that flushes the 129 MB L2, and is timed
+with CUDA events recorded by the library on its own launching stream. The
+e2e figure times the same steps through the C ABI with host buffers: step,
+then read every body's transform into host memory.
+
+--impl reference times the CPU restatement of the reference step (oracle/,
+plain C, all host threads it uses) on the same scene and frames; it is the
+reference arm because the reference's Box2D sources are not available on
+the GPU host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s on 1 GB300: plain vs batched/learned-warm-start at equal penetration"
+HBM_FALLBACK = 6800.0
+
+WORKLOADS = {
+    "pile100k": dict(scene="pile", kw=dict(count=100_000, seed=1234),
+                     desc="100k mixed circles/capsules/polygons (40/30/30), spawn 400x800 above a static U container, "
+                          "density 1, friction 0.6, restitution U[0,0.3], dt=1/60, 4 substeps, 600 frames"),
+    "pyramid": dict(scene="pyramid", kw=dict(),
+                    desc="40-row pyramid of 820 unit boxes on a 100x2 static box, dt=1/60, 4 substeps, 256 frames"),
+    "pyramids_chains": dict(scene="pyramids_chains", kw=dict(),
+                            desc="64 pyramids (52,480 boxes) + 200 revolute chains of 50 capsules (10k joints), "
+                                 "dt=1/60, 4 substeps, 512 frames"),
+}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+def ncu_traffic(kernel="k_solve", workload="pile100k"):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch: N')."""
+    path = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload))
+    try:
+        for line in open(path):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def solver_bytes(c):
+    """Algorithmic bytes of one launch of the persistent solver kernel
+    (substeps x {warm start, solve, relax} per touching contact, body
+    integration, restitution and impulse storage), per-unit figures as
+    stated in the design doc."""
+    sub = 4
+    per_contact = sub * (100 + 24 + 204 + 52 + 204 + 52) + 112 + 72
+    per_body = sub * (56 + 44)
+    return c["touching"] * per_contact + c["awake_bodies"] * per_body
+
+
+def reduce_over_ranks(ms_total, world, device):
+    """The job's timed milliseconds: the maximum over ranks (every replica
+    runs the same number of steps, so the slowest rank bounds the job)."""
+    if world is None:
+        return ms_total, 1
+    import torch
+    t = torch.tensor([ms_total], dtype=torch.float64, device=device)
+    world.all_reduce(t, op=world.ReduceOp.MAX)
+    return float(t.item()), world.get_world_size()
+
+
+def job_throughput(nranks, bodies_per_rank, steps, ms_total):
+    """Body-steps per second of the whole job (weak scaling: every rank
+    steps its own replica of the workload)."""
+    return nranks * bodies_per_rank * steps / (ms_total * 1e-3)
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from forge2d_gb300 import scenes
+    from forge2d_gb300.world import GpuWorld
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    spec = WORKLOADS[args.workload]
+    wd = scenes.world_def(enableSleep=0, enableContinuous=1)
+    g = GpuWorld(wd)
+    scenes.build(g, spec["scene"], **spec["kw"])
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        st = g.step(1.0 / 60.0, 4)
+    st = g.sync()
+    counters = g.counters()
+    bodies = counters["awake_bodies"]
+
+    # ---- device-timed value -------------------------------------------
+    if world is not None:
+        world.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    total_ms = 0.0
+    status = 0
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        status |= g.step(1.0 / 60.0, 4)
+        status |= g.sync()
+        total_ms += g.last_step_ms()
+        launches += g.last_step_launches()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if world is not None:
+        world.barrier()
+    clk = clocks.stop()
+    counters_after = g.counters()
+
+    # ---- e2e through the C ABI with host buffers ----------------------
+    import numpy as np
+
+    n = g.lib.f2d_world_body_capacity(g.id)
+    host = np.zeros((n, 12), np.float32)
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 60))
+    t1 = time.perf_counter()
+    import ctypes as C
+    ptr = host.ctypes.data_as(C.POINTER(C.c_float))
+    for _ in range(e2e_steps):
+        g.lib.f2d_world_step(g.id, 1.0 / 60.0, 4)
+        g.lib.f2d_world_get_bodies(g.id, ptr, n)
+    e2e_s = time.perf_counter() - t1
+
+    # ---- live roofline of the dominant kernel (profiled steps) ---------
+    g.set_profiling(True)
+    reps = 3
+    solve_ms = []
+    phases = np.zeros(6)
+    for _ in range(reps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        g.step(1.0 / 60.0, 4)
+        g.sync()
+        p = g.phase_ms()
+        phases += p
+        solve_ms.append(p[4])
+    g.set_profiling(False)
+    c_prof = g.counters()
+    phases /= reps
+    solve_avg = sum(solve_ms) / len(solve_ms)
+    alg = solver_bytes(c_prof)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (solve_avg * 1e-3) / 1e9 if solve_avg > 0 else None
+    traffic = ncu_traffic()
+
+    # ---- reduce over ranks -------------------------------------------
+    ms_total, nranks = reduce_over_ranks(total_ms, world, "cuda")
+    value = job_throughput(nranks, bodies, args.steps, ms_total)
+    e2e_value = nranks * bodies * e2e_steps / e2e_s
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "body-steps/s",
+        "n_gpus": nranks,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene generator, forge2d_gb300/scenes.py)",
+        "config": {"workload": args.workload, "description": spec["desc"], "bodies_per_gpu": bodies,
+                   "frames": "timed frames %d..%d of the scene" % (args.warmup, args.warmup + args.steps - 1),
+                   "sleep": False, "continuous": True, "substeps": 4,
+                   "l2": "flushed before every timed step (512 MB write, untimed)",
+                   "parallelism": "replicas" if nranks > 1 else "single world",
+                   "contacts_live_end": counters_after["contacts"],
+                   "touching_end": counters_after["touching"]},
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(n * 12 * 4),
+                "what": "f2d_world_step + f2d_world_get_bodies (all body transforms/velocities to a host buffer)",
+                "steps": e2e_steps},
+        "roofline": {"kernel": "k_solve (persistent cooperative solver)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg,
+                     "avg_launch_ms": solve_avg},
+        "phases_ms": {"broadphase": phases[0], "narrowphase": phases[1], "colouring": phases[2],
+                      "solver_setup": phases[3], "solver_kernel": phases[4], "finalize": phases[5]},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "status": status,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0 and args.cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args, bodies_hint=bodies)
+    return result, rank
+
+
+def cpu_baseline(args, bodies_hint=None, budget_s=None):
+    """Bounded sample of the CPU restatement on this host's cores."""
+    from forge2d_gb300 import scenes
+    from oracle.oracle import PortWorld
+
+    spec = WORKLOADS[args.workload]
+    wd = scenes.world_def(enableSleep=0, enableContinuous=1)
+    p = PortWorld(wd)
+    scenes.build(p, spec["scene"], **spec["kw"])
+    for _ in range(args.warmup):
+        p.step(1.0 / 60.0, 4)
+    budget = args.cpu_budget if budget_s is None else budget_s
+    frames, spent = 0, 0.0
+    while spent < budget and frames < args.steps:
+        spent += p.step_timed(1.0 / 60.0, 4, 1)
+        frames += 1
+    bodies = p.awake_body_count()
+    threads = int(os.environ.get("OMP_NUM_THREADS", "0")) or (os.cpu_count() or 1)
+    value = bodies * frames / spent
+    p.close()
+    return {"value": value, "unit": "body-steps/s", "cores": port_threads(threads), "kind": "port",
+            "sample": "frames %d..%d of the %s scene (%d frames, %.1f s of CPU step time)" % (
+                args.warmup, args.warmup + frames - 1, args.workload, frames, spent)}
+
+
+def port_threads(default):
+    try:
+        from oracle.oracle import PortWorld  # noqa
+        import ctypes
+        lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libf2d_port.so"))
+        fn = getattr(lib, "orc_thread_count", None)
+        if fn is None:
+            return 1
+        fn.restype = ctypes.c_int
+        return int(fn())
+    except Exception:
+        return 1
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    base = cpu_baseline(args, budget_s=args.cpu_budget)
+    line = {"metric": METRIC, "value": base["value"], "unit": "body-steps/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene generator, forge2d_gb300/scenes.py)",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"]},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="pile100k", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", 0))
+    wsize = int(os.environ.get("WORLD_SIZE", 1))
+    world = None
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if wsize > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.gpus > 1 else "gloo")
+        world = dist
+    result, rank = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world is not None:
+        world.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -31,6 +31,7 @@ struct StepScratch
 	int shapeIdBits;
 	int solverBlocks;  // persistent solver grid (co-resident)
 	int solverThreads;
+	cudaEvent_t evSolveStart; // recorded right before the cooperative solver launch when non-null
 };
 
 void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode );

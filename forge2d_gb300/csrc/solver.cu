@@ -896,5 +896,7 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 	int* jointSlots = s.tmpB;
 	int* jointStart = s.tmpB + w.jointCap;
 	void* args[] = { &w, &p, &jointSlots, &jointStart };
+	if ( s.evSolveStart )
+		cudaEventRecord( s.evSolveStart, st );
 	cudaLaunchCooperativeKernel( (void*)k_solve, dim3( s.solverBlocks ), dim3( SOLVER_THREADS ), args, 0, st );
 }

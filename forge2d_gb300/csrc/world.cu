@@ -49,6 +49,10 @@ struct HostWorld
 	float lastStepMs = 0.0f;
 	int lastLaunches = 0;
 
+	// phase timing (profiling mode: no graph, events between phases)
+	bool profiling = false;
+	cudaEvent_t ph[7] = {};
+
 	// graph replay
 	cudaGraphExec_t graphExec = nullptr;
 	float graphDt = 0.0f;
@@ -1103,12 +1107,30 @@ extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )
 static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 {
 	DWorld& d = W->d;
+	bool prof = W->profiling;
+	if ( prof && W->ph[0] == nullptr )
+		for ( int i = 0; i < 7; ++i )
+			cudaEventCreate( W->ph + i );
+	W->s.evSolveStart = prof ? W->ph[4] : nullptr;
 	launch_reset_counters( d, W->stream );
+	if ( prof )
+		cudaEventRecord( W->ph[0], W->stream );
 	launch_broadphase( d, W->s, W->stream, planMode );
+	if ( prof )
+		cudaEventRecord( W->ph[1], W->stream );
 	launch_narrowphase( d, W->s, W->stream );
+	if ( prof )
+		cudaEventRecord( W->ph[2], W->stream );
 	launch_graph( d, W->s, W->stream );
+	if ( prof )
+		cudaEventRecord( W->ph[3], W->stream );
 	launch_solver( d, W->s, W->stream, dt, subSteps );
+	if ( prof )
+		cudaEventRecord( W->ph[5], W->stream );
 	launch_finalize( d, W->s, W->stream, dt );
+	if ( prof )
+		cudaEventRecord( W->ph[6], W->stream );
+	W->s.evSolveStart = nullptr;
 }
 
 static int count_kernel_nodes( cudaGraph_t g )
@@ -1157,7 +1179,7 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	}
 	cudaMemsetAsync( &W->d.sc->error, 0, sizeof( int ), W->stream );
 	cudaEventRecord( W->evStart, W->stream );
-	bool useGraph = planMode == 0;
+	bool useGraph = planMode == 0 && !W->profiling;
 	if ( useGraph && ( W->graphDirty || W->graphExec == nullptr || W->graphDt != dt || W->graphSubSteps != subSteps ) )
 	{
 		if ( W->graphExec )
@@ -1861,6 +1883,66 @@ extern "C" F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* 
 		m += 1;
 	}
 	return m;
+}
+
+// ---------------------------------------------------------------------------
+// profiling and counters
+// ---------------------------------------------------------------------------
+extern "C" F2D_API void f2d_world_set_profiling( int32_t worldId, int32_t enabled )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->profiling = enabled != 0;
+}
+
+extern "C" F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 )
+{
+	for ( int i = 0; i < 6; ++i )
+		out6[i] = 0.0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || W->ph[0] == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	// broadphase, narrowphase, colouring, solver set-up, solver kernel, finalize
+	const int a[6] = { 0, 1, 2, 3, 4, 5 };
+	const int b[6] = { 1, 2, 3, 4, 5, 6 };
+	for ( int i = 0; i < 6; ++i )
+	{
+		float ms = 0.0f;
+		if ( cudaEventElapsedTime( &ms, W->ph[a[i]], W->ph[b[i]] ) == cudaSuccess )
+			out6[i] = ms;
+	}
+}
+
+extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )
+{
+	for ( int i = 0; i < 8; ++i )
+		out8[i] = 0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	int awake = 0;
+	for ( int b = 0; b < W->bodyCount; ++b )
+	{
+		int f = W->bflags[b];
+		if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
+			awake += 1;
+	}
+	int active = 0;
+	for ( int c = 0; c < 11; ++c )
+		active += sc.colorCount[c] > 0 ? 1 : 0;
+	out8[0] = awake;
+	out8[1] = sc.contactIdCount - sc.contactFreeCount;
+	out8[2] = sc.touchingCount;
+	out8[3] = sc.overflowCount;
+	out8[4] = active;
+	out8[5] = sc.colorRounds;
+	out8[6] = W->shapeCount;
+	out8[7] = W->jointCount;
 }
 
 // ---------------------------------------------------------------------------

@@ -111,7 +111,8 @@ def _polygon_points(rng, n, radius):
 
 
 def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
-         frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False):
+         frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False,
+         enable_contact_events=False):
     """BASELINE config 2: ``count`` bodies drawn from ``seed`` -- 40% circles
     r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
     30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
@@ -137,7 +138,8 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
         a = float(angles[k])
         body = b.create_body(body_def(type=DYNAMIC, positionX=float(xs[k]), positionY=float(ys[k]),
                                       rotationCos=math.cos(a), rotationSin=math.sin(a)))
-        sd = shape_def(restitution=float(rest[k]), enableHitEvents=int(enable_hit_events))
+        sd = shape_def(restitution=float(rest[k]), enableHitEvents=int(enable_hit_events),
+                       enableContactEvents=int(enable_contact_events))
         u = kinds[k]
         if u < frac_circle:
             b.create_circle(body, sd, 0.0, 0.0, float(rng.uniform(0.25, 0.75)))

@@ -137,6 +137,21 @@ class GpuWorld:
     def last_step_launches(self) -> int:
         return self.lib.f2d_world_last_step_launches(self.id)
 
+    def set_profiling(self, enabled: bool):
+        self.lib.f2d_world_set_profiling(self.id, int(enabled))
+
+    def phase_ms(self) -> np.ndarray:
+        out = np.zeros(6, np.float64)
+        self.lib.f2d_world_get_phase_ms(self.id, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def counters(self) -> dict:
+        out = np.zeros(8, np.int32)
+        self.lib.f2d_world_get_counters(self.id, _iptr(out))
+        keys = ("awake_bodies", "contacts", "touching", "overflow", "active_colors", "color_rounds", "shapes",
+                "joints")
+        return {k: int(v) for k, v in zip(keys, out)}
+
     def set_contact_plan(self, plan):
         plan = np.ascontiguousarray(np.asarray(plan, dtype=np.int32).reshape(-1, 3))
         self.lib.f2d_world_set_contact_plan(self.id, _iptr(plan), len(plan))

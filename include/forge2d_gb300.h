@@ -289,6 +289,15 @@ F2D_API void f2d_world_set_contact_plan( int32_t worldId, const int32_t* rows3, 
 F2D_API double f2d_world_last_step_ms( int32_t worldId );
 /* Number of kernel launches the last step enqueued. */
 F2D_API int32_t f2d_world_last_step_launches( int32_t worldId );
+/* Profiling mode: steps are enqueued without the CUDA graph and with CUDA
+ * events between phases (b2Profile's per-stage timers, types.h:466-490). */
+F2D_API void f2d_world_set_profiling( int32_t worldId, int32_t enabled );
+/* Last profiled step, ms: broadphase, narrowphase, colouring, solver set-up,
+ * solver kernel, finalize. */
+F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 );
+/* awake bodies, live contacts, touching contacts, overflow contacts, active
+ * colours, colouring rounds, shapes, joints (b2Counters, types.h:493-506). */
+F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 );
 /* Capacities chosen at creation can be raised before the first step. */
 F2D_API void f2d_world_reserve( int32_t worldId, int32_t bodies, int32_t shapes, int32_t contacts, int32_t joints );
 

@@ -287,10 +287,10 @@ typedef struct World
 	int endCount, endCap;
 	int* hitShapes;
 	float* hitData;
-	int hitCount, hitCap;
+	int hitCount, hitCap, hitDataCap;
 	int* moveEventBodies;
 	float* moveEventXf;
-	int moveEventCount, moveEventCap;
+	int moveEventCount, moveEventCap, moveEventXfCap;
 
 	int stepIndex;
 } World;

@@ -1,0 +1,304 @@
+// World queries of the restatement: closest ray hit and AABB overlap.
+// TEST INFRASTRUCTURE (oracle).
+//
+// Reference (packages/forge2d/third_party/box2d/src/):
+//   world.c:2050-2098  b2World_OverlapAABB: every proxy whose tree box (the
+//                      fat AABB) overlaps the query box and whose filter
+//                      passes b2ShouldQueryCollide (shape.h:132-135)
+//   world.c:2185-2310  b2World_CastRayClosest: ray against the shapes in the
+//                      three trees, hits at fraction 0 (initial overlap)
+//                      ignored, the closest hit kept
+//   shape.c:792-832    b2RayCastShape: cast in the shape's local frame
+//   geometry.c:506-870 circle, capsule, segment and zero-radius polygon casts
+//
+// The trees only cull; the answer is the minimum-fraction hit over all shapes,
+// found here by a linear scan. Equal fractions resolve to the lower shape id.
+#include "port.h"
+
+#include <stddef.h>
+
+World* p_world( int w ); // pworld.c
+
+typedef struct CastOut
+{
+	v2 point, normal;
+	float fraction;
+	int hit;
+} CastOut;
+
+static CastOut cast_none( void )
+{
+	CastOut o;
+	o.point = V( 0.0f, 0.0f );
+	o.normal = V( 0.0f, 0.0f );
+	o.fraction = 0.0f;
+	o.hit = 0;
+	return o;
+}
+
+// geometry.c:506-580
+static CastOut ray_circle( v2 origin, v2 translation, float maxFraction, v2 center, float r )
+{
+	CastOut o = cast_none();
+	v2 s = sub( origin, center );
+	float rr = r * r;
+	float len;
+	v2 d = lengthAndNormalize( &len, translation );
+	if ( len == 0.0f )
+	{
+		if ( lengthSq( s ) < rr )
+		{
+			o.point = origin;
+			o.hit = 1;
+		}
+		return o;
+	}
+	float t = -dot( s, d );
+	v2 c = mulAdd( s, t, d );
+	float cc = dot( c, c );
+	if ( cc > rr )
+		return o;
+	float h = sqrtf( rr - cc );
+	float fraction = t - h;
+	if ( fraction < 0.0f || maxFraction * len < fraction )
+	{
+		if ( lengthSq( s ) < rr )
+		{
+			o.point = origin;
+			o.hit = 1;
+		}
+		return o;
+	}
+	v2 hp = mulAdd( s, fraction, d );
+	o.fraction = fraction / len;
+	o.normal = normalize( hp );
+	o.point = mulAdd( center, r, o.normal );
+	o.hit = 1;
+	return o;
+}
+
+// geometry.c:582-716
+static CastOut ray_capsule( v2 origin, v2 translation, float maxFraction, v2 v1, v2 v2p, float radius )
+{
+	CastOut o = cast_none();
+	float capLen;
+	v2 a = lengthAndNormalize( &capLen, sub( v2p, v1 ) );
+	if ( capLen < FLT_EPSILON )
+		return ray_circle( origin, translation, maxFraction, v1, radius );
+	v2 q = sub( origin, v1 );
+	float qa = dot( q, a );
+	v2 qp = mulAdd( q, -qa, a );
+	if ( dot( qp, qp ) < radius * radius )
+	{
+		// origin inside the capsule's rectangle band or one of its end caps
+		if ( qa < 0.0f )
+			return ray_circle( origin, translation, maxFraction, v1, radius );
+		if ( qa > capLen )
+			return ray_circle( origin, translation, maxFraction, v2p, radius );
+		o.point = origin;
+		o.hit = 1;
+		return o;
+	}
+	v2 n = V( a.y, -a.x );
+	float rayLen;
+	v2 u = lengthAndNormalize( &rayLen, translation );
+	float den = -a.x * u.y + u.x * a.y;
+	if ( -FLT_EPSILON < den && den < FLT_EPSILON )
+		return o;
+	v2 b1 = mulSub( q, radius, n );
+	v2 b2 = mulAdd( q, radius, n );
+	float invDen = 1.0f / den;
+	float s21 = ( a.x * b1.y - b1.x * a.y ) * invDen;
+	float s22 = ( a.x * b2.y - b2.x * a.y ) * invDen;
+	float s2;
+	v2 b;
+	if ( s21 < s22 )
+	{
+		s2 = s21;
+		b = b1;
+	}
+	else
+	{
+		s2 = s22;
+		b = b2;
+		n = neg( n );
+	}
+	if ( s2 < 0.0f || maxFraction * rayLen < s2 )
+		return o;
+	float s1 = ( -b.x * u.y + u.x * b.y ) * invDen;
+	if ( s1 < 0.0f )
+		return ray_circle( origin, translation, maxFraction, v1, radius );
+	if ( capLen < s1 )
+		return ray_circle( origin, translation, maxFraction, v2p, radius );
+	o.fraction = s2 / rayLen;
+	o.point = add( lerp( v1, v2p, s1 / capLen ), mulSV( radius, n ) );
+	o.normal = n;
+	o.hit = 1;
+	return o;
+}
+
+// geometry.c:718-797 (two-sided)
+static CastOut ray_segment( v2 origin, v2 translation, float maxFraction, v2 v1, v2 v2p )
+{
+	CastOut o = cast_none();
+	float len;
+	v2 eu = lengthAndNormalize( &len, sub( v2p, v1 ) );
+	if ( len == 0.0f )
+		return o;
+	v2 normal = rightPerp( eu );
+	float num = dot( normal, sub( v1, origin ) );
+	float den = dot( normal, translation );
+	if ( den == 0.0f )
+		return o;
+	float t = num / den;
+	if ( t < 0.0f || maxFraction < t )
+		return o;
+	v2 p = mulAdd( origin, t, translation );
+	float s = dot( sub( p, v1 ), eu );
+	if ( s < 0.0f || len < s )
+		return o;
+	if ( num > 0.0f )
+		normal = neg( normal );
+	o.fraction = t;
+	o.point = p;
+	o.normal = normal;
+	o.hit = 1;
+	return o;
+}
+
+// geometry.c:799-878, zero-radius branch
+static CastOut ray_polygon( v2 origin, v2 d, float maxFraction, const Polygon* poly )
+{
+	CastOut o = cast_none();
+	v2 base = poly->vertices[0];
+	v2 p1 = sub( origin, base );
+	float lower = 0.0f, upper = maxFraction;
+	int index = -1;
+	for ( int i = 0; i < poly->count; ++i )
+	{
+		v2 vertex = sub( poly->vertices[i], base );
+		float num = dot( poly->normals[i], sub( vertex, p1 ) );
+		float den = dot( poly->normals[i], d );
+		if ( den == 0.0f )
+		{
+			if ( num < 0.0f )
+				return o;
+		}
+		else if ( den < 0.0f && num < lower * den )
+		{
+			lower = num / den;
+			index = i;
+		}
+		else if ( den > 0.0f && num < upper * den )
+			upper = num / den;
+		if ( upper < lower )
+			return o;
+	}
+	if ( index >= 0 )
+	{
+		o.fraction = lower;
+		o.normal = poly->normals[index];
+		o.point = mulAdd( origin, lower, d );
+	}
+	else
+		o.point = origin;
+	o.hit = 1;
+	return o;
+}
+
+static int query_collide( const Shape* s, uint64_t cat, uint64_t mask )
+{
+	return ( s->categoryBits & mask ) != 0 && ( s->maskBits & cat ) != 0;
+}
+
+// shape.c:792-832
+static CastOut ray_shape( const Shape* s, xform xf, v2 origin, v2 translation )
+{
+	v2 lo = invXfPoint( xf, origin );
+	v2 lt = invRotate( xf.q, translation );
+	CastOut o;
+	switch ( s->g.type )
+	{
+		case SHAPE_CIRCLE:
+			o = ray_circle( lo, lt, 1.0f, s->g.c1, s->g.radius );
+			break;
+		case SHAPE_CAPSULE:
+			o = ray_capsule( lo, lt, 1.0f, s->g.c1, s->g.c2, s->g.radius );
+			break;
+		case SHAPE_SEGMENT:
+			o = ray_segment( lo, lt, 1.0f, s->g.c1, s->g.c2 );
+			break;
+		case SHAPE_POLYGON:
+			if ( s->g.poly.radius != 0.0f )
+				return cast_none(); // rounded polygons take the shape-cast path, not restated
+			o = ray_polygon( lo, lt, 1.0f, &s->g.poly );
+			break;
+		default:
+			return cast_none();
+	}
+	o.point = xfPoint( xf, o.point );
+	o.normal = rotate( xf.q, o.normal );
+	return o;
+}
+
+int orc_cast_ray_closest( int wi, double ox, double oy, double tx, double ty, long long cat, long long mask, int* shape,
+						  float* out )
+{
+	World* w = p_world( wi );
+	if ( w == NULL )
+		return 0;
+	v2 origin = V( (float)ox, (float)oy ), translation = V( (float)tx, (float)ty );
+	int best = -1;
+	CastOut bo = cast_none();
+	for ( int i = 0; i < w->shapeCount; ++i )
+	{
+		const Shape* s = w->shapes + i;
+		if ( s->used == 0 || s->proxyKey == P_NULL )
+			continue;
+		if ( query_collide( s, (uint64_t)cat, (uint64_t)mask ) == 0 )
+			continue;
+		CastOut o = ray_shape( s, w->bodies[s->bodyId].xf, origin, translation );
+		if ( o.hit == 0 || o.fraction == 0.0f )
+			continue;
+		if ( best < 0 || o.fraction < bo.fraction )
+		{
+			best = i;
+			bo = o;
+		}
+	}
+	if ( best < 0 )
+		return 0;
+	*shape = best;
+	out[0] = bo.point.x;
+	out[1] = bo.point.y;
+	out[2] = bo.normal.x;
+	out[3] = bo.normal.y;
+	out[4] = bo.fraction;
+	return 1;
+}
+
+int orc_overlap_aabb( int wi, double lx, double ly, double ux, double uy, long long cat, long long mask, int* out,
+					  int cap )
+{
+	World* w = p_world( wi );
+	if ( w == NULL )
+		return 0;
+	box2 q;
+	q.lo = V( (float)lx, (float)ly );
+	q.hi = V( (float)ux, (float)uy );
+	int n = 0;
+	for ( int i = 0; i < w->shapeCount; ++i )
+	{
+		const Shape* s = w->shapes + i;
+		if ( s->used == 0 || s->proxyKey == P_NULL )
+			continue;
+		if ( query_collide( s, (uint64_t)cat, (uint64_t)mask ) == 0 )
+			continue;
+		if ( boxOverlaps( s->fatAABB, q ) == false )
+			continue;
+		if ( n < cap )
+			out[n] = i;
+		n += 1;
+	}
+	return n;
+}

@@ -522,11 +522,8 @@ static void store_impulses( World* w, const Constraint* c, int graphLane )
 
 static void push_hit( World* w, int a, int b, v2 point, v2 normal, float speed )
 {
-	int cap = w->hitCap;
-	w->hitShapes = grow( w->hitShapes, &cap, 2 * ( w->hitCount + 1 ), sizeof( int ) );
-	int cap2 = w->hitCap;
-	w->hitData = grow( w->hitData, &cap2, 5 * ( w->hitCount + 1 ), sizeof( float ) );
-	w->hitCap = cap < cap2 ? cap : cap2;
+	w->hitShapes = grow( w->hitShapes, &w->hitCap, 2 * ( w->hitCount + 1 ), sizeof( int ) );
+	w->hitData = grow( w->hitData, &w->hitDataCap, 5 * ( w->hitCount + 1 ), sizeof( float ) );
 	w->hitShapes[2 * w->hitCount] = a;
 	w->hitShapes[2 * w->hitCount + 1] = b;
 	float* d = w->hitData + 5 * w->hitCount;
@@ -591,11 +588,8 @@ static void finalize_body( World* w, int id, float dt, float inv_dt )
 	b->xf.p = sub( b->center, rotate( b->xf.q, b->localCenter ) );
 	// move event
 	{
-		int cap = w->moveEventCap;
-		w->moveEventBodies = grow( w->moveEventBodies, &cap, w->moveEventCount + 1, sizeof( int ) );
-		int cap2 = w->moveEventCap;
-		w->moveEventXf = grow( w->moveEventXf, &cap2, 4 * ( w->moveEventCount + 1 ), sizeof( float ) );
-		w->moveEventCap = cap < cap2 ? cap : cap2;
+		w->moveEventBodies = grow( w->moveEventBodies, &w->moveEventCap, w->moveEventCount + 1, sizeof( int ) );
+		w->moveEventXf = grow( w->moveEventXf, &w->moveEventXfCap, 4 * ( w->moveEventCount + 1 ), sizeof( float ) );
 		w->moveEventBodies[w->moveEventCount] = id;
 		float* x = w->moveEventXf + 4 * w->moveEventCount;
 		x[0] = b->xf.p.x;
@@ -804,7 +798,9 @@ void p_solve( World* w, float dt, int subStepCount )
 		if ( body_awake( w->bodies + b ) )
 			finalize_body( w, b, dt, inv_dt );
 
-	// hit events (solver.c:1758-1818): colour arrays in order, overflow last
+	// hit events (solver.c:1758-1818): colours in order, overflow last. Within a
+	// colour the reference follows its colour array (append / swap-remove); this
+	// port walks contact ids, so the event ORDER inside a colour can differ.
 	for ( int pass = 0; pass < 2; ++pass )
 	{
 		int lo = pass == 0 ? overflowCount : 0;

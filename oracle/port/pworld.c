@@ -17,6 +17,7 @@
 
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #define MAX_WORLDS 64
 static World s_worlds[MAX_WORLDS];
@@ -752,7 +753,6 @@ static void update_pairs( World* w )
 		if ( u == 0 || cands[u - 1].key != cands[i].key )
 			cands[u++] = cands[i];
 	nc = u;
-
 	// create contacts in native order (ascending pair key) or per plan
 	for ( int i = 0; i < nc; ++i )
 	{
@@ -1056,7 +1056,15 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
 }
 
-double orc_world_step_timed( int wi, double dt, int subSteps, int steps );
+double orc_world_step_timed( int wi, double dt, int subSteps, int steps )
+{
+	struct timespec t0, t1;
+	clock_gettime( CLOCK_MONOTONIC, &t0 );
+	for ( int i = 0; i < steps; ++i )
+		orc_world_step( wi, dt, subSteps );
+	clock_gettime( CLOCK_MONOTONIC, &t1 );
+	return ( t1.tv_sec - t0.tv_sec ) + 1e-9 * ( t1.tv_nsec - t0.tv_nsec );
+}
 
 // ---------------------------------------------------------------------------
 // dumps (same layouts as ref_harness.c)

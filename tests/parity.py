@@ -1,0 +1,47 @@
+"""Lock-step helpers shared by the parity tests.
+
+``lockstep(ref, other, steps)`` steps a reference-side world and a
+candidate world together; before each candidate step it hands the candidate
+the contact ids the reference created in that step (parity mode), so that
+colour assignment and every downstream result can be compared bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def new_contacts(prev: set, ints: np.ndarray):
+    cur = set((int(a), int(b), int(c)) for a, b, c in ints[:, :3])
+    return cur, sorted(cur - prev)
+
+
+def body_rows(world) -> np.ndarray:
+    return world.bodies()[:, :9]
+
+
+def first_mismatch(a: np.ndarray, b: np.ndarray):
+    bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))))
+    return None if len(bad) == 0 else bad[0].tolist()
+
+
+def contact_table(world):
+    ints, fl = world.contacts()
+    return {int(r[0]): (r, f) for r, f in zip(ints, fl)}
+
+
+def compare_contacts(a, b):
+    """Contacts keyed by id: shape pair, colour, point count, point ids and
+    every manifold float must agree. Returns a list of differences."""
+    ta, tb = contact_table(a), contact_table(b)
+    diffs = []
+    if set(ta) != set(tb):
+        diffs.append(("ids", sorted(set(ta) ^ set(tb))[:5]))
+        return diffs
+    for cid in ta:
+        ra, fa = ta[cid]
+        rb, fb = tb[cid]
+        if not (np.array_equal(ra[[1, 2, 3, 4, 7, 8]], rb[[1, 2, 3, 4, 7, 8]]) and np.array_equal(fa, fb)):
+            diffs.append((cid, ra.tolist(), rb.tolist()))
+            if len(diffs) > 5:
+                break
+    return diffs

@@ -1,0 +1,129 @@
+"""Pins the CPU restatement to the live reference (needs the reference
+checkout; skipped elsewhere, where the committed fixtures stand in).
+
+The reference world and the port are stepped in lock step; before each port
+step the port is handed the contact ids the reference created in that step
+(parity mode). Bodies, manifolds, colours, events and query answers must then
+agree bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from forge2d_gb300 import scenes
+
+from parity import compare_contacts, new_contacts
+
+
+def lockstep(ref, port, frames, each=None):
+    prev = set()
+    for f in range(1, frames + 1):
+        ref.step(1.0 / 60.0, 4)
+        ints, _ = ref.contacts()
+        prev, created = new_contacts(prev, ints)
+        if created:
+            port.set_contact_plan(np.array(created, np.int32))
+        port.step(1.0 / 60.0, 4)
+        rb, pb = ref.bodies()[:, :9], port.bodies()[:, :9]
+        bad = np.argwhere(rb.view(np.uint32) != pb.view(np.uint32))
+        assert len(bad) == 0, "frame %d: body/field %s ref %r port %r" % (
+            f, bad[0].tolist(), rb[tuple(bad[0])], pb[tuple(bad[0])])
+        if each is not None:
+            each(f)
+
+
+SCENES = [
+    ("pile_mixed_ccd", dict(enableSleep=0, enableContinuous=1), "pile",
+     dict(count=500, seed=3, width=24.0, height=60.0), 150),
+    ("pile_no_ccd", dict(enableSleep=0, enableContinuous=0), "pile",
+     dict(count=400, seed=7, width=20.0, height=30.0), 120),
+    ("pyramid_small", dict(enableSleep=0), "pyramid", dict(rows=12), 200),
+]
+
+
+@pytest.mark.parametrize("name,wkw,scene,kw,frames", SCENES, ids=[s[0] for s in SCENES])
+def test_port_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene, kw, frames):
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, scene, **kw)
+    scenes.build(port, scene, **kw)
+
+    def each(f):
+        if f % 25 == 0 or f == frames:
+            assert compare_contacts(ref, port) == []
+            assert np.array_equal(ref.color_counts(), port.color_counts())
+
+    lockstep(ref, port, frames, each)
+    ref.close()
+    port.close()
+
+
+def hit_rows(w):
+    ints, fl = w.hit_events()
+    return sorted(tuple(i) + tuple(f) for i, f in zip(ints.tolist(), fl.view(np.uint32).tolist()))
+
+
+def test_port_events_match_reference(ref_lib, port_lib):
+    """Begin/end touch events, hit events and body move events per frame
+    (contact.c:500-560, solver.c:1740-1800, body move events world.c)."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    kw = dict(count=200, seed=21, width=16.0, height=20.0, enable_hit_events=True, enable_contact_events=True)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        scenes.build(w, "pile", **kw)
+
+    totals = np.zeros(4, np.int64)
+
+    def each(f):
+        assert np.array_equal(ref.event_counts(), port.event_counts()), f
+        for a, b in ((ref.begin_events(), port.begin_events()), (ref.end_events(), port.end_events())):
+            assert sorted(map(tuple, a.tolist())) == sorted(map(tuple, b.tolist())), f
+        # hit events: same multiset; the order inside one colour follows the
+        # reference's colour arrays, which the port does not keep
+        assert hit_rows(ref) == hit_rows(port), f
+        ri, rf = ref.move_events()
+        pi, pf = port.move_events()
+        assert np.array_equal(ri, pi) and np.array_equal(rf.view(np.uint32), pf.view(np.uint32)), f
+        totals[:] += ref.event_counts()
+
+    lockstep(ref, port, 90, each)
+    assert totals[0] > 0 and totals[1] > 0 and totals[2] > 0 and totals[3] > 0
+    ref.close()
+    port.close()
+
+
+def test_port_queries_on_moving_scene(ref_lib, port_lib):
+    """Closest-ray and AABB-overlap answers over a settling pile."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    kw = dict(count=300, seed=4, width=20.0, height=20.0)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        scenes.build(w, "pile", **kw)
+    rng = np.random.default_rng(9)
+    hits = [0]
+
+    def each(f):
+        if f % 10:
+            return
+        for _ in range(20):
+            o = rng.uniform(-12, 12, 2)
+            t = rng.uniform(-15, 15, 2)
+            a = ref.cast_ray_closest(o[0], o[1], t[0], t[1])
+            b = port.cast_ray_closest(o[0], o[1], t[0], t[1])
+            assert (a is None) == (b is None)
+            if a is not None:
+                hits[0] += 1
+                assert a[0] == b[0]
+                assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+            lo = rng.uniform(-12, 8, 2)
+            hi = lo + rng.uniform(0.1, 6, 2)
+            assert sorted(ref.overlap_aabb(lo[0], lo[1], hi[0], hi[1]).tolist()) == \
+                sorted(port.overlap_aabb(lo[0], lo[1], hi[0], hi[1]).tolist())
+
+    lockstep(ref, port, 60, each)
+    assert hits[0] > 20
+    ref.close()
+    port.close()
