@@ -40,6 +40,26 @@ struct DManifold
 	int count;
 };
 
+// Every manifold starts zeroed, like the reference's `b2Manifold manifold =
+// { 0 }`: a slot past pointCount then holds exactly what the manifold
+// function left there (b2CollidePolygons' vertex-vertex fallback keeps the
+// second clip point), and the stored manifold reproduces it.
+__device__ __forceinline__ DManifold dm_empty()
+{
+	DManifold m;
+	m.normal = mk( 0.0f, 0.0f );
+	for ( int k = 0; k < 2; ++k )
+	{
+		m.p[k].anchorA = mk( 0.0f, 0.0f );
+		m.p[k].anchorB = mk( 0.0f, 0.0f );
+		m.p[k].point = mk( 0.0f, 0.0f );
+		m.p[k].separation = 0.0f;
+		m.p[k].id = 0u;
+	}
+	m.count = 0;
+	return m;
+}
+
 __device__ __forceinline__ DGeom load_geom( const float4* __restrict__ g, int type )
 {
 	DGeom o;
@@ -143,8 +163,7 @@ __device__ __forceinline__ void one_point( DManifold& m, fxf xfA, fxf xfB, fv2 c
 // manifold.c:40-75 (b2CollideCircles)
 __device__ __forceinline__ DManifold collide_circles( fv2 cA, float rA, fxf xfA, fv2 cB, float rB, fxf xfB )
 {
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	fxf xf = xinvmul( xfA, xfB );
 	fv2 pointA = cA;
 	fv2 pointB = xpoint( xf, cB );
@@ -165,8 +184,7 @@ __device__ __forceinline__ DManifold collide_circles( fv2 cA, float rA, fxf xfA,
 __device__ __forceinline__ DManifold collide_capsule_circle( fv2 p1, fv2 p2, float rA, fxf xfA, fv2 cB, float rB,
 															 fxf xfB )
 {
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	fxf xf = xinvmul( xfA, xfB );
 	fv2 pB = xpoint( xf, cB );
 	fv2 e = vsub( p2, p1 );
@@ -198,8 +216,7 @@ __device__ __forceinline__ DManifold collide_capsule_circle( fv2 p1, fv2 p2, flo
 // manifold.c:141-259 (b2CollidePolygonAndCircle)
 __device__ __forceinline__ DManifold collide_polygon_circle( const DPoly& pa, fxf xfA, fv2 cB, float rB, fxf xfB )
 {
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	fxf xf = xinvmul( xfA, xfB );
 	fv2 center = xpoint( xf, cB );
 	float rA = pa.radius;
@@ -298,8 +315,7 @@ static __device__ __noinline__ DManifold collide_capsules( fv2 a1, fv2 a2, float
 	fv2 closest1 = vmuladd( p1, f1, d1 );
 	fv2 closest2 = vmuladd( p2, f2, d2 );
 	float distanceSquared = vdist2( closest1, closest2 );
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	float radius = rA + rB;
 	float maxDistance = radius + F2D_SPECULATIVE;
 	if ( distanceSquared > maxDistance * maxDistance )
@@ -470,8 +486,7 @@ __device__ __forceinline__ float find_max_sep( int* edge, const DPoly& p1, const
 // manifold.c:545-678 (b2ClipPolygons)
 __device__ __forceinline__ DManifold clip_polygons( const DPoly& pA, const DPoly& pB, int edgeA, int edgeB, bool flip )
 {
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	const DPoly& poly1 = flip ? pB : pA;
 	const DPoly& poly2 = flip ? pA : pB;
 	int i11, i12, i21, i22;
@@ -589,8 +604,7 @@ static __device__ __noinline__ DManifold collide_polygons( const DPoly& polygonA
 	int edgeB = 0;
 	float separationB = find_max_sep( &edgeB, lb, la );
 	float radius = la.radius + lb.radius;
-	DManifold m;
-	m.count = 0;
+	DManifold m = dm_empty();
 	if ( separationA > F2D_SPECULATIVE + radius || separationB > F2D_SPECULATIVE + radius )
 		return m;
 	bool flip;
@@ -677,8 +691,7 @@ static __device__ __noinline__ DManifold collide_polygons( const DPoly& polygonA
 // contact.c:60-124 dispatch; A already carries the registered first type
 __device__ __forceinline__ DManifold compute_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB )
 {
-	DManifold zero;
-	zero.count = 0;
+	DManifold zero = dm_empty();
 	switch ( a.type )
 	{
 		case ST_CIRCLE:

@@ -109,8 +109,6 @@ __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
 						ni = oldNI[j];
 						ti = oldTI[j];
 						persisted = 1;
-						oldNI[j] = 0.0f;
-						oldTI[j] = 0.0f;
 						break;
 					}
 				}
@@ -121,8 +119,12 @@ __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
 			}
 			else
 			{
-				w.mpA[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-				w.mpB[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, __int_as_float( 0 ) );
+				// slot past pointCount: kept as the manifold function left it
+				// (contact.c:472-560 replaces the whole manifold and touches
+				// only the first pointCount points)
+				DPoint p = m.p[i];
+				w.mpA[2 * c + i] = make_float4( p.anchorA.x, p.anchorA.y, p.anchorB.x, p.anchorB.y );
+				w.mpB[2 * c + i] = make_float4( p.point.x, p.point.y, p.separation, __int_as_float( (int)p.id ) );
 				w.mpI[2 * c + i] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 			}
 		}

@@ -69,6 +69,7 @@ struct HostWorld
 	std::vector<int> bodyFree;
 	int bodyCount = 0, bodyUploaded = 0;
 	std::vector<int> bodyDirty;
+	std::vector<uint8_t> bodyIsDirty; // host row newer than the device row
 
 	std::vector<float4> geom, aabb, fat, mat;
 	std::vector<unsigned long long> cat, mask;
@@ -452,7 +453,9 @@ static void upload_joint_rows( HostWorld* W, int lo, int hi )
 // bring one existing body's device-updated fields into the host mirror
 static void pull_body( HostWorld* W, int b )
 {
-	if ( b >= W->bodyUploaded )
+	// rows not yet uploaded, or edited on the host since the last upload, are
+	// authoritative on the host
+	if ( b >= W->bodyUploaded || ( b < (int)W->bodyIsDirty.size() && W->bodyIsDirty[b] ) )
 		return;
 	cudaStreamSynchronize( W->stream );
 	DWorld& d = W->d;
@@ -467,8 +470,15 @@ static void pull_body( HostWorld* W, int b )
 
 static void mark_body( HostWorld* W, int b )
 {
-	if ( b < W->bodyUploaded )
+	if ( b >= W->bodyUploaded )
+		return;
+	if ( (int)W->bodyIsDirty.size() <= b )
+		W->bodyIsDirty.resize( (size_t)W->bodyCount, 0 );
+	if ( W->bodyIsDirty[b] == 0 )
+	{
+		W->bodyIsDirty[b] = 1;
 		W->bodyDirty.push_back( b );
+	}
 }
 
 static void mark_shape( HostWorld* W, int s )
@@ -486,7 +496,10 @@ static void flush_uploads( HostWorld* W )
 		W->bodyUploaded = W->bodyCount;
 	}
 	for ( int b : W->bodyDirty )
+	{
 		upload_body_rows( W, b, b + 1 );
+		W->bodyIsDirty[b] = 0;
+	}
 	W->bodyDirty.clear();
 	if ( W->shapeUploaded < W->shapeCount )
 	{
@@ -1598,6 +1611,14 @@ extern "C" F2D_API int32_t f2d_world_get_bodies( int32_t worldId, float* out, in
 		cudaMemcpy( vel.data(), W->d.vel, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
 		cudaMemcpy( force.data(), W->d.force, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
 		cudaMemcpy( center.data(), W->d.center, sizeof( float2 ) * up, cudaMemcpyDeviceToHost );
+		for ( int b : W->bodyDirty )
+			if ( b < n )
+			{
+				xf[b] = W->xf[b];
+				vel[b] = W->vel[b];
+				force[b] = W->force[b];
+				center[b] = W->center[b];
+			}
 	}
 	for ( int i = 0; i < n; ++i )
 	{

@@ -17,6 +17,8 @@ Scenes:
                       scaled-down parity variants).
 * ``pyramids_chains`` -- side-by-side pyramids plus revolute-joint capsule
                       chains hanging from static anchors.
+* ``joint_gallery`` -- revolute limits, motors, springs, dynamic-dynamic
+                      hinges and collideConnected joints.
 """
 from __future__ import annotations
 
@@ -192,6 +194,53 @@ def pyramids_chains(b, pyramids=64, rows=40, chains=200, links=50, gap=2.0):
         chain(b, left + (c + 0.25) * span, rows + 20.0 + 1.0 * (c % 2), links=links)
 
 
+def joint_gallery(b, copies=4):
+    """Revolute features side by side, ``copies`` times: a pendulum held by
+    an angle limit, a motor-driven wheel against a torque cap with a box
+    resting on it, a spring-loaded arm with a target angle, a two-body
+    hinge between dynamic boxes (limit + motor), and a joint with
+    collideConnected set, over a ground box."""
+    g = b.create_body(body_def(type=STATIC, positionY=-1.0))
+    b.create_box(g, shape_def(), 20.0 * copies, 1.0)
+    for k in range(copies):
+        x0 = -20.0 * copies + 10.0 + 20.0 * k
+        # limited pendulum
+        anchor = b.create_body(body_def(type=STATIC, positionX=x0, positionY=8.0))
+        bob = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 2.0, positionY=8.0))
+        b.create_capsule(bob, shape_def(), -1.0, 0.0, 1.0, 0.0, 0.2)
+        b.create_revolute(revolute_def(bodyA=anchor, bodyB=bob, localAnchorBX=-2.0, enableLimit=1,
+                                       lowerAngle=-0.5 - 0.1 * k, upperAngle=0.25))
+        # motor wheel carrying a box
+        wheel = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 5.0, positionY=1.0))
+        b.create_circle(wheel, shape_def(friction=0.9), 0.0, 0.0, 1.0)
+        hub = b.create_body(body_def(type=STATIC, positionX=x0 + 5.0, positionY=1.0))
+        b.create_revolute(revolute_def(bodyA=hub, bodyB=wheel, enableMotor=1, motorSpeed=2.0 + k,
+                                       maxMotorTorque=50.0))
+        load = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 5.0, positionY=2.6))
+        b.create_box(load, shape_def(), 0.5, 0.5)
+        # spring arm
+        base = b.create_body(body_def(type=STATIC, positionX=x0 + 9.0, positionY=4.0))
+        arm = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 10.0, positionY=4.0))
+        b.create_box(arm, shape_def(), 1.0, 0.1)
+        b.create_revolute(revolute_def(bodyA=base, bodyB=arm, localAnchorBX=-1.0, enableSpring=1,
+                                       hertz=2.0 + k, dampingRatio=0.3, targetAngle=0.4))
+        # dynamic-dynamic hinge with limit and motor, dropping onto the ground
+        p = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 13.0, positionY=3.0))
+        b.create_box(p, shape_def(), 1.0, 0.25)
+        q = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 15.0, positionY=3.0, angularVelocity=1.0))
+        b.create_box(q, shape_def(), 1.0, 0.25)
+        b.create_revolute(revolute_def(bodyA=p, bodyB=q, localAnchorAX=1.0, localAnchorBX=-1.0, enableLimit=1,
+                                       lowerAngle=-1.0, upperAngle=1.0, enableMotor=1, motorSpeed=-1.0,
+                                       maxMotorTorque=5.0, referenceAngle=0.1))
+        # overlapping bodies that keep colliding through their joint
+        r1 = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 17.0, positionY=2.0))
+        b.create_box(r1, shape_def(), 0.5, 0.5)
+        r2 = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 17.6, positionY=2.0))
+        b.create_box(r2, shape_def(), 0.5, 0.5)
+        b.create_revolute(revolute_def(bodyA=r1, bodyB=r2, localAnchorAX=0.3, localAnchorBX=-0.3,
+                                       collideConnected=1))
+
+
 def build(b, name, **kw):
     if name == "pyramid":
         return pyramid(b, **kw)
@@ -199,4 +248,6 @@ def build(b, name, **kw):
         return pile(b, **kw)
     if name == "pyramids_chains":
         return pyramids_chains(b, **kw)
+    if name == "joint_gallery":
+        return joint_gallery(b, **kw)
     raise ValueError(name)

@@ -327,6 +327,7 @@ ShapeProxy p_shape_proxy( const Geometry* g );
 float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sweep sb, float maxFraction, int* state );
 
 // joints (pjoint.c)
+Softness p_make_soft( float hertz, float zeta, float h );
 void p_prepare_joint( World* w, Joint* j, float h, float inv_h, Softness jointSoftness );
 void p_warm_start_joint( World* w, Joint* j );
 void p_solve_joint( World* w, Joint* j, float h, float inv_h, int useBias );

@@ -720,9 +720,9 @@ void p_solve( World* w, float dt, int subStepCount )
 	colorStart[P_OVERFLOW] = nk;
 	Constraint* K = w->constraints;
 
-	// joints
+	// joints in the constraint graph (colours and overflow)
 	for ( int j = 0; j < w->jointCount; ++j )
-		if ( w->joints[j].used )
+		if ( w->joints[j].used && w->joints[j].color != P_NULL )
 			p_prepare_joint( w, w->joints + j, h, inv_h, jointSoftness );
 
 	float maxAngularSpeed = P_MAX_ROTATION * inv_dt;

@@ -480,6 +480,124 @@ int orc_create_polygon_shape( int wi, int body, const f2d_shape_def* d, const do
 }
 
 // ---------------------------------------------------------------------------
+// revolute joints (joint.c:146-330 b2CreateJoint, :~560 b2CreateRevoluteJoint;
+// constraint_graph.c:214-288 b2AssignJointColor / b2CreateJointInGraph)
+// ---------------------------------------------------------------------------
+static int assign_joint_color( World* w, int ia, int ib )
+{
+	Body* a = w->bodies + ia;
+	Body* b = w->bodies + ib;
+	int staticA = a->type == BODY_STATIC;
+	int staticB = b->type == BODY_STATIC;
+	// unlike contacts, joints against a static body may take colour 0
+	for ( int i = 0; i < P_OVERFLOW; ++i )
+	{
+		uint16_t bit = (uint16_t)( 1u << i );
+		if ( ( staticA == 0 && ( a->colorMask & bit ) ) || ( staticB == 0 && ( b->colorMask & bit ) ) )
+			continue;
+		if ( staticA == 0 )
+			a->colorMask |= bit;
+		if ( staticB == 0 )
+			b->colorMask |= bit;
+		return i;
+	}
+	return P_OVERFLOW;
+}
+
+int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || d->bodyA < 0 || d->bodyA >= w->bodyCount || d->bodyB < 0 || d->bodyB >= w->bodyCount )
+		return -1;
+	int cap = w->jointCap;
+	int id = alloc_id( &w->jointFree, &w->jointFreeCount, &w->jointCount );
+	w->joints = grow( w->joints, &cap, w->jointCount, sizeof( Joint ) );
+	w->jointCap = cap;
+	Joint* j = w->joints + id;
+	int gen = j->generation;
+	memset( j, 0, sizeof( *j ) );
+	j->generation = gen + 1;
+	j->used = 1;
+	j->bodyA = d->bodyA;
+	j->bodyB = d->bodyB;
+	j->collideConnected = d->collideConnected != 0;
+	j->color = P_NULL;
+	j->overflowIndex = P_NULL;
+	// doubly linked joint lists on both bodies, new joint at the head
+	Body* a = w->bodies + d->bodyA;
+	Body* b = w->bodies + d->bodyB;
+	j->prevA = P_NULL;
+	j->nextA = a->headJoint;
+	if ( a->headJoint != P_NULL )
+	{
+		Joint* h = w->joints + ( a->headJoint >> 1 );
+		if ( a->headJoint & 1 )
+			h->prevB = id << 1;
+		else
+			h->prevA = id << 1;
+	}
+	a->headJoint = id << 1;
+	a->jointCount += 1;
+	j->prevB = P_NULL;
+	j->nextB = b->headJoint;
+	if ( b->headJoint != P_NULL )
+	{
+		Joint* h = w->joints + ( b->headJoint >> 1 );
+		if ( b->headJoint & 1 )
+			h->prevB = ( id << 1 ) | 1;
+		else
+			h->prevA = ( id << 1 ) | 1;
+	}
+	b->headJoint = ( id << 1 ) | 1;
+	b->jointCount += 1;
+
+	j->type = 1;
+	j->localOriginAnchorA = V( (float)d->localAnchorAX, (float)d->localAnchorAY );
+	j->localOriginAnchorB = V( (float)d->localAnchorBX, (float)d->localAnchorBY );
+	j->referenceAngle = fclampp( (float)d->referenceAngle, -P_PI, P_PI );
+	j->targetAngle = fclampp( (float)d->targetAngle, -P_PI, P_PI );
+	j->hertz = (float)d->hertz;
+	j->dampingRatio = (float)d->dampingRatio;
+	j->lowerAngle = (float)d->lowerAngle;
+	j->upperAngle = (float)d->upperAngle;
+	j->maxMotorTorque = (float)d->maxMotorTorque;
+	j->motorSpeed = (float)d->motorSpeed;
+	j->enableSpring = d->enableSpring != 0;
+	j->enableLimit = d->enableLimit != 0;
+	j->enableMotor = d->enableMotor != 0;
+	j->drawSize = (float)d->drawSize;
+	j->constraintHertz = 60.0f;
+	j->constraintDampingRatio = 2.0f;
+	j->constraintSoftness.biasRate = 0.0f;
+	j->constraintSoftness.massScale = 1.0f;
+	j->constraintSoftness.impulseScale = 0.0f;
+
+	// a joint between two static bodies lives in the static set, outside the
+	// graph; every other joint between enabled bodies is coloured now
+	int staticA = a->type == BODY_STATIC, staticB = b->type == BODY_STATIC;
+	if ( a->enabled && b->enabled && !( staticA && staticB ) )
+	{
+		j->color = assign_joint_color( w, d->bodyA, d->bodyB );
+		if ( j->color == P_OVERFLOW )
+		{
+			w->overflowJoints =
+				grow( w->overflowJoints, &w->overflowJointCap, w->overflowJointCount + 1, sizeof( int ) );
+			j->overflowIndex = w->overflowJointCount;
+			w->overflowJoints[w->overflowJointCount++] = id;
+		}
+	}
+	return id;
+}
+
+int orc_joint_color( int wi, int joint )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || joint < 0 || joint >= w->jointCount )
+		return P_NULL;
+	return w->joints[joint].color;
+}
+
+// ---------------------------------------------------------------------------
 // joint exclusion (body.c:1861-1897 b2ShouldBodiesCollide)
 // ---------------------------------------------------------------------------
 static int should_bodies_collide( World* w, int ia, int ib )

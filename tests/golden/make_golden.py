@@ -29,6 +29,10 @@ CASES = {
     "pile": dict(world=dict(enableSleep=0, enableContinuous=1),
                  scene=("pile", dict(count=300, seed=11, width=30.0, height=40.0)), frames=256,
                  checkpoints=[1, 30, 60, 120, 256]),
+    "chains": dict(world=dict(enableSleep=0), scene=("pyramids_chains", dict(pyramids=2, rows=10, chains=6, links=20)),
+                   frames=256, checkpoints=[1, 64, 256]),
+    "joints": dict(world=dict(enableSleep=0), scene=("joint_gallery", dict()), frames=256,
+                   checkpoints=[1, 64, 256]),
 }
 
 

@@ -17,7 +17,7 @@ import pytest
 from forge2d_gb300 import scenes
 
 from parity import compare_contacts
-from test_oracle_golden import CASES, GOLD, frame_stats, replay
+from test_oracle_golden import CASES, GOLD, STATS_CASES, frame_stats, replay
 
 pytestmark = pytest.mark.gpu
 
@@ -43,6 +43,8 @@ NATIVE = [
      dict(count=600, seed=2, width=24.0, height=60.0), 200, 25),
     ("pile_dense_overflow", dict(enableSleep=0, enableContinuous=1), "pile",
      dict(count=1500, seed=3, width=12.0, height=120.0, wall_height=130.0), 150, 30),
+    ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300, 25),
+    ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400, 25),
 ]
 
 
@@ -129,7 +131,7 @@ def test_gpu_replays_reference_fixture_bit_exact(gpu_lib, name):
     g.close()
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", STATS_CASES)
 def test_gpu_stats_series_parity_mode(gpu_lib, name):
     """256-frame max-penetration and KE series in parity mode: identical to
     the reference's (tolerance 0; the benchmark spec's bound is 1%)."""
@@ -145,7 +147,7 @@ def test_gpu_stats_series_parity_mode(gpu_lib, name):
     g.close()
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", STATS_CASES)
 def test_gpu_stats_series_native_mode(gpu_lib, name):
     """Native contact order (no reference ids): the GPU series equals the
     port's native series bit for bit; against the reference's series the

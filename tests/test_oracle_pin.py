@@ -39,6 +39,8 @@ SCENES = [
     ("pile_no_ccd", dict(enableSleep=0, enableContinuous=0), "pile",
      dict(count=400, seed=7, width=20.0, height=30.0), 120),
     ("pyramid_small", dict(enableSleep=0), "pyramid", dict(rows=12), 200),
+    ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300),
+    ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400),
 ]
 
 
