@@ -436,3 +436,171 @@ extern "C" F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lx, d
 	}
 	return n;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free AABB overlap. The scratch is one file-scope device array:
+// per-block hit counts, their exclusive scan and the compacted shape ids.
+// Three launches make the result order ascending by construction (count per
+// block, scan the counts, write each hit at its block's base plus its rank in
+// the block), so no sort and no host buffer is needed.
+// ---------------------------------------------------------------------------
+#define OVERLAP_BLOCK 256
+#define OVERLAP_NOALLOC_BLOCKS ( F2D_OVERLAP_NOALLOC_MAX_SHAPES / OVERLAP_BLOCK )
+#define NOALLOC_MAX_DEVICES 64
+
+static_assert( OVERLAP_NOALLOC_BLOCKS <= 1024, "the scan kernel runs one 1024-thread block" );
+
+struct OverlapScratch
+{
+	int total;
+	int pad[63];
+	int blockBase[OVERLAP_NOALLOC_BLOCKS];
+	int ids[F2D_OVERLAP_NOALLOC_MAX_SHAPES];
+};
+
+static __device__ __align__( 256 ) OverlapScratch g_overlapScratch;
+
+// device address of g_overlapScratch per device ordinal, resolved on first use
+static OverlapScratch* s_overlapScratch[NOALLOC_MAX_DEVICES];
+
+static OverlapScratch* overlap_scratch()
+{
+	int dev = 0;
+	if ( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES )
+		return nullptr;
+	if ( s_overlapScratch[dev] == nullptr )
+	{
+		void* p = nullptr;
+		if ( cudaGetSymbolAddress( &p, g_overlapScratch ) != cudaSuccess )
+			return nullptr;
+		s_overlapScratch[dev] = (OverlapScratch*)p;
+	}
+	return s_overlapScratch[dev];
+}
+
+__device__ __forceinline__ bool overlap_hit( const DWorld& w, int s, fbox box, unsigned long long cat,
+											 unsigned long long msk )
+{
+	if ( s >= w.shapeCount )
+		return false;
+	int f = w.sflags[s];
+	if ( ( f & ( SF_USED | SF_PROXY ) ) != ( SF_USED | SF_PROXY ) )
+		return false;
+	if ( !query_collide( w, s, cat, msk ) )
+		return false;
+	return box_overlaps( box_from4( w.fat[s] ), box );
+}
+
+__global__ void __launch_bounds__( OVERLAP_BLOCK ) k_overlap_count( DWorld w, fbox box, unsigned long long cat,
+																	 unsigned long long msk, OverlapScratch* scr )
+{
+	int s = blockIdx.x * OVERLAP_BLOCK + threadIdx.x;
+	int c = __syncthreads_count( overlap_hit( w, s, box, cat, msk ) );
+	if ( threadIdx.x == 0 )
+		scr->blockBase[blockIdx.x] = c;
+}
+
+// exclusive scan of the per-block counts; one block of 1024 threads
+__global__ void __launch_bounds__( 1024 ) k_overlap_scan( OverlapScratch* scr, int blocks )
+{
+	__shared__ int warpSum[32];
+	int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+	int v = t < blocks ? scr->blockBase[t] : 0;
+	int x = v;
+	for ( int o = 1; o < 32; o <<= 1 )
+	{
+		int y = __shfl_up_sync( 0xffffffffu, x, o );
+		if ( lane >= o )
+			x += y;
+	}
+	if ( lane == 31 )
+		warpSum[wid] = x;
+	__syncthreads();
+	if ( wid == 0 )
+	{
+		int ws = warpSum[lane];
+		for ( int o = 1; o < 32; o <<= 1 )
+		{
+			int y = __shfl_up_sync( 0xffffffffu, ws, o );
+			if ( lane >= o )
+				ws += y;
+		}
+		warpSum[lane] = ws;
+	}
+	__syncthreads();
+	int inclusive = x + ( wid > 0 ? warpSum[wid - 1] : 0 );
+	if ( t < blocks )
+		scr->blockBase[t] = inclusive - v;
+	if ( t == 1023 )
+		scr->total = inclusive;
+}
+
+__global__ void __launch_bounds__( OVERLAP_BLOCK ) k_overlap_write( DWorld w, fbox box, unsigned long long cat,
+																	 unsigned long long msk, OverlapScratch* scr )
+{
+	__shared__ int warpBase[OVERLAP_BLOCK / 32];
+	int s = blockIdx.x * OVERLAP_BLOCK + threadIdx.x;
+	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	bool hit = overlap_hit( w, s, box, cat, msk );
+	unsigned ballot = __ballot_sync( 0xffffffffu, hit );
+	if ( lane == 0 )
+		warpBase[wid] = __popc( ballot );
+	__syncthreads();
+	if ( threadIdx.x == 0 )
+	{
+		int acc = 0;
+		for ( int k = 0; k < OVERLAP_BLOCK / 32; ++k )
+		{
+			int c = warpBase[k];
+			warpBase[k] = acc;
+			acc += c;
+		}
+	}
+	__syncthreads();
+	if ( hit )
+		scr->ids[scr->blockBase[blockIdx.x] + warpBase[wid] + __popc( ballot & ( ( 1u << lane ) - 1u ) )] = s;
+}
+
+DWorld* f2d_internal_world_noalloc( int32_t worldId, cudaStream_t* st, int maxShapes, int* code );
+
+extern "C" F2D_API int32_t f2d_world_overlap_aabb_noalloc( int32_t worldId, double lx, double ly, double ux,
+														   double uy, int64_t categoryBits, int64_t maskBits,
+														   int32_t* shapes2, int32_t capacity )
+{
+	cudaStream_t st;
+	int code = 0;
+	DWorld* w = f2d_internal_world_noalloc( worldId, &st, F2D_OVERLAP_NOALLOC_MAX_SHAPES, &code );
+	if ( w == nullptr )
+		return code;
+	OverlapScratch* scr = overlap_scratch();
+	if ( scr == nullptr )
+		return F2D_NOALLOC_DEVICE_SETUP;
+	int shapeCount = w->shapeCount;
+	if ( shapeCount == 0 )
+		return 0;
+	int blocks = ( shapeCount + OVERLAP_BLOCK - 1 ) / OVERLAP_BLOCK;
+	fbox box;
+	box.lo = mk( (float)lx, (float)ly );
+	box.hi = mk( (float)ux, (float)uy );
+	unsigned long long cat = (unsigned long long)categoryBits, msk = (unsigned long long)maskBits;
+	k_overlap_count<<<blocks, OVERLAP_BLOCK, 0, st>>>( *w, box, cat, msk, scr );
+	k_overlap_scan<<<1, 1024, 0, st>>>( scr, blocks );
+	k_overlap_write<<<blocks, OVERLAP_BLOCK, 0, st>>>( *w, box, cat, msk, scr );
+	int n = 0;
+	cudaMemcpyAsync( &n, &scr->total, sizeof( int ), cudaMemcpyDeviceToHost, st );
+	cudaStreamSynchronize( st );
+	int m = n < capacity ? n : capacity;
+	if ( m <= 0 || shapes2 == nullptr )
+		return n;
+	cudaMemcpyAsync( shapes2, scr->ids, sizeof( int ) * (size_t)m, cudaMemcpyDeviceToHost, st );
+	cudaStreamSynchronize( st );
+	// widen shape indices to (index1, worldAndGeneration) pairs in place, back to front
+	int world0 = f2d_internal_world0( worldId );
+	for ( int i = m - 1; i >= 0; --i )
+	{
+		int s = shapes2[i];
+		shapes2[2 * i + 1] = world0 | ( (int)f2d_internal_shape_gen( worldId, s ) << 16 );
+		shapes2[2 * i] = s + 1;
+	}
+	return n;
+}

@@ -1982,6 +1982,33 @@ DWorld* f2d_internal_world( int32_t worldId, cudaStream_t* st, int* gens, int ge
 	return &W->d;
 }
 
+// For the allocation-free queries: the world's device rows after pending
+// uploads, or nullptr with *code set when serving them would need an
+// allocation (capacities exceeded since the last step) or the world has more
+// shapes than the caller's scratch holds. Uploads themselves only copy.
+DWorld* f2d_internal_world_noalloc( int32_t worldId, cudaStream_t* st, int maxShapes, int* code )
+{
+	*code = 0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return nullptr;
+	if ( W->shapeCount > maxShapes )
+	{
+		*code = F2D_NOALLOC_TOO_MANY_SHAPES;
+		return nullptr;
+	}
+	const DWorld& d = W->d;
+	if ( W->bodyCount > d.bodyCap || W->shapeCount > d.shapeCap || W->jointCount > d.jointCap )
+	{
+		*code = F2D_NOALLOC_NEEDS_GROWTH;
+		return nullptr;
+	}
+	flush_uploads( W );
+	cudaStreamSynchronize( W->stream );
+	*st = W->stream;
+	return &W->d;
+}
+
 uint16_t f2d_internal_shape_gen( int32_t worldId, int shape )
 {
 	HostWorld* W = world_from_id( worldId );

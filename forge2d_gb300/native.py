@@ -122,6 +122,7 @@ _SIGS = [
     ("f2d_world_get_body_events", _i, [_i, _P(_i), _P(_f), _i]),
     ("f2d_world_cast_ray_closest", _i, [_i, _d, _d, _d, _d, _i64, _i64, _P(_i), _P(_f)]),
     ("f2d_world_overlap_aabb", _i, [_i, _d, _d, _d, _d, _i64, _i64, _P(_i), _i]),
+    ("f2d_world_overlap_aabb_noalloc", _i, [_i, _d, _d, _d, _d, _i64, _i64, _P(_i), _i]),
     ("f2d_world_body_capacity", _i, [_i]),
     ("f2d_world_get_bodies", _i, [_i, _P(_f), _i]),
     ("f2d_world_contact_capacity", _i, [_i]),

@@ -233,6 +233,13 @@ class GpuWorld:
         n = self.lib.f2d_world_overlap_aabb(self.id, lx, ly, ux, uy, cat, mask, _iptr(out), cap)
         return out[:min(n, cap), 0] - 1
 
+    def overlap_aabb_noalloc(self, lx, ly, ux, uy, cat=1, mask=-1, capacity=1 << 16):
+        """f2d_world_overlap_aabb_noalloc: returns (count or negative code,
+        the written (index1, worldAndGeneration) rows)."""
+        out = np.zeros((max(capacity, 1), 2), np.int32)
+        n = self.lib.f2d_world_overlap_aabb_noalloc(self.id, lx, ly, ux, uy, cat, mask, _iptr(out), capacity)
+        return n, out[:max(0, min(n, capacity))]
+
 
 # ---------------------------------------------------------------------------
 # forge2d-style object API

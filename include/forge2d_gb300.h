@@ -264,6 +264,29 @@ F2D_API int32_t f2d_world_cast_ray_closest( int32_t worldId, double originX, dou
 F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lowerX, double lowerY, double upperX, double upperY,
 										int64_t categoryBits, int64_t maskBits, int32_t* shapes2, int32_t capacity );
 
+/* Allocation-free variant of f2d_world_overlap_aabb. It has no reference
+ * counterpart: Box2D's b2World_OverlapAABB walks its trees on the CPU and
+ * needs no scratch. Same arguments, result order (ascending shape id) and
+ * return value as f2d_world_overlap_aabb, but the device scratch is a
+ * file-scope __device__ array sized for F2D_OVERLAP_NOALLOC_MAX_SHAPES
+ * shapes, and the call makes no cudaMalloc / cudaFree or any other device or
+ * host allocation. The first call on each device resolves that array's
+ * address with cudaGetSymbolAddress and caches it; make that first call
+ * before capturing any stream. Calls that overlap in time on one device
+ * share the array and race; serialise them.
+ * Returns F2D_NOALLOC_TOO_MANY_SHAPES when the world holds more shapes than
+ * the array can take, F2D_NOALLOC_NEEDS_GROWTH when bodies or shapes were
+ * created past the world's device capacities since the last step (step the
+ * world or call f2d_world_reserve first), F2D_NOALLOC_DEVICE_SETUP when the
+ * array's address cannot be resolved. No output is written in those cases. */
+#define F2D_OVERLAP_NOALLOC_MAX_SHAPES 262144
+#define F2D_NOALLOC_TOO_MANY_SHAPES ( -1 )
+#define F2D_NOALLOC_NEEDS_GROWTH ( -2 )
+#define F2D_NOALLOC_DEVICE_SETUP ( -3 )
+F2D_API int32_t f2d_world_overlap_aabb_noalloc( int32_t worldId, double lowerX, double lowerY, double upperX,
+												double upperY, int64_t categoryBits, int64_t maskBits,
+												int32_t* shapes2, int32_t capacity );
+
 /* ---- bulk state access (for batch readers and parity checks) ------------ */
 /* Per body id, 12 floats: p.xy q.cs v.xy w centre.xy valid type sleepTime. */
 F2D_API int32_t f2d_world_body_capacity( int32_t worldId );
