@@ -13,6 +13,7 @@
 //   3. new pairs are sorted by their 64-bit shape-pair key, the order in
 //      which contact ids are then drawn from the LIFO id pool.
 #include "dscan.cuh"
+#include "dsort.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
 
@@ -400,7 +401,6 @@ __global__ void k_find_pairs( DWorld w )
 							{
 								int lo = si < sj ? si : sj, hi = si < sj ? sj : si;
 								w.pairKeys[slot] = ( (unsigned long long)lo << w.pairKeyBits ) | (unsigned)hi;
-								w.pairVal[slot] = slot;
 							}
 							else
 								atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
@@ -575,20 +575,22 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, st>>>( w );
 	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, st>>>( w );
 	k_leaf_flags<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA );
-	scan_exclusive( s.tmpA, s.tmpB, s.scanTmp, nullptr, w.shapeCount, w.shapeCap, &w.sc->treeLeafCount, st );
+	scan_lookback( s.tmpA, s.tmpB, nullptr, w.shapeCount, w.shapeCap, &w.sc->treeLeafCount, s.scanState, &w.sc->error,
+				   st );
 	k_leaf_compact<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA, s.tmpB );
 	k_bounds_partial<<<s.boundsBlocks, BP_THREADS, 0, st>>>( w, s.bounds );
 	k_bounds_final<<<1, BP_THREADS, 0, st>>>( s.bounds, s.boundsBlocks );
 	k_morton<<<gridS, BP_THREADS, 0, st>>>( w, s.bounds );
-	radix_sort<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount,
-						  w.shapeCap, 30, w.sortHist, s.scanTmp, st );
+	sort_coop<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount, 30,
+						 w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks32, st );
 	k_build_tree<<<gridS, BP_THREADS, 0, st>>>( w );
 	k_tree_boxes<<<gridS, BP_THREADS, 0, st>>>( w );
 	k_find_pairs<<<gridS, BP_THREADS, 0, st>>>( w );
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );
 	int bits = 2 * w.pairKeyBits;
-	radix_sort<unsigned long long>( w.pairKeys, w.pairVal, w.pairKeysAlt, w.pairValAlt, &w.sc->newPairCount,
-									w.pairCap, bits, w.sortHist, s.scanTmp, st );
+	// new pair keys are unique, so the key order alone fixes the result
+	sort_coop<unsigned long long>( w.pairKeys, nullptr, w.pairKeysAlt, nullptr, &w.sc->newPairCount, bits, w.sortHist,
+								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
 	k_create_contacts<<<grid_for( w.pairCap ), BP_THREADS, 0, st>>>( w, planMode );
 	k_after_create<<<gridS, BP_THREADS, 0, st>>>( w, planMode );
 }

@@ -26,6 +26,8 @@ struct StepScratch
 	int* tmpA;	  // >= max(shapeCap, contactCap, bodyCap) ints
 	int* tmpB;
 	int* scanTmp; // scan tile sums
+	unsigned long long* scanState; // look-back scan tile states
+	int sortBlocks32, sortBlocks64; // co-resident grids of the one-launch sorts
 	float4* bounds;
 	int boundsBlocks;
 	int shapeIdBits;

@@ -7,6 +7,7 @@
 // (world.c:586-686).
 #include "dnarrow.cuh"
 #include "dscan.cuh"
+#include "dsort.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
 
@@ -182,7 +183,8 @@ void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st )
 		g = F2D_SMS * 16;
 	k_narrowphase<<<g, NP_THREADS, 0, st>>>( w );
 	k_op_flags<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA );
-	scan_exclusive( s.tmpA, s.tmpB, s.scanTmp, &w.sc->contactIdCount, 0, w.contactCap, &w.sc->opCount, st );
+	scan_lookback( s.tmpA, s.tmpB, &w.sc->contactIdCount, 0, w.contactCap, &w.sc->opCount, s.scanState, &w.sc->error,
+				   st );
 	k_op_compact<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA, s.tmpB );
 	k_op_clamp<<<1, 1, 0, st>>>( w );
 }

@@ -17,12 +17,12 @@
 // functions (contact_solver.c:24-510). Built with -fmad=false the results
 // are bit-identical to the reference C code.
 #include "dscan.cuh"
+#include "dsync.cuh"
 #include "dworld.cuh"
 #include "joint.cuh"
 #include "kernels.cuh"
 
-#define SOLVER_THREADS 256
-#define BARRIER_SPIN_LIMIT ( 1ll << 25 )
+#define SOLVER_THREADS 512
 
 struct SolveParams
 {
@@ -612,44 +612,6 @@ static __device__ void restitution_overflow( const DWorld& w, int k, float thres
 	store_vel( w, idx.y, B );
 }
 
-// ---------------------------------------------------------------------------
-// bounded grid barrier (co-residency guaranteed by the cooperative launch)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ bool grid_barrier( DScalars* sc )
-{
-	__syncthreads();
-	if ( threadIdx.x == 0 )
-	{
-		volatile unsigned* genp = &sc->barrierGen;
-		volatile int* errp = &sc->error;
-		unsigned gen = *genp;
-		__threadfence();
-		unsigned arrived = atomicAdd( &sc->barrierCount, 1u );
-		if ( arrived == gridDim.x - 1 )
-		{
-			sc->barrierCount = 0;
-			__threadfence();
-			atomicAdd( &sc->barrierGen, 1u );
-		}
-		else
-		{
-			long long spins = 0;
-			while ( *genp == gen )
-			{
-				if ( ( *errp & ERR_BARRIER_TIMEOUT ) || ++spins > BARRIER_SPIN_LIMIT )
-				{
-					atomicOr( &sc->error, ERR_BARRIER_TIMEOUT );
-					break;
-				}
-				__nanosleep( 32 );
-			}
-		}
-		__threadfence();
-	}
-	__syncthreads();
-	return ( *(volatile int*)&sc->error & ERR_BARRIER_TIMEOUT ) == 0;
-}
-
 __device__ __forceinline__ void integrate_velocity( const DWorld& w, int b, const SolveParams& p )
 {
 	float4 v4 = w.vel[b];
@@ -735,6 +697,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 {
 	int gtid = blockIdx.x * blockDim.x + threadIdx.x;
 	int gstride = gridDim.x * blockDim.x;
+	unsigned epoch = 0;
 	int nb = w.bodyCount;
 	int novf = w.sc->overflowCount;
 	int novfJ = w.sc->overflowJointCount;
@@ -751,7 +714,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 		for ( int b = gtid; b < nb; b += gstride )
 			if ( body_awake( w.bflags[b] ) )
 				integrate_velocity( w, b, p );
-		if ( !grid_barrier( w.sc ) )
+		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 		for ( int kind = 0; kind < 3; ++kind )
 		{
@@ -771,7 +734,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 					fv2 dp = vmuladd( mk( d.x, d.y ), p.h, mk( v.x, v.y ) );
 					__stcg( w.delta + b, make_float4( dp.x, dp.y, dq.c, dq.s ) );
 				}
-				if ( !grid_barrier( w.sc ) )
+				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
 			if ( serialStage )
@@ -794,7 +757,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 							solve_overflow( w, k, p.inv_h, p.pushout, kind == 1 );
 					}
 				}
-				if ( !grid_barrier( w.sc ) )
+				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
 			for ( int a = 0; a < nActive; ++a )
@@ -802,7 +765,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 				int c = active[a];
 				joint_colour_stage( w, c, kind, p, gtid, gstride, jointSlots, jointStart );
 				colour_stage( w, c, kind, p, gtid, gstride );
-				if ( !grid_barrier( w.sc ) )
+				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
 		}
@@ -813,7 +776,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 		if ( gtid == 0 )
 			for ( int k = 0; k < novf; ++k )
 				restitution_overflow( w, k, p.restitutionThreshold );
-		if ( !grid_barrier( w.sc ) )
+		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
 	for ( int a = 0; a < nActive; ++a )
@@ -822,7 +785,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 		if ( w.sc->colorCount[c] == 0 )
 			continue;
 		colour_stage( w, c, 3, p, gtid, gstride );
-		if ( !grid_barrier( w.sc ) )
+		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
 	// store impulses (contact_solver.c:480-509, :2078-2120)
@@ -848,19 +811,21 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
+// One block of SOLVER_THREADS per SM: every block is co-resident (the
+// cooperative launch checks it) and a grid barrier waits for one arrival per
+// SM.
 int solver_max_blocks( int threads )
 {
+	(void)threads;
 	int perSM = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_solve, threads, 0 );
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_solve, SOLVER_THREADS, 0 );
 	int dev = 0;
 	cudaGetDevice( &dev );
 	int sms = 0;
 	cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
 	if ( perSM < 1 )
-		perSM = 1;
-	if ( perSM > 2 )
-		perSM = 2;
-	return perSM * sms;
+		return 0;
+	return sms;
 }
 
 void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps )
@@ -896,6 +861,7 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 	int* jointSlots = s.tmpB;
 	int* jointStart = s.tmpB + w.jointCap;
 	void* args[] = { &w, &p, &jointSlots, &jointStart };
+	cudaMemsetAsync( &w.sc->barrierCount, 0, sizeof( unsigned ), st );
 	if ( s.evSolveStart )
 		cudaEventRecord( s.evSolveStart, st );
 	cudaLaunchCooperativeKernel( (void*)k_solve, dim3( s.solverBlocks ), dim3( SOLVER_THREADS ), args, 0, st );

@@ -10,6 +10,7 @@
 // and step parameters stay the same.
 #include "../../include/forge2d_gb300.h"
 #include "dscan.cuh"
+#include "dsort.cuh"
 #include "dworld.cuh"
 #include "hgeom.h"
 #include "kernels.cuh"
@@ -145,7 +146,11 @@ static void alloc_scratch( HostWorld* W )
 	int scanN = std::max( 256 * sortBlocks, m );
 	dgrow( s.scanTmp, 0, (size_t)( scanN + SCAN_TILE - 1 ) / SCAN_TILE + 64 );
 	dfree( d.sortHist );
-	dgrow( d.sortHist, 0, (size_t)256 * sortBlocks + 256 );
+	dgrow( d.sortHist, 0, std::max( (size_t)256 * sortBlocks + 256, (size_t)256 * CSORT_MAX_BLOCKS + 256 ) );
+	dfree( s.scanState );
+	dgrow( s.scanState, 0, (size_t)( m + LB_TILE - 1 ) / LB_TILE + 8 );
+	s.sortBlocks32 = sort_coop_blocks<unsigned>();
+	s.sortBlocks64 = sort_coop_blocks<unsigned long long>();
 	s.boundsBlocks = 64;
 	dgrow( s.bounds, 0, (size_t)s.boundsBlocks );
 	int bits = 1;
@@ -153,8 +158,8 @@ static void alloc_scratch( HostWorld* W )
 		bits += 1;
 	s.shapeIdBits = bits;
 	d.pairKeyBits = bits;
-	s.solverThreads = 256;
-	s.solverBlocks = solver_max_blocks( 256 );
+	s.solverThreads = 512;
+	s.solverBlocks = solver_max_blocks( 512 );
 }
 
 static void grow_bodies( HostWorld* W, int cap )
@@ -617,6 +622,7 @@ static void free_world( HostWorld* W )
 	dfree( W->s.tmpA );
 	dfree( W->s.tmpB );
 	dfree( W->s.scanTmp );
+	dfree( W->s.scanState );
 	dfree( W->s.bounds );
 	cudaFreeHost( W->hostError );
 	cudaEventDestroy( W->evStart );
