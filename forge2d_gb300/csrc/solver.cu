@@ -237,23 +237,56 @@ __device__ __forceinline__ float lmin( float a, float b )
 	return a < b ? a : b;
 }
 
-// contact_solver.c:1671-1727
-static __device__ void warm_lane( const DWorld& w, int k )
+// A graph-colour constraint held in registers for the whole solver launch:
+// its static rows are read once, its impulses accumulate in place and are
+// written back once (see k_solve).
+struct Lane
 {
-	int2 idx = w.kIndex[k];
-	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
-	float4 ms = w.kMass[k];
-	float4 nm = w.kNormal[k];
-	float4 imp = __ldcg( w.kImp + k );
-	float4 misc = __ldcg( w.kMisc + k );
+	int2 idx;
+	float4 ms;	 // invMassA invIA invMassB invIB
+	float4 nm;	 // normal.xy friction tangentSpeed
+	float4 sf;	 // biasRate massScale impulseScale pointCount
+	float4 misc; // restitution rollingResistance rollingMass rollingImpulse
+	float4 imp;	 // normalImpulse1 normalImpulse2 tangentImpulse1 tangentImpulse2
+	float2 tot;	 // totalNormalImpulse1 totalNormalImpulse2
+	float4 an[2];
+	float4 pt[2];
+};
+
+__device__ __forceinline__ void lane_load( const DWorld& w, int k, Lane& L )
+{
+	L.idx = w.kIndex[k];
+	L.ms = w.kMass[k];
+	L.nm = w.kNormal[k];
+	L.sf = w.kSoft[k];
+	L.misc = __ldcg( w.kMisc + k );
+	L.imp = __ldcg( w.kImp + k );
+	L.tot = __ldcg( w.kTot + k );
+	L.an[0] = w.kAnch1[k];
+	L.an[1] = w.kAnch2[k];
+	L.pt[0] = w.kP1[k];
+	L.pt[1] = w.kP2[k];
+}
+
+__device__ __forceinline__ void lane_store( const DWorld& w, int k, const Lane& L )
+{
+	__stcg( w.kImp + k, L.imp );
+	__stcg( w.kTot + k, L.tot );
+	__stcg( w.kMisc + k, L.misc );
+}
+
+// contact_solver.c:1671-1727
+__device__ __forceinline__ void lane_warm( const DWorld& w, const Lane& L )
+{
+	BState A = load_state( w, L.idx.x ), B = load_state( w, L.idx.y );
+	const float4 ms = L.ms, nm = L.nm;
 	float tx = nm.y;
 	float ty = 0.0f - nm.x;
-	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
-	float nis[2] = { imp.x, imp.y };
-	float tis[2] = { imp.z, imp.w };
+	float nis[2] = { L.imp.x, L.imp.y };
+	float tis[2] = { L.imp.z, L.imp.w };
 	for ( int j = 0; j < 2; ++j )
 	{
-		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float rAx = L.an[j].x, rAy = L.an[j].y, rBx = L.an[j].z, rBy = L.an[j].w;
 		float Px = nis[j] * nm.x + tis[j] * tx;
 		float Py = nis[j] * nm.y + tis[j] * ty;
 		A.w = A.w - ms.y * ( rAx * Py - rAy * Px );
@@ -263,23 +296,18 @@ static __device__ void warm_lane( const DWorld& w, int k )
 		B.vx = B.vx + ms.z * Px;
 		B.vy = B.vy + ms.z * Py;
 	}
-	A.w = A.w - ms.y * misc.w;
-	B.w = B.w + ms.w * misc.w;
-	store_vel( w, idx.x, A );
-	store_vel( w, idx.y, B );
+	A.w = A.w - ms.y * L.misc.w;
+	B.w = B.w + ms.w * L.misc.w;
+	store_vel( w, L.idx.x, A );
+	store_vel( w, L.idx.y, B );
 }
 
 // contact_solver.c:1729-1967
-static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float minBiasVel, bool useBias )
+__device__ __forceinline__ void lane_solve( const DWorld& w, Lane& L, float inv_h, float minBiasVel, bool useBias )
 {
-	int2 idx = w.kIndex[k];
-	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
-	float4 ms = w.kMass[k];
-	float4 nm = w.kNormal[k];
-	float4 sf = w.kSoft[k];
-	float4 misc = __ldcg( w.kMisc + k );
-	float4 imp = __ldcg( w.kImp + k );
-	float2 tot = __ldcg( w.kTot + k );
+	BState A = load_state( w, L.idx.x ), B = load_state( w, L.idx.y );
+	const float4 ms = L.ms, nm = L.nm, sf = L.sf;
+	float4 misc = L.misc;
 	float biasRate, massScale, impulseScale;
 	if ( useBias )
 	{
@@ -296,21 +324,19 @@ static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float mi
 	float totalNormalImpulse = 0.0f;
 	float dpx = B.dpx - A.dpx;
 	float dpy = B.dpy - A.dpy;
-	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
-	float4 pt[2] = { w.kP1[k], w.kP2[k] };
-	float nis[2] = { imp.x, imp.y };
-	float tis[2] = { imp.z, imp.w };
-	float tots[2] = { tot.x, tot.y };
+	float nis[2] = { L.imp.x, L.imp.y };
+	float tis[2] = { L.imp.z, L.imp.w };
+	float tots[2] = { L.tot.x, L.tot.y };
 	for ( int j = 0; j < 2; ++j )
 	{
-		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float rAx = L.an[j].x, rAy = L.an[j].y, rBx = L.an[j].z, rBy = L.an[j].w;
 		float rsAx = A.dqc * rAx - A.dqs * rAy;
 		float rsAy = A.dqs * rAx + A.dqc * rAy;
 		float rsBx = B.dqc * rBx - B.dqs * rBy;
 		float rsBy = B.dqs * rBx + B.dqc * rBy;
 		float dsx = dpx + ( rsBx - rsAx );
 		float dsy = dpy + ( rsBy - rsAy );
-		float s = ( nm.x * dsx + nm.y * dsy ) + pt[j].x;
+		float s = ( nm.x * dsx + nm.y * dsy ) + L.pt[j].x;
 		bool mask = s > 0.0f;
 		float specBias = s * inv_h;
 		float softBias = lmax( biasRate * s, minBiasVel );
@@ -320,7 +346,7 @@ static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float mi
 		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
 		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
 		float vn = dvx * nm.x + dvy * nm.y;
-		float negImpulse = pt[j].y * ( pointMassScale * ( vn + bias ) ) + pointImpulseScale * nis[j];
+		float negImpulse = L.pt[j].y * ( pointMassScale * ( vn + bias ) ) + pointImpulseScale * nis[j];
 		float newImpulse = lmax( nis[j] - negImpulse, 0.0f );
 		float impulse = newImpulse - nis[j];
 		nis[j] = newImpulse;
@@ -339,12 +365,12 @@ static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float mi
 	float ty = 0.0f - nm.x;
 	for ( int j = 0; j < 2; ++j )
 	{
-		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float rAx = L.an[j].x, rAy = L.an[j].y, rBx = L.an[j].z, rBy = L.an[j].w;
 		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
 		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
 		float vt = dvx * tx + dvy * ty;
 		vt = vt - nm.w;
-		float negImpulse = pt[j].z * vt;
+		float negImpulse = L.pt[j].z * vt;
 		float maxFriction = nm.z * nis[j];
 		float newImpulse = tis[j] - negImpulse;
 		newImpulse = lmax( 0.0f - maxFriction, lmin( newImpulse, maxFriction ) );
@@ -370,40 +396,33 @@ static __device__ void solve_lane( const DWorld& w, int k, float inv_h, float mi
 		A.w = A.w - ms.y * deltaLambda;
 		B.w = B.w + ms.w * deltaLambda;
 	}
-	__stcg( w.kImp + k, make_float4( nis[0], nis[1], tis[0], tis[1] ) );
-	__stcg( w.kTot + k, make_float2( tots[0], tots[1] ) );
-	__stcg( w.kMisc + k, misc );
-	store_vel( w, idx.x, A );
-	store_vel( w, idx.y, B );
+	L.imp = make_float4( nis[0], nis[1], tis[0], tis[1] );
+	L.tot = make_float2( tots[0], tots[1] );
+	L.misc = misc;
+	store_vel( w, L.idx.x, A );
+	store_vel( w, L.idx.y, B );
 }
 
 // contact_solver.c:1969-2076 (lanes with restitution 0 are unchanged)
-static __device__ void restitution_lane( const DWorld& w, int k, float threshold )
+__device__ __forceinline__ void lane_restitution( const DWorld& w, Lane& L, float threshold )
 {
-	float4 misc = __ldcg( w.kMisc + k );
-	float restitution = misc.x;
+	float restitution = L.misc.x;
 	if ( restitution == 0.0f )
 		return;
-	int2 idx = w.kIndex[k];
-	BState A = load_state( w, idx.x ), B = load_state( w, idx.y );
-	float4 ms = w.kMass[k];
-	float4 nm = w.kNormal[k];
-	float4 imp = __ldcg( w.kImp + k );
-	float2 tot = __ldcg( w.kTot + k );
-	float4 an[2] = { w.kAnch1[k], w.kAnch2[k] };
-	float4 pt[2] = { w.kP1[k], w.kP2[k] };
-	float nis[2] = { imp.x, imp.y };
-	float tots[2] = { tot.x, tot.y };
+	BState A = load_state( w, L.idx.x ), B = load_state( w, L.idx.y );
+	const float4 ms = L.ms, nm = L.nm;
+	float nis[2] = { L.imp.x, L.imp.y };
+	float tots[2] = { L.tot.x, L.tot.y };
 	for ( int j = 0; j < 2; ++j )
 	{
-		bool mask1 = ( pt[j].w + threshold ) > 0.0f;
+		bool mask1 = ( L.pt[j].w + threshold ) > 0.0f;
 		bool mask2 = tots[j] == 0.0f;
-		float mass = ( mask1 || mask2 ) ? 0.0f : pt[j].y;
-		float rAx = an[j].x, rAy = an[j].y, rBx = an[j].z, rBy = an[j].w;
+		float mass = ( mask1 || mask2 ) ? 0.0f : L.pt[j].y;
+		float rAx = L.an[j].x, rAy = L.an[j].y, rBx = L.an[j].z, rBy = L.an[j].w;
 		float dvx = ( B.vx - B.w * rBy ) - ( A.vx - A.w * rAy );
 		float dvy = ( B.vy + B.w * rBx ) - ( A.vy + A.w * rAx );
 		float vn = dvx * nm.x + dvy * nm.y;
-		float negImpulse = mass * ( vn + restitution * pt[j].w );
+		float negImpulse = mass * ( vn + restitution * L.pt[j].w );
 		float newImpulse = lmax( nis[j] - negImpulse, 0.0f );
 		float impulse = newImpulse - nis[j];
 		nis[j] = newImpulse;
@@ -416,9 +435,10 @@ static __device__ void restitution_lane( const DWorld& w, int k, float threshold
 		B.vy = B.vy + ms.z * Py;
 		B.w = B.w + ms.w * ( rBx * Py - rBy * Px );
 	}
-	__stcg( w.kImp + k, make_float4( nis[0], nis[1], imp.z, imp.w ) );
-	store_vel( w, idx.x, A );
-	store_vel( w, idx.y, B );
+	L.imp.x = nis[0];
+	L.imp.y = nis[1];
+	store_vel( w, L.idx.x, A );
+	store_vel( w, L.idx.y, B );
 }
 
 // contact_solver.c:160-225
@@ -654,32 +674,23 @@ __device__ __forceinline__ bool body_awake( int f )
 	return ( f & ( BF_USED | BF_ENABLED ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
 }
 
-// One colour stage: joints of colour c then contacts of colour c, spread over
-// the grid. kind 0 warm start, 1 solve (bias), 2 relax, 3 restitution.
-__device__ __forceinline__ void colour_stage( const DWorld& w, int c, int kind, const SolveParams& p, int gtid,
-											  int gstride )
+__device__ __forceinline__ void lane_op( const DWorld& w, Lane& L, int kind, const SolveParams& p )
 {
-	int start = w.sc->colorStart[c];
-	int count = w.sc->colorCount[c];
-	for ( int k = gtid; k < count; k += gstride )
-	{
-		int slot = start + k;
-		if ( kind == 0 )
-			warm_lane( w, slot );
-		else if ( kind == 1 )
-			solve_lane( w, slot, p.inv_h, p.minBiasVel, true );
-		else if ( kind == 2 )
-			solve_lane( w, slot, p.inv_h, p.minBiasVel, false );
-		else
-			restitution_lane( w, slot, p.restitutionThreshold );
-	}
+	if ( kind == 0 )
+		lane_warm( w, L );
+	else if ( kind == 1 )
+		lane_solve( w, L, p.inv_h, p.minBiasVel, true );
+	else if ( kind == 2 )
+		lane_solve( w, L, p.inv_h, p.minBiasVel, false );
+	else
+		lane_restitution( w, L, p.restitutionThreshold );
 }
 
 __device__ __forceinline__ void joint_colour_stage( const DWorld& w, int c, int kind, const SolveParams& p, int gtid,
-													int gstride, const int* jointSlots, const int* jointStart )
+													int gstride, const int* jointSlots, const int* sJStart )
 {
-	int start = jointStart[c];
-	int count = jointStart[c + 1] - start;
+	int start = sJStart[c];
+	int count = sJStart[c + 1] - start;
 	for ( int k = gtid; k < count; k += gstride )
 	{
 		int j = jointSlots[start + k];
@@ -692,22 +703,72 @@ __device__ __forceinline__ void joint_colour_stage( const DWorld& w, int c, int 
 	}
 }
 
+// Manifold write-back of one constraint (contact_solver.c:480-509 overflow,
+// :2078-2120 graph lanes; graph lanes store both points, zeros for a
+// one-point manifold).
+__device__ __forceinline__ void store_manifold( const DWorld& w, int k, float4 imp, float2 tot, float rolling,
+												float rv1, float rv2, int count, bool lane )
+{
+	int c = w.slotContact[k];
+	w.mpI[2 * c + 0] = make_float4( imp.x, imp.z, tot.x, rv1 );
+	if ( lane || count > 1 )
+		w.mpI[2 * c + 1] = make_float4( imp.y, imp.w, tot.y, rv2 );
+	float4 mn = w.mnorm[c];
+	mn.z = rolling;
+	w.mnorm[c] = mn;
+}
+
+__device__ __forceinline__ void store_manifold_global( const DWorld& w, int k, bool lane )
+{
+	float4 imp = __ldcg( w.kImp + k );
+	float2 tot = __ldcg( w.kTot + k );
+	float4 misc = __ldcg( w.kMisc + k );
+	store_manifold( w, k, imp, tot, misc.w, w.kP1[k].w, w.kP2[k].w, __float_as_int( w.kSoft[k].w ), lane );
+}
+
+// The persistent solver. Graph-colour constraint slots (after the overflow
+// slots) are dealt to threads round-robin over the blocks: thread t of block
+// b owns colour slot r = t * gridDim.x + b (and r + gridDim.x * blockDim.x,
+// ... when the graph holds more constraints than the grid has threads). The
+// first owned constraint lives in registers for the whole launch; a colour
+// stage then costs one load and one store of each of its two bodies.
 __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolveParams p, const int* jointSlots,
 															 const int* jointStart )
 {
+	__shared__ int sStart[F2D_COLORS], sCount[F2D_COLORS], sJStart[F2D_OVERFLOW + 1];
+	if ( threadIdx.x < F2D_COLORS )
+	{
+		sStart[threadIdx.x] = w.sc->colorStart[threadIdx.x];
+		sCount[threadIdx.x] = w.sc->colorCount[threadIdx.x];
+	}
+	if ( threadIdx.x <= F2D_OVERFLOW )
+		sJStart[threadIdx.x] = jointStart[threadIdx.x];
+	__syncthreads();
+
 	int gtid = blockIdx.x * blockDim.x + threadIdx.x;
 	int gstride = gridDim.x * blockDim.x;
 	unsigned epoch = 0;
 	int nb = w.bodyCount;
 	int novf = w.sc->overflowCount;
 	int novfJ = w.sc->overflowJointCount;
+	int nColour = w.sc->touchingCount - novf;
 	bool serialStage = novf > 0 || novfJ > 0;
-	// active colours: any contact or joint
-	int active[F2D_OVERFLOW];
-	int nActive = 0;
+	unsigned activeMask = 0;
 	for ( int c = 0; c < F2D_OVERFLOW; ++c )
-		if ( w.sc->colorCount[c] > 0 || jointStart[c + 1] > jointStart[c] )
-			active[nActive++] = c;
+		if ( sCount[c] > 0 || sJStart[c + 1] > sJStart[c] )
+			activeMask |= 1u << c;
+
+	const int r0 = threadIdx.x * gridDim.x + blockIdx.x;
+	Lane L0;
+	int col0 = -1;
+	if ( r0 < nColour )
+	{
+		int k0 = novf + r0;
+		lane_load( w, k0, L0 );
+		for ( int c = 0; c < F2D_OVERFLOW; ++c )
+			if ( k0 >= sStart[c] && k0 < sStart[c] + sCount[c] )
+				col0 = c;
+	}
 
 	for ( int sub = 0; sub < p.subSteps; ++sub )
 	{
@@ -760,11 +821,24 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
-			for ( int a = 0; a < nActive; ++a )
+			for ( int c = 0; c < F2D_OVERFLOW; ++c )
 			{
-				int c = active[a];
-				joint_colour_stage( w, c, kind, p, gtid, gstride, jointSlots, jointStart );
-				colour_stage( w, c, kind, p, gtid, gstride );
+				if ( ( activeMask & ( 1u << c ) ) == 0 )
+					continue;
+				joint_colour_stage( w, c, kind, p, gtid, gstride, jointSlots, sJStart );
+				if ( col0 == c )
+					lane_op( w, L0, kind, p );
+				for ( int r = r0 + gstride; r < nColour; r += gstride )
+				{
+					int k = novf + r;
+					if ( k >= sStart[c] && k < sStart[c] + sCount[c] )
+					{
+						Lane L;
+						lane_load( w, k, L );
+						lane_op( w, L, kind, p );
+						lane_store( w, k, L );
+					}
+				}
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
@@ -779,33 +853,34 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
-	for ( int a = 0; a < nActive; ++a )
+	for ( int c = 0; c < F2D_OVERFLOW; ++c )
 	{
-		int c = active[a];
-		if ( w.sc->colorCount[c] == 0 )
+		if ( sCount[c] == 0 )
 			continue;
-		colour_stage( w, c, 3, p, gtid, gstride );
+		if ( col0 == c )
+			lane_op( w, L0, 3, p );
+		for ( int r = r0 + gstride; r < nColour; r += gstride )
+		{
+			int k = novf + r;
+			if ( k >= sStart[c] && k < sStart[c] + sCount[c] )
+			{
+				Lane L;
+				lane_load( w, k, L );
+				lane_op( w, L, 3, p );
+				lane_store( w, k, L );
+			}
+		}
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
-	// store impulses (contact_solver.c:480-509, :2078-2120)
-	int n = w.sc->touchingCount;
-	for ( int k = gtid; k < n; k += gstride )
-	{
-		int c = w.slotContact[k];
-		float4 imp = w.kImp[k];
-		float2 tot = w.kTot[k];
-		float4 misc = w.kMisc[k];
-		float4 p1 = w.kP1[k], p2 = w.kP2[k];
-		int count = __float_as_int( w.kSoft[k].w );
-		bool lane = k >= novf; // graph lanes store both points (zeros for a 1-point manifold)
-		w.mpI[2 * c + 0] = make_float4( imp.x, imp.z, tot.x, p1.w );
-		if ( lane || count > 1 )
-			w.mpI[2 * c + 1] = make_float4( imp.y, imp.w, tot.y, p2.w );
-		float4 mn = w.mnorm[c];
-		mn.z = misc.w;
-		w.mnorm[c] = mn;
-	}
+	// store impulses into the manifolds
+	for ( int k = gtid; k < novf; k += gstride )
+		store_manifold_global( w, k, false );
+	if ( col0 >= 0 )
+		store_manifold( w, novf + r0, L0.imp, L0.tot, L0.misc.w, L0.pt[0].w, L0.pt[1].w,
+						__float_as_int( L0.sf.w ), true );
+	for ( int r = r0 + gstride; r < nColour; r += gstride )
+		store_manifold_global( w, novf + r, true );
 }
 
 // ---------------------------------------------------------------------------
