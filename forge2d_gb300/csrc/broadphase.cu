@@ -6,10 +6,15 @@
 // with overlapping fat AABBs, at least one of them a dynamic proxy and at
 // least one of them moved, that passes the filters and has no contact yet.
 // This file computes the same set GPU-first:
-//   1. a linear BVH (Karras 2012) over all proxies' fat AABBs, rebuilt each
-//      step from 30-bit Morton codes sorted with the stable radix sort;
-//   2. one thread per moved proxy traverses it (leaves in Morton order, so
-//      neighbouring threads walk neighbouring subtrees);
+//   1. an implicit 32-ary bounding-volume tree over all proxies' fat AABBs,
+//      rebuilt each step: leaves in the order of their 30-bit Morton codes
+//      (one-launch radix sort), node k of level l bounding children
+//      32k..32k+31 of level l-1, so no topology is stored and a refit is one
+//      launch whose longest dependency chain is the tree height (4 levels
+//      at 1e6 proxies);
+//   2. one thread per moved proxy walks it depth first (leaves in Morton
+//      order, so neighbouring threads walk neighbouring subtrees; the 32
+//      children of a node are contiguous);
 //   3. new pairs are sorted by their 64-bit shape-pair key, the order in
 //      which contact ids are then drawn from the LIFO id pool.
 #include "dscan.cuh"
@@ -18,7 +23,42 @@
 #include "kernels.cuh"
 
 #define BP_THREADS 256
-#define TRAVERSE_STACK 64
+#define WIDE 32
+#define WIDE_MAX_LEVELS 6
+
+// Level sizes of the implicit tree over n leaves: level 0 holds the leaves,
+// level l has ceil(count[l-1] / 32) nodes; all levels share nodeBox, level l
+// starting at offset[l]. top is the root's level (0 when n == 1).
+struct WideLevels
+{
+	int count[WIDE_MAX_LEVELS + 1];
+	int offset[WIDE_MAX_LEVELS + 1];
+	int top;
+};
+
+__device__ __forceinline__ WideLevels wide_levels( int n )
+{
+	WideLevels L;
+	L.count[0] = n;
+	L.offset[0] = 0;
+	int off = n, c = n, k = 0;
+	while ( c > 1 && k < WIDE_MAX_LEVELS )
+	{
+		c = ( c + WIDE - 1 ) / WIDE;
+		k += 1;
+		L.count[k] = c;
+		L.offset[k] = off;
+		off += c;
+	}
+	L.top = k;
+	return L;
+}
+
+// refit counters exist for the nodes of levels >= 2
+__device__ __forceinline__ int wide_counter( const WideLevels& L, int level, int node )
+{
+	return L.offset[level] - L.offset[2] + node;
+}
 
 __device__ __forceinline__ unsigned long long pair_key( int a, int b )
 {
@@ -177,100 +217,87 @@ __global__ void k_morton( DWorld w, const float4* bounds )
 		unsigned qy = (unsigned)fminf( fmaxf( ( cy - b.y ) * iny, 0.0f ), 32767.0f );
 		w.mortonKeys[i] = ( expand_bits15( qx ) << 1 ) | expand_bits15( qy );
 	}
-}
-
-// Karras 2012 common-prefix length with index tie-break
-__device__ __forceinline__ int delta_fn( const unsigned* keys, int n, int i, int j )
-{
-	if ( j < 0 || j >= n )
-		return -1;
-	unsigned a = keys[i], b = keys[j];
-	if ( a == b )
-		return 32 + __clz( (unsigned)( i ^ j ) );
-	return __clz( a ^ b );
-}
-
-// Internal node i spans a key range; children are internal nodes or leaves
-// (~leaf). nodeParent holds internal parents at [0, n-1) and leaf parents at
-// [n-1, 2n-1).
-__global__ void k_build_tree( DWorld w )
-{
-	int n = w.sc->treeLeafCount;
-	const unsigned* keys = w.mortonKeys;
-	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x )
+	// refit counters of the implicit tree (levels >= 2), used by k_wide_refit
+	WideLevels L = wide_levels( n );
+	if ( L.top >= 2 )
 	{
-		int d = ( delta_fn( keys, n, i, i + 1 ) - delta_fn( keys, n, i, i - 1 ) ) >= 0 ? 1 : -1;
-		int dmin = delta_fn( keys, n, i, i - d );
-		int lmax = 2;
-		while ( delta_fn( keys, n, i, i + lmax * d ) > dmin )
-			lmax <<= 1;
-		int l = 0;
-		for ( int t = lmax >> 1; t >= 1; t >>= 1 )
-			if ( delta_fn( keys, n, i, i + ( l + t ) * d ) > dmin )
-				l += t;
-		int j = i + l * d;
-		int dnode = delta_fn( keys, n, i, j );
-		int s = 0;
-		int len = l;
-		int t = ( len + 1 ) >> 1;
-		while ( true )
-		{
-			if ( delta_fn( keys, n, i, i + ( s + t ) * d ) > dnode )
-				s += t;
-			if ( t == 1 )
-				break;
-			t = ( t + 1 ) >> 1;
-		}
-		int gamma = i + s * d + ( d < 0 ? d : 0 );
-		int lo = i < j ? i : j;
-		int hi = i < j ? j : i;
-		int left = ( lo == gamma ) ? ~gamma : gamma;
-		int right = ( hi == gamma + 1 ) ? ~( gamma + 1 ) : gamma + 1;
-		w.nodeLeft[i] = left;
-		w.nodeRight[i] = right;
-		if ( left < 0 )
-			w.nodeParent[n - 1 + ~left] = i;
-		else
-			w.nodeParent[left] = i;
-		if ( right < 0 )
-			w.nodeParent[n - 1 + ~right] = i;
-		else
-			w.nodeParent[right] = i;
-		w.nodeVisit[i] = 0;
+		int total = L.offset[L.top] + 1 - L.offset[2];
+		for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x )
+			w.nodeVisit[i] = 0;
 	}
-	if ( blockIdx.x == 0 && threadIdx.x == 0 && n > 0 )
-		w.nodeParent[0] = -1;
 }
 
-// leaf boxes live at nodeBox[n-1+leaf]; walk up, second arrival merges
-__global__ void k_tree_boxes( DWorld w )
+__device__ __forceinline__ float4 box_union4( float4 a, float4 b )
 {
-	int n = w.sc->treeLeafCount;
-	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	return make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fmaxf( a.z, b.z ), fmaxf( a.w, b.w ) );
+}
+
+__device__ __forceinline__ float4 warp_box_union( float4 b )
+{
+#pragma unroll
+	for ( int o = 16; o > 0; o >>= 1 )
 	{
-		int s = w.leafShape[i];
-		w.nodeBox[n - 1 + i] = w.fat[s];
-		if ( n == 1 )
-			continue;
-		__threadfence();
-		int node = w.nodeParent[n - 1 + i];
-		for ( int guard = 0; node >= 0; ++guard )
+		float4 t;
+		t.x = __shfl_xor_sync( 0xffffffffu, b.x, o );
+		t.y = __shfl_xor_sync( 0xffffffffu, b.y, o );
+		t.z = __shfl_xor_sync( 0xffffffffu, b.z, o );
+		t.w = __shfl_xor_sync( 0xffffffffu, b.w, o );
+		b = box_union4( b, t );
+	}
+	return b;
+}
+
+__device__ __forceinline__ int atom_add_acq_rel( int* p, int v )
+{
+	int old;
+	asm volatile( "atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"( old ) : "l"( p ), "r"( v ) : "memory" );
+	return old;
+}
+
+// One warp per level-1 node: the 32 leaf boxes (fat AABBs in Morton order)
+// and their union. The last child to finish a node of level >= 2 (atomic
+// counter) unions that node's children, up to the root.
+__global__ void k_wide_refit( DWorld w )
+{
+	const int n = w.sc->treeLeafCount;
+	const WideLevels L = wide_levels( n );
+	const int lane = threadIdx.x & 31;
+	const int warps = ( gridDim.x * blockDim.x ) >> 5;
+	const float4 empty = make_float4( FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX );
+	const int groups = ( n + WIDE - 1 ) / WIDE;
+	for ( int g = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5; g < groups; g += warps )
+	{
+		int i = g * WIDE + lane;
+		float4 b = empty;
+		if ( i < n )
 		{
-			if ( guard > 4096 || node >= n - 1 )
-			{
-				atomicOr( &w.sc->error, ERR_TREE );
-				break;
-			}
-			int prev = atomicAdd( w.nodeVisit + node, 1 );
-			if ( prev == 0 )
+			b = w.fat[w.leafShape[i]];
+			w.nodeBox[i] = b;
+		}
+		if ( L.top == 0 )
+			continue;
+		b = warp_box_union( b );
+		if ( lane == 0 )
+			w.nodeBox[L.offset[1] + g] = b;
+		int level = 1, node = g;
+		while ( level < L.top )
+		{
+			int parent = node / WIDE;
+			int nchild = min( WIDE, L.count[level] - parent * WIDE );
+			int prev = 0;
+			if ( lane == 0 )
+				prev = atom_add_acq_rel( w.nodeVisit + wide_counter( L, level + 1, parent ), 1 );
+			prev = __shfl_sync( 0xffffffffu, prev, 0 );
+			if ( prev != nchild - 1 )
 				break;
 			__threadfence();
-			int l = w.nodeLeft[node], r = w.nodeRight[node];
-			float4 a = __ldcg( w.nodeBox + ( l < 0 ? n - 1 + ~l : l ) );
-			float4 b = __ldcg( w.nodeBox + ( r < 0 ? n - 1 + ~r : r ) );
-			w.nodeBox[node] = make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fmaxf( a.z, b.z ), fmaxf( a.w, b.w ) );
-			__threadfence();
-			node = w.nodeParent[node];
+			int ci = parent * WIDE + lane;
+			float4 cb = lane < nchild ? __ldcg( w.nodeBox + L.offset[level] + ci ) : empty;
+			cb = warp_box_union( cb );
+			level += 1;
+			node = parent;
+			if ( lane == 0 )
+				w.nodeBox[L.offset[level] + node] = cb;
 		}
 	}
 }
@@ -340,10 +367,59 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 
 // One thread per moved proxy. A pair found by both of its moved proxies is
 // reported by the one with the smaller shape id.
-__global__ void k_find_pairs( DWorld w )
+// Candidate pair (si moved, sj its overlapping leaf): the filters of
+// b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup.
+__device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int typeI, int bi, int sj )
 {
-	int n = w.sc->treeLeafCount;
-	for ( int li = blockIdx.x * blockDim.x + threadIdx.x; li < n; li += gridDim.x * blockDim.x )
+	if ( sj == si )
+		return;
+	int fj = w.sflags[sj];
+	int typeJ = w.proxyKey[sj] & 3;
+	bool movedJ = ( fj & SF_MOVED ) != 0;
+	if ( movedJ && sj < si )
+		return; // reported by sj
+	if ( typeI != 2 && typeJ != 2 )
+		return;
+	bool primaryUnused;
+	if ( !registered( shape_type( fi ), shape_type( fj ), &primaryUnused ) )
+		return; // no manifold function: b2CreateContact makes no contact
+	int bj = w.shapeBody[sj];
+	if ( bj == bi || ( fi & SF_SENSOR ) || ( fj & SF_SENSOR ) )
+		return;
+	if ( !shapes_collide( w, si, sj ) || !bodies_collide( w, bi, bj ) )
+		return;
+	if ( hash_contains( w, pair_key( si, sj ) ) )
+		return;
+	int slot = atomicAdd( &w.sc->newPairCount, 1 );
+	if ( slot < w.pairCap )
+	{
+		int lo = si < sj ? si : sj, hi = si < sj ? sj : si;
+		w.pairKeys[slot] = ( (unsigned long long)lo << w.pairKeyBits ) | (unsigned)hi;
+	}
+	else
+		atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
+}
+
+// One warp per moved proxy: the 32 children of a node are tested by the 32
+// lanes at once (one coalesced load), overlapping inner children are pushed
+// on a per-warp stack in shared memory, overlapping leaves are tested by
+// their lanes in parallel. The visiting order does not matter: new pairs are
+// sorted by key afterwards.
+#define FIND_WARPS ( BP_THREADS / 32 )
+#define FIND_STACK ( WIDE * WIDE_MAX_LEVELS )
+
+__global__ void __launch_bounds__( BP_THREADS ) k_find_pairs( DWorld w )
+{
+	__shared__ int stack[FIND_WARPS][FIND_STACK];
+	const int n = w.sc->treeLeafCount;
+	if ( n < 2 )
+		return;
+	const WideLevels L = wide_levels( n );
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	const unsigned below = ( 1u << lane ) - 1u;
+	int* stk = stack[wib];
+	const int warps = ( gridDim.x * blockDim.x ) >> 5;
+	for ( int li = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5; li < n; li += warps )
 	{
 		int si = w.leafShape[li];
 		int fi = w.sflags[si];
@@ -352,91 +428,48 @@ __global__ void k_find_pairs( DWorld w )
 		int typeI = w.proxyKey[si] & 3;
 		fbox q = box_from4( w.fat[si] );
 		int bi = w.shapeBody[si];
-		int stack[TRAVERSE_STACK];
-		int sp = 0;
-		int node = n == 1 ? ~0 : 0;
-		for ( int guard = 0;; ++guard )
+		// stack entries: level << 26 | node
+		int sp = 1;
+		if ( lane == 0 )
+			stk[0] = L.top << 26;
+		__syncwarp();
+		for ( int guard = 0; sp > 0; ++guard )
 		{
-			if ( guard > 4 * n + 64 || node >= n - 1 + ( n == 1 ) || ~node >= n )
+			if ( guard > 2 * n + 64 )
 			{
-				atomicOr( &w.sc->error, ERR_TREE );
+				if ( lane == 0 )
+					atomicOr( &w.sc->error, ERR_TREE );
 				break;
 			}
-			if ( node < 0 )
+			sp -= 1;
+			int e = stk[sp];
+			__syncwarp();
+			int level = e >> 26, node = e & ( ( 1 << 26 ) - 1 );
+			int nchild = min( WIDE, L.count[level - 1] - node * WIDE );
+			int child = node * WIDE + lane;
+			bool ov = lane < nchild && box_overlaps( q, box_from4( w.nodeBox[L.offset[level - 1] + child] ) );
+			unsigned mask = __ballot_sync( 0xffffffffu, ov );
+			if ( level == 1 )
 			{
-				int leaf = ~node;
-				int sj = w.leafShape[leaf];
-				if ( sj != si )
-				{
-					fbox bj = box_from4( w.nodeBox[n - 1 + leaf] );
-					if ( box_overlaps( q, bj ) )
-					{
-						int fj = w.sflags[sj];
-						int typeJ = w.proxyKey[sj] & 3;
-						bool movedJ = ( fj & SF_MOVED ) != 0;
-						bool ok = true;
-						if ( movedJ && sj < si )
-							ok = false; // reported by sj
-						if ( typeI != 2 && typeJ != 2 )
-							ok = false;
-						bool primaryUnused;
-						if ( ok && !registered( shape_type( fi ), shape_type( fj ), &primaryUnused ) )
-							ok = false; // no manifold function: b2CreateContact makes no contact
-						if ( ok )
-						{
-							int bj2 = w.shapeBody[sj];
-							if ( bj2 == bi || ( fi & SF_SENSOR ) || ( fj & SF_SENSOR ) )
-								ok = false;
-							else if ( !shapes_collide( w, si, sj ) )
-								ok = false;
-							else if ( !bodies_collide( w, bi, bj2 ) )
-								ok = false;
-							else if ( hash_contains( w, pair_key( si, sj ) ) )
-								ok = false;
-						}
-						if ( ok )
-						{
-							int slot = atomicAdd( &w.sc->newPairCount, 1 );
-							if ( slot < w.pairCap )
-							{
-								int lo = si < sj ? si : sj, hi = si < sj ? sj : si;
-								w.pairKeys[slot] = ( (unsigned long long)lo << w.pairKeyBits ) | (unsigned)hi;
-							}
-							else
-								atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
-						}
-					}
-				}
-				if ( sp == 0 )
-					break;
-				node = stack[--sp];
-				continue;
+				if ( ov )
+					test_pair( w, si, fi, typeI, bi, w.leafShape[child] );
 			}
-			// internal node: test children
-			int l = w.nodeLeft[node], r = w.nodeRight[node];
-			fbox bl = box_from4( w.nodeBox[l < 0 ? n - 1 + ~l : l] );
-			fbox br = box_from4( w.nodeBox[r < 0 ? n - 1 + ~r : r] );
-			bool ol = box_overlaps( q, bl );
-			bool orr = box_overlaps( q, br );
-			if ( ol && orr )
-			{
-				if ( sp < TRAVERSE_STACK )
-					stack[sp++] = r;
-				else
-					atomicOr( &w.sc->error, ERR_TREE );
-				node = l;
-			}
-			else if ( ol )
-				node = l;
-			else if ( orr )
-				node = r;
 			else
 			{
-				if ( sp == 0 )
+				int cnt = __popc( mask );
+				if ( sp + cnt > FIND_STACK )
+				{
+					if ( lane == 0 )
+						atomicOr( &w.sc->error, ERR_TREE );
 					break;
-				node = stack[--sp];
+				}
+				if ( ov )
+					stk[sp + __popc( mask & below )] = ( ( level - 1 ) << 26 ) | child;
+				sp += cnt;
 			}
+			__syncwarp();
 		}
+		__syncwarp();
 	}
 }
 
@@ -583,9 +616,8 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_morton<<<gridS, BP_THREADS, 0, st>>>( w, s.bounds );
 	sort_coop<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount, 30,
 						 w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks32, st );
-	k_build_tree<<<gridS, BP_THREADS, 0, st>>>( w );
-	k_tree_boxes<<<gridS, BP_THREADS, 0, st>>>( w );
-	k_find_pairs<<<gridS, BP_THREADS, 0, st>>>( w );
+	k_wide_refit<<<( ( w.shapeCap + WIDE - 1 ) / WIDE + 7 ) / 8, BP_THREADS, 0, st>>>( w );
+	k_find_pairs<<<( w.shapeCap + FIND_WARPS - 1 ) / FIND_WARPS, BP_THREADS, 0, st>>>( w );
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );
 	int bits = 2 * w.pairKeyBits;
 	// new pair keys are unique, so the key order alone fixes the result
