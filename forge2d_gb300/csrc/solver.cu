@@ -40,19 +40,24 @@ struct SolveParams
 // ---------------------------------------------------------------------------
 // constraint slots: overflow first (overflow-array order), then colours
 // ---------------------------------------------------------------------------
+// Colour occupancy of the touching contacts: per-block counts in shared
+// memory, one global add per colour and block.
 __global__ void k_count_colors( DWorld w, int* fill )
 {
-	if ( blockIdx.x == 0 && threadIdx.x < F2D_COLORS )
-	{
-		// counts are produced by the previous kernel; fill is cleared here
-	}
+	__shared__ int cnt[F2D_OVERFLOW];
+	if ( threadIdx.x < F2D_OVERFLOW )
+		cnt[threadIdx.x] = 0;
+	__syncthreads();
 	int n = w.sc->contactIdCount;
 	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
 	{
 		int col = w.ccolor[c];
 		if ( col >= 0 && col < F2D_OVERFLOW && ( w.cflags[c] & CF_USED ) )
-			atomicAdd( fill + col, 1 );
+			atomicAdd( cnt + col, 1 );
 	}
+	__syncthreads();
+	if ( threadIdx.x < F2D_OVERFLOW && cnt[threadIdx.x] > 0 )
+		atomicAdd( fill + threadIdx.x, cnt[threadIdx.x] );
 }
 
 __global__ void k_zero_ints( int* p, int n )
@@ -78,20 +83,40 @@ __global__ void k_color_offsets( DWorld w, int* fill )
 	w.sc->touchingCount = start;
 }
 
+// Constraint slots: overflow contacts first (overflow-array order), then
+// each colour's contacts in a contiguous range. Inside a colour the slot
+// order is arbitrary (no two constraints of a colour share a dynamic body);
+// each block reserves its range with one global add per colour.
 __global__ void k_fill_slots( DWorld w, int* fill )
 {
+	__shared__ int cnt[F2D_OVERFLOW], base[F2D_OVERFLOW];
 	int n = w.sc->contactIdCount;
 	int nov = w.sc->overflowCount;
 	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < nov; i += gridDim.x * blockDim.x )
 		w.slotContact[i] = w.overflowList[i];
-	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	int stride = gridDim.x * blockDim.x;
+	for ( int c0 = blockIdx.x * blockDim.x; c0 < n; c0 += stride )
 	{
-		int col = w.ccolor[c];
-		if ( col >= 0 && col < F2D_OVERFLOW && ( w.cflags[c] & CF_USED ) )
+		if ( threadIdx.x < F2D_OVERFLOW )
+			cnt[threadIdx.x] = 0;
+		__syncthreads();
+		int c = c0 + threadIdx.x;
+		int col = -1, rank = 0;
+		if ( c < n )
 		{
-			int slot = w.sc->colorStart[col] + atomicAdd( fill + col, 1 );
-			w.slotContact[slot] = c;
+			col = w.ccolor[c];
+			if ( col >= 0 && col < F2D_OVERFLOW && ( w.cflags[c] & CF_USED ) )
+				rank = atomicAdd( cnt + col, 1 );
+			else
+				col = -1;
 		}
+		__syncthreads();
+		if ( threadIdx.x < F2D_OVERFLOW )
+			base[threadIdx.x] = cnt[threadIdx.x] > 0 ? atomicAdd( fill + threadIdx.x, cnt[threadIdx.x] ) : 0;
+		__syncthreads();
+		if ( col >= 0 )
+			w.slotContact[w.sc->colorStart[col] + base[col] + rank] = c;
+		__syncthreads();
 	}
 }
 

@@ -92,6 +92,10 @@ struct HostWorld
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
 
+	// device staging of the bulk body reader (12 floats per body)
+	float* packedBodies = nullptr;
+	int packedCap = 0;
+
 	// plan (parity mode)
 	std::vector<unsigned long long> planKeys;
 	std::vector<int> planIds;
@@ -623,6 +627,10 @@ static void free_world( HostWorld* W )
 	dfree( W->s.tmpB );
 	dfree( W->s.scanTmp );
 	dfree( W->s.scanState );
+	if ( W->packedBodies )
+		cudaFree( W->packedBodies );
+	W->packedBodies = nullptr;
+	W->packedCap = 0;
 	dfree( W->s.bounds );
 	cudaFreeHost( W->hostError );
 	cudaEventDestroy( W->evStart );
@@ -1600,51 +1608,82 @@ extern "C" F2D_API int32_t f2d_world_body_capacity( int32_t worldId )
 	return W ? W->bodyCount : 0;
 }
 
+// Packs the bulk body rows on the device so that one copy brings them home.
+__global__ void k_pack_bodies( DWorld w, float* out, int n )
+{
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		float* o = out + 12 * (size_t)i;
+		int f = w.bflags[i];
+		if ( ( f & BF_USED ) == 0 )
+		{
+			for ( int k = 0; k < 12; ++k )
+				o[k] = 0.0f;
+			continue;
+		}
+		float4 x = w.xf[i], v = w.vel[i], fo = w.force[i];
+		float2 c = w.center[i];
+		o[0] = x.x;
+		o[1] = x.y;
+		o[2] = x.z;
+		o[3] = x.w;
+		o[4] = v.x;
+		o[5] = v.y;
+		o[6] = v.z;
+		o[7] = c.x;
+		o[8] = c.y;
+		o[9] = 1.0f;
+		o[10] = body_type( f ) == 0 ? 0.0f : 2.0f;
+		o[11] = fo.w;
+	}
+}
+
+static void host_body_row( const HostWorld* W, int i, float* o )
+{
+	memset( o, 0, sizeof( float ) * 12 );
+	if ( ( W->bflags[i] & BF_USED ) == 0 )
+		return;
+	o[0] = W->xf[i].x;
+	o[1] = W->xf[i].y;
+	o[2] = W->xf[i].z;
+	o[3] = W->xf[i].w;
+	o[4] = W->vel[i].x;
+	o[5] = W->vel[i].y;
+	o[6] = W->vel[i].z;
+	o[7] = W->center[i].x;
+	o[8] = W->center[i].y;
+	o[9] = 1.0f;
+	o[10] = body_type( W->bflags[i] ) == 0 ? 0.0f : 2.0f;
+	o[11] = W->force[i].w;
+}
+
 extern "C" F2D_API int32_t f2d_world_get_bodies( int32_t worldId, float* out, int32_t cap )
 {
 	HostWorld* W = world_from_id( worldId );
 	if ( W == nullptr )
 		return 0;
-	cudaStreamSynchronize( W->stream );
 	int n = std::min( W->bodyCount, cap );
 	int up = std::min( n, W->bodyUploaded );
-	std::vector<float4> xf( W->xf.begin(), W->xf.begin() + n ), vel( W->vel.begin(), W->vel.begin() + n ),
-		force( W->force.begin(), W->force.begin() + n );
-	std::vector<float2> center( W->center.begin(), W->center.begin() + n );
 	if ( up > 0 )
 	{
-		cudaMemcpy( xf.data(), W->d.xf, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
-		cudaMemcpy( vel.data(), W->d.vel, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
-		cudaMemcpy( force.data(), W->d.force, sizeof( float4 ) * up, cudaMemcpyDeviceToHost );
-		cudaMemcpy( center.data(), W->d.center, sizeof( float2 ) * up, cudaMemcpyDeviceToHost );
+		if ( W->packedCap < W->d.bodyCap )
+		{
+			cudaStreamSynchronize( W->stream );
+			if ( W->packedBodies )
+				cudaFree( W->packedBodies );
+			cudaMalloc( (void**)&W->packedBodies, sizeof( float ) * 12 * (size_t)W->d.bodyCap );
+			W->packedCap = W->d.bodyCap;
+		}
+		k_pack_bodies<<<grid_for( up ), 256, 0, W->stream>>>( W->d, W->packedBodies, up );
+		cudaMemcpyAsync( out, W->packedBodies, sizeof( float ) * 12 * (size_t)up, cudaMemcpyDeviceToHost, W->stream );
+		cudaStreamSynchronize( W->stream );
+		// rows edited on the host since the last upload are newer than the device
 		for ( int b : W->bodyDirty )
-			if ( b < n )
-			{
-				xf[b] = W->xf[b];
-				vel[b] = W->vel[b];
-				force[b] = W->force[b];
-				center[b] = W->center[b];
-			}
+			if ( b < up )
+				host_body_row( W, b, out + 12 * (size_t)b );
 	}
-	for ( int i = 0; i < n; ++i )
-	{
-		float* o = out + 12 * i;
-		memset( o, 0, sizeof( float ) * 12 );
-		if ( ( W->bflags[i] & BF_USED ) == 0 )
-			continue;
-		o[0] = xf[i].x;
-		o[1] = xf[i].y;
-		o[2] = xf[i].z;
-		o[3] = xf[i].w;
-		o[4] = vel[i].x;
-		o[5] = vel[i].y;
-		o[6] = vel[i].z;
-		o[7] = center[i].x;
-		o[8] = center[i].y;
-		o[9] = 1.0f;
-		o[10] = body_type( W->bflags[i] ) == 0 ? 0.0f : 2.0f;
-		o[11] = force[i].w;
-	}
+	for ( int i = up; i < n; ++i )
+		host_body_row( W, i, out + 12 * (size_t)i );
 	return n;
 }
 
