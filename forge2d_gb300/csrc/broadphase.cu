@@ -82,6 +82,11 @@ __global__ void k_hash_clear( DWorld w )
 {
 	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.hashCap; i += gridDim.x * blockDim.x )
 		w.pairHash[i] = 0ull;
+	// refit counters of the implicit tree (levels >= 2 hold fewer than one
+	// node per 1000 leaves), used by k_wide_refit
+	int counters = min( w.shapeCap, w.shapeCount / 512 + 8 );
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < counters; i += gridDim.x * blockDim.x )
+		w.nodeVisit[i] = 0;
 }
 
 __global__ void k_hash_insert( DWorld w )
@@ -127,12 +132,16 @@ __device__ __forceinline__ bool hash_contains( const DWorld& w, unsigned long lo
 // ---------------------------------------------------------------------------
 __global__ void k_leaf_flags( DWorld w, int* flags )
 {
+	if ( w.sc->rebuildOrder == 0 )
+		return;
 	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
 		flags[s] = ( w.sflags[s] & ( SF_USED | SF_PROXY ) ) == ( SF_USED | SF_PROXY ) ? 1 : 0;
 }
 
 __global__ void k_leaf_compact( DWorld w, const int* flags, const int* offs )
 {
+	if ( w.sc->rebuildOrder == 0 )
+		return;
 	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
 		if ( flags[s] )
 			w.leafShape[offs[s]] = s;
@@ -142,6 +151,8 @@ __global__ void k_leaf_compact( DWorld w, const int* flags, const int* offs )
 __global__ void k_bounds_partial( DWorld w, float4* partial )
 {
 	__shared__ float4 red[BP_THREADS];
+	if ( w.sc->rebuildOrder == 0 )
+		return;
 	int n = w.sc->treeLeafCount;
 	float4 b = make_float4( FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX );
 	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
@@ -168,9 +179,11 @@ __global__ void k_bounds_partial( DWorld w, float4* partial )
 		partial[blockIdx.x] = red[0];
 }
 
-__global__ void k_bounds_final( float4* partial, int count )
+__global__ void k_bounds_final( const int* rebuild, float4* partial, int count )
 {
 	__shared__ float4 red[BP_THREADS];
+	if ( *rebuild == 0 )
+		return;
 	float4 b = make_float4( FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX );
 	for ( int i = threadIdx.x; i < count; i += blockDim.x )
 	{
@@ -204,6 +217,8 @@ __device__ __forceinline__ unsigned expand_bits15( unsigned v )
 
 __global__ void k_morton( DWorld w, const float4* bounds )
 {
+	if ( w.sc->rebuildOrder == 0 )
+		return;
 	int n = w.sc->treeLeafCount;
 	float4 b = bounds[0];
 	float sx = b.z - b.x, sy = b.w - b.y;
@@ -216,14 +231,6 @@ __global__ void k_morton( DWorld w, const float4* bounds )
 		unsigned qx = (unsigned)fminf( fmaxf( ( cx - b.x ) * inx, 0.0f ), 32767.0f );
 		unsigned qy = (unsigned)fminf( fmaxf( ( cy - b.y ) * iny, 0.0f ), 32767.0f );
 		w.mortonKeys[i] = ( expand_bits15( qx ) << 1 ) | expand_bits15( qy );
-	}
-	// refit counters of the implicit tree (levels >= 2), used by k_wide_refit
-	WideLevels L = wide_levels( n );
-	if ( L.top >= 2 )
-	{
-		int total = L.offset[L.top] + 1 - L.offset[2];
-		for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x )
-			w.nodeVisit[i] = 0;
 	}
 }
 
@@ -609,13 +616,13 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, st>>>( w );
 	k_leaf_flags<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA );
 	scan_lookback( s.tmpA, s.tmpB, nullptr, w.shapeCount, w.shapeCap, &w.sc->treeLeafCount, s.scanState, &w.sc->error,
-				   st );
+				   st, &w.sc->rebuildOrder );
 	k_leaf_compact<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA, s.tmpB );
 	k_bounds_partial<<<s.boundsBlocks, BP_THREADS, 0, st>>>( w, s.bounds );
-	k_bounds_final<<<1, BP_THREADS, 0, st>>>( s.bounds, s.boundsBlocks );
+	k_bounds_final<<<1, BP_THREADS, 0, st>>>( &w.sc->rebuildOrder, s.bounds, s.boundsBlocks );
 	k_morton<<<gridS, BP_THREADS, 0, st>>>( w, s.bounds );
 	sort_coop<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount, 30,
-						 w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks32, st );
+						 w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks32, st, &w.sc->rebuildOrder );
 	k_wide_refit<<<( ( w.shapeCap + WIDE - 1 ) / WIDE + 7 ) / 8, BP_THREADS, 0, st>>>( w );
 	k_find_pairs<<<( w.shapeCap + FIND_WARPS - 1 ) / FIND_WARPS, BP_THREADS, 0, st>>>( w );
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );

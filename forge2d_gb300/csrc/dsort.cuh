@@ -56,10 +56,12 @@ union CSortSmem
 template <typename K>
 __global__ void __launch_bounds__( CSORT_THREADS )
 	k_sort_coop( K* keys, int* vals, K* keysAlt, int* valsAlt, const int* nPtr, int bits, unsigned* hist,
-				 unsigned* counter, int* err )
+				 unsigned* counter, int* err, const int* enable )
 {
 	__shared__ CSortSmem sm;
 	const int tid = threadIdx.x;
+	if ( enable && *enable == 0 )
+		return;
 	const int n = *nPtr;
 	if ( n <= 1 )
 		return;
@@ -223,17 +225,19 @@ __global__ void __launch_bounds__( CSORT_THREADS )
 
 // Sorts (keys, vals) by the low `bits` bits of the keys; vals may be null.
 // n from device memory. hist needs 256 * CSORT_MAX_BLOCKS unsigned; counter
-// is a device word used by the grid barrier (zeroed here).
+// is a device word used by the grid barrier (zeroed here). When enable is
+// non-null the sort runs only if *enable != 0.
 template <typename K>
 static inline void sort_coop( K* keys, int* vals, K* keysAlt, int* valsAlt, const int* nPtr, int bits,
-							  unsigned* hist, unsigned* counter, int* err, int blocks, cudaStream_t st )
+							  unsigned* hist, unsigned* counter, int* err, int blocks, cudaStream_t st,
+							  const int* enable = nullptr )
 {
 	if ( blocks > CSORT_MAX_BLOCKS )
 		blocks = CSORT_MAX_BLOCKS;
 	if ( vals == nullptr )
 		valsAlt = nullptr;
 	cudaMemsetAsync( counter, 0, sizeof( unsigned ), st );
-	void* args[] = { &keys, &vals, &keysAlt, &valsAlt, &nPtr, &bits, &hist, &counter, &err };
+	void* args[] = { &keys, &vals, &keysAlt, &valsAlt, &nPtr, &bits, &hist, &counter, &err, &enable };
 	cudaLaunchCooperativeKernel( (void*)k_sort_coop<K>, dim3( blocks ), dim3( CSORT_THREADS ), args, 0, st );
 }
 
@@ -255,10 +259,12 @@ template <typename K> static inline int sort_coop_blocks()
 // ---------------------------------------------------------------------------
 static __global__ void __launch_bounds__( LB_THREADS )
 	k_scan_lookback( const int* __restrict__ in, int* __restrict__ out, const int* __restrict__ nPtr, int nConst,
-					 unsigned long long* state, int* __restrict__ totalOut, int* err )
+					 unsigned long long* state, int* __restrict__ totalOut, int* err, const int* enable )
 {
 	__shared__ int smem[32];
 	__shared__ int s_tile, s_prefix;
+	if ( enable && *enable == 0 )
+		return;
 	int n = nPtr ? *nPtr : nConst;
 	if ( threadIdx.x == 0 )
 		s_tile = (int)atomicAdd( (unsigned*)state, 1u );
@@ -330,13 +336,15 @@ static __global__ void __launch_bounds__( LB_THREADS )
 
 // Exclusive scan of n ints (n from nPtr when non-null, else nConst); cap
 // bounds the grid; state needs cap / LB_TILE + 2 words; totalOut (device)
-// receives the sum when non-null.
+// receives the sum when non-null. When enable is non-null the scan runs only
+// if *enable != 0.
 static inline void scan_lookback( const int* in, int* out, const int* nPtr, int nConst, int cap, int* totalOut,
-								  unsigned long long* state, int* err, cudaStream_t st )
+								  unsigned long long* state, int* err, cudaStream_t st,
+								  const int* enable = nullptr )
 {
 	int tiles = ( cap + LB_TILE - 1 ) / LB_TILE;
 	if ( tiles < 1 )
 		tiles = 1;
 	cudaMemsetAsync( state, 0, sizeof( unsigned long long ) * (size_t)( tiles + 1 ), st );
-	k_scan_lookback<<<tiles, LB_THREADS, 0, st>>>( in, out, nPtr, nConst, state, totalOut, err );
+	k_scan_lookback<<<tiles, LB_THREADS, 0, st>>>( in, out, nPtr, nConst, state, totalOut, err, enable );
 }

@@ -68,6 +68,10 @@
 //   g[2..5] polygon vertices, g[6..9] polygon normals
 #define GEOM_F4 10
 
+// The tree's leaf order only sets its tightness, never the pairs it finds
+// (new pairs are sorted by key), so it is refreshed periodically.
+#define ORDER_REBUILD_PERIOD 8
+
 // Per-step scalars kept in device memory so that no launch needs a host
 // round trip.
 struct DScalars
@@ -92,7 +96,12 @@ struct DScalars
 	int treeLeafCount;
 	float contactSpeed;
 	int stepIndex;
-	int pad[8];
+	// leaf order of the broadphase tree: re-sorted when forced (proxy set or
+	// shape rows changed) or every ORDER_REBUILD_PERIOD steps, reused between
+	int rebuildOrder;
+	int forceRebuild;
+	int orderAge;
+	int pad[5];
 };
 
 struct DWorld

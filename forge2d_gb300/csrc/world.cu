@@ -92,6 +92,9 @@ struct HostWorld
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
 
+	// the broadphase must re-sort its leaf order at the next step
+	bool forceRebuild = true;
+
 	// device staging of the bulk body reader (12 floats per body)
 	float* packedBodies = nullptr;
 	int packedCap = 0;
@@ -514,9 +517,12 @@ static void flush_uploads( HostWorld* W )
 	{
 		upload_shape_rows( W, W->shapeUploaded, W->shapeCount );
 		W->shapeUploaded = W->shapeCount;
+		W->forceRebuild = true;
 	}
 	for ( int s : W->shapeDirty )
 		upload_shape_rows( W, s, s + 1 );
+	if ( !W->shapeDirty.empty() )
+		W->forceRebuild = true;
 	W->shapeDirty.clear();
 	if ( W->jointUploaded < W->jointCount )
 	{
@@ -1205,6 +1211,11 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 		planMode = 1;
 	}
 	cudaMemsetAsync( &W->d.sc->error, 0, sizeof( int ), W->stream );
+	if ( W->forceRebuild )
+	{
+		cudaMemsetAsync( &W->d.sc->forceRebuild, 1, 1, W->stream );
+		W->forceRebuild = false;
+	}
 	cudaEventRecord( W->evStart, W->stream );
 	bool useGraph = planMode == 0 && !W->profiling;
 	if ( useGraph && ( W->graphDirty || W->graphExec == nullptr || W->graphDt != dt || W->graphSubSteps != subSteps ) )
