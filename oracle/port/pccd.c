@@ -138,9 +138,9 @@ void p_solve_continuous( World* w, int bodyId )
 		fast->center0 = c;
 		// the move event of this body was already written with the
 		// unadvanced transform; patch it (solver.c:472-474)
-		if ( w->moveEventCount > 0 && w->moveEventBodies[w->moveEventCount - 1] == bodyId )
+		if ( w->moveEventBodies[fast->moveEventIndex] == bodyId )
 		{
-			float* x = w->moveEventXf + 4 * ( w->moveEventCount - 1 );
+			float* x = w->moveEventXf + 4 * fast->moveEventIndex;
 			x[0] = transform.p.x;
 			x[1] = transform.p.y;
 			x[2] = transform.q.c;

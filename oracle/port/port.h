@@ -104,6 +104,7 @@ typedef struct Body
 	// constraint-graph membership: bit c set when the body holds a
 	// constraint in colour c < P_OVERFLOW (constraint_graph.c bodySet bitsets)
 	uint16_t colorMask;
+	int moveEventIndex; // this step's move event slot (finalize)
 } Body;
 
 typedef struct Shape
@@ -291,6 +292,10 @@ typedef struct World
 	int* moveEventBodies;
 	float* moveEventXf;
 	int moveEventCount, moveEventCap, moveEventXfCap;
+	int* constraintOrder; // contact id per constraint slot
+	int constraintOrderCap;
+	int* jointOrder; // graph-colour joints grouped by colour
+	int jointOrderCap;
 
 	int stepIndex;
 } World;
@@ -328,6 +333,11 @@ float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sw
 
 // joints (pjoint.c)
 Softness p_make_soft( float hertz, float zeta, float h );
+
+// cumulative seconds per step phase: pairs, collide, state changes, solver
+// set-up, substeps, restitution + store, finalize + continuous, events
+double p_now( void );
+extern double g_portPhase[8];
 void p_prepare_joint( World* w, Joint* j, float h, float inv_h, Softness jointSoftness );
 void p_warm_start_joint( World* w, Joint* j );
 void p_solve_joint( World* w, Joint* j, float h, float inv_h, int useBias );

@@ -7,6 +7,9 @@
 // lane is restated here as scalar code with the same operand order);
 // solver.h:140-180 (b2MakeSoft).
 #include "port.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include <stdlib.h>
 #include <string.h>
@@ -586,17 +589,14 @@ static void finalize_body( World* w, int id, float dt, float inv_dt )
 	b->dq.c = 1.0f;
 	b->dq.s = 0.0f;
 	b->xf.p = sub( b->center, rotate( b->xf.q, b->localCenter ) );
-	// move event
+	// move event (slot reserved before the parallel finalize)
 	{
-		w->moveEventBodies = grow( w->moveEventBodies, &w->moveEventCap, w->moveEventCount + 1, sizeof( int ) );
-		w->moveEventXf = grow( w->moveEventXf, &w->moveEventXfCap, 4 * ( w->moveEventCount + 1 ), sizeof( float ) );
-		w->moveEventBodies[w->moveEventCount] = id;
-		float* x = w->moveEventXf + 4 * w->moveEventCount;
+		w->moveEventBodies[b->moveEventIndex] = id;
+		float* x = w->moveEventXf + 4 * b->moveEventIndex;
 		x[0] = b->xf.p.x;
 		x[1] = b->xf.p.y;
 		x[2] = b->xf.q.c;
 		x[3] = b->xf.q.s;
-		w->moveEventCount += 1;
 	}
 	b->force = V( 0.0f, 0.0f );
 	b->torque = 0.0f;
@@ -688,115 +688,180 @@ void p_solve( World* w, float dt, int subStepCount )
 	if ( awakeCount == 0 )
 		return;
 
-	// gather constraints: overflow first (array order), then colours
-	int touching = 0;
-	for ( int id = 0; id < w->contactCount; ++id )
-		if ( w->contacts[id].used && w->contacts[id].color >= 0 )
-			touching += 1;
-	w->constraints = grow( w->constraints, &w->constraintCap, touching + 1, sizeof( Constraint ) );
-	int colorStart[P_COLORS + 1];
+	double tp0 = p_now();
+	// constraint order: overflow first (array order), then each colour's
+	// contacts in contact-id order
 	int nk = 0;
-	float warmStartScale = w->enableWarmStarting ? 1.0f : 0.0f;
+	w->constraintOrder = grow( w->constraintOrder, &w->constraintOrderCap, w->contactCount + 1, sizeof( int ) );
+	int* order = w->constraintOrder;
 	for ( int k = 0; k < w->overflowCount; ++k )
-	{
-		Contact* c = w->contacts + w->overflowContacts[k];
-		prepare_contact( w, w->constraints + nk, c, contactSoftness, staticSoftness, warmStartScale );
-		nk += 1;
-	}
+		order[nk++] = w->overflowContacts[k];
 	int overflowCount = nk;
-	for ( int color = 0; color < P_OVERFLOW; ++color )
+	int colorStart[P_COLORS + 1];
 	{
-		colorStart[color] = nk;
+		int cnt[P_OVERFLOW] = { 0 };
 		for ( int id = 0; id < w->contactCount; ++id )
 		{
 			Contact* c = w->contacts + id;
-			if ( c->used && c->color == color )
-			{
-				prepare_contact( w, w->constraints + nk, c, contactSoftness, staticSoftness, warmStartScale );
-				nk += 1;
-			}
+			if ( c->used && c->color >= 0 && c->color < P_OVERFLOW )
+				cnt[c->color] += 1;
+		}
+		int pos[P_OVERFLOW];
+		for ( int color = 0; color < P_OVERFLOW; ++color )
+		{
+			colorStart[color] = nk;
+			pos[color] = nk;
+			nk += cnt[color];
+		}
+		colorStart[P_OVERFLOW] = nk;
+		for ( int id = 0; id < w->contactCount; ++id )
+		{
+			Contact* c = w->contacts + id;
+			if ( c->used && c->color >= 0 && c->color < P_OVERFLOW )
+				order[pos[c->color]++] = id;
 		}
 	}
-	colorStart[P_OVERFLOW] = nk;
+	w->constraints = grow( w->constraints, &w->constraintCap, nk + 1, sizeof( Constraint ) );
 	Constraint* K = w->constraints;
+	float warmStartScale = w->enableWarmStarting ? 1.0f : 0.0f;
+#pragma omp parallel for schedule( static )
+	for ( int k = 0; k < nk; ++k )
+		prepare_contact( w, K + k, w->contacts + order[k], contactSoftness, staticSoftness, warmStartScale );
 
+	// graph-colour joints per colour (joint-id order)
+	w->jointOrder = grow( w->jointOrder, &w->jointOrderCap, w->jointCount + 1, sizeof( int ) );
+	int* jorder = w->jointOrder;
+	int jStart[P_COLORS + 1];
+	{
+		int nj = 0;
+		for ( int color = 0; color < P_OVERFLOW; ++color )
+		{
+			jStart[color] = nj;
+			for ( int j = 0; j < w->jointCount; ++j )
+				if ( w->joints[j].used && w->joints[j].color == color )
+					jorder[nj++] = j;
+		}
+		jStart[P_OVERFLOW] = nj;
+	}
 	// joints in the constraint graph (colours and overflow)
-	for ( int j = 0; j < w->jointCount; ++j )
+	int jointCount = w->jointCount;
+#pragma omp parallel for schedule( static )
+	for ( int j = 0; j < jointCount; ++j )
 		if ( w->joints[j].used && w->joints[j].color != P_NULL )
 			p_prepare_joint( w, w->joints + j, h, inv_h, jointSoftness );
 
+	double tp1 = p_now();
 	float maxAngularSpeed = P_MAX_ROTATION * inv_dt;
 	float minBiasVel = -w->contactSpeed;
-	for ( int i = 0; i < subStepCount; ++i )
+	int bodyCount = w->bodyCount;
+	// One team for all substeps. Within a colour no two constraints share a
+	// dynamic body, so each colour's constraints run in parallel; the serial
+	// overflow constraints run on one thread; implicit barriers separate the
+	// stages exactly where the reference's stage order requires.
+#pragma omp parallel
 	{
-		for ( int b = 0; b < w->bodyCount; ++b )
-			if ( body_awake( w->bodies + b ) )
-				integrate_velocities( w, w->bodies + b, h, w->maximumLinearSpeed, maxAngularSpeed );
-		// warm start
-		for ( int k = 0; k < w->overflowJointCount; ++k )
-			p_warm_start_joint( w, w->joints + w->overflowJoints[k] );
-		for ( int k = 0; k < overflowCount; ++k )
-			warm_start_overflow( w, K + k );
-		for ( int color = 0; color < P_OVERFLOW; ++color )
+		for ( int i = 0; i < subStepCount; ++i )
 		{
-			for ( int j = 0; j < w->jointCount; ++j )
-				if ( w->joints[j].used && w->joints[j].color == color )
-					p_warm_start_joint( w, w->joints + j );
-			for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
-				warm_start_lane( w, K + k );
-		}
-		// solve
-		for ( int k = 0; k < w->overflowJointCount; ++k )
-			p_solve_joint( w, w->joints + w->overflowJoints[k], h, inv_h, 1 );
-		for ( int k = 0; k < overflowCount; ++k )
-			solve_overflow( w, K + k, inv_h, w->maxContactPushSpeed, 1 );
-		for ( int color = 0; color < P_OVERFLOW; ++color )
-		{
-			for ( int j = 0; j < w->jointCount; ++j )
-				if ( w->joints[j].used && w->joints[j].color == color )
-					p_solve_joint( w, w->joints + j, h, inv_h, 1 );
-			for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
-				solve_lane( w, K + k, inv_h, minBiasVel, 1 );
-		}
-		// integrate positions (solver.c:182-200)
-		for ( int b = 0; b < w->bodyCount; ++b )
-		{
-			Body* body = w->bodies + b;
-			if ( !body_awake( body ) )
-				continue;
-			body->dq = integrateRot( body->dq, h * body->w );
-			body->dp = mulAdd( body->dp, h, body->v );
-		}
-		// relax
-		for ( int k = 0; k < w->overflowJointCount; ++k )
-			p_solve_joint( w, w->joints + w->overflowJoints[k], h, inv_h, 0 );
-		for ( int k = 0; k < overflowCount; ++k )
-			solve_overflow( w, K + k, inv_h, w->maxContactPushSpeed, 0 );
-		for ( int color = 0; color < P_OVERFLOW; ++color )
-		{
-			for ( int j = 0; j < w->jointCount; ++j )
-				if ( w->joints[j].used && w->joints[j].color == color )
-					p_solve_joint( w, w->joints + j, h, inv_h, 0 );
-			for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
-				solve_lane( w, K + k, inv_h, minBiasVel, 0 );
+#pragma omp for schedule( static )
+			for ( int b = 0; b < bodyCount; ++b )
+				if ( body_awake( w->bodies + b ) )
+					integrate_velocities( w, w->bodies + b, h, w->maximumLinearSpeed, maxAngularSpeed );
+			// warm start
+#pragma omp single
+			{
+				for ( int k = 0; k < w->overflowJointCount; ++k )
+					p_warm_start_joint( w, w->joints + w->overflowJoints[k] );
+				for ( int k = 0; k < overflowCount; ++k )
+					warm_start_overflow( w, K + k );
+			}
+			for ( int color = 0; color < P_OVERFLOW; ++color )
+			{
+#pragma omp for schedule( static ) nowait
+				for ( int q = jStart[color]; q < jStart[color + 1]; ++q )
+					p_warm_start_joint( w, w->joints + jorder[q] );
+#pragma omp for schedule( static )
+				for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
+					warm_start_lane( w, K + k );
+			}
+			// solve
+#pragma omp single
+			{
+				for ( int k = 0; k < w->overflowJointCount; ++k )
+					p_solve_joint( w, w->joints + w->overflowJoints[k], h, inv_h, 1 );
+				for ( int k = 0; k < overflowCount; ++k )
+					solve_overflow( w, K + k, inv_h, w->maxContactPushSpeed, 1 );
+			}
+			for ( int color = 0; color < P_OVERFLOW; ++color )
+			{
+#pragma omp for schedule( static ) nowait
+				for ( int q = jStart[color]; q < jStart[color + 1]; ++q )
+					p_solve_joint( w, w->joints + jorder[q], h, inv_h, 1 );
+#pragma omp for schedule( static )
+				for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
+					solve_lane( w, K + k, inv_h, minBiasVel, 1 );
+			}
+			// integrate positions (solver.c:182-200)
+#pragma omp for schedule( static )
+			for ( int b = 0; b < bodyCount; ++b )
+			{
+				Body* body = w->bodies + b;
+				if ( !body_awake( body ) )
+					continue;
+				body->dq = integrateRot( body->dq, h * body->w );
+				body->dp = mulAdd( body->dp, h, body->v );
+			}
+			// relax
+#pragma omp single
+			{
+				for ( int k = 0; k < w->overflowJointCount; ++k )
+					p_solve_joint( w, w->joints + w->overflowJoints[k], h, inv_h, 0 );
+				for ( int k = 0; k < overflowCount; ++k )
+					solve_overflow( w, K + k, inv_h, w->maxContactPushSpeed, 0 );
+			}
+			for ( int color = 0; color < P_OVERFLOW; ++color )
+			{
+#pragma omp for schedule( static ) nowait
+				for ( int q = jStart[color]; q < jStart[color + 1]; ++q )
+					p_solve_joint( w, w->joints + jorder[q], h, inv_h, 0 );
+#pragma omp for schedule( static )
+				for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
+					solve_lane( w, K + k, inv_h, minBiasVel, 0 );
+			}
 		}
 	}
+	double tp2 = p_now();
 	// restitution
 	for ( int k = 0; k < overflowCount; ++k )
 		restitution_overflow( w, K + k, w->restitutionThreshold );
 	for ( int color = 0; color < P_OVERFLOW; ++color )
+	{
+#pragma omp parallel for schedule( static )
 		for ( int k = colorStart[color]; k < colorStart[color + 1]; ++k )
 			restitution_lane( w, K + k, w->restitutionThreshold );
+	}
 	// store
 	for ( int k = 0; k < overflowCount; ++k )
 		store_impulses( w, K + k, 0 );
+#pragma omp parallel for schedule( static )
 	for ( int k = overflowCount; k < nk; ++k )
 		store_impulses( w, K + k, 1 );
 
-	// finalize bodies (body id order)
-	for ( int b = 0; b < w->bodyCount; ++b )
+	double tp3 = p_now();
+	// finalize bodies; move events in body id order, one slot per awake body
+	{
+		int ne = 0;
+		for ( int b = 0; b < bodyCount; ++b )
+			if ( body_awake( w->bodies + b ) )
+				w->bodies[b].moveEventIndex = ne++;
+		w->moveEventBodies = grow( w->moveEventBodies, &w->moveEventCap, ne + 1, sizeof( int ) );
+		w->moveEventXf = grow( w->moveEventXf, &w->moveEventXfCap, 4 * ( ne + 1 ), sizeof( float ) );
+		w->moveEventCount = ne;
+	}
+#pragma omp parallel for schedule( dynamic, 512 )
+	for ( int b = 0; b < bodyCount; ++b )
 		if ( body_awake( w->bodies + b ) )
 			finalize_body( w, b, dt, inv_dt );
+	double tp4 = p_now();
 
 	// hit events (solver.c:1758-1818): colours in order, overflow last. Within a
 	// colour the reference follows its colour array (append / swap-remove); this
@@ -846,4 +911,10 @@ void p_solve( World* w, float dt, int subStepCount )
 			}
 		}
 	}
+	double tp5 = p_now();
+	g_portPhase[3] += tp1 - tp0;
+	g_portPhase[4] += tp2 - tp1;
+	g_portPhase[5] += tp3 - tp2;
+	g_portPhase[6] += tp4 - tp3;
+	g_portPhase[7] += tp5 - tp4;
 }

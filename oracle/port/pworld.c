@@ -18,6 +18,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define MAX_WORLDS 64
 static World s_worlds[MAX_WORLDS];
@@ -223,6 +226,8 @@ void orc_destroy_world( int wi )
 	free( w->hitData );
 	free( w->moveEventBodies );
 	free( w->moveEventXf );
+	free( w->constraintOrder );
+	free( w->jointOrder );
 	memset( w, 0, sizeof( *w ) );
 }
 
@@ -743,13 +748,36 @@ typedef struct GridEntry
 	int shape;
 } GridEntry;
 
-static int cmp_grid( const void* x, const void* y )
+// Stable LSD radix sort by cell key (16-bit digits, passes whose digit is
+// the same for every entry skipped). Entries are inserted in shape order, so
+// the result is ordered by (cell, shape).
+static void sort_grid( GridEntry* a, int n )
 {
-	const GridEntry* a = x;
-	const GridEntry* b = y;
-	if ( a->cell != b->cell )
-		return a->cell < b->cell ? -1 : 1;
-	return a->shape - b->shape;
+	if ( n < 2 )
+		return;
+	GridEntry* tmp = malloc( sizeof( GridEntry ) * (size_t)n );
+	int* hist = malloc( sizeof( int ) * 65536 );
+	for ( int pass = 0; pass < 4; ++pass )
+	{
+		int shift = 16 * pass;
+		memset( hist, 0, sizeof( int ) * 65536 );
+		for ( int i = 0; i < n; ++i )
+			hist[( (uint64_t)a[i].cell >> shift ) & 0xffff] += 1;
+		if ( hist[( (uint64_t)a[0].cell >> shift ) & 0xffff] == n )
+			continue;
+		int sum = 0;
+		for ( int d = 0; d < 65536; ++d )
+		{
+			int c = hist[d];
+			hist[d] = sum;
+			sum += c;
+		}
+		for ( int i = 0; i < n; ++i )
+			tmp[hist[( (uint64_t)a[i].cell >> shift ) & 0xffff]++] = a[i];
+		memcpy( a, tmp, sizeof( GridEntry ) * (size_t)n );
+	}
+	free( hist );
+	free( tmp );
 }
 
 static int shape_active( World* w, int s )
@@ -818,53 +846,117 @@ static void update_pairs( World* w )
 	float inv = 1.0f / cell;
 	int* large = NULL;
 	int nl = 0, capl = 0;
-	GridEntry* grid = NULL;
-	int ng = 0, capg = 0;
+	// shapes no larger than a cell go into every cell their fat AABB
+	// touches (at most 4); larger ones are paired against all shapes
+	int* gcount = malloc( sizeof( int ) * (size_t)( ns + 1 ) );
+#pragma omp parallel for schedule( static )
+	for ( int s = 0; s < ns; ++s )
+	{
+		gcount[s] = 0;
+		if ( !shape_active( w, s ) )
+			continue;
+		box2 f = w->shapes[s].fatAABB;
+		if ( f.hi.x - f.lo.x > cell || f.hi.y - f.lo.y > cell )
+			continue;
+		int64_t x0 = (int64_t)floorf( f.lo.x * inv ), x1 = (int64_t)floorf( f.hi.x * inv );
+		int64_t y0 = (int64_t)floorf( f.lo.y * inv ), y1 = (int64_t)floorf( f.hi.y * inv );
+		gcount[s] = (int)( ( x1 - x0 + 1 ) * ( y1 - y0 + 1 ) );
+	}
+	int ng = 0;
+	for ( int s = 0; s < ns; ++s )
+	{
+		int c = gcount[s];
+		gcount[s] = ng;
+		ng += c;
+		if ( c == 0 && shape_active( w, s ) )
+		{
+			large = grow( large, &capl, nl + 1, sizeof( int ) );
+			large[nl++] = s;
+		}
+	}
+	GridEntry* grid = malloc( sizeof( GridEntry ) * (size_t)( ng > 0 ? ng : 1 ) );
+#pragma omp parallel for schedule( static )
 	for ( int s = 0; s < ns; ++s )
 	{
 		if ( !shape_active( w, s ) )
 			continue;
 		box2 f = w->shapes[s].fatAABB;
 		if ( f.hi.x - f.lo.x > cell || f.hi.y - f.lo.y > cell )
-		{
-			large = grow( large, &capl, nl + 1, sizeof( int ) );
-			large[nl++] = s;
 			continue;
-		}
 		int64_t x0 = (int64_t)floorf( f.lo.x * inv ), x1 = (int64_t)floorf( f.hi.x * inv );
 		int64_t y0 = (int64_t)floorf( f.lo.y * inv ), y1 = (int64_t)floorf( f.hi.y * inv );
+		int k = gcount[s];
 		for ( int64_t x = x0; x <= x1; ++x )
 			for ( int64_t y = y0; y <= y1; ++y )
 			{
-				grid = grow( grid, &capg, ng + 1, sizeof( GridEntry ) );
-				grid[ng].cell = (int64_t)( ( (uint64_t)(uint32_t)x << 32 ) | (uint64_t)(uint32_t)y );
-				grid[ng].shape = s;
-				ng += 1;
+				grid[k].cell = (int64_t)( ( (uint64_t)(uint32_t)x << 32 ) | (uint64_t)(uint32_t)y );
+				grid[k].shape = s;
+				k += 1;
 			}
 	}
-	qsort( grid, (size_t)ng, sizeof( GridEntry ), cmp_grid );
-	Cand* cands = NULL;
-	int nc = 0, capc = 0;
-	for ( int i = 0; i < ng; )
+	free( gcount );
+	sort_grid( grid, ng );
+	// cell boundaries, then every cell and every large shape is examined in
+	// parallel into per-thread candidate lists (their order does not matter:
+	// the candidates are sorted by key below)
+	int* cellStart = NULL;
+	int ncell = 0, capcell = 0;
+	for ( int i = 0; i < ng; ++i )
+		if ( i == 0 || grid[i].cell != grid[i - 1].cell )
+		{
+			cellStart = grow( cellStart, &capcell, ncell + 2, sizeof( int ) );
+			cellStart[ncell++] = i;
+		}
+	if ( cellStart )
+		cellStart[ncell] = ng;
+	int nthreads = 1;
+#ifdef _OPENMP
+	nthreads = omp_get_max_threads();
+#endif
+	Cand** tc = calloc( (size_t)nthreads, sizeof( Cand* ) );
+	int* tn = calloc( (size_t)nthreads, sizeof( int ) );
+	int* tcap = calloc( (size_t)nthreads, sizeof( int ) );
+#pragma omp parallel
 	{
-		int j = i;
-		while ( j < ng && grid[j].cell == grid[i].cell )
-			++j;
-		for ( int p = i; p < j; ++p )
-			for ( int q = p + 1; q < j; ++q )
-				consider_pair( w, grid[p].shape, grid[q].shape, &cands, &nc, &capc );
-		i = j;
-	}
-	for ( int i = 0; i < nl; ++i )
-	{
+		int t = 0;
+#ifdef _OPENMP
+		t = omp_get_thread_num();
+#endif
+#pragma omp for schedule( dynamic, 64 )
+		for ( int ci = 0; ci < ncell; ++ci )
+		{
+			int i = cellStart[ci], j = cellStart[ci + 1];
+			for ( int p = i; p < j; ++p )
+				for ( int q = p + 1; q < j; ++q )
+					consider_pair( w, grid[p].shape, grid[q].shape, tc + t, tn + t, tcap + t );
+		}
+		// large-large pairs are visited twice; the sort+unique below drops repeats
+#pragma omp for schedule( dynamic, 1024 )
 		for ( int s = 0; s < ns; ++s )
 		{
-			if ( s == large[i] || !shape_active( w, s ) )
+			if ( !shape_active( w, s ) )
 				continue;
-			// large-large pairs are visited twice; the sort+unique below drops repeats
-			consider_pair( w, large[i], s, &cands, &nc, &capc );
+			for ( int i = 0; i < nl; ++i )
+				if ( s != large[i] )
+					consider_pair( w, large[i], s, tc + t, tn + t, tcap + t );
 		}
 	}
+	Cand* cands = NULL;
+	int nc = 0, capc = 0;
+	for ( int t = 0; t < nthreads; ++t )
+	{
+		if ( tn[t] > 0 )
+		{
+			cands = grow( cands, &capc, nc + tn[t], sizeof( Cand ) );
+			memcpy( cands + nc, tc[t], sizeof( Cand ) * (size_t)tn[t] );
+			nc += tn[t];
+		}
+		free( tc[t] );
+	}
+	free( tc );
+	free( tn );
+	free( tcap );
+	free( cellStart );
 	qsort( cands, (size_t)nc, sizeof( Cand ), cmp_cand );
 	int u = 0;
 	for ( int i = 0; i < nc; ++i )
@@ -1154,6 +1246,36 @@ static void process_state_changes( World* w )
 // ---------------------------------------------------------------------------
 // step (world.c:695-812)
 // ---------------------------------------------------------------------------
+double g_portPhase[8];
+
+double p_now( void )
+{
+	struct timespec t;
+	clock_gettime( CLOCK_MONOTONIC, &t );
+	return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+int orc_thread_count( void )
+{
+#ifdef _OPENMP
+	return omp_get_max_threads();
+#else
+	return 1;
+#endif
+}
+
+void orc_phase_seconds( double* out8 )
+{
+	for ( int i = 0; i < 8; ++i )
+		out8[i] = g_portPhase[i];
+}
+
+void orc_reset_phase_seconds( void )
+{
+	for ( int i = 0; i < 8; ++i )
+		g_portPhase[i] = 0.0;
+}
+
 void orc_world_step( int wi, double timeStep, int subStepCount )
 {
 	World* w = p_world( wi );
@@ -1166,11 +1288,20 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	float dt = (float)timeStep;
 	if ( dt == 0.0f )
 		return;
+	double t0 = p_now();
 	update_pairs( w );
-	for ( int id = 0; id < w->contactCount; ++id )
+	double t1 = p_now();
+	int nc = w->contactCount;
+#pragma omp parallel for schedule( dynamic, 256 )
+	for ( int id = 0; id < nc; ++id )
 		if ( w->contacts[id].used )
 			update_contact( w, w->contacts + id );
+	double t2 = p_now();
 	process_state_changes( w );
+	double t3 = p_now();
+	g_portPhase[0] += t1 - t0;
+	g_portPhase[1] += t2 - t1;
+	g_portPhase[2] += t3 - t2;
 	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
 }
 
