@@ -80,8 +80,9 @@ void p_solve_continuous( World* w, int bodyId )
 		v2 centroid2 = xfPoint( xf2, fastShape->localCentroid );
 		(void)centroid1;
 		(void)centroid2;
-		for ( int si = 0; si < w->shapeCount; ++si )
+		for ( int k = 0; k < w->staticShapeCount; ++k )
 		{
+			int si = w->staticShapes[k];
 			Shape* shape = w->shapes + si;
 			if ( shape->used == 0 || shape->proxyKey == P_NULL || ( shape->proxyKey & 3 ) != BODY_STATIC )
 				continue;

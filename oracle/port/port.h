@@ -292,6 +292,8 @@ typedef struct World
 	int* moveEventBodies;
 	float* moveEventXf;
 	int moveEventCount, moveEventCap, moveEventXfCap;
+	int* staticShapes; // static-body shapes with a proxy, ascending id
+	int staticShapeCount, staticShapeCap;
 	int* constraintOrder; // contact id per constraint slot
 	int constraintOrderCap;
 	int* jointOrder; // graph-colour joints grouped by colour

@@ -227,6 +227,7 @@ void orc_destroy_world( int wi )
 	free( w->moveEventBodies );
 	free( w->moveEventXf );
 	free( w->constraintOrder );
+	free( w->staticShapes );
 	free( w->jointOrder );
 	memset( w, 0, sizeof( *w ) );
 }
@@ -414,6 +415,18 @@ static int create_shape( World* w, int bodyId, const f2d_shape_def* d, const Geo
 		s->fatAABB.hi.y = aabb.hi.y + margin;
 		int proxyId = tree_create_proxy( w->trees + proxyType );
 		s->proxyKey = ( proxyId << 2 ) | proxyType;
+		if ( proxyType == BODY_STATIC )
+		{
+			// candidates of continuous collision, kept in shape-id order
+			w->staticShapes = grow( w->staticShapes, &w->staticShapeCap, w->staticShapeCount + 1, sizeof( int ) );
+			int k = w->staticShapeCount++;
+			while ( k > 0 && w->staticShapes[k - 1] > id )
+			{
+				w->staticShapes[k] = w->staticShapes[k - 1];
+				k -= 1;
+			}
+			w->staticShapes[k] = id;
+		}
 		int force = d->invokeContactCreation != 0 || d->isSensor != 0;
 		if ( proxyType != BODY_STATIC || force )
 			push_move( w, id );
