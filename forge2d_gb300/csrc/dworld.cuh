@@ -104,6 +104,14 @@ struct DScalars
 	int pad[5];
 };
 
+// Solver view of one body: velocity and the substep position/rotation
+// deltas (b2BodyState, body.h:101-113).
+struct BState
+{
+	float vx, vy, w;
+	float dpx, dpy, dqc, dqs;
+};
+
 struct DWorld
 {
 	// capacities

@@ -18,35 +18,31 @@ __device__ __forceinline__ float unwind_angle( float r )
 	return remainderf( r, 2.0f * F2D_PI );
 }
 
-__device__ __forceinline__ void jstate_load( const DWorld& w, int i, fv2& v, float& wv, fv2& dp, frot& dq )
+template <class BA>
+__device__ __forceinline__ void jstate_load( const BA& ba, int i, fv2& v, float& wv, fv2& dp, frot& dq )
 {
-	if ( i < 0 )
-	{
-		v = mk( 0.0f, 0.0f );
-		wv = 0.0f;
-		dp = mk( 0.0f, 0.0f );
-		dq.c = 1.0f;
-		dq.s = 0.0f;
-		return;
-	}
-	float4 a = __ldcg( w.vel + i );
-	float4 d = __ldcg( w.delta + i );
-	v = mk( a.x, a.y );
-	wv = a.z;
-	dp = mk( d.x, d.y );
-	dq.c = d.z;
-	dq.s = d.w;
+	BState s = ba.load( i );
+	v = mk( s.vx, s.vy );
+	wv = s.w;
+	dp = mk( s.dpx, s.dpy );
+	dq.c = s.dqc;
+	dq.s = s.dqs;
 }
 
-__device__ __forceinline__ void jstate_store( const DWorld& w, int i, fv2 v, float wv )
+template <class BA> __device__ __forceinline__ void jstate_store( const BA& ba, int i, fv2 v, float wv )
 {
-	if ( i < 0 )
-		return;
-	__stcg( w.vel + i, make_float4( v.x, v.y, wv, 0.0f ) );
+	BState s;
+	s.vx = v.x;
+	s.vy = v.y;
+	s.w = wv;
+	s.dpx = s.dpy = 0.0f;
+	s.dqc = 1.0f;
+	s.dqs = 0.0f;
+	ba.store( i, s );
 }
 
 // revolute_joint.c:261-287
-__device__ __forceinline__ void joint_warm_start( const DWorld& w, int j )
+template <class BA> __device__ __forceinline__ void joint_warm_start( const DWorld& w, const BA& ba, int j )
 {
 	int2 idx = w.jindex[j];
 	float4 m = w.jprepM[j];
@@ -57,8 +53,8 @@ __device__ __forceinline__ void joint_warm_start( const DWorld& w, int j )
 	fv2 vA, vB, dpA, dpB;
 	float wA, wB;
 	frot dqA, dqB;
-	jstate_load( w, idx.x, vA, wA, dpA, dqA );
-	jstate_load( w, idx.y, vB, wB, dpB, dqB );
+	jstate_load( ba, idx.x, vA, wA, dpA, dqA );
+	jstate_load( ba, idx.y, vB, wB, dpB, dqB );
 	fv2 rA = rrot( dqA, mk( p0.x, p0.y ) );
 	fv2 rB = rrot( dqB, mk( p0.z, p0.w ) );
 	fv2 linearImpulse = mk( imp.x, imp.y );
@@ -67,12 +63,13 @@ __device__ __forceinline__ void joint_warm_start( const DWorld& w, int j )
 	wA -= iA * ( vcross( rA, linearImpulse ) + axialImpulse );
 	vB = vmuladd( vB, mB, linearImpulse );
 	wB += iB * ( vcross( rB, linearImpulse ) + axialImpulse );
-	jstate_store( w, idx.x, vA, wA );
-	jstate_store( w, idx.y, vB, wB );
+	jstate_store( ba, idx.x, vA, wA );
+	jstate_store( ba, idx.y, vB, wB );
 }
 
 // revolute_joint.c:289-455
-__device__ __forceinline__ void joint_solve( const DWorld& w, int j, float h, float inv_h, bool useBias )
+template <class BA>
+__device__ __forceinline__ void joint_solve( const DWorld& w, const BA& ba, int j, float h, float inv_h, bool useBias )
 {
 	int2 idx = w.jindex[j];
 	int flags = w.jflags[j];
@@ -91,8 +88,8 @@ __device__ __forceinline__ void joint_solve( const DWorld& w, int j, float h, fl
 	fv2 vA, vB, dcA, dcB;
 	float wA, wB;
 	frot dqA, dqB;
-	jstate_load( w, idx.x, vA, wA, dcA, dqA );
-	jstate_load( w, idx.y, vB, wB, dcB, dqB );
+	jstate_load( ba, idx.x, vA, wA, dcA, dqA );
+	jstate_load( ba, idx.y, vB, wB, dcB, dqB );
 	float axialMass = p1.w;
 	float deltaAngle = p1.z;
 	bool fixedRotation = ( iA + iB == 0.0f );
@@ -195,8 +192,8 @@ __device__ __forceinline__ void joint_solve( const DWorld& w, int j, float h, fl
 	}
 	__stcg( w.jimp + j, make_float4( linearImpulse.x, linearImpulse.y, springImpulse, motorImpulse ) );
 	__stcg( w.jimp2 + j, make_float2( lowerImpulse, upperImpulse ) );
-	jstate_store( w, idx.x, vA, wA );
-	jstate_store( w, idx.y, vB, wB );
+	jstate_store( ba, idx.x, vA, wA );
+	jstate_store( ba, idx.y, vB, wB );
 }
 
 void launch_prepare_joints( DWorld& w, StepScratch& s, cudaStream_t st, float h, float inv_h, Soft jointSoft );

@@ -33,6 +33,7 @@ struct StepScratch
 	int shapeIdBits;
 	int solverBlocks;  // persistent solver grid (co-resident)
 	int solverThreads;
+	int clusterCapacity; // bodies the cluster solver takes (0: cooperative solver only)
 	cudaEvent_t evSolveStart; // recorded right before the cooperative solver launch when non-null
 };
 
@@ -43,3 +44,4 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
 void launch_joint_ops( DWorld& w, cudaStream_t st );
 int solver_max_blocks( int threads );
+int solver_cluster_capacity();

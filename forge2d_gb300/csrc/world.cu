@@ -95,6 +95,10 @@ struct HostWorld
 	// the broadphase must re-sort its leaf order at the next step
 	bool forceRebuild = true;
 
+	// solve on the grid-wide cooperative kernel even when the world fits a
+	// thread-block cluster (F2D_NO_CLUSTER_SOLVER set at world creation)
+	bool gridSolverOnly = false;
+
 	// device staging of the bulk body reader (12 floats per body)
 	float* packedBodies = nullptr;
 	int packedCap = 0;
@@ -167,6 +171,7 @@ static void alloc_scratch( HostWorld* W )
 	d.pairKeyBits = bits;
 	s.solverThreads = 512;
 	s.solverBlocks = solver_max_blocks( 512 );
+	s.clusterCapacity = W->gridSolverOnly ? 0 : solver_cluster_capacity();
 }
 
 static void grow_bodies( HostWorld* W, int cap )
@@ -548,6 +553,9 @@ static void flush_uploads( HostWorld* W )
 		W->pendingJoints.clear();
 		W->graphDirty = true;
 	}
+	// counts are kernel parameters of the captured step: a change re-captures
+	if ( W->d.bodyCount != W->bodyCount || W->d.shapeCount != W->shapeCount || W->d.jointCount != W->jointCount )
+		W->graphDirty = true;
 	W->d.bodyCount = W->bodyCount;
 	W->d.shapeCount = W->shapeCount;
 	W->d.jointCount = W->jointCount;
@@ -577,6 +585,7 @@ extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
 	W->used = true;
 	W->generation = (uint16_t)( gen + 1 );
 	W->index = slot;
+	W->gridSolverOnly = getenv( "F2D_NO_CLUSTER_SOLVER" ) != nullptr;
 	DWorld& d = W->d;
 	memset( &d, 0, sizeof( d ) );
 	d.gravity = mk( (float)def->gravityX, (float)def->gravityY );

@@ -22,9 +22,17 @@ from test_oracle_golden import CASES, GOLD, STATS_CASES, frame_stats, replay
 pytestmark = pytest.mark.gpu
 
 
-def gpu_world(gpu_lib, wkw):
+def gpu_world(gpu_lib, wkw, solver="auto"):
+    """solver "grid" forces the grid-wide cooperative solver kernel (the one
+    large worlds use) instead of the thread-block-cluster one."""
+    import os
     from forge2d_gb300.world import GpuWorld
-    return GpuWorld(scenes.world_def(**wkw))
+    if solver == "grid":
+        os.environ["F2D_NO_CLUSTER_SOLVER"] = "1"
+    try:
+        return GpuWorld(scenes.world_def(**wkw))
+    finally:
+        os.environ.pop("F2D_NO_CLUSTER_SOLVER", None)
 
 
 def assert_bodies_equal(g, p, frame):
@@ -48,9 +56,10 @@ NATIVE = [
 ]
 
 
+@pytest.mark.parametrize("solver", ["auto", "grid"])
 @pytest.mark.parametrize("name,wkw,scene,kw,frames,every", NATIVE, ids=[n[0] for n in NATIVE])
-def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, frames, every):
-    g = gpu_world(gpu_lib, wkw)
+def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, frames, every, solver):
+    g = gpu_world(gpu_lib, wkw, solver)
     p = port_lib.PortWorld(scenes.world_def(**wkw))
     scenes.build(g, scene, **kw)
     scenes.build(p, scene, **kw)
