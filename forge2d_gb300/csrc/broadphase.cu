@@ -19,41 +19,11 @@
 //      which contact ids are then drawn from the LIFO id pool.
 #include "dscan.cuh"
 #include "dsort.cuh"
+#include "dtree.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
 
 #define BP_THREADS 256
-#define WIDE 32
-#define WIDE_MAX_LEVELS 6
-
-// Level sizes of the implicit tree over n leaves: level 0 holds the leaves,
-// level l has ceil(count[l-1] / 32) nodes; all levels share nodeBox, level l
-// starting at offset[l]. top is the root's level (0 when n == 1).
-struct WideLevels
-{
-	int count[WIDE_MAX_LEVELS + 1];
-	int offset[WIDE_MAX_LEVELS + 1];
-	int top;
-};
-
-__device__ __forceinline__ WideLevels wide_levels( int n )
-{
-	WideLevels L;
-	L.count[0] = n;
-	L.offset[0] = 0;
-	int off = n, c = n, k = 0;
-	while ( c > 1 && k < WIDE_MAX_LEVELS )
-	{
-		c = ( c + WIDE - 1 ) / WIDE;
-		k += 1;
-		L.count[k] = c;
-		L.offset[k] = off;
-		off += c;
-	}
-	L.top = k;
-	return L;
-}
-
 // refit counters exist for the nodes of levels >= 2
 __device__ __forceinline__ int wide_counter( const WideLevels& L, int level, int node )
 {
@@ -378,7 +348,7 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 // b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup.
 __device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int typeI, int bi, int sj )
 {
-	if ( sj == si )
+	if ( sj == si || ( w.subCount > 0 && w.shapeSub[si] != w.shapeSub[sj] ) )
 		return;
 	int fj = w.sflags[sj];
 	int typeJ = w.proxyKey[sj] & 3;

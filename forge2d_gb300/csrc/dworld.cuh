@@ -131,6 +131,7 @@ struct DWorld
 	float contactHertz, contactDampingRatio, maxContactPushSpeed, maxLinearSpeed;
 	float jointHertz, jointDampingRatio;
 	int enableSleep, enableContinuous, enableWarmStarting;
+	int subCount; // batched form: independent sub-worlds (0 = one world)
 
 	// ---------------- bodies (by body id) ----------------
 	float4* xf;			// p.x p.y q.c q.s
@@ -142,6 +143,7 @@ struct DWorld
 	float4* massv;		// invMass invInertia minExtent maxExtent
 	float4* damp;		// linearDamping angularDamping gravityScale sleepThreshold
 	float4* force;		// force.x force.y torque sleepTime
+	float2* bodyGravity; // gravity of the body's sub-world (batched form, subCount > 0)
 	int* bflags;
 	int* headShape;
 	int* headJoint; // joint key list: (jointId << 1) | edge
@@ -161,6 +163,7 @@ struct DWorld
 	int* sflags;
 	int* proxyKey;
 	int* nextShape;
+	int* shapeSub; // sub-world of the owning body (batched form)
 
 	// ---------------- contacts (by contact id) ----------------
 	int2* cshape; // shapeA shapeB

@@ -6,6 +6,7 @@
 // (b2FinalizeBodiesTask), :1758-1913 (hit events, enlarged proxies).
 #include "dnarrow.cuh"
 #include "dtoi.cuh"
+#include "dtree.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
 
@@ -229,6 +230,9 @@ __device__ __forceinline__ bool joint_allows( const DWorld& w, int ia, int ib )
 
 // solver.c:390-541: one thread per fast body; candidate static shapes are
 // visited in shape-id order
+#define CCD_LIST_MAX 64
+#define CCD_CANDIDATES 32
+
 __global__ void k_continuous( DWorld w )
 {
 	int n = w.sc->fastCount;
@@ -262,23 +266,23 @@ __global__ void k_continuous( DWorld w )
 			w.aabb[fs] = box_to4( box2 );
 			if ( sff & SF_SENSOR )
 				continue;
-			for ( int k = 0; k < w.staticCount; ++k )
-			{
-				int ss = w.staticShapes[k];
+			// b2ContinuousQueryCallback (solver.c:196-388) for one static shape
+			auto consider = [&]( int ss ) {
 				int sfs = w.sflags[ss];
 				if ( ( sfs & SF_USED ) == 0 )
-					continue;
+					return;
 				if ( !box_overlaps( box_from4( w.fat[ss] ), box ) )
-					continue;
+					return;
 				int sb = w.shapeBody[ss];
-				if ( ss == fs || sb == b || ( sfs & SF_SENSOR ) )
-					continue;
+				if ( ss == fs || sb == b || ( sfs & SF_SENSOR ) ||
+					 ( w.subCount > 0 && w.shapeSub[ss] != w.shapeSub[fs] ) )
+					return;
 				if ( !filters_collide( w, fs, ss ) )
-					continue;
+					return;
 				if ( w.bflags[sb] & BF_BULLET )
-					continue;
+					return;
 				if ( !joint_allows( w, b, sb ) )
-					continue;
+					return;
 				const float4* gs = w.geom + (size_t)ss * GEOM_F4;
 				DProxy pa = make_proxy( gs, shape_type( sfs ) );
 				DProxy pb = make_proxy( gf, tf );
@@ -312,6 +316,43 @@ __global__ void k_continuous( DWorld w )
 					if ( 0.0f < f && f < fraction )
 						fraction = f;
 				}
+			};
+			// candidates in shape-id order: the static list when it is short,
+			// else the tree's static leaves overlapping the sweep box
+			bool scanList = w.staticCount <= CCD_LIST_MAX;
+			int cand[CCD_CANDIDATES];
+			int nc = 0;
+			if ( !scanList )
+			{
+				bool overflow = false;
+				bool done = tree_query( w, w.sc->treeLeafCount, box, [&]( int leaf ) {
+					int ss = w.leafShape[leaf];
+					if ( ( w.proxyKey[ss] & 3 ) != 0 )
+						return;
+					if ( nc == CCD_CANDIDATES )
+					{
+						overflow = true;
+						return;
+					}
+					int k = nc++;
+					while ( k > 0 && cand[k - 1] > ss )
+					{
+						cand[k] = cand[k - 1];
+						k -= 1;
+					}
+					cand[k] = ss;
+				} );
+				scanList = overflow || !done;
+			}
+			if ( scanList )
+			{
+				for ( int k = 0; k < w.staticCount; ++k )
+					consider( w.staticShapes[k] );
+			}
+			else
+			{
+				for ( int k = 0; k < nc; ++k )
+					consider( cand[k] );
 			}
 		}
 		if ( fraction < 1.0f )

@@ -772,7 +772,13 @@ __device__ __forceinline__ void integrate_velocity( const DWorld& w, int b, cons
 	float linearDamping = 1.0f / ( 1.0f + h * dmp.x );
 	float angularDamping = 1.0f / ( 1.0f + h * dmp.y );
 	float gravityScale = m.x > 0.0f ? dmp.z : 0.0f;
-	fv2 lvd = vadd( vscale( h * m.x, mk( f.x, f.y ) ), vscale( h * gravityScale, p.gravity ) );
+	fv2 g = p.gravity;
+	if ( w.subCount > 0 )
+	{
+		float2 gb = w.bodyGravity[b];
+		g = mk( gb.x, gb.y );
+	}
+	fv2 lvd = vadd( vscale( h * m.x, mk( f.x, f.y ) ), vscale( h * gravityScale, g ) );
 	float avd = h * m.y * f.z;
 	v = vmuladd( lvd, linearDamping, v );
 	wv = avd + angularDamping * wv;
@@ -851,6 +857,40 @@ __device__ __forceinline__ void store_manifold_global( const DWorld& w, int k, b
 	float2 tot = __ldcg( w.kTot + k );
 	float4 misc = __ldcg( w.kMisc + k );
 	store_manifold( w, k, imp, tot, misc.w, w.kP1[k].w, w.kP2[k].w, __float_as_int( w.kSoft[k].w ), lane );
+}
+
+// Colour-c constraint slots beyond the register-resident first stride of
+// slots: consecutive threads take consecutive slots (coalesced row loads);
+// their impulses go through the constraint rows between stages.
+template <class BA>
+__device__ __forceinline__ void colour_lanes_extra( const DWorld& w, const BA& ba, int c, const int* sStart,
+													const int* sCount, int novf, int tid, int stride, int kind,
+													const SolveParams& p )
+{
+	int lo = max( sStart[c], novf + stride ), hi = sStart[c] + sCount[c];
+	for ( int k = lo + tid; k < hi; k += stride )
+	{
+		Lane L;
+		if ( kind == 0 )
+		{
+			// warm start reads no softness or point rows and changes no impulse
+			L.idx = w.kIndex[k];
+			L.ms = w.kMass[k];
+			L.nm = w.kNormal[k];
+			L.misc = __ldcg( w.kMisc + k );
+			L.imp = __ldcg( w.kImp + k );
+			L.an[0] = w.kAnch1[k];
+			L.an[1] = w.kAnch2[k];
+			lane_warm( ba, L );
+			continue;
+		}
+		lane_load( w, k, L );
+		lane_op( ba, L, kind, p );
+		if ( kind == 3 )
+			__stcg( w.kImp + k, L.imp );
+		else
+			lane_store( w, k, L );
+	}
 }
 
 // The persistent solver. Graph-colour constraint slots (after the overflow
@@ -956,17 +996,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 				joint_colour_stage( w, gb, c, kind, p, gtid, gstride, jointSlots, sJStart );
 				if ( col0 == c )
 					lane_op( gb, L0, kind, p );
-				for ( int r = r0 + gstride; r < nColour; r += gstride )
-				{
-					int k = novf + r;
-					if ( k >= sStart[c] && k < sStart[c] + sCount[c] )
-					{
-						Lane L;
-						lane_load( w, k, L );
-						lane_op( gb, L, kind, p );
-						lane_store( w, k, L );
-					}
-				}
+				colour_lanes_extra( w, gb, c, sStart, sCount, novf, gtid, gstride, kind, p );
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
@@ -987,17 +1017,7 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 			continue;
 		if ( col0 == c )
 			lane_op( gb, L0, 3, p );
-		for ( int r = r0 + gstride; r < nColour; r += gstride )
-		{
-			int k = novf + r;
-			if ( k >= sStart[c] && k < sStart[c] + sCount[c] )
-			{
-				Lane L;
-				lane_load( w, k, L );
-				lane_op( gb, L, 3, p );
-				lane_store( w, k, L );
-			}
-		}
+		colour_lanes_extra( w, gb, c, sStart, sCount, novf, gtid, gstride, 3, p );
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
@@ -1007,8 +1027,8 @@ __global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolvePara
 	if ( col0 >= 0 )
 		store_manifold( w, novf + r0, L0.imp, L0.tot, L0.misc.w, L0.pt[0].w, L0.pt[1].w,
 						__float_as_int( L0.sf.w ), true );
-	for ( int r = r0 + gstride; r < nColour; r += gstride )
-		store_manifold_global( w, novf + r, true );
+	for ( int k = novf + gstride + gtid; k < novf + nColour; k += gstride )
+		store_manifold_global( w, k, true );
 }
 
 // ---------------------------------------------------------------------------
@@ -1037,7 +1057,13 @@ __device__ __forceinline__ void integrate_velocity_smem( const DWorld& w, int b,
 	float linearDamping = 1.0f / ( 1.0f + h * dmp.x );
 	float angularDamping = 1.0f / ( 1.0f + h * dmp.y );
 	float gravityScale = m.x > 0.0f ? dmp.z : 0.0f;
-	fv2 lvd = vadd( vscale( h * m.x, mk( f.x, f.y ) ), vscale( h * gravityScale, p.gravity ) );
+	fv2 g = p.gravity;
+	if ( w.subCount > 0 )
+	{
+		float2 gb = w.bodyGravity[b];
+		g = mk( gb.x, gb.y );
+	}
+	fv2 lvd = vadd( vscale( h * m.x, mk( f.x, f.y ) ), vscale( h * gravityScale, g ) );
 	float avd = h * m.y * f.z;
 	v = vmuladd( lvd, linearDamping, v );
 	wv = avd + angularDamping * wv;
@@ -1058,25 +1084,6 @@ __device__ __forceinline__ void integrate_velocity_smem( const DWorld& w, int b,
 	if ( capped )
 		w.bflags[b] = flags | BF_SPEED_CAPPED;
 	v4 = make_float4( v.x, v.y, wv, 0.0f );
-}
-
-// colour-c slots owned by this thread beyond the register-resident one
-template <class BA>
-__device__ __forceinline__ void colour_lanes_extra( const DWorld& w, const BA& ba, int c, const int* sStart,
-													const int* sCount, int novf, int nColour, int r0, int stride,
-													int kind, const SolveParams& p )
-{
-	for ( int r = r0 + stride; r < nColour; r += stride )
-	{
-		int k = novf + r;
-		if ( k >= sStart[c] && k < sStart[c] + sCount[c] )
-		{
-			Lane L;
-			lane_load( w, k, L );
-			lane_op( ba, L, kind, p );
-			lane_store( w, k, L );
-		}
-	}
 }
 
 __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, SolveParams p, const int* jointSlots,
@@ -1190,7 +1197,7 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 				joint_colour_stage( w, cb, c, kind, p, tid, stride, jointSlots, sJStart );
 				if ( col0 == c )
 					lane_op( cb, L0, kind, p );
-				colour_lanes_extra( w, cb, c, sStart, sCount, novf, nColour, r0, stride, kind, p );
+				colour_lanes_extra( w, cb, c, sStart, sCount, novf, tid, stride, kind, p );
 				cl.sync();
 			}
 		}
@@ -1209,7 +1216,7 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 			continue;
 		if ( col0 == c )
 			lane_op( cb, L0, 3, p );
-		colour_lanes_extra( w, cb, c, sStart, sCount, novf, nColour, r0, stride, 3, p );
+		colour_lanes_extra( w, cb, c, sStart, sCount, novf, tid, stride, 3, p );
 		cl.sync();
 	}
 	// body rows back to the device, impulses into the manifolds
@@ -1227,8 +1234,8 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 	if ( col0 >= 0 )
 		store_manifold( w, novf + r0, L0.imp, L0.tot, L0.misc.w, L0.pt[0].w, L0.pt[1].w,
 						__float_as_int( L0.sf.w ), true );
-	for ( int r = r0 + stride; r < nColour; r += stride )
-		store_manifold_global( w, novf + r, true );
+	for ( int k = novf + stride + tid; k < novf + nColour; k += stride )
+		store_manifold_global( w, k, true );
 	// no block leaves while another may still address its shared memory
 	cl.sync();
 }

@@ -63,6 +63,8 @@ struct HostWorld
 
 	// ---- host mirrors (same layout as the device rows) ----
 	std::vector<float4> xf, vel, delta, sweep0, massv, damp, force;
+	std::vector<float2> bgrav;
+	std::vector<int> bsub;
 	std::vector<float2> center, localCenter;
 	std::vector<int> bflags, headShape, headJoint, jointCountB;
 	std::vector<uint16_t> bgen;
@@ -74,7 +76,7 @@ struct HostWorld
 
 	std::vector<float4> geom, aabb, fat, mat;
 	std::vector<unsigned long long> cat, mask;
-	std::vector<int> group, shapeBody, sflags, proxyKey, nextShape;
+	std::vector<int> group, shapeBody, sflags, proxyKey, nextShape, ssub;
 	std::vector<float> density;
 	std::vector<uint16_t> sgen;
 	std::vector<HShapeGeom> hgeomv;
@@ -94,6 +96,9 @@ struct HostWorld
 
 	// the broadphase must re-sort its leaf order at the next step
 	bool forceRebuild = true;
+
+	// batched form: gravity of the sub-world bodies are created into
+	float2 subGravity = { 0.0f, 0.0f };
 
 	// solve on the grid-wide cooperative kernel even when the world fits a
 	// thread-block cluster (F2D_NO_CLUSTER_SOLVER set at world creation)
@@ -186,6 +191,7 @@ static void grow_bodies( HostWorld* W, int cap )
 	dgrow( d.localCenter, o, cap );
 	dgrow( d.massv, o, cap );
 	dgrow( d.damp, o, cap );
+	dgrow( d.bodyGravity, o, cap );
 	dgrow( d.force, o, cap );
 	dgrow( d.bflags, o, cap );
 	dgrow( d.headShape, o, cap );
@@ -257,6 +263,7 @@ static void grow_shapes( HostWorld* W, int cap )
 	dgrow( d.mask, o, cap );
 	dgrow( d.group, o, cap );
 	dgrow( d.shapeBody, o, cap );
+	dgrow( d.shapeSub, o, cap );
 	dgrow( d.sflags, o, cap );
 	dgrow( d.proxyKey, o, cap );
 	dgrow( d.nextShape, o, cap );
@@ -430,6 +437,7 @@ static void upload_body_rows( HostWorld* W, int lo, int hi )
 	up( d.localCenter, W->localCenter, lo, hi, st );
 	up( d.massv, W->massv, lo, hi, st );
 	up( d.damp, W->damp, lo, hi, st );
+	up( d.bodyGravity, W->bgrav, lo, hi, st );
 	up( d.force, W->force, lo, hi, st );
 	up( d.bflags, W->bflags, lo, hi, st );
 	up( d.headShape, W->headShape, lo, hi, st );
@@ -449,6 +457,7 @@ static void upload_shape_rows( HostWorld* W, int lo, int hi )
 	up( d.mask, W->mask, lo, hi, st );
 	up( d.group, W->group, lo, hi, st );
 	up( d.shapeBody, W->shapeBody, lo, hi, st );
+	up( d.shapeSub, W->ssub, lo, hi, st );
 	up( d.sflags, W->sflags, lo, hi, st );
 	up( d.proxyKey, W->proxyKey, lo, hi, st );
 	up( d.nextShape, W->nextShape, lo, hi, st );
@@ -624,7 +633,7 @@ static void free_world( HostWorld* W )
 	(void)ptrs;
 	// free every device array
 #define F( p ) dfree( d.p )
-	F( xf ); F( vel ); F( delta ); F( center ); F( sweep0 ); F( localCenter ); F( massv ); F( damp ); F( force );
+	F( xf ); F( vel ); F( delta ); F( center ); F( sweep0 ); F( localCenter ); F( massv ); F( damp ); F( force ); F( bodyGravity ); F( shapeSub );
 	F( bflags ); F( headShape ); F( headJoint ); F( jointCountB ); F( colorMask ); F( colorLock );
 	F( geom ); F( aabb ); F( fat ); F( mat ); F( cat ); F( mask ); F( group ); F( shapeBody ); F( sflags );
 	F( proxyKey ); F( nextShape ); F( cshape ); F( cbody ); F( cflags ); F( ccolor ); F( coverflowIndex ); F( cmat );
@@ -737,6 +746,8 @@ extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def*
 	vset( W->sweep0, id, make_float4( p.x, p.y, q.c, q.s ) );
 	vset( W->localCenter, id, make_float2( 0.0f, 0.0f ) );
 	vset( W->massv, id, make_float4( 0.0f, 0.0f, F2D_HUGE, 0.0f ) );
+	vset( W->bgrav, id, W->d.subCount > 0 ? W->subGravity : make_float2( 0.0f, 0.0f ) );
+	vset( W->bsub, id, W->d.subCount > 0 ? W->d.subCount - 1 : 0 );
 	vset( W->damp, id,
 		  make_float4( (float)def->linearDamping, (float)def->angularDamping, (float)def->gravityScale,
 					   (float)def->sleepThreshold ) );
@@ -914,6 +925,7 @@ static int create_shape( HostWorld* W, int b, const f2d_shape_def* def, const HS
 	vset( W->mask, id, (unsigned long long)def->maskBits );
 	vset( W->group, id, def->groupIndex );
 	vset( W->shapeBody, id, b );
+	vset( W->ssub, id, W->bsub[b] );
 	int flags = SF_USED | ( g.type << SF_TYPE_SHIFT );
 	if ( def->isSensor )
 		flags |= SF_SENSOR;
@@ -1343,6 +1355,23 @@ extern "C" F2D_API void f2d_world_set_gravity( int32_t worldId, double x, double
 		return;
 	W->d.gravity = mk( (float)x, (float)y );
 	W->graphDirty = true;
+}
+
+extern "C" F2D_API int32_t f2d_world_begin_subworld( int32_t worldId, double gravityX, double gravityY )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return -1;
+	W->subGravity = make_float2( (float)gravityX, (float)gravityY );
+	W->d.subCount += 1;
+	W->graphDirty = true;
+	return W->d.subCount - 1;
+}
+
+extern "C" F2D_API int32_t f2d_world_subworld_count( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	return W ? W->d.subCount : 0;
 }
 
 extern "C" F2D_API void f2d_world_get_gravity( int32_t worldId, double* x, double* y )

@@ -83,6 +83,8 @@ _SIGS = [
     ("f2d_world_sync", _i, [_i]),
     ("f2d_world_set_gravity", None, [_i, _d, _d]),
     ("f2d_world_get_gravity", None, [_i, _P(_d), _P(_d)]),
+    ("f2d_world_begin_subworld", _i, [_i, _d, _d]),
+    ("f2d_world_subworld_count", _i, [_i]),
     ("f2d_world_enable_sleeping", None, [_i, _i]),
     ("f2d_world_is_sleeping_enabled", _i, [_i]),
     ("f2d_world_enable_continuous", None, [_i, _i]),

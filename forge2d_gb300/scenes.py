@@ -19,6 +19,8 @@ Scenes:
                       chains hanging from static anchors.
 * ``joint_gallery`` -- revolute limits, motors, springs, dynamic-dynamic
                       hinges and collideConnected joints.
+* ``batched``      -- thousands of independent sub-worlds (pyramids, piles,
+                      chains) with tilted gravity, stepped as one world.
 """
 from __future__ import annotations
 
@@ -241,6 +243,62 @@ def joint_gallery(b, copies=4):
                                        collideConnected=1))
 
 
+def batched(b, worlds=4096, seed=7, tile=220.0, columns=64):
+    """BASELINE config 4: ``worlds`` independent sub-worlds of uneven size,
+    each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
+    (20-500 shapes with the config-2 mix, in a U container sized to the
+    count) or a revolute chain (10-100 links), with gravity (0, -10) tilted
+    by U[-15, 15] degrees. World k sits in its own ``tile`` x ``tile`` cell of
+    a ``columns``-wide grid; sub-worlds never interact even when bodies
+    leave their cell. The builder needs ``begin_subworld(gx, gy)``."""
+    rng = np.random.default_rng(seed)
+    kinds = rng.integers(0, 3, worlds)
+    tilts = np.radians(rng.uniform(-15.0, 15.0, worlds))
+    sizes = rng.random(worlds)
+    seeds = rng.integers(0, 2 ** 31 - 1, worlds)
+    for k in range(worlds):
+        t = float(tilts[k])
+        b.begin_subworld(10.0 * math.sin(t), -10.0 * math.cos(t))
+        ox = (k % columns) * tile
+        oy = (k // columns) * tile
+        if kinds[k] == 0:
+            rows = 5 + int(sizes[k] * 26)
+            g = b.create_body(body_def(type=STATIC, positionX=ox, positionY=oy - 1.0))
+            b.create_box(g, shape_def(), 0.5 * rows + 10.0, 1.0)
+            pyramid(b, rows=rows, x0=ox - 0.5 * (rows - 1), y0=oy, ground=False)
+        elif kinds[k] == 1:
+            n = 20 + int(sizes[k] * 481)
+            width = max(8.0, 1.6 * math.sqrt(n))
+            height = 2.5 * n / width + 4.0
+            w0 = b.create_body(body_def(type=STATIC, positionX=ox, positionY=oy))
+            sub = _PileOffset(b, ox, oy)
+            pile(sub, count=n, seed=int(seeds[k]), width=width, height=height, with_container=False)
+            hw = 0.5 * width
+            sd = shape_def()
+            b.create_box(w0, sd, hw + 2.0, 1.0, 0.0, -1.0, 1.0, 0.0, 0.0)
+            b.create_box(w0, sd, 1.0, height, -hw - 1.0, height, 1.0, 0.0, 0.0)
+            b.create_box(w0, sd, 1.0, height, hw + 1.0, height, 1.0, 0.0, 0.0)
+        else:
+            links = 10 + int(sizes[k] * 91)
+            chain(b, ox - 0.25 * links, oy + 0.6 * tile, links=links)
+
+
+class _PileOffset:
+    """Builder proxy that shifts every body created through it by (ox, oy)."""
+
+    def __init__(self, b, ox, oy):
+        self.b, self.ox, self.oy = b, ox, oy
+
+    def create_body(self, d):
+        d = dict(d)
+        d["positionX"] = d.get("positionX", 0.0) + self.ox
+        d["positionY"] = d.get("positionY", 0.0) + self.oy
+        return self.b.create_body(d)
+
+    def __getattr__(self, name):
+        return getattr(self.b, name)
+
+
 def build(b, name, **kw):
     if name == "pyramid":
         return pyramid(b, **kw)
@@ -250,4 +308,6 @@ def build(b, name, **kw):
         return pyramids_chains(b, **kw)
     if name == "joint_gallery":
         return joint_gallery(b, **kw)
+    if name == "batched":
+        return batched(b, **kw)
     raise ValueError(name)

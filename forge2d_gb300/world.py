@@ -124,6 +124,9 @@ class GpuWorld:
         ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def begin_subworld(self, gx, gy):
+        return self.lib.f2d_world_begin_subworld(self.id, gx, gy)
+
     # stepping ---------------------------------------------------------
     def step(self, dt=1.0 / 60.0, substeps=4):
         return self.lib.f2d_world_step(self.id, dt, substeps)

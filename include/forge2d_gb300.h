@@ -159,6 +159,15 @@ F2D_API int32_t f2d_world_is_sleeping_enabled( int32_t worldId );
 F2D_API void f2d_world_enable_continuous( int32_t worldId, int32_t enabled );
 F2D_API int32_t f2d_world_is_continuous_enabled( int32_t worldId );
 
+/* ---- batched form (no reference counterpart) ---------------------------
+ * Thousands of independent worlds advance together as sub-worlds of one
+ * world: every step phase, including the persistent solver kernel, runs once
+ * for all of them. Bodies created after f2d_world_begin_subworld belong to
+ * the new sub-world and feel its gravity; shapes of different sub-worlds
+ * never make contacts. Returns the sub-world index, -1 for an invalid world. */
+F2D_API int32_t f2d_world_begin_subworld( int32_t worldId, double gravityX, double gravityY );
+F2D_API int32_t f2d_world_subworld_count( int32_t worldId );
+
 /* ---- bodies ------------------------------------------------------------- */
 
 /* RawBox2D.createBody (raw_box2d.dart:71; raw_box2d_ffi.dart:135 -> b2CreateBody). */

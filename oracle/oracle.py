@@ -334,6 +334,13 @@ class PortWorld(_CpuWorld):
             lib.orc_set_contact_plan.argtypes = [C.c_int, _P(C.c_int), C.c_int]
         super().__init__(world_def, workers)
 
+    def begin_subworld(self, gx, gy):
+        """Batched form: later bodies form a new sub-world with this gravity."""
+        fn = PortWorld._lib.orc_begin_subworld
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_int, C.c_double, C.c_double]
+        return fn(self.w, gx, gy)
+
     def set_contact_plan(self, plan: np.ndarray):
         """Parity mode: contacts created during the next step take the given
         ids. ``plan`` rows are (contactId, shapeIdA, shapeIdB)."""

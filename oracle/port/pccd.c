@@ -88,7 +88,7 @@ void p_solve_continuous( World* w, int bodyId )
 				continue;
 			if ( boxOverlaps( shape->fatAABB, box ) == 0 )
 				continue;
-			if ( si == fs || shape->bodyId == fastShape->bodyId || shape->isSensor )
+			if ( si == fs || shape->bodyId == fastShape->bodyId || shape->isSensor || shape->sub != fastShape->sub )
 				continue;
 			if ( should_collide_filters( fastShape, shape ) == 0 )
 				continue;

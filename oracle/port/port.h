@@ -87,6 +87,8 @@ typedef struct Body
 	float invMass, invInertia;
 	float minExtent, maxExtent;
 	float linearDamping, angularDamping, gravityScale;
+	v2 gravity; // gravity of the body's sub-world (the world's when none)
+	int sub;	// sub-world index
 	float mass, inertia;
 	int isBullet, isSpeedCapped, allowFastRotation, isFast, enlargeAABB, fixedRotation;
 	// state (body.h:101-113)
@@ -119,6 +121,7 @@ typedef struct Shape
 	int groupIndex;
 	int isSensor, enableContactEvents, enableHitEvents, enableSensorEvents, enablePreSolveEvents;
 	box2 aabb, fatAABB;
+	int sub; // sub-world of the owning body
 	int enlarged;
 	int moved; // in the move buffer (broad_phase.h:74-82)
 	int proxyKey;
@@ -292,6 +295,10 @@ typedef struct World
 	int* moveEventBodies;
 	float* moveEventXf;
 	int moveEventCount, moveEventCap, moveEventXfCap;
+	// batched form: independent sub-worlds in one world, each with its own
+	// gravity; shapes of different sub-worlds never interact
+	int subCount; // 0 = no sub-worlds (one world, world gravity)
+	v2 subGravity;
 	int* staticShapes; // static-body shapes with a proxy, ascending id
 	int staticShapeCount, staticShapeCap;
 	int* constraintOrder; // contact id per constraint slot

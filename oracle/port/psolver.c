@@ -548,7 +548,7 @@ static void integrate_velocities( World* w, Body* b, float h, float maxLinearSpe
 	float linearDamping = 1.0f / ( 1.0f + h * b->linearDamping );
 	float angularDamping = 1.0f / ( 1.0f + h * b->angularDamping );
 	float gravityScale = b->invMass > 0.0f ? b->gravityScale : 0.0f;
-	v2 lvd = add( mulSV( h * b->invMass, b->force ), mulSV( h * gravityScale, w->gravity ) );
+	v2 lvd = add( mulSV( h * b->invMass, b->force ), mulSV( h * gravityScale, w->subCount > 0 ? b->gravity : w->gravity ) );
 	float avd = h * b->invInertia * b->torque;
 	v = mulAdd( lvd, linearDamping, v );
 	wv = avd + angularDamping * wv;

@@ -273,6 +273,8 @@ int orc_create_body( int wi, const f2d_body_def* d )
 	b->linearDamping = (float)d->linearDamping;
 	b->angularDamping = (float)d->angularDamping;
 	b->gravityScale = (float)d->gravityScale;
+	b->sub = w->subCount > 0 ? w->subCount - 1 : 0;
+	b->gravity = w->subCount > 0 ? w->subGravity : w->gravity;
 	b->isBullet = d->isBullet != 0;
 	b->allowFastRotation = d->allowFastRotation != 0;
 	b->fixedRotation = d->fixedRotation != 0;
@@ -382,6 +384,7 @@ static int create_shape( World* w, int bodyId, const f2d_shape_def* d, const Geo
 	s->generation = gen + 1;
 	s->used = 1;
 	s->bodyId = bodyId;
+	s->sub = w->bodies[bodyId].sub;
 	s->g = *g;
 	s->density = (float)d->density;
 	s->friction = (float)d->friction;
@@ -813,7 +816,7 @@ static void consider_pair( World* w, int s1, int s2, Cand** cands, int* n, int* 
 	uint64_t key = pair_key( s1, s2 );
 	if ( pairset_contains( &w->pairs, key ) )
 		return;
-	if ( a->bodyId == b->bodyId )
+	if ( a->bodyId == b->bodyId || a->sub != b->sub )
 		return;
 	if ( a->isSensor || b->isSensor )
 		return;
@@ -1266,6 +1269,18 @@ double p_now( void )
 	struct timespec t;
 	clock_gettime( CLOCK_MONOTONIC, &t );
 	return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+// Batched form: bodies created after this call form a new sub-world with
+// the given gravity; shapes of different sub-worlds never make contacts.
+int orc_begin_subworld( int wi, double gravityX, double gravityY )
+{
+	World* w = p_world( wi );
+	if ( w == NULL )
+		return -1;
+	w->subGravity = V( (float)gravityX, (float)gravityY );
+	w->subCount += 1;
+	return w->subCount - 1;
 }
 
 int orc_thread_count( void )
