@@ -283,9 +283,148 @@ def run_gpu(args, rank, world):
         "status": status,
         "wall_s_timed_region": wall,
     }
+    if args.batched:
+        result["forms"] = {"batched": run_batched(args, torch)}
     if rank == 0 and args.cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, bodies_hint=bodies)
     return result, rank
+
+
+class _SubRecorder:
+    """Builder proxy that records the sub-world of every body it creates."""
+
+    def __init__(self, g):
+        self.g = g
+        self.body_sub = []
+        self.sub = -1
+
+    def begin_subworld(self, gx, gy):
+        self.sub = self.g.begin_subworld(gx, gy)
+        return self.sub
+
+    def create_body(self, d):
+        h = self.g.create_body(d)
+        self.body_sub.append(self.sub)
+        return h
+
+    def __getattr__(self, name):
+        return getattr(self.g, name)
+
+
+class _PlainBuilder:
+    """Builder proxy without sub-worlds (a plain world)."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def create_body(self, d):
+        return self.g.create_body(d)
+
+    def create_box(self, *a, **k):
+        return self.g.create_box(*a, **k)
+
+    def create_circle(self, *a, **k):
+        return self.g.create_circle(*a, **k)
+
+    def create_capsule(self, *a, **k):
+        return self.g.create_capsule(*a, **k)
+
+    def create_polygon(self, *a, **k):
+        return self.g.create_polygon(*a, **k)
+
+    def create_revolute(self, *a, **k):
+        return self.g.create_revolute(*a, **k)
+
+
+def max_penetration(world, group_of_shape=None, groups=0):
+    """Max penetration (-min separation of touching manifold points), overall
+    or per group of shapes."""
+    import numpy as np
+    ints, fl = world.contacts()
+    if len(ints) == 0:
+        return 0.0 if group_of_shape is None else np.zeros(groups)
+    sep = np.full(len(ints), np.inf, np.float64)
+    for k in range(2):
+        ok = ints[:, 4] > k
+        sep[ok] = np.minimum(sep[ok], fl[ok, 3 + 11 * k + 6])
+    pen = np.maximum(0.0, -sep)
+    pen[~np.isfinite(pen)] = 0.0
+    if group_of_shape is None:
+        return float(pen.max())
+    out = np.zeros(groups)
+    np.maximum.at(out, group_of_shape[ints[:, 1]], pen)
+    return out
+
+
+def run_batched(args, torch):
+    """The batched form (BASELINE config 4): 4096 sub-worlds stepped as one
+    world after the autotuner picked the launch shapes, against the same
+    worlds stepped one at a time as plain worlds (a seeded sample), at the
+    same frame, with max penetration compared."""
+    import numpy as np
+
+    from forge2d_gb300 import scenes
+    from forge2d_gb300.world import GpuWorld
+
+    worlds, seed = args.batch_worlds, 7
+    wd = scenes.world_def(enableSleep=0, enableContinuous=1)
+    g = GpuWorld(wd)
+    rec = _SubRecorder(g)
+    scenes.batched(rec, worlds=worlds, seed=seed)
+    body_sub = np.array(rec.body_sub, np.int32)
+    _, sh = g.shapes()
+    shape_sub = body_sub[sh[:, 1]]
+    for _ in range(3):
+        g.step(1.0 / 60.0, 4)
+    st, chosen, taken = g.autotune(1.0 / 60.0, 4, 2)
+    frames = 3 + taken
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.batch_steps):
+        st |= g.step(1.0 / 60.0, 4)
+        st |= g.sync()
+        ms.append(g.last_step_ms())
+    frames += args.batch_steps
+    c = g.counters()
+    pen_b = max_penetration(g, shape_sub, worlds)
+    bms = float(np.mean(ms))
+    g.close()
+    # plain: a seeded sample of the same worlds, each its own world
+    rng = np.random.default_rng(3)
+    sample = sorted(rng.choice(worlds, size=min(args.batch_sample, worlds), replace=False).tolist())
+    pms, pen_p = [], []
+    for k in sample:
+        gx, gy = scenes.batched_gravity(k, worlds, seed)
+        p = GpuWorld(scenes.world_def(enableSleep=0, enableContinuous=1, gravityX=gx, gravityY=gy))
+        scenes.batched(_PlainBuilder(p), worlds=worlds, seed=seed, only=k)
+        t = []
+        for f in range(frames):
+            p.step(1.0 / 60.0, 4)
+            if f >= frames - args.batch_steps:
+                p.sync()
+                t.append(p.last_step_ms())
+        pms.append(float(np.mean(t)))
+        pen_p.append(max_penetration(p))
+        p.close()
+    plain_ws = 1000.0 / float(np.mean(pms))
+    batched_ws = worlds * 1000.0 / bms
+    return {
+        "workload": "%d sub-worlds (pyramids rows U{5..30}, piles of 20-500 mixed shapes, chains of 10-100 "
+                    "links; gravity tilted U[-15,15] deg; seed %d), dt=1/60, 4 substeps" % (worlds, seed),
+        "worlds": worlds, "bodies": c["awake_bodies"], "touching": c["touching"], "joints": c["joints"],
+        "ms_per_step": bms, "world_steps_per_s": batched_ws, "body_steps_per_s": c["awake_bodies"] * 1000.0 / bms,
+        "autotune": {"solver_variant": ["auto", "cluster", "grid512", "grid256"][chosen[0]],
+                     "leaf_order_period": chosen[1], "tuning_steps": taken},
+        "frame": frames, "status": st,
+        "plain": {"sample_worlds": len(sample), "ms_per_world_step": float(np.mean(pms)),
+                  "world_steps_per_s": plain_ws,
+                  "max_penetration_sample": float(np.max(pen_p)),
+                  "mean_max_penetration_sample": float(np.mean(pen_p))},
+        "max_penetration_batched_sample": float(np.max(pen_b[sample])),
+        "mean_max_penetration_batched_sample": float(np.mean(pen_b[sample])),
+        "max_penetration_batched_all": float(pen_b.max()),
+        "world_steps_ratio_vs_plain": batched_ws / plain_ws,
+    }
 
 
 def cpu_baseline(args, bodies_hint=None, budget_s=None):
@@ -350,6 +489,11 @@ def main():
     ap.add_argument("--workload", default="pile100k", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the batched form (4096 sub-worlds) beside the headline workload")
+    ap.add_argument("--batch-worlds", type=int, default=4096)
+    ap.add_argument("--batch-steps", type=int, default=30)
+    ap.add_argument("--batch-sample", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -101,7 +101,8 @@ struct DScalars
 	int rebuildOrder;
 	int forceRebuild;
 	int orderAge;
-	int pad[5];
+	int orderPeriod; // steps between re-sorts (0: ORDER_REBUILD_PERIOD)
+	int pad[4];
 };
 
 // Solver view of one body: velocity and the substep position/rotation

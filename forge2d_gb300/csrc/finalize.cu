@@ -460,7 +460,8 @@ __global__ void k_reset_step_counters( DWorld w )
 	w.sc->hitCount = 0;
 	w.sc->fastCount = 0;
 	int age = w.sc->orderAge;
-	int rebuild = ( w.sc->forceRebuild != 0 || age >= ORDER_REBUILD_PERIOD - 1 ) ? 1 : 0;
+	int period = w.sc->orderPeriod > 0 ? w.sc->orderPeriod : ORDER_REBUILD_PERIOD;
+	int rebuild = ( w.sc->forceRebuild != 0 || age >= period - 1 ) ? 1 : 0;
 	w.sc->rebuildOrder = rebuild;
 	w.sc->orderAge = rebuild ? 0 : age + 1;
 	w.sc->forceRebuild = 0;

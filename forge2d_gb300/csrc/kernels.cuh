@@ -34,8 +34,16 @@ struct StepScratch
 	int solverBlocks;  // persistent solver grid (co-resident)
 	int solverThreads;
 	int clusterCapacity; // bodies the cluster solver takes (0: cooperative solver only)
+	int solverBlocks256; // grid of the 256-thread variant of the grid-wide solver
+	int solverVariant;	 // SOLVER_* (the autotuner's choice; results never depend on it)
 	cudaEvent_t evSolveStart; // recorded right before the cooperative solver launch when non-null
 };
+
+// solver variants: same arithmetic, different launch shapes
+#define SOLVER_AUTO 0	 // cluster solver up to 2e4 bodies, else grid-wide with 512-thread blocks
+#define SOLVER_CLUSTER 1 // one thread-block cluster (when the bodies fit its shared memory)
+#define SOLVER_GRID512 2 // grid-wide, one 512-thread block per SM
+#define SOLVER_GRID256 3 // grid-wide, two 256-thread blocks per SM
 
 void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode );
 void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st );

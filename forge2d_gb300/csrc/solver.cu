@@ -24,7 +24,6 @@
 #include "joint.cuh"
 #include "kernels.cuh"
 
-#define SOLVER_THREADS 512
 
 struct SolveParams
 {
@@ -899,8 +898,9 @@ __device__ __forceinline__ void colour_lanes_extra( const DWorld& w, const BA& b
 // ... when the graph holds more constraints than the grid has threads). The
 // first owned constraint lives in registers for the whole launch; a colour
 // stage then costs one load and one store of each of its two bodies.
-__global__ void __launch_bounds__( SOLVER_THREADS ) k_solve( DWorld w, SolveParams p, const int* jointSlots,
-															 const int* jointStart )
+template <int THREADS>
+__global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, const int* jointSlots,
+													  const int* jointStart )
 {
 	__shared__ int sStart[F2D_COLORS], sCount[F2D_COLORS], sJStart[F2D_OVERFLOW + 1];
 	if ( threadIdx.x < F2D_COLORS )
@@ -1279,21 +1279,24 @@ int solver_cluster_capacity()
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
-// One block of SOLVER_THREADS per SM: every block is co-resident (the
-// cooperative launch checks it) and a grid barrier waits for one arrival per
-// SM.
-int solver_max_blocks( int threads )
+// Co-resident grid of the grid-wide solver: one block of 512 threads or two
+// of 256 per SM (the cooperative launch checks co-residency).
+template <int THREADS> static int grid_blocks( int perSMWanted )
 {
-	(void)threads;
 	int perSM = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_solve, SOLVER_THREADS, 0 );
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_solve<THREADS>, THREADS, 0 );
 	int dev = 0;
 	cudaGetDevice( &dev );
 	int sms = 0;
 	cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
 	if ( perSM < 1 )
 		return 0;
-	return sms;
+	return sms * ( perSM < perSMWanted ? perSM : perSMWanted );
+}
+
+int solver_max_blocks( int threads )
+{
+	return threads == 256 ? grid_blocks<256>( 2 ) : grid_blocks<512>( 1 );
 }
 
 void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps )
@@ -1334,7 +1337,10 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 	// bodies the cluster's 16 SMs no longer hold the constraints in registers
 	// and the grid-wide solver is faster (measured: pyramid 0.11 vs 0.17 ms,
 	// 25k pile equal, 100k pile 0.75 vs 0.26 ms).
-	if ( s.clusterCapacity > 0 && w.bodyCount <= s.clusterCapacity && w.bodyCount <= CLUSTER_SOLVER_MAX_BODIES )
+	bool useCluster = s.clusterCapacity > 0 && w.bodyCount <= s.clusterCapacity &&
+					  ( s.solverVariant == SOLVER_CLUSTER ||
+						( s.solverVariant == SOLVER_AUTO && w.bodyCount <= CLUSTER_SOLVER_MAX_BODIES ) );
+	if ( useCluster )
 	{
 		int slots = ( w.bodyCount + F2D_CLUSTER - 1 ) / F2D_CLUSTER;
 		cudaLaunchConfig_t cfg = {};
@@ -1357,5 +1363,8 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 	cudaMemsetAsync( &w.sc->barrierCount, 0, sizeof( unsigned ), st );
 	if ( s.evSolveStart )
 		cudaEventRecord( s.evSolveStart, st );
-	cudaLaunchCooperativeKernel( (void*)k_solve, dim3( s.solverBlocks ), dim3( SOLVER_THREADS ), args, 0, st );
+	if ( s.solverVariant == SOLVER_GRID256 && s.solverBlocks256 > 0 )
+		cudaLaunchCooperativeKernel( (void*)k_solve<256>, dim3( s.solverBlocks256 ), dim3( 256 ), args, 0, st );
+	else
+		cudaLaunchCooperativeKernel( (void*)k_solve<512>, dim3( s.solverBlocks ), dim3( 512 ), args, 0, st );
 }

@@ -100,6 +100,9 @@ struct HostWorld
 	// batched form: gravity of the sub-world bodies are created into
 	float2 subGravity = { 0.0f, 0.0f };
 
+	// autotuner choice of the tree's leaf-order period (0: default)
+	int orderPeriod = 0;
+
 	// solve on the grid-wide cooperative kernel even when the world fits a
 	// thread-block cluster (F2D_NO_CLUSTER_SOLVER set at world creation)
 	bool gridSolverOnly = false;
@@ -176,6 +179,7 @@ static void alloc_scratch( HostWorld* W )
 	d.pairKeyBits = bits;
 	s.solverThreads = 512;
 	s.solverBlocks = solver_max_blocks( 512 );
+	s.solverBlocks256 = solver_max_blocks( 256 );
 	s.clusterCapacity = W->gridSolverOnly ? 0 : solver_cluster_capacity();
 }
 
@@ -1282,6 +1286,78 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	int st = W->statusAccum;
 	W->statusAccum = 0;
 	return st;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: launch shapes that change timing but never results
+// ---------------------------------------------------------------------------
+static void apply_tuning( HostWorld* W, int variant, int period )
+{
+	W->s.solverVariant = variant;
+	W->orderPeriod = period;
+	cudaMemcpyAsync( &W->d.sc->orderPeriod, &W->orderPeriod, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+	cudaStreamSynchronize( W->stream );
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API int32_t f2d_world_autotune( int32_t worldId, double timeStep, int32_t subStepCount,
+											   int32_t stepsPerCandidate, int32_t* chosen3 )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return F2D_STATUS_INVALID;
+	flush_uploads( W );
+	int variants[3];
+	int nv = 0;
+	if ( W->s.clusterCapacity > 0 && W->bodyCount <= W->s.clusterCapacity )
+		variants[nv++] = SOLVER_CLUSTER;
+	variants[nv++] = SOLVER_GRID512;
+	if ( W->s.solverBlocks256 > 0 )
+		variants[nv++] = SOLVER_GRID256;
+	const int periods[4] = { 4, 8, 16, 32 };
+	int reps = stepsPerCandidate < 1 ? 1 : stepsPerCandidate;
+	int status = 0;
+	int taken = 0;
+	double best = 1e30;
+	int bestV = SOLVER_AUTO, bestP = 0;
+	for ( int vi = 0; vi < nv; ++vi )
+		for ( int pi = 0; pi < 4; ++pi )
+		{
+			apply_tuning( W, variants[vi], periods[pi] );
+			// the first step re-captures the graph; the leaf order is re-sorted
+			// at least once per period, so a candidate is timed over a period
+			status |= f2d_world_step( worldId, timeStep, subStepCount );
+			int n = reps > periods[pi] ? reps : periods[pi];
+			taken += 1 + n;
+			double ms = 0.0;
+			for ( int k = 0; k < n; ++k )
+			{
+				status |= f2d_world_step( worldId, timeStep, subStepCount );
+				ms += f2d_world_last_step_ms( worldId );
+			}
+			ms /= n;
+			if ( ms < best )
+			{
+				best = ms;
+				bestV = variants[vi];
+				bestP = periods[pi];
+			}
+		}
+	apply_tuning( W, bestV, bestP );
+	if ( chosen3 )
+	{
+		chosen3[0] = bestV;
+		chosen3[1] = bestP;
+		chosen3[2] = taken;
+	}
+	return status | f2d_world_sync( worldId );
+}
+
+extern "C" F2D_API void f2d_world_get_tuning( int32_t worldId, int32_t* out2 )
+{
+	HostWorld* W = world_from_id( worldId );
+	out2[0] = W ? W->s.solverVariant : 0;
+	out2[1] = W ? W->orderPeriod : 0;
 }
 
 extern "C" F2D_API int32_t f2d_world_sync( int32_t worldId )

@@ -243,22 +243,27 @@ def joint_gallery(b, copies=4):
                                        collideConnected=1))
 
 
-def batched(b, worlds=4096, seed=7, tile=220.0, columns=64):
+def batched(b, worlds=4096, seed=7, tile=220.0, columns=64, only=None):
     """BASELINE config 4: ``worlds`` independent sub-worlds of uneven size,
     each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
     (20-500 shapes with the config-2 mix, in a U container sized to the
     count) or a revolute chain (10-100 links), with gravity (0, -10) tilted
     by U[-15, 15] degrees. World k sits in its own ``tile`` x ``tile`` cell of
     a ``columns``-wide grid; sub-worlds never interact even when bodies
-    leave their cell. The builder needs ``begin_subworld(gx, gy)``."""
+    leave their cell. The builder needs ``begin_subworld(gx, gy)``; with
+    ``only=k`` just world k is built (same draws), as a plain world when the
+    builder has no ``begin_subworld``."""
     rng = np.random.default_rng(seed)
     kinds = rng.integers(0, 3, worlds)
     tilts = np.radians(rng.uniform(-15.0, 15.0, worlds))
     sizes = rng.random(worlds)
     seeds = rng.integers(0, 2 ** 31 - 1, worlds)
     for k in range(worlds):
+        if only is not None and k != only:
+            continue
         t = float(tilts[k])
-        b.begin_subworld(10.0 * math.sin(t), -10.0 * math.cos(t))
+        if hasattr(b, "begin_subworld"):
+            b.begin_subworld(10.0 * math.sin(t), -10.0 * math.cos(t))
         ox = (k % columns) * tile
         oy = (k // columns) * tile
         if kinds[k] == 0:
@@ -281,6 +286,14 @@ def batched(b, worlds=4096, seed=7, tile=220.0, columns=64):
         else:
             links = 10 + int(sizes[k] * 91)
             chain(b, ox - 0.25 * links, oy + 0.6 * tile, links=links)
+
+
+def batched_gravity(k, worlds=4096, seed=7):
+    """Gravity of sub-world k of ``batched(worlds=worlds, seed=seed)``."""
+    rng = np.random.default_rng(seed)
+    rng.integers(0, 3, worlds)
+    t = float(np.radians(rng.uniform(-15.0, 15.0, worlds))[k])
+    return 10.0 * math.sin(t), -10.0 * math.cos(t)
 
 
 class _PileOffset:

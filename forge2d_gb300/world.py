@@ -124,6 +124,18 @@ class GpuWorld:
         ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def autotune(self, dt=1.0 / 60.0, substeps=4, steps_per_candidate=3):
+        """Steps through the launch configurations and keeps the fastest;
+        returns (status, (solver variant, leaf-order period), steps taken)."""
+        out = np.zeros(3, np.int32)
+        st = self.lib.f2d_world_autotune(self.id, dt, substeps, steps_per_candidate, _iptr(out))
+        return st, (int(out[0]), int(out[1])), int(out[2])
+
+    def tuning(self):
+        out = np.zeros(2, np.int32)
+        self.lib.f2d_world_get_tuning(self.id, _iptr(out))
+        return int(out[0]), int(out[1])
+
     def begin_subworld(self, gx, gy):
         return self.lib.f2d_world_begin_subworld(self.id, gx, gy)
 

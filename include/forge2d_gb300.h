@@ -330,6 +330,18 @@ F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 );
 /* awake bodies, live contacts, touching contacts, overflow contacts, active
  * colours, colouring rounds, shapes, joints (b2Counters, types.h:493-506). */
 F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 );
+/* Autotuner (no reference counterpart). Steps the world through every
+ * candidate launch configuration -- solver kernel shape (1 thread-block
+ * cluster when the bodies fit, grid-wide with 512- or 256-thread blocks) x
+ * broadphase leaf-order refresh period (4, 8, 16, 32 steps) -- timing each
+ * over max(stepsPerCandidate, period) steps, and keeps the fastest. The
+ * tuning steps are ordinary steps of the world; no configuration changes any
+ * result. chosen3 (optional) receives {solver variant, period, steps
+ * taken}. Returns the accumulated F2D_STATUS_* bits. */
+F2D_API int32_t f2d_world_autotune( int32_t worldId, double timeStep, int32_t subStepCount,
+									int32_t stepsPerCandidate, int32_t* chosen3 );
+/* Current {solver variant, leaf-order period} (0 = defaults). */
+F2D_API void f2d_world_get_tuning( int32_t worldId, int32_t* out2 );
 /* Capacities chosen at creation can be raised before the first step. */
 F2D_API void f2d_world_reserve( int32_t worldId, int32_t bodies, int32_t shapes, int32_t contacts, int32_t joints );
 

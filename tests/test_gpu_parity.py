@@ -188,3 +188,30 @@ def test_gpu_stats_series_native_mode(gpu_lib, name):
     assert abs(ke_mean) < 0.25, ke_mean
     g.close()
     p.close()
+
+
+@pytest.mark.parametrize("scene,kw", [("pile", dict(count=3000, seed=9, width=40.0, height=120.0)),
+                                      ("batched", dict(worlds=48, seed=5))], ids=["pile3000", "batched48"])
+def test_autotune_changes_timing_only(gpu_lib, scene, kw):
+    """The autotuner's candidates (solver launch shape, leaf-order period)
+    leave every result unchanged: a tuned world equals an untuned twin
+    stepped the same number of times, bit for bit."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    a = gpu_world(gpu_lib, wkw)
+    b = gpu_world(gpu_lib, wkw)
+    scenes.build(a, scene, **kw)
+    scenes.build(b, scene, **kw)
+    st, chosen, taken = a.autotune(1.0 / 60.0, 4, 2)
+    assert st == 0 and taken > 0
+    assert chosen[0] in (1, 2, 3) and chosen[1] in (4, 8, 16, 32)
+    assert a.tuning() == chosen
+    for _ in range(taken):
+        assert b.step(1.0 / 60.0, 4) == 0
+    for _ in range(20):
+        a.step(1.0 / 60.0, 4)
+        b.step(1.0 / 60.0, 4)
+    assert a.sync() == 0 and b.sync() == 0
+    ab, bb = a.bodies()[:, :9], b.bodies()[:, :9]
+    assert np.array_equal(ab.view(np.uint32), bb.view(np.uint32))
+    a.close()
+    b.close()
