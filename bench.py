@@ -283,8 +283,13 @@ def run_gpu(args, rank, world):
         "status": status,
         "wall_s_timed_region": wall,
     }
+    forms = {}
     if args.batched:
-        result["forms"] = {"batched": run_batched(args, torch)}
+        forms["batched"] = run_batched(args, torch)
+    if args.learned:
+        forms["learned_warm_start"] = run_learned(args, torch)
+    if forms:
+        result["forms"] = forms
     if rank == 0 and args.cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, bodies_hint=bodies)
     return result, rank
@@ -427,6 +432,90 @@ def run_batched(args, torch):
     }
 
 
+def kinetic_energy(world, mass):
+    import numpy as np
+    b = world.bodies()
+    m = mass[:, 0].astype(np.float64)
+    inertia = mass[:, 1].astype(np.float64)
+    v = b[:, 4:6].astype(np.float64)
+    w = b[:, 6].astype(np.float64)
+    return float(np.sum(0.5 * m * (v * v).sum(1) + 0.5 * inertia * w * w))
+
+
+def run_learned(args, torch):
+    """The learned warm start (BASELINE config 5): samples recorded by the
+    plain solver on seeded scenes of configs 2-4, the MLP trained on the GPU,
+    then the config-2 pile at 200k bodies stepped plain at 4 and 2 substeps
+    and with the learned warm start at 2 and 4 substeps: max penetration,
+    kinetic-energy drift against plain at 4 substeps, world-steps/s."""
+    import numpy as np
+
+    from forge2d_gb300 import scenes
+    from forge2d_gb300.world import GpuWorld, WarmStartModel
+
+    wd = scenes.world_def(enableSleep=0, enableContinuous=1)
+    t0 = time.perf_counter()
+    samples = []
+    for name, kw, frames in (("pile", dict(count=20000, seed=21, width=100.0, height=200.0), 240),
+                             ("batched", dict(worlds=256, seed=22), 240),
+                             ("pyramids_chains", dict(pyramids=4, rows=30, chains=40, links=30), 240)):
+        g = GpuWorld(wd)
+        scenes.build(g, name, **kw)
+        g.set_sample_recording(args.learn_samples)
+        for _ in range(frames):
+            g.step(1.0 / 60.0, 4)
+        samples.append(g.samples())
+        g.close()
+    samples = np.concatenate(samples)
+    rec_s = time.perf_counter() - t0
+    model = WarmStartModel(seed=3)
+    model.fit_normalization(samples)
+    loss0 = model.gradient(samples)[1]
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss = model.train(samples, epochs=args.learn_epochs, batch=4096, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+
+    kw = dict(count=args.learn_bodies, seed=1234, width=400.0 * math.sqrt(args.learn_bodies / 1e5),
+              height=800.0 * math.sqrt(args.learn_bodies / 1e5))
+    runs = {}
+    ke_ref = None
+    for label, sub, use in (("plain_4", 4, False), ("plain_2", 2, False), ("learned_2", 2, True),
+                            ("learned_4", 4, True)):
+        g = GpuWorld(wd)
+        scenes.build(g, "pile", **kw)
+        mass = g.mass()
+        if use:
+            g.set_warm_start_model(model)
+        pens, kes, ms = [], [], []
+        for f in range(args.learn_frames):
+            g.step(1.0 / 60.0, sub)
+            if f % 20 == 19:
+                g.sync()
+                ms.append(g.last_step_ms())
+                pens.append(max_penetration(g))
+                kes.append(kinetic_energy(g, mass))
+        g.close()
+        kes = np.array(kes)
+        if ke_ref is None:
+            ke_ref = kes
+        runs[label] = {"substeps": sub, "ms_per_step": float(np.median(ms)),
+                       "world_steps_per_s": 1000.0 / float(np.median(ms)),
+                       "mean_max_penetration": float(np.mean(pens)), "max_penetration": float(np.max(pens)),
+                       "ke_drift_vs_plain_4": float(np.mean(np.abs(kes - ke_ref) / np.maximum(ke_ref, 1e-9)))}
+    model.close()
+    return {
+        "workload": "config-2 pile at %d bodies (seed 1234), %d frames, dt=1/60; samples from a 20k pile, "
+                    "256 batched sub-worlds and a pyramids+chains scene (4 substeps, 240 frames each)"
+                    % (args.learn_bodies, args.learn_frames),
+        "samples": int(len(samples)), "record_s": rec_s, "train_s": train_s, "epochs": args.learn_epochs,
+        "loss_initial": float(loss0), "loss_final": float(loss), "network": "MLP 12-64-64-2, BF16 weights, "
+        "FP32 accumulation, mma.sync m16n8k16 tensor-core kernels (forward, backward, Adam)",
+        "runs": runs,
+    }
+
+
 def cpu_baseline(args, bodies_hint=None, budget_s=None):
     """Bounded sample of the CPU restatement on this host's cores."""
     from forge2d_gb300 import scenes
@@ -494,6 +583,12 @@ def main():
     ap.add_argument("--batch-worlds", type=int, default=4096)
     ap.add_argument("--batch-steps", type=int, default=30)
     ap.add_argument("--batch-sample", type=int, default=16)
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned warm start (200k pile) beside the headline workload")
+    ap.add_argument("--learn-bodies", type=int, default=200_000)
+    ap.add_argument("--learn-frames", type=int, default=240)
+    ap.add_argument("--learn-epochs", type=int, default=10)
+    ap.add_argument("--learn-samples", type=int, default=1_000_000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -102,7 +102,9 @@ struct DScalars
 	int forceRebuild;
 	int orderAge;
 	int orderPeriod; // steps between re-sorts (0: ORDER_REBUILD_PERIOD)
-	int pad[4];
+	int newPointCount; // new manifold points listed by the prepare stage (learned warm start)
+	int sampleCount;   // training samples recorded so far
+	int pad[2];
 };
 
 // Solver view of one body: velocity and the substep position/rotation
@@ -133,6 +135,17 @@ struct DWorld
 	float jointHertz, jointDampingRatio;
 	int enableSleep, enableContinuous, enableWarmStarting;
 	int subCount; // batched form: independent sub-worlds (0 = one world)
+
+	// learned warm start: bit 0 records (features, final impulses) of new
+	// manifold points as training samples, bit 1 predicts their initial
+	// impulses with model mlpModel
+	int learnMode;
+	int mlpModel;
+	int newPointCap;
+	int2* newPoint; // (constraint slot, point index)
+	float* newFeat; // 12 features per new point
+	int sampleCap;
+	float* samples; // 14 floats per sample
 
 	// ---------------- bodies (by body id) ----------------
 	float4* xf;			// p.x p.y q.c q.s

@@ -52,4 +52,6 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
 void launch_joint_ops( DWorld& w, cudaStream_t st );
 int solver_max_blocks( int threads );
+void launch_learned_warm_start( DWorld& w, cudaStream_t st );
+void launch_record_samples( DWorld& w, cudaStream_t st );
 int solver_cluster_capacity();

@@ -204,6 +204,28 @@ __global__ void k_prepare_contacts( DWorld w, SolveParams p )
 			fv2 vrB = vadd( vB, vcrossSV( wB, rB ) );
 			float relVel = vdot( normal, vsub( vrB, vrA ) );
 			pp[j] = make_float4( baseSeparation, normalMass, tangentMass, relVel );
+			// learned warm start: features of a point that has no cached impulse
+			if ( w.learnMode != 0 && ( ( float_to_bits( b.w ) >> 16 ) & 1 ) == 0 )
+			{
+				int q = atomicAdd( &w.sc->newPointCount, 1 );
+				if ( q < w.newPointCap )
+				{
+					w.newPoint[q] = make_int2( k, j );
+					float* f = w.newFeat + 12 * (size_t)q;
+					f[0] = normal.x;
+					f[1] = normal.y;
+					f[2] = relVel;
+					f[3] = vdot( tangent, vsub( vrB, vrA ) );
+					f[4] = b.z;
+					f[5] = vdot( rA, tangent );
+					f[6] = vdot( rB, tangent );
+					f[7] = vdot( rA, normal );
+					f[8] = vdot( rB, normal );
+					f[9] = normalMass;
+					f[10] = tangentMass;
+					f[11] = cmat.x;
+				}
+			}
 		}
 		w.kAnch1[k] = anch[0];
 		w.kAnch2[k] = anch[1];
@@ -1327,6 +1349,8 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 	k_color_offsets<<<1, 1, 0, st>>>( w, fill );
 	k_fill_slots<<<grid_for( w.contactCap ), 256, 0, st>>>( w, fill );
 	k_prepare_contacts<<<grid_for( w.contactCap ), 256, 0, st>>>( w, p );
+	if ( w.learnMode & 2 )
+		launch_learned_warm_start( w, st );
 	launch_prepare_joints( w, s, st, p.h, p.inv_h, p.jointSoft );
 
 	int* jointSlots = s.tmpB;

@@ -649,7 +649,7 @@ static void free_world( HostWorld* W )
 	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 );
 	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
-	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp );
+	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F
 	dfree( W->s.tmpA );
 	dfree( W->s.tmpB );
@@ -1183,6 +1183,8 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	if ( prof )
 		cudaEventRecord( W->ph[3], W->stream );
 	launch_solver( d, W->s, W->stream, dt, subSteps );
+	if ( d.learnMode & 1 )
+		launch_record_samples( d, W->stream );
 	if ( prof )
 		cudaEventRecord( W->ph[5], W->stream );
 	launch_finalize( d, W->s, W->stream, dt );
@@ -1207,6 +1209,8 @@ static int count_kernel_nodes( cudaGraph_t g )
 	}
 	return k;
 }
+
+static void ensure_learning_buffers( HostWorld* W );
 
 extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int32_t subStepCount )
 {
@@ -1235,6 +1239,8 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 		W->planPending = false;
 		planMode = 1;
 	}
+	if ( W->d.learnMode != 0 )
+		ensure_learning_buffers( W );
 	cudaMemsetAsync( &W->d.sc->error, 0, sizeof( int ), W->stream );
 	if ( W->forceRebuild )
 	{
@@ -1358,6 +1364,89 @@ extern "C" F2D_API void f2d_world_get_tuning( int32_t worldId, int32_t* out2 )
 	HostWorld* W = world_from_id( worldId );
 	out2[0] = W ? W->s.solverVariant : 0;
 	out2[1] = W ? W->orderPeriod : 0;
+}
+
+// ---------------------------------------------------------------------------
+// learned warm start: sample recording and model binding
+// ---------------------------------------------------------------------------
+bool f2d_internal_mlp_valid( int32_t handle ); // mlp.cu
+
+static void ensure_learning_buffers( HostWorld* W )
+{
+	DWorld& d = W->d;
+	if ( d.newPointCap < d.contactCap )
+	{
+		cudaStreamSynchronize( W->stream );
+		dfree( d.newPoint );
+		dfree( d.newFeat );
+		dgrow( d.newPoint, 0, (size_t)d.contactCap );
+		dgrow( d.newFeat, 0, (size_t)d.contactCap * 12 );
+		d.newPointCap = d.contactCap;
+	}
+}
+
+extern "C" F2D_API void f2d_world_set_sample_recording( int32_t worldId, int32_t capacity )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	DWorld& d = W->d;
+	dfree( d.samples );
+	d.sampleCap = 0;
+	if ( capacity > 0 )
+	{
+		dgrow( d.samples, 0, (size_t)capacity * 14 );
+		d.sampleCap = capacity;
+		ensure_learning_buffers( W );
+		d.learnMode |= 1;
+	}
+	else
+		d.learnMode &= ~1;
+	cudaMemsetAsync( &d.sc->sampleCount, 0, sizeof( int ), W->stream );
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API int32_t f2d_world_sample_count( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	int n = 0;
+	cudaMemcpy( &n, &W->d.sc->sampleCount, sizeof( int ), cudaMemcpyDeviceToHost );
+	return std::min( n, W->d.sampleCap );
+}
+
+extern "C" F2D_API int32_t f2d_world_get_samples( int32_t worldId, float* out14, int32_t capacity )
+{
+	int n = std::min( f2d_world_sample_count( worldId ), capacity );
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || n <= 0 )
+		return 0;
+	cudaMemcpy( out14, W->d.samples, sizeof( float ) * 14 * (size_t)n, cudaMemcpyDeviceToHost );
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_world_set_warm_start_model( int32_t worldId, int32_t model )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	if ( model > 0 && f2d_internal_mlp_valid( model ) )
+	{
+		ensure_learning_buffers( W );
+		W->d.mlpModel = model - 1;
+		W->d.learnMode |= 2;
+	}
+	else
+	{
+		W->d.mlpModel = -1;
+		W->d.learnMode &= ~2;
+	}
+	W->graphDirty = true;
+	return 1;
 }
 
 extern "C" F2D_API int32_t f2d_world_sync( int32_t worldId )

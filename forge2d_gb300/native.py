@@ -138,6 +138,19 @@ _SIGS = [
     ("f2d_world_last_step_launches", _i, [_i]),
     ("f2d_world_reserve", None, [_i, _i, _i, _i, _i]),
     ("f2d_world_autotune", _i, [_i, _d, _i, _i, _P(_i)]),
+    ("f2d_world_set_sample_recording", None, [_i, _i]),
+    ("f2d_world_sample_count", _i, [_i]),
+    ("f2d_world_get_samples", _i, [_i, _P(_f), _i]),
+    ("f2d_world_set_warm_start_model", _i, [_i, _i]),
+    ("f2d_mlp_create", _i, [C.c_uint32]),
+    ("f2d_mlp_destroy", None, [_i]),
+    ("f2d_mlp_param_count", _i, []),
+    ("f2d_mlp_get_params", None, [_i, _P(_f)]),
+    ("f2d_mlp_set_params", None, [_i, _P(_f)]),
+    ("f2d_mlp_set_normalization", None, [_i, _P(_f), _P(_f)]),
+    ("f2d_mlp_gradient", _f, [_i, _P(_f), _i, _P(_f)]),
+    ("f2d_mlp_train", _f, [_i, _P(_f), _i, _i, _i, _f, C.c_uint32]),
+    ("f2d_mlp_predict", None, [_i, _P(_f), _i, _P(_f)]),
     ("f2d_world_get_tuning", None, [_i, _P(_i)]),
     ("f2d_world_set_profiling", None, [_i, _i]),
     ("f2d_world_get_phase_ms", None, [_i, _P(_d)]),

@@ -136,6 +136,20 @@ class GpuWorld:
         self.lib.f2d_world_get_tuning(self.id, _iptr(out))
         return int(out[0]), int(out[1])
 
+    # learned warm start ---------------------------------------------------
+    def set_sample_recording(self, capacity):
+        self.lib.f2d_world_set_sample_recording(self.id, int(capacity))
+
+    def samples(self):
+        n = self.lib.f2d_world_sample_count(self.id)
+        out = np.zeros((max(n, 1), 14), np.float32)
+        m = self.lib.f2d_world_get_samples(self.id, _fptr(out), n)
+        return out[:m]
+
+    def set_warm_start_model(self, model):
+        """model: a WarmStartModel (or None to switch prediction off)."""
+        self.lib.f2d_world_set_warm_start_model(self.id, model.handle if model is not None else 0)
+
     def begin_subworld(self, gx, gy):
         return self.lib.f2d_world_begin_subworld(self.id, gx, gy)
 
@@ -254,6 +268,69 @@ class GpuWorld:
         out = np.zeros((max(capacity, 1), 2), np.int32)
         n = self.lib.f2d_world_overlap_aabb_noalloc(self.id, lx, ly, ux, uy, cat, mask, _iptr(out), capacity)
         return n, out[:max(0, min(n, capacity))]
+
+
+class WarmStartModel:
+    """The learned warm-start MLP [12 -> 64 -> 64 -> 2] on the GPU: BF16
+    weights, FP32 accumulation, trained with the library's own forward and
+    backward kernels."""
+
+    def __init__(self, seed=1):
+        self.lib = native.lib()
+        self.handle = self.lib.f2d_mlp_create(seed)
+        if self.handle == 0:
+            raise RuntimeError("f2d_mlp_create failed")
+        self.n_params = self.lib.f2d_mlp_param_count()
+        self.mean = np.zeros(14, np.float32)
+        self.inv_std = np.ones(14, np.float32)
+
+    def close(self):
+        if self.handle:
+            self.lib.f2d_mlp_destroy(self.handle)
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        out = np.zeros(self.n_params, np.float32)
+        self.lib.f2d_mlp_get_params(self.handle, _fptr(out))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self.lib.f2d_mlp_set_params(self.handle, _fptr(p))
+
+    def set_normalization(self, mean, inv_std):
+        self.mean = np.ascontiguousarray(mean, np.float32)
+        self.inv_std = np.ascontiguousarray(inv_std, np.float32)
+        self.lib.f2d_mlp_set_normalization(self.handle, _fptr(self.mean), _fptr(self.inv_std))
+
+    def fit_normalization(self, samples):
+        s = np.asarray(samples, np.float64)
+        mean = s.mean(0)
+        std = s.std(0)
+        std[std < 1e-6] = 1.0
+        self.set_normalization(mean.astype(np.float32), (1.0 / std).astype(np.float32))
+
+    def gradient(self, samples):
+        s = np.ascontiguousarray(samples, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = self.lib.f2d_mlp_gradient(self.handle, _fptr(s), len(s), _fptr(g))
+        return g, loss
+
+    def train(self, samples, epochs=4, batch=4096, lr=2e-3, seed=1):
+        s = np.ascontiguousarray(samples, np.float32)
+        return self.lib.f2d_mlp_train(self.handle, _fptr(s), len(s), epochs, batch, lr, seed)
+
+    def predict(self, feats):
+        f = np.ascontiguousarray(feats, np.float32)
+        out = np.zeros((len(f), 2), np.float32)
+        self.lib.f2d_mlp_predict(self.handle, _fptr(f), len(f), _fptr(out))
+        return out
 
 
 # ---------------------------------------------------------------------------

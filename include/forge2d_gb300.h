@@ -330,6 +330,42 @@ F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 );
 /* awake bodies, live contacts, touching contacts, overflow contacts, active
  * colours, colouring rounds, shapes, joints (b2Counters, types.h:493-506). */
 F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 );
+/* ---- learned warm start (no reference counterpart) ----------------------
+ * A small MLP [12 -> 64 -> 64 -> 2] (BF16 weights, FP32 accumulation,
+ * tensor-core MMA) predicts the normal and tangent impulses of manifold
+ * points that have no cached impulse; persisting points keep Box2D's cached
+ * impulses and every solver iteration still runs. Features per new point:
+ * normal.xy, normal and tangent relative velocity, separation, anchorA and
+ * anchorB along the tangent and the normal, the effective normal and
+ * tangent masses (from the inverse masses and inertias), friction. A sample
+ * is the 12 features plus the normal and tangent impulse the plain solver
+ * ended the step with. */
+/* Record up to `capacity` samples from the following steps (0 stops). */
+F2D_API void f2d_world_set_sample_recording( int32_t worldId, int32_t capacity );
+F2D_API int32_t f2d_world_sample_count( int32_t worldId );
+/* Copies recorded samples (14 floats each); returns the number written. */
+F2D_API int32_t f2d_world_get_samples( int32_t worldId, float* out14, int32_t capacity );
+/* Predict warm-start impulses of new points with `model` (0 disables). */
+F2D_API int32_t f2d_world_set_warm_start_model( int32_t worldId, int32_t model );
+/* Model handle (> 0), He-uniform weights from seed; 0 on failure. */
+F2D_API int32_t f2d_mlp_create( uint32_t seed );
+F2D_API void f2d_mlp_destroy( int32_t model );
+/* FP32 master parameters: W1 [64][16] (columns 12..15 zero), W2 [64][64],
+ * W3 [8][64] (rows 2..7 zero), b1 [64], b2 [64], b3 [8]. */
+F2D_API int32_t f2d_mlp_param_count( void );
+F2D_API void f2d_mlp_get_params( int32_t model, float* out );
+F2D_API void f2d_mlp_set_params( int32_t model, const float* in );
+/* Per-column mean and 1/std of the 12 features and 2 targets. */
+F2D_API void f2d_mlp_set_normalization( int32_t model, const float* mean14, const float* invStd14 );
+/* Gradient of 0.5 * mean ||y - t||^2 (normalised units) over n samples at
+ * the current parameters, no update; returns the loss. */
+F2D_API float f2d_mlp_gradient( int32_t model, const float* samples14, int32_t n, float* grad );
+/* Adam training on the GPU; returns the mean loss of the last epoch. */
+F2D_API float f2d_mlp_train( int32_t model, const float* samples14, int32_t n, int32_t epochs, int32_t batch,
+							 float learningRate, uint32_t seed );
+/* Predicted (normal, tangent) impulses of n raw feature rows. */
+F2D_API void f2d_mlp_predict( int32_t model, const float* feats12, int32_t n, float* out2 );
+
 /* Autotuner (no reference counterpart). Steps the world through every
  * candidate launch configuration -- solver kernel shape (1 thread-block
  * cluster when the bodies fit, grid-wide with 512- or 256-thread blocks) x
