@@ -249,6 +249,12 @@ struct DWorld
 	float4* jprepM; // invMassA invIA invMassB invIB
 	int2* jindex;	// solver body indices
 	int* overflowJoints;
+	// overflow levels (solver scratch): body owner per level round, level
+	// per overflow constraint, constraints in level order beyond the
+	// shared-memory list
+	int* ovfOwner; // bodyCap
+	int* ovfLevel; // contactCap + jointCap
+	int* ovfOrder; // contactCap + jointCap
 	int* pendingJointOps; // joint ids whose colour must be assigned at next step
 	int pendingJointCount;
 

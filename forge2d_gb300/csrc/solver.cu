@@ -779,6 +779,149 @@ template <class BA> static __device__ void restitution_overflow( const DWorld& w
 	ba.store( idx.y, B );
 }
 
+// ---------------------------------------------------------------------------
+// Overflow levels. The reference solves the overflow joints and then the
+// overflow contacts one after another on its main thread (solver.c:1008-1009,
+// 1027-1028, 1055-1056, 1077). Here those constraints are split into levels:
+// constraint e (joints first, then contacts, each in overflow-array order)
+// joins level r when every earlier overflow constraint that shares a
+// non-static body with it sits in a level below r (as-soon-as-possible
+// scheduling of each body's constraint order). Constraints of one level touch
+// disjoint bodies and every body meets its constraints in the serial order,
+// so one block solving the levels one after another, with a block barrier
+// between levels, produces the serial sweep's values bit for bit.
+#define OVF_MAX_LEVELS 64	 // rounds of level assignment; the rest go serial
+#define OVF_SMEM_ITEMS 3072 // level-ordered list kept in shared memory
+
+struct OvfPlan
+{
+	const int* order; // constraints in level order
+	int levels;		  // parallel levels
+	int n;			  // overflow joints + contacts
+	int nj;			  // overflow joints
+};
+
+static __device__ __forceinline__ int2 ovf_bodies( const DWorld& w, int e, int nj )
+{
+	return e < nj ? w.jindex[w.overflowJoints[e]] : w.kIndex[e - nj];
+}
+
+// All threads of one block. Writes the level-ordered list into order (n
+// entries) and the level starts into levelStart (OVF_MAX_LEVELS + 1 entries,
+// shared memory). Constraints left after OVF_MAX_LEVELS rounds follow in
+// ascending order as one serial tail.
+static __device__ OvfPlan ovf_schedule( const DWorld& w, int* order, int* levelStart )
+{
+	__shared__ int sPos;
+	OvfPlan plan;
+	plan.nj = w.sc->overflowJointCount;
+	plan.n = plan.nj + w.sc->overflowCount;
+	plan.order = order;
+	const int n = plan.n, nj = plan.nj;
+	int* level = w.ovfLevel;
+	int* owner = w.ovfOwner;
+	for ( int e = threadIdx.x; e < n; e += blockDim.x )
+		__stcg( level + e, -1 );
+	if ( threadIdx.x == 0 )
+	{
+		sPos = 0;
+		levelStart[0] = 0;
+	}
+	__syncthreads();
+	int r = 0;
+	while ( r < OVF_MAX_LEVELS && sPos < n )
+	{
+		for ( int e = threadIdx.x; e < n; e += blockDim.x )
+			if ( __ldcg( level + e ) < 0 )
+			{
+				int2 b = ovf_bodies( w, e, nj );
+				if ( b.x >= 0 )
+					__stcg( owner + b.x, 0x7fffffff );
+				if ( b.y >= 0 )
+					__stcg( owner + b.y, 0x7fffffff );
+			}
+		__syncthreads();
+		for ( int e = threadIdx.x; e < n; e += blockDim.x )
+			if ( __ldcg( level + e ) < 0 )
+			{
+				int2 b = ovf_bodies( w, e, nj );
+				if ( b.x >= 0 )
+					atomicMin( owner + b.x, e );
+				if ( b.y >= 0 )
+					atomicMin( owner + b.y, e );
+			}
+		__syncthreads();
+		for ( int e = threadIdx.x; e < n; e += blockDim.x )
+			if ( __ldcg( level + e ) < 0 )
+			{
+				int2 b = ovf_bodies( w, e, nj );
+				bool first = ( b.x < 0 || __ldcg( owner + b.x ) == e ) && ( b.y < 0 || __ldcg( owner + b.y ) == e );
+				if ( first )
+				{
+					__stcg( level + e, r );
+					order[atomicAdd( &sPos, 1 )] = e;
+				}
+			}
+		__syncthreads();
+		r += 1;
+		if ( threadIdx.x == 0 )
+			levelStart[r] = sPos;
+		__syncthreads();
+	}
+	plan.levels = r;
+	if ( threadIdx.x == 0 && sPos < n )
+	{
+		int pos = sPos;
+		for ( int e = 0; e < n; ++e )
+			if ( __ldcg( level + e ) < 0 )
+				order[pos++] = e;
+	}
+	__syncthreads();
+	return plan;
+}
+
+// kind 0 warm start, 1 solve, 2 relax, 3 restitution (contacts only)
+template <class BA>
+static __device__ __forceinline__ void ovf_item( const DWorld& w, const BA& ba, int e, int nj, int kind,
+												  const SolveParams& p )
+{
+	if ( e < nj )
+	{
+		int j = w.overflowJoints[e];
+		if ( kind == 0 )
+			joint_warm_start( w, ba, j );
+		else if ( kind < 3 )
+			joint_solve( w, ba, j, p.h, p.inv_h, kind == 1 );
+		return;
+	}
+	int k = e - nj;
+	if ( kind == 0 )
+		warm_overflow( w, ba, k );
+	else if ( kind < 3 )
+		solve_overflow( w, ba, k, p.inv_h, p.pushout, kind == 1 );
+	else
+		restitution_overflow( w, ba, k, p.restitutionThreshold );
+}
+
+// All threads of the scheduling block: the overflow constraints level by
+// level, then the serial tail on thread 0.
+template <class BA>
+static __device__ void ovf_stage( const DWorld& w, const BA& ba, const OvfPlan& plan, const int* levelStart, int kind,
+								  const SolveParams& p )
+{
+	for ( int l = 0; l < plan.levels; ++l )
+	{
+		int end = levelStart[l + 1];
+		for ( int i = levelStart[l] + threadIdx.x; i < end; i += blockDim.x )
+			ovf_item( w, ba, plan.order[i], plan.nj, kind, p );
+		__syncthreads();
+	}
+	if ( threadIdx.x == 0 )
+		for ( int i = levelStart[plan.levels]; i < plan.n; ++i )
+			ovf_item( w, ba, plan.order[i], plan.nj, kind, p );
+	__syncthreads();
+}
+
 __device__ __forceinline__ void integrate_velocity( const DWorld& w, int b, const SolveParams& p )
 {
 	float4 v4 = w.vel[b];
@@ -947,6 +1090,12 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 	for ( int c = 0; c < F2D_OVERFLOW; ++c )
 		if ( sCount[c] > 0 || sJStart[c + 1] > sJStart[c] )
 			activeMask |= 1u << c;
+	// block 0 solves the overflow constraints, level by level
+	__shared__ int sLevelStart[OVF_MAX_LEVELS + 1];
+	__shared__ int sOrder[OVF_SMEM_ITEMS];
+	OvfPlan plan = {};
+	if ( serialStage && blockIdx.x == 0 )
+		plan = ovf_schedule( w, novf + novfJ <= OVF_SMEM_ITEMS ? sOrder : w.ovfOrder, sLevelStart );
 
 	const int r0 = threadIdx.x * gridDim.x + blockIdx.x;
 	Lane L0;
@@ -990,24 +1139,8 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 			}
 			if ( serialStage )
 			{
-				if ( gtid == 0 )
-				{
-					for ( int k = 0; k < novfJ; ++k )
-					{
-						int j = w.overflowJoints[k];
-						if ( kind == 0 )
-							joint_warm_start( w, gb, j );
-						else
-							joint_solve( w, gb, j, p.h, p.inv_h, kind == 1 );
-					}
-					for ( int k = 0; k < novf; ++k )
-					{
-						if ( kind == 0 )
-							warm_overflow( w, gb, k );
-						else
-							solve_overflow( w, gb, k, p.inv_h, p.pushout, kind == 1 );
-					}
-				}
+				if ( blockIdx.x == 0 )
+					ovf_stage( w, gb, plan, sLevelStart, kind, p );
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
@@ -1027,9 +1160,8 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 	// restitution: overflow then colours (solver.c:1103-1117)
 	if ( novf > 0 )
 	{
-		if ( gtid == 0 )
-			for ( int k = 0; k < novf; ++k )
-				restitution_overflow( w, gb, k, p.restitutionThreshold );
+		if ( blockIdx.x == 0 )
+			ovf_stage( w, gb, plan, sLevelStart, 3, p );
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
@@ -1146,6 +1278,12 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 	for ( int c = 0; c < F2D_OVERFLOW; ++c )
 		if ( sCount[c] > 0 || sJStart[c + 1] > sJStart[c] )
 			activeMask |= 1u << c;
+	// block 0 of the cluster solves the overflow constraints, level by level
+	__shared__ int sLevelStart[OVF_MAX_LEVELS + 1];
+	__shared__ int sOrder[OVF_SMEM_ITEMS];
+	OvfPlan plan = {};
+	if ( serialStage && rank == 0 )
+		plan = ovf_schedule( w, novf + novfJ <= OVF_SMEM_ITEMS ? sOrder : w.ovfOrder, sLevelStart );
 	// colour slot r = threadIdx.x * F2D_CLUSTER + rank (+ stride ...) belongs to
 	// this thread; the first one stays in registers for the whole launch
 	const int r0 = threadIdx.x * F2D_CLUSTER + rank;
@@ -1192,24 +1330,8 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 			}
 			if ( serialStage )
 			{
-				if ( tid == 0 )
-				{
-					for ( int k = 0; k < novfJ; ++k )
-					{
-						int j = w.overflowJoints[k];
-						if ( kind == 0 )
-							joint_warm_start( w, cb, j );
-						else
-							joint_solve( w, cb, j, p.h, p.inv_h, kind == 1 );
-					}
-					for ( int k = 0; k < novf; ++k )
-					{
-						if ( kind == 0 )
-							warm_overflow( w, cb, k );
-						else
-							solve_overflow( w, cb, k, p.inv_h, p.pushout, kind == 1 );
-					}
-				}
+				if ( rank == 0 )
+					ovf_stage( w, cb, plan, sLevelStart, kind, p );
 				cl.sync();
 			}
 			for ( int c = 0; c < F2D_OVERFLOW; ++c )
@@ -1227,9 +1349,8 @@ __global__ void __launch_bounds__( CLUSTER_THREADS ) k_solve_cluster( DWorld w, 
 	// restitution: overflow then colours (solver.c:1103-1117)
 	if ( novf > 0 )
 	{
-		if ( tid == 0 )
-			for ( int k = 0; k < novf; ++k )
-				restitution_overflow( w, cb, k, p.restitutionThreshold );
+		if ( rank == 0 )
+			ovf_stage( w, cb, plan, sLevelStart, 3, p );
 		cl.sync();
 	}
 	for ( int c = 0; c < F2D_OVERFLOW; ++c )
@@ -1269,7 +1390,13 @@ int solver_cluster_capacity()
 	int dev = 0, optin = 0;
 	cudaGetDevice( &dev );
 	cudaDeviceGetAttribute( &optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev );
-	int dyn = optin - 1024; // static shared memory of the kernel and a margin
+	cudaFuncAttributes fa = {};
+	if ( cudaFuncGetAttributes( &fa, k_solve_cluster ) != cudaSuccess )
+	{
+		cudaGetLastError();
+		return 0;
+	}
+	int dyn = optin - (int)fa.sharedSizeBytes - 256; // less the static shared memory and a margin
 	if ( dyn < 32 * 64 )
 		return 0;
 	if ( cudaFuncSetAttribute( k_solve_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) != cudaSuccess ||

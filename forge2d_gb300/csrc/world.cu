@@ -177,6 +177,12 @@ static void alloc_scratch( HostWorld* W )
 		bits += 1;
 	s.shapeIdBits = bits;
 	d.pairKeyBits = bits;
+	dfree( d.ovfOwner );
+	dfree( d.ovfLevel );
+	dfree( d.ovfOrder );
+	dgrow( d.ovfOwner, 0, (size_t)d.bodyCap );
+	dgrow( d.ovfLevel, 0, (size_t)d.contactCap + d.jointCap );
+	dgrow( d.ovfOrder, 0, (size_t)d.contactCap + d.jointCap );
 	s.solverThreads = 512;
 	s.solverBlocks = solver_max_blocks( 512 );
 	s.solverBlocks256 = solver_max_blocks( 256 );
@@ -647,7 +653,7 @@ static void free_world( HostWorld* W )
 	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( slotContact ); F( overflowList );
 	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
 	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 );
-	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints );
+	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F

@@ -243,6 +243,44 @@ def joint_gallery(b, copies=4):
                                        collideConnected=1))
 
 
+def overflow_heap(b, platforms=6, per=24, long_count=160, spokes=16):
+    """Bodies with more constraints than the graph has colours: ``platforms``
+    dynamic planks each carrying a row of ``per`` circles (r 0.25) with a
+    second row on top, one long plank under ``long_count`` circles (one body
+    whose overflow contacts form a single long chain), and a hub with
+    ``spokes`` revolute spokes (overflow joints), over a static ground."""
+    g = b.create_body(body_def(type=STATIC, positionY=-1.0))
+    b.create_box(g, shape_def(), 200.0, 1.0)
+    x = -150.0
+    for k in range(platforms):
+        hx = 0.25 * per
+        plank = b.create_body(body_def(type=DYNAMIC, positionX=x + hx, positionY=0.3))
+        b.create_box(plank, shape_def(), hx, 0.25)
+        for row in range(2):
+            for i in range(per - row):
+                c = b.create_body(body_def(type=DYNAMIC, positionX=x + 0.25 + 0.5 * i + 0.25 * row,
+                                           positionY=0.8 + 0.45 * row + 0.01 * k))
+                b.create_circle(c, shape_def(friction=0.4), 0.0, 0.0, 0.25)
+        x += 2.0 * hx + 3.0
+    hx = 0.25 * long_count
+    plank = b.create_body(body_def(type=DYNAMIC, positionX=x + hx, positionY=0.3))
+    b.create_box(plank, shape_def(), hx, 0.25)
+    for i in range(long_count):
+        c = b.create_body(body_def(type=DYNAMIC, positionX=x + 0.25 + 0.5 * i, positionY=0.8))
+        b.create_circle(c, shape_def(), 0.0, 0.0, 0.25)
+    x += 2.0 * hx + 5.0
+    hub = b.create_body(body_def(type=DYNAMIC, positionX=x, positionY=3.0))
+    b.create_circle(hub, shape_def(), 0.0, 0.0, 0.5)
+    for k in range(spokes):
+        a = 2.0 * math.pi * k / spokes
+        sx, sy = x + 1.5 * math.cos(a), 3.0 + 1.5 * math.sin(a)
+        s = b.create_body(body_def(type=DYNAMIC, positionX=sx, positionY=sy,
+                                   rotationCos=math.cos(a), rotationSin=math.sin(a)))
+        b.create_box(s, shape_def(), 0.3, 0.15)
+        b.create_revolute(revolute_def(bodyA=hub, bodyB=s, localAnchorBX=-1.5,
+                                       enableSpring=1, hertz=4.0, dampingRatio=0.5))
+
+
 def batched(b, worlds=4096, seed=7, tile=220.0, columns=64, only=None):
     """BASELINE config 4: ``worlds`` independent sub-worlds of uneven size,
     each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
@@ -323,4 +361,6 @@ def build(b, name, **kw):
         return joint_gallery(b, **kw)
     if name == "batched":
         return batched(b, **kw)
+    if name == "overflow_heap":
+        return overflow_heap(b, **kw)
     raise ValueError(name)

@@ -54,6 +54,12 @@ NATIVE = [
     ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300, 25),
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400, 25),
     ("batched24", dict(enableSleep=0, enableContinuous=1), "batched", dict(worlds=24, seed=3), 200, 25),
+    # overflow constraints solved by levels: a 150-deep chain (past the
+    # parallel levels, into the serial tail), overflow joints, and many
+    # short independent chains
+    ("overflow_heap", dict(enableSleep=0, enableContinuous=1), "overflow_heap", dict(), 200, 25),
+    ("overflow_platforms", dict(enableSleep=0), "overflow_heap",
+     dict(platforms=12, per=30, long_count=8, spokes=0), 120, 20),
 ]
 
 
@@ -75,7 +81,7 @@ def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, fra
             assert np.array_equal(gc, pc), "frame %d colours gpu %s port %s" % (f, gc, pc)
             saw_overflow |= bool(gc[11] > 0)
     assert g.sync() == 0
-    if name == "pile_dense_overflow":
+    if name in ("pile_dense_overflow", "overflow_heap", "overflow_platforms"):
         assert saw_overflow, "scene meant to exercise the overflow colour did not reach it"
     g.close()
     p.close()
