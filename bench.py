@@ -153,6 +153,16 @@ def reduce_over_ranks(ms_total, world, device):
     return float(t.item()), world.get_world_size()
 
 
+def reduce_seconds_over_ranks(seconds, world):
+    """Host-clock seconds of the slowest rank."""
+    if world is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device="cuda")
+    world.all_reduce(t, op=world.ReduceOp.MAX)
+    return float(t.item())
+
+
 def job_throughput(nranks, bodies_per_rank, steps, ms_total):
     """Body-steps per second of the whole job (weak scaling: every rank
     steps its own replica of the workload)."""
@@ -187,6 +197,7 @@ def run_gpu(args, rank, world):
     status = 0
     launches = 0
     t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("timed_steps")
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -195,6 +206,7 @@ def run_gpu(args, rank, world):
         total_ms += g.last_step_ms()
         launches += g.last_step_launches()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     wall = time.perf_counter() - t0
     if world is not None:
         world.barrier()
@@ -202,21 +214,38 @@ def run_gpu(args, rank, world):
     counters_after = g.counters()
 
     # ---- e2e through the C ABI with host buffers ----------------------
+    # a second copy of the scene steps the same frames (W warm-up, then the
+    # K timed ones), each step followed by the read of every body row into
+    # a host buffer, timed on the host clock
+    import ctypes as C
+
     import numpy as np
 
-    n = g.lib.f2d_world_body_capacity(g.id)
-    host = np.zeros((n, 12), np.float32)
+    g2 = GpuWorld(wd)
+    scenes.build(g2, spec["scene"], **spec["kw"])
+    for _ in range(args.warmup):
+        g2.step(1.0 / 60.0, 4)
+    g2.sync()
+    n = g2.lib.f2d_world_body_capacity(g2.id)
+    host = torch.empty((max(n, 1), 12), dtype=torch.float32, pin_memory=True)
+    ptr = C.cast(host.data_ptr(), C.POINTER(C.c_float))
+    e2e_steps = args.steps
+    rows = 0
+    if world is not None:
+        world.barrier()
     torch.cuda.synchronize()
-    e2e_steps = max(1, min(args.steps, 60))
     t1 = time.perf_counter()
-    import ctypes as C
-    ptr = host.ctypes.data_as(C.POINTER(C.c_float))
     for _ in range(e2e_steps):
-        g.lib.f2d_world_step(g.id, 1.0 / 60.0, 4)
-        g.lib.f2d_world_get_bodies(g.id, ptr, n)
+        status |= g2.lib.f2d_world_step(g2.id, 1.0 / 60.0, 4)
+        rows = g2.lib.f2d_world_get_bodies(g2.id, ptr, n)
     e2e_s = time.perf_counter() - t1
+    status |= g2.sync()
+    e2e_s = reduce_seconds_over_ranks(e2e_s, world)
+    g2.close()
 
     # ---- live roofline of the dominant kernel (profiled steps) ---------
+    # three more steps of the first world after the timed frames, at the
+    # scene's densest state, with per-phase events
     g.set_profiling(True)
     reps = 3
     solve_ms, alg_bytes = [], []
@@ -264,8 +293,9 @@ def run_gpu(args, rank, world):
                    "contacts_live_end": counters_after["contacts"],
                    "touching_end": counters_after["touching"]},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(n * 12 * 4),
-                "what": "f2d_world_step + f2d_world_get_bodies (all body transforms/velocities to a host buffer)",
+                "d2h_bytes_per_step": int(rows * 12 * 4),
+                "what": "f2d_world_step + f2d_world_get_bodies (every body row: transform, velocities, "
+                        "to a pinned host buffer) on a second copy of the scene over the same frames, host clock",
                 "steps": e2e_steps},
         "roofline": {"kernel": "k_solve (persistent cooperative solver)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -572,7 +602,7 @@ def run_reference(args, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=595)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="pile100k", choices=sorted(WORKLOADS))

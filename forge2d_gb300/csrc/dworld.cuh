@@ -68,6 +68,17 @@
 //   g[2..5] polygon vertices, g[6..9] polygon normals
 #define GEOM_F4 10
 
+// Narrowphase manifold classes (one bucket and one kernel each): circle pairs,
+// capsule/segment vs circle, capsule/segment vs capsule, polygon vs circle,
+// and the pairs that go through the polygon clipper (or have no manifold).
+#define NP_CLASSES 5
+
+// Colouring op outputs: tiles of OPS_TILE ops, four look-back chains
+// (freed ids, begin events, end events, overflow ops) after a ticket word.
+#define OPS_TILE 1024
+#define OPS_SCAN_CHAINS 4
+#define OPS_SCAN_WORDS( cap ) ( 1 + OPS_SCAN_CHAINS * ( ( ( cap ) + OPS_TILE - 1 ) / OPS_TILE + 1 ) )
+
 // The tree's leaf order only sets its tightness, never the pairs it finds
 // (new pairs are sorted by key), so it is refreshed periodically.
 #define ORDER_REBUILD_PERIOD 8
@@ -104,6 +115,9 @@ struct DScalars
 	int orderPeriod; // steps between re-sorts (0: ORDER_REBUILD_PERIOD)
 	int newPointCount; // new manifold points listed by the prepare stage (learned warm start)
 	int sampleCount;   // training samples recorded so far
+	int npCount[8];	   // narrowphase: live overlapping contacts per manifold class
+	int pendingOps;	   // colouring: ops left after the first round
+	int overflowOps;   // colouring: ops that add to / remove from the overflow colour
 	int pad[2];
 };
 
@@ -217,6 +231,8 @@ struct DWorld
 	int* opKind;	// 0 destroy, 1 begin, 2 end
 	int* opColor;	// colour result / colour removed
 	int* opDone;
+	int2* opBodies; // solver body indices of the op's contact (-1 static)
+	unsigned long long* opScan; // look-back state of the op output scans
 
 	// ---------------- constraints (by slot, grouped by colour) ----------------
 	int* slotContact;
@@ -252,6 +268,7 @@ struct DWorld
 	// overflow levels (solver scratch): body owner per level round, level
 	// per overflow constraint, constraints in level order beyond the
 	// shared-memory list
+	int* npBucket; // narrowphase: contact ids by manifold class, NP_CLASSES x contactCap
 	int* ovfOwner; // bodyCap
 	int* ovfLevel; // contactCap + jointCap
 	int* ovfOrder; // contactCap + jointCap

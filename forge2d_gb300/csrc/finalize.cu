@@ -460,6 +460,8 @@ __global__ void k_reset_step_counters( DWorld w )
 	w.sc->hitCount = 0;
 	w.sc->fastCount = 0;
 	w.sc->newPointCount = 0;
+	for ( int k = 0; k < 8; ++k )
+		w.sc->npCount[k] = 0;
 	int age = w.sc->orderAge;
 	int period = w.sc->orderPeriod > 0 ? w.sc->orderPeriod : ORDER_REBUILD_PERIOD;
 	int rebuild = ( w.sc->forceRebuild != 0 || age >= period - 1 ) ? 1 : 0;

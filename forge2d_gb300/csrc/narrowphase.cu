@@ -18,24 +18,93 @@ __device__ __forceinline__ float shape_radius( int type, const float4* g )
 	return ( type == ST_CIRCLE || type == ST_CAPSULE || type == ST_POLYGON ) ? g[1].x : 0.0f;
 }
 
-__global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
+// Manifold class of a contact (shape A's type >= shape B's type, the
+// registry order of contact.c:151-205).
+__device__ __forceinline__ int manifold_class( int ta, int tb )
 {
-	int n = w.sc->contactIdCount;
-	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	if ( ta == ST_CIRCLE && tb == ST_CIRCLE )
+		return 0;
+	if ( ( ta == ST_CAPSULE || ta == ST_SEGMENT ) && tb == ST_CIRCLE )
+		return 1;
+	if ( ( ta == ST_CAPSULE || ta == ST_SEGMENT ) && tb == ST_CAPSULE )
+		return 2;
+	if ( ta == ST_POLYGON && tb == ST_CIRCLE )
+		return 3;
+	return 4;
+}
+
+// The manifold function compute_manifold selects for the class, called
+// directly so that each class kernel holds only its own path.
+template <int CLS>
+__device__ __forceinline__ DManifold class_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB )
+{
+	if ( CLS == 0 )
+		return collide_circles( a.c1, a.radius, xfA, b.c1, b.radius, xfB );
+	if ( CLS == 1 )
+		return collide_capsule_circle( a.c1, a.c2, a.type == ST_SEGMENT ? 0.0f : a.radius, xfA, b.c1, b.radius, xfB );
+	if ( CLS == 2 )
+		return collide_capsules( a.c1, a.c2, a.type == ST_SEGMENT ? 0.0f : a.radius, xfA, b.c1, b.c2, b.radius, xfB );
+	if ( CLS == 3 )
+		return collide_polygon_circle( a.poly, xfA, b.c1, b.radius, xfB );
+	return compute_manifold( a, xfA, b, xfB );
+}
+
+// Fat-AABB test of every live contact (b2CollideTask's disjoint check); the
+// overlapping ones are listed by manifold class so that every warp of a
+// class kernel runs one manifold function. Bucket order is irrelevant: each
+// contact's update depends on that contact alone.
+__global__ void k_np_classify( DWorld w )
+{
+	const int n = w.sc->contactIdCount;
+	const unsigned lane = threadIdx.x & 31u;
+	// grid-stride with a block-uniform trip count: the append is warp-collective
+	for ( int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x )
 	{
-		int flags = w.cflags[c];
-		if ( ( flags & CF_USED ) == 0 )
-			continue;
-		int2 sh = w.cshape[c];
-		fbox fa = box_from4( w.fat[sh.x] );
-		fbox fb = box_from4( w.fat[sh.y] );
-		if ( !box_overlaps( fa, fb ) )
+		int c = base + threadIdx.x;
+		int cls = -1;
+		if ( c < n )
 		{
-			flags |= CF_DISJOINT;
-			flags &= ~CF_SIM_TOUCHING;
-			w.cflags[c] = flags;
-			continue;
+			int flags = w.cflags[c];
+			if ( flags & CF_USED )
+			{
+				int2 sh = w.cshape[c];
+				fbox fa = box_from4( w.fat[sh.x] );
+				fbox fb = box_from4( w.fat[sh.y] );
+				if ( !box_overlaps( fa, fb ) )
+				{
+					flags |= CF_DISJOINT;
+					flags &= ~CF_SIM_TOUCHING;
+					w.cflags[c] = flags;
+				}
+				else
+					cls = manifold_class( shape_type( w.sflags[sh.x] ), shape_type( w.sflags[sh.y] ) );
+			}
 		}
+		// warp-aggregated append per class
+		unsigned peers = __match_any_sync( 0xffffffffu, cls );
+		if ( cls >= 0 )
+		{
+			int leader = __ffs( peers ) - 1;
+			int slot = 0;
+			if ( (int)lane == leader )
+				slot = atomicAdd( w.sc->npCount + cls, __popc( peers ) );
+			slot = __shfl_sync( peers, slot, leader );
+			int rank = __popc( peers & ( ( 1u << lane ) - 1u ) );
+			w.npBucket[(size_t)cls * w.contactCap + slot + rank] = c;
+		}
+	}
+}
+
+// b2UpdateContact (contact.c:472-600) for the contacts of one class.
+template <int CLS> __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
+{
+	const int n = w.sc->npCount[CLS];
+	const int* bucket = w.npBucket + (size_t)CLS * w.contactCap;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		int c = bucket[i];
+		int flags = w.cflags[c];
+		int2 sh = w.cshape[c];
 		bool wasTouching = ( flags & CF_SIM_TOUCHING ) != 0;
 		int2 bd = w.cbody[c];
 		float4 ma = w.massv[bd.x], mb = w.massv[bd.y];
@@ -57,7 +126,7 @@ __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
 		const float4* gb = w.geom + (size_t)sh.y * GEOM_F4;
 		DGeom A = load_geom( ga, ta );
 		DGeom B = load_geom( gb, tb );
-		DManifold m = compute_manifold( A, xfA, B, xfB );
+		DManifold m = class_manifold<CLS>( A, xfA, B, xfB );
 
 		float4 mta = w.mat[sh.x], mtb = w.mat[sh.y];
 		float friction = sqrtf( mta.x * mtb.x );
@@ -179,9 +248,14 @@ __global__ void k_op_clamp( DWorld w )
 void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st )
 {
 	int g = ( w.contactCap + NP_THREADS - 1 ) / NP_THREADS;
-	if ( g > F2D_SMS * 16 )
-		g = F2D_SMS * 16;
-	k_narrowphase<<<g, NP_THREADS, 0, st>>>( w );
+	if ( g > F2D_SMS * 8 )
+		g = F2D_SMS * 8;
+	k_np_classify<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
+	k_narrowphase<0><<<g, NP_THREADS, 0, st>>>( w );
+	k_narrowphase<1><<<g, NP_THREADS, 0, st>>>( w );
+	k_narrowphase<2><<<g, NP_THREADS, 0, st>>>( w );
+	k_narrowphase<3><<<g, NP_THREADS, 0, st>>>( w );
+	k_narrowphase<4><<<g, NP_THREADS, 0, st>>>( w );
 	k_op_flags<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA );
 	scan_lookback( s.tmpA, s.tmpB, &w.sc->contactIdCount, 0, w.contactCap, &w.sc->opCount, s.scanState, &w.sc->error,
 				   st );

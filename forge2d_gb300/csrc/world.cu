@@ -235,8 +235,11 @@ static void grow_contacts( HostWorld* W, int cap )
 	dgrow( d.opKind, 0, cap );
 	dgrow( d.opColor, 0, cap );
 	dgrow( d.opDone, 0, cap );
+	dgrow( d.opBodies, 0, cap );
+	dgrow( d.opScan, 0, (size_t)OPS_SCAN_WORDS( cap ) );
 	dgrow( d.slotContact, 0, cap );
 	dgrow( d.overflowList, o, cap );
+	dgrow( d.npBucket, 0, (size_t)NP_CLASSES * cap );
 	dgrow( d.kIndex, 0, cap );
 	dgrow( d.kMass, 0, cap );
 	dgrow( d.kNormal, 0, cap );
@@ -650,10 +653,10 @@ static void free_world( HostWorld* W )
 	F( cmass ); F( mnorm ); F( mpA ); F( mpB ); F( mpI ); F( contactFree ); F( pairHash ); F( mortonKeys );
 	F( mortonKeysAlt ); F( leafShape ); F( leafShapeAlt ); F( nodeLeft ); F( nodeRight ); F( nodeParent ); F( nodeBox );
 	F( nodeVisit ); F( sortHist ); F( pairKeys ); F( pairKeysAlt ); F( pairVal ); F( pairValAlt ); F( planIds );
-	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( slotContact ); F( overflowList );
+	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( opBodies ); F( opScan ); F( slotContact ); F( overflowList );
 	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
 	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 );
-	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
+	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F

@@ -250,7 +250,7 @@ def overflow_heap(b, platforms=6, per=24, long_count=160, spokes=16):
     whose overflow contacts form a single long chain), and a hub with
     ``spokes`` revolute spokes (overflow joints), over a static ground."""
     g = b.create_body(body_def(type=STATIC, positionY=-1.0))
-    b.create_box(g, shape_def(), 200.0, 1.0)
+    b.create_box(g, shape_def(), 200.0 + 0.5 * long_count, 1.0)
     x = -150.0
     for k in range(platforms):
         hx = 0.25 * per

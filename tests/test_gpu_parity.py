@@ -60,6 +60,8 @@ NATIVE = [
     ("overflow_heap", dict(enableSleep=0, enableContinuous=1), "overflow_heap", dict(), 200, 25),
     ("overflow_platforms", dict(enableSleep=0), "overflow_heap",
      dict(platforms=12, per=30, long_count=8, spokes=0), 120, 20),
+    # more overflow constraints than the shared-memory lists hold
+    ("overflow_long", dict(enableSleep=0), "overflow_heap", dict(platforms=0, long_count=3200, spokes=0), 40, 10),
 ]
 
 
@@ -81,7 +83,7 @@ def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, fra
             assert np.array_equal(gc, pc), "frame %d colours gpu %s port %s" % (f, gc, pc)
             saw_overflow |= bool(gc[11] > 0)
     assert g.sync() == 0
-    if name in ("pile_dense_overflow", "overflow_heap", "overflow_platforms"):
+    if name in ("pile_dense_overflow", "overflow_heap", "overflow_platforms", "overflow_long"):
         assert saw_overflow, "scene meant to exercise the overflow colour did not reach it"
     g.close()
     p.close()

@@ -1,11 +1,11 @@
 """The full-size workload (100k-body mixed pile) on the GPU.
 
-Bit-exact against the oracle for the first frames (the restatement takes
-about a second per frame at this size), then size-independent properties
-over a longer run: every step ends with status 0, states stay finite, the run
-is deterministic, every colour 0..10 holds at most one constraint per
-dynamic body, and the contact table holds one contact per shape pair with
-1-2 manifold points on every touching contact.
+Bit-exact against the oracle over the scene's whole 600 frames (the
+multithreaded restatement steps them in about ten seconds), and
+size-independent properties over a run: every step ends with status 0,
+states stay finite, the run is deterministic, every colour 0..10 holds at
+most one constraint per dynamic body, and the contact table holds one
+contact per shape pair with 1-2 manifold points on every touching contact.
 """
 from __future__ import annotations
 
@@ -43,6 +43,28 @@ def test_pile100k_first_frames_bit_exact(gpu_lib, port_lib):
         assert len(bad) == 0, "frame %d: %s" % (f, bad[0].tolist())
     assert compare_contacts(g, p) == []
     assert np.array_equal(g.color_counts(), p.color_counts())
+    g.close()
+    p.close()
+
+
+def test_pile100k_600_frames_bit_exact(gpu_lib, port_lib):
+    """The whole scene: by frame 600 the pile holds ~3.5e5 contacts (more
+    than one launch grid of threads), ~2.2e5 touching and ~1e3 overflow
+    constraints."""
+    g = make_gpu()
+    p = port_lib.PortWorld(scenes.world_def(**WKW))
+    scenes.build(p, "pile", **PILE)
+    for f in range(1, 601):
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        if f % 150 == 0:
+            gb, pb = g.bodies()[:, :9], p.bodies()[:, :9]
+            bad = np.argwhere(gb.view(np.uint32) != pb.view(np.uint32))
+            assert len(bad) == 0, "frame %d: %s" % (f, bad[0].tolist())
+            assert np.array_equal(g.color_counts(), p.color_counts()), "frame %d" % f
+    c = g.counters()
+    assert c["contacts"] > 311_296 and c["overflow"] > 0, c
+    assert compare_contacts(g, p) == []
     g.close()
     p.close()
 
