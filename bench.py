@@ -134,8 +134,10 @@ class ClockSampler:
 def solver_bytes(c):
     """Algorithmic bytes of one launch of the persistent solver kernel
     (substeps x {warm start, solve, relax} per touching contact, body
-    integration, restitution and impulse storage), per-unit figures as
-    stated in DESIGN.md."""
+    integration, restitution and impulse storage): per touching contact and
+    substep 100 + 24 B warm start, 204 + 52 B solve, 204 + 52 B relax, then
+    112 B restitution and 72 B impulse store; per awake body and substep
+    56 B velocity and 44 B position integration."""
     sub = 4
     per_contact = sub * (100 + 24 + 204 + 52 + 204 + 52) + 112 + 72
     per_body = sub * (56 + 44)
@@ -392,7 +394,7 @@ def max_penetration(world, group_of_shape=None, groups=0):
 
 
 def run_batched(args, torch):
-    """The batched form (BASELINE config 4): 4096 sub-worlds stepped as one
+    """The batched form: 4096 sub-worlds stepped as one
     world after the autotuner picked the launch shapes, against the same
     worlds stepped one at a time as plain worlds (a seeded sample), at the
     same frame, with max penetration compared."""
@@ -473,9 +475,9 @@ def kinetic_energy(world, mass):
 
 
 def run_learned(args, torch):
-    """The learned warm start (BASELINE config 5): samples recorded by the
+    """The learned warm start: samples recorded by the
     plain solver on seeded scenes of configs 2-4, the MLP trained on the GPU,
-    then the config-2 pile at 200k bodies stepped plain at 4 and 2 substeps
+    then the mixed pile at 200k bodies stepped plain at 4 and 2 substeps
     and with the learned warm start at 2 and 4 substeps: max penetration,
     kinetic-energy drift against plain at 4 substeps, world-steps/s."""
     import numpy as np
@@ -536,7 +538,7 @@ def run_learned(args, torch):
                        "ke_drift_vs_plain_4": float(np.mean(np.abs(kes - ke_ref) / np.maximum(ke_ref, 1e-9)))}
     model.close()
     return {
-        "workload": "config-2 pile at %d bodies (seed 1234), %d frames, dt=1/60; samples from a 20k pile, "
+        "workload": "mixed pile at %d bodies (seed 1234), %d frames, dt=1/60; samples from a 20k pile, "
                     "256 batched sub-worlds and a pyramids+chains scene (4 substeps, 240 frames each)"
                     % (args.learn_bodies, args.learn_frames),
         "samples": int(len(samples)), "record_s": rec_s, "train_s": train_s, "epochs": args.learn_epochs,

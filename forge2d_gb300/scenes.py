@@ -86,7 +86,7 @@ def revolute_def(**kw):
 
 def pyramid(b, rows=40, x0=None, y0=0.0, ground=True, half=0.5, friction=0.6,
             density=1.0, restitution=0.0, **shape_kw):
-    """BASELINE config 1 layout: row r has rows-r boxes, spacing 1.0, offset
+    """The 40-row pyramid layout: row r has rows-r boxes, spacing 1.0, offset
     0.5 per row, resting on a static box 100x2 centred at y=-1."""
     ids = []
     if ground:
@@ -117,7 +117,7 @@ def _polygon_points(rng, n, radius):
 def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
          frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False,
          enable_contact_events=False):
-    """BASELINE config 2: ``count`` bodies drawn from ``seed`` -- 40% circles
+    """The mixed pile: ``count`` bodies drawn from ``seed`` -- 40% circles
     r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
     30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
     uniform spawn in a width x height region above a static U-shaped
@@ -181,7 +181,7 @@ def chain(b, anchor_x, anchor_y, links=50, half_length=0.25, radius=0.1, density
 
 
 def pyramids_chains(b, pyramids=64, rows=40, chains=200, links=50, gap=2.0):
-    """BASELINE config 3: ``pyramids`` copies of the 40-row pyramid side by
+    """Stacking plus joints: ``pyramids`` copies of the 40-row pyramid side by
     side ``gap`` units apart plus ``chains`` revolute chains of ``links``
     capsule links (half-length 0.25, r 0.1) fixed to static anchors."""
     pitch = rows + gap
@@ -282,9 +282,9 @@ def overflow_heap(b, platforms=6, per=24, long_count=160, spokes=16):
 
 
 def batched(b, worlds=4096, seed=7, tile=220.0, columns=64, only=None):
-    """BASELINE config 4: ``worlds`` independent sub-worlds of uneven size,
+    """The batched scene: ``worlds`` independent sub-worlds of uneven size,
     each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
-    (20-500 shapes with the config-2 mix, in a U container sized to the
+    (20-500 shapes with the mixed pile's shape mix, in a U container sized to the
     count) or a revolute chain (10-100 links), with gravity (0, -10) tilted
     by U[-15, 15] degrees. World k sits in its own ``tile`` x ``tile`` cell of
     a ``columns``-wide grid; sub-worlds never interact even when bodies

@@ -3,10 +3,10 @@
 * ``RefWorld`` drives the unmodified Box2D v3.1.1 C library that forge2d
   vendors (packages/forge2d/third_party/box2d), compiled into
   ``oracle/_ref/libbox2d_ref.so`` together with ``oracle/ref_harness.c``.
-  It exists only where the reference checkout exists (this build container).
+  It exists only where the reference checkout exists.
 * ``PortWorld`` drives ``oracle/_build/libf2d_port.so``, the plain-C
   restatement in ``oracle/port/`` that travels with the repository and is the
-  parity checker and CPU baseline on machines without the reference.
+  parity reference and CPU baseline on machines without the reference.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline arm may
 import this module; the product package never does.

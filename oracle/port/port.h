@@ -1,5 +1,5 @@
 // Internal types of the CPU restatement of Box2D v3.1.1's world step.
-// TEST INFRASTRUCTURE (oracle): the parity checker for the CUDA path and the
+// TEST INFRASTRUCTURE (oracle): the parity reference for the CUDA path and the
 // CPU baseline on machines without the reference checkout. Each function in
 // the .c files cites the reference file:line it restates
 // (packages/forge2d/third_party/box2d/src/...).
