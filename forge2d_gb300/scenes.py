@@ -116,12 +116,17 @@ def _polygon_points(rng, n, radius):
 
 def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
          frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False,
-         enable_contact_events=False):
+         enable_contact_events=False, filters=False):
     """The mixed pile: ``count`` bodies drawn from ``seed`` -- 40% circles
     r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
     30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
     uniform spawn in a width x height region above a static U-shaped
-    container of three boxes; density 1, friction 0.6, restitution U[0,0.3]."""
+    container of three boxes; density 1, friction 0.6, restitution U[0,0.3].
+    ``filters`` gives the shapes collision filters by index: categories
+    1, 2, 4 in turn, every 5th shape's mask excludes the next category,
+    every 7th shape is in group -1 (never collides within the group), every
+    11th in group 2 (always collides within the group), every 13th is a
+    sensor."""
     rng = np.random.default_rng(seed)
     hw = 0.5 * width
     if wall_height is None:
@@ -142,8 +147,20 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
         a = float(angles[k])
         body = b.create_body(body_def(type=DYNAMIC, positionX=float(xs[k]), positionY=float(ys[k]),
                                       rotationCos=math.cos(a), rotationSin=math.sin(a)))
+        extra = {}
+        if filters:
+            cat = 1 << (k % 3)
+            extra["categoryBits"] = cat
+            if k % 5 == 0:
+                extra["maskBits"] = -1 ^ (1 << ((k + 1) % 3))
+            if k % 7 == 0:
+                extra["groupIndex"] = -1
+            elif k % 11 == 0:
+                extra["groupIndex"] = 2
+            if k % 13 == 0:
+                extra["isSensor"] = 1
         sd = shape_def(restitution=float(rest[k]), enableHitEvents=int(enable_hit_events),
-                       enableContactEvents=int(enable_contact_events))
+                       enableContactEvents=int(enable_contact_events), **extra)
         u = kinds[k]
         if u < frac_circle:
             b.create_circle(body, sd, 0.0, 0.0, float(rng.uniform(0.25, 0.75)))

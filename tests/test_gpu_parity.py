@@ -51,6 +51,8 @@ NATIVE = [
      dict(count=600, seed=2, width=24.0, height=60.0), 200, 25),
     ("pile_dense_overflow", dict(enableSleep=0, enableContinuous=1), "pile",
      dict(count=1500, seed=3, width=12.0, height=120.0, wall_height=130.0), 150, 30),
+    ("pile_filtered", dict(enableSleep=0, enableContinuous=1), "pile",
+     dict(count=700, seed=4, width=30.0, height=60.0, filters=True), 200, 25),
     ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300, 25),
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400, 25),
     ("batched24", dict(enableSleep=0, enableContinuous=1), "batched", dict(worlds=24, seed=3), 200, 25),
