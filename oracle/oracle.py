@@ -144,6 +144,8 @@ def _bind(lib, prefix):
         "cast_ray_closest": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), _P(C.c_float)]),
         "overlap_aabb": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), i]),
         "joint_color": (i, [i, i]),
+        "body_set_awake": (None, [i, i, i]),
+        "world_enable_sleeping": (None, [i, i]),
     }
     out = {}
     for name, (res, args) in sig.items():
@@ -306,6 +308,12 @@ class _CpuWorld:
 
     def awake_body_count(self):
         return self._fns["awake_body_count"](self.w)
+
+    def set_awake(self, body, awake):
+        self._fns["body_set_awake"](self.w, body, int(awake))
+
+    def enable_sleeping(self, enabled):
+        self._fns["world_enable_sleeping"](self.w, int(enabled))
 
 
 class RefWorld(_CpuWorld):

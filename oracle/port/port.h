@@ -107,6 +107,12 @@ typedef struct Body
 	// constraint in colour c < P_OVERFLOW (constraint_graph.c bodySet bitsets)
 	uint16_t colorMask;
 	int moveEventIndex; // this step's move event slot (finalize)
+	// solver set and island (body.h:17-90)
+	int setIndex, localIndex;
+	int islandId, islandPrev, islandNext;
+	int headContactKey; // contact edge list: (contactId << 1) | edge
+	int contactCount;
+	int isMarked;
 } Body;
 
 typedef struct Shape
@@ -152,6 +158,11 @@ typedef struct Contact
 	float friction, restitution, rollingResistance, tangentSpeed;
 	float invMassA, invIA, invMassB, invIB;
 	Manifold m;
+	// solver set, island and body edge lists (contact.h:44-96)
+	int setIndex;
+	int islandId, islandPrev, islandNext;
+	int edgePrev[2], edgeNext[2]; // edge 0 on bodyA's list, edge 1 on bodyB's
+	int isMarked;
 } Contact;
 
 // Per-constraint solver data (contact_solver.c:1034-1064 lanes / contact_solver.h)
@@ -214,7 +225,50 @@ typedef struct Joint
 	float axialMass;
 	Softness springSoftness, constraintSoftness;
 	float invMassA, invMassB, invIA, invIB;
+	// solver set and island (joint.h:60-100)
+	int setIndex;
+	int islandId, islandPrev, islandNext;
+	int isMarked;
 } Joint;
+
+// growable int array and LIFO id pool (id_pool.c)
+typedef struct IntArr
+{
+	int* data;
+	int count, cap;
+} IntArr;
+
+typedef struct IdPool
+{
+	IntArr freeIds;
+	int next;
+} IdPool;
+
+// solver sets (solver_set.h): 0 static, 1 disabled, 2 awake, 3.. sleeping
+enum
+{
+	SET_STATIC = 0,
+	SET_DISABLED = 1,
+	SET_AWAKE = 2,
+	SET_FIRST_SLEEPING = 3,
+};
+
+typedef struct SolverSet
+{
+	int setIndex; // P_NULL when free
+	IntArr bodies, contacts, joints, islands; // ids in set order
+} SolverSet;
+
+// island.h:30-60
+typedef struct Island
+{
+	int setIndex, localIndex, islandId;
+	int headBody, tailBody, bodyCount;
+	int headContact, tailContact, contactCount;
+	int headJoint, tailJoint, jointCount;
+	int parentIsland;
+	int constraintRemoveCount;
+} Island;
 
 typedef struct TreeIds
 {
@@ -307,7 +361,46 @@ typedef struct World
 	int jointOrderCap;
 
 	int stepIndex;
+
+	// islands and solver sets
+	Island* islands;
+	int islandCap;
+	IdPool islandPool;
+	SolverSet* sets;
+	int setCap;
+	IdPool setPool;
+	int splitIslandId;
+	int* moveEventAsleep; // fellAsleep flag per move event
+	int moveEventAsleepCap;
 } World;
+
+// islands and solver sets (pisland.c)
+void ia_push( IntArr* a, int v );
+int ia_remove_swap( IntArr* a, int index );
+void ia_free( IntArr* a );
+void p_sets_init( World* w );
+void p_sets_free( World* w );
+int p_set_body_add( World* w, int setId, int bodyId );
+void p_create_island_for_body( World* w, int setId, int bodyId );
+void p_contact_edges_link( World* w, int cid );
+void p_contact_edges_unlink( World* w, int cid );
+void p_link_contact( World* w, int cid );
+void p_unlink_contact( World* w, int cid );
+void p_link_joint( World* w, int jid, int mergeIslands );
+void p_merge_awake_islands( World* w );
+void p_split_island( World* w, int baseId );
+void p_try_sleep_island( World* w, int islandId );
+void p_wake_solver_set( World* w, int setId );
+void p_sleep_islands( World* w, const unsigned char* awakeIslandBits, int splitCandidate );
+int p_body_awake( const World* w, int bodyId );
+int p_new_sleeping_set( World* w );
+void p_set_joint_add( World* w, int setId, int jid );
+void p_merge_solver_sets( World* w, int setId1, int setId2 );
+// constraint graph (pworld.c)
+void p_add_contact_to_graph( World* w, int cid );
+void p_remove_contact_from_graph( World* w, int cid );
+void p_add_joint_to_graph( World* w, int jid );
+void p_remove_joint_from_graph( World* w, int jid );
 
 // geometry (pgeom.c)
 int p_compute_hull( const v2* points, int count, v2* hull );

@@ -570,7 +570,7 @@ static void integrate_velocities( World* w, Body* b, float h, float maxLinearSpe
 
 static int body_awake( const Body* b )
 {
-	return b->used && b->enabled && b->type != BODY_STATIC;
+	return b->used && b->setIndex == SET_AWAKE;
 }
 
 // solver.c:543-726 (b2FinalizeBodiesTask), excluding island bookkeeping
@@ -681,10 +681,10 @@ void p_solve( World* w, float dt, int subStepCount )
 	float jointHertz = fminp( 60.0f, 0.25f * inv_h );
 	Softness jointSoftness = p_make_soft( jointHertz, 2.0f, h );
 
-	int awakeCount = 0;
-	for ( int i = 0; i < w->bodyCount; ++i )
-		if ( body_awake( w->bodies + i ) )
-			awakeCount += 1;
+	// solver.c:1194-1220: merge islands linked this step; nothing to solve
+	// without awake bodies
+	p_merge_awake_islands( w );
+	int awakeCount = w->sets[SET_AWAKE].bodies.count;
 	if ( awakeCount == 0 )
 		return;
 
@@ -847,20 +847,50 @@ void p_solve( World* w, float dt, int subStepCount )
 		store_impulses( w, K + k, 1 );
 
 	double tp3 = p_now();
-	// finalize bodies; move events in body id order, one slot per awake body
+	// island split of the previous step's candidate (solver.c:1473-1487,
+	// finished before the bodies are finalized)
+	if ( w->splitIslandId != P_NULL )
+		p_split_island( w, w->splitIslandId );
+	w->splitIslandId = P_NULL;
+	// finalize bodies; move events in awake-set order, one slot per awake body
+	const IntArr* awakeBodies = &w->sets[SET_AWAKE].bodies;
+	int awakeIslandCount = w->sets[SET_AWAKE].islands.count;
 	{
-		int ne = 0;
-		for ( int b = 0; b < bodyCount; ++b )
-			if ( body_awake( w->bodies + b ) )
-				w->bodies[b].moveEventIndex = ne++;
+		int ne = awakeBodies->count;
+		for ( int i = 0; i < ne; ++i )
+			w->bodies[awakeBodies->data[i]].moveEventIndex = i;
 		w->moveEventBodies = grow( w->moveEventBodies, &w->moveEventCap, ne + 1, sizeof( int ) );
 		w->moveEventXf = grow( w->moveEventXf, &w->moveEventXfCap, 4 * ( ne + 1 ), sizeof( float ) );
+		w->moveEventAsleep = grow( w->moveEventAsleep, &w->moveEventAsleepCap, ne + 1, sizeof( int ) );
+		memset( w->moveEventAsleep, 0, sizeof( int ) * (size_t)( ne + 1 ) );
 		w->moveEventCount = ne;
 	}
 #pragma omp parallel for schedule( dynamic, 512 )
 	for ( int b = 0; b < bodyCount; ++b )
 		if ( body_awake( w->bodies + b ) )
 			finalize_body( w, b, dt, inv_dt );
+	// island keep-awake bits and the split candidate (solver.c:658-675), in
+	// awake-set order as one task context sees them
+	unsigned char* awakeIslandBits = (unsigned char*)calloc( (size_t)awakeIslandCount + 1, 1 );
+	int splitCandidate = P_NULL;
+	{
+		float splitSleepTime = 0.0f;
+		for ( int i = 0; i < awakeBodies->count; ++i )
+		{
+			Body* b = w->bodies + awakeBodies->data[i];
+			Island* isl = w->islands + b->islandId;
+			if ( b->sleepTime < P_TIME_TO_SLEEP )
+				awakeIslandBits[isl->localIndex] = 1;
+			else if ( isl->constraintRemoveCount > 0 )
+			{
+				if ( b->sleepTime > splitSleepTime )
+				{
+					splitCandidate = b->islandId;
+					splitSleepTime = b->sleepTime;
+				}
+			}
+		}
+	}
 	double tp4 = p_now();
 
 	// hit events (solver.c:1758-1818): colours in order, overflow last. Within a
@@ -911,6 +941,10 @@ void p_solve( World* w, float dt, int subStepCount )
 			}
 		}
 	}
+	// island sleeping, last (solver.c:1995-2048)
+	if ( w->enableSleep )
+		p_sleep_islands( w, awakeIslandBits, splitCandidate );
+	free( awakeIslandBits );
 	double tp5 = p_now();
 	g_portPhase[3] += tp1 - tp0;
 	g_portPhase[4] += tp2 - tp1;

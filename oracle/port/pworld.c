@@ -196,6 +196,7 @@ int orc_create_world( const f2d_world_def* d, int workerCount )
 	w->enableSleep = d->enableSleep != 0;
 	w->enableContinuous = d->enableContinuous != 0;
 	w->enableWarmStarting = 1;
+	p_sets_init( w );
 	return slot;
 }
 
@@ -229,6 +230,7 @@ void orc_destroy_world( int wi )
 	free( w->constraintOrder );
 	free( w->staticShapes );
 	free( w->jointOrder );
+	p_sets_free( w );
 	memset( w, 0, sizeof( *w ) );
 }
 
@@ -289,6 +291,23 @@ int orc_create_body( int wi, const f2d_body_def* d )
 	b->headJoint = P_NULL;
 	b->sleepThreshold = (float)d->sleepThreshold;
 	b->enableSleep = d->enableSleep != 0;
+	b->islandId = b->islandPrev = b->islandNext = P_NULL;
+	b->headContactKey = P_NULL;
+	b->moveEventIndex = P_NULL;
+	// solver set (body.c:225-260): disabled, static, awake, or a new sleeping
+	// set; dynamic and kinematic bodies get an island
+	int setId;
+	if ( b->enabled == 0 )
+		setId = SET_DISABLED;
+	else if ( b->type == BODY_STATIC )
+		setId = SET_STATIC;
+	else if ( d->isAwake )
+		setId = SET_AWAKE;
+	else
+		setId = p_new_sleeping_set( w );
+	p_set_body_add( w, setId, id );
+	if ( setId >= SET_AWAKE )
+		p_create_island_for_body( w, setId, id );
 	return id;
 }
 
@@ -593,21 +612,75 @@ int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
 	j->constraintSoftness.massScale = 1.0f;
 	j->constraintSoftness.impulseScale = 0.0f;
 
-	// a joint between two static bodies lives in the static set, outside the
-	// graph; every other joint between enabled bodies is coloured now
-	int staticA = a->type == BODY_STATIC, staticB = b->type == BODY_STATIC;
-	if ( a->enabled && b->enabled && !( staticA && staticB ) )
+	// solver set of the joint (joint.c:196-292): disabled, static, awake (in
+	// the graph, waking the other body's set), or the sleeping set of its
+	// bodies; then the island edge (joint.c:300-306)
+	j->islandId = j->islandPrev = j->islandNext = P_NULL;
+	int setA = a->setIndex, setB = b->setIndex;
+	int maxSet = setA > setB ? setA : setB;
+	if ( setA == SET_DISABLED || setB == SET_DISABLED )
+		j->setIndex = SET_DISABLED;
+	else if ( setA == SET_STATIC && setB == SET_STATIC )
+		j->setIndex = SET_STATIC;
+	else if ( setA == SET_AWAKE || setB == SET_AWAKE )
 	{
-		j->color = assign_joint_color( w, d->bodyA, d->bodyB );
-		if ( j->color == P_OVERFLOW )
-		{
-			w->overflowJoints =
-				grow( w->overflowJoints, &w->overflowJointCap, w->overflowJointCount + 1, sizeof( int ) );
-			j->overflowIndex = w->overflowJointCount;
-			w->overflowJoints[w->overflowJointCount++] = id;
-		}
+		if ( maxSet >= SET_FIRST_SLEEPING )
+			p_wake_solver_set( w, maxSet );
+		j->setIndex = SET_AWAKE;
+		p_add_joint_to_graph( w, id );
 	}
+	else
+	{
+		j->setIndex = maxSet;
+		p_set_joint_add( w, maxSet, id );
+		if ( setA != setB && setA >= SET_FIRST_SLEEPING && setB >= SET_FIRST_SLEEPING )
+			p_merge_solver_sets( w, setA, setB );
+	}
+	if ( j->setIndex > SET_DISABLED )
+		p_link_joint( w, id, 1 );
 	return id;
+}
+
+// constraint_graph.c:271-288 b2CreateJointInGraph / b2AddJointToGraph
+void p_add_joint_to_graph( World* w, int jid )
+{
+	Joint* j = w->joints + jid;
+	j->color = assign_joint_color( w, j->bodyA, j->bodyB );
+	if ( j->color == P_OVERFLOW )
+	{
+		w->overflowJoints = grow( w->overflowJoints, &w->overflowJointCap, w->overflowJointCount + 1, sizeof( int ) );
+		j->overflowIndex = w->overflowJointCount;
+		w->overflowJoints[w->overflowJointCount++] = jid;
+	}
+}
+
+// constraint_graph.c:290-318 b2RemoveJointFromGraph (swap-remove in the
+// overflow array; colour bits cleared otherwise)
+void p_remove_joint_from_graph( World* w, int jid )
+{
+	Joint* j = w->joints + jid;
+	if ( j->color == P_NULL )
+		return;
+	if ( j->color != P_OVERFLOW )
+	{
+		uint16_t bit = (uint16_t)( 1u << j->color );
+		w->bodies[j->bodyA].colorMask &= (uint16_t)~bit;
+		w->bodies[j->bodyB].colorMask &= (uint16_t)~bit;
+	}
+	else
+	{
+		int idx = j->overflowIndex;
+		int last = w->overflowJointCount - 1;
+		if ( idx != last )
+		{
+			int moved = w->overflowJoints[last];
+			w->overflowJoints[idx] = moved;
+			w->joints[moved].overflowIndex = idx;
+		}
+		w->overflowJointCount -= 1;
+		j->overflowIndex = P_NULL;
+	}
+	j->color = P_NULL;
 }
 
 int orc_joint_color( int wi, int joint )
@@ -704,6 +777,10 @@ static int create_contact_with_id( World* w, int shapeIdA, int shapeIdB, int id 
 	c->simFlags = 0;
 	if ( sa->enablePreSolveEvents || sb->enablePreSolveEvents )
 		c->simFlags |= SIM_PRESOLVE;
+	// contact.c:206-215: awake set when either body is awake, else disabled
+	c->setIndex = ( p_body_awake( w, c->bodyA ) || p_body_awake( w, c->bodyB ) ) ? SET_AWAKE : SET_DISABLED;
+	c->islandId = c->islandPrev = c->islandNext = P_NULL;
+	p_contact_edges_link( w, id );
 	pairset_add( &w->pairs, pair_key( shapeIdA, shapeIdB ) );
 	return id;
 }
@@ -979,22 +1056,61 @@ static void update_pairs( World* w )
 		if ( u == 0 || cands[u - 1].key != cands[i].key )
 			cands[u++] = cands[i];
 	nc = u;
-	// create contacts in native order (ascending pair key) or per plan
+	// create contacts in native order (ascending pair key) or per plan. A
+	// plan's contacts are created in the order the reference's id pool handed
+	// their ids out (LIFO free list, then fresh ids), which is the order the
+	// reference created them in; that order is visible in the bodies'
+	// contact lists and, through island splits, in what sleeps and wakes.
+	int* planId = (int*)malloc( sizeof( int ) * (size_t)( nc > 0 ? nc : 1 ) );
+	long long* rank = (long long*)malloc( sizeof( long long ) * (size_t)( nc > 0 ? nc : 1 ) );
+	int* createOrder = (int*)malloc( sizeof( int ) * (size_t)( nc > 0 ? nc : 1 ) );
 	for ( int i = 0; i < nc; ++i )
 	{
-		int id = -1;
-		if ( w->planCount > 0 )
+		planId[i] = -1;
+		rank[i] = (long long)i;
+		createOrder[i] = i;
+		if ( w->planCount == 0 )
+			continue;
+		for ( int k = 0; k < w->planCount; ++k )
 		{
-			for ( int k = 0; k < w->planCount; ++k )
+			const int* row = w->plan + 3 * k;
+			if ( pair_key( row[1], row[2] ) == cands[i].key )
 			{
-				const int* row = w->plan + 3 * k;
-				if ( pair_key( row[1], row[2] ) == cands[i].key )
-				{
-					id = row[0];
-					break;
-				}
+				planId[i] = row[0];
+				break;
 			}
 		}
+		int id = planId[i];
+		long long r = 4ll * nc + 4ll * w->contactCount + i;
+		for ( int k = w->contactFreeCount - 1; k >= 0 && id >= 0; --k )
+			if ( w->contactFree[k] == id )
+			{
+				r = (long long)( w->contactFreeCount - 1 - k );
+				break;
+			}
+		if ( id >= w->contactCount )
+			r = (long long)w->contactFreeCount + ( id - w->contactCount );
+		rank[i] = r;
+	}
+	if ( w->planCount > 0 )
+	{
+		// insertion sort by rank (a step creates few contacts)
+		for ( int i = 1; i < nc; ++i )
+		{
+			int v = createOrder[i];
+			int j = i - 1;
+			while ( j >= 0 && rank[createOrder[j]] > rank[v] )
+			{
+				createOrder[j + 1] = createOrder[j];
+				j -= 1;
+			}
+			createOrder[j + 1] = v;
+		}
+	}
+	for ( int o = 0; o < nc; ++o )
+	{
+		int i = createOrder[o];
+		int id = planId[i];
 		if ( id >= 0 )
 		{
 			take_contact_id( w, id );
@@ -1005,6 +1121,9 @@ static void update_pairs( World* w )
 		}
 		create_contact_with_id( w, cands[i].a, cands[i].b, id );
 	}
+	free( planId );
+	free( rank );
+	free( createOrder );
 	// reset move buffer
 	for ( int i = 0; i < w->moveCount; ++i )
 		w->shapes[w->moveArray[i]].moved = 0;
@@ -1121,7 +1240,7 @@ static void overflow_remove( World* w, int cid )
 	w->contacts[cid].overflowIndex = P_NULL;
 }
 
-static void add_contact_to_graph( World* w, int cid )
+void p_add_contact_to_graph( World* w, int cid )
 {
 	Contact* c = w->contacts + cid;
 	Body* a = w->bodies + c->bodyA;
@@ -1192,7 +1311,7 @@ static void add_contact_to_graph( World* w, int cid )
 	}
 }
 
-static void remove_contact_from_graph( World* w, int cid )
+void p_remove_contact_from_graph( World* w, int cid )
 {
 	Contact* c = w->contacts + cid;
 	int color = c->color;
@@ -1215,14 +1334,18 @@ static void push_pair( int** arr, int* count, int* cap, int a, int b )
 	*count += 1;
 }
 
+// contact.c:340-440 b2DestroyContact (no wake)
 static void destroy_contact( World* w, int cid )
 {
 	Contact* c = w->contacts + cid;
 	pairset_remove( &w->pairs, pair_key( c->shapeA, c->shapeB ) );
 	if ( c->touchingFlag && c->enableContactEvents )
 		push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
+	p_contact_edges_unlink( w, cid );
+	if ( c->islandId != P_NULL )
+		p_unlink_contact( w, cid );
 	if ( c->color != P_NULL )
-		remove_contact_from_graph( w, cid );
+		p_remove_contact_from_graph( w, cid );
 	c->used = 0;
 	free_contact_id( w, cid );
 }
@@ -1244,9 +1367,12 @@ static void process_state_changes( World* w )
 		{
 			if ( c->enableContactEvents )
 				push_pair( &w->beginEvents, &w->beginCount, &w->beginCap, c->shapeA, c->shapeB );
+			// link first: this wakes a sleeping set the contact touches
 			c->touchingFlag = 1;
+			p_link_contact( w, id );
+			c = w->contacts + id;
 			c->simFlags &= ~SIM_STARTED;
-			add_contact_to_graph( w, id );
+			p_add_contact_to_graph( w, id );
 		}
 		else if ( f & SIM_STOPPED )
 		{
@@ -1254,7 +1380,8 @@ static void process_state_changes( World* w )
 			c->touchingFlag = 0;
 			if ( c->enableContactEvents )
 				push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
-			remove_contact_from_graph( w, id );
+			p_unlink_contact( w, id );
+			p_remove_contact_from_graph( w, id );
 		}
 	}
 }
@@ -1322,7 +1449,7 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	int nc = w->contactCount;
 #pragma omp parallel for schedule( dynamic, 256 )
 	for ( int id = 0; id < nc; ++id )
-		if ( w->contacts[id].used )
+		if ( w->contacts[id].used && w->contacts[id].setIndex == SET_AWAKE )
 			update_contact( w, w->contacts + id );
 	double t2 = p_now();
 	process_state_changes( w );
@@ -1372,7 +1499,7 @@ int orc_get_bodies( int wi, float* out, int cap )
 		o[7] = b->center.x;
 		o[8] = b->center.y;
 		o[9] = 1.0f;
-		o[10] = b->type == BODY_STATIC ? 0.0f : 2.0f;
+		o[10] = (float)b->setIndex;
 		o[11] = b->sleepTime;
 	}
 	return n;
@@ -1520,14 +1647,40 @@ void orc_get_color_counts( int wi, int* out )
 	}
 }
 
+// body.c:1480-1510 b2Body_SetAwake
+void orc_body_set_awake( int wi, int body, int awake )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || body < 0 || body >= w->bodyCount || w->bodies[body].used == 0 )
+		return;
+	Body* b = w->bodies + body;
+	if ( awake && b->setIndex >= SET_FIRST_SLEEPING )
+		p_wake_solver_set( w, b->setIndex );
+	else if ( awake == 0 && b->setIndex == SET_AWAKE )
+	{
+		if ( w->islands[b->islandId].constraintRemoveCount > 0 )
+			p_split_island( w, b->islandId );
+		p_try_sleep_island( w, w->bodies[body].islandId );
+	}
+}
+
+// world.c:1715-1740 b2World_EnableSleeping: disabling wakes every set
+void orc_world_enable_sleeping( int wi, int enabled )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || ( enabled != 0 ) == ( w->enableSleep != 0 ) )
+		return;
+	w->enableSleep = enabled != 0;
+	if ( enabled == 0 )
+		for ( int i = SET_FIRST_SLEEPING; i < w->setCap; ++i )
+			if ( w->sets[i].setIndex != P_NULL && w->sets[i].bodies.count > 0 )
+				p_wake_solver_set( w, i );
+}
+
 int orc_awake_body_count( int wi )
 {
 	World* w = p_world( wi );
-	int n = 0;
-	for ( int i = 0; i < w->bodyCount; ++i )
-		if ( w->bodies[i].used && w->bodies[i].type != BODY_STATIC && w->bodies[i].enabled )
-			n += 1;
-	return n;
+	return w->sets[SET_AWAKE].bodies.count;
 }
 
 void orc_event_counts( int wi, int* out )
@@ -1571,7 +1724,7 @@ int orc_get_move_events( int wi, int* ints, float* floats, int cap )
 	for ( int i = 0; i < n; ++i )
 	{
 		ints[2 * i] = w->moveEventBodies[i];
-		ints[2 * i + 1] = 0;
+		ints[2 * i + 1] = w->moveEventAsleep ? w->moveEventAsleep[i] : 0;
 	}
 	memcpy( floats, w->moveEventXf, sizeof( float ) * 4 * (size_t)n );
 	return n;

@@ -604,6 +604,17 @@ int ref_awake_body_count( int w )
 	return b2World_GetAwakeBodyCount( s_worlds[w] );
 }
 
+// b2Body_SetAwake / b2World_EnableSleeping
+void ref_body_set_awake( int w, int body, int awake )
+{
+	b2Body_SetAwake( ref_body_id( w, body ), awake != 0 );
+}
+
+void ref_world_enable_sleeping( int w, int enabled )
+{
+	b2World_EnableSleeping( s_worlds[w], enabled != 0 );
+}
+
 // Sleep-related: island id per body
 int ref_body_island( int w, int body )
 {

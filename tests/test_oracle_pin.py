@@ -61,6 +61,82 @@ def test_port_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene, kw, f
     port.close()
 
 
+SLEEP_SCENES = [
+    ("pyramid_sleep", dict(enableSleep=1), "pyramid", dict(rows=12), 300),
+    ("pile_sleep", dict(enableSleep=1, enableContinuous=1), "pile",
+     dict(count=300, seed=3, width=20.0, height=30.0), 450),
+    ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
+]
+
+
+def lockstep_full(ref, port, frames, start=1):
+    """Lock step comparing every body row: transform, velocity, centre,
+    solver set (awake, sleeping set id) and sleep time."""
+    prev = set(tuple(r) for r in ref.contacts()[0][:, :3].tolist()) if start > 1 else set()
+    for f in range(start, start + frames):
+        ref.step(1.0 / 60.0, 4)
+        ints, _ = ref.contacts()
+        prev, created = new_contacts(prev, ints)
+        if created:
+            port.set_contact_plan(np.array(created, np.int32))
+        port.step(1.0 / 60.0, 4)
+        rb, pb = ref.bodies(), port.bodies()
+        bad = np.argwhere(rb.view(np.uint32) != pb.view(np.uint32))
+        assert len(bad) == 0, "frame %d: body/field %s ref %r port %r" % (
+            f, bad[0].tolist(), rb[tuple(bad[0])], pb[tuple(bad[0])])
+        assert ref.awake_body_count() == port.awake_body_count(), f
+        if f % 25 == 0:
+            assert compare_contacts(ref, port) == [], f
+            assert np.array_equal(ref.color_counts(), port.color_counts()), f
+    return prev
+
+
+@pytest.mark.parametrize("name,wkw,scene,kw,frames", SLEEP_SCENES, ids=[s[0] for s in SLEEP_SCENES])
+def test_port_sleep_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene, kw, frames):
+    """Islands, sleeping solver sets and the split of the sleepiest island:
+    bodies fall asleep on the same frame with the same set ids."""
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, scene, **kw)
+    scenes.build(port, scene, **kw)
+    lockstep_full(ref, port, frames)
+    if name != "chains_sleep":
+        assert ref.awake_body_count() == 0
+    ref.close()
+    port.close()
+
+
+def test_port_wake_by_contact_and_api(ref_lib, port_lib):
+    """A sleeping pyramid woken by falling bodies created later (its set's
+    contacts and joints re-enter the graph inside the serial contact update),
+    then bodies put to sleep and woken through b2Body_SetAwake, then
+    sleeping disabled world-wide."""
+    wkw = dict(enableSleep=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        scenes.build(w, "pyramid", rows=10)
+        scenes.build(w, "pyramids_chains", pyramids=1, rows=4, chains=3, links=6, gap=30.0)
+    lockstep_full(ref, port, 150)
+    assert ref.awake_body_count() < 30
+    for w in (ref, port):
+        b = w.create_body(scenes.body_def(type=scenes.DYNAMIC, positionX=0.3, positionY=14.0))
+        w.create_circle(b, scenes.shape_def(), 0.0, 0.0, 0.5)
+        b2 = w.create_body(scenes.body_def(type=scenes.DYNAMIC, positionX=-3.2, positionY=16.0))
+        w.create_box(b2, scenes.shape_def(), 0.4, 0.4)
+    lockstep_full(ref, port, 120, start=151)
+    for w in (ref, port):
+        w.set_awake(5, False)
+        w.set_awake(30, True)
+    lockstep_full(ref, port, 40, start=271)
+    for w in (ref, port):
+        w.enable_sleeping(False)
+    assert ref.awake_body_count() == port.awake_body_count()
+    lockstep_full(ref, port, 40, start=311)
+    ref.close()
+    port.close()
+
+
 def hit_rows(w):
     ints, fl = w.hit_events()
     return sorted(tuple(i) + tuple(f) for i, f in zip(ints.tolist(), fl.view(np.uint32).tolist()))
