@@ -601,5 +601,7 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	sort_coop<unsigned long long>( w.pairKeys, nullptr, w.pairKeysAlt, nullptr, &w.sc->newPairCount, bits, w.sortHist,
 								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
 	k_create_contacts<<<grid_for( w.pairCap ), BP_THREADS, 0, st>>>( w, planMode );
+	if ( w.isl )
+		launch_isl_new_contacts( w, st, planMode );
 	k_after_create<<<gridS, BP_THREADS, 0, st>>>( w, planMode );
 }

@@ -22,6 +22,7 @@
 #define BF_SPEED_CAPPED 0x40
 #define BF_IS_FAST 0x80
 #define BF_ENLARGE 0x100
+#define BF_ASLEEP 0x200 // in a sleeping solver set
 #define BF_TYPE_SHIFT 16 // 2 bits: 0 static 1 kinematic 2 dynamic
 
 // shape flags
@@ -51,6 +52,7 @@
 #define CF_STOPPED 0x80000
 #define CF_HIT_EVENT 0x100000
 #define CF_PRESOLVE 0x200000
+#define CF_INACTIVE 0x400000 // not in the awake set (disabled or sleeping): not collided
 
 // error bits in DScalars::error
 #define ERR_CONTACT_CAPACITY 0x1
@@ -119,6 +121,93 @@ struct DScalars
 	int pendingOps;	   // colouring: ops left after the first round
 	int overflowOps;   // colouring: ops that add to / remove from the overflow colour
 	int pad[2];
+};
+
+// ---------------------------------------------------------------------------
+// Islands and solver sets (island.h, solver_set.h), kept on the device in
+// worlds with sleeping enabled and updated by single-thread kernels in the
+// reference's serial order (island.cu). Set ids: 0 static, 1 disabled,
+// 2 awake, 3.. sleeping. A sleeping set's members are kept as append-only
+// lists (its array order); the awake set's bodies and islands as arrays with
+// swap-remove, as the reference keeps them.
+// ---------------------------------------------------------------------------
+#define SET_STATIC 0
+#define SET_DISABLED 1
+#define SET_AWAKE 2
+#define SET_FIRST_SLEEPING 3
+
+struct DIsland
+{
+	int setIndex, localIndex;
+	int headBody, tailBody, bodyCount;
+	int headContact, tailContact, contactCount;
+	int headJoint, tailJoint, jointCount;
+	int parent, removeCount;
+	int setNext; // next island of the same sleeping set
+};
+
+struct DSet
+{
+	int used;
+	int headBody, tailBody, bodyCount;
+	int headContact, tailContact, contactCount;
+	int headJoint, tailJoint, jointCount;
+	int headIsland, tailIsland, islandCount;
+};
+
+struct DIslands
+{
+	int bodyCap, contactCap, jointCap, islandCap, setCap;
+	// bodies
+	int* bSet;
+	int* bLocal; // index in the awake body array
+	int* bIsland;
+	int* bIslandPrev;
+	int* bIslandNext;
+	int* bHeadContact; // contact edge list: (contactId << 1) | edge
+	int* bSetNext;
+	int* bMark;
+	int* bMoveIndex; // this step's move-event slot, -1 when none
+	// contacts
+	int* cSet;
+	int* cIsland;
+	int* cIslandPrev;
+	int* cIslandNext;
+	int* cSetNext;
+	int* cMark;
+	int4* cEdge; // prev0 next0 prev1 next1 (edge 0 on bodyA's list)
+	// joints
+	int* jSet;
+	int* jIsland;
+	int* jIslandPrev;
+	int* jIslandNext;
+	int* jSetNext;
+	int* jMark;
+	int* jOverflowIndex;
+	// islands, sets, pools
+	DIsland* islands;
+	int* islandFree;
+	DSet* sets;
+	int* setFree;
+	int* awakeBodies;
+	int* awakeIslands;
+	unsigned char* islandBits;
+	int* stack;	   // split scratch, bodyCap
+	int* seeds;	   // split scratch, bodyCap
+	int* order;	   // new-contact creation order, contactCap
+	int* moveBody;	   // move events of the step in awake order
+	int* moveAsleep;   // fellAsleep per move event
+	int* log;		   // creation log: (kind << 30) | id, kind 0 body, 1 joint
+	int logCap;
+	int logCount;
+	int bodyKnown; // bodies below this id have set and island records
+	int islandFreeCount, islandNext;
+	int setFreeCount, setNext;
+	int awakeBodyCount, awakeIslandCount;
+	int splitIslandId;
+	int moveCount;
+	int splitCandidate;
+	int error;
 };
 
 // Solver view of one body: velocity and the substep position/rotation
@@ -269,6 +358,7 @@ struct DWorld
 	// per overflow constraint, constraints in level order beyond the
 	// shared-memory list
 	int* npBucket; // narrowphase: contact ids by manifold class, NP_CLASSES x contactCap
+	DIslands* isl;  // islands and solver sets (sleeping worlds only, else null)
 	int* ovfOwner; // bodyCap
 	int* ovfLevel; // contactCap + jointCap
 	int* ovfOrder; // contactCap + jointCap

@@ -12,7 +12,7 @@
 
 __device__ __forceinline__ bool awake_flags( int f )
 {
-	return ( f & ( BF_USED | BF_ENABLED ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
+	return ( f & ( BF_USED | BF_ENABLED | BF_ASLEEP ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
 }
 
 __device__ __forceinline__ fbox shape_aabb( const float4* g, int type, fxf xf )
@@ -473,10 +473,14 @@ __global__ void k_reset_step_counters( DWorld w )
 void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt )
 {
 	(void)s;
+	if ( w.isl )
+		launch_isl_split( w, st );
 	k_finalize<<<grid_for( w.bodyCount ), 256, 0, st>>>( w, dt, 1.0f / dt );
 	k_continuous<<<grid_for( w.bodyCount ), 64, 0, st>>>( w );
 	k_hit_events<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
 	k_moved_flags<<<grid_for( w.shapeCount ), 256, 0, st>>>( w );
+	if ( w.isl )
+		launch_isl_sleep( w, st );
 }
 
 void launch_reset_counters( DWorld& w, cudaStream_t st )

@@ -278,7 +278,7 @@ __device__ __forceinline__ int op_chain( unsigned long long* st, int tile, int a
 // Freed ids, begin/end events, contact flags and the list of overflow ops,
 // all in op order (world.c:586-686). Tiles are claimed in launch order and
 // chained by decoupled look-back.
-__global__ void __launch_bounds__( OPS_TILE ) k_op_outputs( DWorld w, const int* gkind, int* ovOps )
+__global__ void __launch_bounds__( OPS_TILE ) k_op_outputs( DWorld w, const int* gkind, int* ovOps, int serialGraph )
 {
 	__shared__ int smem[32];
 	__shared__ int s_tile, s_prefix[OPS_SCAN_CHAINS];
@@ -310,7 +310,8 @@ __global__ void __launch_bounds__( OPS_TILE ) k_op_outputs( DWorld w, const int*
 		isFree = kind == 0;
 		isBegin = kind == 1 && ( f & CF_EVENTS );
 		isEnd = ( kind == 2 || ( kind == 0 && ( f & CF_TOUCHING ) ) ) && ( f & CF_EVENTS );
-		isOvf = gkind[k] != OP_NONE && w.opColor[k] == F2D_OVERFLOW;
+		// the serial island path maintains the overflow array itself
+		isOvf = !serialGraph && gkind[k] != OP_NONE && w.opColor[k] == F2D_OVERFLOW;
 	}
 	// per-tile counts stay below 2^16: two counters per scanned int
 	int t01, t23;
@@ -571,13 +572,23 @@ void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st )
 	int* ovOps = s.tmpA + cap; // reuses the pending flags once the rounds are done
 	int g = grid_for( w.opCap );
 	k_op_prepare<<<g, 256, 0, st>>>( w, gkind );
+	if ( w.isl )
+	{
+		// sleeping worlds: the state changes run serially with their island
+		// links and the wakes they cause (island.cu)
+		launch_isl_ops( w, st, gkind );
+		cudaMemsetAsync( w.opScan, 0, sizeof( unsigned long long ) * (size_t)OPS_SCAN_WORDS( w.opCap ), st );
+		k_op_outputs<<<( w.opCap + OPS_TILE - 1 ) / OPS_TILE, OPS_TILE, 0, st>>>( w, gkind, ovOps, 1 );
+		k_overflow_ops<<<1, GRAPH_THREADS, 0, st>>>( w, gkind, ovOps );
+		return;
+	}
 	k_op_lock<<<g, 256, 0, st>>>( w );
 	k_op_round<<<g, 256, 0, st>>>( w, gkind, pending );
 	scan_lookback( pending, pos, &w.sc->opCount, 0, w.opCap, &w.sc->pendingOps, s.scanState, &w.sc->error, st );
 	k_op_pending_list<<<g, 256, 0, st>>>( w, pending, pos, list );
 	k_color_rounds<<<1, GRAPH_THREADS, 0, st>>>( w, gkind, list );
 	cudaMemsetAsync( w.opScan, 0, sizeof( unsigned long long ) * (size_t)OPS_SCAN_WORDS( w.opCap ), st );
-	k_op_outputs<<<( w.opCap + OPS_TILE - 1 ) / OPS_TILE, OPS_TILE, 0, st>>>( w, gkind, ovOps );
+	k_op_outputs<<<( w.opCap + OPS_TILE - 1 ) / OPS_TILE, OPS_TILE, 0, st>>>( w, gkind, ovOps, 0 );
 	k_overflow_ops<<<1, GRAPH_THREADS, 0, st>>>( w, gkind, ovOps );
 }
 

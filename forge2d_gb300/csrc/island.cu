@@ -1,0 +1,1173 @@
+// Islands, sleeping solver sets and waking on the device (island.c,
+// solver_set.c; body.c:84-96, 1483-1508; joint.c:196-306; world.c:586-686,
+// 1710-1740; solver.c:543-726, 1194-1220, 1473-1487, 1995-2048).
+//
+// Only worlds with sleeping enabled use this file. The reference keeps its
+// islands with linked lists, union-find roots and swap-remove arrays whose
+// orders decide which contacts re-enter the constraint graph, and in what
+// order, when a set wakes; every function here follows those orders exactly
+// and runs on one device thread (launch <<<1, 1>>>): the bookkeeping is
+// serial by nature and touches few rows per step. The parallel phases of the
+// step read the outcome through two flags: BF_ASLEEP on sleeping bodies (not
+// integrated, not finalized) and CF_INACTIVE on contacts outside the awake
+// set (not collided).
+#include "dworld.cuh"
+#include "kernels.cuh"
+
+#define ISL_NULL ( -1 )
+#define F2D_TIME_TO_SLEEP 0.5f // constants.h:47
+#define ISL_ERR_CAPACITY 1
+
+__device__ __forceinline__ bool isl_static( const DWorld& w, int b )
+{
+	return body_type( w.bflags[b] ) == 0;
+}
+
+// ---------------------------------------------------------------------------
+// constraint graph (constraint_graph.c:68-318), serial form
+// ---------------------------------------------------------------------------
+__device__ int isl_graph_add_contact( const DWorld& w, int c )
+{
+	int2 bd = w.cbody[c];
+	int a = isl_static( w, bd.x ) ? -1 : bd.x, b = isl_static( w, bd.y ) ? -1 : bd.y;
+	int color = F2D_OVERFLOW;
+	if ( a >= 0 && b >= 0 )
+	{
+		unsigned used = w.colorMask[a] | w.colorMask[b];
+		for ( int i = 0; i < F2D_OVERFLOW; ++i )
+			if ( ( used & ( 1u << i ) ) == 0 )
+			{
+				color = i;
+				break;
+			}
+		if ( color != F2D_OVERFLOW )
+		{
+			w.colorMask[a] |= 1u << color;
+			w.colorMask[b] |= 1u << color;
+		}
+	}
+	else
+	{
+		// no static contacts in colour 0
+		int d = a >= 0 ? a : b;
+		for ( int i = 1; i < F2D_OVERFLOW; ++i )
+			if ( ( w.colorMask[d] & ( 1u << i ) ) == 0 )
+			{
+				color = i;
+				break;
+			}
+		if ( color != F2D_OVERFLOW )
+			w.colorMask[d] |= 1u << color;
+	}
+	w.ccolor[c] = color;
+	if ( color == F2D_OVERFLOW )
+	{
+		int idx = w.sc->overflowCount;
+		w.overflowList[idx] = c;
+		w.coverflowIndex[c] = idx;
+		w.sc->overflowCount = idx + 1;
+	}
+	return color;
+}
+
+__device__ void isl_graph_remove_contact( const DWorld& w, int c )
+{
+	int color = w.ccolor[c];
+	if ( color == F2D_NULL )
+		return;
+	int2 bd = w.cbody[c];
+	if ( color != F2D_OVERFLOW )
+	{
+		unsigned bit = 1u << color;
+		if ( !isl_static( w, bd.x ) )
+			w.colorMask[bd.x] &= ~bit;
+		if ( !isl_static( w, bd.y ) )
+			w.colorMask[bd.y] &= ~bit;
+	}
+	else
+	{
+		int idx = w.coverflowIndex[c];
+		int last = w.sc->overflowCount - 1;
+		if ( idx >= 0 && idx <= last )
+		{
+			if ( idx != last )
+			{
+				int moved = w.overflowList[last];
+				w.overflowList[idx] = moved;
+				w.coverflowIndex[moved] = idx;
+			}
+			w.sc->overflowCount = last;
+		}
+		w.coverflowIndex[c] = F2D_NULL;
+	}
+	w.ccolor[c] = F2D_NULL;
+}
+
+// joints may take colour 0 even against a static body (constraint_graph.c:214-267)
+__device__ void isl_graph_add_joint( const DWorld& w, DIslands& I, int j )
+{
+	int2 jb = w.jbody[j];
+	int a = isl_static( w, jb.x ) ? -1 : jb.x, b = isl_static( w, jb.y ) ? -1 : jb.y;
+	int color = F2D_OVERFLOW;
+	if ( a >= 0 && b >= 0 )
+	{
+		unsigned used = w.colorMask[a] | w.colorMask[b];
+		for ( int c = 0; c < F2D_OVERFLOW; ++c )
+			if ( ( used & ( 1u << c ) ) == 0 )
+			{
+				color = c;
+				break;
+			}
+		if ( color != F2D_OVERFLOW )
+		{
+			w.colorMask[a] |= 1u << color;
+			w.colorMask[b] |= 1u << color;
+		}
+	}
+	else if ( a >= 0 || b >= 0 )
+	{
+		int d = a >= 0 ? a : b;
+		for ( int c = 0; c < F2D_OVERFLOW; ++c )
+			if ( ( w.colorMask[d] & ( 1u << c ) ) == 0 )
+			{
+				color = c;
+				break;
+			}
+		if ( color != F2D_OVERFLOW )
+			w.colorMask[d] |= 1u << color;
+	}
+	w.jcolor[j] = color;
+	if ( color == F2D_OVERFLOW )
+	{
+		int idx = w.sc->overflowJointCount;
+		w.overflowJoints[idx] = j;
+		I.jOverflowIndex[j] = idx;
+		w.sc->overflowJointCount = idx + 1;
+	}
+}
+
+__device__ void isl_graph_remove_joint( const DWorld& w, DIslands& I, int j )
+{
+	int color = w.jcolor[j];
+	if ( color == F2D_NULL )
+		return;
+	int2 jb = w.jbody[j];
+	if ( color != F2D_OVERFLOW )
+	{
+		unsigned bit = 1u << color;
+		if ( !isl_static( w, jb.x ) )
+			w.colorMask[jb.x] &= ~bit;
+		if ( !isl_static( w, jb.y ) )
+			w.colorMask[jb.y] &= ~bit;
+	}
+	else
+	{
+		int idx = I.jOverflowIndex[j];
+		int last = w.sc->overflowJointCount - 1;
+		if ( idx >= 0 && idx <= last )
+		{
+			if ( idx != last )
+			{
+				int moved = w.overflowJoints[last];
+				w.overflowJoints[idx] = moved;
+				I.jOverflowIndex[moved] = idx;
+			}
+			w.sc->overflowJointCount = last;
+		}
+		I.jOverflowIndex[j] = F2D_NULL;
+	}
+	w.jcolor[j] = F2D_NULL;
+}
+
+// ---------------------------------------------------------------------------
+// id pools (id_pool.c:19-38) and sets
+// ---------------------------------------------------------------------------
+__device__ int isl_set_create( DIslands& I )
+{
+	int id = I.setFreeCount > 0 ? I.setFree[--I.setFreeCount] : I.setNext++;
+	if ( id >= I.setCap )
+	{
+		I.error |= ISL_ERR_CAPACITY;
+		id = I.setCap - 1;
+	}
+	DSet& s = I.sets[id];
+	s.used = 1;
+	s.headBody = s.tailBody = ISL_NULL;
+	s.headContact = s.tailContact = ISL_NULL;
+	s.headJoint = s.tailJoint = ISL_NULL;
+	s.headIsland = s.tailIsland = ISL_NULL;
+	s.bodyCount = s.contactCount = s.jointCount = s.islandCount = 0;
+	return id;
+}
+
+__device__ void isl_set_destroy( DIslands& I, int id )
+{
+	I.sets[id].used = 0;
+	I.setFree[I.setFreeCount++] = id;
+}
+
+// append to a sleeping set's list (its array order)
+__device__ void isl_set_push_body( DIslands& I, int setId, int b )
+{
+	DSet& s = I.sets[setId];
+	I.bSetNext[b] = ISL_NULL;
+	if ( s.tailBody != ISL_NULL )
+		I.bSetNext[s.tailBody] = b;
+	else
+		s.headBody = b;
+	s.tailBody = b;
+	s.bodyCount += 1;
+	I.bSet[b] = setId;
+}
+
+__device__ void isl_set_push_contact( DIslands& I, int setId, int c )
+{
+	DSet& s = I.sets[setId];
+	I.cSetNext[c] = ISL_NULL;
+	if ( s.tailContact != ISL_NULL )
+		I.cSetNext[s.tailContact] = c;
+	else
+		s.headContact = c;
+	s.tailContact = c;
+	s.contactCount += 1;
+	I.cSet[c] = setId;
+}
+
+__device__ void isl_set_push_joint( DIslands& I, int setId, int j )
+{
+	DSet& s = I.sets[setId];
+	I.jSetNext[j] = ISL_NULL;
+	if ( s.tailJoint != ISL_NULL )
+		I.jSetNext[s.tailJoint] = j;
+	else
+		s.headJoint = j;
+	s.tailJoint = j;
+	s.jointCount += 1;
+	I.jSet[j] = setId;
+}
+
+__device__ void isl_set_push_island( DIslands& I, int setId, int id )
+{
+	DSet& s = I.sets[setId];
+	I.islands[id].setNext = ISL_NULL;
+	if ( s.tailIsland != ISL_NULL )
+		I.islands[s.tailIsland].setNext = id;
+	else
+		s.headIsland = id;
+	s.tailIsland = id;
+	s.islandCount += 1;
+	I.islands[id].setIndex = setId;
+	I.islands[id].localIndex = s.islandCount - 1;
+}
+
+// the awake set's body array (swap-remove)
+__device__ void isl_awake_add_body( const DWorld& w, DIslands& I, int b )
+{
+	int idx = I.awakeBodyCount++;
+	I.awakeBodies[idx] = b;
+	I.bLocal[b] = idx;
+	I.bSet[b] = SET_AWAKE;
+	w.bflags[b] &= ~BF_ASLEEP;
+}
+
+__device__ void isl_awake_remove_body( DIslands& I, int b )
+{
+	int idx = I.bLocal[b];
+	int last = I.awakeBodyCount - 1;
+	if ( idx != last )
+	{
+		int moved = I.awakeBodies[last];
+		I.awakeBodies[idx] = moved;
+		I.bLocal[moved] = idx;
+	}
+	I.awakeBodyCount = last;
+	I.bLocal[b] = ISL_NULL;
+}
+
+// ---------------------------------------------------------------------------
+// islands (island.c)
+// ---------------------------------------------------------------------------
+__device__ int isl_island_create( DIslands& I, int setId )
+{
+	int id = I.islandFreeCount > 0 ? I.islandFree[--I.islandFreeCount] : I.islandNext++;
+	if ( id >= I.islandCap )
+	{
+		I.error |= ISL_ERR_CAPACITY;
+		id = I.islandCap - 1;
+	}
+	DIsland& isl = I.islands[id];
+	isl.headBody = isl.tailBody = ISL_NULL;
+	isl.headContact = isl.tailContact = ISL_NULL;
+	isl.headJoint = isl.tailJoint = ISL_NULL;
+	isl.bodyCount = isl.contactCount = isl.jointCount = 0;
+	isl.parent = ISL_NULL;
+	isl.removeCount = 0;
+	isl.setNext = ISL_NULL;
+	if ( setId == SET_AWAKE )
+	{
+		isl.setIndex = SET_AWAKE;
+		isl.localIndex = I.awakeIslandCount;
+		I.awakeIslands[I.awakeIslandCount++] = id;
+	}
+	else
+		isl_set_push_island( I, setId, id );
+	return id;
+}
+
+// island.c:58-84 (awake islands only are destroyed)
+__device__ void isl_island_destroy( DIslands& I, int id )
+{
+	if ( I.splitIslandId == id )
+		I.splitIslandId = ISL_NULL;
+	DIsland& isl = I.islands[id];
+	int idx = isl.localIndex;
+	int last = I.awakeIslandCount - 1;
+	if ( idx != last )
+	{
+		int moved = I.awakeIslands[last];
+		I.awakeIslands[idx] = moved;
+		I.islands[moved].localIndex = idx;
+	}
+	I.awakeIslandCount = last;
+	isl.setIndex = ISL_NULL;
+	isl.localIndex = ISL_NULL;
+	I.islandFree[I.islandFreeCount++] = id;
+}
+
+__device__ int isl_root( DIslands& I, int id )
+{
+	for ( int guard = 0; I.islands[id].parent != ISL_NULL && guard < I.islandCap; ++guard )
+	{
+		int parentId = I.islands[id].parent;
+		int grand = I.islands[parentId].parent;
+		if ( grand != ISL_NULL )
+			I.islands[id].parent = grand;
+		id = parentId;
+	}
+	return id;
+}
+
+__device__ void isl_add_contact( DIslands& I, int islandId, int c )
+{
+	DIsland& isl = I.islands[islandId];
+	I.cIslandPrev[c] = ISL_NULL;
+	I.cIslandNext[c] = ISL_NULL;
+	if ( isl.headContact != ISL_NULL )
+	{
+		I.cIslandNext[c] = isl.headContact;
+		I.cIslandPrev[isl.headContact] = c;
+	}
+	isl.headContact = c;
+	if ( isl.tailContact == ISL_NULL )
+		isl.tailContact = c;
+	isl.contactCount += 1;
+	I.cIsland[c] = islandId;
+}
+
+__device__ void isl_add_joint( DIslands& I, int islandId, int j )
+{
+	DIsland& isl = I.islands[islandId];
+	I.jIslandPrev[j] = ISL_NULL;
+	I.jIslandNext[j] = ISL_NULL;
+	if ( isl.headJoint != ISL_NULL )
+	{
+		I.jIslandNext[j] = isl.headJoint;
+		I.jIslandPrev[isl.headJoint] = j;
+	}
+	isl.headJoint = j;
+	if ( isl.tailJoint == ISL_NULL )
+		isl.tailJoint = j;
+	isl.jointCount += 1;
+	I.jIsland[j] = islandId;
+}
+
+__device__ void isl_wake_set( const DWorld& w, DIslands& I, int setId );
+
+// island.c:116-218
+__device__ void isl_link_contact( const DWorld& w, DIslands& I, int c )
+{
+	int2 bd = w.cbody[c];
+	if ( I.bSet[bd.x] == SET_AWAKE && I.bSet[bd.y] >= SET_FIRST_SLEEPING )
+		isl_wake_set( w, I, I.bSet[bd.y] );
+	if ( I.bSet[bd.y] == SET_AWAKE && I.bSet[bd.x] >= SET_FIRST_SLEEPING )
+		isl_wake_set( w, I, I.bSet[bd.x] );
+	int idA = I.bIsland[bd.x], idB = I.bIsland[bd.y];
+	if ( idA == idB )
+	{
+		isl_add_contact( I, idA, c );
+		return;
+	}
+	int rootA = idA != ISL_NULL ? isl_root( I, idA ) : ISL_NULL;
+	int rootB = idB != ISL_NULL ? isl_root( I, idB ) : ISL_NULL;
+	if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
+		I.islands[rootB].parent = rootA;
+	isl_add_contact( I, rootA != ISL_NULL ? rootA : rootB, c );
+}
+
+// island.c:221-261
+__device__ void isl_unlink_contact( DIslands& I, int c )
+{
+	int id = I.cIsland[c];
+	if ( id == ISL_NULL )
+		return;
+	DIsland& isl = I.islands[id];
+	int prev = I.cIslandPrev[c], next = I.cIslandNext[c];
+	if ( prev != ISL_NULL )
+		I.cIslandNext[prev] = next;
+	if ( next != ISL_NULL )
+		I.cIslandPrev[next] = prev;
+	if ( isl.headContact == c )
+		isl.headContact = next;
+	if ( isl.tailContact == c )
+		isl.tailContact = prev;
+	isl.contactCount -= 1;
+	isl.removeCount += 1;
+	I.cIsland[c] = I.cIslandPrev[c] = I.cIslandNext[c] = ISL_NULL;
+}
+
+__device__ void isl_merge_awake( DIslands& I );
+
+// island.c:291-382
+__device__ void isl_link_joint( const DWorld& w, DIslands& I, int j, bool merge )
+{
+	int2 jb = w.jbody[j];
+	if ( I.bSet[jb.x] == SET_AWAKE && I.bSet[jb.y] >= SET_FIRST_SLEEPING )
+		isl_wake_set( w, I, I.bSet[jb.y] );
+	else if ( I.bSet[jb.y] == SET_AWAKE && I.bSet[jb.x] >= SET_FIRST_SLEEPING )
+		isl_wake_set( w, I, I.bSet[jb.x] );
+	int idA = I.bIsland[jb.x], idB = I.bIsland[jb.y];
+	if ( idA == idB )
+	{
+		isl_add_joint( I, idA, j );
+		return;
+	}
+	int rootA = idA != ISL_NULL ? isl_root( I, idA ) : ISL_NULL;
+	int rootB = idB != ISL_NULL ? isl_root( I, idB ) : ISL_NULL;
+	if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
+		I.islands[rootB].parent = rootA;
+	isl_add_joint( I, rootA != ISL_NULL ? rootA : rootB, j );
+	if ( merge )
+		isl_merge_awake( I );
+}
+
+// island.c:429-528
+__device__ void isl_merge_one( DIslands& I, int id )
+{
+	DIsland& isl = I.islands[id];
+	int rootId = isl.parent;
+	DIsland& root = I.islands[rootId];
+	for ( int b = isl.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; b = I.bIslandNext[b], ++g )
+		I.bIsland[b] = rootId;
+	for ( int c = isl.headContact, g = 0; c != ISL_NULL && g < I.contactCap; c = I.cIslandNext[c], ++g )
+		I.cIsland[c] = rootId;
+	for ( int j = isl.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; j = I.jIslandNext[j], ++g )
+		I.jIsland[j] = rootId;
+	I.bIslandNext[root.tailBody] = isl.headBody;
+	I.bIslandPrev[isl.headBody] = root.tailBody;
+	root.tailBody = isl.tailBody;
+	root.bodyCount += isl.bodyCount;
+	if ( root.headContact == ISL_NULL )
+	{
+		root.headContact = isl.headContact;
+		root.tailContact = isl.tailContact;
+		root.contactCount = isl.contactCount;
+	}
+	else if ( isl.headContact != ISL_NULL )
+	{
+		I.cIslandNext[root.tailContact] = isl.headContact;
+		I.cIslandPrev[isl.headContact] = root.tailContact;
+		root.tailContact = isl.tailContact;
+		root.contactCount += isl.contactCount;
+	}
+	if ( root.headJoint == ISL_NULL )
+	{
+		root.headJoint = isl.headJoint;
+		root.tailJoint = isl.tailJoint;
+		root.jointCount = isl.jointCount;
+	}
+	else if ( isl.headJoint != ISL_NULL )
+	{
+		I.jIslandNext[root.tailJoint] = isl.headJoint;
+		I.jIslandPrev[isl.headJoint] = root.tailJoint;
+		root.tailJoint = isl.tailJoint;
+		root.jointCount += isl.jointCount;
+	}
+	root.removeCount += isl.removeCount;
+}
+
+// island.c:539-600
+__device__ void isl_merge_awake( DIslands& I )
+{
+	int n = I.awakeIslandCount;
+	for ( int i = 0; i < n; ++i )
+	{
+		int id = I.awakeIslands[i];
+		int root = isl_root( I, id );
+		if ( root != id )
+			I.islands[id].parent = root;
+	}
+	for ( int i = n - 1; i >= 0; --i )
+	{
+		int id = I.awakeIslands[i];
+		if ( I.islands[id].parent == ISL_NULL )
+			continue;
+		isl_merge_one( I, id );
+		isl_island_destroy( I, id );
+	}
+}
+
+// island.c:602-832
+__device__ void isl_split( const DWorld& w, DIslands& I, int baseId )
+{
+	DIsland& base = I.islands[baseId];
+	if ( base.setIndex != SET_AWAKE || base.removeCount == 0 )
+		return;
+	int bodyCount = base.bodyCount;
+	int index = 0;
+	for ( int b = base.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; b = I.bIslandNext[b], ++g )
+	{
+		I.seeds[index++] = b;
+		I.bMark[b] = 0;
+	}
+	for ( int c = base.headContact, g = 0; c != ISL_NULL && g < I.contactCap; c = I.cIslandNext[c], ++g )
+		I.cMark[c] = 0;
+	for ( int j = base.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; j = I.jIslandNext[j], ++g )
+		I.jMark[j] = 0;
+	isl_island_destroy( I, baseId );
+
+	for ( int i = 0; i < bodyCount; ++i )
+	{
+		int seed = I.seeds[i];
+		if ( I.bMark[seed] )
+			continue;
+		int sp = 0;
+		I.stack[sp++] = seed;
+		I.bMark[seed] = 1;
+		int id = isl_island_create( I, SET_AWAKE );
+		while ( sp > 0 )
+		{
+			int b = I.stack[--sp];
+			DIsland& isl = I.islands[id];
+			I.bIsland[b] = id;
+			if ( isl.tailBody != ISL_NULL )
+				I.bIslandNext[isl.tailBody] = b;
+			I.bIslandPrev[b] = isl.tailBody;
+			I.bIslandNext[b] = ISL_NULL;
+			isl.tailBody = b;
+			if ( isl.headBody == ISL_NULL )
+				isl.headBody = b;
+			isl.bodyCount += 1;
+
+			for ( int key = I.bHeadContact[b], g = 0; key != ISL_NULL && g < I.contactCap; ++g )
+			{
+				int c = key >> 1, edge = key & 1;
+				int4 e = I.cEdge[c];
+				key = edge == 0 ? e.y : e.w;
+				if ( I.cMark[c] )
+					continue;
+				if ( ( w.cflags[c] & CF_TOUCHING ) == 0 )
+					continue;
+				I.cMark[c] = 1;
+				int2 bd = w.cbody[c];
+				int other = edge == 0 ? bd.y : bd.x;
+				if ( I.bMark[other] == 0 && I.bSet[other] != SET_STATIC )
+				{
+					if ( sp < I.bodyCap )
+						I.stack[sp++] = other;
+					I.bMark[other] = 1;
+				}
+				I.cIsland[c] = id;
+				if ( isl.tailContact != ISL_NULL )
+					I.cIslandNext[isl.tailContact] = c;
+				I.cIslandPrev[c] = isl.tailContact;
+				I.cIslandNext[c] = ISL_NULL;
+				isl.tailContact = c;
+				if ( isl.headContact == ISL_NULL )
+					isl.headContact = c;
+				isl.contactCount += 1;
+			}
+
+			for ( int key = w.headJoint[b], g = 0; key != F2D_NULL && g < I.jointCap; ++g )
+			{
+				int j = key >> 1, edge = key & 1;
+				key = w.jnext[2 * j + edge];
+				if ( I.jMark[j] )
+					continue;
+				I.jMark[j] = 1;
+				int2 jb = w.jbody[j];
+				int other = edge == 0 ? jb.y : jb.x;
+				if ( I.bSet[other] == SET_DISABLED )
+					continue;
+				if ( I.bMark[other] == 0 && I.bSet[other] == SET_AWAKE )
+				{
+					if ( sp < I.bodyCap )
+						I.stack[sp++] = other;
+					I.bMark[other] = 1;
+				}
+				I.jIsland[j] = id;
+				if ( isl.tailJoint != ISL_NULL )
+					I.jIslandNext[isl.tailJoint] = j;
+				I.jIslandPrev[j] = isl.tailJoint;
+				I.jIslandNext[j] = ISL_NULL;
+				isl.tailJoint = j;
+				if ( isl.headJoint == ISL_NULL )
+					isl.headJoint = j;
+				isl.jointCount += 1;
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// body contact edge lists (contact.c:240-283, 355-410)
+// ---------------------------------------------------------------------------
+__device__ void isl_edges_link( const DWorld& w, DIslands& I, int c )
+{
+	int2 bd = w.cbody[c];
+	int4 e = make_int4( ISL_NULL, ISL_NULL, ISL_NULL, ISL_NULL );
+	for ( int edge = 0; edge < 2; ++edge )
+	{
+		int b = edge == 0 ? bd.x : bd.y;
+		int key = ( c << 1 ) | edge;
+		int head = I.bHeadContact[b];
+		if ( edge == 0 )
+			e.y = head;
+		else
+			e.w = head;
+		if ( head != ISL_NULL )
+		{
+			// the head is another contact's edge (bodies A and B differ)
+			int4 he = I.cEdge[head >> 1];
+			if ( head & 1 )
+				he.z = key;
+			else
+				he.x = key;
+			I.cEdge[head >> 1] = he;
+		}
+		I.bHeadContact[b] = key;
+	}
+	I.cEdge[c] = e;
+}
+
+__device__ void isl_edges_unlink( const DWorld& w, DIslands& I, int c )
+{
+	int2 bd = w.cbody[c];
+	for ( int edge = 0; edge < 2; ++edge )
+	{
+		int4 e = I.cEdge[c];
+		int prev = edge == 0 ? e.x : e.z;
+		int next = edge == 0 ? e.y : e.w;
+		if ( prev != ISL_NULL )
+		{
+			int4 pe = I.cEdge[prev >> 1];
+			if ( prev & 1 )
+				pe.w = next;
+			else
+				pe.y = next;
+			I.cEdge[prev >> 1] = pe;
+		}
+		if ( next != ISL_NULL )
+		{
+			int4 ne = I.cEdge[next >> 1];
+			if ( next & 1 )
+				ne.z = prev;
+			else
+				ne.x = prev;
+			I.cEdge[next >> 1] = ne;
+		}
+		int b = edge == 0 ? bd.x : bd.y;
+		if ( I.bHeadContact[b] == ( ( c << 1 ) | edge ) )
+			I.bHeadContact[b] = next;
+	}
+	I.cEdge[c] = make_int4( ISL_NULL, ISL_NULL, ISL_NULL, ISL_NULL );
+}
+
+// ---------------------------------------------------------------------------
+// sleeping and waking (solver_set.c)
+// ---------------------------------------------------------------------------
+// solver_set.c:36-147
+__device__ void isl_wake_set( const DWorld& w, DIslands& I, int setId )
+{
+	DSet s = I.sets[setId];
+	for ( int b = s.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; ++g )
+	{
+		int next = I.bSetNext[b];
+		isl_awake_add_body( w, I, b );
+		float4 fo = w.force[b];
+		w.force[b] = make_float4( fo.x, fo.y, fo.z, 0.0f ); // sleep time reset
+		w.vel[b] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );	  // b2_identityBodyState
+		w.delta[b] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+		for ( int key = I.bHeadContact[b], k = 0; key != ISL_NULL && k < I.contactCap; ++k )
+		{
+			int c = key >> 1;
+			int4 e = I.cEdge[c];
+			key = ( key & 1 ) ? e.w : e.y;
+			if ( I.cSet[c] != SET_DISABLED )
+				continue;
+			I.cSet[c] = SET_AWAKE;
+			w.cflags[c] &= ~CF_INACTIVE;
+		}
+		b = next;
+	}
+	for ( int c = s.headContact, g = 0; c != ISL_NULL && g < I.contactCap; ++g )
+	{
+		int next = I.cSetNext[c];
+		isl_graph_add_contact( w, c );
+		I.cSet[c] = SET_AWAKE;
+		w.cflags[c] &= ~CF_INACTIVE;
+		c = next;
+	}
+	for ( int j = s.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; ++g )
+	{
+		int next = I.jSetNext[j];
+		isl_graph_add_joint( w, I, j );
+		I.jSet[j] = SET_AWAKE;
+		j = next;
+	}
+	for ( int id = s.headIsland, g = 0; id != ISL_NULL && g < I.islandCap; ++g )
+	{
+		int next = I.islands[id].setNext;
+		DIsland& isl = I.islands[id];
+		isl.setIndex = SET_AWAKE;
+		isl.localIndex = I.awakeIslandCount;
+		isl.setNext = ISL_NULL;
+		I.awakeIslands[I.awakeIslandCount++] = id;
+		id = next;
+	}
+	isl_set_destroy( I, setId );
+}
+
+// solver_set.c:156-414
+__device__ void isl_try_sleep( const DWorld& w, DIslands& I, int islandId )
+{
+	if ( I.islands[islandId].removeCount > 0 )
+		return;
+	int sleepId = isl_set_create( I );
+	DIsland& isl = I.islands[islandId];
+	for ( int b = isl.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; ++g )
+	{
+		if ( I.bMoveIndex[b] != ISL_NULL )
+		{
+			I.moveAsleep[I.bMoveIndex[b]] = 1;
+			I.bMoveIndex[b] = ISL_NULL;
+		}
+		isl_awake_remove_body( I, b );
+		isl_set_push_body( I, sleepId, b );
+		w.bflags[b] |= BF_ASLEEP;
+		w.vel[b] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+		w.delta[b] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+		for ( int key = I.bHeadContact[b], k = 0; key != ISL_NULL && k < I.contactCap; ++k )
+		{
+			int c = key >> 1, edge = key & 1;
+			int4 e = I.cEdge[c];
+			key = edge == 0 ? e.y : e.w;
+			if ( I.cSet[c] == SET_DISABLED )
+				continue;
+			if ( w.ccolor[c] != F2D_NULL )
+				continue;
+			int2 bd = w.cbody[c];
+			int other = edge == 0 ? bd.y : bd.x;
+			if ( I.bSet[other] == SET_AWAKE )
+				continue;
+			I.cSet[c] = SET_DISABLED;
+			w.cflags[c] |= CF_INACTIVE;
+		}
+		b = I.bIslandNext[b];
+	}
+	for ( int c = isl.headContact, g = 0; c != ISL_NULL && g < I.contactCap; ++g )
+	{
+		isl_graph_remove_contact( w, c );
+		isl_set_push_contact( I, sleepId, c );
+		w.cflags[c] |= CF_INACTIVE;
+		c = I.cIslandNext[c];
+	}
+	for ( int j = isl.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; ++g )
+	{
+		isl_graph_remove_joint( w, I, j );
+		isl_set_push_joint( I, sleepId, j );
+		j = I.jIslandNext[j];
+	}
+	int idx = isl.localIndex;
+	int last = I.awakeIslandCount - 1;
+	if ( idx != last )
+	{
+		int moved = I.awakeIslands[last];
+		I.awakeIslands[idx] = moved;
+		I.islands[moved].localIndex = idx;
+	}
+	I.awakeIslandCount = last;
+	isl_set_push_island( I, sleepId, islandId );
+	I.islands[islandId].localIndex = 0;
+}
+
+// solver_set.c:419-517
+__device__ void isl_merge_sets( DIslands& I, int s1, int s2 )
+{
+	if ( I.sets[s1].bodyCount < I.sets[s2].bodyCount )
+	{
+		int t = s1;
+		s1 = s2;
+		s2 = t;
+	}
+	DSet src = I.sets[s2];
+	for ( int b = src.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; ++g )
+	{
+		int next = I.bSetNext[b];
+		isl_set_push_body( I, s1, b );
+		b = next;
+	}
+	for ( int c = src.headContact, g = 0; c != ISL_NULL && g < I.contactCap; ++g )
+	{
+		int next = I.cSetNext[c];
+		isl_set_push_contact( I, s1, c );
+		c = next;
+	}
+	for ( int j = src.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; ++g )
+	{
+		int next = I.jSetNext[j];
+		isl_set_push_joint( I, s1, j );
+		j = next;
+	}
+	for ( int id = src.headIsland, g = 0; id != ISL_NULL && g < I.islandCap; ++g )
+	{
+		int next = I.islands[id].setNext;
+		isl_set_push_island( I, s1, id );
+		id = next;
+	}
+	isl_set_destroy( I, s2 );
+}
+
+// ---------------------------------------------------------------------------
+// kernels (all <<<1, 1>>>)
+// ---------------------------------------------------------------------------
+// Bodies and joints created since the last step, in creation order
+// (body.c:225-330 set and island; joint.c:196-306 set, graph and island).
+__global__ void k_isl_create( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	for ( int i = 0; i < I.logCount; ++i )
+	{
+		int kind = (unsigned)I.log[i] >> 30;
+		int id = I.log[i] & 0x3fffffff;
+		if ( kind == 0 )
+		{
+			if ( id + 1 > I.bodyKnown )
+				I.bodyKnown = id + 1;
+			int f = w.bflags[id];
+			I.bIsland[id] = I.bIslandPrev[id] = I.bIslandNext[id] = ISL_NULL;
+			I.bHeadContact[id] = ISL_NULL;
+			I.bMoveIndex[id] = ISL_NULL;
+			I.bLocal[id] = ISL_NULL;
+			int setId;
+			if ( ( f & BF_ENABLED ) == 0 )
+				setId = SET_DISABLED;
+			else if ( body_type( f ) == 0 )
+				setId = SET_STATIC;
+			else if ( ( f & BF_ASLEEP ) == 0 )
+				setId = SET_AWAKE;
+			else
+				setId = isl_set_create( I );
+			if ( setId == SET_AWAKE )
+				isl_awake_add_body( w, I, id );
+			else if ( setId >= SET_FIRST_SLEEPING )
+				isl_set_push_body( I, setId, id );
+			else
+				I.bSet[id] = setId;
+			if ( setId >= SET_AWAKE )
+			{
+				int isl = isl_island_create( I, setId );
+				I.bIsland[id] = isl;
+				I.islands[isl].headBody = I.islands[isl].tailBody = id;
+				I.islands[isl].bodyCount = 1;
+			}
+		}
+		else
+		{
+			int2 jb = w.jbody[id];
+			I.jIsland[id] = I.jIslandPrev[id] = I.jIslandNext[id] = ISL_NULL;
+			I.jOverflowIndex[id] = ISL_NULL;
+			int sa = I.bSet[jb.x], sb = I.bSet[jb.y];
+			int maxSet = sa > sb ? sa : sb;
+			w.jcolor[id] = F2D_NULL;
+			if ( sa == SET_DISABLED || sb == SET_DISABLED )
+				I.jSet[id] = SET_DISABLED;
+			else if ( sa == SET_STATIC && sb == SET_STATIC )
+				I.jSet[id] = SET_STATIC;
+			else if ( sa == SET_AWAKE || sb == SET_AWAKE )
+			{
+				if ( maxSet >= SET_FIRST_SLEEPING )
+					isl_wake_set( w, I, maxSet );
+				I.jSet[id] = SET_AWAKE;
+				isl_graph_add_joint( w, I, id );
+			}
+			else
+			{
+				isl_set_push_joint( I, maxSet, id );
+				if ( sa != sb && sa >= SET_FIRST_SLEEPING && sb >= SET_FIRST_SLEEPING )
+					isl_merge_sets( I, sa, sb );
+			}
+			if ( I.jSet[id] > SET_DISABLED )
+				isl_link_joint( w, I, id, true );
+		}
+	}
+	I.logCount = 0;
+}
+
+// New contacts of the step in creation order: set and body edge lists
+// (contact.c:206-283). Native order is the new-pair key order; in parity
+// mode, the order the id pool handed the planned ids out.
+__global__ void k_isl_new_contacts( DWorld w, DIslands* Ip, int planMode )
+{
+	DIslands& I = *Ip;
+	int n = w.sc->newPairCount;
+	int F = w.sc->contactFreeCount;
+	int base = w.sc->contactIdCount;
+	int m = 0;
+	for ( int r = 0; r < n; ++r )
+	{
+		int id;
+		if ( planMode )
+			id = r < w.sc->planCount ? w.planIds[r] : -1;
+		else
+			id = r < F ? w.contactFree[F - 1 - r] : base + ( r - F );
+		if ( id < 0 || id >= w.contactCap || ( w.cflags[id] & CF_USED ) == 0 )
+			continue;
+		I.order[m++] = id;
+	}
+	if ( planMode )
+	{
+		// rank = position in the LIFO pop order, then fresh ids ascending
+		for ( int i = 1; i < m; ++i )
+		{
+			int v = I.order[i];
+			long long rv = v >= base ? (long long)F + ( v - base ) : 0;
+			if ( v < base )
+				for ( int k = F - 1; k >= 0; --k )
+					if ( w.contactFree[k] == v )
+					{
+						rv = F - 1 - k;
+						break;
+					}
+			int j = i - 1;
+			while ( j >= 0 )
+			{
+				int u = I.order[j];
+				long long ru = u >= base ? (long long)F + ( u - base ) : 0;
+				if ( u < base )
+					for ( int k = F - 1; k >= 0; --k )
+						if ( w.contactFree[k] == u )
+						{
+							ru = F - 1 - k;
+							break;
+						}
+				if ( ru <= rv )
+					break;
+				I.order[j + 1] = u;
+				j -= 1;
+			}
+			I.order[j + 1] = v;
+		}
+	}
+	for ( int i = 0; i < m; ++i )
+	{
+		int c = I.order[i];
+		int2 bd = w.cbody[c];
+		bool awake = I.bSet[bd.x] == SET_AWAKE || I.bSet[bd.y] == SET_AWAKE;
+		I.cSet[c] = awake ? SET_AWAKE : SET_DISABLED;
+		I.cIsland[c] = I.cIslandPrev[c] = I.cIslandNext[c] = ISL_NULL;
+		I.cMark[c] = 0;
+		if ( !awake )
+			w.cflags[c] |= CF_INACTIVE;
+		isl_edges_link( w, I, c );
+	}
+}
+
+// The step's contact state changes in contact-id order (world.c:586-686)
+// with island links, unlinks and the wakes they cause, then the island
+// merge that opens b2Solve (solver.c:1194-1199).
+__global__ void k_isl_ops( DWorld w, DIslands* Ip, const int* gkind )
+{
+	DIslands& I = *Ip;
+	int nOps = w.sc->opCount;
+	if ( nOps > w.opCap )
+		nOps = w.opCap;
+	for ( int k = 0; k < nOps; ++k )
+	{
+		int c = w.opContact[k];
+		int kind = w.opKind[k];
+		if ( kind == 0 )
+		{
+			// b2DestroyContact: edges, island, graph
+			isl_edges_unlink( w, I, c );
+			isl_unlink_contact( I, c );
+			w.opColor[k] = w.ccolor[c];
+			isl_graph_remove_contact( w, c );
+		}
+		else if ( kind == 1 )
+		{
+			w.cflags[c] |= CF_TOUCHING;
+			isl_link_contact( w, I, c );
+			w.opColor[k] = isl_graph_add_contact( w, c );
+		}
+		else
+		{
+			isl_unlink_contact( I, c );
+			w.opColor[k] = w.ccolor[c];
+			isl_graph_remove_contact( w, c );
+		}
+	}
+	(void)gkind;
+	w.sc->overflowOps = 0;
+	w.sc->colorRounds = 1;
+	isl_merge_awake( I );
+}
+
+// Split of the previous step's candidate, before the bodies are finalized
+// (solver.c:1473-1487, 1700-1706); move-event slots in awake order.
+__global__ void k_isl_split( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	I.moveCount = 0;
+	if ( I.awakeBodyCount == 0 )
+		return;
+	if ( I.splitIslandId != ISL_NULL )
+		isl_split( w, I, I.splitIslandId );
+	I.splitIslandId = ISL_NULL;
+	I.moveCount = I.awakeBodyCount;
+	for ( int i = 0; i < I.awakeBodyCount; ++i )
+	{
+		int b = I.awakeBodies[i];
+		I.bMoveIndex[b] = i;
+		I.moveBody[i] = b;
+		I.moveAsleep[i] = 0;
+	}
+}
+
+// Keep-awake bits and the split candidate in awake order (solver.c:658-675),
+// then islands whose bit stayed clear fall asleep, last first
+// (solver.c:2003-2048).
+__global__ void k_isl_sleep( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.awakeBodyCount == 0 || I.moveCount == 0 )
+		return;
+	for ( int i = 0; i < I.awakeIslandCount; ++i )
+		I.islandBits[i] = 0;
+	int candidate = ISL_NULL;
+	float candidateTime = 0.0f;
+	for ( int i = 0; i < I.awakeBodyCount; ++i )
+	{
+		int b = I.awakeBodies[i];
+		float sleepTime = w.force[b].w;
+		DIsland& isl = I.islands[I.bIsland[b]];
+		if ( sleepTime < F2D_TIME_TO_SLEEP )
+			I.islandBits[isl.localIndex] = 1;
+		else if ( isl.removeCount > 0 && sleepTime > candidateTime )
+		{
+			candidate = I.bIsland[b];
+			candidateTime = sleepTime;
+		}
+	}
+	if ( w.enableSleep == 0 )
+		return;
+	I.splitIslandId = candidate;
+	for ( int i = I.awakeIslandCount - 1; i >= 0; --i )
+	{
+		if ( I.islandBits[i] )
+			continue;
+		isl_try_sleep( w, I, I.awakeIslands[i] );
+	}
+}
+
+// b2Body_SetAwake (body.c:1483-1508), b2Body_EnableSleep(false) and the wake
+// of b2Body_Apply*/SetVelocity (wake = 1), b2World_EnableSleeping(false)
+// (world.c:1710-1740): op 0 wake the body's set, 1 put its island to sleep,
+// 2 wake every sleeping set.
+__global__ void k_isl_api( DWorld w, DIslands* Ip, int op, int body )
+{
+	DIslands& I = *Ip;
+	if ( op == 0 )
+	{
+		if ( I.bSet[body] >= SET_FIRST_SLEEPING )
+			isl_wake_set( w, I, I.bSet[body] );
+	}
+	else if ( op == 1 )
+	{
+		if ( I.bSet[body] == SET_AWAKE )
+		{
+			if ( I.islands[I.bIsland[body]].removeCount > 0 )
+				isl_split( w, I, I.bIsland[body] );
+			isl_try_sleep( w, I, I.bIsland[body] );
+		}
+	}
+	else
+	{
+		for ( int s = SET_FIRST_SLEEPING; s < I.setNext; ++s )
+			if ( I.sets[s].used && I.sets[s].bodyCount > 0 )
+				isl_wake_set( w, I, s );
+	}
+}
+
+// Solver set per body for the state dump (0 static, 1 disabled, 2 awake, 3..).
+__global__ void k_isl_body_sets( DWorld w, DIslands* Ip, int* out, int n )
+{
+	for ( int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x )
+		out[b] = Ip->bSet[b];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+void launch_isl_create( DWorld& w, cudaStream_t st )
+{
+	k_isl_create<<<1, 1, 0, st>>>( w, w.isl );
+}
+
+void launch_isl_new_contacts( DWorld& w, cudaStream_t st, int planMode )
+{
+	k_isl_new_contacts<<<1, 1, 0, st>>>( w, w.isl, planMode );
+}
+
+void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind )
+{
+	k_isl_ops<<<1, 1, 0, st>>>( w, w.isl, gkind );
+}
+
+void launch_isl_split( DWorld& w, cudaStream_t st )
+{
+	k_isl_split<<<1, 1, 0, st>>>( w, w.isl );
+}
+
+void launch_isl_sleep( DWorld& w, cudaStream_t st )
+{
+	k_isl_sleep<<<1, 1, 0, st>>>( w, w.isl );
+}
+
+void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body )
+{
+	k_isl_api<<<1, 1, 0, st>>>( w, w.isl, op, body );
+}
+
+void launch_isl_body_sets( DWorld& w, cudaStream_t st, int* out, int n )
+{
+	k_isl_body_sets<<<grid_for( n ), 256, 0, st>>>( w, w.isl, out, n );
+}
+
+// Re-applies BF_ASLEEP to bodies whose host rows were uploaded (the host
+// mirror does not track sleeping).
+__global__ void k_isl_fix_flags( DWorld w, DIslands* Ip, int n )
+{
+	const DIslands& I = *Ip;
+	int known = n < I.bodyKnown ? n : I.bodyKnown;
+	for ( int b = blockIdx.x * blockDim.x + threadIdx.x; b < known; b += gridDim.x * blockDim.x )
+	{
+		int f = w.bflags[b];
+		int s = I.bSet[b];
+		w.bflags[b] = s >= SET_FIRST_SLEEPING ? ( f | BF_ASLEEP ) : ( f & ~BF_ASLEEP );
+	}
+}
+
+void launch_isl_fix_flags( DWorld& w, cudaStream_t st, int n )
+{
+	k_isl_fix_flags<<<grid_for( n ), 256, 0, st>>>( w, w.isl, n );
+}

@@ -8,7 +8,8 @@ __global__ void k_prepare_joints( DWorld w, float h, float inv_h, Soft jointSoft
 	int n = w.jointCount;
 	for ( int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x )
 	{
-		if ( ( w.jflags[j] & JF_USED ) == 0 )
+		// joints outside the graph (sleeping sets) are not solved
+		if ( ( w.jflags[j] & JF_USED ) == 0 || w.jcolor[j] == F2D_NULL )
 			continue;
 		int2 jb = w.jbody[j];
 		int a = jb.x, b = jb.y;

@@ -52,6 +52,14 @@ void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int su
 void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
 void launch_joint_ops( DWorld& w, cudaStream_t st );
 int solver_max_blocks( int threads );
+// islands and sleeping (island.cu; worlds with sleeping enabled)
+void launch_isl_create( DWorld& w, cudaStream_t st );
+void launch_isl_new_contacts( DWorld& w, cudaStream_t st, int planMode );
+void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind );
+void launch_isl_split( DWorld& w, cudaStream_t st );
+void launch_isl_sleep( DWorld& w, cudaStream_t st );
+void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body );
+void launch_isl_fix_flags( DWorld& w, cudaStream_t st, int n );
 void launch_learned_warm_start( DWorld& w, cudaStream_t st );
 void launch_record_samples( DWorld& w, cudaStream_t st );
 int solver_cluster_capacity();

@@ -65,7 +65,9 @@ __global__ void k_np_classify( DWorld w )
 		if ( c < n )
 		{
 			int flags = w.cflags[c];
-			if ( flags & CF_USED )
+			// contacts outside the awake set are not collided (b2Collide walks
+			// the awake contact array)
+			if ( ( flags & ( CF_USED | CF_INACTIVE ) ) == CF_USED )
 			{
 				int2 sh = w.cshape[c];
 				fbox fa = box_from4( w.fat[sh.x] );

@@ -967,7 +967,7 @@ __device__ __forceinline__ void integrate_velocity( const DWorld& w, int b, cons
 
 __device__ __forceinline__ bool body_awake( int f )
 {
-	return ( f & ( BF_USED | BF_ENABLED ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
+	return ( f & ( BF_USED | BF_ENABLED | BF_ASLEEP ) ) == ( BF_USED | BF_ENABLED ) && body_type( f ) != 0;
 }
 
 template <class BA> __device__ __forceinline__ void lane_op( const BA& ba, Lane& L, int kind, const SolveParams& p )

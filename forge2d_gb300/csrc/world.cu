@@ -94,6 +94,16 @@ struct HostWorld
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
 
+	// islands and solver sets (worlds with sleeping enabled): host copy of the
+	// device record's pointers and capacities, the device record, and the
+	// creation log of bodies and joints since the last upload
+	bool islOn = false;
+	DIslands islHost = {};
+	DIslands* islDev = nullptr;
+	std::vector<int> islLog;
+	int islLogCount = 0;
+	bool islBodiesUploaded = false;
+
 	// the broadphase must re-sort its leaf order at the next step
 	bool forceRebuild = true;
 
@@ -327,6 +337,122 @@ static void grow_joints( HostWorld* W, int cap )
 	d.jointCap = cap;
 }
 
+// Island arrays follow the body, contact and joint capacities; contents are
+// kept across growth (the device record's scalars are read back first).
+static void isl_ensure( HostWorld* W )
+{
+	if ( !W->islOn )
+		return;
+	DWorld& d = W->d;
+	DIslands& h = W->islHost;
+	bool fresh = W->islDev == nullptr;
+	if ( !fresh && h.bodyCap == d.bodyCap && h.contactCap == d.contactCap && h.jointCap == d.jointCap &&
+		 h.logCap >= d.bodyCap + d.jointCap )
+		return;
+	cudaStreamSynchronize( W->stream );
+	if ( fresh )
+	{
+		memset( &h, 0, sizeof( h ) );
+		h.setNext = SET_FIRST_SLEEPING;
+		h.splitIslandId = -1;
+		cudaMalloc( (void**)&W->islDev, sizeof( DIslands ) );
+	}
+	else
+	{
+		DIslands cur;
+		cudaMemcpy( &cur, W->islDev, sizeof( DIslands ), cudaMemcpyDeviceToHost );
+		h = cur;
+	}
+	size_t ob = h.bodyCap, oc = h.contactCap, oj = h.jointCap;
+	size_t nb = d.bodyCap, nc = d.contactCap, nj = d.jointCap;
+	if ( ob != nb )
+	{
+		dgrow( h.bSet, ob, nb );
+		dgrow( h.bLocal, ob, nb );
+		dgrow( h.bIsland, ob, nb );
+		dgrow( h.bIslandPrev, ob, nb );
+		dgrow( h.bIslandNext, ob, nb );
+		dgrow( h.bHeadContact, ob, nb );
+		dgrow( h.bSetNext, ob, nb );
+		dgrow( h.bMark, ob, nb );
+		dgrow( h.bMoveIndex, ob, nb );
+		dgrow( h.islands, ob, nb );
+		dgrow( h.islandFree, ob, nb );
+		dgrow( h.sets, ob + ( ob ? 8 : 0 ), nb + 8 );
+		dgrow( h.setFree, ob + ( ob ? 8 : 0 ), nb + 8 );
+		dgrow( h.awakeBodies, ob, nb );
+		dgrow( h.awakeIslands, ob, nb );
+		dgrow( h.islandBits, 0, nb );
+		dgrow( h.stack, 0, nb );
+		dgrow( h.seeds, 0, nb );
+		dgrow( h.moveBody, ob, nb );
+		dgrow( h.moveAsleep, ob, nb );
+		h.bodyCap = (int)nb;
+		h.islandCap = (int)nb;
+		h.setCap = (int)nb + 8;
+	}
+	if ( oc != nc )
+	{
+		dgrow( h.cSet, oc, nc );
+		dgrow( h.cIsland, oc, nc );
+		dgrow( h.cIslandPrev, oc, nc );
+		dgrow( h.cIslandNext, oc, nc );
+		dgrow( h.cSetNext, oc, nc );
+		dgrow( h.cMark, oc, nc );
+		dgrow( h.cEdge, oc, nc );
+		dgrow( h.order, 0, nc );
+		h.contactCap = (int)nc;
+	}
+	if ( oj != nj )
+	{
+		dgrow( h.jSet, oj, nj );
+		dgrow( h.jIsland, oj, nj );
+		dgrow( h.jIslandPrev, oj, nj );
+		dgrow( h.jIslandNext, oj, nj );
+		dgrow( h.jSetNext, oj, nj );
+		dgrow( h.jMark, oj, nj );
+		dgrow( h.jOverflowIndex, oj, nj );
+		h.jointCap = (int)nj;
+	}
+	if ( h.logCap < d.bodyCap + d.jointCap )
+	{
+		dfree( h.log );
+		dgrow( h.log, 0, (size_t)d.bodyCap + d.jointCap );
+		h.logCap = d.bodyCap + d.jointCap;
+	}
+	cudaMemcpy( W->islDev, &h, sizeof( DIslands ), cudaMemcpyHostToDevice );
+	d.isl = W->islDev;
+	W->graphDirty = true;
+}
+
+static void isl_free( HostWorld* W )
+{
+	DIslands& h = W->islHost;
+	if ( W->islDev )
+	{
+		int* pi[] = { h.bSet, h.bLocal, h.bIsland, h.bIslandPrev, h.bIslandNext, h.bHeadContact, h.bSetNext, h.bMark,
+					  h.bMoveIndex, h.islandFree, h.setFree, h.awakeBodies, h.awakeIslands, h.stack, h.seeds,
+					  h.moveBody, h.moveAsleep, h.cSet, h.cIsland, h.cIslandPrev, h.cIslandNext, h.cSetNext,
+					  h.cMark, h.order, h.jSet, h.jIsland, h.jIslandPrev, h.jIslandNext, h.jSetNext, h.jMark,
+					  h.jOverflowIndex, h.log };
+		for ( int* p : pi )
+			if ( p )
+				cudaFree( p );
+		if ( h.islands )
+			cudaFree( h.islands );
+		if ( h.sets )
+			cudaFree( h.sets );
+		if ( h.cEdge )
+			cudaFree( h.cEdge );
+		if ( h.islandBits )
+			cudaFree( h.islandBits );
+		cudaFree( W->islDev );
+	}
+	W->islDev = nullptr;
+	W->d.isl = nullptr;
+	memset( &h, 0, sizeof( h ) );
+}
+
 static void ensure_capacity( HostWorld* W )
 {
 	bool changed = false;
@@ -360,6 +486,7 @@ static void ensure_capacity( HostWorld* W )
 		alloc_scratch( W );
 		W->graphDirty = true;
 	}
+	isl_ensure( W );
 }
 
 // ---------------------------------------------------------------------------
@@ -533,11 +660,13 @@ static void flush_uploads( HostWorld* W )
 	{
 		upload_body_rows( W, W->bodyUploaded, W->bodyCount );
 		W->bodyUploaded = W->bodyCount;
+		W->islBodiesUploaded = true;
 	}
 	for ( int b : W->bodyDirty )
 	{
 		upload_body_rows( W, b, b + 1 );
 		W->bodyIsDirty[b] = 0;
+		W->islBodiesUploaded = true;
 	}
 	W->bodyDirty.clear();
 	if ( W->shapeUploaded < W->shapeCount )
@@ -564,6 +693,23 @@ static void flush_uploads( HostWorld* W )
 		W->d.staticCount = (int)W->staticShapes.size();
 		W->staticDirty = false;
 		W->graphDirty = true;
+	}
+	if ( W->islOn && W->d.isl )
+	{
+		if ( W->islBodiesUploaded )
+			launch_isl_fix_flags( W->d, W->stream, W->bodyCount );
+		W->islBodiesUploaded = false;
+		if ( !W->islLog.empty() )
+		{
+			int n = (int)W->islLog.size();
+			cudaMemcpyAsync( W->islHost.log, W->islLog.data(), sizeof( int ) * n, cudaMemcpyHostToDevice, W->stream );
+			W->islLogCount = n;
+			cudaMemcpyAsync( &W->islDev->logCount, &W->islLogCount, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+			cudaStreamSynchronize( W->stream );
+			launch_isl_create( W->d, W->stream );
+			W->islLog.clear();
+			W->graphDirty = true;
+		}
 	}
 	if ( !W->pendingJoints.empty() )
 	{
@@ -633,6 +779,9 @@ extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
 	grow_shapes( W, 1024 );
 	grow_joints( W, 256 );
 	alloc_scratch( W );
+	// islands and solver sets are kept in worlds created with sleeping on
+	W->islOn = def->enableSleep != 0;
+	isl_ensure( W );
 	return ( slot + 1 ) | ( (int)W->generation << 16 );
 }
 
@@ -641,6 +790,7 @@ static void free_world( HostWorld* W )
 	cudaStreamSynchronize( W->stream );
 	if ( W->graphExec )
 		cudaGraphExecDestroy( W->graphExec );
+	isl_free( W );
 	DWorld& d = W->d;
 	void** ptrs = (void**)&d;
 	(void)ptrs;
@@ -710,6 +860,7 @@ extern "C" F2D_API void f2d_world_reserve( int32_t worldId, int32_t bodies, int3
 	if ( joints > W->d.jointCap )
 		grow_joints( W, joints );
 	alloc_scratch( W );
+	isl_ensure( W );
 	W->graphDirty = true;
 }
 
@@ -776,6 +927,13 @@ extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def*
 		flags |= BF_FIXED_ROT;
 	if ( def->enableSleep )
 		flags |= BF_ENABLE_SLEEP;
+	if ( W->islOn )
+	{
+		// a body created asleep starts its own sleeping set (body.c:225-260)
+		if ( !def->isAwake && type != 0 && def->isEnabled )
+			flags |= BF_ASLEEP;
+		W->islLog.push_back( id );
+	}
 	vset( W->bflags, id, flags );
 	vset( W->headShape, id, F2D_NULL );
 	vset( W->headJoint, id, F2D_NULL );
@@ -1150,7 +1308,9 @@ extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d
 					   (float)def->motorSpeed ) );
 	// joints between two static bodies never enter the graph
 	bool staticA = body_type( W->bflags[a] ) == 0, staticB = body_type( W->bflags[b] ) == 0;
-	if ( !( staticA && staticB ) )
+	if ( W->islOn )
+		W->islLog.push_back( ( 1 << 30 ) | j ); // set, colour and island at the next upload
+	else if ( !( staticA && staticB ) )
 		W->pendingJoints.push_back( j );
 	if ( index1 )
 		*index1 = j + 1;
@@ -1562,8 +1722,16 @@ extern "C" F2D_API void f2d_world_enable_sleeping( int32_t worldId, int32_t enab
 	HostWorld* W = world_from_id( worldId );
 	if ( W == nullptr )
 		return;
+	if ( ( enabled != 0 ) == ( W->d.enableSleep != 0 ) )
+		return;
 	W->d.enableSleep = enabled != 0;
 	W->graphDirty = true;
+	// world.c:1726-1738: disabling wakes every sleeping set
+	if ( !enabled && W->islOn && W->d.isl )
+	{
+		flush_uploads( W );
+		launch_isl_api( W->d, W->stream, 2, 0 );
+	}
 }
 
 extern "C" F2D_API int32_t f2d_world_is_sleeping_enabled( int32_t worldId )
@@ -1667,11 +1835,35 @@ extern "C" F2D_API void f2d_body_get_linear_velocity( int32_t index1, int32_t wg
 	*y = W->vel[b].y;
 }
 
+// Sleeping worlds: the wake of an edit (body.c b2WakeBody) runs on the device
+// before the row is read back; an edit of a body that stays asleep is
+// dropped, as the reference finds no body state for it. Returns whether the
+// edit applies.
+static int isl_set_of( HostWorld* W, int b )
+{
+	int s = SET_AWAKE;
+	cudaStreamSynchronize( W->stream );
+	cudaMemcpy( &s, W->islHost.bSet + b, sizeof( int ), cudaMemcpyDeviceToHost );
+	return s;
+}
+
+static bool isl_edit( HostWorld* W, int b, bool wake )
+{
+	if ( !W->islOn )
+		return true;
+	flush_uploads( W );
+	if ( wake )
+		launch_isl_api( W->d, W->stream, 0, b );
+	return isl_set_of( W, b ) == SET_AWAKE;
+}
+
 extern "C" F2D_API void f2d_body_set_linear_velocity( int32_t index1, int32_t wg, double x, double y )
 {
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) == 0 )
+		return;
+	if ( !isl_edit( W, b, (float)x * (float)x + (float)y * (float)y > 0.0f ) )
 		return;
 	pull_body( W, b );
 	W->vel[b].x = (float)x;
@@ -1695,6 +1887,8 @@ extern "C" F2D_API void f2d_body_set_angular_velocity( int32_t index1, int32_t w
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) == 0 )
 		return;
+	if ( !isl_edit( W, b, (float)w != 0.0f ) )
+		return;
 	pull_body( W, b );
 	W->vel[b].z = (float)w;
 	mark_body( W, b );
@@ -1704,10 +1898,11 @@ extern "C" F2D_API void f2d_body_set_angular_velocity( int32_t index1, int32_t w
 extern "C" F2D_API void f2d_body_apply_force( int32_t index1, int32_t wg, double fx, double fy, double px, double py,
 											  int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	fv2 f = mk( (float)fx, (float)fy );
@@ -1722,10 +1917,11 @@ extern "C" F2D_API void f2d_body_apply_force( int32_t index1, int32_t wg, double
 
 extern "C" F2D_API void f2d_body_apply_force_to_center( int32_t index1, int32_t wg, double fx, double fy, int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	W->force[b].x += (float)fx;
@@ -1735,10 +1931,11 @@ extern "C" F2D_API void f2d_body_apply_force_to_center( int32_t index1, int32_t 
 
 extern "C" F2D_API void f2d_body_apply_torque( int32_t index1, int32_t wg, double torque, int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	W->force[b].z += (float)torque;
@@ -1748,10 +1945,11 @@ extern "C" F2D_API void f2d_body_apply_torque( int32_t index1, int32_t wg, doubl
 extern "C" F2D_API void f2d_body_apply_linear_impulse( int32_t index1, int32_t wg, double ix, double iy, double px,
 													   double py, int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	fv2 impulse = mk( (float)ix, (float)iy );
@@ -1767,10 +1965,11 @@ extern "C" F2D_API void f2d_body_apply_linear_impulse( int32_t index1, int32_t w
 extern "C" F2D_API void f2d_body_apply_linear_impulse_to_center( int32_t index1, int32_t wg, double ix, double iy,
 																 int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	float4 v = W->vel[b];
@@ -1782,10 +1981,11 @@ extern "C" F2D_API void f2d_body_apply_linear_impulse_to_center( int32_t index1,
 
 extern "C" F2D_API void f2d_body_apply_angular_impulse( int32_t index1, int32_t wg, double impulse, int32_t wake )
 {
-	(void)wake;
 	HostWorld* W;
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 || body_type( W->bflags[b] ) != 2 )
+		return;
+	if ( !isl_edit( W, b, wake != 0 ) )
 		return;
 	pull_body( W, b );
 	W->vel[b].z += W->massv[b].y * (float)impulse;
@@ -1819,7 +2019,70 @@ extern "C" F2D_API int32_t f2d_body_is_awake( int32_t index1, int32_t wg )
 	int b = body_from( index1, wg, &W );
 	if ( b < 0 )
 		return 0;
+	if ( W->islOn )
+	{
+		flush_uploads( W );
+		return isl_set_of( W, b ) == SET_AWAKE;
+	}
 	return body_type( W->bflags[b] ) != 0 && ( W->bflags[b] & BF_ENABLED );
+}
+
+// RawBox2D.bodySetAwake (raw_box2d.dart:232 -> b2Body_SetAwake, body.c:1483-1508)
+extern "C" F2D_API void f2d_body_set_awake( int32_t index1, int32_t wg, int32_t awake )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || !W->islOn )
+		return;
+	flush_uploads( W );
+	launch_isl_api( W->d, W->stream, awake ? 0 : 1, b );
+}
+
+// RawBox2D.bodyIsSleepEnabled / bodyEnableSleep (raw_box2d.dart:235-242;
+// b2Body_EnableSleep wakes the body when sleep is disabled)
+extern "C" F2D_API int32_t f2d_body_is_sleep_enabled( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	return b < 0 ? 0 : ( W->bflags[b] & BF_ENABLE_SLEEP ) != 0;
+}
+
+extern "C" F2D_API void f2d_body_enable_sleep( int32_t index1, int32_t wg, int32_t enabled )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	if ( !enabled && W->islOn )
+	{
+		flush_uploads( W );
+		launch_isl_api( W->d, W->stream, 0, b );
+	}
+	pull_body( W, b );
+	if ( enabled )
+		W->bflags[b] |= BF_ENABLE_SLEEP;
+	else
+		W->bflags[b] &= ~BF_ENABLE_SLEEP;
+	mark_body( W, b );
+}
+
+// RawBox2D.bodyGetSleepThreshold / bodySetSleepThreshold (raw_box2d.dart:245-248)
+extern "C" F2D_API double f2d_body_get_sleep_threshold( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	return b < 0 ? 0.0 : W->damp[b].w;
+}
+
+extern "C" F2D_API void f2d_body_set_sleep_threshold( int32_t index1, int32_t wg, double value )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	W->damp[b].w = (float)value;
+	mark_body( W, b );
 }
 
 // ---------------------------------------------------------------------------
@@ -1856,7 +2119,7 @@ __global__ void k_pack_bodies( DWorld w, float* out, int n )
 		o[7] = c.x;
 		o[8] = c.y;
 		o[9] = 1.0f;
-		o[10] = body_type( f ) == 0 ? 0.0f : 2.0f;
+		o[10] = w.isl ? (float)w.isl->bSet[i] : ( body_type( f ) == 0 ? 0.0f : 2.0f );
 		o[11] = fo.w;
 	}
 }
@@ -2087,12 +2350,15 @@ extern "C" F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* co
 	counts4[1] = sc.endCount;
 	counts4[2] = std::min( sc.hitCount, W->d.eventCap );
 	int moved = 0;
-	for ( int b = 0; b < W->bodyCount; ++b )
-	{
-		int f = W->bflags[b];
-		if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
-			moved += 1;
-	}
+	if ( W->islOn && W->islDev )
+		cudaMemcpy( &moved, &W->islDev->moveCount, sizeof( int ), cudaMemcpyDeviceToHost );
+	else
+		for ( int b = 0; b < W->bodyCount; ++b )
+		{
+			int f = W->bflags[b];
+			if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
+				moved += 1;
+		}
 	counts4[3] = moved;
 }
 
@@ -2156,6 +2422,31 @@ extern "C" F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* 
 	std::vector<float4> ev( n );
 	if ( n > 0 )
 		cudaMemcpy( ev.data(), W->d.moveEvXf, sizeof( float4 ) * n, cudaMemcpyDeviceToHost );
+	if ( W->islOn && W->islDev )
+	{
+		// awake-set order with the fellAsleep flags (solver.c:603-611, solver_set.c:202-212)
+		int count = 0;
+		cudaMemcpy( &count, &W->islDev->moveCount, sizeof( int ), cudaMemcpyDeviceToHost );
+		count = std::min( count, (int)cap );
+		std::vector<int> mb( std::max( count, 1 ) ), ma( std::max( count, 1 ) );
+		if ( count > 0 )
+		{
+			cudaMemcpy( mb.data(), W->islHost.moveBody, sizeof( int ) * count, cudaMemcpyDeviceToHost );
+			cudaMemcpy( ma.data(), W->islHost.moveAsleep, sizeof( int ) * count, cudaMemcpyDeviceToHost );
+		}
+		for ( int i = 0; i < count; ++i )
+		{
+			int b = mb[i];
+			ints3[3 * i + 0] = b + 1;
+			ints3[3 * i + 1] = pack_wg( W, W->bgen[b] );
+			ints3[3 * i + 2] = ma[i];
+			floats4[4 * i + 0] = ev[b].x;
+			floats4[4 * i + 1] = ev[b].y;
+			floats4[4 * i + 2] = ev[b].z;
+			floats4[4 * i + 3] = ev[b].w;
+		}
+		return count;
+	}
 	int m = 0;
 	for ( int b = 0; b < n && m < cap; ++b )
 	{
@@ -2215,12 +2506,15 @@ extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )
 	DScalars sc;
 	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
 	int awake = 0;
-	for ( int b = 0; b < W->bodyCount; ++b )
-	{
-		int f = W->bflags[b];
-		if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
-			awake += 1;
-	}
+	if ( W->islOn && W->islDev )
+		cudaMemcpy( &awake, &W->islDev->awakeBodyCount, sizeof( int ), cudaMemcpyDeviceToHost );
+	else
+		for ( int b = 0; b < W->bodyCount; ++b )
+		{
+			int f = W->bflags[b];
+			if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
+				awake += 1;
+		}
 	int active = 0;
 	for ( int c = 0; c < 11; ++c )
 		active += sc.colorCount[c] > 0 ? 1 : 0;

@@ -108,6 +108,11 @@ _SIGS = [
     ("f2d_body_get_rotational_inertia", _d, [_i, _i]),
     ("f2d_body_get_type", _i, [_i, _i]),
     ("f2d_body_is_awake", _i, [_i, _i]),
+    ("f2d_body_set_awake", None, [_i, _i, _i]),
+    ("f2d_body_is_sleep_enabled", _i, [_i, _i]),
+    ("f2d_body_enable_sleep", None, [_i, _i, _i]),
+    ("f2d_body_get_sleep_threshold", _d, [_i, _i]),
+    ("f2d_body_set_sleep_threshold", None, [_i, _i, _d]),
     ("f2d_create_circle_shape", _i, [_i, _i, _P(ShapeDef), _d, _d, _d, _P(_i), _P(_i)]),
     ("f2d_create_capsule_shape", _i, [_i, _i, _P(ShapeDef), _d, _d, _d, _d, _d, _P(_i), _P(_i)]),
     ("f2d_create_segment_shape", _i, [_i, _i, _P(ShapeDef), _d, _d, _d, _d, _P(_i), _P(_i)]),

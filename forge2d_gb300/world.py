@@ -46,6 +46,7 @@ class GpuWorld:
         wd = dict(WORLD_DEFAULTS)
         if world_def:
             wd.update(world_def)
+        self._body_ids = []
         self.id = self.lib.f2d_create_world(C.byref(_fill(native.WorldDef(), wd)))
         if self.id == 0:
             raise RuntimeError("f2d_create_world failed (no CUDA device?)")
@@ -72,7 +73,27 @@ class GpuWorld:
         i1, wg = C.c_int32(0), C.c_int32(0)
         if not self.lib.f2d_create_body(self.id, C.byref(_fill(native.BodyDef(), bd)), C.byref(i1), C.byref(wg)):
             raise RuntimeError("createBody failed")
+        self._body_ids.append((i1.value, wg.value))
         return (i1.value, wg.value)
+
+    def _body(self, body):
+        return self._body_ids[body] if isinstance(body, int) else body
+
+    # sleeping ---------------------------------------------------------
+    def set_awake(self, body, awake):
+        """b2Body_SetAwake; ``body`` is a creation handle or a body index."""
+        b = self._body(body)
+        self.lib.f2d_body_set_awake(b[0], b[1], int(awake))
+
+    def is_awake(self, body):
+        b = self._body(body)
+        return bool(self.lib.f2d_body_is_awake(b[0], b[1]))
+
+    def enable_sleeping(self, enabled):
+        self.lib.f2d_world_enable_sleeping(self.id, int(enabled))
+
+    def awake_body_count(self):
+        return self.counters()["awake_bodies"]
 
     def _sd(self, sd):
         d = dict(SHAPE_DEFAULTS)
@@ -430,6 +451,28 @@ class Body:
 
     def apply_angular_impulse(self, impulse, wake=True):
         self.lib.f2d_body_apply_angular_impulse(self.id[0], self.id[1], impulse, int(wake))
+
+    @property
+    def is_awake(self):
+        return bool(self.lib.f2d_body_is_awake(*self.id))
+
+    def set_awake(self, awake):
+        self.lib.f2d_body_set_awake(self.id[0], self.id[1], int(awake))
+
+    @property
+    def sleep_threshold(self):
+        return self.lib.f2d_body_get_sleep_threshold(*self.id)
+
+    @sleep_threshold.setter
+    def sleep_threshold(self, value):
+        self.lib.f2d_body_set_sleep_threshold(self.id[0], self.id[1], value)
+
+    @property
+    def is_sleep_enabled(self):
+        return bool(self.lib.f2d_body_is_sleep_enabled(*self.id))
+
+    def enable_sleep(self, enabled):
+        self.lib.f2d_body_enable_sleep(self.id[0], self.id[1], int(enabled))
 
     @property
     def mass(self):

@@ -188,8 +188,9 @@ F2D_API double f2d_body_get_angular_velocity( int32_t index1, int32_t worldAndGe
 F2D_API void f2d_body_set_angular_velocity( int32_t index1, int32_t worldAndGeneration, double w );
 /* RawBox2D.bodyApplyForce / bodyApplyForceToCenter / bodyApplyTorque /
  * bodyApplyLinearImpulse / bodyApplyLinearImpulseToCenter /
- * bodyApplyAngularImpulse (raw_box2d.dart:136-190). wake is accepted and,
- * with sleeping handled per world, has no further effect. */
+ * bodyApplyAngularImpulse (raw_box2d.dart:136-190). wake = 1 wakes a
+ * sleeping body first; the push is dropped on a body that stays asleep, as
+ * in body.c:1000-1110. */
 F2D_API void f2d_body_apply_force( int32_t index1, int32_t worldAndGeneration, double fx, double fy, double px,
 								   double py, int32_t wake );
 F2D_API void f2d_body_apply_force_to_center( int32_t index1, int32_t worldAndGeneration, double fx, double fy,
@@ -206,6 +207,18 @@ F2D_API double f2d_body_get_mass( int32_t index1, int32_t worldAndGeneration );
 F2D_API double f2d_body_get_rotational_inertia( int32_t index1, int32_t worldAndGeneration );
 F2D_API int32_t f2d_body_get_type( int32_t index1, int32_t worldAndGeneration );
 F2D_API int32_t f2d_body_is_awake( int32_t index1, int32_t worldAndGeneration );
+/* RawBox2D.bodySetAwake (raw_box2d.dart:232 -> b2Body_SetAwake): wakes the
+ * body's sleeping set, or puts its island to sleep (splitting it first when
+ * constraints were removed). Worlds created with sleeping off keep every body
+ * awake and ignore it. */
+F2D_API void f2d_body_set_awake( int32_t index1, int32_t worldAndGeneration, int32_t awake );
+/* RawBox2D.bodyIsSleepEnabled / bodyEnableSleep (raw_box2d.dart:235-242 ->
+ * b2Body_IsSleepEnabled / b2Body_EnableSleep; disabling wakes the body). */
+F2D_API int32_t f2d_body_is_sleep_enabled( int32_t index1, int32_t worldAndGeneration );
+F2D_API void f2d_body_enable_sleep( int32_t index1, int32_t worldAndGeneration, int32_t enabled );
+/* RawBox2D.bodyGetSleepThreshold / bodySetSleepThreshold (raw_box2d.dart:245-248). */
+F2D_API double f2d_body_get_sleep_threshold( int32_t index1, int32_t worldAndGeneration );
+F2D_API void f2d_body_set_sleep_threshold( int32_t index1, int32_t worldAndGeneration, double value );
 
 /* ---- shapes ------------------------------------------------------------- */
 

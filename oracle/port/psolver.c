@@ -681,6 +681,8 @@ void p_solve( World* w, float dt, int subStepCount )
 	float jointHertz = fminp( 60.0f, 0.25f * inv_h );
 	Softness jointSoftness = p_make_soft( jointHertz, 2.0f, h );
 
+	// world.c:709: the step's move events start empty
+	w->moveEventCount = 0;
 	// solver.c:1194-1220: merge islands linked this step; nothing to solve
 	// without awake bodies
 	p_merge_awake_islands( w );

@@ -31,6 +31,11 @@ def test_box_drop_comes_to_rest(gpu_lib):
     gx, gy = GOLD["drop"]["position"]
     assert abs(x - gx) < 1e-4 and abs(y - gy) < 1e-3
     assert box.mass == pytest.approx(1.0)
+    # the reference's box is asleep by then (sleeping on by default)
+    assert w._w.awake_body_count() == GOLD["drop"]["awake_bodies"] == 0
+    assert not box.is_awake
+    box.set_awake(True)
+    assert box.is_awake
     w.destroy()
 
 
