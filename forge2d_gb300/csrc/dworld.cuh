@@ -195,6 +195,11 @@ struct DIslands
 	int* stack;	   // split scratch, bodyCap
 	int* seeds;	   // split scratch, bodyCap
 	int* order;	   // new-contact creation order, contactCap
+	int* flag;		   // per awake island: scan input (bodyCap)
+	int* pos;		   // scan output (bodyCap)
+	int* list;		   // compacted island ids (bodyCap)
+	int listCount;
+	unsigned long long candKey; // split candidate: sleep-time bits << 32 | ~awake index
 	int* moveBody;	   // move events of the step in awake order
 	int* moveAsleep;   // fellAsleep per move event
 	int* log;		   // creation log: (kind << 30) | id, kind 0 body, 1 joint
@@ -359,6 +364,8 @@ struct DWorld
 	// shared-memory list
 	int* npBucket; // narrowphase: contact ids by manifold class, NP_CLASSES x contactCap
 	DIslands* isl;  // islands and solver sets (sleeping worlds only, else null)
+	int* islFlag;	// device copies of isl->flag and isl->pos (scan arguments)
+	int* islPos;
 	int* ovfOwner; // bodyCap
 	int* ovfLevel; // contactCap + jointCap
 	int* ovfOrder; // contactCap + jointCap

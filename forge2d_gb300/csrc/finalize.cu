@@ -480,7 +480,7 @@ void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt )
 	k_hit_events<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
 	k_moved_flags<<<grid_for( w.shapeCount ), 256, 0, st>>>( w );
 	if ( w.isl )
-		launch_isl_sleep( w, st );
+		launch_isl_sleep( w, st, s.scanState );
 }
 
 void launch_reset_counters( DWorld& w, cudaStream_t st )

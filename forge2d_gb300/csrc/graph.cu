@@ -576,7 +576,7 @@ void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st )
 	{
 		// sleeping worlds: the state changes run serially with their island
 		// links and the wakes they cause (island.cu)
-		launch_isl_ops( w, st, gkind );
+		launch_isl_ops( w, st, gkind, s.scanState );
 		cudaMemsetAsync( w.opScan, 0, sizeof( unsigned long long ) * (size_t)OPS_SCAN_WORDS( w.opCap ), st );
 		k_op_outputs<<<( w.opCap + OPS_TILE - 1 ) / OPS_TILE, OPS_TILE, 0, st>>>( w, gkind, ovOps, 1 );
 		k_overflow_ops<<<1, GRAPH_THREADS, 0, st>>>( w, gkind, ovOps );

@@ -11,8 +11,11 @@
 // step read the outcome through two flags: BF_ASLEEP on sleeping bodies (not
 // integrated, not finalized) and CF_INACTIVE on contacts outside the awake
 // set (not collided).
+#include "dsort.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
+
+#include <cstddef>
 
 #define ISL_NULL ( -1 )
 #define F2D_TIME_TO_SLEEP 0.5f // constants.h:47
@@ -1019,7 +1022,47 @@ __global__ void k_isl_ops( DWorld w, DIslands* Ip, const int* gkind )
 	(void)gkind;
 	w.sc->overflowOps = 0;
 	w.sc->colorRounds = 1;
-	isl_merge_awake( I );
+}
+
+// Island merge at the start of b2Solve (island.c:539-600) in three parts:
+// every awake island points at its root (parallel; roots never change), the
+// islands that have a parent are listed in array order (scan), and one
+// thread merges them into their roots from the last to the first, as the
+// reference's reverse loop does.
+__global__ void k_isl_merge_roots( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.awakeIslandCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		int id = I.awakeIslands[i];
+		int root = id;
+		for ( int g = 0; I.islands[root].parent != ISL_NULL && g < I.islandCap; ++g )
+			root = I.islands[root].parent;
+		I.flag[i] = root != id ? 1 : 0;
+		if ( root != id )
+			I.islands[id].parent = root;
+	}
+}
+
+__global__ void k_isl_list( DIslands* Ip, const int* count )
+{
+	DIslands& I = *Ip;
+	int n = *count;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+		if ( I.flag[i] )
+			I.list[I.pos[i]] = I.awakeIslands[i];
+}
+
+__global__ void k_isl_merge_apply( DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	for ( int k = I.listCount - 1; k >= 0; --k )
+	{
+		int id = I.list[k];
+		isl_merge_one( I, id );
+		isl_island_destroy( I, id );
+	}
 }
 
 // Split of the previous step's candidate, before the bodies are finalized
@@ -1027,20 +1070,63 @@ __global__ void k_isl_ops( DWorld w, DIslands* Ip, const int* gkind )
 __global__ void k_isl_split( DWorld w, DIslands* Ip )
 {
 	DIslands& I = *Ip;
-	I.moveCount = 0;
 	if ( I.awakeBodyCount == 0 )
 		return;
 	if ( I.splitIslandId != ISL_NULL )
 		isl_split( w, I, I.splitIslandId );
 	I.splitIslandId = ISL_NULL;
-	I.moveCount = I.awakeBodyCount;
-	for ( int i = 0; i < I.awakeBodyCount; ++i )
+}
+
+// Move-event slots in awake order, cleared keep-awake bits and candidate.
+__global__ void k_isl_move_slots( DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.awakeBodyCount;
+	if ( blockIdx.x == 0 && threadIdx.x == 0 )
+	{
+		I.moveCount = n;
+		I.candKey = 0ull;
+	}
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
 	{
 		int b = I.awakeBodies[i];
 		I.bMoveIndex[b] = i;
 		I.moveBody[i] = b;
 		I.moveAsleep[i] = 0;
 	}
+	int ni = I.awakeIslandCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x )
+		I.islandBits[i] = 0;
+}
+
+// Keep-awake bits and the split candidate (solver.c:658-675): the first body
+// in awake order with the largest sleep time wins, as one task context scans.
+__global__ void k_isl_bits( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.moveCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	{
+		int b = I.awakeBodies[i];
+		float sleepTime = w.force[b].w;
+		const DIsland& isl = I.islands[I.bIsland[b]];
+		if ( sleepTime < F2D_TIME_TO_SLEEP )
+			I.islandBits[isl.localIndex] = 1;
+		else if ( isl.removeCount > 0 && sleepTime > 0.0f )
+		{
+			unsigned long long key =
+				( (unsigned long long)__float_as_uint( sleepTime ) << 32 ) | (unsigned)( 0xffffffffu - (unsigned)i );
+			atomicMax( &I.candKey, key );
+		}
+	}
+}
+
+__global__ void k_isl_sleep_flags( DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.awakeIslandCount;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+		I.flag[i] = I.islandBits[i] ? 0 : 1;
 }
 
 // Keep-awake bits and the split candidate in awake order (solver.c:658-675),
@@ -1049,34 +1135,18 @@ __global__ void k_isl_split( DWorld w, DIslands* Ip )
 __global__ void k_isl_sleep( DWorld w, DIslands* Ip )
 {
 	DIslands& I = *Ip;
-	if ( I.awakeBodyCount == 0 || I.moveCount == 0 )
+	if ( I.moveCount == 0 || w.enableSleep == 0 )
 		return;
-	for ( int i = 0; i < I.awakeIslandCount; ++i )
-		I.islandBits[i] = 0;
 	int candidate = ISL_NULL;
-	float candidateTime = 0.0f;
-	for ( int i = 0; i < I.awakeBodyCount; ++i )
+	if ( I.candKey != 0ull )
 	{
-		int b = I.awakeBodies[i];
-		float sleepTime = w.force[b].w;
-		DIsland& isl = I.islands[I.bIsland[b]];
-		if ( sleepTime < F2D_TIME_TO_SLEEP )
-			I.islandBits[isl.localIndex] = 1;
-		else if ( isl.removeCount > 0 && sleepTime > candidateTime )
-		{
-			candidate = I.bIsland[b];
-			candidateTime = sleepTime;
-		}
+		int i = (int)( 0xffffffffu - (unsigned)( I.candKey & 0xffffffffull ) );
+		candidate = I.bIsland[I.awakeBodies[i]];
 	}
-	if ( w.enableSleep == 0 )
-		return;
 	I.splitIslandId = candidate;
-	for ( int i = I.awakeIslandCount - 1; i >= 0; --i )
-	{
-		if ( I.islandBits[i] )
-			continue;
-		isl_try_sleep( w, I, I.awakeIslands[i] );
-	}
+	// islands whose bit stayed clear, listed in array order: last first
+	for ( int k = I.listCount - 1; k >= 0; --k )
+		isl_try_sleep( w, I, I.list[k] );
 }
 
 // b2Body_SetAwake (body.c:1483-1508), b2Body_EnableSleep(false) and the wake
@@ -1128,18 +1198,38 @@ void launch_isl_new_contacts( DWorld& w, cudaStream_t st, int planMode )
 	k_isl_new_contacts<<<1, 1, 0, st>>>( w, w.isl, planMode );
 }
 
-void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind )
+static int* isl_field( DIslands* I, size_t offset )
+{
+	return (int*)( (char*)I + offset );
+}
+
+static void isl_list( DWorld& w, unsigned long long* scanState, cudaStream_t st )
+{
+	int* count = isl_field( w.isl, offsetof( DIslands, awakeIslandCount ) );
+	int* total = isl_field( w.isl, offsetof( DIslands, listCount ) );
+	scan_lookback( w.islFlag, w.islPos, count, 0, w.bodyCap, total, scanState, &w.sc->error, st );
+	k_isl_list<<<grid_for( w.bodyCap ), 256, 0, st>>>( w.isl, count );
+}
+
+void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long long* scanState )
 {
 	k_isl_ops<<<1, 1, 0, st>>>( w, w.isl, gkind );
+	k_isl_merge_roots<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, w.isl );
+	isl_list( w, scanState, st );
+	k_isl_merge_apply<<<1, 1, 0, st>>>( w.isl );
 }
 
 void launch_isl_split( DWorld& w, cudaStream_t st )
 {
 	k_isl_split<<<1, 1, 0, st>>>( w, w.isl );
+	k_isl_move_slots<<<grid_for( w.bodyCap ), 256, 0, st>>>( w.isl );
 }
 
-void launch_isl_sleep( DWorld& w, cudaStream_t st )
+void launch_isl_sleep( DWorld& w, cudaStream_t st, unsigned long long* scanState )
 {
+	k_isl_bits<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, w.isl );
+	k_isl_sleep_flags<<<grid_for( w.bodyCap ), 256, 0, st>>>( w.isl );
+	isl_list( w, scanState, st );
 	k_isl_sleep<<<1, 1, 0, st>>>( w, w.isl );
 }
 

@@ -385,6 +385,9 @@ static void isl_ensure( HostWorld* W )
 		dgrow( h.islandBits, 0, nb );
 		dgrow( h.stack, 0, nb );
 		dgrow( h.seeds, 0, nb );
+		dgrow( h.flag, 0, nb );
+		dgrow( h.pos, 0, nb );
+		dgrow( h.list, 0, nb );
 		dgrow( h.moveBody, ob, nb );
 		dgrow( h.moveAsleep, ob, nb );
 		h.bodyCap = (int)nb;
@@ -422,6 +425,8 @@ static void isl_ensure( HostWorld* W )
 	}
 	cudaMemcpy( W->islDev, &h, sizeof( DIslands ), cudaMemcpyHostToDevice );
 	d.isl = W->islDev;
+	d.islFlag = h.flag;
+	d.islPos = h.pos;
 	W->graphDirty = true;
 }
 
@@ -432,7 +437,7 @@ static void isl_free( HostWorld* W )
 	{
 		int* pi[] = { h.bSet, h.bLocal, h.bIsland, h.bIslandPrev, h.bIslandNext, h.bHeadContact, h.bSetNext, h.bMark,
 					  h.bMoveIndex, h.islandFree, h.setFree, h.awakeBodies, h.awakeIslands, h.stack, h.seeds,
-					  h.moveBody, h.moveAsleep, h.cSet, h.cIsland, h.cIslandPrev, h.cIslandNext, h.cSetNext,
+					  h.moveBody, h.moveAsleep, h.flag, h.pos, h.list, h.cSet, h.cIsland, h.cIslandPrev, h.cIslandNext, h.cSetNext,
 					  h.cMark, h.order, h.jSet, h.jIsland, h.jIslandPrev, h.jIslandNext, h.jSetNext, h.jMark,
 					  h.jOverflowIndex, h.log };
 		for ( int* p : pi )
@@ -450,6 +455,7 @@ static void isl_free( HostWorld* W )
 	}
 	W->islDev = nullptr;
 	W->d.isl = nullptr;
+	W->d.islFlag = W->d.islPos = nullptr;
 	memset( &h, 0, sizeof( h ) );
 }
 
@@ -2310,6 +2316,26 @@ extern "C" F2D_API int32_t f2d_world_get_mass( int32_t worldId, float* out, int3
 	return n;
 }
 
+// Contacts per graph colour as they stand now (the counts of the solver's
+// stage set-up predate the islands that fell asleep at the end of the step).
+__global__ void k_color_census( DWorld w, int* out12 )
+{
+	__shared__ int cnt[12];
+	if ( threadIdx.x < 12 )
+		cnt[threadIdx.x] = 0;
+	__syncthreads();
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int col = w.ccolor[c];
+		if ( col >= 0 && col < 12 && ( w.cflags[c] & CF_USED ) )
+			atomicAdd( cnt + col, 1 );
+	}
+	__syncthreads();
+	if ( threadIdx.x < 12 && cnt[threadIdx.x] > 0 )
+		atomicAdd( out12 + threadIdx.x, cnt[threadIdx.x] );
+}
+
 extern "C" F2D_API void f2d_world_get_color_counts( int32_t worldId, int32_t* out12 )
 {
 	HostWorld* W = world_from_id( worldId );
@@ -2317,12 +2343,12 @@ extern "C" F2D_API void f2d_world_get_color_counts( int32_t worldId, int32_t* ou
 		out12[i] = 0;
 	if ( W == nullptr )
 		return;
+	flush_uploads( W );
+	int* dOut = W->s.tmpA;
+	cudaMemsetAsync( dOut, 0, sizeof( int ) * 12, W->stream );
+	k_color_census<<<grid_for( W->d.contactCap ), 256, 0, W->stream>>>( W->d, dOut );
+	cudaMemcpyAsync( out12, dOut, sizeof( int ) * 12, cudaMemcpyDeviceToHost, W->stream );
 	cudaStreamSynchronize( W->stream );
-	DScalars sc;
-	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
-	for ( int i = 0; i < 11; ++i )
-		out12[i] = sc.colorCount[i];
-	out12[11] = sc.overflowCount;
 	if ( W->jointCount > 0 )
 	{
 		std::vector<int> jc( W->jointCount );

@@ -33,6 +33,12 @@ CASES = {
                    frames=256, checkpoints=[1, 64, 256]),
     "joints": dict(world=dict(enableSleep=0), scene=("joint_gallery", dict()), frames=256,
                    checkpoints=[1, 64, 256]),
+    # sleeping on: islands, sleeping solver sets, island splits
+    "pyramid_sleep": dict(world=dict(enableSleep=1), scene=("pyramid", dict(rows=12)), frames=120,
+                          checkpoints=[1, 30, 44, 60, 120]),
+    "pile_sleep": dict(world=dict(enableSleep=1, enableContinuous=1),
+                       scene=("pile", dict(count=300, seed=3, width=20.0, height=30.0)), frames=360,
+                       checkpoints=[1, 100, 250, 300, 360]),
 }
 
 
@@ -51,7 +57,11 @@ def record(name, spec):
             plan_rows.append((f,) + row)
         prev = cur
         if f in spec["checkpoints"]:
-            out["bodies_%d" % f] = w.bodies()[:, :9].copy()
+            b = w.bodies()
+            out["bodies_%d" % f] = b[:, :9].copy()
+            # solver set (0 static, 2 awake, 3.. sleeping set id) and sleep time
+            out["sets_%d" % f] = b[:, 10].copy()
+            out["sleep_%d" % f] = b[:, 11].copy()
             out["colors_%d" % f] = w.color_counts().copy()
             if f == spec["checkpoints"][0]:
                 out["contact_ints_%d" % f] = ints.copy()

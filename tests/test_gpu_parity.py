@@ -17,7 +17,7 @@ import pytest
 from forge2d_gb300 import scenes
 
 from parity import compare_contacts
-from test_oracle_golden import CASES, GOLD, STATS_CASES, frame_stats, replay
+from test_oracle_golden import CASES, GOLD, STATS_CASES, check_sets, frame_stats, replay
 
 pytestmark = pytest.mark.gpu
 
@@ -134,10 +134,12 @@ def test_gpu_replays_reference_fixture_bit_exact(gpu_lib, name):
     def on_frame(f):
         if f not in checks:
             return
-        b = g.bodies()[:, :9]
+        full = g.bodies()
+        b = full[:, :9]
         ref = gold["bodies_%d" % f]
         bad = np.argwhere(b.view(np.uint32) != ref.view(np.uint32))
         assert len(bad) == 0, "frame %d: first differing (body, field) %s" % (f, bad[0].tolist())
+        check_sets(full, gold, f)
         assert np.array_equal(g.color_counts(), gold["colors_%d" % f]), f
         if f == first:
             ints, fl = g.contacts()

@@ -24,6 +24,8 @@ CASES = {
     "pile": (dict(enableSleep=0, enableContinuous=1), "pile", dict(count=300, seed=11, width=30.0, height=40.0)),
     "chains": (dict(enableSleep=0), "pyramids_chains", dict(pyramids=2, rows=10, chains=6, links=20)),
     "joints": (dict(enableSleep=0), "joint_gallery", dict()),
+    "pyramid_sleep": (dict(enableSleep=1), "pyramid", dict(rows=12)),
+    "pile_sleep": (dict(enableSleep=1, enableContinuous=1), "pile", dict(count=300, seed=3, width=20.0, height=30.0)),
 }
 STATS_CASES = ("pyramid", "pile")
 
@@ -65,6 +67,16 @@ def replay(world, name, frames=None, on_frame=None):
     return gold
 
 
+def check_sets(full_rows, gold, f):
+    """Solver set of every body (static, awake, sleeping set id) and its
+    sleep time, where the fixture holds them."""
+    if "sets_%d" % f not in gold.files:
+        return
+    assert np.array_equal(full_rows[:, 10], gold["sets_%d" % f]), "frame %d solver sets" % f
+    assert np.array_equal(full_rows[:, 11].view(np.uint32), gold["sleep_%d" % f].view(np.uint32)), \
+        "frame %d sleep times" % f
+
+
 def make_port(port_lib, name):
     wkw, scene, kw = CASES[name]
     w = port_lib.PortWorld(scenes.world_def(**wkw))
@@ -83,11 +95,13 @@ def test_port_replays_reference_bit_exact(port_lib, name):
     def on_frame(f):
         if f not in checks:
             return
-        b = w.bodies()[:, :9]
+        full = w.bodies()
+        b = full[:, :9]
         ref = gold["bodies_%d" % f]
         assert b.shape == ref.shape
         bad = np.argwhere(b.view(np.uint32) != ref.view(np.uint32))
         assert len(bad) == 0, "frame %d: first differing (body, field) %s" % (f, bad[0].tolist())
+        check_sets(full, gold, f)
         assert np.array_equal(w.color_counts(), gold["colors_%d" % f]), "frame %d colours" % f
         if f == first:
             ints, fl = w.contacts()
