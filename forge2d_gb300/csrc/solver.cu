@@ -1057,6 +1057,63 @@ __device__ __forceinline__ void colour_lanes_extra( const DWorld& w, const BA& b
 	}
 }
 
+// Tail colours: the highest active colours, without joints, holding at most
+// TAIL_MAX constraints together. Block 0 runs them one after another with
+// block barriers in between; the grid then needs one barrier for all of
+// them instead of one per colour. A constraint's colour and its colour's
+// place in the order are unchanged, so results are too.
+#define TAIL_MAX 1024
+
+__device__ __forceinline__ int tail_first_colour( const int* sCount, const int* sJStart, unsigned activeMask )
+{
+	int first = F2D_OVERFLOW, colours = 0, total = 0;
+	for ( int c = F2D_OVERFLOW - 1; c >= 0; --c )
+	{
+		if ( ( activeMask & ( 1u << c ) ) == 0 )
+			continue;
+		if ( sJStart[c + 1] > sJStart[c] || total + sCount[c] > TAIL_MAX )
+			break;
+		total += sCount[c];
+		first = c;
+		colours += 1;
+	}
+	return colours >= 2 ? first : F2D_OVERFLOW;
+}
+
+template <class BA>
+__device__ void tail_stage( const DWorld& w, const BA& ba, const int* sStart, const int* sCount, int first,
+							unsigned activeMask, int kind, const SolveParams& p )
+{
+	for ( int c = first; c < F2D_OVERFLOW; ++c )
+	{
+		if ( ( activeMask & ( 1u << c ) ) == 0 )
+			continue;
+		for ( int k = sStart[c] + threadIdx.x; k < sStart[c] + sCount[c]; k += blockDim.x )
+		{
+			Lane L;
+			if ( kind == 0 )
+			{
+				L.idx = w.kIndex[k];
+				L.ms = w.kMass[k];
+				L.nm = w.kNormal[k];
+				L.misc = __ldcg( w.kMisc + k );
+				L.imp = __ldcg( w.kImp + k );
+				L.an[0] = w.kAnch1[k];
+				L.an[1] = w.kAnch2[k];
+				lane_warm( ba, L );
+				continue;
+			}
+			lane_load( w, k, L );
+			lane_op( ba, L, kind, p );
+			if ( kind == 3 )
+				__stcg( w.kImp + k, L.imp );
+			else
+				lane_store( w, k, L );
+		}
+		__syncthreads();
+	}
+}
+
 // The persistent solver. Graph-colour constraint slots (after the overflow
 // slots) are dealt to threads round-robin over the blocks: thread t of block
 // b owns colour slot r = t * gridDim.x + b (and r + gridDim.x * blockDim.x,
@@ -1097,10 +1154,14 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 	if ( serialStage && blockIdx.x == 0 )
 		plan = ovf_schedule( w, novf + novfJ <= OVF_SMEM_ITEMS ? sOrder : w.ovfOrder, sLevelStart );
 
+	// tail colours run in block 0; their constraints stay in global memory
+	const int tailFirst = tail_first_colour( sCount, sJStart, activeMask );
+	const int tailSlot = tailFirst < F2D_OVERFLOW ? sStart[tailFirst] : novf + nColour;
+
 	const int r0 = threadIdx.x * gridDim.x + blockIdx.x;
 	Lane L0;
 	int col0 = -1;
-	if ( r0 < nColour )
+	if ( r0 < nColour && novf + r0 < tailSlot )
 	{
 		int k0 = novf + r0;
 		lane_load( w, k0, L0 );
@@ -1144,7 +1205,7 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
-			for ( int c = 0; c < F2D_OVERFLOW; ++c )
+			for ( int c = 0; c < tailFirst; ++c )
 			{
 				if ( ( activeMask & ( 1u << c ) ) == 0 )
 					continue;
@@ -1152,6 +1213,13 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 				if ( col0 == c )
 					lane_op( gb, L0, kind, p );
 				colour_lanes_extra( w, gb, c, sStart, sCount, novf, gtid, gstride, kind, p );
+				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
+					return;
+			}
+			if ( tailFirst < F2D_OVERFLOW )
+			{
+				if ( blockIdx.x == 0 )
+					tail_stage( w, gb, sStart, sCount, tailFirst, activeMask, kind, p );
 				if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 					return;
 			}
@@ -1165,13 +1233,20 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
-	for ( int c = 0; c < F2D_OVERFLOW; ++c )
+	for ( int c = 0; c < tailFirst; ++c )
 	{
 		if ( sCount[c] == 0 )
 			continue;
 		if ( col0 == c )
 			lane_op( gb, L0, 3, p );
 		colour_lanes_extra( w, gb, c, sStart, sCount, novf, gtid, gstride, 3, p );
+		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
+			return;
+	}
+	if ( tailFirst < F2D_OVERFLOW )
+	{
+		if ( blockIdx.x == 0 )
+			tail_stage( w, gb, sStart, sCount, tailFirst, activeMask, 3, p );
 		if ( !grid_barrier( &w.sc->barrierCount, &w.sc->error, epoch ) )
 			return;
 	}
@@ -1182,6 +1257,9 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 		store_manifold( w, novf + r0, L0.imp, L0.tot, L0.misc.w, L0.pt[0].w, L0.pt[1].w,
 						__float_as_int( L0.sf.w ), true );
 	for ( int k = novf + gstride + gtid; k < novf + nColour; k += gstride )
+		store_manifold_global( w, k, true );
+	// tail constraints below the extras' range had no register lane
+	for ( int k = tailSlot + gtid; k < min( novf + gstride, novf + nColour ); k += gstride )
 		store_manifold_global( w, k, true );
 }
 
