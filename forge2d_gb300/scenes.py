@@ -58,6 +58,21 @@ REVOLUTE_DEFAULTS = dict(
 )
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+JOINT_WELD, JOINT_DISTANCE = 2, 3
+
+JOINT_DEFAULTS = dict(
+    type=JOINT_WELD, bodyA=0, bodyB=0, collideConnected=0,
+    localAnchorAX=0.0, localAnchorAY=0.0, localAnchorBX=0.0, localAnchorBY=0.0,
+    referenceAngle=0.0, linearHertz=0.0, linearDampingRatio=0.0, angularHertz=0.0, angularDampingRatio=0.0,
+    length=1.0, minLength=0.0, maxLength=100000.0, hertz=0.0, dampingRatio=0.0,
+    maxMotorForce=0.0, motorSpeed=0.0, enableSpring=0, enableLimit=0, enableMotor=0,
+)
+
+
+def joint_def(**kw):
+    d = dict(JOINT_DEFAULTS)
+    d.update(kw)
+    return d
 
 
 def world_def(**kw):
@@ -298,6 +313,49 @@ def overflow_heap(b, platforms=6, per=24, long_count=160, spokes=16):
                                        enableSpring=1, hertz=4.0, dampingRatio=0.5))
 
 
+def joint_zoo(b, copies=3):
+    """Weld and distance joints side by side, ``copies`` times over a ground
+    box: a cantilever of six boxes welded end to end (stiff on even copies,
+    soft linear/angular springs on odd ones), a rigid distance pendulum, a
+    box hanging on a damped distance spring between length limits, and two
+    boxes pushed apart by a distance motor."""
+    g = b.create_body(body_def(type=STATIC, positionY=-1.0))
+    b.create_box(g, shape_def(), 30.0 * copies, 1.0)
+    for k in range(copies):
+        x0 = -30.0 * copies + 10.0 + 30.0 * k
+        soft = k % 2 == 1
+        wall = b.create_body(body_def(type=STATIC, positionX=x0, positionY=6.0))
+        b.create_box(wall, shape_def(), 0.25, 1.0)
+        prev, prev_x = wall, x0
+        for i in range(6):
+            x = x0 + 0.75 + 1.0 * i
+            seg = b.create_body(body_def(type=DYNAMIC, positionX=x, positionY=6.0))
+            b.create_box(seg, shape_def(), 0.5, 0.125)
+            b.create_joint(joint_def(type=JOINT_WELD, bodyA=prev, bodyB=seg,
+                                     localAnchorAX=0.25 if i == 0 else 0.5, localAnchorBX=-0.5,
+                                     linearHertz=5.0 if soft else 0.0, linearDampingRatio=0.7,
+                                     angularHertz=3.0 if soft else 0.0, angularDampingRatio=0.5,
+                                     referenceAngle=0.05 * k))
+            prev, prev_x = seg, x
+        anchor = b.create_body(body_def(type=STATIC, positionX=x0 + 10.0, positionY=8.0))
+        bob = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 13.0, positionY=8.0))
+        b.create_circle(bob, shape_def(), 0.0, 0.0, 0.4)
+        b.create_joint(joint_def(type=JOINT_DISTANCE, bodyA=anchor, bodyB=bob, length=3.0))
+        hook = b.create_body(body_def(type=STATIC, positionX=x0 + 17.0, positionY=9.0))
+        weight = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 17.5, positionY=6.5))
+        b.create_box(weight, shape_def(), 0.4, 0.4)
+        b.create_joint(joint_def(type=JOINT_DISTANCE, bodyA=hook, bodyB=weight, length=2.0, minLength=1.0,
+                                 maxLength=3.5, enableSpring=1, hertz=2.0 + k, dampingRatio=0.3,
+                                 enableLimit=1, localAnchorBY=0.3))
+        p1 = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 22.0, positionY=1.0))
+        b.create_box(p1, shape_def(), 0.5, 0.5)
+        p2 = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 24.0, positionY=1.0))
+        b.create_box(p2, shape_def(), 0.5, 0.5)
+        b.create_joint(joint_def(type=JOINT_DISTANCE, bodyA=p1, bodyB=p2, length=2.0, enableSpring=1,
+                                 hertz=0.0, enableMotor=1, maxMotorForce=20.0, motorSpeed=1.0 + k,
+                                 enableLimit=1, minLength=1.5, maxLength=4.0))
+
+
 def batched(b, worlds=4096, seed=7, tile=220.0, columns=64, only=None):
     """The batched scene: ``worlds`` independent sub-worlds of uneven size,
     each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
@@ -380,4 +438,6 @@ def build(b, name, **kw):
         return batched(b, **kw)
     if name == "overflow_heap":
         return overflow_heap(b, **kw)
+    if name == "joint_zoo":
+        return joint_zoo(b, **kw)
     raise ValueError(name)

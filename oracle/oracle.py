@@ -85,6 +85,22 @@ class RevoluteDef(C.Structure):
     ]
 
 
+class JointDef(C.Structure):
+    """f2d_joint_def: weld (type 2) and distance (type 3) joints."""
+    _fields_ = [
+        ("type", C.c_int32), ("bodyA", C.c_int32), ("bodyB", C.c_int32), ("collideConnected", C.c_int32),
+        ("localAnchorAX", C.c_double), ("localAnchorAY", C.c_double),
+        ("localAnchorBX", C.c_double), ("localAnchorBY", C.c_double),
+        ("referenceAngle", C.c_double),
+        ("linearHertz", C.c_double), ("linearDampingRatio", C.c_double),
+        ("angularHertz", C.c_double), ("angularDampingRatio", C.c_double),
+        ("length", C.c_double), ("minLength", C.c_double), ("maxLength", C.c_double),
+        ("hertz", C.c_double), ("dampingRatio", C.c_double),
+        ("maxMotorForce", C.c_double), ("motorSpeed", C.c_double),
+        ("enableSpring", C.c_int32), ("enableLimit", C.c_int32), ("enableMotor", C.c_int32), ("pad0", C.c_int32),
+    ]
+
+
 def _fill(struct, values: dict):
     for k, v in values.items():
         setattr(struct, k, v)
@@ -145,6 +161,7 @@ def _bind(lib, prefix):
         "overlap_aabb": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), i]),
         "joint_color": (i, [i, i]),
         "body_set_awake": (None, [i, i, i]),
+        "create_joint": (i, [i, _P(JointDef)]),
         "world_enable_sleeping": (None, [i, i]),
     }
     out = {}
@@ -308,6 +325,10 @@ class _CpuWorld:
 
     def awake_body_count(self):
         return self._fns["awake_body_count"](self.w)
+
+    def create_joint(self, jd: dict) -> int:
+        """Weld or distance joint from a scenes.joint_def dict."""
+        return self._fns["create_joint"](self.w, C.byref(_fill(JointDef(), jd)))
 
     def set_awake(self, body, awake):
         self._fns["body_set_awake"](self.w, body, int(awake))

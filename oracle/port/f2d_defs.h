@@ -88,6 +88,30 @@ typedef struct f2d_revolute_def
 	int32_t pad3;
 } f2d_revolute_def;
 
+// Joints other than revolute, one definition for every type (fields a type
+// does not use are ignored): b2WeldJointDef, b2DistanceJointDef.
+#define F2D_JOINT_REVOLUTE 1
+#define F2D_JOINT_WELD 2
+#define F2D_JOINT_DISTANCE 3
+
+typedef struct f2d_joint_def
+{
+	int32_t type;
+	int32_t bodyA, bodyB; // 0-based body ids
+	int32_t collideConnected;
+	double localAnchorAX, localAnchorAY;
+	double localAnchorBX, localAnchorBY;
+	double referenceAngle;
+	// weld
+	double linearHertz, linearDampingRatio;
+	double angularHertz, angularDampingRatio;
+	// distance
+	double length, minLength, maxLength;
+	double hertz, dampingRatio;
+	double maxMotorForce, motorSpeed;
+	int32_t enableSpring, enableLimit, enableMotor, pad0;
+} f2d_joint_def;
+
 // Dump strides used by the ref_get_* / orc_get_* state readers.
 #define F2D_BODY_DUMP_STRIDE 12
 #define F2D_CONTACT_DUMP_INTS 9

@@ -195,6 +195,13 @@ typedef struct Softness
 	float biasRate, massScale, impulseScale;
 } Softness;
 
+enum
+{
+	P_JOINT_REVOLUTE = 1,
+	P_JOINT_WELD = 2,
+	P_JOINT_DISTANCE = 3,
+};
+
 typedef struct Joint
 {
 	int used;
@@ -225,6 +232,14 @@ typedef struct Joint
 	float axialMass;
 	Softness springSoftness, constraintSoftness;
 	float invMassA, invMassB, invIA, invIB;
+	// weld (weld_joint.c)
+	float linearHertz, linearDampingRatio, angularHertz, angularDampingRatio;
+	float angularImpulse;
+	Softness linearSoftness, angularSoftness;
+	// distance (distance_joint.c)
+	float length, minLength, maxLength, maxMotorForce;
+	float impulse;
+	Softness distanceSoftness;
 	// solver set and island (joint.h:60-100)
 	int setIndex;
 	int islandId, islandPrev, islandNext;

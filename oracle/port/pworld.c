@@ -544,11 +544,11 @@ static int assign_joint_color( World* w, int ia, int ib )
 	return P_OVERFLOW;
 }
 
-int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
+// joint.c:146-330 b2CreateJointInternal: id, body joint lists (new joint at
+// the head), then the type's fields (set by the caller), then
+// joint_finish: solver set, graph colour and island edge.
+static int joint_create_common( World* w, int bodyA, int bodyB, int collideConnected, int type )
 {
-	World* w = p_world( wi );
-	if ( w == NULL || d->bodyA < 0 || d->bodyA >= w->bodyCount || d->bodyB < 0 || d->bodyB >= w->bodyCount )
-		return -1;
 	int cap = w->jointCap;
 	int id = alloc_id( &w->jointFree, &w->jointFreeCount, &w->jointCount );
 	w->joints = grow( w->joints, &cap, w->jointCount, sizeof( Joint ) );
@@ -558,14 +558,14 @@ int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
 	memset( j, 0, sizeof( *j ) );
 	j->generation = gen + 1;
 	j->used = 1;
-	j->bodyA = d->bodyA;
-	j->bodyB = d->bodyB;
-	j->collideConnected = d->collideConnected != 0;
+	j->type = type;
+	j->bodyA = bodyA;
+	j->bodyB = bodyB;
+	j->collideConnected = collideConnected != 0;
 	j->color = P_NULL;
 	j->overflowIndex = P_NULL;
-	// doubly linked joint lists on both bodies, new joint at the head
-	Body* a = w->bodies + d->bodyA;
-	Body* b = w->bodies + d->bodyB;
+	Body* a = w->bodies + bodyA;
+	Body* b = w->bodies + bodyB;
 	j->prevA = P_NULL;
 	j->nextA = a->headJoint;
 	if ( a->headJoint != P_NULL )
@@ -590,31 +590,22 @@ int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
 	}
 	b->headJoint = ( id << 1 ) | 1;
 	b->jointCount += 1;
-
-	j->type = 1;
-	j->localOriginAnchorA = V( (float)d->localAnchorAX, (float)d->localAnchorAY );
-	j->localOriginAnchorB = V( (float)d->localAnchorBX, (float)d->localAnchorBY );
-	j->referenceAngle = fclampp( (float)d->referenceAngle, -P_PI, P_PI );
-	j->targetAngle = fclampp( (float)d->targetAngle, -P_PI, P_PI );
-	j->hertz = (float)d->hertz;
-	j->dampingRatio = (float)d->dampingRatio;
-	j->lowerAngle = (float)d->lowerAngle;
-	j->upperAngle = (float)d->upperAngle;
-	j->maxMotorTorque = (float)d->maxMotorTorque;
-	j->motorSpeed = (float)d->motorSpeed;
-	j->enableSpring = d->enableSpring != 0;
-	j->enableLimit = d->enableLimit != 0;
-	j->enableMotor = d->enableMotor != 0;
-	j->drawSize = (float)d->drawSize;
 	j->constraintHertz = 60.0f;
 	j->constraintDampingRatio = 2.0f;
 	j->constraintSoftness.biasRate = 0.0f;
 	j->constraintSoftness.massScale = 1.0f;
 	j->constraintSoftness.impulseScale = 0.0f;
+	return id;
+}
 
-	// solver set of the joint (joint.c:196-292): disabled, static, awake (in
-	// the graph, waking the other body's set), or the sleeping set of its
-	// bodies; then the island edge (joint.c:300-306)
+// solver set of the joint (joint.c:196-292): disabled, static, awake (in the
+// graph, waking the other body's set), or the sleeping set of its bodies;
+// then the island edge (joint.c:300-306)
+static void joint_finish( World* w, int id )
+{
+	Joint* j = w->joints + id;
+	Body* a = w->bodies + j->bodyA;
+	Body* b = w->bodies + j->bodyB;
 	j->islandId = j->islandPrev = j->islandNext = P_NULL;
 	int setA = a->setIndex, setB = b->setIndex;
 	int maxSet = setA > setB ? setA : setB;
@@ -636,8 +627,69 @@ int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
 		if ( setA != setB && setA >= SET_FIRST_SLEEPING && setB >= SET_FIRST_SLEEPING )
 			p_merge_solver_sets( w, setA, setB );
 	}
-	if ( j->setIndex > SET_DISABLED )
+	if ( w->joints[id].setIndex > SET_DISABLED )
 		p_link_joint( w, id, 1 );
+}
+
+int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || d->bodyA < 0 || d->bodyA >= w->bodyCount || d->bodyB < 0 || d->bodyB >= w->bodyCount )
+		return -1;
+	int id = joint_create_common( w, d->bodyA, d->bodyB, d->collideConnected, P_JOINT_REVOLUTE );
+	Joint* j = w->joints + id;
+	j->localOriginAnchorA = V( (float)d->localAnchorAX, (float)d->localAnchorAY );
+	j->localOriginAnchorB = V( (float)d->localAnchorBX, (float)d->localAnchorBY );
+	j->referenceAngle = fclampp( (float)d->referenceAngle, -P_PI, P_PI );
+	j->targetAngle = fclampp( (float)d->targetAngle, -P_PI, P_PI );
+	j->hertz = (float)d->hertz;
+	j->dampingRatio = (float)d->dampingRatio;
+	j->lowerAngle = (float)d->lowerAngle;
+	j->upperAngle = (float)d->upperAngle;
+	j->maxMotorTorque = (float)d->maxMotorTorque;
+	j->motorSpeed = (float)d->motorSpeed;
+	j->enableSpring = d->enableSpring != 0;
+	j->enableLimit = d->enableLimit != 0;
+	j->enableMotor = d->enableMotor != 0;
+	j->drawSize = (float)d->drawSize;
+	joint_finish( w, id );
+	return id;
+}
+
+// joint.c:609-649 b2CreateWeldJoint, :353-404 b2CreateDistanceJoint
+int orc_create_joint( int wi, const f2d_joint_def* d )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || d->bodyA < 0 || d->bodyA >= w->bodyCount || d->bodyB < 0 || d->bodyB >= w->bodyCount )
+		return -1;
+	if ( d->type != P_JOINT_WELD && d->type != P_JOINT_DISTANCE )
+		return -1;
+	int id = joint_create_common( w, d->bodyA, d->bodyB, d->collideConnected, d->type );
+	Joint* j = w->joints + id;
+	j->localOriginAnchorA = V( (float)d->localAnchorAX, (float)d->localAnchorAY );
+	j->localOriginAnchorB = V( (float)d->localAnchorBX, (float)d->localAnchorBY );
+	if ( d->type == P_JOINT_WELD )
+	{
+		j->referenceAngle = (float)d->referenceAngle;
+		j->linearHertz = (float)d->linearHertz;
+		j->linearDampingRatio = (float)d->linearDampingRatio;
+		j->angularHertz = (float)d->angularHertz;
+		j->angularDampingRatio = (float)d->angularDampingRatio;
+	}
+	else
+	{
+		j->length = fmaxp( (float)d->length, P_LINEAR_SLOP );
+		j->hertz = (float)d->hertz;
+		j->dampingRatio = (float)d->dampingRatio;
+		j->minLength = fmaxp( (float)d->minLength, P_LINEAR_SLOP );
+		j->maxLength = fmaxp( (float)d->minLength, (float)d->maxLength );
+		j->maxMotorForce = (float)d->maxMotorForce;
+		j->motorSpeed = (float)d->motorSpeed;
+		j->enableSpring = d->enableSpring != 0;
+		j->enableLimit = d->enableLimit != 0;
+		j->enableMotor = d->enableMotor != 0;
+	}
+	joint_finish( w, id );
 	return id;
 }
 

@@ -419,6 +419,52 @@ int ref_create_revolute_joint( int w, const f2d_revolute_def* d )
 	return id.index1 - 1;
 }
 
+// Weld and distance joints (b2CreateWeldJoint, b2CreateDistanceJoint)
+int ref_create_joint( int w, const f2d_joint_def* d )
+{
+	b2JointId id = { 0 };
+	b2Vec2 la = { (float)d->localAnchorAX, (float)d->localAnchorAY };
+	b2Vec2 lb = { (float)d->localAnchorBX, (float)d->localAnchorBY };
+	if ( d->type == F2D_JOINT_WELD )
+	{
+		b2WeldJointDef def = b2DefaultWeldJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.localAnchorA = la;
+		def.localAnchorB = lb;
+		def.referenceAngle = (float)d->referenceAngle;
+		def.linearHertz = (float)d->linearHertz;
+		def.linearDampingRatio = (float)d->linearDampingRatio;
+		def.angularHertz = (float)d->angularHertz;
+		def.angularDampingRatio = (float)d->angularDampingRatio;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreateWeldJoint( s_worlds[w], &def );
+	}
+	else if ( d->type == F2D_JOINT_DISTANCE )
+	{
+		b2DistanceJointDef def = b2DefaultDistanceJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.localAnchorA = la;
+		def.localAnchorB = lb;
+		def.length = (float)d->length;
+		def.minLength = (float)d->minLength;
+		def.maxLength = (float)d->maxLength;
+		def.hertz = (float)d->hertz;
+		def.dampingRatio = (float)d->dampingRatio;
+		def.maxMotorForce = (float)d->maxMotorForce;
+		def.motorSpeed = (float)d->motorSpeed;
+		def.enableSpring = d->enableSpring != 0;
+		def.enableLimit = d->enableLimit != 0;
+		def.enableMotor = d->enableMotor != 0;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreateDistanceJoint( s_worlds[w], &def );
+	}
+	else
+		return -1;
+	return id.index1 - 1;
+}
+
 // ---------------------------------------------------------------------------
 // State dumps
 // ---------------------------------------------------------------------------

@@ -33,6 +33,8 @@ CASES = {
                    frames=256, checkpoints=[1, 64, 256]),
     "joints": dict(world=dict(enableSleep=0), scene=("joint_gallery", dict()), frames=256,
                    checkpoints=[1, 64, 256]),
+    "joint_zoo": dict(world=dict(enableSleep=0), scene=("joint_zoo", dict()), frames=256,
+                      checkpoints=[1, 64, 256]),
     # sleeping on: islands, sleeping solver sets, island splits
     "pyramid_sleep": dict(world=dict(enableSleep=1), scene=("pyramid", dict(rows=12)), frames=120,
                           checkpoints=[1, 30, 44, 60, 120]),

@@ -41,6 +41,7 @@ SCENES = [
     ("pyramid_small", dict(enableSleep=0), "pyramid", dict(rows=12), 200),
     ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300),
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400),
+    ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=4), 400),
 ]
 
 
@@ -66,6 +67,7 @@ SLEEP_SCENES = [
     ("pile_sleep", dict(enableSleep=1, enableContinuous=1), "pile",
      dict(count=300, seed=3, width=20.0, height=30.0), 450),
     ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
+    ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
 ]
 
 
@@ -100,7 +102,7 @@ def test_port_sleep_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene,
     scenes.build(ref, scene, **kw)
     scenes.build(port, scene, **kw)
     lockstep_full(ref, port, frames)
-    if name != "chains_sleep":
+    if name in ("pyramid_sleep", "pile_sleep"):
         assert ref.awake_body_count() == 0
     ref.close()
     port.close()
