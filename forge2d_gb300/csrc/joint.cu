@@ -30,6 +30,46 @@ __global__ void k_prepare_joints( DWorld w, float h, float inv_h, Soft jointSoft
 		fv2 anchorB = rrot( qB, vsub( mk( d0.z, d0.w ), mk( lcb.x, lcb.y ) ) );
 		float2 ca = w.center[a], cb = w.center[b];
 		fv2 deltaCenter = vsub( mk( cb.x, cb.y ), mk( ca.x, ca.y ) );
+		int type = joint_type( w.jflags[j] );
+		if ( type == JT_WELD )
+		{
+			// weld_joint.c:116-140
+			float4 d1 = w.jdef1[j]; // referenceAngle linearHertz linearDampingRatio angularHertz
+			float4 d2 = w.jdef2[j]; // angularDampingRatio
+			float deltaAngle = unwind_angle( relative_angle( qB, qA ) - d1.x );
+			float k = iA + iB;
+			float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+			Soft ls = d1.y == 0.0f ? jointSoft : make_soft( d1.y, d1.z, h );
+			Soft as = d1.w == 0.0f ? jointSoft : make_soft( d1.w, d2.x, h );
+			w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+			w.jprep1[j] = make_float4( deltaCenter.x, deltaCenter.y, deltaAngle, axialMass );
+			w.jprep2[j] = make_float4( ls.biasRate, ls.massScale, ls.impulseScale, 0.0f );
+			w.jprep2[w.jointCap + j] = make_float4( as.biasRate, as.massScale, as.impulseScale, 0.0f );
+			if ( w.enableWarmStarting == 0 )
+				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			continue;
+		}
+		if ( type == JT_DISTANCE )
+		{
+			// distance_joint.c:179-205
+			float4 d1 = w.jdef1[j]; // length minLength maxLength hertz
+			float4 d2 = w.jdef2[j]; // dampingRatio maxMotorForce motorSpeed
+			fv2 separation = vadd( vsub( anchorB, anchorA ), deltaCenter );
+			fv2 axis = vnormalize( separation );
+			float crA = vcross( anchorA, axis );
+			float crB = vcross( anchorB, axis );
+			float k = mA + mB + iA * crA * crA + iB * crB * crB;
+			float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+			Soft ds = make_soft( d1.w, d2.x, h );
+			w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+			w.jprep1[j] = make_float4( deltaCenter.x, deltaCenter.y, 0.0f, axialMass );
+			w.jprep2[j] = make_float4( ds.biasRate, ds.massScale, ds.impulseScale, 0.0f );
+			w.jprep2[w.jointCap + j] =
+				make_float4( jointSoft.biasRate, jointSoft.massScale, jointSoft.impulseScale, 0.0f );
+			if ( w.enableWarmStarting == 0 )
+				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			continue;
+		}
 		float deltaAngle = relative_angle( qB, qA );
 		float k = iA + iB;
 		float axialMass = k > 0.0f ? 1.0f / k : 0.0f;

@@ -13,6 +13,7 @@
 #include "dsort.cuh"
 #include "dworld.cuh"
 #include "hgeom.h"
+#include "joint.cuh"
 #include "kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -1260,35 +1261,15 @@ extern "C" F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t wg )
 // ---------------------------------------------------------------------------
 // joints (joint.c:146-330, :507-560)
 // ---------------------------------------------------------------------------
-extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
-													  int32_t* wg )
+// Shared tail of the joint constructors (joint.c:146-330): slot, generation,
+// body joint lists, definition rows, then the graph / island log.
+static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0, float4 d1, float4 d2,
+								int32_t* index1, int32_t* wg )
 {
-	if ( index1 )
-		*index1 = 0;
-	if ( wg )
-		*wg = 0;
-	HostWorld* W = world_from_id( worldId );
-	if ( W == nullptr || def == nullptr )
-		return 0;
-	HostWorld* WA;
-	HostWorld* WB;
-	int a = body_from( def->bodyAIndex1, def->bodyAWorldAndGeneration, &WA );
-	int b = body_from( def->bodyBIndex1, def->bodyBWorldAndGeneration, &WB );
-	if ( a < 0 || b < 0 || WA != W || WB != W )
-		return 0;
 	int j = W->jointCount++;
 	uint16_t gen = (uint16_t)( ( j < (int)W->jgen.size() ? W->jgen[j] : 0 ) + 1 );
 	vset( W->jgen, j, gen );
 	vset( W->jbody, j, make_int2( a, b ) );
-	int flags = 0x1;
-	if ( def->enableSpring )
-		flags |= 0x2;
-	if ( def->enableLimit )
-		flags |= 0x4;
-	if ( def->enableMotor )
-		flags |= 0x8;
-	if ( def->collideConnected )
-		flags |= 0x10;
 	vset( W->jflags, j, flags );
 	vset( W->jcolor, j, F2D_NULL );
 	if ( (int)W->jnext.size() < 2 * ( j + 1 ) )
@@ -1303,15 +1284,9 @@ extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d
 	W->jointCountB[b] += 1;
 	mark_body( W, a );
 	mark_body( W, b );
-	float ref = fclamp_s( (float)def->referenceAngle, -F2D_PI, F2D_PI );
-	float target = fclamp_s( (float)def->targetAngle, -F2D_PI, F2D_PI );
-	vset( W->jdef0, j,
-		  make_float4( (float)def->localAnchorAX, (float)def->localAnchorAY, (float)def->localAnchorBX,
-					   (float)def->localAnchorBY ) );
-	vset( W->jdef1, j, make_float4( ref, target, (float)def->hertz, (float)def->dampingRatio ) );
-	vset( W->jdef2, j,
-		  make_float4( (float)def->lowerAngle, (float)def->upperAngle, (float)def->maxMotorTorque,
-					   (float)def->motorSpeed ) );
+	vset( W->jdef0, j, d0 );
+	vset( W->jdef1, j, d1 );
+	vset( W->jdef2, j, d2 );
 	// joints between two static bodies never enter the graph
 	bool staticA = body_type( W->bflags[a] ) == 0, staticB = body_type( W->bflags[b] ) == 0;
 	if ( W->islOn )
@@ -1323,6 +1298,95 @@ extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d
 	if ( wg )
 		*wg = pack_wg( W, gen );
 	return 1;
+}
+
+static HostWorld* joint_bodies( int32_t worldId, int32_t aIndex1, int32_t aWg, int32_t bIndex1, int32_t bWg, int* a,
+								int* b )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return nullptr;
+	HostWorld* WA;
+	HostWorld* WB;
+	*a = body_from( aIndex1, aWg, &WA );
+	*b = body_from( bIndex1, bWg, &WB );
+	if ( *a < 0 || *b < 0 || WA != W || WB != W )
+		return nullptr;
+	return W;
+}
+
+extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
+													  int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	if ( def == nullptr )
+		return 0;
+	int a, b;
+	HostWorld* W = joint_bodies( worldId, def->bodyAIndex1, def->bodyAWorldAndGeneration, def->bodyBIndex1,
+								 def->bodyBWorldAndGeneration, &a, &b );
+	if ( W == nullptr )
+		return 0;
+	int flags = JF_USED;
+	if ( def->enableSpring )
+		flags |= JF_SPRING;
+	if ( def->enableLimit )
+		flags |= JF_LIMIT;
+	if ( def->enableMotor )
+		flags |= JF_MOTOR;
+	if ( def->collideConnected )
+		flags |= JF_COLLIDE;
+	float ref = fclamp_s( (float)def->referenceAngle, -F2D_PI, F2D_PI );
+	float target = fclamp_s( (float)def->targetAngle, -F2D_PI, F2D_PI );
+	return create_joint_common(
+		W, a, b, flags,
+		make_float4( (float)def->localAnchorAX, (float)def->localAnchorAY, (float)def->localAnchorBX,
+					 (float)def->localAnchorBY ),
+		make_float4( ref, target, (float)def->hertz, (float)def->dampingRatio ),
+		make_float4( (float)def->lowerAngle, (float)def->upperAngle, (float)def->maxMotorTorque, (float)def->motorSpeed ),
+		index1, wg );
+}
+
+// weld_joint.c b2CreateWeldJoint (joint.c:575-600), distance_joint.c
+// b2CreateDistanceJoint (joint.c:400-440): lengths clamped to the linear slop,
+// maxLength at least minLength.
+extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_def* def, int32_t* index1, int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	if ( def == nullptr || ( def->type != F2D_JOINT_WELD && def->type != F2D_JOINT_DISTANCE ) )
+		return 0;
+	int a, b;
+	HostWorld* W = joint_bodies( worldId, def->bodyAIndex1, def->bodyAWorldAndGeneration, def->bodyBIndex1,
+								 def->bodyBWorldAndGeneration, &a, &b );
+	if ( W == nullptr )
+		return 0;
+	int flags = JF_USED | ( def->type << JF_TYPE_SHIFT );
+	if ( def->collideConnected )
+		flags |= JF_COLLIDE;
+	float4 d0 = make_float4( (float)def->localAnchorAX, (float)def->localAnchorAY, (float)def->localAnchorBX,
+							 (float)def->localAnchorBY );
+	if ( def->type == F2D_JOINT_WELD )
+		return create_joint_common( W, a, b, flags, d0,
+									make_float4( (float)def->referenceAngle, (float)def->linearHertz,
+												 (float)def->linearDampingRatio, (float)def->angularHertz ),
+									make_float4( (float)def->angularDampingRatio, 0.0f, 0.0f, 0.0f ), index1, wg );
+	if ( def->enableSpring )
+		flags |= JF_SPRING;
+	if ( def->enableLimit )
+		flags |= JF_LIMIT;
+	if ( def->enableMotor )
+		flags |= JF_MOTOR;
+	float minLength = fmax_s( (float)def->minLength, F2D_LINEAR_SLOP );
+	return create_joint_common(
+		W, a, b, flags, d0,
+		make_float4( fmax_s( (float)def->length, F2D_LINEAR_SLOP ), minLength,
+					 fmax_s( (float)def->minLength, (float)def->maxLength ), (float)def->hertz ),
+		make_float4( (float)def->dampingRatio, (float)def->maxMotorForce, (float)def->motorSpeed, 0.0f ), index1, wg );
 }
 
 extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )

@@ -73,6 +73,25 @@ class RevoluteDef(C.Structure):
     ]
 
 
+class JointDef(C.Structure):
+    """f2d_joint_def: weld (type 2) and distance (type 3) joints."""
+    _fields_ = [
+        ("type", C.c_int32),
+        ("bodyAIndex1", C.c_int32), ("bodyAWorldAndGeneration", C.c_int32),
+        ("bodyBIndex1", C.c_int32), ("bodyBWorldAndGeneration", C.c_int32),
+        ("collideConnected", C.c_int32),
+        ("localAnchorAX", C.c_double), ("localAnchorAY", C.c_double),
+        ("localAnchorBX", C.c_double), ("localAnchorBY", C.c_double),
+        ("referenceAngle", C.c_double),
+        ("linearHertz", C.c_double), ("linearDampingRatio", C.c_double),
+        ("angularHertz", C.c_double), ("angularDampingRatio", C.c_double),
+        ("length", C.c_double), ("minLength", C.c_double), ("maxLength", C.c_double),
+        ("hertz", C.c_double), ("dampingRatio", C.c_double),
+        ("maxMotorForce", C.c_double), ("motorSpeed", C.c_double),
+        ("enableSpring", C.c_int32), ("enableLimit", C.c_int32), ("enableMotor", C.c_int32), ("pad0", C.c_int32),
+    ]
+
+
 # (name, restype, argtypes)
 _i, _d, _f, _i64 = C.c_int32, C.c_double, C.c_float, C.c_int64
 _SIGS = [
@@ -121,6 +140,7 @@ _SIGS = [
     ("f2d_shape_is_valid", _i, [_i, _i]),
     ("f2d_shape_get_type", _i, [_i, _i]),
     ("f2d_create_revolute_joint", _i, [_i, _P(RevoluteDef), _P(_i), _P(_i)]),
+    ("f2d_create_joint", _i, [_i, _P(JointDef), _P(_i), _P(_i)]),
     ("f2d_joint_is_valid", _i, [_i, _i]),
     ("f2d_world_get_event_counts", None, [_i, _P(_i)]),
     ("f2d_world_get_begin_events", _i, [_i, _P(_i), _i]),

@@ -16,7 +16,8 @@ import ctypes as C
 import numpy as np
 
 from . import native
-from .scenes import BODY_DEFAULTS, SHAPE_DEFAULTS, WORLD_DEFAULTS, REVOLUTE_DEFAULTS
+from .scenes import (BODY_DEFAULTS, JOINT_DEFAULTS, JOINT_DISTANCE, JOINT_WELD, REVOLUTE_DEFAULTS,
+                     SHAPE_DEFAULTS, WORLD_DEFAULTS)
 
 BODY_STRIDE = 12
 CONTACT_INTS = 9
@@ -143,6 +144,18 @@ class GpuWorld:
         rd.bodyBIndex1, rd.bodyBWorldAndGeneration = b
         i1, wg = C.c_int32(0), C.c_int32(0)
         ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def create_joint(self, jd: dict):
+        """Weld (type 2) or distance (type 3) joint from an f2d_joint_def dict."""
+        d = dict(JOINT_DEFAULTS)
+        d.update(jd)
+        a, b = d.pop("bodyA"), d.pop("bodyB")
+        rd = _fill(native.JointDef(), d)
+        rd.bodyAIndex1, rd.bodyAWorldAndGeneration = a
+        rd.bodyBIndex1, rd.bodyBWorldAndGeneration = b
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
     def autotune(self, dt=1.0 / 60.0, substeps=4, steps_per_candidate=3):
@@ -527,6 +540,14 @@ class World:
         jd["bodyA"] = body_a.id
         jd["bodyB"] = body_b.id
         return Joint(self, self._w.create_revolute(jd))
+
+    def create_weld_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_WELD, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_distance_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_DISTANCE, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
 
     @property
     def gravity(self):

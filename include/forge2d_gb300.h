@@ -122,6 +122,30 @@ typedef struct f2d_revolute_def
 	int32_t pad3;
 } f2d_revolute_def;
 
+/* Mirrors RawBox2D.createWeldJoint / createDistanceJoint (raw_box2d.dart:
+ * 582-600, 679-692 -> b2CreateWeldJoint / b2CreateDistanceJoint): one
+ * definition for both types; fields the type does not use are ignored. */
+#define F2D_JOINT_WELD 2
+#define F2D_JOINT_DISTANCE 3
+typedef struct f2d_joint_def
+{
+	int32_t type;
+	int32_t bodyAIndex1, bodyAWorldAndGeneration;
+	int32_t bodyBIndex1, bodyBWorldAndGeneration;
+	int32_t collideConnected;
+	double localAnchorAX, localAnchorAY;
+	double localAnchorBX, localAnchorBY;
+	double referenceAngle;
+	/* weld */
+	double linearHertz, linearDampingRatio;
+	double angularHertz, angularDampingRatio;
+	/* distance */
+	double length, minLength, maxLength;
+	double hertz, dampingRatio;
+	double maxMotorForce, motorSpeed;
+	int32_t enableSpring, enableLimit, enableMotor, pad0;
+} f2d_joint_def;
+
 #define F2D_STATUS_OK 0
 #define F2D_STATUS_CONTACT_CAPACITY 0x1
 #define F2D_STATUS_PAIR_CAPACITY 0x2
@@ -256,6 +280,9 @@ F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t worldAndGeneration )
 /* ---- joints ------------------------------------------------------------- */
 
 /* RawBox2D.createRevoluteJoint (world.dart:297-321 -> b2CreateRevoluteJoint, joint.c:507). */
+/* RawBox2D.createWeldJoint / createDistanceJoint (raw_box2d.dart:582, 679). */
+F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_def* def, int32_t* index1,
+								  int32_t* worldAndGeneration );
 F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
 										   int32_t* worldAndGeneration );
 F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );

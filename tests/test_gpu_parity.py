@@ -55,6 +55,8 @@ NATIVE = [
      dict(count=700, seed=4, width=30.0, height=60.0, filters=True), 200, 25),
     ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300, 25),
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400, 25),
+    # weld cantilevers (stiff and soft), distance rods, springs with limits, motors
+    ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=8), 400, 25),
     ("batched24", dict(enableSleep=0, enableContinuous=1), "batched", dict(worlds=24, seed=3), 200, 25),
     # overflow constraints solved by levels: a 150-deep chain (past the
     # parallel levels, into the serial tail), overflow joints, and many

@@ -53,6 +53,8 @@ SCENES = [
     ("pile_sleep", dict(enableSleep=1, enableContinuous=1), "pile",
      dict(count=300, seed=3, width=20.0, height=30.0), 450),
     ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
+    # weld and distance joints link islands and sleep with them
+    ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
 ]
 
 
