@@ -58,7 +58,7 @@ REVOLUTE_DEFAULTS = dict(
 )
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
-JOINT_WELD, JOINT_DISTANCE = 2, 3
+JOINT_WELD, JOINT_DISTANCE, JOINT_PRISMATIC, JOINT_WHEEL, JOINT_MOTOR, JOINT_MOUSE, JOINT_FILTER = 2, 3, 4, 5, 6, 7, 8
 
 JOINT_DEFAULTS = dict(
     type=JOINT_WELD, bodyA=0, bodyB=0, collideConnected=0,
@@ -66,6 +66,9 @@ JOINT_DEFAULTS = dict(
     referenceAngle=0.0, linearHertz=0.0, linearDampingRatio=0.0, angularHertz=0.0, angularDampingRatio=0.0,
     length=1.0, minLength=0.0, maxLength=100000.0, hertz=0.0, dampingRatio=0.0,
     maxMotorForce=0.0, motorSpeed=0.0, enableSpring=0, enableLimit=0, enableMotor=0,
+    localAxisAX=1.0, localAxisAY=0.0, targetTranslation=0.0, lowerTranslation=0.0, upperTranslation=0.0,
+    maxMotorTorque=0.0, linearOffsetX=0.0, linearOffsetY=0.0, angularOffset=0.0,
+    maxForce=1.0, maxTorque=1.0, correctionFactor=0.3, targetX=0.0, targetY=0.0,
 )
 
 
@@ -356,6 +359,61 @@ def joint_zoo(b, copies=3):
                                  enableLimit=1, minLength=1.5, maxLength=4.0))
 
 
+def joint_rigs(b, copies=3):
+    """Prismatic, wheel, motor, mouse and filter joints, ``copies`` times over
+    a ground box: an elevator (vertical prismatic with limits and a motor)
+    carrying a box, a horizontal prismatic spring, a two-wheeled cart on
+    sprung, limited, motored wheel joints, a box led by a motor joint, a box
+    held up by a mouse joint, and two overlapping boxes a filter joint keeps
+    from colliding. Returns the mouse joints' ids."""
+    g = b.create_body(body_def(type=STATIC, positionY=-1.0))
+    b.create_box(g, shape_def(), 30.0 * copies, 1.0)
+    mice = []
+    for k in range(copies):
+        x0 = -30.0 * copies + 5.0 + 30.0 * k
+        base = b.create_body(body_def(type=STATIC, positionX=x0, positionY=0.5))
+        b.create_box(base, shape_def(), 0.2, 0.2)
+        lift = b.create_body(body_def(type=DYNAMIC, positionX=x0, positionY=1.0))
+        b.create_box(lift, shape_def(), 1.0, 0.1)
+        b.create_joint(joint_def(type=JOINT_PRISMATIC, bodyA=base, bodyB=lift, localAnchorAY=0.5,
+                                 localAxisAX=0.0, localAxisAY=1.0, enableLimit=1, lowerTranslation=0.0,
+                                 upperTranslation=3.0 + k, enableMotor=1, maxMotorForce=60.0,
+                                 motorSpeed=1.0 + 0.5 * k))
+        cargo = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 0.2, positionY=1.5))
+        b.create_box(cargo, shape_def(), 0.3, 0.3)
+        slider = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 4.0, positionY=3.0))
+        b.create_box(slider, shape_def(), 0.4, 0.2)
+        b.create_joint(joint_def(type=JOINT_PRISMATIC, bodyA=base, bodyB=slider, localAnchorAX=3.0,
+                                 localAnchorAY=2.5, localAxisAX=1.0, localAxisAY=0.2 * k, referenceAngle=0.1,
+                                 enableSpring=1, hertz=1.5, dampingRatio=0.2, targetTranslation=1.0))
+        cx, cy = x0 + 9.0, 1.5
+        chassis = b.create_body(body_def(type=DYNAMIC, positionX=cx, positionY=cy))
+        b.create_box(chassis, shape_def(), 1.2, 0.25)
+        for side in (-1.0, 1.0):
+            wheel = b.create_body(body_def(type=DYNAMIC, positionX=cx + 0.9 * side, positionY=cy - 0.6))
+            b.create_circle(wheel, shape_def(friction=0.9), 0.0, 0.0, 0.35)
+            b.create_joint(joint_def(type=JOINT_WHEEL, bodyA=chassis, bodyB=wheel, localAnchorAX=0.9 * side,
+                                     localAnchorAY=-0.6, localAxisAX=0.0, localAxisAY=1.0, enableSpring=1,
+                                     hertz=4.0, dampingRatio=0.7, enableLimit=1, lowerTranslation=-0.25,
+                                     upperTranslation=0.25, enableMotor=1, maxMotorTorque=8.0,
+                                     motorSpeed=-2.0 - k))
+        led = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 15.0, positionY=0.5))
+        b.create_box(led, shape_def(), 0.5, 0.5)
+        b.create_joint(joint_def(type=JOINT_MOTOR, bodyA=g, bodyB=led, linearOffsetX=x0 + 16.0,
+                                 linearOffsetY=4.0, angularOffset=0.5 + 0.2 * k, maxForce=80.0, maxTorque=20.0,
+                                 correctionFactor=0.3))
+        held = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 20.0, positionY=0.5))
+        b.create_box(held, shape_def(), 0.4, 0.6)
+        mice.append(b.create_joint(joint_def(type=JOINT_MOUSE, bodyA=g, bodyB=held, targetX=x0 + 20.3,
+                                             targetY=3.0, hertz=5.0, dampingRatio=0.7, maxForce=200.0)))
+        under = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 25.0, positionY=0.5))
+        b.create_box(under, shape_def(), 0.5, 0.5)
+        over = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 25.2, positionY=1.2))
+        b.create_box(over, shape_def(), 0.5, 0.5)
+        b.create_joint(joint_def(type=JOINT_FILTER, bodyA=under, bodyB=over))
+    return mice
+
+
 def batched(b, worlds=4096, seed=7, tile=220.0, columns=64, only=None):
     """The batched scene: ``worlds`` independent sub-worlds of uneven size,
     each drawn from ``seed`` as a pyramid (rows U{5..30}), a random pile
@@ -440,4 +498,6 @@ def build(b, name, **kw):
         return overflow_heap(b, **kw)
     if name == "joint_zoo":
         return joint_zoo(b, **kw)
+    if name == "joint_rigs":
+        return joint_rigs(b, **kw)
     raise ValueError(name)

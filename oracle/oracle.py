@@ -86,7 +86,8 @@ class RevoluteDef(C.Structure):
 
 
 class JointDef(C.Structure):
-    """f2d_joint_def: weld (type 2) and distance (type 3) joints."""
+    """f2d_joint_def: weld 2, distance 3, prismatic 4, wheel 5, motor 6,
+    mouse 7 and filter 8 joints."""
     _fields_ = [
         ("type", C.c_int32), ("bodyA", C.c_int32), ("bodyB", C.c_int32), ("collideConnected", C.c_int32),
         ("localAnchorAX", C.c_double), ("localAnchorAY", C.c_double),
@@ -98,6 +99,12 @@ class JointDef(C.Structure):
         ("hertz", C.c_double), ("dampingRatio", C.c_double),
         ("maxMotorForce", C.c_double), ("motorSpeed", C.c_double),
         ("enableSpring", C.c_int32), ("enableLimit", C.c_int32), ("enableMotor", C.c_int32), ("pad0", C.c_int32),
+        ("localAxisAX", C.c_double), ("localAxisAY", C.c_double),
+        ("targetTranslation", C.c_double), ("lowerTranslation", C.c_double), ("upperTranslation", C.c_double),
+        ("maxMotorTorque", C.c_double),
+        ("linearOffsetX", C.c_double), ("linearOffsetY", C.c_double), ("angularOffset", C.c_double),
+        ("maxForce", C.c_double), ("maxTorque", C.c_double), ("correctionFactor", C.c_double),
+        ("targetX", C.c_double), ("targetY", C.c_double),
     ]
 
 
@@ -162,6 +169,7 @@ def _bind(lib, prefix):
         "joint_color": (i, [i, i]),
         "body_set_awake": (None, [i, i, i]),
         "create_joint": (i, [i, _P(JointDef)]),
+        "mouse_joint_set_target": (None, [i, i, d, d]),
         "world_enable_sleeping": (None, [i, i]),
     }
     out = {}
@@ -329,6 +337,9 @@ class _CpuWorld:
     def create_joint(self, jd: dict) -> int:
         """Weld or distance joint from a scenes.joint_def dict."""
         return self._fns["create_joint"](self.w, C.byref(_fill(JointDef(), jd)))
+
+    def mouse_set_target(self, joint, x, y):
+        self._fns["mouse_joint_set_target"](self.w, joint, x, y)
 
     def set_awake(self, body, awake):
         self._fns["body_set_awake"](self.w, body, int(awake))

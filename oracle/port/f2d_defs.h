@@ -89,10 +89,17 @@ typedef struct f2d_revolute_def
 } f2d_revolute_def;
 
 // Joints other than revolute, one definition for every type (fields a type
-// does not use are ignored): b2WeldJointDef, b2DistanceJointDef.
+// does not use are ignored): b2WeldJointDef, b2DistanceJointDef,
+// b2PrismaticJointDef, b2WheelJointDef, b2MotorJointDef, b2MouseJointDef,
+// b2FilterJointDef (types.h:530-780).
 #define F2D_JOINT_REVOLUTE 1
 #define F2D_JOINT_WELD 2
 #define F2D_JOINT_DISTANCE 3
+#define F2D_JOINT_PRISMATIC 4
+#define F2D_JOINT_WHEEL 5
+#define F2D_JOINT_MOTOR 6
+#define F2D_JOINT_MOUSE 7
+#define F2D_JOINT_FILTER 8
 
 typedef struct f2d_joint_def
 {
@@ -110,6 +117,15 @@ typedef struct f2d_joint_def
 	double hertz, dampingRatio;
 	double maxMotorForce, motorSpeed;
 	int32_t enableSpring, enableLimit, enableMotor, pad0;
+	// prismatic and wheel
+	double localAxisAX, localAxisAY;
+	double targetTranslation, lowerTranslation, upperTranslation;
+	double maxMotorTorque;
+	// motor (maxForce also the mouse joint's)
+	double linearOffsetX, linearOffsetY, angularOffset;
+	double maxForce, maxTorque, correctionFactor;
+	// mouse
+	double targetX, targetY;
 } f2d_joint_def;
 
 // Dump strides used by the ref_get_* / orc_get_* state readers.

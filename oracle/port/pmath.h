@@ -256,6 +256,22 @@ static inline v2 solve22( v2 cx, v2 cy, v2 b )
 // math_functions.c:61-102 (minimax atan2) and :108-151 (Bhaskara cos/sin)
 float p_atan2( float y, float x );
 void p_cossin( float radians, float* c, float* s );
+// math_functions.h:541-565 b2MulMV, b2GetInverse22 (columns cx, cy)
+static inline v2 mulMV( v2 cx, v2 cy, v2 v )
+{
+	return V( cx.x * v.x + cy.x * v.y, cx.y * v.x + cy.y * v.y );
+}
+
+static inline void inverse22( v2 cx, v2 cy, v2* icx, v2* icy )
+{
+	float a = cx.x, b = cy.x, c = cx.y, d = cy.y;
+	float det = a * d - b * c;
+	if ( det != 0.0f )
+		det = 1.0f / det;
+	*icx = V( det * d, -det * c );
+	*icy = V( -det * b, det * a );
+}
+
 static inline float relativeAngle( rot b, rot a )
 {
 	float s = b.s * a.c - b.c * a.s;

@@ -200,13 +200,18 @@ enum
 	P_JOINT_REVOLUTE = 1,
 	P_JOINT_WELD = 2,
 	P_JOINT_DISTANCE = 3,
+	P_JOINT_PRISMATIC = 4,
+	P_JOINT_WHEEL = 5,
+	P_JOINT_MOTOR = 6,
+	P_JOINT_MOUSE = 7,
+	P_JOINT_FILTER = 8,
 };
 
 typedef struct Joint
 {
 	int used;
 	int generation;
-	int type; // revolute only here
+	int type; // P_JOINT_*
 	int bodyA, bodyB;
 	int color;
 	int overflowIndex;
@@ -240,6 +245,17 @@ typedef struct Joint
 	float length, minLength, maxLength, maxMotorForce;
 	float impulse;
 	Softness distanceSoftness;
+	// prismatic and wheel (prismatic_joint.c, wheel_joint.c)
+	v2 localAxisA, axisA;
+	float targetTranslation, lowerTranslation, upperTranslation;
+	v2 prismaticImpulse; // perpendicular, angular
+	float perpImpulse, perpMass, motorMass;
+	// motor and mouse (motor_joint.c, mouse_joint.c)
+	v2 linearOffset;
+	float angularOffset, maxForce, maxTorque, correctionFactor;
+	v2 linearMassCx, linearMassCy;
+	float angularMass;
+	v2 targetA;
 	// solver set and island (joint.h:60-100)
 	int setIndex;
 	int islandId, islandPrev, islandNext;

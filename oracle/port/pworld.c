@@ -662,13 +662,64 @@ int orc_create_joint( int wi, const f2d_joint_def* d )
 	World* w = p_world( wi );
 	if ( w == NULL || d->bodyA < 0 || d->bodyA >= w->bodyCount || d->bodyB < 0 || d->bodyB >= w->bodyCount )
 		return -1;
-	if ( d->type != P_JOINT_WELD && d->type != P_JOINT_DISTANCE )
+	if ( d->type < P_JOINT_WELD || d->type > P_JOINT_FILTER )
 		return -1;
-	int id = joint_create_common( w, d->bodyA, d->bodyB, d->collideConnected, d->type );
+	// joint.c:444-478 the mouse joint reads the bodies' transforms before the
+	// joint exists; joint.c:480-502 a filter joint never lets the bodies collide
+	xform xfA = w->bodies[d->bodyA].xf, xfB = w->bodies[d->bodyB].xf;
+	int collide = d->type == P_JOINT_FILTER ? 0 : d->collideConnected;
+	int id = joint_create_common( w, d->bodyA, d->bodyB, collide, d->type );
 	Joint* j = w->joints + id;
 	j->localOriginAnchorA = V( (float)d->localAnchorAX, (float)d->localAnchorAY );
 	j->localOriginAnchorB = V( (float)d->localAnchorBX, (float)d->localAnchorBY );
-	if ( d->type == P_JOINT_WELD )
+	if ( d->type == P_JOINT_PRISMATIC || d->type == P_JOINT_WHEEL )
+	{
+		// joint.c:559-649
+		j->localAxisA = normalize( V( (float)d->localAxisAX, (float)d->localAxisAY ) );
+		j->lowerTranslation = (float)d->lowerTranslation;
+		j->upperTranslation = (float)d->upperTranslation;
+		j->hertz = (float)d->hertz;
+		j->dampingRatio = (float)d->dampingRatio;
+		j->motorSpeed = (float)d->motorSpeed;
+		j->enableSpring = d->enableSpring != 0;
+		j->enableLimit = d->enableLimit != 0;
+		j->enableMotor = d->enableMotor != 0;
+		if ( d->type == P_JOINT_PRISMATIC )
+		{
+			j->referenceAngle = (float)d->referenceAngle;
+			j->targetTranslation = (float)d->targetTranslation;
+			j->maxMotorForce = (float)d->maxMotorForce;
+		}
+		else
+			j->maxMotorTorque = (float)d->maxMotorTorque;
+	}
+	else if ( d->type == P_JOINT_MOTOR )
+	{
+		// joint.c:406-442
+		j->localOriginAnchorA = V( 0.0f, 0.0f );
+		j->localOriginAnchorB = V( 0.0f, 0.0f );
+		j->linearOffset = V( (float)d->linearOffsetX, (float)d->linearOffsetY );
+		j->angularOffset = (float)d->angularOffset;
+		j->maxForce = (float)d->maxForce;
+		j->maxTorque = (float)d->maxTorque;
+		j->correctionFactor = fclampp( (float)d->correctionFactor, 0.0f, 1.0f );
+	}
+	else if ( d->type == P_JOINT_MOUSE )
+	{
+		v2 target = V( (float)d->targetX, (float)d->targetY );
+		j->localOriginAnchorA = invXfPoint( xfA, target );
+		j->localOriginAnchorB = invXfPoint( xfB, target );
+		j->targetA = target;
+		j->hertz = (float)d->hertz;
+		j->dampingRatio = (float)d->dampingRatio;
+		j->maxForce = (float)d->maxForce;
+	}
+	else if ( d->type == P_JOINT_FILTER )
+	{
+		j->localOriginAnchorA = V( 0.0f, 0.0f );
+		j->localOriginAnchorB = V( 0.0f, 0.0f );
+	}
+	else if ( d->type == P_JOINT_WELD )
 	{
 		j->referenceAngle = (float)d->referenceAngle;
 		j->linearHertz = (float)d->linearHertz;
@@ -691,6 +742,15 @@ int orc_create_joint( int wi, const f2d_joint_def* d )
 	}
 	joint_finish( w, id );
 	return id;
+}
+
+// mouse_joint.c:14-19 b2MouseJoint_SetTarget (no wake)
+void orc_mouse_joint_set_target( int wi, int jid, double x, double y )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || jid < 0 || jid >= w->jointCount || w->joints[jid].type != P_JOINT_MOUSE )
+		return;
+	w->joints[jid].targetA = V( (float)x, (float)y );
 }
 
 // constraint_graph.c:271-288 b2CreateJointInGraph / b2AddJointToGraph

@@ -460,9 +460,91 @@ int ref_create_joint( int w, const f2d_joint_def* d )
 		def.collideConnected = d->collideConnected != 0;
 		id = b2CreateDistanceJoint( s_worlds[w], &def );
 	}
+	else if ( d->type == F2D_JOINT_PRISMATIC )
+	{
+		b2PrismaticJointDef def = b2DefaultPrismaticJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.localAnchorA = la;
+		def.localAnchorB = lb;
+		def.localAxisA = ( b2Vec2 ){ (float)d->localAxisAX, (float)d->localAxisAY };
+		def.referenceAngle = (float)d->referenceAngle;
+		def.targetTranslation = (float)d->targetTranslation;
+		def.enableSpring = d->enableSpring != 0;
+		def.hertz = (float)d->hertz;
+		def.dampingRatio = (float)d->dampingRatio;
+		def.enableLimit = d->enableLimit != 0;
+		def.lowerTranslation = (float)d->lowerTranslation;
+		def.upperTranslation = (float)d->upperTranslation;
+		def.enableMotor = d->enableMotor != 0;
+		def.maxMotorForce = (float)d->maxMotorForce;
+		def.motorSpeed = (float)d->motorSpeed;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreatePrismaticJoint( s_worlds[w], &def );
+	}
+	else if ( d->type == F2D_JOINT_WHEEL )
+	{
+		b2WheelJointDef def = b2DefaultWheelJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.localAnchorA = la;
+		def.localAnchorB = lb;
+		def.localAxisA = ( b2Vec2 ){ (float)d->localAxisAX, (float)d->localAxisAY };
+		def.enableSpring = d->enableSpring != 0;
+		def.hertz = (float)d->hertz;
+		def.dampingRatio = (float)d->dampingRatio;
+		def.enableLimit = d->enableLimit != 0;
+		def.lowerTranslation = (float)d->lowerTranslation;
+		def.upperTranslation = (float)d->upperTranslation;
+		def.enableMotor = d->enableMotor != 0;
+		def.maxMotorTorque = (float)d->maxMotorTorque;
+		def.motorSpeed = (float)d->motorSpeed;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreateWheelJoint( s_worlds[w], &def );
+	}
+	else if ( d->type == F2D_JOINT_MOTOR )
+	{
+		b2MotorJointDef def = b2DefaultMotorJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.linearOffset = ( b2Vec2 ){ (float)d->linearOffsetX, (float)d->linearOffsetY };
+		def.angularOffset = (float)d->angularOffset;
+		def.maxForce = (float)d->maxForce;
+		def.maxTorque = (float)d->maxTorque;
+		def.correctionFactor = (float)d->correctionFactor;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreateMotorJoint( s_worlds[w], &def );
+	}
+	else if ( d->type == F2D_JOINT_MOUSE )
+	{
+		b2MouseJointDef def = b2DefaultMouseJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		def.target = ( b2Vec2 ){ (float)d->targetX, (float)d->targetY };
+		def.hertz = (float)d->hertz;
+		def.dampingRatio = (float)d->dampingRatio;
+		def.maxForce = (float)d->maxForce;
+		def.collideConnected = d->collideConnected != 0;
+		id = b2CreateMouseJoint( s_worlds[w], &def );
+	}
+	else if ( d->type == F2D_JOINT_FILTER )
+	{
+		b2FilterJointDef def = b2DefaultFilterJointDef();
+		def.bodyIdA = ref_body_id( w, d->bodyA );
+		def.bodyIdB = ref_body_id( w, d->bodyB );
+		id = b2CreateFilterJoint( s_worlds[w], &def );
+	}
 	else
 		return -1;
 	return id.index1 - 1;
+}
+
+void ref_mouse_joint_set_target( int w, int j, double x, double y )
+{
+	b2World* world = ref_world( w );
+	b2Joint* joint = b2JointArray_Get( &world->joints, j );
+	b2JointId id = { j + 1, world->worldId, joint->generation };
+	b2MouseJoint_SetTarget( id, ( b2Vec2 ){ (float)x, (float)y } );
 }
 
 // ---------------------------------------------------------------------------

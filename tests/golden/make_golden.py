@@ -35,6 +35,10 @@ CASES = {
                    checkpoints=[1, 64, 256]),
     "joint_zoo": dict(world=dict(enableSleep=0), scene=("joint_zoo", dict()), frames=256,
                       checkpoints=[1, 64, 256]),
+    "joint_rigs": dict(world=dict(enableSleep=0), scene=("joint_rigs", dict()), frames=256,
+                       checkpoints=[1, 64, 256]),
+    "joint_rigs_sleep": dict(world=dict(enableSleep=1), scene=("joint_rigs", dict()), frames=300,
+                             checkpoints=[1, 100, 200, 300]),
     # sleeping on: islands, sleeping solver sets, island splits
     "pyramid_sleep": dict(world=dict(enableSleep=1), scene=("pyramid", dict(rows=12)), frames=120,
                           checkpoints=[1, 30, 44, 60, 120]),
@@ -158,8 +162,12 @@ def api_cases():
 
 
 if __name__ == "__main__":
+    only = sys.argv[1:]
     for name, spec in CASES.items():
-        record(name, spec)
+        if not only or name in only:
+            record(name, spec)
+    if only:
+        sys.exit(0)
     record_stats("pyramid", dict(enableSleep=0), "pyramid", dict(), 256)
     record_stats("pile", dict(enableSleep=0, enableContinuous=1), "pile",
                  dict(count=300, seed=11, width=30.0, height=40.0), 256)

@@ -25,6 +25,8 @@ CASES = {
     "chains": (dict(enableSleep=0), "pyramids_chains", dict(pyramids=2, rows=10, chains=6, links=20)),
     "joints": (dict(enableSleep=0), "joint_gallery", dict()),
     "joint_zoo": (dict(enableSleep=0), "joint_zoo", dict()),
+    "joint_rigs": (dict(enableSleep=0), "joint_rigs", dict()),
+    "joint_rigs_sleep": (dict(enableSleep=1), "joint_rigs", dict()),
     "pyramid_sleep": (dict(enableSleep=1), "pyramid", dict(rows=12)),
     "pile_sleep": (dict(enableSleep=1, enableContinuous=1), "pile", dict(count=300, seed=3, width=20.0, height=30.0)),
 }

@@ -42,6 +42,7 @@ SCENES = [
     ("chains", dict(enableSleep=0), "pyramids_chains", dict(pyramids=3, rows=8, chains=10, links=25), 300),
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400),
     ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=4), 400),
+    ("joint_rigs", dict(enableSleep=0), "joint_rigs", dict(copies=4), 400),
 ]
 
 
@@ -68,6 +69,7 @@ SLEEP_SCENES = [
      dict(count=300, seed=3, width=20.0, height=30.0), 450),
     ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
     ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
+    ("joint_rigs_sleep", dict(enableSleep=1), "joint_rigs", dict(copies=3), 400),
 ]
 
 
@@ -104,6 +106,26 @@ def test_port_sleep_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene,
     lockstep_full(ref, port, frames)
     if name in ("pyramid_sleep", "pile_sleep"):
         assert ref.awake_body_count() == 0
+    ref.close()
+    port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_mouse_target_moves_with_reference(ref_lib, port_lib, sleep):
+    """b2MouseJoint_SetTarget between steps: the held boxes follow the new
+    targets (no wake: a sleeping box stays asleep) bit for bit."""
+    wkw = dict(enableSleep=sleep)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    mr = scenes.build(ref, "joint_rigs", copies=3)
+    mp = scenes.build(port, "joint_rigs", copies=3)
+    assert mr == mp
+    lockstep_full(ref, port, 60)
+    for t, (dx, dy) in enumerate([(-1.5, 4.0), (2.0, 1.5), (0.5, 6.0)]):
+        for w in (ref, port):
+            for k, j in enumerate(mr):
+                w.mouse_set_target(j, -90.0 + 5.0 + 30.0 * k + 20.0 + dx, dy)
+        lockstep_full(ref, port, 80, start=61 + 80 * t)
     ref.close()
     port.close()
 
