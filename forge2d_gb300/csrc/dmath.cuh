@@ -293,6 +293,20 @@ HD fv2 solve22( fv2 cx, fv2 cy, fv2 b )
 }
 
 // math_functions.c:61-102 minimax atan2 (operand order kept)
+// math_functions.h:541-565 b2MulMV, b2GetInverse22 (matrix by columns cx, cy)
+HD fv2 mulMV( fv2 cx, fv2 cy, fv2 v )
+{
+	return mk( cx.x * v.x + cy.x * v.y, cx.y * v.x + cy.y * v.y );
+}
+HD float4 inverse22( fv2 cx, fv2 cy )
+{
+	float a = cx.x, b = cy.x, c = cx.y, d = cy.y;
+	float det = a * d - b * c;
+	if ( det != 0.0f )
+		det = 1.0f / det;
+	return make_float4( det * d, -det * c, -det * b, det * a );
+}
+
 HD float f2d_atan2( float y, float x )
 {
 	if ( x == 0.0f && y == 0.0f )

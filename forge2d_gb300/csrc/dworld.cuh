@@ -345,17 +345,21 @@ struct DWorld
 
 	// ---------------- joints (by joint id) ----------------
 	int2* jbody;
-	int* jflags; // used, enableSpring, enableLimit, enableMotor, collideConnected
+	int* jflags; // used, enableSpring, enableLimit, enableMotor, collideConnected; type in bits 8-11
 	int* jcolor;
 	int* jnext;	 // [2*id+edge] next joint key in the body list
+	// definition, impulse and prepared rows; the revolute layout is given,
+	// the other types' layouts sit beside their solvers
 	float4* jdef0; // localOriginAnchorA.xy localOriginAnchorB.xy
 	float4* jdef1; // referenceAngle targetAngle hertz dampingRatio
 	float4* jdef2; // lowerAngle upperAngle maxMotorTorque motorSpeed
+	float4* jdef3; // type-specific (prismatic spring hertz, damping ratio)
 	float4* jimp;  // linearImpulse.xy springImpulse motorImpulse
 	float2* jimp2; // lowerImpulse upperImpulse
 	float4* jprep0; // anchorA.xy anchorB.xy
 	float4* jprep1; // deltaCenter.xy deltaAngle axialMass
 	float4* jprep2; // springSoftness biasRate massScale impulseScale, pad
+	float4* jprep3; // type-specific (joint axis, 2x2 effective mass)
 	float4* jprepM; // invMassA invIA invMassB invIB
 	int2* jindex;	// solver body indices
 	int* overflowJoints;

@@ -1,6 +1,8 @@
 // Joint preparation and the per-colour joint slot lists of the solver.
-// Reference: packages/forge2d/third_party/box2d/src/joint.c:1346-1352
-// (softness clamp), revolute_joint.c:195-259 (b2PrepareRevoluteJoint).
+// Reference: packages/forge2d/third_party/box2d/src/joint.c:1346-1390
+// (softness clamp, type dispatch), revolute_joint.c:195-259,
+// weld_joint.c:83-140, distance_joint.c:158-205, prismatic_joint.c:279-346,
+// wheel_joint.c:183-262, motor_joint.c:99-160, mouse_joint.c:77-128.
 #include "joint.cuh"
 
 __global__ void k_prepare_joints( DWorld w, float h, float inv_h, Soft jointSoft )
@@ -49,6 +51,97 @@ __global__ void k_prepare_joints( DWorld w, float h, float inv_h, Soft jointSoft
 				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 			continue;
 		}
+		if ( type == JT_PRISMATIC || type == JT_WHEEL )
+		{
+			// prismatic_joint.c:316-346, wheel_joint.c:220-262
+			float4 d1 = w.jdef1[j];
+			fv2 axisA = rrot( qA, mk( d1.x, d1.y ) );
+			fv2 rA = anchorA, rB = anchorB;
+			fv2 d = vadd( deltaCenter, vsub( rB, rA ) );
+			float a1 = vcross( vadd( d, rA ), axisA );
+			float a2 = vcross( rB, axisA );
+			w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+			w.jprep2[w.jointCap + j] =
+				make_float4( jointSoft.biasRate, jointSoft.massScale, jointSoft.impulseScale, 0.0f );
+			if ( type == JT_PRISMATIC )
+			{
+				float deltaAngle = unwind_angle( relative_angle( qB, qA ) - d1.z );
+				float k = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+				float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+				float4 d3 = w.jdef3[j];
+				Soft sp = make_soft( d3.x, d3.y, h );
+				w.jprep1[j] = make_float4( deltaCenter.x, deltaCenter.y, deltaAngle, axialMass );
+				w.jprep2[j] = make_float4( sp.biasRate, sp.massScale, sp.impulseScale, 0.0f );
+				w.jprep3[j] = make_float4( axisA.x, axisA.y, 0.0f, 0.0f );
+			}
+			else
+			{
+				fv2 perpA = vleft( axisA );
+				float s1 = vcross( vadd( d, rA ), perpA );
+				float s2 = vcross( rB, perpA );
+				float kp = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+				float perpMass = kp > 0.0f ? 1.0f / kp : 0.0f;
+				float ka = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+				float axialMass = ka > 0.0f ? 1.0f / ka : 0.0f;
+				Soft sp = make_soft( d1.z, d1.w, h );
+				float km = iA + iB;
+				float motorMass = km > 0.0f ? 1.0f / km : 0.0f;
+				w.jprep1[j] = make_float4( deltaCenter.x, deltaCenter.y, perpMass, axialMass );
+				w.jprep2[j] = make_float4( sp.biasRate, sp.massScale, sp.impulseScale, 0.0f );
+				w.jprep3[j] = make_float4( axisA.x, axisA.y, motorMass, 0.0f );
+			}
+			if ( w.enableWarmStarting == 0 )
+			{
+				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+				w.jimp2[j] = make_float2( 0.0f, 0.0f );
+			}
+			continue;
+		}
+		if ( type == JT_MOTOR )
+		{
+			// motor_joint.c:138-160
+			float4 d1 = w.jdef1[j]; // linearOffset.xy angularOffset maxForce
+			fv2 dc = vsub( deltaCenter, mk( d1.x, d1.y ) );
+			float deltaAngle = relative_angle( qB, qA ) - d1.z;
+			fv2 rA = anchorA, rB = anchorB;
+			fv2 cx, cy;
+			cx.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+			cx.y = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+			cy.x = cx.y;
+			cy.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+			float ka = iA + iB;
+			float angularMass = ka > 0.0f ? 1.0f / ka : 0.0f;
+			w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+			w.jprep1[j] = make_float4( dc.x, dc.y, deltaAngle, angularMass );
+			w.jprep3[j] = inverse22( cx, cy );
+			if ( w.enableWarmStarting == 0 )
+				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			continue;
+		}
+		if ( type == JT_MOUSE )
+		{
+			// mouse_joint.c:77-128
+			float4 d1 = w.jdef1[j]; // target.xy hertz dampingRatio
+			Soft ls = make_soft( d1.z, d1.w, h );
+			Soft as = make_soft( 0.5f, 0.1f, h );
+			fv2 rB = anchorB;
+			fv2 cx, cy;
+			cx.x = mB + iB * rB.y * rB.y;
+			cx.y = -iB * rB.x * rB.y;
+			cy.x = cx.y;
+			cy.y = mB + iB * rB.x * rB.x;
+			fv2 dc = vsub( mk( cb.x, cb.y ), mk( d1.x, d1.y ) );
+			w.jprep0[j] = make_float4( anchorA.x, anchorA.y, anchorB.x, anchorB.y );
+			w.jprep1[j] = make_float4( dc.x, dc.y, 0.0f, 0.0f );
+			w.jprep2[j] = make_float4( ls.biasRate, ls.massScale, ls.impulseScale, 0.0f );
+			w.jprep2[w.jointCap + j] = make_float4( as.biasRate, as.massScale, as.impulseScale, 0.0f );
+			w.jprep3[j] = inverse22( cx, cy );
+			if ( w.enableWarmStarting == 0 )
+				w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+			continue;
+		}
+		if ( type == JT_FILTER )
+			continue;
 		if ( type == JT_DISTANCE )
 		{
 			// distance_joint.c:179-205

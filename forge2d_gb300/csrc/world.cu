@@ -90,7 +90,8 @@ struct HostWorld
 
 	std::vector<int2> jbody;
 	std::vector<int> jflags, jcolor, jnext;
-	std::vector<float4> jdef0, jdef1, jdef2;
+	std::vector<float4> jdef0, jdef1, jdef2, jdef3;
+	std::vector<int> jointDirty; // uploaded joints whose definition rows changed on the host
 	std::vector<uint16_t> jgen;
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
@@ -326,11 +327,13 @@ static void grow_joints( HostWorld* W, int cap )
 	dgrow( d.jdef0, o, cap );
 	dgrow( d.jdef1, o, cap );
 	dgrow( d.jdef2, o, cap );
+	dgrow( d.jdef3, o, cap );
 	dgrow( d.jimp, o, cap );
 	dgrow( d.jimp2, o, cap );
 	dgrow( d.jprep0, 0, cap );
 	dgrow( d.jprep1, 0, cap );
 	dgrow( d.jprep2, 0, 2 * (size_t)cap );
+	dgrow( d.jprep3, 0, cap );
 	dgrow( d.jprepM, 0, cap );
 	dgrow( d.jindex, 0, cap );
 	dgrow( d.overflowJoints, o, cap );
@@ -621,6 +624,7 @@ static void upload_joint_rows( HostWorld* W, int lo, int hi )
 	up( d.jdef0, W->jdef0, lo, hi, st );
 	up( d.jdef1, W->jdef1, lo, hi, st );
 	up( d.jdef2, W->jdef2, lo, hi, st );
+	up( d.jdef3, W->jdef3, lo, hi, st );
 }
 
 // bring one existing body's device-updated fields into the host mirror
@@ -692,6 +696,15 @@ static void flush_uploads( HostWorld* W )
 		upload_joint_rows( W, W->jointUploaded, W->jointCount );
 		W->jointUploaded = W->jointCount;
 	}
+	for ( int j : W->jointDirty )
+	{
+		DWorld& d = W->d;
+		up( d.jdef0, W->jdef0, j, j + 1, W->stream );
+		up( d.jdef1, W->jdef1, j, j + 1, W->stream );
+		up( d.jdef2, W->jdef2, j, j + 1, W->stream );
+		up( d.jdef3, W->jdef3, j, j + 1, W->stream );
+	}
+	W->jointDirty.clear();
 	if ( W->staticDirty )
 	{
 		if ( !W->staticShapes.empty() )
@@ -812,8 +825,8 @@ static void free_world( HostWorld* W )
 	F( nodeVisit ); F( sortHist ); F( pairKeys ); F( pairKeysAlt ); F( pairVal ); F( pairValAlt ); F( planIds );
 	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( opBodies ); F( opScan ); F( slotContact ); F( overflowList );
 	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
-	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 );
-	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
+	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 ); F( jdef3 );
+	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprep3 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F
@@ -1264,7 +1277,7 @@ extern "C" F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t wg )
 // Shared tail of the joint constructors (joint.c:146-330): slot, generation,
 // body joint lists, definition rows, then the graph / island log.
 static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0, float4 d1, float4 d2,
-								int32_t* index1, int32_t* wg )
+								int32_t* index1, int32_t* wg, float4 d3 = make_float4( 0.0f, 0.0f, 0.0f, 0.0f ) )
 {
 	int j = W->jointCount++;
 	uint16_t gen = (uint16_t)( ( j < (int)W->jgen.size() ? W->jgen[j] : 0 ) + 1 );
@@ -1287,6 +1300,7 @@ static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0
 	vset( W->jdef0, j, d0 );
 	vset( W->jdef1, j, d1 );
 	vset( W->jdef2, j, d2 );
+	vset( W->jdef3, j, d3 );
 	// joints between two static bodies never enter the graph
 	bool staticA = body_type( W->bflags[a] ) == 0, staticB = body_type( W->bflags[b] ) == 0;
 	if ( W->islOn )
@@ -1349,44 +1363,122 @@ extern "C" F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d
 		index1, wg );
 }
 
-// weld_joint.c b2CreateWeldJoint (joint.c:575-600), distance_joint.c
-// b2CreateDistanceJoint (joint.c:400-440): lengths clamped to the linear slop,
-// maxLength at least minLength.
+// b2Create{Weld,Distance,Prismatic,Wheel,Motor,Mouse,Filter}Joint
+// (joint.c:400-720): distance lengths clamped to the linear slop with
+// maxLength at least minLength; joint axes normalised; the motor joint's
+// anchors at the body origins and its correction factor clamped to [0, 1];
+// the mouse joint's anchors are the target in each body's frame at creation;
+// the filter joint never lets its bodies collide. Definition rows per type:
+//   weld       d1 referenceAngle linearHertz linearDampingRatio angularHertz
+//              d2 angularDampingRatio
+//   distance   d1 length minLength maxLength hertz
+//              d2 dampingRatio maxMotorForce motorSpeed
+//   prismatic  d1 localAxisA.xy referenceAngle targetTranslation
+//              d2 lowerTranslation upperTranslation maxMotorForce motorSpeed
+//              d3 hertz dampingRatio
+//   wheel      d1 localAxisA.xy hertz dampingRatio
+//              d2 lowerTranslation upperTranslation maxMotorTorque motorSpeed
+//   motor      d1 linearOffset.xy angularOffset maxForce
+//              d2 maxTorque correctionFactor
+//   mouse      d1 target.xy hertz dampingRatio
+//              d2 maxForce
 extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_def* def, int32_t* index1, int32_t* wg )
 {
 	if ( index1 )
 		*index1 = 0;
 	if ( wg )
 		*wg = 0;
-	if ( def == nullptr || ( def->type != F2D_JOINT_WELD && def->type != F2D_JOINT_DISTANCE ) )
+	if ( def == nullptr || def->type < F2D_JOINT_WELD || def->type > F2D_JOINT_FILTER )
 		return 0;
 	int a, b;
 	HostWorld* W = joint_bodies( worldId, def->bodyAIndex1, def->bodyAWorldAndGeneration, def->bodyBIndex1,
 								 def->bodyBWorldAndGeneration, &a, &b );
 	if ( W == nullptr )
 		return 0;
-	int flags = JF_USED | ( def->type << JF_TYPE_SHIFT );
-	if ( def->collideConnected )
+	int type = def->type;
+	int flags = JF_USED | ( type << JF_TYPE_SHIFT );
+	if ( def->collideConnected && type != F2D_JOINT_FILTER )
 		flags |= JF_COLLIDE;
+	if ( type == F2D_JOINT_DISTANCE || type == F2D_JOINT_PRISMATIC || type == F2D_JOINT_WHEEL )
+	{
+		if ( def->enableSpring )
+			flags |= JF_SPRING;
+		if ( def->enableLimit )
+			flags |= JF_LIMIT;
+		if ( def->enableMotor )
+			flags |= JF_MOTOR;
+	}
+	const float4 zero = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 	float4 d0 = make_float4( (float)def->localAnchorAX, (float)def->localAnchorAY, (float)def->localAnchorBX,
 							 (float)def->localAnchorBY );
-	if ( def->type == F2D_JOINT_WELD )
-		return create_joint_common( W, a, b, flags, d0,
-									make_float4( (float)def->referenceAngle, (float)def->linearHertz,
-												 (float)def->linearDampingRatio, (float)def->angularHertz ),
-									make_float4( (float)def->angularDampingRatio, 0.0f, 0.0f, 0.0f ), index1, wg );
-	if ( def->enableSpring )
-		flags |= JF_SPRING;
-	if ( def->enableLimit )
-		flags |= JF_LIMIT;
-	if ( def->enableMotor )
-		flags |= JF_MOTOR;
-	float minLength = fmax_s( (float)def->minLength, F2D_LINEAR_SLOP );
-	return create_joint_common(
-		W, a, b, flags, d0,
-		make_float4( fmax_s( (float)def->length, F2D_LINEAR_SLOP ), minLength,
-					 fmax_s( (float)def->minLength, (float)def->maxLength ), (float)def->hertz ),
-		make_float4( (float)def->dampingRatio, (float)def->maxMotorForce, (float)def->motorSpeed, 0.0f ), index1, wg );
+	float4 d1 = zero, d2 = zero, d3 = zero;
+	fv2 axis = vnormalize( mk( (float)def->localAxisAX, (float)def->localAxisAY ) );
+	switch ( type )
+	{
+		case F2D_JOINT_WELD:
+			d1 = make_float4( (float)def->referenceAngle, (float)def->linearHertz, (float)def->linearDampingRatio,
+							  (float)def->angularHertz );
+			d2 = make_float4( (float)def->angularDampingRatio, 0.0f, 0.0f, 0.0f );
+			break;
+		case F2D_JOINT_DISTANCE:
+			d1 = make_float4( fmax_s( (float)def->length, F2D_LINEAR_SLOP ),
+							  fmax_s( (float)def->minLength, F2D_LINEAR_SLOP ),
+							  fmax_s( (float)def->minLength, (float)def->maxLength ), (float)def->hertz );
+			d2 = make_float4( (float)def->dampingRatio, (float)def->maxMotorForce, (float)def->motorSpeed, 0.0f );
+			break;
+		case F2D_JOINT_PRISMATIC:
+			d1 = make_float4( axis.x, axis.y, (float)def->referenceAngle, (float)def->targetTranslation );
+			d2 = make_float4( (float)def->lowerTranslation, (float)def->upperTranslation, (float)def->maxMotorForce,
+							  (float)def->motorSpeed );
+			d3 = make_float4( (float)def->hertz, (float)def->dampingRatio, 0.0f, 0.0f );
+			break;
+		case F2D_JOINT_WHEEL:
+			d1 = make_float4( axis.x, axis.y, (float)def->hertz, (float)def->dampingRatio );
+			d2 = make_float4( (float)def->lowerTranslation, (float)def->upperTranslation, (float)def->maxMotorTorque,
+							  (float)def->motorSpeed );
+			break;
+		case F2D_JOINT_MOTOR:
+			d0 = zero;
+			d1 = make_float4( (float)def->linearOffsetX, (float)def->linearOffsetY, (float)def->angularOffset,
+							  (float)def->maxForce );
+			d2 = make_float4( (float)def->maxTorque, fclamp_s( (float)def->correctionFactor, 0.0f, 1.0f ), 0.0f, 0.0f );
+			break;
+		case F2D_JOINT_MOUSE:
+		{
+			pull_body( W, a );
+			pull_body( W, b );
+			float tx = (float)def->targetX, ty = (float)def->targetY;
+			float4 xa = W->xf[a], xb = W->xf[b];
+			float ax = tx - xa.x, ay = ty - xa.y;
+			float bx = tx - xb.x, by = ty - xb.y;
+			d0 = make_float4( xa.z * ax + xa.w * ay, -xa.w * ax + xa.z * ay, xb.z * bx + xb.w * by,
+							  -xb.w * bx + xb.z * by );
+			d1 = make_float4( tx, ty, (float)def->hertz, (float)def->dampingRatio );
+			d2 = make_float4( (float)def->maxForce, 0.0f, 0.0f, 0.0f );
+			break;
+		}
+		default: // filter
+			d0 = zero;
+			break;
+	}
+	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
+}
+
+// b2MouseJoint_SetTarget (mouse_joint.c:14-19): no wake
+extern "C" F2D_API void f2d_mouse_joint_set_target( int32_t index1, int32_t wg, double x, double y )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return;
+	int j = index1 - 1;
+	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) ||
+		 ( ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf ) != F2D_JOINT_MOUSE )
+		return;
+	W->jdef1[j].x = (float)x;
+	W->jdef1[j].y = (float)y;
+	if ( j < W->jointUploaded &&
+		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
+		W->jointDirty.push_back( j );
 }
 
 extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )

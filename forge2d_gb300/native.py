@@ -74,7 +74,8 @@ class RevoluteDef(C.Structure):
 
 
 class JointDef(C.Structure):
-    """f2d_joint_def: weld (type 2) and distance (type 3) joints."""
+    """f2d_joint_def: weld 2, distance 3, prismatic 4, wheel 5, motor 6,
+    mouse 7 and filter 8 joints."""
     _fields_ = [
         ("type", C.c_int32),
         ("bodyAIndex1", C.c_int32), ("bodyAWorldAndGeneration", C.c_int32),
@@ -89,6 +90,12 @@ class JointDef(C.Structure):
         ("hertz", C.c_double), ("dampingRatio", C.c_double),
         ("maxMotorForce", C.c_double), ("motorSpeed", C.c_double),
         ("enableSpring", C.c_int32), ("enableLimit", C.c_int32), ("enableMotor", C.c_int32), ("pad0", C.c_int32),
+        ("localAxisAX", C.c_double), ("localAxisAY", C.c_double),
+        ("targetTranslation", C.c_double), ("lowerTranslation", C.c_double), ("upperTranslation", C.c_double),
+        ("maxMotorTorque", C.c_double),
+        ("linearOffsetX", C.c_double), ("linearOffsetY", C.c_double), ("angularOffset", C.c_double),
+        ("maxForce", C.c_double), ("maxTorque", C.c_double), ("correctionFactor", C.c_double),
+        ("targetX", C.c_double), ("targetY", C.c_double),
     ]
 
 
@@ -141,6 +148,7 @@ _SIGS = [
     ("f2d_shape_get_type", _i, [_i, _i]),
     ("f2d_create_revolute_joint", _i, [_i, _P(RevoluteDef), _P(_i), _P(_i)]),
     ("f2d_create_joint", _i, [_i, _P(JointDef), _P(_i), _P(_i)]),
+    ("f2d_mouse_joint_set_target", None, [_i, _i, _d, _d]),
     ("f2d_joint_is_valid", _i, [_i, _i]),
     ("f2d_world_get_event_counts", None, [_i, _P(_i)]),
     ("f2d_world_get_begin_events", _i, [_i, _P(_i), _i]),

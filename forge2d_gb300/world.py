@@ -16,8 +16,8 @@ import ctypes as C
 import numpy as np
 
 from . import native
-from .scenes import (BODY_DEFAULTS, JOINT_DEFAULTS, JOINT_DISTANCE, JOINT_WELD, REVOLUTE_DEFAULTS,
-                     SHAPE_DEFAULTS, WORLD_DEFAULTS)
+from .scenes import (BODY_DEFAULTS, JOINT_DEFAULTS, JOINT_DISTANCE, JOINT_FILTER, JOINT_MOTOR, JOINT_MOUSE,
+                     JOINT_PRISMATIC, JOINT_WELD, JOINT_WHEEL, REVOLUTE_DEFAULTS, SHAPE_DEFAULTS, WORLD_DEFAULTS)
 
 BODY_STRIDE = 12
 CONTACT_INTS = 9
@@ -157,6 +157,9 @@ class GpuWorld:
         i1, wg = C.c_int32(0), C.c_int32(0)
         ok = self.lib.f2d_create_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
+
+    def mouse_set_target(self, joint, x, y):
+        self.lib.f2d_mouse_joint_set_target(joint[0], joint[1], x, y)
 
     def autotune(self, dt=1.0 / 60.0, substeps=4, steps_per_candidate=3):
         """Steps through the launch configurations and keeps the fastest;
@@ -512,6 +515,10 @@ class Joint:
     def is_valid(self):
         return bool(self.world.lib.f2d_joint_is_valid(*self.id))
 
+    def set_target(self, x, y):
+        """MouseJoint.setTarget: takes effect at the next step."""
+        self.world.lib.f2d_mouse_joint_set_target(self.id[0], self.id[1], x, y)
+
 
 class World:
     """forge2d ``World``: step, createBody, createRevoluteJoint, events, queries."""
@@ -547,6 +554,26 @@ class World:
 
     def create_distance_joint(self, body_a, body_b, **jd):
         jd = dict(jd, type=JOINT_DISTANCE, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_prismatic_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_PRISMATIC, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_wheel_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_WHEEL, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_motor_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_MOTOR, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_mouse_joint(self, body_a, body_b, **jd):
+        jd = dict(jd, type=JOINT_MOUSE, bodyA=body_a.id, bodyB=body_b.id)
+        return Joint(self, self._w.create_joint(jd))
+
+    def create_filter_joint(self, body_a, body_b):
+        jd = dict(type=JOINT_FILTER, bodyA=body_a.id, bodyB=body_b.id)
         return Joint(self, self._w.create_joint(jd))
 
     @property

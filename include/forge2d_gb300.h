@@ -122,11 +122,17 @@ typedef struct f2d_revolute_def
 	int32_t pad3;
 } f2d_revolute_def;
 
-/* Mirrors RawBox2D.createWeldJoint / createDistanceJoint (raw_box2d.dart:
- * 582-600, 679-692 -> b2CreateWeldJoint / b2CreateDistanceJoint): one
- * definition for both types; fields the type does not use are ignored. */
+/* Mirrors RawBox2D.create{Distance,Filter,Motor,Mouse,Prismatic,Weld,Wheel}
+ * Joint (raw_box2d.dart:582-712 -> b2Create*Joint, joint.c:400-720): one
+ * definition for every type; fields the type does not use are ignored. The
+ * bodies are (index1, worldAndGeneration) id pairs. */
 #define F2D_JOINT_WELD 2
 #define F2D_JOINT_DISTANCE 3
+#define F2D_JOINT_PRISMATIC 4
+#define F2D_JOINT_WHEEL 5
+#define F2D_JOINT_MOTOR 6
+#define F2D_JOINT_MOUSE 7
+#define F2D_JOINT_FILTER 8
 typedef struct f2d_joint_def
 {
 	int32_t type;
@@ -144,6 +150,15 @@ typedef struct f2d_joint_def
 	double hertz, dampingRatio;
 	double maxMotorForce, motorSpeed;
 	int32_t enableSpring, enableLimit, enableMotor, pad0;
+	/* prismatic and wheel */
+	double localAxisAX, localAxisAY;
+	double targetTranslation, lowerTranslation, upperTranslation;
+	double maxMotorTorque;
+	/* motor (maxForce also the mouse joint's) */
+	double linearOffsetX, linearOffsetY, angularOffset;
+	double maxForce, maxTorque, correctionFactor;
+	/* mouse */
+	double targetX, targetY;
 } f2d_joint_def;
 
 #define F2D_STATUS_OK 0
@@ -280,9 +295,13 @@ F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t worldAndGeneration )
 /* ---- joints ------------------------------------------------------------- */
 
 /* RawBox2D.createRevoluteJoint (world.dart:297-321 -> b2CreateRevoluteJoint, joint.c:507). */
-/* RawBox2D.createWeldJoint / createDistanceJoint (raw_box2d.dart:582, 679). */
+/* RawBox2D.create{Distance,Filter,Motor,Mouse,Prismatic,Weld,Wheel}Joint
+ * (raw_box2d.dart:582-712). */
 F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_def* def, int32_t* index1,
 								  int32_t* worldAndGeneration );
+/* RawBox2D.mouseJointSetTarget (raw_box2d.dart:913 -> b2MouseJoint_SetTarget,
+ * mouse_joint.c:14): takes effect at the next step; wakes nothing. */
+F2D_API void f2d_mouse_joint_set_target( int32_t index1, int32_t worldAndGeneration, double x, double y );
 F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
 										   int32_t* worldAndGeneration );
 F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );

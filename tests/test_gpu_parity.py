@@ -57,6 +57,8 @@ NATIVE = [
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400, 25),
     # weld cantilevers (stiff and soft), distance rods, springs with limits, motors
     ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=8), 400, 25),
+    # prismatic lifts and springs, wheeled carts, motor, mouse and filter joints
+    ("joint_rigs", dict(enableSleep=0), "joint_rigs", dict(copies=8), 400, 25),
     ("batched24", dict(enableSleep=0, enableContinuous=1), "batched", dict(worlds=24, seed=3), 200, 25),
     # overflow constraints solved by levels: a 150-deep chain (past the
     # parallel levels, into the serial tail), overflow joints, and many

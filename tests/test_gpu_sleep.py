@@ -55,7 +55,33 @@ SCENES = [
     ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
     # weld and distance joints link islands and sleep with them
     ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
+    ("joint_rigs_sleep", dict(enableSleep=1), "joint_rigs", dict(copies=3), 400),
 ]
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_mouse_target_moves(gpu_lib, port_lib, sleep):
+    """MouseJoint.setTarget between steps (uploaded with the next step; no
+    wake): the held boxes follow the new targets as in the oracle."""
+    wkw = dict(enableSleep=sleep)
+    g = gpu_world(wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    mg = scenes.build(g, "joint_rigs", copies=3)
+    mp = scenes.build(p, "joint_rigs", copies=3)
+    f = 0
+    for t, (dx, dy) in enumerate([(0.0, 0.0), (-1.5, 4.0), (2.0, 1.5), (0.5, 6.0)]):
+        if t:
+            for k in range(3):
+                x = -90.0 + 5.0 + 30.0 * k + 20.0 + dx
+                g.mouse_set_target(mg[k], x, dy)
+                p.mouse_set_target(mp[k], x, dy)
+        for _ in range(80):
+            f += 1
+            step_both(g, p, f)
+        compare_state(g, p, f)
+    assert g.sync() == 0
+    g.close()
+    p.close()
 
 
 @pytest.mark.parametrize("solver", ["auto", "grid"])
