@@ -321,19 +321,20 @@ __device__ __forceinline__ bool bodies_collide( const DWorld& w, int ia, int ib 
 
 __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 {
-	// contact.c:151-175 registry: (first, second) has a manifold function
+	// contact.c:151-184 registry: (first, second) has a manifold function
 	// circle-circle, capsule-circle, capsule-capsule, polygon-circle,
 	// polygon-capsule, polygon-polygon, segment-circle, segment-capsule,
-	// segment-polygon
-	const unsigned reg = ( 1u << ( 0 * 4 + 0 ) ) | ( 1u << ( 1 * 4 + 0 ) ) | ( 1u << ( 1 * 4 + 1 ) ) |
-						 ( 1u << ( 3 * 4 + 0 ) ) | ( 1u << ( 3 * 4 + 1 ) ) | ( 1u << ( 3 * 4 + 3 ) ) |
-						 ( 1u << ( 2 * 4 + 0 ) ) | ( 1u << ( 2 * 4 + 1 ) ) | ( 1u << ( 2 * 4 + 3 ) );
-	if ( reg & ( 1u << ( ta * 4 + tb ) ) )
+	// segment-polygon, chain-circle, chain-capsule, chain-polygon
+	const unsigned reg = ( 1u << ( 0 * 5 + 0 ) ) | ( 1u << ( 1 * 5 + 0 ) ) | ( 1u << ( 1 * 5 + 1 ) ) |
+						 ( 1u << ( 3 * 5 + 0 ) ) | ( 1u << ( 3 * 5 + 1 ) ) | ( 1u << ( 3 * 5 + 3 ) ) |
+						 ( 1u << ( 2 * 5 + 0 ) ) | ( 1u << ( 2 * 5 + 1 ) ) | ( 1u << ( 2 * 5 + 3 ) ) |
+						 ( 1u << ( 4 * 5 + 0 ) ) | ( 1u << ( 4 * 5 + 1 ) ) | ( 1u << ( 4 * 5 + 3 ) );
+	if ( reg & ( 1u << ( ta * 5 + tb ) ) )
 	{
 		*primary = true;
 		return true;
 	}
-	if ( reg & ( 1u << ( tb * 4 + ta ) ) )
+	if ( reg & ( 1u << ( tb * 5 + ta ) ) )
 	{
 		*primary = false;
 		return true;
@@ -520,6 +521,7 @@ __global__ void k_create_contacts( DWorld w, int planMode )
 		w.cmat[id] = make_float4( sqrtf( ma.x * mb.x ), ma.y > mb.y ? ma.y : mb.y, 0.0f, 0.0f );
 		w.cmass[id] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
 		w.mnorm[id] = make_float4( 0.0f, 0.0f, 0.0f, __int_as_float( 0 ) );
+		w.csimplex[id] = make_int2( 0, 0 );
 		for ( int k = 0; k < 2; ++k )
 		{
 			w.mpA[2 * id + k] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );

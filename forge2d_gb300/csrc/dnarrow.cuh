@@ -6,6 +6,7 @@
 #pragma once
 
 #include "dmath.cuh"
+#include "dtoi.cuh"
 #include "dworld.cuh"
 
 #define MAKE_ID( A, B ) ( (unsigned)( ( ( (unsigned)(A)&0xffu ) << 8 ) | ( (unsigned)(B)&0xffu ) ) )
@@ -24,6 +25,7 @@ struct DGeom
 	fv2 c1, c2;
 	float radius;
 	DPoly poly;
+	fv2 g1, g2; // chain segment ghost vertices
 };
 
 struct DPoint
@@ -71,6 +73,12 @@ __device__ __forceinline__ DGeom load_geom( const float4* __restrict__ g, int ty
 	o.radius = g1.x;
 	o.poly.radius = g1.x;
 	o.poly.count = __float_as_int( g1.y );
+	if ( type == ST_CHAIN )
+	{
+		float4 gh = g[2];
+		o.g1 = mk( gh.x, gh.y );
+		o.g2 = mk( gh.z, gh.w );
+	}
 	if ( type == 3 )
 	{
 #pragma unroll
@@ -688,8 +696,408 @@ static __device__ __noinline__ DManifold collide_polygons( const DPoly& polygonA
 	return m;
 }
 
-// contact.c:60-124 dispatch; A already carries the registered first type
-__device__ __forceinline__ DManifold compute_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB )
+// manifold.c:1089-1168 b2CollideChainSegmentAndCircle: one-sided, with the
+// ghost vertices' Voronoi regions
+__device__ __forceinline__ DManifold collide_chain_circle( const DGeom& a, fxf xfA, fv2 cB, float radius, fxf xfB )
+{
+	DManifold m = dm_empty();
+	fxf xf = xinvmul( xfA, xfB );
+	fv2 pB = xpoint( xf, cB );
+	fv2 p1 = a.c1, p2 = a.c2;
+	fv2 e = vsub( p2, p1 );
+	float offset = vdot( vright( e ), vsub( pB, p1 ) );
+	if ( offset < 0.0f )
+		return m;
+	float u = vdot( e, vsub( p2, pB ) );
+	float v = vdot( e, vsub( pB, p1 ) );
+	fv2 pA;
+	if ( v <= 0.0f )
+	{
+		fv2 prevEdge = vsub( p1, a.g1 );
+		float uPrev = vdot( prevEdge, vsub( pB, p1 ) );
+		if ( uPrev <= 0.0f )
+			return m;
+		pA = p1;
+	}
+	else if ( u <= 0.0f )
+	{
+		fv2 nextEdge = vsub( a.g2, p2 );
+		float vNext = vdot( nextEdge, vsub( pB, p2 ) );
+		if ( vNext > 0.0f )
+			return m;
+		pA = p2;
+	}
+	else
+	{
+		float ee = vdot( e, e );
+		pA = mk( u * p1.x + v * p2.x, u * p1.y + v * p2.y );
+		pA = ee > 0.0f ? vscale( 1.0f / ee, pA ) : p1;
+	}
+	float distance;
+	fv2 normal = vlen_norm( &distance, vsub( pB, pA ) );
+	float separation = distance - radius;
+	if ( separation > F2D_SPECULATIVE )
+		return m;
+	fv2 cA = pA;
+	fv2 cb = vmuladd( pB, -radius, normal );
+	fv2 cp = vlerp( cA, cb, 0.5f );
+	m.normal = rrot( xfA.q, normal );
+	one_point( m, xfA, xfB, cp, separation, 0 );
+	return m;
+}
+
+// manifold.c:1177-1254 b2ClipSegments (frame of the segment, unrotated)
+__device__ __forceinline__ DManifold clip_segments( fv2 a1, fv2 a2, fv2 b1, fv2 b2, fv2 normal, float ra, float rb,
+													unsigned id1, unsigned id2 )
+{
+	DManifold m = dm_empty();
+	fv2 tangent = vleft( normal );
+	float lower1 = 0.0f;
+	float upper1 = vdot( vsub( a2, a1 ), tangent );
+	float upper2 = vdot( vsub( b1, a1 ), tangent );
+	float lower2 = vdot( vsub( b2, a1 ), tangent );
+	if ( upper2 < lower1 || upper1 < lower2 )
+		return m;
+	fv2 vLower;
+	if ( lower2 < lower1 && upper2 - lower2 > FLT_EPSILON )
+		vLower = vlerp( b2, b1, ( lower1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vLower = b2;
+	fv2 vUpper;
+	if ( upper2 > upper1 && upper2 - lower2 > FLT_EPSILON )
+		vUpper = vlerp( b2, b1, ( upper1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vUpper = b1;
+	float separationLower = vdot( vsub( vLower, a1 ), normal );
+	float separationUpper = vdot( vsub( vUpper, a1 ), normal );
+	vLower = vmuladd( vLower, 0.5f * ( ra - rb - separationLower ), normal );
+	vUpper = vmuladd( vUpper, 0.5f * ( ra - rb - separationUpper ), normal );
+	float radius = ra + rb;
+	m.normal = normal;
+	m.p[0].anchorA = vLower;
+	m.p[0].separation = separationLower - radius;
+	m.p[0].id = id1;
+	m.p[1].anchorA = vUpper;
+	m.p[1].separation = separationUpper - radius;
+	m.p[1].id = id2;
+	m.count = 2;
+	return m;
+}
+
+#define NORMAL_SKIP 0
+#define NORMAL_ADMIT 1
+#define NORMAL_SNAP 2
+
+struct DChainParams
+{
+	fv2 edge1, normal0, normal2;
+	bool convex1, convex2;
+};
+
+// manifold.c:1270-1316 b2ClassifyNormal
+__device__ __forceinline__ int classify_normal( const DChainParams& p, fv2 normal )
+{
+	const float sinTol = 0.01f;
+	if ( vdot( normal, p.edge1 ) <= 0.0f )
+	{
+		if ( p.convex1 )
+			return vcross( normal, p.normal0 ) > sinTol ? NORMAL_SKIP : NORMAL_ADMIT;
+		return NORMAL_SNAP;
+	}
+	if ( p.convex2 )
+		return vcross( p.normal2, normal ) > sinTol ? NORMAL_SKIP : NORMAL_ADMIT;
+	return NORMAL_SNAP;
+}
+
+__device__ __forceinline__ void finish_clip( DManifold& m, fxf xfA, fxf xfB, fv2 normalLocal )
+{
+	if ( m.count != 2 )
+		return;
+	m.normal = rrot( xfA.q, normalLocal );
+	m.p[0].anchorA = rrot( xfA.q, m.p[0].anchorA );
+	m.p[1].anchorA = rrot( xfA.q, m.p[1].anchorA );
+	fv2 pAB = vsub( xfA.p, xfB.p );
+	m.p[0].anchorB = vadd( m.p[0].anchorA, pAB );
+	m.p[1].anchorB = vadd( m.p[1].anchorA, pAB );
+	m.p[0].point = vadd( xfA.p, m.p[0].anchorA );
+	m.p[1].point = vadd( xfA.p, m.p[1].anchorA );
+}
+
+// manifold.c:1318-1726 b2CollideChainSegmentAndPolygon: GJK warm-started from
+// the contact's simplex cache selects vertex-vertex, vertex-edge or the SAT
+// over the segment normal, its convex neighbours and the admitted polygon
+// normals; the Gauss map of the chain vertices skips or snaps ghost normals
+static __device__ DManifold collide_chain_polygon( const DGeom& a, fxf xfA, const DPoly& polygonB, fv2 polygonCentroid,
+										   fxf xfB, DCache& cache )
+{
+	DManifold m = dm_empty();
+	fxf xf = xinvmul( xfA, xfB );
+	fv2 centroidB = xpoint( xf, polygonCentroid );
+	float radiusB = polygonB.radius;
+	fv2 p1 = a.c1, p2 = a.c2;
+	fv2 edge1 = vnormalize( vsub( p2, p1 ) );
+	DChainParams sp;
+	sp.edge1 = edge1;
+	const float convexTol = 0.01f;
+	fv2 edge0 = vnormalize( vsub( p1, a.g1 ) );
+	sp.normal0 = vright( edge0 );
+	sp.convex1 = vcross( edge0, edge1 ) >= convexTol;
+	fv2 edge2 = vnormalize( vsub( a.g2, p2 ) );
+	sp.normal2 = vright( edge2 );
+	sp.convex2 = vcross( edge1, edge2 ) >= convexTol;
+	fv2 normal1 = vright( edge1 );
+	bool behind1 = vdot( normal1, vsub( centroidB, p1 ) ) < 0.0f;
+	bool behind0 = true, behind2 = true;
+	if ( sp.convex1 )
+		behind0 = vdot( sp.normal0, vsub( centroidB, p1 ) ) < 0.0f;
+	if ( sp.convex2 )
+		behind2 = vdot( sp.normal2, vsub( centroidB, p2 ) ) < 0.0f;
+	if ( behind1 && behind0 && behind2 )
+		return m;
+	int count = polygonB.count;
+	fv2 vertices[F2D_MAX_POLY];
+	fv2 normals[F2D_MAX_POLY];
+	for ( int i = 0; i < count; ++i )
+	{
+		vertices[i] = xpoint( xf, polygonB.v[i] );
+		normals[i] = rrot( xf.q, polygonB.n[i] );
+	}
+	DProxy proxyA, proxyB;
+	proxyA.p[0] = p1;
+	proxyA.p[1] = p2;
+	proxyA.count = 2;
+	proxyA.radius = 0.0f;
+	for ( int i = 0; i < count; ++i )
+		proxyB.p[i] = vertices[i];
+	proxyB.count = count;
+	proxyB.radius = 0.0f;
+	fxf identity;
+	identity.p = mk( 0.0f, 0.0f );
+	identity.q.c = 1.0f;
+	identity.q.s = 0.0f;
+	fv2 pointA = mk( 0.0f, 0.0f ), pointB = mk( 0.0f, 0.0f );
+	float distance = gjk_distance( proxyA, proxyB, identity, identity, cache, &pointA, &pointB );
+	if ( distance > radiusB + F2D_SPECULATIVE )
+		return m;
+	fv2 n0 = sp.convex1 ? sp.normal0 : normal1;
+	fv2 n2 = sp.convex2 ? sp.normal2 : normal1;
+	int incidentIndex = -1;
+	int incidentNormal = -1;
+	if ( behind1 == false && distance > 0.1f * F2D_LINEAR_SLOP )
+	{
+		if ( cache.count == 1 )
+		{
+			fv2 normal = vnormalize( vsub( pointB, pointA ) );
+			int type = classify_normal( sp, normal );
+			if ( type == NORMAL_SKIP )
+				return m;
+			if ( type == NORMAL_ADMIT )
+			{
+				m.normal = rrot( xfA.q, normal );
+				m.p[0].anchorA = rrot( xfA.q, pointA );
+				m.p[0].anchorB = vadd( m.p[0].anchorA, vsub( xfA.p, xfB.p ) );
+				m.p[0].point = vadd( xfA.p, m.p[0].anchorA );
+				m.p[0].separation = distance - radiusB;
+				m.p[0].id = MAKE_ID( cache.indexA[0], cache.indexB[0] );
+				m.count = 1;
+				return m;
+			}
+			incidentIndex = cache.indexB[0];
+		}
+		else
+		{
+			int ia1 = cache.indexA[0];
+			int ia2 = cache.indexA[1];
+			int ib1 = cache.indexB[0];
+			int ib2 = cache.indexB[1];
+			if ( ia1 == ia2 )
+			{
+				fv2 normalB = vsub( pointA, pointB );
+				float dot1 = vdot( normalB, normals[ib1] );
+				float dot2 = vdot( normalB, normals[ib2] );
+				int ib = dot1 > dot2 ? ib1 : ib2;
+				normalB = normals[ib];
+				int type = classify_normal( sp, vneg( normalB ) );
+				if ( type == NORMAL_SKIP )
+					return m;
+				if ( type == NORMAL_ADMIT )
+				{
+					ib1 = ib;
+					ib2 = ib < count - 1 ? ib + 1 : 0;
+					fv2 b1 = vertices[ib1];
+					fv2 b2 = vertices[ib2];
+					dot1 = vdot( normalB, vsub( p1, b1 ) );
+					dot2 = vdot( normalB, vsub( p2, b1 ) );
+					if ( dot1 < dot2 )
+					{
+						if ( vdot( n0, normalB ) < vdot( normal1, normalB ) )
+							return m;
+					}
+					else
+					{
+						if ( vdot( n2, normalB ) < vdot( normal1, normalB ) )
+							return m;
+					}
+					m = clip_segments( b1, b2, p1, p2, normalB, radiusB, 0.0f, MAKE_ID( ib1, 1 ), MAKE_ID( ib2, 0 ) );
+					finish_clip( m, xfA, xfB, vneg( normalB ) );
+					return m;
+				}
+				incidentNormal = ib;
+			}
+			else
+			{
+				float dot1 = vdot( normal1, vsub( vertices[ib1], p1 ) );
+				float dot2 = vdot( normal1, vsub( vertices[ib2], p2 ) );
+				incidentIndex = dot1 < dot2 ? ib1 : ib2;
+			}
+		}
+	}
+	else
+	{
+		float edgeSeparation = FLT_MAX;
+		for ( int i = 0; i < count; ++i )
+		{
+			float s = vdot( normal1, vsub( vertices[i], p1 ) );
+			if ( s < edgeSeparation )
+			{
+				edgeSeparation = s;
+				incidentIndex = i;
+			}
+		}
+		if ( sp.convex1 )
+		{
+			float s0 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = vdot( sp.normal0, vsub( vertices[i], p1 ) );
+				if ( s < s0 )
+					s0 = s;
+			}
+			if ( s0 > edgeSeparation )
+			{
+				edgeSeparation = s0;
+				incidentIndex = -1;
+			}
+		}
+		if ( sp.convex2 )
+		{
+			float s2 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = vdot( sp.normal2, vsub( vertices[i], p2 ) );
+				if ( s < s2 )
+					s2 = s;
+			}
+			if ( s2 > edgeSeparation )
+			{
+				edgeSeparation = s2;
+				incidentIndex = -1;
+			}
+		}
+		float polygonSeparation = -FLT_MAX;
+		int referenceIndex = -1;
+		for ( int i = 0; i < count; ++i )
+		{
+			fv2 n = normals[i];
+			if ( classify_normal( sp, vneg( n ) ) != NORMAL_ADMIT )
+				continue;
+			fv2 p = vertices[i];
+			float s = fmin_s( vdot( n, vsub( p2, p ) ), vdot( n, vsub( p1, p ) ) );
+			if ( s > polygonSeparation )
+			{
+				polygonSeparation = s;
+				referenceIndex = i;
+			}
+		}
+		if ( polygonSeparation > edgeSeparation )
+		{
+			int ia1 = referenceIndex;
+			int ia2 = ia1 < count - 1 ? ia1 + 1 : 0;
+			fv2 a1 = vertices[ia1];
+			fv2 a2 = vertices[ia2];
+			fv2 n = normals[ia1];
+			float dot1 = vdot( n, vsub( p1, a1 ) );
+			float dot2 = vdot( n, vsub( p2, a1 ) );
+			if ( dot1 < dot2 )
+			{
+				if ( vdot( n0, n ) < vdot( normal1, n ) )
+					return m;
+			}
+			else
+			{
+				if ( vdot( n2, n ) < vdot( normal1, n ) )
+					return m;
+			}
+			m = clip_segments( a1, a2, p1, p2, normals[ia1], radiusB, 0.0f, MAKE_ID( ia1, 1 ), MAKE_ID( ia2, 0 ) );
+			finish_clip( m, xfA, xfB, vneg( normals[ia1] ) );
+			return m;
+		}
+		if ( incidentIndex == -1 )
+			return m;
+	}
+	fv2 b1, b2;
+	int ib1, ib2;
+	if ( incidentNormal != -1 )
+	{
+		ib1 = incidentNormal;
+		ib2 = ib1 < count - 1 ? ib1 + 1 : 0;
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	else
+	{
+		int i2 = incidentIndex;
+		int i1 = i2 > 0 ? i2 - 1 : count - 1;
+		float d1 = vdot( normal1, normals[i1] );
+		float d2 = vdot( normal1, normals[i2] );
+		if ( d1 < d2 )
+		{
+			ib1 = i1, ib2 = i2;
+			b1 = vertices[ib1];
+			b2 = vertices[ib2];
+		}
+		else
+		{
+			ib1 = i2, ib2 = i2 < count - 1 ? i2 + 1 : 0;
+			b1 = vertices[ib1];
+			b2 = vertices[ib2];
+		}
+	}
+	m = clip_segments( p1, p2, b1, b2, normal1, 0.0f, radiusB, MAKE_ID( 0, ib2 ), MAKE_ID( 1, ib1 ) );
+	finish_clip( m, xfA, xfB, m.normal );
+	return m;
+}
+
+__device__ __forceinline__ DCache unpack_cache( int2 c )
+{
+	DCache k;
+	k.count = c.x & 0xff;
+	for ( int i = 0; i < 3; ++i )
+	{
+		k.indexA[i] = ( c.x >> ( 8 + 8 * i ) ) & 0xff;
+		k.indexB[i] = ( c.y >> ( 8 * i ) ) & 0xff;
+	}
+	return k;
+}
+
+__device__ __forceinline__ int2 pack_cache( const DCache& k )
+{
+	int2 c;
+	c.x = k.count & 0xff;
+	c.y = 0;
+	for ( int i = 0; i < k.count; ++i )
+	{
+		c.x |= ( k.indexA[i] & 0xff ) << ( 8 + 8 * i );
+		c.y |= ( k.indexB[i] & 0xff ) << ( 8 * i );
+	}
+	return c;
+}
+
+// contact.c:60-148 dispatch; A already carries the registered first type.
+// `cache` is the contact's simplex cache, read and written by the chain
+// segment manifolds only.
+__device__ __forceinline__ DManifold compute_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB,
+													   DCache& cache )
 {
 	DManifold zero = dm_empty();
 	switch ( a.type )
@@ -727,6 +1135,18 @@ __device__ __forceinline__ DManifold compute_manifold( const DGeom& a, fxf xfA, 
 				capsule_poly( pa, a.c1, a.c2, 0.0f );
 				return collide_polygons( pa, xfA, b.poly, xfB );
 			}
+			break;
+		case ST_CHAIN:
+			if ( b.type == ST_CIRCLE )
+				return collide_chain_circle( a, xfA, b.c1, b.radius, xfB );
+			if ( b.type == ST_CAPSULE )
+			{
+				DPoly pb;
+				capsule_poly( pb, b.c1, b.c2, b.radius );
+				return collide_chain_polygon( a, xfA, pb, vlerp( b.c1, b.c2, 0.5f ), xfB, cache );
+			}
+			if ( b.type == ST_POLYGON )
+				return collide_chain_polygon( a, xfA, b.poly, b.c1, xfB, cache );
 			break;
 		default:
 			break;

@@ -165,9 +165,31 @@ __device__ __forceinline__ fv2 solve3( DSimplex& s )
 	return mk( 0.0f, 0.0f );
 }
 
-// b2ShapeDistance with useRadii = false; returns the distance and updates
-// the cache (distance.c:381-560)
-static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf xfA, fxf xfB, DCache& cache )
+__device__ __forceinline__ void gjk_witness( const DSimplex& s, fv2& la, fv2& lb )
+{
+	if ( s.count == 1 )
+	{
+		la = s.v[0].wA;
+		lb = s.v[0].wB;
+	}
+	else if ( s.count == 2 )
+	{
+		la = mk( s.v[0].a * s.v[0].wA.x + s.v[1].a * s.v[1].wA.x, s.v[0].a * s.v[0].wA.y + s.v[1].a * s.v[1].wA.y );
+		lb = mk( s.v[0].a * s.v[0].wB.x + s.v[1].a * s.v[1].wB.x, s.v[0].a * s.v[0].wB.y + s.v[1].a * s.v[1].wB.y );
+	}
+	else
+	{
+		la = mk( s.v[0].a * s.v[0].wA.x + s.v[1].a * s.v[1].wA.x + s.v[2].a * s.v[2].wA.x,
+				 s.v[0].a * s.v[0].wA.y + s.v[1].a * s.v[1].wA.y + s.v[2].a * s.v[2].wA.y );
+		lb = la;
+	}
+}
+
+// b2ShapeDistance with useRadii = false (distance.c:421-606): returns the
+// distance, updates the cache (left alone when the shapes overlap) and, when
+// asked, gives the witness points in the world frame of A
+static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf xfA, fxf xfB, DCache& cache,
+									  fv2* pointA = nullptr, fv2* pointB = nullptr )
 {
 	DProxy pb;
 	{
@@ -215,10 +237,17 @@ static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf 
 			d = solve2( s );
 		else if ( s.count == 3 )
 			d = solve3( s );
-		if ( s.count == 3 )
+		if ( s.count == 3 || vdot( d, d ) < FLT_EPSILON * FLT_EPSILON )
+		{
+			if ( pointA != nullptr )
+			{
+				fv2 la, lb;
+				gjk_witness( s, la, lb );
+				*pointA = xpoint( xfA, la );
+				*pointB = xpoint( xfA, lb );
+			}
 			return 0.0f;
-		if ( vdot( d, d ) < FLT_EPSILON * FLT_EPSILON )
-			return 0.0f;
+		}
 		DSimplexVertex& vx = s.v[s.count];
 		vx.indexA = support( pa, d );
 		vx.wA = pa.p[vx.indexA];
@@ -238,24 +267,14 @@ static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf 
 		s.count += 1;
 	}
 	fv2 la, lb;
-	if ( s.count == 1 )
-	{
-		la = s.v[0].wA;
-		lb = s.v[0].wB;
-	}
-	else if ( s.count == 2 )
-	{
-		la = mk( s.v[0].a * s.v[0].wA.x + s.v[1].a * s.v[1].wA.x, s.v[0].a * s.v[0].wA.y + s.v[1].a * s.v[1].wA.y );
-		lb = mk( s.v[0].a * s.v[0].wB.x + s.v[1].a * s.v[1].wB.x, s.v[0].a * s.v[0].wB.y + s.v[1].a * s.v[1].wB.y );
-	}
-	else
-	{
-		la = mk( s.v[0].a * s.v[0].wA.x + s.v[1].a * s.v[1].wA.x + s.v[2].a * s.v[2].wA.x,
-				 s.v[0].a * s.v[0].wA.y + s.v[1].a * s.v[1].wA.y + s.v[2].a * s.v[2].wA.y );
-		lb = la;
-	}
+	gjk_witness( s, la, lb );
 	float dx = lb.x - la.x, dy = lb.y - la.y;
 	float distance = sqrtf( dx * dx + dy * dy );
+	if ( pointA != nullptr )
+	{
+		*pointA = xpoint( xfA, la );
+		*pointB = xpoint( xfA, lb );
+	}
 	cache.count = s.count;
 	for ( int i = 0; i < s.count; ++i )
 	{

@@ -41,6 +41,7 @@
 #define ST_CAPSULE 1
 #define ST_SEGMENT 2
 #define ST_POLYGON 3
+#define ST_CHAIN 4 // chain segment (one-sided, with ghost vertices)
 
 // contact flags (contact.h:74-93 sim flags plus the b2Contact flags)
 #define CF_USED 0x1
@@ -68,6 +69,7 @@
 //   g[0] = c1.x c1.y c2.x c2.y   (circle centre; capsule/segment ends; polygon centroid)
 //   g[1] = radius, count (int bits), localCentroid.x, localCentroid.y
 //   g[2..5] polygon vertices, g[6..9] polygon normals
+//   chain segment: g[0] = point1 point2, g[2] = ghost1.xy ghost2.xy
 #define GEOM_F4 10
 
 // Narrowphase manifold classes (one bucket and one kernel each): circle pairs,
@@ -296,6 +298,7 @@ struct DWorld
 	float4* cmat;  // friction restitution rollingResistance tangentSpeed
 	float4* cmass; // invMassA invIA invMassB invIB
 	float4* mnorm; // normal.x normal.y rollingImpulse pointCount(bits)
+	int2* csimplex; // GJK cache of chain segment manifolds: count | indexA[0..2] << 8.., indexB[0..2]
 	float4* mpA;   // [2*id+k] anchorA.xy anchorB.xy
 	float4* mpB;   // [2*id+k] point.xy separation id(bits, bit16 = persisted)
 	float4* mpI;   // [2*id+k] normalImpulse tangentImpulse totalNormalImpulse normalVelocity

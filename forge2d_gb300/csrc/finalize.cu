@@ -28,7 +28,7 @@ __device__ __forceinline__ fbox shape_aabb( const float4* g, int type, fxf xf )
 		b.hi = mk( p.x + r, p.y + r );
 		return b;
 	}
-	if ( type == ST_CAPSULE || type == ST_SEGMENT )
+	if ( type == ST_CAPSULE || type == ST_SEGMENT || type == ST_CHAIN )
 	{
 		fv2 v1 = xpoint( xf, mk( g0.x, g0.y ) );
 		fv2 v2 = xpoint( xf, mk( g0.z, g0.w ) );
@@ -149,7 +149,7 @@ __device__ __forceinline__ DProxy make_proxy( const float4* g, int type )
 		p.count = 1;
 		p.radius = g1.x;
 	}
-	else if ( type == ST_CAPSULE || type == ST_SEGMENT )
+	else if ( type == ST_CAPSULE || type == ST_SEGMENT || type == ST_CHAIN )
 	{
 		p.p[0] = mk( g0.x, g0.y );
 		p.p[1] = mk( g0.z, g0.w );
@@ -177,7 +177,7 @@ __device__ __forceinline__ float shape_min_extent( const float4* g, int type )
 	float4 g1 = g[1];
 	if ( type == ST_CIRCLE || type == ST_CAPSULE )
 		return g1.x;
-	if ( type == ST_SEGMENT )
+	if ( type == ST_SEGMENT || type == ST_CHAIN )
 		return 0.0f;
 	int count = __float_as_int( g1.y );
 	fv2 centroid = mk( g[0].x, g[0].y );
@@ -251,9 +251,12 @@ __global__ void k_continuous( DWorld w )
 		sweep.q1.s = s0.w;
 		sweep.q2.c = x4.z;
 		sweep.q2.s = x4.w;
-		fxf xf2;
+		fxf xf1, xf2;
+		xf1.q = sweep.q1;
+		xf1.p = vsub( sweep.c1, rrot( sweep.q1, sweep.localCenter ) );
 		xf2.q = sweep.q2;
 		xf2.p = vsub( sweep.c2, rrot( sweep.q2, sweep.localCenter ) );
+		float minExtent = w.massv[b].z;
 		float fraction = 1.0f;
 		for ( int fs = w.headShape[b], guard = 0; fs != F2D_NULL && guard < ( 1 << 20 ); fs = w.nextShape[fs], ++guard )
 		{
@@ -266,6 +269,9 @@ __global__ void k_continuous( DWorld w )
 			w.aabb[fs] = box_to4( box2 );
 			if ( sff & SF_SENSOR )
 				continue;
+			float4 gf1 = gf[1];
+			fv2 centroid1 = xpoint( xf1, mk( gf1.z, gf1.w ) );
+			fv2 centroid2 = xpoint( xf2, mk( gf1.z, gf1.w ) );
 			// b2ContinuousQueryCallback (solver.c:196-388) for one static shape
 			auto consider = [&]( int ss ) {
 				int sfs = w.sflags[ss];
@@ -284,6 +290,28 @@ __global__ void k_continuous( DWorld w )
 				if ( !joint_allows( w, b, sb ) )
 					return;
 				const float4* gs = w.geom + (size_t)ss * GEOM_F4;
+				// solver.c:283-304: no pausing on chain segment junctions
+				if ( shape_type( sfs ) == ST_CHAIN )
+				{
+					float4 st = w.xf[sb];
+					fxf t;
+					t.p = mk( st.x, st.y );
+					t.q.c = st.z;
+					t.q.s = st.w;
+					float4 s0g = gs[0];
+					fv2 p1 = xpoint( t, mk( s0g.x, s0g.y ) );
+					fv2 p2 = xpoint( t, mk( s0g.z, s0g.w ) );
+					float len;
+					fv2 e = vlen_norm( &len, vsub( p2, p1 ) );
+					if ( len > F2D_LINEAR_SLOP )
+					{
+						float offset1 = vcross( vsub( centroid1, p1 ), e );
+						float offset2 = vcross( vsub( centroid2, p1 ), e );
+						const float allowedFraction = 0.25f;
+						if ( offset1 < 0.0f || offset1 - offset2 < allowedFraction * minExtent )
+							return;
+					}
+				}
 				DProxy pa = make_proxy( gs, shape_type( sfs ) );
 				DProxy pb = make_proxy( gf, tf );
 				float4 ss0 = w.sweep0[sb];

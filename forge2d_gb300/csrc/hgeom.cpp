@@ -372,6 +372,7 @@ fv2 h_shape_centroid( const HShapeGeom& g )
 	{
 		case ST_CAPSULE:
 		case ST_SEGMENT:
+		case ST_CHAIN:
 			return vlerp( g.c1, g.c2, 0.5f );
 		case ST_CIRCLE:
 			return g.c1;

@@ -23,6 +23,7 @@ struct HShapeGeom
 	fv2 c1, c2;
 	float radius;
 	HPoly poly;
+	fv2 g1, g2; // chain segment ghost vertices (before c1, after c2)
 };
 
 struct HMass

@@ -36,7 +36,7 @@ __device__ __forceinline__ int manifold_class( int ta, int tb )
 // The manifold function compute_manifold selects for the class, called
 // directly so that each class kernel holds only its own path.
 template <int CLS>
-__device__ __forceinline__ DManifold class_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB )
+__device__ __forceinline__ DManifold class_manifold( const DGeom& a, fxf xfA, const DGeom& b, fxf xfB, DCache& cache )
 {
 	if ( CLS == 0 )
 		return collide_circles( a.c1, a.radius, xfA, b.c1, b.radius, xfB );
@@ -46,7 +46,7 @@ __device__ __forceinline__ DManifold class_manifold( const DGeom& a, fxf xfA, co
 		return collide_capsules( a.c1, a.c2, a.type == ST_SEGMENT ? 0.0f : a.radius, xfA, b.c1, b.c2, b.radius, xfB );
 	if ( CLS == 3 )
 		return collide_polygon_circle( a.poly, xfA, b.c1, b.radius, xfB );
-	return compute_manifold( a, xfA, b, xfB );
+	return compute_manifold( a, xfA, b, xfB, cache );
 }
 
 // Fat-AABB test of every live contact (b2CollideTask's disjoint check); the
@@ -128,7 +128,15 @@ template <int CLS> __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase
 		const float4* gb = w.geom + (size_t)sh.y * GEOM_F4;
 		DGeom A = load_geom( ga, ta );
 		DGeom B = load_geom( gb, tb );
-		DManifold m = class_manifold<CLS>( A, xfA, B, xfB );
+		// the contact's GJK cache (chain segments against capsules and polygons)
+		bool chain = CLS == 4 && ta == ST_CHAIN;
+		DCache cache;
+		cache.count = 0;
+		if ( chain )
+			cache = unpack_cache( w.csimplex[c] );
+		DManifold m = class_manifold<CLS>( A, xfA, B, xfB, cache );
+		if ( chain )
+			w.csimplex[c] = pack_cache( cache );
 
 		float4 mta = w.mat[sh.x], mtb = w.mat[sh.y];
 		float friction = sqrtf( mta.x * mtb.x );

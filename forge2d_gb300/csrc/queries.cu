@@ -164,6 +164,22 @@ __device__ RayHit ray_segment( fv2 origin, fv2 translation, float maxFraction, f
 	return out;
 }
 
+// geometry.c:718-729: a chain segment is one-sided; rays starting on its
+// left pass through
+__device__ RayHit ray_segment_sided( fv2 origin, fv2 translation, fv2 p1, fv2 p2, bool oneSided )
+{
+	if ( oneSided && vcross( vsub( origin, p1 ), vsub( p2, p1 ) ) < 0.0f )
+	{
+		RayHit none;
+		none.hit = false;
+		none.point = mk( 0.0f, 0.0f );
+		none.normal = mk( 0.0f, 0.0f );
+		none.fraction = 0.0f;
+		return none;
+	}
+	return ray_segment( origin, translation, 1.0f, p1, p2 );
+}
+
 __device__ RayHit ray_polygon( fv2 origin, fv2 d, float maxFraction, const float4* g )
 {
 	RayHit out;
@@ -288,8 +304,8 @@ __global__ void k_ray_closest( DWorld w, fv2 origin, fv2 translation, unsigned l
 			h = ray_circle( lo, lt, 1.0f, mk( g0.x, g0.y ), g1.x );
 		else if ( type == ST_CAPSULE )
 			h = ray_capsule( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ), g1.x );
-		else if ( type == ST_SEGMENT )
-			h = ray_segment( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ) );
+		else if ( type == ST_SEGMENT || type == ST_CHAIN )
+			h = ray_segment_sided( lo, lt, mk( g0.x, g0.y ), mk( g0.z, g0.w ), type == ST_CHAIN );
 		else
 			h = ray_polygon( lo, lt, 1.0f, g );
 		if ( !h.hit || h.fraction == 0.0f )
@@ -324,8 +340,8 @@ __global__ void k_ray_result( DWorld w, fv2 origin, fv2 translation, const unsig
 		h = ray_circle( lo, lt, 1.0f, mk( g0.x, g0.y ), g1.x );
 	else if ( type == ST_CAPSULE )
 		h = ray_capsule( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ), g1.x );
-	else if ( type == ST_SEGMENT )
-		h = ray_segment( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ) );
+	else if ( type == ST_SEGMENT || type == ST_CHAIN )
+		h = ray_segment_sided( lo, lt, mk( g0.x, g0.y ), mk( g0.z, g0.w ), type == ST_CHAIN );
 	else
 		h = ray_polygon( lo, lt, 1.0f, g );
 	fv2 p = xpoint( xf, h.point );

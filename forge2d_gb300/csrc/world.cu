@@ -86,6 +86,10 @@ struct HostWorld
 	std::vector<int> shapeDirty;
 	TreeIds trees[3];
 	std::vector<int> staticShapes;
+	// chains: segment shape ids and generation per chain id (LIFO id reuse)
+	std::vector<std::vector<int>> chainSegments;
+	std::vector<uint16_t> chainGen;
+	std::vector<int> chainFree;
 	bool staticDirty = false;
 
 	std::vector<int2> jbody;
@@ -238,6 +242,7 @@ static void grow_contacts( HostWorld* W, int cap )
 	dgrow( d.cmat, o, cap );
 	dgrow( d.cmass, o, cap );
 	dgrow( d.mnorm, o, cap );
+	dgrow( d.csimplex, o, cap );
 	dgrow( d.mpA, 2 * o, 2 * (size_t)cap );
 	dgrow( d.mpB, 2 * o, 2 * (size_t)cap );
 	dgrow( d.mpI, 2 * o, 2 * (size_t)cap );
@@ -820,7 +825,7 @@ static void free_world( HostWorld* W )
 	F( bflags ); F( headShape ); F( headJoint ); F( jointCountB ); F( colorMask ); F( colorLock );
 	F( geom ); F( aabb ); F( fat ); F( mat ); F( cat ); F( mask ); F( group ); F( shapeBody ); F( sflags );
 	F( proxyKey ); F( nextShape ); F( cshape ); F( cbody ); F( cflags ); F( ccolor ); F( coverflowIndex ); F( cmat );
-	F( cmass ); F( mnorm ); F( mpA ); F( mpB ); F( mpI ); F( contactFree ); F( pairHash ); F( mortonKeys );
+	F( cmass ); F( mnorm ); F( csimplex ); F( mpA ); F( mpB ); F( mpI ); F( contactFree ); F( pairHash ); F( mortonKeys );
 	F( mortonKeysAlt ); F( leafShape ); F( leafShapeAlt ); F( nodeLeft ); F( nodeRight ); F( nodeParent ); F( nodeBox );
 	F( nodeVisit ); F( sortHist ); F( pairKeys ); F( pairKeysAlt ); F( pairVal ); F( pairValAlt ); F( planIds );
 	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( opBodies ); F( opScan ); F( slotContact ); F( overflowList );
@@ -1082,6 +1087,8 @@ static void pack_geom( const HShapeGeom& g, float4* out )
 	{
 		out[0] = make_float4( g.c1.x, g.c1.y, g.c2.x, g.c2.y );
 		out[1] = make_float4( g.radius, bits_to_float( 0 ), centroid.x, centroid.y );
+		if ( g.type == ST_CHAIN )
+			out[2] = make_float4( g.g1.x, g.g1.y, g.g2.x, g.g2.y );
 	}
 }
 
@@ -1213,6 +1220,114 @@ extern "C" F2D_API int32_t f2d_create_segment_shape( int32_t bi, int32_t bwg, co
 	g.c1 = mk( (float)x1, (float)y1 );
 	g.c2 = mk( (float)x2, (float)y2 );
 	return create_shape( W, b, def, g, index1, wg );
+}
+
+// shape.c:339-486 b2CreateChain: count >= 4 points; a loop makes count
+// segments, an open chain count - 3 (its end points are ghosts only).
+// Materials are six values each (friction, restitution, rollingResistance,
+// tangentSpeed, userMaterialId, customColor), one for every segment or one
+// per point, a segment taking its leading point's. The segments get the
+// default shape definition without contact or hit events and leave the body
+// mass alone.
+extern "C" F2D_API int32_t f2d_create_chain( int32_t bi, int32_t bwg, const double* points, int32_t count,
+											 const double* materials, int32_t materialCount, int64_t categoryBits,
+											 int64_t maskBits, int32_t groupIndex, int32_t isLoop,
+											 int32_t enableSensorEvents, int32_t* index1, int32_t* wg )
+{
+	if ( index1 )
+		*index1 = 0;
+	if ( wg )
+		*wg = 0;
+	HostWorld* W;
+	int b = body_from( bi, bwg, &W );
+	if ( b < 0 || points == nullptr || materials == nullptr || count < 4 || count > ( 1 << 20 ) ||
+		 ( materialCount != 1 && materialCount != count ) )
+		return 0;
+	int id;
+	if ( !W->chainFree.empty() )
+	{
+		id = W->chainFree.back();
+		W->chainFree.pop_back();
+	}
+	else
+	{
+		id = (int)W->chainSegments.size();
+		W->chainSegments.emplace_back();
+		W->chainGen.push_back( 0 );
+	}
+	W->chainGen[id] = (uint16_t)( W->chainGen[id] + 1 );
+	std::vector<int>& segs = W->chainSegments[id];
+	segs.clear();
+	int n = isLoop ? count : count - 3;
+	f2d_shape_def d = {};
+	d.density = 1.0;
+	d.categoryBits = categoryBits;
+	d.maskBits = maskBits;
+	d.groupIndex = groupIndex;
+	d.enableSensorEvents = enableSensorEvents != 0;
+	d.invokeContactCreation = 1;
+	d.updateBodyMass = 0;
+	auto pt = [&]( int i ) { return mk( (float)points[2 * i], (float)points[2 * i + 1] ); };
+	for ( int k = 0; k < n; ++k )
+	{
+		int i0, i1, i2, i3, mi;
+		if ( isLoop )
+		{
+			i0 = ( k + count - 1 ) % count;
+			i1 = k;
+			i2 = ( k + 1 ) % count;
+			i3 = ( k + 2 ) % count;
+			mi = k;
+		}
+		else
+		{
+			i0 = k;
+			i1 = k + 1;
+			i2 = k + 2;
+			i3 = k + 3;
+			mi = k + 1;
+		}
+		const double* m = materials + 6 * ( materialCount == 1 ? 0 : mi );
+		d.friction = m[0];
+		d.restitution = m[1];
+		d.rollingResistance = m[2];
+		d.tangentSpeed = m[3];
+		d.userMaterialId = (int)m[4];
+		HShapeGeom g = {};
+		g.type = ST_CHAIN;
+		g.g1 = pt( i0 );
+		g.c1 = pt( i1 );
+		g.c2 = pt( i2 );
+		g.g2 = pt( i3 );
+		int32_t si = 0, swg = 0;
+		create_shape( W, b, &d, g, &si, &swg );
+		segs.push_back( si - 1 );
+	}
+	if ( index1 )
+		*index1 = id + 1;
+	if ( wg )
+		*wg = pack_wg( W, W->chainGen[id] );
+	return 1;
+}
+
+// RawBox2D.chainGetSegments (raw_box2d.dart:571): segment shape ids as
+// (index1, worldAndGeneration) pairs; returns the segment count
+extern "C" F2D_API int32_t f2d_chain_get_segments( int32_t index1, int32_t wg, int32_t* out2, int32_t capacity )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return 0;
+	int id = index1 - 1;
+	if ( id < 0 || id >= (int)W->chainSegments.size() || W->chainGen[id] != ( ( wg >> 16 ) & 0xffff ) )
+		return 0;
+	const std::vector<int>& segs = W->chainSegments[id];
+	int n = (int)segs.size();
+	for ( int i = 0; i < n && i < capacity && out2 != nullptr; ++i )
+	{
+		out2[2 * i] = segs[i] + 1;
+		out2[2 * i + 1] = pack_wg( W, W->sgen[segs[i]] );
+	}
+	return n;
 }
 
 extern "C" F2D_API int32_t f2d_create_box_shape( int32_t bi, int32_t bwg, const f2d_shape_def* def, double hx,

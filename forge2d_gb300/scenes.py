@@ -359,6 +359,31 @@ def joint_zoo(b, copies=3):
                                  enableLimit=1, minLength=1.5, maxLength=4.0))
 
 
+def chain_terrain(b, count=400, seed=5, width=40.0, height=40.0, bumps=6, materials=None):
+    """Chain shapes: a closed loop container (clockwise, so the one-sided
+    segments face inwards) with a wavy floor of convex and concave
+    vertices, an open bumpy ramp (its end points ghosts only) and the mixed
+    pile's shapes (``count`` from ``seed``) dropped on them."""
+    g = b.create_body(body_def(type=STATIC))
+    hw = 0.5 * width + 1.0
+    top = height + 6.0
+    pts = [(-hw, top), (hw, top), (hw, 0.0)]
+    n = 8 * bumps
+    for i in range(1, n):
+        x = hw - 2.0 * hw * i / n
+        pts.append((x, 0.6 * math.sin(bumps * math.pi * x / hw) + 0.25 * math.cos(3.1 * x)))
+    pts.append((-hw, 0.0))
+    mats = materials if materials is not None else [(0.6, 0.0, 0.0, 0.0, 0, 0)]
+    b.create_chain(g, pts, materials=mats, isLoop=True)
+    ramp = [(0.6 * hw + 2.0, 0.45 * top + 3.0)]
+    for i in range(7):
+        x = 0.6 * hw - 1.2 * hw * i / 6.0
+        ramp.append((x, 0.45 * top - 0.25 * (0.6 * hw - x) + 0.4 * math.sin(2.0 * x)))
+    ramp.append((-0.6 * hw - 2.0, 0.45 * top - 0.35 * hw - 1.5))
+    b.create_chain(g, ramp, materials=[(0.4, 0.1, 0.0, 0.0, 0, 0)], isLoop=False)
+    return pile(b, count=count, seed=seed, width=width - 2.0, height=height, with_container=False)
+
+
 def joint_rigs(b, copies=3):
     """Prismatic, wheel, motor, mouse and filter joints, ``copies`` times over
     a ground box: an elevator (vertical prismatic with limits and a motor)
@@ -500,4 +525,6 @@ def build(b, name, **kw):
         return joint_zoo(b, **kw)
     if name == "joint_rigs":
         return joint_rigs(b, **kw)
+    if name == "chain_terrain":
+        return chain_terrain(b, **kw)
     raise ValueError(name)

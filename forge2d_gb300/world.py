@@ -146,6 +146,24 @@ class GpuWorld:
         ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def create_chain(self, body, points, materials=((0.6, 0.0, 0.0, 0.0, 0, 0),), categoryBits=1, maskBits=-1,
+                     groupIndex=0, isLoop=False, enableSensorEvents=False):
+        """Chain of one-sided segments on ``body`` (b2CreateChain); returns the
+        chain id pair."""
+        pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1))
+        mats = np.ascontiguousarray(np.asarray(materials, np.float64).reshape(-1))
+        i1, wg = C.c_int32(0), C.c_int32(0)
+        ok = self.lib.f2d_create_chain(body[0], body[1], pts.ctypes.data_as(C.POINTER(C.c_double)), len(pts) // 2,
+                                       mats.ctypes.data_as(C.POINTER(C.c_double)), len(mats) // 6, categoryBits,
+                                       maskBits, groupIndex, int(isLoop), int(enableSensorEvents),
+                                       C.byref(i1), C.byref(wg))
+        return self._ret(ok, i1, wg)
+
+    def chain_segments(self, chain):
+        out = np.zeros(2 * (1 << 16), np.int32)
+        n = self.lib.f2d_chain_get_segments(chain[0], chain[1], _iptr(out), len(out) // 2)
+        return [tuple(r) for r in out[:2 * n].reshape(-1, 2).tolist()]
+
     def create_joint(self, jd: dict):
         """Weld (type 2) or distance (type 3) joint from an f2d_joint_def dict."""
         d = dict(JOINT_DEFAULTS)

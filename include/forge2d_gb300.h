@@ -288,6 +288,18 @@ F2D_API int32_t f2d_create_box_shape( int32_t bodyIndex1, int32_t bodyWorldAndGe
 F2D_API int32_t f2d_create_polygon_shape( int32_t bodyIndex1, int32_t bodyWorldAndGeneration,
 										  const f2d_shape_def* def, const double* points, int32_t count,
 										  double radius, int32_t* index1, int32_t* worldAndGeneration );
+/* RawBox2D.createChain (raw_box2d.dart:537 -> b2CreateChain, shape.c:339):
+ * points packed [x0, y0, x1, y1, ...], count >= 4; materials six values each
+ * (friction, restitution, rollingResistance, tangentSpeed, userMaterialId,
+ * customColor), one or one per point. Returns the chain id pair. */
+F2D_API int32_t f2d_create_chain( int32_t bodyIndex1, int32_t bodyWorldAndGeneration, const double* points,
+								  int32_t count, const double* materials, int32_t materialCount, int64_t categoryBits,
+								  int64_t maskBits, int32_t groupIndex, int32_t isLoop, int32_t enableSensorEvents,
+								  int32_t* index1, int32_t* worldAndGeneration );
+/* RawBox2D.chainGetSegments (raw_box2d.dart:571): the segment shape id pairs
+ * (index1, worldAndGeneration) in creation order; returns the count. */
+F2D_API int32_t f2d_chain_get_segments( int32_t index1, int32_t worldAndGeneration, int32_t* out2,
+										int32_t capacity );
 /* RawBox2D.shapeIsValid / shapeGetType (raw_box2d.dart:397-400). */
 F2D_API int32_t f2d_shape_is_valid( int32_t index1, int32_t worldAndGeneration );
 F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t worldAndGeneration );

@@ -146,6 +146,8 @@ def _bind(lib, prefix):
         "create_circle_shape": (i, [i, i, _P(ShapeDef), d, d, d]),
         "create_capsule_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d]),
         "create_segment_shape": (i, [i, i, _P(ShapeDef), d, d, d, d]),
+        "create_chain": (i, [i, i, _P(d), i, _P(d), i, C.c_longlong, C.c_longlong, i, i, i]),
+        "chain_get_segments": (i, [i, i, _P(i), i]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
         "create_revolute_joint": (i, [i, _P(RevoluteDef)]),
@@ -227,6 +229,22 @@ class _CpuWorld:
 
     def create_segment(self, body, sd, x1, y1, x2, y2):
         return self._fns["create_segment_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), x1, y1, x2, y2)
+
+    def create_chain(self, body, points, materials=((0.6, 0.0, 0.0, 0.0, 0, 0),), categoryBits=1, maskBits=-1,
+                     groupIndex=0, isLoop=False, enableSensorEvents=False):
+        """b2CreateChain: ``points`` (n, 2), ``materials`` one or n rows of
+        (friction, restitution, rollingResistance, tangentSpeed,
+        userMaterialId, customColor)."""
+        pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1))
+        mats = np.ascontiguousarray(np.asarray(materials, np.float64).reshape(-1))
+        return self._fns["create_chain"](self.w, body, pts.ctypes.data_as(_P(C.c_double)), len(pts) // 2,
+                                         mats.ctypes.data_as(_P(C.c_double)), len(mats) // 6, categoryBits,
+                                         maskBits, groupIndex, int(isLoop), int(enableSensorEvents))
+
+    def chain_segments(self, chain):
+        out = np.zeros(1 << 16, np.int32)
+        n = self._fns["chain_get_segments"](self.w, chain, out.ctypes.data_as(_P(C.c_int)), len(out))
+        return out[:n].copy()
 
     def create_box(self, body, sd, hx, hy, cx=0.0, cy=0.0, c=1.0, s=0.0, radius=0.0):
         return self._fns["create_box_shape"](self.w, body, C.byref(_fill(ShapeDef(), sd)), hx, hy, cx, cy, c, s, radius)

@@ -78,8 +78,6 @@ void p_solve_continuous( World* w, int bodyId )
 			continue;
 		v2 centroid1 = xfPoint( xf1, fastShape->localCentroid );
 		v2 centroid2 = xfPoint( xf2, fastShape->localCentroid );
-		(void)centroid1;
-		(void)centroid2;
 		for ( int k = 0; k < w->staticShapeCount; ++k )
 		{
 			int si = w->staticShapes[k];
@@ -97,6 +95,25 @@ void p_solve_continuous( World* w, int bodyId )
 				continue;
 			if ( bodies_collide( w, bodyId, shape->bodyId ) == 0 )
 				continue;
+			// solver.c:283-304: no pausing on chain segment junctions (the fast
+			// shape starts behind, or crosses by less than a quarter of the
+			// body's minimum extent)
+			if ( shape->g.type == SHAPE_CHAIN_SEGMENT )
+			{
+				xform transform = body->xf;
+				v2 p1 = xfPoint( transform, shape->g.c1 );
+				v2 p2 = xfPoint( transform, shape->g.c2 );
+				float len;
+				v2 e = lengthAndNormalize( &len, sub( p2, p1 ) );
+				if ( len > P_LINEAR_SLOP )
+				{
+					float offset1 = cross( sub( centroid1, p1 ), e );
+					float offset2 = cross( sub( centroid2, p1 ), e );
+					const float allowedFraction = 0.25f;
+					if ( offset1 < 0.0f || offset1 - offset2 < allowedFraction * fast->minExtent )
+						continue;
+				}
+			}
 			ShapeProxy pa = p_shape_proxy( &shape->g );
 			ShapeProxy pb = p_shape_proxy( &fastShape->g );
 			Sweep sa = make_sweep( body );

@@ -20,13 +20,6 @@ typedef struct Simplex
 	int count;
 } Simplex;
 
-typedef struct SimplexCache
-{
-	int count;
-	uint8_t indexA[3];
-	uint8_t indexB[3];
-} SimplexCache;
-
 static xform sweep_xf( const Sweep* s, float time )
 {
 	xform xf;
@@ -241,9 +234,11 @@ static v2 solve3( Simplex* s )
 	return V( 0.0f, 0.0f );
 }
 
-// distance.c:381-560 with useRadii = false; only the distance and the cache
-// are consumed by the time-of-impact loop
-static float shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform xfA, xform xfB, SimplexCache* cache )
+// distance.c:421-606 b2ShapeDistance with useRadii = false: the distance,
+// the witness points in the world frame of A (optional) and the updated
+// cache (left alone when the shapes overlap)
+float p_shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform xfA, xform xfB, SimplexCache* cache,
+						v2* pointA, v2* pointB )
 {
 	ShapeProxy pb;
 	{
@@ -282,10 +277,17 @@ static float shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform
 			default:
 				break;
 		}
-		if ( simplex.count == 3 )
+		if ( simplex.count == 3 || dot( d, d ) < FLT_EPSILON * FLT_EPSILON )
+		{
+			if ( pointA != NULL )
+			{
+				v2 la, lb;
+				witness( &la, &lb, &simplex );
+				*pointA = xfPoint( xfA, la );
+				*pointB = xfPoint( xfA, lb );
+			}
 			return 0.0f;
-		if ( dot( d, d ) < FLT_EPSILON * FLT_EPSILON )
-			return 0.0f;
+		}
 		nonUnitNormal = d;
 		SimplexVertex* vertex = vs[simplex.count];
 		vertex->indexA = find_support( pa, d );
@@ -313,6 +315,11 @@ static float shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform
 	float dx = lb.x - la.x;
 	float dy = lb.y - la.y;
 	float distance = sqrtf( dx * dx + dy * dy );
+	if ( pointA != NULL )
+	{
+		*pointA = xfPoint( xfA, la );
+		*pointB = xfPoint( xfA, lb );
+	}
 	cache->count = simplex.count;
 	for ( int i = 0; i < simplex.count; ++i )
 	{
@@ -476,7 +483,7 @@ float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sw
 	{
 		xform xfA = sweep_xf( &sa, t1 );
 		xform xfB = sweep_xf( &sb, t1 );
-		float distance = shape_distance( pa, pb, xfA, xfB, &cache );
+		float distance = p_shape_distance( pa, pb, xfA, xfB, &cache, NULL, NULL );
 		distanceIterations += 1;
 		if ( distance <= 0.0f )
 		{

@@ -439,6 +439,7 @@ v2 p_shape_centroid( const Geometry* g )
 		case SHAPE_POLYGON:
 			return g->poly.centroid;
 		case SHAPE_SEGMENT:
+		case SHAPE_CHAIN_SEGMENT:
 			return lerp( g->c1, g->c2, 0.5f );
 		default:
 			return V( 0.0f, 0.0f );

@@ -627,6 +627,376 @@ static Manifold collide_polygons( const Polygon* polygonA, xform xfA, const Poly
 	return m;
 }
 
+// manifold.c:1089-1168: one-sided, with the ghost vertices' Voronoi regions
+static Manifold collide_chain_circle( const Geometry* segA, xform xfA, v2 centerB, float radius, xform xfB )
+{
+	Manifold m = { 0 };
+	xform xf = invMulXf( xfA, xfB );
+	v2 pB = xfPoint( xf, centerB );
+	v2 p1 = segA->c1;
+	v2 p2 = segA->c2;
+	v2 e = sub( p2, p1 );
+	float offset = dot( rightPerp( e ), sub( pB, p1 ) );
+	if ( offset < 0.0f )
+		return m;
+	float u = dot( e, sub( p2, pB ) );
+	float v = dot( e, sub( pB, p1 ) );
+	v2 pA;
+	if ( v <= 0.0f )
+	{
+		v2 prevEdge = sub( p1, segA->g1 );
+		float uPrev = dot( prevEdge, sub( pB, p1 ) );
+		if ( uPrev <= 0.0f )
+			return m;
+		pA = p1;
+	}
+	else if ( u <= 0.0f )
+	{
+		v2 nextEdge = sub( segA->g2, p2 );
+		float vNext = dot( nextEdge, sub( pB, p2 ) );
+		if ( vNext > 0.0f )
+			return m;
+		pA = p2;
+	}
+	else
+	{
+		float ee = dot( e, e );
+		pA = V( u * p1.x + v * p2.x, u * p1.y + v * p2.y );
+		pA = ee > 0.0f ? mulSV( 1.0f / ee, pA ) : p1;
+	}
+	float distance;
+	v2 normal = lengthAndNormalize( &distance, sub( pB, pA ) );
+	float separation = distance - radius;
+	if ( separation > P_SPECULATIVE )
+		return m;
+	v2 cA = pA;
+	v2 cB = mulAdd( pB, -radius, normal );
+	v2 contactPointA = lerp( cA, cB, 0.5f );
+	m.normal = rotate( xfA.q, normal );
+	finish_point( &m, xfA, xfB, contactPointA, separation, 0, 0 );
+	return m;
+}
+
+// manifold.c:1177-1254 b2ClipSegments (points in the frame of A, unrotated)
+static Manifold clip_segments( v2 a1, v2 a2, v2 b1, v2 b2, v2 normal, float ra, float rb, uint16_t id1,
+							   uint16_t id2 )
+{
+	Manifold m = { 0 };
+	v2 tangent = leftPerp( normal );
+	float lower1 = 0.0f;
+	float upper1 = dot( sub( a2, a1 ), tangent );
+	float upper2 = dot( sub( b1, a1 ), tangent );
+	float lower2 = dot( sub( b2, a1 ), tangent );
+	if ( upper2 < lower1 || upper1 < lower2 )
+		return m;
+	v2 vLower;
+	if ( lower2 < lower1 && upper2 - lower2 > FLT_EPSILON )
+		vLower = lerp( b2, b1, ( lower1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vLower = b2;
+	v2 vUpper;
+	if ( upper2 > upper1 && upper2 - lower2 > FLT_EPSILON )
+		vUpper = lerp( b2, b1, ( upper1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vUpper = b1;
+	float separationLower = dot( sub( vLower, a1 ), normal );
+	float separationUpper = dot( sub( vUpper, a1 ), normal );
+	vLower = mulAdd( vLower, 0.5f * ( ra - rb - separationLower ), normal );
+	vUpper = mulAdd( vUpper, 0.5f * ( ra - rb - separationUpper ), normal );
+	float radius = ra + rb;
+	m.normal = normal;
+	m.points[0].anchorA = vLower;
+	m.points[0].separation = separationLower - radius;
+	m.points[0].id = id1;
+	m.points[1].anchorA = vUpper;
+	m.points[1].separation = separationUpper - radius;
+	m.points[1].id = id2;
+	m.pointCount = 2;
+	return m;
+}
+
+enum
+{
+	NORMAL_SKIP = 0,
+	NORMAL_ADMIT = 1,
+	NORMAL_SNAP = 2,
+};
+
+typedef struct ChainParams
+{
+	v2 edge1, normal0, normal2;
+	int convex1, convex2;
+} ChainParams;
+
+// manifold.c:1270-1316 b2ClassifyNormal (Gauss map of the chain vertex)
+static int classify_normal( const ChainParams* p, v2 normal )
+{
+	const float sinTol = 0.01f;
+	if ( dot( normal, p->edge1 ) <= 0.0f )
+	{
+		if ( p->convex1 )
+			return cross( normal, p->normal0 ) > sinTol ? NORMAL_SKIP : NORMAL_ADMIT;
+		return NORMAL_SNAP;
+	}
+	if ( p->convex2 )
+		return cross( p->normal2, normal ) > sinTol ? NORMAL_SKIP : NORMAL_ADMIT;
+	return NORMAL_SNAP;
+}
+
+// rotates a clipped two-point manifold from the segment frame to the world
+static void finish_clip( Manifold* m, xform xfA, xform xfB, v2 normalLocal )
+{
+	if ( m->pointCount != 2 )
+		return;
+	m->normal = rotate( xfA.q, normalLocal );
+	m->points[0].anchorA = rotate( xfA.q, m->points[0].anchorA );
+	m->points[1].anchorA = rotate( xfA.q, m->points[1].anchorA );
+	v2 pAB = sub( xfA.p, xfB.p );
+	m->points[0].anchorB = add( m->points[0].anchorA, pAB );
+	m->points[1].anchorB = add( m->points[1].anchorA, pAB );
+	m->points[0].point = add( xfA.p, m->points[0].anchorA );
+	m->points[1].point = add( xfA.p, m->points[1].anchorA );
+}
+
+// manifold.c:1318-1726 b2CollideChainSegmentAndPolygon: GJK (warm-started
+// from the contact's simplex cache) picks vertex-vertex, vertex-edge or the
+// SAT over the segment normal, its convex neighbours and the admitted
+// polygon normals; ghost collisions are skipped or snapped by the Gauss map
+static Manifold collide_chain_polygon( const Geometry* segA, xform xfA, const Polygon* polygonB, xform xfB,
+									   SimplexCache* cache )
+{
+	Manifold m = { 0 };
+	xform xf = invMulXf( xfA, xfB );
+	v2 centroidB = xfPoint( xf, polygonB->centroid );
+	float radiusB = polygonB->radius;
+	v2 p1 = segA->c1;
+	v2 p2 = segA->c2;
+	v2 edge1 = normalize( sub( p2, p1 ) );
+	ChainParams sp = { 0 };
+	sp.edge1 = edge1;
+	const float convexTol = 0.01f;
+	v2 edge0 = normalize( sub( p1, segA->g1 ) );
+	sp.normal0 = rightPerp( edge0 );
+	sp.convex1 = cross( edge0, edge1 ) >= convexTol;
+	v2 edge2 = normalize( sub( segA->g2, p2 ) );
+	sp.normal2 = rightPerp( edge2 );
+	sp.convex2 = cross( edge1, edge2 ) >= convexTol;
+	v2 normal1 = rightPerp( edge1 );
+	int behind1 = dot( normal1, sub( centroidB, p1 ) ) < 0.0f;
+	int behind0 = 1, behind2 = 1;
+	if ( sp.convex1 )
+		behind0 = dot( sp.normal0, sub( centroidB, p1 ) ) < 0.0f;
+	if ( sp.convex2 )
+		behind2 = dot( sp.normal2, sub( centroidB, p2 ) ) < 0.0f;
+	if ( behind1 && behind0 && behind2 )
+		return m;
+	int count = polygonB->count;
+	v2 vertices[P_MAX_POLY];
+	v2 normals[P_MAX_POLY];
+	for ( int i = 0; i < count; ++i )
+	{
+		vertices[i] = xfPoint( xf, polygonB->vertices[i] );
+		normals[i] = rotate( xf.q, polygonB->normals[i] );
+	}
+	ShapeProxy proxyA = p_make_proxy( &segA->c1, 2, 0.0f );
+	ShapeProxy proxyB = p_make_proxy( vertices, count, 0.0f );
+	xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+	v2 pointA = V( 0.0f, 0.0f ), pointB = V( 0.0f, 0.0f );
+	float distance = p_shape_distance( &proxyA, &proxyB, identity, identity, cache, &pointA, &pointB );
+	if ( distance > radiusB + P_SPECULATIVE )
+		return m;
+	v2 n0 = sp.convex1 ? sp.normal0 : normal1;
+	v2 n2 = sp.convex2 ? sp.normal2 : normal1;
+	int incidentIndex = -1;
+	int incidentNormal = -1;
+	if ( behind1 == 0 && distance > 0.1f * P_LINEAR_SLOP )
+	{
+		if ( cache->count == 1 )
+		{
+			v2 pA = pointA;
+			v2 pB = pointB;
+			v2 normal = normalize( sub( pB, pA ) );
+			int type = classify_normal( &sp, normal );
+			if ( type == NORMAL_SKIP )
+				return m;
+			if ( type == NORMAL_ADMIT )
+			{
+				m.normal = rotate( xfA.q, normal );
+				ManifoldPoint* cp = m.points + 0;
+				cp->anchorA = rotate( xfA.q, pA );
+				cp->anchorB = add( cp->anchorA, sub( xfA.p, xfB.p ) );
+				cp->point = add( xfA.p, cp->anchorA );
+				cp->separation = distance - radiusB;
+				cp->id = MAKE_ID( cache->indexA[0], cache->indexB[0] );
+				m.pointCount = 1;
+				return m;
+			}
+			incidentIndex = cache->indexB[0];
+		}
+		else
+		{
+			int ia1 = cache->indexA[0];
+			int ia2 = cache->indexA[1];
+			int ib1 = cache->indexB[0];
+			int ib2 = cache->indexB[1];
+			if ( ia1 == ia2 )
+			{
+				v2 normalB = sub( pointA, pointB );
+				float dot1 = dot( normalB, normals[ib1] );
+				float dot2 = dot( normalB, normals[ib2] );
+				int ib = dot1 > dot2 ? ib1 : ib2;
+				normalB = normals[ib];
+				int type = classify_normal( &sp, neg( normalB ) );
+				if ( type == NORMAL_SKIP )
+					return m;
+				if ( type == NORMAL_ADMIT )
+				{
+					ib1 = ib;
+					ib2 = ib < count - 1 ? ib + 1 : 0;
+					v2 b1 = vertices[ib1];
+					v2 b2 = vertices[ib2];
+					dot1 = dot( normalB, sub( p1, b1 ) );
+					dot2 = dot( normalB, sub( p2, b1 ) );
+					if ( dot1 < dot2 )
+					{
+						if ( dot( n0, normalB ) < dot( normal1, normalB ) )
+							return m;
+					}
+					else
+					{
+						if ( dot( n2, normalB ) < dot( normal1, normalB ) )
+							return m;
+					}
+					m = clip_segments( b1, b2, p1, p2, normalB, radiusB, 0.0f, MAKE_ID( ib1, 1 ), MAKE_ID( ib2, 0 ) );
+					finish_clip( &m, xfA, xfB, neg( normalB ) );
+					return m;
+				}
+				incidentNormal = ib;
+			}
+			else
+			{
+				float dot1 = dot( normal1, sub( vertices[ib1], p1 ) );
+				float dot2 = dot( normal1, sub( vertices[ib2], p2 ) );
+				incidentIndex = dot1 < dot2 ? ib1 : ib2;
+			}
+		}
+	}
+	else
+	{
+		float edgeSeparation = FLT_MAX;
+		for ( int i = 0; i < count; ++i )
+		{
+			float s = dot( normal1, sub( vertices[i], p1 ) );
+			if ( s < edgeSeparation )
+			{
+				edgeSeparation = s;
+				incidentIndex = i;
+			}
+		}
+		if ( sp.convex1 )
+		{
+			float s0 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = dot( sp.normal0, sub( vertices[i], p1 ) );
+				if ( s < s0 )
+					s0 = s;
+			}
+			if ( s0 > edgeSeparation )
+			{
+				edgeSeparation = s0;
+				incidentIndex = -1;
+			}
+		}
+		if ( sp.convex2 )
+		{
+			float s2 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = dot( sp.normal2, sub( vertices[i], p2 ) );
+				if ( s < s2 )
+					s2 = s;
+			}
+			if ( s2 > edgeSeparation )
+			{
+				edgeSeparation = s2;
+				incidentIndex = -1;
+			}
+		}
+		float polygonSeparation = -FLT_MAX;
+		int referenceIndex = -1;
+		for ( int i = 0; i < count; ++i )
+		{
+			v2 n = normals[i];
+			if ( classify_normal( &sp, neg( n ) ) != NORMAL_ADMIT )
+				continue;
+			v2 p = vertices[i];
+			float s = fminp( dot( n, sub( p2, p ) ), dot( n, sub( p1, p ) ) );
+			if ( s > polygonSeparation )
+			{
+				polygonSeparation = s;
+				referenceIndex = i;
+			}
+		}
+		if ( polygonSeparation > edgeSeparation )
+		{
+			int ia1 = referenceIndex;
+			int ia2 = ia1 < count - 1 ? ia1 + 1 : 0;
+			v2 a1 = vertices[ia1];
+			v2 a2 = vertices[ia2];
+			v2 n = normals[ia1];
+			float dot1 = dot( n, sub( p1, a1 ) );
+			float dot2 = dot( n, sub( p2, a1 ) );
+			if ( dot1 < dot2 )
+			{
+				if ( dot( n0, n ) < dot( normal1, n ) )
+					return m;
+			}
+			else
+			{
+				if ( dot( n2, n ) < dot( normal1, n ) )
+					return m;
+			}
+			m = clip_segments( a1, a2, p1, p2, normals[ia1], radiusB, 0.0f, MAKE_ID( ia1, 1 ), MAKE_ID( ia2, 0 ) );
+			finish_clip( &m, xfA, xfB, neg( normals[ia1] ) );
+			return m;
+		}
+		if ( incidentIndex == -1 )
+			return m;
+	}
+	v2 b1, b2;
+	int ib1, ib2;
+	if ( incidentNormal != -1 )
+	{
+		ib1 = incidentNormal;
+		ib2 = ib1 < count - 1 ? ib1 + 1 : 0;
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	else
+	{
+		int i2 = incidentIndex;
+		int i1 = i2 > 0 ? i2 - 1 : count - 1;
+		float d1 = dot( normal1, normals[i1] );
+		float d2 = dot( normal1, normals[i2] );
+		if ( d1 < d2 )
+		{
+			ib1 = i1, ib2 = i2;
+			b1 = vertices[ib1];
+			b2 = vertices[ib2];
+		}
+		else
+		{
+			ib1 = i2, ib2 = i2 < count - 1 ? i2 + 1 : 0;
+			b1 = vertices[ib1];
+			b2 = vertices[ib2];
+		}
+	}
+	m = clip_segments( p1, p2, b1, b2, normal1, 0.0f, radiusB, MAKE_ID( 0, ib2 ), MAKE_ID( 1, ib1 ) );
+	finish_clip( &m, xfA, xfB, m.normal );
+	return m;
+}
+
 // contact.c:126-152: the manifold function registry. Returns nonzero when a
 // function exists for (typeA, typeB); *primary is 0 when the pair must be
 // flipped so that A has the registered first type.
@@ -634,14 +1004,15 @@ int p_manifold_registered( int typeA, int typeB, int* primary )
 {
 	// registered (first, second): circle-circle, capsule-circle, capsule-capsule,
 	// polygon-circle, polygon-capsule, polygon-polygon, segment-circle,
-	// segment-capsule, segment-polygon (chain segments are not in this port)
+	// segment-capsule, segment-polygon, chain-circle, chain-capsule,
+	// chain-polygon
 	static const int reg[5][5] = {
 		//            circle capsule segment polygon chain
 		/* circle  */ { 1, 0, 0, 0, 0 },
 		/* capsule */ { 1, 1, 0, 0, 0 },
 		/* segment */ { 1, 1, 0, 1, 0 },
 		/* polygon */ { 1, 1, 0, 1, 0 },
-		/* chain   */ { 0, 0, 0, 0, 0 },
+		/* chain   */ { 1, 1, 0, 1, 0 },
 	};
 	if ( reg[typeA][typeB] )
 	{
@@ -658,7 +1029,7 @@ int p_manifold_registered( int typeA, int typeB, int* primary )
 }
 
 // contact.c:60-124 dispatch (A already has the primary type)
-Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB )
+Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB, SimplexCache* cache )
 {
 	Manifold zero = { 0 };
 	switch ( a->type )
@@ -694,6 +1065,17 @@ Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB )
 				Polygon pa = make_capsule_poly( a->c1, a->c2, 0.0f );
 				return collide_polygons( &pa, xfA, &b->poly, xfB );
 			}
+			break;
+		case SHAPE_CHAIN_SEGMENT:
+			if ( b->type == SHAPE_CIRCLE )
+				return collide_chain_circle( a, xfA, b->c1, b->radius, xfB );
+			if ( b->type == SHAPE_CAPSULE )
+			{
+				Polygon pb = make_capsule_poly( b->c1, b->c2, b->radius );
+				return collide_chain_polygon( a, xfA, &pb, xfB, cache );
+			}
+			if ( b->type == SHAPE_POLYGON )
+				return collide_chain_polygon( a, xfA, &b->poly, xfB, cache );
 			break;
 		default:
 			break;

@@ -36,11 +36,22 @@ typedef struct Polygon
 typedef struct Geometry
 {
 	int type;
-	// circle: c1 = center; capsule: c1, c2, radius; segment: c1, c2
+	// circle: c1 = center; capsule: c1, c2, radius; segment: c1, c2; chain
+	// segment: c1, c2 and the ghost vertices g1 (before c1), g2 (after c2)
 	v2 c1, c2;
 	float radius;
 	Polygon poly;
+	v2 g1, g2;
+	int chainId;
 } Geometry;
+
+// distance.h b2SimplexCache: GJK warm start kept per contact
+typedef struct SimplexCache
+{
+	int count;
+	uint8_t indexA[3];
+	uint8_t indexB[3];
+} SimplexCache;
 
 typedef struct MassData
 {
@@ -158,6 +169,7 @@ typedef struct Contact
 	float friction, restitution, rollingResistance, tangentSpeed;
 	float invMassA, invIA, invMassB, invIB;
 	Manifold m;
+	SimplexCache cache; // chain segment manifolds (contact.h:126)
 	// solver set, island and body edge lists (contact.h:44-96)
 	int setIndex;
 	int islandId, islandPrev, islandNext;
@@ -317,6 +329,13 @@ typedef struct PairSet
 	int count;
 } PairSet;
 
+typedef struct PChain
+{
+	int used, generation, bodyId;
+	int count;
+	int* shapeIds;
+} PChain;
+
 typedef struct World
 {
 	int used;
@@ -346,6 +365,12 @@ typedef struct World
 	int jointCount, jointCap;
 	int* jointFree;
 	int jointFreeCount;
+
+	// chains (shape.c:339-486): the segment shape ids of each chain
+	struct PChain* chains;
+	int chainCount, chainCap;
+	int* chainFree;
+	int chainFreeCount;
 
 	TreeIds trees[3];
 	PairSet pairs;
@@ -444,7 +469,7 @@ void p_shape_extent( const Shape* s, v2 localCenter, float* minExtent, float* ma
 float p_shape_radius( const Geometry* g );
 
 // manifolds (pmanifold.c)
-Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB );
+Manifold p_collide( const Geometry* a, xform xfA, const Geometry* b, xform xfB, SimplexCache* cache );
 int p_manifold_registered( int typeA, int typeB, int* primary );
 
 // distance / time of impact (pdistance.c)
@@ -460,6 +485,8 @@ typedef struct Sweep
 	v2 c1, c2;
 	rot q1, q2;
 } Sweep;
+float p_shape_distance( const ShapeProxy* pa, const ShapeProxy* pb, xform xfA, xform xfB, SimplexCache* cache,
+						v2* pointA, v2* pointB );
 ShapeProxy p_make_proxy( const v2* pts, int count, float radius );
 ShapeProxy p_shape_proxy( const Geometry* g );
 float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sweep sb, float maxFraction, int* state );

@@ -228,6 +228,12 @@ static CastOut ray_shape( const Shape* s, xform xf, v2 origin, v2 translation )
 		case SHAPE_SEGMENT:
 			o = ray_segment( lo, lt, 1.0f, s->g.c1, s->g.c2 );
 			break;
+		case SHAPE_CHAIN_SEGMENT:
+			// geometry.c:718-729: one-sided, rays from the left side pass
+			if ( cross( sub( lo, s->g.c1 ), sub( s->g.c2, s->g.c1 ) ) < 0.0f )
+				return cast_none();
+			o = ray_segment( lo, lt, 1.0f, s->g.c1, s->g.c2 );
+			break;
 		case SHAPE_POLYGON:
 			if ( s->g.poly.radius != 0.0f )
 				return cast_none(); // rounded polygons take the shape-cast path, not restated

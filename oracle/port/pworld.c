@@ -213,6 +213,10 @@ void orc_destroy_world( int wi )
 	free( w->contactFree );
 	free( w->joints );
 	free( w->jointFree );
+	for ( int i = 0; i < w->chainCount; ++i )
+		free( w->chains[i].shapeIds );
+	free( w->chains );
+	free( w->chainFree );
 	for ( int i = 0; i < 3; ++i )
 		free( w->trees[i].freeStack );
 	free( w->pairs.keys );
@@ -491,6 +495,94 @@ int orc_create_segment_shape( int wi, int body, const f2d_shape_def* d, double x
 	g.c1 = V( (float)x1, (float)y1 );
 	g.c2 = V( (float)x2, (float)y2 );
 	return create_shape( p_world( wi ), body, d, &g );
+}
+
+// shape.c:339-486 b2CreateChain: count >= 4 points; a loop makes count
+// segments, an open chain count - 3 (the end points are ghosts only). Each
+// material is six values (friction, restitution, rollingResistance,
+// tangentSpeed, userMaterialId, customColor); one for all segments or one per
+// point, the segment taking its leading point's. The segments use the
+// default shape definition with no contact or hit events and no mass update.
+int orc_create_chain( int wi, int body, const double* points, int count, const double* materials, int materialCount,
+					  long long categoryBits, long long maskBits, int groupIndex, int isLoop, int enableSensorEvents )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || body < 0 || body >= w->bodyCount || count < 4 || count > 1 << 20 ||
+		 ( materialCount != 1 && materialCount != count ) )
+		return -1;
+	int cap = w->chainCap;
+	int id = alloc_id( &w->chainFree, &w->chainFreeCount, &w->chainCount );
+	w->chains = grow( w->chains, &cap, w->chainCount, sizeof( PChain ) );
+	w->chainCap = cap;
+	PChain* ch = w->chains + id;
+	int gen = ch->generation;
+	memset( ch, 0, sizeof( *ch ) );
+	ch->generation = gen + 1;
+	ch->used = 1;
+	ch->bodyId = body;
+	ch->count = isLoop ? count : count - 3;
+	ch->shapeIds = (int*)malloc( sizeof( int ) * (size_t)ch->count );
+	f2d_shape_def d = { 0 };
+	d.density = 1.0;
+	d.categoryBits = categoryBits;
+	d.maskBits = maskBits;
+	d.groupIndex = groupIndex;
+	d.enableSensorEvents = enableSensorEvents != 0;
+	d.invokeContactCreation = 1;
+	d.updateBodyMass = 0;
+	v2* pts = (v2*)malloc( sizeof( v2 ) * (size_t)count );
+	for ( int i = 0; i < count; ++i )
+		pts[i] = V( (float)points[2 * i], (float)points[2 * i + 1] );
+	for ( int k = 0; k < ch->count; ++k )
+	{
+		// ghost1, point1, point2, ghost2 and the material's point index
+		int i0, i1, i2, i3, mi;
+		if ( isLoop )
+		{
+			i0 = ( k + count - 1 ) % count;
+			i1 = k;
+			i2 = ( k + 1 ) % count;
+			i3 = ( k + 2 ) % count;
+			mi = k;
+		}
+		else
+		{
+			i0 = k;
+			i1 = k + 1;
+			i2 = k + 2;
+			i3 = k + 3;
+			mi = k + 1;
+		}
+		const double* m = materials + 6 * ( materialCount == 1 ? 0 : mi );
+		d.friction = m[0];
+		d.restitution = m[1];
+		d.rollingResistance = m[2];
+		d.tangentSpeed = m[3];
+		d.userMaterialId = (int)m[4];
+		Geometry g = { 0 };
+		g.type = SHAPE_CHAIN_SEGMENT;
+		g.g1 = pts[i0];
+		g.c1 = pts[i1];
+		g.c2 = pts[i2];
+		g.g2 = pts[i3];
+		g.chainId = id;
+		ch->shapeIds[k] = create_shape( w, body, &d, &g );
+	}
+	free( pts );
+	return id;
+}
+
+// b2Chain_GetSegments: the chain's segment shape ids in creation order
+int orc_chain_get_segments( int wi, int chain, int* out, int capacity )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || chain < 0 || chain >= w->chainCount || w->chains[chain].used == 0 )
+		return 0;
+	const PChain* ch = w->chains + chain;
+	int n = ch->count < capacity ? ch->count : capacity;
+	for ( int i = 0; i < n; ++i )
+		out[i] = ch->shapeIds[i];
+	return ch->count;
 }
 
 int orc_create_box_shape( int wi, int body, const f2d_shape_def* d, double hx, double hy, double cx, double cy,
@@ -1272,7 +1364,7 @@ static void update_contact( World* w, Contact* c )
 	v2 centerOffsetB = rotate( xfB.q, bb->localCenter );
 
 	Manifold old = c->m;
-	c->m = p_collide( &sa->g, xfA, &sb->g, xfB );
+	c->m = p_collide( &sa->g, xfA, &sb->g, xfB, &c->cache );
 	c->friction = sqrtf( sa->friction * sb->friction );
 	c->restitution = sa->restitution > sb->restitution ? sa->restitution : sb->restitution;
 	if ( sa->rollingResistance > 0.0f || sb->rollingResistance > 0.0f )

@@ -367,6 +367,50 @@ int ref_create_segment_shape( int w, int body, const f2d_shape_def* d, double x1
 	return id.index1 - 1;
 }
 
+int ref_create_chain( int w, int body, const double* points, int count, const double* materials, int materialCount,
+					  long long categoryBits, long long maskBits, int groupIndex, int isLoop, int enableSensorEvents )
+{
+	b2Vec2* pts = (b2Vec2*)malloc( sizeof( b2Vec2 ) * (size_t)count );
+	b2SurfaceMaterial* mats = (b2SurfaceMaterial*)malloc( sizeof( b2SurfaceMaterial ) * (size_t)materialCount );
+	for ( int i = 0; i < count; ++i )
+		pts[i] = ( b2Vec2 ){ (float)points[2 * i], (float)points[2 * i + 1] };
+	for ( int i = 0; i < materialCount; ++i )
+	{
+		const double* m = materials + 6 * i;
+		mats[i] = ( b2SurfaceMaterial ){ 0 };
+		mats[i].friction = (float)m[0];
+		mats[i].restitution = (float)m[1];
+		mats[i].rollingResistance = (float)m[2];
+		mats[i].tangentSpeed = (float)m[3];
+		mats[i].userMaterialId = (int)m[4];
+		mats[i].customColor = (uint32_t)m[5];
+	}
+	b2ChainDef def = b2DefaultChainDef();
+	def.points = pts;
+	def.count = count;
+	def.materials = mats;
+	def.materialCount = materialCount;
+	def.filter.categoryBits = (uint64_t)categoryBits;
+	def.filter.maskBits = (uint64_t)maskBits;
+	def.filter.groupIndex = groupIndex;
+	def.isLoop = isLoop != 0;
+	def.enableSensorEvents = enableSensorEvents != 0;
+	b2ChainId id = b2CreateChain( ref_body_id( w, body ), &def );
+	free( pts );
+	free( mats );
+	return id.index1 - 1;
+}
+
+int ref_chain_get_segments( int w, int chain, int* out, int capacity )
+{
+	b2World* world = ref_world( w );
+	b2ChainShape* ch = world->chainShapes.data + chain;
+	int n = ch->count < capacity ? ch->count : capacity;
+	for ( int i = 0; i < n; ++i )
+		out[i] = ch->shapeIndices[i];
+	return ch->count;
+}
+
 int ref_create_box_shape( int w, int body, const f2d_shape_def* d, double hx, double hy, double cx, double cy,
 						  double c, double s, double radius )
 {

@@ -39,6 +39,8 @@ CASES = {
                        checkpoints=[1, 64, 256]),
     "joint_rigs_sleep": dict(world=dict(enableSleep=1), scene=("joint_rigs", dict()), frames=300,
                              checkpoints=[1, 100, 200, 300]),
+    "chain_terrain": dict(world=dict(enableSleep=0, enableContinuous=0), scene=("chain_terrain", dict(count=300)),
+                          frames=256, checkpoints=[1, 64, 256]),
     # sleeping on: islands, sleeping solver sets, island splits
     "pyramid_sleep": dict(world=dict(enableSleep=1), scene=("pyramid", dict(rows=12)), frames=120,
                           checkpoints=[1, 30, 44, 60, 120]),

@@ -95,6 +95,40 @@ def test_queries_match_oracle_on_moving_pile(gpu_lib, port_lib):
     p.close()
 
 
+def test_chain_queries_match_oracle(gpu_lib, port_lib):
+    """Chain segments: the segment ids of each chain, and ray casts that
+    pass one-sided segments from behind, against the oracle."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    from forge2d_gb300.world import GpuWorld
+    g = GpuWorld(scenes.world_def(**wkw))
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(g, "chain_terrain", count=150)
+    scenes.build(p, "chain_terrain", count=150)
+    ch = g.create_chain(g.create_body(scenes.body_def(type=scenes.STATIC)), [(0, 0), (1, 0), (2, 0), (3, 1)])
+    segs = g.chain_segments(ch)
+    assert len(segs) == 1 and g.lib.f2d_shape_get_type(*segs[0]) == 4
+    rng = np.random.default_rng(3)
+    hits = 0
+    for f in range(1, 41):
+        g.step(1.0 / 60.0, 4)
+        p.step(1.0 / 60.0, 4)
+        if f % 10:
+            continue
+        for _ in range(40):
+            o = rng.uniform(-24, 24, 2) + np.array([0.0, 20.0])
+            t = rng.uniform(-30, 30, 2)
+            a = g.cast_ray_closest(o[0], o[1], t[0], t[1])
+            b = p.cast_ray_closest(o[0], o[1], t[0], t[1])
+            assert (a is None) == (b is None)
+            if a is not None:
+                hits += 1
+                assert a[0] == b[0]
+                assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+    assert hits > 50
+    g.close()
+    p.close()
+
+
 def test_body_accessors_and_impulses(gpu_lib):
     from forge2d_gb300.world import World
     w = World(gravity=(0.0, 0.0))

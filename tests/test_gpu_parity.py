@@ -59,6 +59,10 @@ NATIVE = [
     ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=8), 400, 25),
     # prismatic lifts and springs, wheeled carts, motor, mouse and filter joints
     ("joint_rigs", dict(enableSleep=0), "joint_rigs", dict(copies=8), 400, 25),
+    # chain shapes (one-sided segments, GJK-cached manifolds), with and
+    # without continuous collision
+    ("chain_terrain", dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(count=600), 300, 25),
+    ("chain_terrain_ccd", dict(enableSleep=0, enableContinuous=1), "chain_terrain", dict(count=600), 300, 25),
     ("batched24", dict(enableSleep=0, enableContinuous=1), "batched", dict(worlds=24, seed=3), 200, 25),
     # overflow constraints solved by levels: a 150-deep chain (past the
     # parallel levels, into the serial tail), overflow joints, and many

@@ -56,6 +56,7 @@ SCENES = [
     # weld and distance joints link islands and sleep with them
     ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
     ("joint_rigs_sleep", dict(enableSleep=1), "joint_rigs", dict(copies=3), 400),
+    ("chain_terrain_sleep", dict(enableSleep=1, enableContinuous=1), "chain_terrain", dict(count=200), 500),
 ]
 
 

@@ -27,6 +27,7 @@ CASES = {
     "joint_zoo": (dict(enableSleep=0), "joint_zoo", dict()),
     "joint_rigs": (dict(enableSleep=0), "joint_rigs", dict()),
     "joint_rigs_sleep": (dict(enableSleep=1), "joint_rigs", dict()),
+    "chain_terrain": (dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(count=300)),
     "pyramid_sleep": (dict(enableSleep=1), "pyramid", dict(rows=12)),
     "pile_sleep": (dict(enableSleep=1, enableContinuous=1), "pile", dict(count=300, seed=3, width=20.0, height=30.0)),
 }

@@ -43,6 +43,10 @@ SCENES = [
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400),
     ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=4), 400),
     ("joint_rigs", dict(enableSleep=0), "joint_rigs", dict(copies=4), 400),
+    # chain shapes: one-sided segments with ghost vertices (continuous off:
+    # with it on, a fast body meeting several segments at once visits them in
+    # the reference's static-tree order, the restatement in shape-id order)
+    ("chain_terrain", dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(), 300),
 ]
 
 
@@ -70,6 +74,7 @@ SLEEP_SCENES = [
     ("chains_sleep", dict(enableSleep=1), "pyramids_chains", dict(pyramids=2, rows=6, chains=4, links=10), 400),
     ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
     ("joint_rigs_sleep", dict(enableSleep=1), "joint_rigs", dict(copies=3), 400),
+    ("chain_terrain_sleep", dict(enableSleep=1, enableContinuous=0), "chain_terrain", dict(count=200), 500),
 ]
 
 
@@ -106,6 +111,34 @@ def test_port_sleep_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene,
     lockstep_full(ref, port, frames)
     if name in ("pyramid_sleep", "pile_sleep"):
         assert ref.awake_body_count() == 0
+    ref.close()
+    port.close()
+
+
+CHAIN_RAYS = [
+    # (origin, translation): down onto the floor, up through the floor's back
+    # (one-sided: no hit on it), across the ramp from both sides
+    ((0.3, 30.0), (0.0, -40.0)), ((5.0, -3.0), (0.0, 60.0)), ((-21.0, 12.0), (42.0, 0.5)),
+    ((12.0, 30.0), (0.0, -25.0)), ((12.0, 10.0), (0.0, 10.0)), ((-30.0, 5.0), (60.0, 0.0)),
+]
+
+
+def test_port_chain_queries_with_reference(ref_lib, port_lib):
+    """Chain segment ids and one-sided ray casts (b2RayCastSegment with
+    oneSided) agree with the reference after the pile has settled a little."""
+    wkw = dict(enableSleep=0, enableContinuous=0)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, "chain_terrain", count=100)
+    scenes.build(port, "chain_terrain", count=100)
+    for c in (0, 1):
+        assert np.array_equal(ref.chain_segments(c), port.chain_segments(c))
+    assert len(ref.chain_segments(0)) == 51 and len(ref.chain_segments(1)) == 6
+    lockstep_full(ref, port, 60)
+    for o, t in CHAIN_RAYS:
+        rs, rf = ref.cast_ray_closest(o[0], o[1], t[0], t[1])
+        ps, pf = port.cast_ray_closest(o[0], o[1], t[0], t[1])
+        assert rs == ps and np.array_equal(rf.view(np.uint32), pf.view(np.uint32)), (o, t)
     ref.close()
     port.close()
 
