@@ -34,6 +34,7 @@
 #define SF_ENLARGED 0x20
 #define SF_MOVED 0x40
 #define SF_PROXY 0x80 // has a broadphase proxy
+#define SF_SENSOR_EVENTS 0x100 // enableSensorEvents
 #define SF_TYPE_SHIFT 16
 
 // shape types (b2ShapeType)
@@ -122,7 +123,8 @@ struct DScalars
 	int npCount[8];	   // narrowphase: live overlapping contacts per manifold class
 	int pendingOps;	   // colouring: ops left after the first round
 	int overflowOps;   // colouring: ops that add to / remove from the overflow colour
-	int pad[2];
+	int sensorCur, sensorPrev;	   // sensor overlaps this step / last step
+	int sensorBegin, sensorEnd;	   // sensor events of this step
 };
 
 // ---------------------------------------------------------------------------
@@ -388,6 +390,12 @@ struct DWorld
 	int* moveEvBody;
 	float4* moveEvXf;
 	int* staticShapes; // compact list of static proxies (CCD candidates)
+	// sensors (sensor.c): sensor shapes in creation order; sorted overlap keys
+	// (sensor index << 32 | visitor shape) of this step and the last; events
+	int* sensorShapes;
+	int sensorCount, sensorPairCap;
+	unsigned long long *sensorKeys, *sensorKeysAlt, *sensorPrevKeys;
+	int2 *sensorBeginEv, *sensorEndEv; // (sensor shape, visitor shape)
 	int staticCount;
 
 	DScalars* sc;

@@ -50,6 +50,7 @@ void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st );
 void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st );
 void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps );
 void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
+void launch_sensors( DWorld& w, StepScratch& s, cudaStream_t st );
 void launch_joint_ops( DWorld& w, cudaStream_t st );
 int solver_max_blocks( int threads );
 // islands and sleeping (island.cu; worlds with sleeping enabled)

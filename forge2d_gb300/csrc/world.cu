@@ -86,6 +86,8 @@ struct HostWorld
 	std::vector<int> shapeDirty;
 	TreeIds trees[3];
 	std::vector<int> staticShapes;
+	std::vector<int> sensorShapes; // sensor shapes in creation order (sensor.c)
+	bool sensorsDirty = false;
 	// chains: segment shape ids and generation per chain id (LIFO id reuse)
 	std::vector<std::vector<int>> chainSegments;
 	std::vector<uint16_t> chainGen;
@@ -710,6 +712,31 @@ static void flush_uploads( HostWorld* W )
 		up( d.jdef3, W->jdef3, j, j + 1, W->stream );
 	}
 	W->jointDirty.clear();
+	if ( W->sensorsDirty )
+	{
+		// sensor list and overlap buffers; the overlaps of the last step survive
+		DWorld& d = W->d;
+		int S = (int)W->sensorShapes.size();
+		int cap = std::max( 1 << 14, 128 * S );
+		if ( d.sensorShapes )
+			dfree( d.sensorShapes );
+		cudaMalloc( (void**)&d.sensorShapes, sizeof( int ) * (size_t)S );
+		cudaMemcpyAsync( d.sensorShapes, W->sensorShapes.data(), sizeof( int ) * (size_t)S, cudaMemcpyHostToDevice,
+						 W->stream );
+		if ( cap > d.sensorPairCap )
+		{
+			size_t o = (size_t)d.sensorPairCap;
+			dgrow( d.sensorPrevKeys, o, cap );
+			dgrow( d.sensorKeys, 0, cap );
+			dgrow( d.sensorKeysAlt, 0, cap );
+			dgrow( d.sensorBeginEv, 0, cap );
+			dgrow( d.sensorEndEv, 0, cap );
+			d.sensorPairCap = cap;
+		}
+		d.sensorCount = S;
+		W->sensorsDirty = false;
+		W->graphDirty = true;
+	}
 	if ( W->staticDirty )
 	{
 		if ( !W->staticShapes.empty() )
@@ -833,7 +860,8 @@ static void free_world( HostWorld* W )
 	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 ); F( jdef3 );
 	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprep3 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
-	F( moveEvXf ); F( staticShapes ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
+	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
+	F( sensorBeginEv ); F( sensorEndEv ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F
 	dfree( W->s.tmpA );
 	dfree( W->s.tmpB );
@@ -1133,6 +1161,13 @@ static int create_shape( HostWorld* W, int b, const f2d_shape_def* def, const HS
 		flags |= SF_HIT_EVENTS;
 	if ( def->enablePreSolveEvents )
 		flags |= SF_PRESOLVE;
+	if ( def->enableSensorEvents )
+		flags |= SF_SENSOR_EVENTS;
+	if ( def->isSensor )
+	{
+		W->sensorShapes.push_back( id );
+		W->sensorsDirty = true;
+	}
 	int pkey = F2D_NULL;
 	fbox aabb, fat;
 	aabb.lo = aabb.hi = mk( 0.0f, 0.0f );
@@ -1634,6 +1669,7 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	if ( prof )
 		cudaEventRecord( W->ph[5], W->stream );
 	launch_finalize( d, W->s, W->stream, dt );
+	launch_sensors( d, W->s, W->stream );
 	if ( prof )
 		cudaEventRecord( W->ph[6], W->stream );
 	W->s.evSolveStart = nullptr;
@@ -2674,6 +2710,28 @@ static int read_pairs( HostWorld* W, const int* dptr, int count, int32_t* out4, 
 		out4[4 * i + 3] = pack_wg( W, W->sgen[b] );
 	}
 	return n;
+}
+
+// b2World_GetSensorEvents (world.c:1505-1527; RawBox2D.worldGetSensorEvents, raw_box2d.dart:1295):
+// this step's begin events (sensor shape, visitor shape) as id pairs, four
+// ints per event; the end events likewise into end4, their count in
+// *endCount. Returns the begin count.
+extern "C" F2D_API int32_t f2d_world_get_sensor_events( int32_t worldId, int32_t* begin4, int32_t* end4, int32_t cap,
+														 int32_t* endCount )
+{
+	if ( endCount )
+		*endCount = 0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped || W->d.sensorCount == 0 )
+		return 0;
+	cudaStreamSynchronize( W->stream );
+	DScalars sc;
+	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	int nb = read_pairs( W, (const int*)W->d.sensorBeginEv, sc.sensorBegin, begin4, cap );
+	int ne = read_pairs( W, (const int*)W->d.sensorEndEv, sc.sensorEnd, end4, cap );
+	if ( endCount )
+		*endCount = ne;
+	return nb;
 }
 
 extern "C" F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int32_t cap )

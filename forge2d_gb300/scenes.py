@@ -134,7 +134,7 @@ def _polygon_points(rng, n, radius):
 
 def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
          frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False,
-         enable_contact_events=False, filters=False):
+         enable_contact_events=False, filters=False, sensor_visitors=False):
     """The mixed pile: ``count`` bodies drawn from ``seed`` -- 40% circles
     r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
     30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
@@ -144,7 +144,8 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
     1, 2, 4 in turn, every 5th shape's mask excludes the next category,
     every 7th shape is in group -1 (never collides within the group), every
     11th in group 2 (always collides within the group), every 13th is a
-    sensor."""
+    sensor. ``sensor_visitors`` turns on sensor events for three shapes in
+    four, in categories 1 and 2 alternately."""
     rng = np.random.default_rng(seed)
     hw = 0.5 * width
     if wall_height is None:
@@ -177,6 +178,9 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
                 extra["groupIndex"] = 2
             if k % 13 == 0:
                 extra["isSensor"] = 1
+        if sensor_visitors:
+            extra["enableSensorEvents"] = int(k % 4 != 0)
+            extra["categoryBits"] = 1 << (k % 2)
         sd = shape_def(restitution=float(rest[k]), enableHitEvents=int(enable_hit_events),
                        enableContactEvents=int(enable_contact_events), **extra)
         u = kinds[k]
@@ -384,6 +388,30 @@ def chain_terrain(b, count=400, seed=5, width=40.0, height=40.0, bumps=6, materi
     return pile(b, count=count, seed=seed, width=width - 2.0, height=height, with_container=False)
 
 
+def sensor_field(b, count=300, seed=8, width=30.0, height=40.0):
+    """Sensor shapes: four static sensor zones across the container (one
+    masks out category 2, one has its events off), a kinematic body sweeping
+    a sensor circle through the pile, and a falling box carrying a larger
+    sensor circle on its own body; the mixed pile's shapes (``count`` from
+    ``seed``) as visitors, three in four with sensor events on."""
+    hw = 0.5 * width
+    zones = b.create_body(body_def(type=STATIC))
+    for i in range(4):
+        x = -hw + width * (i + 0.5) / 4.0
+        extra = {}
+        if i == 1:
+            extra["maskBits"] = -1 ^ 2
+        b.create_box(zones, shape_def(isSensor=1, enableSensorEvents=int(i != 3), **extra), 2.5, 1.5 + i,
+                     x, 4.0 + 2.0 * i, 1.0, 0.0, 0.0)
+    sweeper = b.create_body(body_def(type=KINEMATIC, positionX=-hw, positionY=3.0, linearVelocityX=3.0,
+                                     angularVelocity=0.5))
+    b.create_circle(sweeper, shape_def(isSensor=1, enableSensorEvents=1), 0.0, 0.0, 2.0)
+    carrier = b.create_body(body_def(type=DYNAMIC, positionX=0.3, positionY=height + 8.0))
+    b.create_box(carrier, shape_def(enableSensorEvents=1), 0.6, 0.6)
+    b.create_circle(carrier, shape_def(isSensor=1, enableSensorEvents=1), 0.0, 0.0, 1.8)
+    return pile(b, count=count, seed=seed, width=width, height=height, sensor_visitors=True)
+
+
 def joint_rigs(b, copies=3):
     """Prismatic, wheel, motor, mouse and filter joints, ``copies`` times over
     a ground box: an elevator (vertical prismatic with limits and a motor)
@@ -527,4 +555,6 @@ def build(b, name, **kw):
         return joint_rigs(b, **kw)
     if name == "chain_terrain":
         return chain_terrain(b, **kw)
+    if name == "sensor_field":
+        return sensor_field(b, **kw)
     raise ValueError(name)

@@ -159,6 +159,16 @@ class GpuWorld:
                                        C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def sensor_events(self):
+        """This step's sensor (begin, end) events as (sensor shape, visitor
+        shape) rows of 0-based shape ids, in the order they were produced."""
+        cap = 1 << 16
+        b = np.zeros((cap, 4), np.int32)
+        e = np.zeros((cap, 4), np.int32)
+        ne = C.c_int32(0)
+        nb = self.lib.f2d_world_get_sensor_events(self.id, _iptr(b), _iptr(e), cap, C.byref(ne))
+        return b[:nb][:, [0, 2]] - 1, e[:ne.value][:, [0, 2]] - 1
+
     def chain_segments(self, chain):
         out = np.zeros(2 * (1 << 16), np.int32)
         n = self.lib.f2d_chain_get_segments(chain[0], chain[1], _iptr(out), len(out) // 2)

@@ -325,6 +325,12 @@ F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* counts4 );
 /* Begin / end touch events as shape id pairs (index1, worldAndGeneration) x 2
  * = 4 ints per event. Return the number written. */
 F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int32_t capacity );
+/* RawBox2D.worldGetSensorEvents (raw_box2d.dart:1295 -> b2World_GetSensorEvents, world.c:1505):
+ * begin and end events of the last step, four ints each (sensor index1,
+ * worldAndGeneration, visitor index1, worldAndGeneration); returns the begin
+ * count, the end count in *endCount. */
+F2D_API int32_t f2d_world_get_sensor_events( int32_t worldId, int32_t* begin4, int32_t* end4, int32_t capacity,
+											 int32_t* endCount );
 F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* out4, int32_t capacity );
 /* Hit events: 4 ints (shape ids) and 5 floats (point.xy normal.xy approachSpeed). */
 F2D_API int32_t f2d_world_get_hit_events( int32_t worldId, int32_t* ints4, float* floats5, int32_t capacity );

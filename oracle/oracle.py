@@ -148,6 +148,7 @@ def _bind(lib, prefix):
         "create_segment_shape": (i, [i, i, _P(ShapeDef), d, d, d, d]),
         "create_chain": (i, [i, i, _P(d), i, _P(d), i, C.c_longlong, C.c_longlong, i, i, i]),
         "chain_get_segments": (i, [i, i, _P(i), i]),
+        "get_sensor_events": (i, [i, _P(i), _P(i), i, _P(i)]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
         "create_revolute_joint": (i, [i, _P(RevoluteDef)]),
@@ -240,6 +241,17 @@ class _CpuWorld:
         return self._fns["create_chain"](self.w, body, pts.ctypes.data_as(_P(C.c_double)), len(pts) // 2,
                                          mats.ctypes.data_as(_P(C.c_double)), len(mats) // 6, categoryBits,
                                          maskBits, groupIndex, int(isLoop), int(enableSensorEvents))
+
+    def sensor_events(self):
+        """This step's sensor (begin, end) events as (sensor shape, visitor
+        shape) rows, in the order they were produced."""
+        cap = 1 << 16
+        b = np.zeros((cap, 2), np.int32)
+        e = np.zeros((cap, 2), np.int32)
+        ne = C.c_int(0)
+        nb = self._fns["get_sensor_events"](self.w, b.ctypes.data_as(_P(C.c_int)), e.ctypes.data_as(_P(C.c_int)),
+                                             cap, C.byref(ne))
+        return b[:nb].copy(), e[:ne.value].copy()
 
     def chain_segments(self, chain):
         out = np.zeros(1 << 16, np.int32)

@@ -144,6 +144,7 @@ typedef struct Shape
 	int proxyKey;
 	v2 localCentroid;
 	int nextShape, prevShape;
+	int sensorIndex; // P_NULL unless a sensor
 } Shape;
 
 enum
@@ -428,7 +429,20 @@ typedef struct World
 	int splitIslandId;
 	int* moveEventAsleep; // fellAsleep flag per move event
 	int moveEventAsleepCap;
+	// sensors (sensor.c): sensor shapes in creation order with their sorted
+	// overlaps of the previous and the current step; this step's events as
+	// (sensor shape, visitor shape) pairs
+	struct PSensor* sensors;
+	int sensorCount, sensorCap;
+	IntArr sensorBegin, sensorEnd;
 } World;
+
+typedef struct PSensor
+{
+	int shapeId;
+	IntArr overlaps1, overlaps2; // visitor shape ids, ascending
+} PSensor;
+void p_overlap_sensors( World* w ); // psensor.c
 
 // islands and solver sets (pisland.c)
 void ia_push( IntArr* a, int v );

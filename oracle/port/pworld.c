@@ -217,6 +217,14 @@ void orc_destroy_world( int wi )
 		free( w->chains[i].shapeIds );
 	free( w->chains );
 	free( w->chainFree );
+	for ( int i = 0; i < w->sensorCount; ++i )
+	{
+		ia_free( &w->sensors[i].overlaps1 );
+		ia_free( &w->sensors[i].overlaps2 );
+	}
+	free( w->sensors );
+	ia_free( &w->sensorBegin );
+	ia_free( &w->sensorEnd );
 	for ( int i = 0; i < 3; ++i )
 		free( w->trees[i].freeStack );
 	free( w->pairs.keys );
@@ -456,6 +464,18 @@ static int create_shape( World* w, int bodyId, const f2d_shape_def* d, const Geo
 		int force = d->invokeContactCreation != 0 || d->isSensor != 0;
 		if ( proxyType != BODY_STATIC || force )
 			push_move( w, id );
+	}
+	s->sensorIndex = P_NULL;
+	if ( s->isSensor )
+	{
+		// shape.c:144-156: a sensor record per sensor shape
+		int cap = w->sensorCap;
+		w->sensors = grow( w->sensors, &cap, w->sensorCount + 1, sizeof( PSensor ) );
+		w->sensorCap = cap;
+		PSensor* sn = w->sensors + w->sensorCount;
+		memset( sn, 0, sizeof( *sn ) );
+		sn->shapeId = id;
+		s->sensorIndex = w->sensorCount++;
 	}
 	if ( b->headShape != P_NULL )
 		w->shapes[b->headShape].prevShape = id;
@@ -1644,6 +1664,8 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	// end events are double-buffered in the reference and reported for the
 	// step that produced them; this port clears them at step start
 	w->endCount = 0;
+	w->sensorBegin.count = 0;
+	w->sensorEnd.count = 0;
 	float dt = (float)timeStep;
 	if ( dt == 0.0f )
 		return;
@@ -1662,6 +1684,21 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	g_portPhase[1] += t2 - t1;
 	g_portPhase[2] += t3 - t2;
 	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
+	p_overlap_sensors( w );
+}
+
+// b2World_GetSensorEvents: begin and end (sensor shape, visitor shape) pairs
+// of the last step; returns the begin count, the end count in *endCount
+int orc_get_sensor_events( int wi, int* begin, int* end, int cap, int* endCount )
+{
+	World* w = p_world( wi );
+	int nb = w->sensorBegin.count / 2, ne = w->sensorEnd.count / 2;
+	for ( int i = 0; i < 2 * nb && i < 2 * cap; ++i )
+		begin[i] = w->sensorBegin.data[i];
+	for ( int i = 0; i < 2 * ne && i < 2 * cap; ++i )
+		end[i] = w->sensorEnd.data[i];
+	*endCount = ne;
+	return nb;
 }
 
 double orc_world_step_timed( int wi, double dt, int subSteps, int steps )

@@ -591,6 +591,23 @@ void ref_mouse_joint_set_target( int w, int j, double x, double y )
 	b2MouseJoint_SetTarget( id, ( b2Vec2 ){ (float)x, (float)y } );
 }
 
+int ref_get_sensor_events( int w, int* begin, int* end, int cap, int* endCount )
+{
+	b2SensorEvents ev = b2World_GetSensorEvents( s_worlds[w] );
+	for ( int i = 0; i < ev.beginCount && i < cap; ++i )
+	{
+		begin[2 * i] = ev.beginEvents[i].sensorShapeId.index1 - 1;
+		begin[2 * i + 1] = ev.beginEvents[i].visitorShapeId.index1 - 1;
+	}
+	for ( int i = 0; i < ev.endCount && i < cap; ++i )
+	{
+		end[2 * i] = ev.endEvents[i].sensorShapeId.index1 - 1;
+		end[2 * i + 1] = ev.endEvents[i].visitorShapeId.index1 - 1;
+	}
+	*endCount = ev.endCount;
+	return ev.beginCount;
+}
+
 // ---------------------------------------------------------------------------
 // State dumps
 // ---------------------------------------------------------------------------

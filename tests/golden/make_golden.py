@@ -41,6 +41,9 @@ CASES = {
                              checkpoints=[1, 100, 200, 300]),
     "chain_terrain": dict(world=dict(enableSleep=0, enableContinuous=0), scene=("chain_terrain", dict(count=300)),
                           frames=256, checkpoints=[1, 64, 256]),
+    # sensor events every frame (rows: frame, sensor shape, visitor shape)
+    "sensor_field": dict(world=dict(enableSleep=1, enableContinuous=1), scene=("sensor_field", dict()), frames=300,
+                         checkpoints=[1, 100, 300], sensors=True),
     # sleeping on: islands, sleeping solver sets, island splits
     "pyramid_sleep": dict(world=dict(enableSleep=1), scene=("pyramid", dict(rows=12)), frames=120,
                           checkpoints=[1, 30, 44, 60, 120]),
@@ -57,8 +60,12 @@ def record(name, spec):
     prev = set()
     plan_rows = []
     out = {}
+    sensor_rows = ([], [])
     for f in range(1, spec["frames"] + 1):
         w.step(1.0 / 60.0, 4)
+        if spec.get("sensors"):
+            for rows, ev in zip(sensor_rows, w.sensor_events()):
+                rows.extend((f, int(r[0]), int(r[1])) for r in ev)
         ints, fl = w.contacts()
         cur = set((int(a), int(b), int(c)) for a, b, c in ints[:, :3])
         for row in sorted(cur - prev):
@@ -75,6 +82,9 @@ def record(name, spec):
                 out["contact_ints_%d" % f] = ints.copy()
                 out["contact_floats_%d" % f] = fl.copy()
     out["plan"] = np.array(plan_rows, np.int32).reshape(-1, 4)
+    if spec.get("sensors"):
+        out["sensor_begin"] = np.array(sensor_rows[0], np.int32).reshape(-1, 3)
+        out["sensor_end"] = np.array(sensor_rows[1], np.int32).reshape(-1, 3)
     out["checkpoints"] = np.array(spec["checkpoints"], np.int32)
     np.savez_compressed(os.path.join(HERE, name + "_ref.npz"), **out)
     w.close()

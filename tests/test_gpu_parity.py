@@ -17,7 +17,8 @@ import pytest
 from forge2d_gb300 import scenes
 
 from parity import compare_contacts
-from test_oracle_golden import CASES, GOLD, STATS_CASES, check_sets, frame_stats, replay
+from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
+                                replay, sensor_rows)
 
 pytestmark = pytest.mark.gpu
 
@@ -99,6 +100,29 @@ def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, fra
     p.close()
 
 
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_sensor_events_match_port(gpu_lib, port_lib, sleep):
+    """Sensor begin / end events of every frame, in order, against the
+    oracle (native contact order)."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(g, "sensor_field", count=500)
+    scenes.build(p, "sensor_field", count=500)
+    totals = [0, 0]
+    for f in range(1, 301):
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
+        for k, (a, b) in enumerate(zip(g.sensor_events(), p.sensor_events())):
+            assert np.array_equal(a, b), (f, k, a[:4], b[:4])
+            totals[k] += len(a)
+    assert totals[0] > 100 and totals[1] > 50, totals
+    assert g.sync() == 0
+    g.close()
+    p.close()
+
+
 def test_gpu_events_match_port(gpu_lib, port_lib):
     wkw = dict(enableSleep=0, enableContinuous=1)
     kw = dict(count=300, seed=21, width=16.0, height=24.0, enable_hit_events=True, enable_contact_events=True)
@@ -138,8 +162,11 @@ def test_gpu_replays_reference_fixture_bit_exact(gpu_lib, name):
     checks = set(int(c) for c in gold["checkpoints"])
     first = int(gold["checkpoints"][0])
     seen = []
+    rows = ([], [])
 
     def on_frame(f):
+        if name in SENSOR_CASES:
+            sensor_rows(g, f, rows)
         if f not in checks:
             return
         full = g.bodies()
@@ -158,6 +185,8 @@ def test_gpu_replays_reference_fixture_bit_exact(gpu_lib, name):
 
     replay(g, name, on_frame=on_frame)
     assert sorted(seen) == sorted(checks)
+    if name in SENSOR_CASES:
+        check_sensor_rows(rows, gold)
     g.close()
 
 

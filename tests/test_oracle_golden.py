@@ -28,6 +28,7 @@ CASES = {
     "joint_rigs": (dict(enableSleep=0), "joint_rigs", dict()),
     "joint_rigs_sleep": (dict(enableSleep=1), "joint_rigs", dict()),
     "chain_terrain": (dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(count=300)),
+    "sensor_field": (dict(enableSleep=1, enableContinuous=1), "sensor_field", dict()),
     "pyramid_sleep": (dict(enableSleep=1), "pyramid", dict(rows=12)),
     "pile_sleep": (dict(enableSleep=1, enableContinuous=1), "pile", dict(count=300, seed=3, width=20.0, height=30.0)),
 }
@@ -69,6 +70,21 @@ def replay(world, name, frames=None, on_frame=None):
         if on_frame is not None:
             on_frame(f)
     return gold
+
+
+SENSOR_CASES = ("sensor_field",)
+
+
+def sensor_rows(world, f, rows):
+    """Appends this step's sensor events as (frame, sensor, visitor) rows."""
+    for out, ev in zip(rows, world.sensor_events()):
+        out.extend((f, int(r[0]), int(r[1])) for r in ev)
+
+
+def check_sensor_rows(rows, gold):
+    for out, key in zip(rows, ("sensor_begin", "sensor_end")):
+        got = np.array(out, np.int32).reshape(-1, 3)
+        assert np.array_equal(got, gold[key]), key
 
 
 def check_sets(full_rows, gold, f):
@@ -167,4 +183,16 @@ def test_port_queries_match_reference(port_lib):
     w.create_circle(c2, scenes.shape_def(), 0.0, 0.0, 0.5)
     assert s1 == gold["overlap"]["inside"]
     assert sorted(int(x) for x in w.overlap_aabb(-6.0, 4.0, -4.0, 6.0)) == gold["overlap"]["result"]
+    w.close()
+
+
+@pytest.mark.parametrize("name", SENSOR_CASES)
+def test_port_sensor_events_match_fixture(port_lib, name):
+    """Sensor begin and end events of every frame, in the reference's order
+    (sensors in creation order, visitors by shape id)."""
+    w = make_port(port_lib, name)
+    rows = ([], [])
+    gold = replay(w, name, on_frame=lambda f: sensor_rows(w, f, rows))
+    assert len(gold["sensor_begin"]) > 50 and len(gold["sensor_end"]) > 20
+    check_sensor_rows(rows, gold)
     w.close()

@@ -115,6 +115,27 @@ def test_port_sleep_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene,
     port.close()
 
 
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_sensor_events_with_reference(ref_lib, port_lib, sleep):
+    """b2OverlapSensors: every frame's sensor begin and end events, in order
+    (static zones, a masked zone, a zone with events off, a kinematic sweeper,
+    a sensor riding a falling body; visitors with and without events)."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, "sensor_field")
+    scenes.build(port, "sensor_field")
+    totals = [0, 0]
+    for f in range(1, 301):
+        lockstep_full(ref, port, 1, start=f)
+        for k, (a, b) in enumerate(zip(ref.sensor_events(), port.sensor_events())):
+            assert np.array_equal(a, b), (f, k)
+            totals[k] += len(a)
+    assert totals[0] > 100 and totals[1] > 50, totals
+    ref.close()
+    port.close()
+
+
 CHAIN_RAYS = [
     # (origin, translation): down onto the floor, up through the floor's back
     # (one-sided: no hit on it), across the ramp from both sides
