@@ -581,7 +581,8 @@ __global__ void k_after_create( DWorld w, int planMode )
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
-void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode )
+void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode, HostHook pairHook,
+						void* hookContext )
 {
 	int gridS = grid_for( w.shapeCount );
 	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, st>>>( w );
@@ -602,6 +603,9 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	// new pair keys are unique, so the key order alone fixes the result
 	sort_coop<unsigned long long>( w.pairKeys, nullptr, w.pairKeysAlt, nullptr, &w.sc->newPairCount, bits, w.sortHist,
 								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
+	// broad_phase.c:267-278: the custom filter sees the new pairs last
+	if ( pairHook )
+		pairHook( hookContext );
 	k_create_contacts<<<grid_for( w.pairCap ), BP_THREADS, 0, st>>>( w, planMode );
 	if ( w.isl )
 		launch_isl_new_contacts( w, st, planMode );

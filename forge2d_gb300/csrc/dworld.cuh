@@ -125,6 +125,7 @@ struct DScalars
 	int overflowOps;   // colouring: ops that add to / remove from the overflow colour
 	int sensorCur, sensorPrev;	   // sensor overlaps this step / last step
 	int sensorBegin, sensorEnd;	   // sensor events of this step
+	int cbList, cbReject;		   // user callbacks: listed candidates, rejected keys
 };
 
 // ---------------------------------------------------------------------------
@@ -396,6 +397,15 @@ struct DWorld
 	int sensorCount, sensorPairCap;
 	unsigned long long *sensorKeys, *sensorKeysAlt, *sensorPrevKeys;
 	int2 *sensorBeginEv, *sensorEndEv; // (sensor shape, visitor shape)
+	// user callbacks (custom filter, pre-solve), evaluated on the host
+	// between launches: candidates the device lists for the host
+	// (continuous pairs static << 32 | fast; pre-solve contact ids with
+	// their manifolds), and the sorted keys the host rejected
+	int callbacks;	 // bit 0 custom filter, bit 1 pre-solve
+	int cbCap;
+	unsigned long long* cbList;
+	float* cbManifold; // 22 per listed pre-solve contact: f2d_manifold_view, shape A, shape B
+	unsigned long long* cbReject;
 	int staticCount;
 
 	DScalars* sc;

@@ -233,7 +233,24 @@ __device__ __forceinline__ bool joint_allows( const DWorld& w, int ia, int ib )
 #define CCD_LIST_MAX 64
 #define CCD_CANDIDATES 32
 
-__global__ void k_continuous( DWorld w )
+__device__ __forceinline__ bool ccd_rejected( const DWorld& w, unsigned long long key )
+{
+	int lo = 0, hi = w.sc->cbReject;
+	while ( lo < hi )
+	{
+		int mid = ( lo + hi ) >> 1;
+		if ( w.cbReject[mid] < key )
+			lo = mid + 1;
+		else
+			hi = mid;
+	}
+	return lo < w.sc->cbReject && w.cbReject[lo] == key;
+}
+
+// listOnly: with a custom filter, a first pass lists the (static shape,
+// fast shape) candidates that reach the filter (solver.c:270-280) for the
+// host and changes nothing; the second pass skips the ones it rejected.
+__global__ void k_continuous( DWorld w, int listOnly )
 {
 	int n = w.sc->fastCount;
 	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
@@ -266,7 +283,8 @@ __global__ void k_continuous( DWorld w )
 			fbox box1 = box_from4( w.aabb[fs] );
 			fbox box2 = shape_aabb( gf, tf, xf2 );
 			fbox box = box_union( box1, box2 );
-			w.aabb[fs] = box_to4( box2 );
+			if ( !listOnly )
+				w.aabb[fs] = box_to4( box2 );
 			if ( sff & SF_SENSOR )
 				continue;
 			float4 gf1 = gf[1];
@@ -289,6 +307,21 @@ __global__ void k_continuous( DWorld w )
 					return;
 				if ( !joint_allows( w, b, sb ) )
 					return;
+				if ( w.callbacks & 1 )
+				{
+					unsigned long long key = ( (unsigned long long)ss << 32 ) | (unsigned)fs;
+					if ( listOnly )
+					{
+						int slot = atomicAdd( &w.sc->cbList, 1 );
+						if ( slot < w.cbCap )
+							w.cbList[slot] = key;
+						else
+							atomicOr( &w.sc->error, ERR_EVENT_CAPACITY );
+						return;
+					}
+					if ( ccd_rejected( w, key ) )
+						return;
+				}
 				const float4* gs = w.geom + (size_t)ss * GEOM_F4;
 				// solver.c:283-304: no pausing on chain segment junctions
 				if ( shape_type( sfs ) == ST_CHAIN )
@@ -383,6 +416,8 @@ __global__ void k_continuous( DWorld w )
 					consider( cand[k] );
 			}
 		}
+		if ( listOnly )
+			continue;
 		if ( fraction < 1.0f )
 		{
 			frot q = rnlerp( sweep.q1, sweep.q2, fraction );
@@ -498,13 +533,19 @@ __global__ void k_reset_step_counters( DWorld w )
 	w.sc->forceRebuild = 0;
 }
 
-void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt )
+void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt, HostHook ccdHook, void* hookContext )
 {
 	(void)s;
 	if ( w.isl )
 		launch_isl_split( w, st );
 	k_finalize<<<grid_for( w.bodyCount ), 256, 0, st>>>( w, dt, 1.0f / dt );
-	k_continuous<<<grid_for( w.bodyCount ), 64, 0, st>>>( w );
+	if ( ccdHook )
+	{
+		cudaMemsetAsync( &w.sc->cbList, 0, sizeof( int ), st );
+		k_continuous<<<grid_for( w.bodyCount ), 64, 0, st>>>( w, 1 );
+		ccdHook( hookContext );
+	}
+	k_continuous<<<grid_for( w.bodyCount ), 64, 0, st>>>( w, 0 );
 	k_hit_events<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
 	k_moved_flags<<<grid_for( w.shapeCount ), 256, 0, st>>>( w );
 	if ( w.isl )

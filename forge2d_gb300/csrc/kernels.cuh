@@ -45,11 +45,17 @@ struct StepScratch
 #define SOLVER_GRID512 2 // grid-wide, one 512-thread block per SM
 #define SOLVER_GRID256 3 // grid-wide, two 256-thread blocks per SM
 
-void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode );
-void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st );
+// A host hook runs between launches when the world has user callbacks
+// (the stream is synchronised by the hook itself).
+typedef void ( *HostHook )( void* context );
+void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode, HostHook pairHook = nullptr,
+						void* hookContext = nullptr );
+void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st, HostHook preSolveHook = nullptr,
+						 void* hookContext = nullptr );
 void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st );
 void launch_solver( DWorld& w, StepScratch& s, cudaStream_t st, float dt, int subSteps );
-void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt );
+void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt, HostHook ccdHook = nullptr,
+					  void* hookContext = nullptr );
 void launch_sensors( DWorld& w, StepScratch& s, cudaStream_t st );
 void launch_joint_ops( DWorld& w, cudaStream_t st );
 int solver_max_blocks( int threads );

@@ -97,6 +97,84 @@ __global__ void k_np_classify( DWorld w )
 	}
 }
 
+__device__ __forceinline__ bool sorted_contains( const unsigned long long* keys, int n, unsigned long long key )
+{
+	int lo = 0, hi = n;
+	while ( lo < hi )
+	{
+		int mid = ( lo + hi ) >> 1;
+		if ( keys[mid] < key )
+			lo = mid + 1;
+		else
+			hi = mid;
+	}
+	return lo < n && keys[lo] == key;
+}
+
+__device__ __forceinline__ fxf xf_of( float4 x )
+{
+	fxf t;
+	t.p = mk( x.x, x.y );
+	t.q.c = x.z;
+	t.q.s = x.w;
+	return t;
+}
+
+// Lists, for the host's pre-solve callback, every awake overlapping contact
+// with pre-solve events whose new manifold has points, with that manifold
+// as the callback sees it (20 floats laid out as f2d_manifold_view: anchors
+// still relative to the body origins) and the two shape ids. The GJK cache is read, not written: the class kernels then
+// compute the same manifold from the same cache.
+__global__ void k_presolve_list( DWorld w )
+{
+	const int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		int flags = w.cflags[c];
+		if ( ( flags & ( CF_USED | CF_INACTIVE | CF_PRESOLVE ) ) != ( CF_USED | CF_PRESOLVE ) )
+			continue;
+		int2 sh = w.cshape[c];
+		if ( !box_overlaps( box_from4( w.fat[sh.x] ), box_from4( w.fat[sh.y] ) ) )
+			continue;
+		int2 bd = w.cbody[c];
+		fxf xfA = xf_of( w.xf[bd.x] ), xfB = xf_of( w.xf[bd.y] );
+		int ta = shape_type( w.sflags[sh.x] ), tb = shape_type( w.sflags[sh.y] );
+		DGeom A = load_geom( w.geom + (size_t)sh.x * GEOM_F4, ta );
+		DGeom B = load_geom( w.geom + (size_t)sh.y * GEOM_F4, tb );
+		DCache cache = unpack_cache( w.csimplex[c] );
+		DManifold m = compute_manifold( A, xfA, B, xfB, cache );
+		if ( m.count == 0 )
+			continue;
+		int slot = atomicAdd( &w.sc->cbList, 1 );
+		if ( slot >= w.cbCap )
+		{
+			atomicOr( &w.sc->error, ERR_EVENT_CAPACITY );
+			continue;
+		}
+		w.cbList[slot] = (unsigned long long)c;
+		float* o = w.cbManifold + (size_t)slot * 22;
+		o[20] = __int_as_float( sh.x );
+		o[21] = __int_as_float( sh.y );
+		o[0] = m.normal.x;
+		o[1] = m.normal.y;
+		o[2] = __int_as_float( m.count );
+		o[3] = 0.0f;
+		for ( int i = 0; i < 2; ++i )
+		{
+			const DPoint& p = m.p[i];
+			float* q = o + 4 + 8 * i;
+			q[0] = p.point.x;
+			q[1] = p.point.y;
+			q[2] = p.anchorA.x;
+			q[3] = p.anchorA.y;
+			q[4] = p.anchorB.x;
+			q[5] = p.anchorB.y;
+			q[6] = p.separation;
+			q[7] = __int_as_float( (int)p.id );
+		}
+	}
+}
+
 // b2UpdateContact (contact.c:472-600) for the contacts of one class.
 template <int CLS> __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase( DWorld w )
 {
@@ -151,7 +229,13 @@ template <int CLS> __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase
 		float tangentSpeed = mta.w + mtb.w;
 		w.cmat[c] = make_float4( friction, restitution, rolling, tangentSpeed );
 
-		int pointCount = m.count;
+		int rawCount = m.count;
+		int pointCount = rawCount;
+		// contact.c:504-517: a pre-solve callback that returned false (the host
+		// listed it in cbReject) disables the contact for this step
+		if ( ( w.callbacks & 2 ) && ( flags & CF_PRESOLVE ) && rawCount > 0 &&
+			 sorted_contains( w.cbReject, w.sc->cbReject, (unsigned long long)c ) )
+			pointCount = 0;
 		bool touching = pointCount > 0;
 		if ( touching && ( ( sfa | sfb ) & SF_HIT_EVENTS ) )
 			flags |= CF_HIT_EVENT;
@@ -171,7 +255,7 @@ template <int CLS> __global__ void __launch_bounds__( NP_THREADS ) k_narrowphase
 			oldTI[k] = im.y;
 		}
 		float rollingImpulse = pointCount > 0 ? oldN.z : 0.0f;
-		fv2 normal = pointCount > 0 ? m.normal : mk( 0.0f, 0.0f );
+		fv2 normal = rawCount > 0 ? m.normal : mk( 0.0f, 0.0f );
 		w.mnorm[c] = make_float4( normal.x, normal.y, rollingImpulse, __int_as_float( pointCount ) );
 		for ( int i = 0; i < 2; ++i )
 		{
@@ -255,11 +339,18 @@ __global__ void k_op_clamp( DWorld w )
 		w.sc->opCount = w.opCap;
 }
 
-void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st )
+void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st, HostHook preSolveHook, void* hookContext )
 {
 	int g = ( w.contactCap + NP_THREADS - 1 ) / NP_THREADS;
 	if ( g > F2D_SMS * 8 )
 		g = F2D_SMS * 8;
+	if ( preSolveHook )
+	{
+		// the callback runs between the listing and the manifold update
+		cudaMemsetAsync( &w.sc->cbList, 0, sizeof( int ), st );
+		k_presolve_list<<<g, NP_THREADS, 0, st>>>( w );
+		preSolveHook( hookContext );
+	}
 	k_np_classify<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
 	k_narrowphase<0><<<g, NP_THREADS, 0, st>>>( w );
 	k_narrowphase<1><<<g, NP_THREADS, 0, st>>>( w );

@@ -87,6 +87,10 @@ struct HostWorld
 	TreeIds trees[3];
 	std::vector<int> staticShapes;
 	std::vector<int> sensorShapes; // sensor shapes in creation order (sensor.c)
+	f2d_custom_filter_fn customFilter = nullptr;
+	void* customFilterContext = nullptr;
+	f2d_pre_solve_fn preSolve = nullptr;
+	void* preSolveContext = nullptr;
 	bool sensorsDirty = false;
 	// chains: segment shape ids and generation per chain id (LIFO id reuse)
 	std::vector<std::vector<int>> chainSegments;
@@ -861,7 +865,7 @@ static void free_world( HostWorld* W )
 	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprep3 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
-	F( sensorBeginEv ); F( sensorEndEv ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
+	F( sensorBeginEv ); F( sensorEndEv ); F( cbList ); F( cbReject ); F( cbManifold ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 #undef F
 	dfree( W->s.tmpA );
 	dfree( W->s.tmpB );
@@ -1643,6 +1647,138 @@ extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )
 // ---------------------------------------------------------------------------
 // step
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// user callbacks, run on the host between launches (the stream is drained
+// first); the device lists candidates in cbList, the host answers with the
+// sorted rejected keys in cbReject
+// ---------------------------------------------------------------------------
+static void cb_ensure( HostWorld* W )
+{
+	DWorld& d = W->d;
+	int cap = std::max( 1 << 16, d.contactCap );
+	if ( cap <= d.cbCap )
+		return;
+	dgrow( d.cbList, 0, cap );
+	dgrow( d.cbReject, 0, cap );
+	dgrow( d.cbManifold, 0, 22 * (size_t)cap );
+	d.cbCap = cap;
+	W->graphDirty = true;
+}
+
+static void upload_rejected( HostWorld* W, std::vector<unsigned long long>& rejected )
+{
+	std::sort( rejected.begin(), rejected.end() );
+	int n = (int)rejected.size();
+	if ( n > 0 )
+		cudaMemcpy( W->d.cbReject, rejected.data(), sizeof( unsigned long long ) * n, cudaMemcpyHostToDevice );
+	cudaMemcpy( &W->d.sc->cbReject, &n, sizeof( int ), cudaMemcpyHostToDevice );
+}
+
+static int listed_count( HostWorld* W )
+{
+	cudaStreamSynchronize( W->stream );
+	int n = 0;
+	cudaMemcpy( &n, &W->d.sc->cbList, sizeof( int ), cudaMemcpyDeviceToHost );
+	return std::min( n, W->d.cbCap );
+}
+
+// broad_phase.c:267-278: new pairs (sorted keys) the filter rejects are
+// dropped before the contacts are created; A has the smaller proxy key
+static void pair_filter_hook( void* context )
+{
+	HostWorld* W = (HostWorld*)context;
+	DWorld& d = W->d;
+	cudaStreamSynchronize( W->stream );
+	int n = 0;
+	cudaMemcpy( &n, &d.sc->newPairCount, sizeof( int ), cudaMemcpyDeviceToHost );
+	n = std::min( n, d.pairCap );
+	if ( n <= 0 )
+		return;
+	std::vector<unsigned long long> keys( (size_t)n );
+	cudaMemcpy( keys.data(), d.pairKeys, sizeof( unsigned long long ) * n, cudaMemcpyDeviceToHost );
+	const unsigned long long low = ( 1ull << d.pairKeyBits ) - 1ull;
+	int kept = 0;
+	for ( int i = 0; i < n; ++i )
+	{
+		int a = (int)( keys[i] >> d.pairKeyBits ), b = (int)( keys[i] & low );
+		if ( W->proxyKey[b] < W->proxyKey[a] )
+			std::swap( a, b );
+		if ( W->customFilter( a + 1, pack_wg( W, W->sgen[a] ), b + 1, pack_wg( W, W->sgen[b] ),
+							  W->customFilterContext ) )
+			keys[kept++] = keys[i];
+	}
+	if ( kept == n )
+		return;
+	if ( kept > 0 )
+		cudaMemcpy( d.pairKeys, keys.data(), sizeof( unsigned long long ) * kept, cudaMemcpyHostToDevice );
+	cudaMemcpy( &d.sc->newPairCount, &kept, sizeof( int ), cudaMemcpyHostToDevice );
+}
+
+// solver.c:270-280: continuous candidates (static shape, fast shape)
+static void ccd_filter_hook( void* context )
+{
+	HostWorld* W = (HostWorld*)context;
+	int n = listed_count( W );
+	std::vector<unsigned long long> keys( (size_t)n ), rejected;
+	if ( n > 0 )
+		cudaMemcpy( keys.data(), W->d.cbList, sizeof( unsigned long long ) * n, cudaMemcpyDeviceToHost );
+	for ( unsigned long long k : keys )
+	{
+		int ss = (int)( k >> 32 ), fs = (int)( k & 0xffffffffull );
+		if ( !W->customFilter( ss + 1, pack_wg( W, W->sgen[ss] ), fs + 1, pack_wg( W, W->sgen[fs] ),
+							   W->customFilterContext ) )
+			rejected.push_back( k );
+	}
+	upload_rejected( W, rejected );
+}
+
+// contact.c:504-517: listed touching contacts with their new manifolds
+static void pre_solve_hook( void* context )
+{
+	HostWorld* W = (HostWorld*)context;
+	int n = listed_count( W );
+	std::vector<unsigned long long> ids( (size_t)n ), rejected;
+	std::vector<float> rec( 22 * (size_t)n );
+	if ( n > 0 )
+	{
+		cudaMemcpy( ids.data(), W->d.cbList, sizeof( unsigned long long ) * n, cudaMemcpyDeviceToHost );
+		cudaMemcpy( rec.data(), W->d.cbManifold, sizeof( float ) * 22 * n, cudaMemcpyDeviceToHost );
+	}
+	for ( int i = 0; i < n; ++i )
+	{
+		const float* r = rec.data() + 22 * (size_t)i;
+		f2d_manifold_view v;
+		static_assert( sizeof( f2d_manifold_view ) == 20 * sizeof( float ), "manifold view layout" );
+		memcpy( &v, r, sizeof( v ) );
+		int a = float_to_bits( r[20] ), b = float_to_bits( r[21] );
+		if ( !W->preSolve( a + 1, pack_wg( W, W->sgen[a] ), b + 1, pack_wg( W, W->sgen[b] ), &v, W->preSolveContext ) )
+			rejected.push_back( ids[i] );
+	}
+	upload_rejected( W, rejected );
+}
+
+extern "C" F2D_API void f2d_world_set_custom_filter( int32_t worldId, f2d_custom_filter_fn fn, void* context )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->customFilter = fn;
+	W->customFilterContext = context;
+	W->d.callbacks = ( W->d.callbacks & ~1 ) | ( fn ? 1 : 0 );
+	W->graphDirty = true;
+}
+
+extern "C" F2D_API void f2d_world_set_pre_solve( int32_t worldId, f2d_pre_solve_fn fn, void* context )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	W->preSolve = fn;
+	W->preSolveContext = context;
+	W->d.callbacks = ( W->d.callbacks & ~2 ) | ( fn ? 2 : 0 );
+	W->graphDirty = true;
+}
+
 static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 {
 	DWorld& d = W->d;
@@ -1654,10 +1790,11 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	launch_reset_counters( d, W->stream );
 	if ( prof )
 		cudaEventRecord( W->ph[0], W->stream );
-	launch_broadphase( d, W->s, W->stream, planMode );
+	bool filter = W->customFilter != nullptr, pre = W->preSolve != nullptr;
+	launch_broadphase( d, W->s, W->stream, planMode, filter ? pair_filter_hook : nullptr, W );
 	if ( prof )
 		cudaEventRecord( W->ph[1], W->stream );
-	launch_narrowphase( d, W->s, W->stream );
+	launch_narrowphase( d, W->s, W->stream, pre ? pre_solve_hook : nullptr, W );
 	if ( prof )
 		cudaEventRecord( W->ph[2], W->stream );
 	launch_graph( d, W->s, W->stream );
@@ -1668,7 +1805,7 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 		launch_record_samples( d, W->stream );
 	if ( prof )
 		cudaEventRecord( W->ph[5], W->stream );
-	launch_finalize( d, W->s, W->stream, dt );
+	launch_finalize( d, W->s, W->stream, dt, filter ? ccd_filter_hook : nullptr, W );
 	launch_sensors( d, W->s, W->stream );
 	if ( prof )
 		cudaEventRecord( W->ph[6], W->stream );
@@ -1730,7 +1867,9 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 		W->forceRebuild = false;
 	}
 	cudaEventRecord( W->evStart, W->stream );
-	bool useGraph = planMode == 0 && !W->profiling;
+	if ( W->d.callbacks )
+		cb_ensure( W );
+	bool useGraph = planMode == 0 && !W->profiling && W->d.callbacks == 0;
 	if ( useGraph && ( W->graphDirty || W->graphExec == nullptr || W->graphDt != dt || W->graphSubSteps != subSteps ) )
 	{
 		if ( W->graphExec )

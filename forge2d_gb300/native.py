@@ -99,6 +99,22 @@ class JointDef(C.Structure):
     ]
 
 
+class ManifoldPointView(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("pointX", "pointY", "anchorAX", "anchorAY", "anchorBX", "anchorBY",
+                                        "separation")] + [("id", C.c_int32)]
+
+
+class ManifoldView(C.Structure):
+    """f2d_manifold_view: the new manifold a pre-solve callback sees."""
+    _fields_ = [("normalX", C.c_float), ("normalY", C.c_float), ("pointCount", C.c_int32), ("pad0", C.c_int32),
+                ("points", ManifoldPointView * 2)]
+
+
+CustomFilterFn = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p)
+PreSolveFn = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(ManifoldView),
+                         C.c_void_p)
+
+
 # (name, restype, argtypes)
 _i, _d, _f, _i64 = C.c_int32, C.c_double, C.c_float, C.c_int64
 _SIGS = [
@@ -152,6 +168,8 @@ _SIGS = [
     ("f2d_create_chain", _i, [_i, _i, _P(_d), _i, _P(_d), _i, _i64, _i64, _i, _i, _i, _P(_i), _P(_i)]),
     ("f2d_chain_get_segments", _i, [_i, _i, _P(_i), _i]),
     ("f2d_world_get_sensor_events", _i, [_i, _P(_i), _P(_i), _i, _P(_i)]),
+    ("f2d_world_set_custom_filter", None, [_i, CustomFilterFn, C.c_void_p]),
+    ("f2d_world_set_pre_solve", None, [_i, PreSolveFn, C.c_void_p]),
     ("f2d_joint_is_valid", _i, [_i, _i]),
     ("f2d_world_get_event_counts", None, [_i, _P(_i)]),
     ("f2d_world_get_begin_events", _i, [_i, _P(_i), _i]),

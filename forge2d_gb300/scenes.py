@@ -134,7 +134,7 @@ def _polygon_points(rng, n, radius):
 
 def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=None,
          frac_circle=0.4, frac_capsule=0.3, with_container=True, enable_hit_events=False,
-         enable_contact_events=False, filters=False, sensor_visitors=False):
+         enable_contact_events=False, filters=False, sensor_visitors=False, presolve=False):
     """The mixed pile: ``count`` bodies drawn from ``seed`` -- 40% circles
     r~U[0.25,0.75], 30% capsules (half-length U[0.2,0.8], r U[0.15,0.4]),
     30% convex polygons with 3-8 vertices on a jittered circle r~U[0.3,0.8];
@@ -145,7 +145,8 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
     every 7th shape is in group -1 (never collides within the group), every
     11th in group 2 (always collides within the group), every 13th is a
     sensor. ``sensor_visitors`` turns on sensor events for three shapes in
-    four, in categories 1 and 2 alternately."""
+    four, in categories 1 and 2 alternately. ``presolve`` turns on pre-solve
+    events for every third shape."""
     rng = np.random.default_rng(seed)
     hw = 0.5 * width
     if wall_height is None:
@@ -178,6 +179,8 @@ def pile(b, count=100_000, seed=1234, width=400.0, height=800.0, wall_height=Non
                 extra["groupIndex"] = 2
             if k % 13 == 0:
                 extra["isSensor"] = 1
+        if presolve:
+            extra["enablePreSolveEvents"] = int(k % 3 == 0)
         if sensor_visitors:
             extra["enableSensorEvents"] = int(k % 4 != 0)
             extra["categoryBits"] = 1 << (k % 2)

@@ -159,6 +159,26 @@ class GpuWorld:
                                        C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def set_custom_filter(self, fn):
+        """fn(shapeA, shapeB) -> bool with 0-based shape ids (A has the smaller
+        proxy key; for continuous collision A is the static shape); None
+        removes the filter."""
+        if fn is None:
+            self._filter_cb = native.CustomFilterFn()
+        else:
+            self._filter_cb = native.CustomFilterFn(lambda a, aw, b, bw, ctx: int(bool(fn(a - 1, b - 1))))
+        self.lib.f2d_world_set_custom_filter(self.id, self._filter_cb, None)
+
+    def set_pre_solve(self, fn):
+        """fn(shapeA, shapeB, ManifoldView) -> bool with 0-based shape ids;
+        None removes the callback."""
+        if fn is None:
+            self._presolve_cb = native.PreSolveFn()
+        else:
+            self._presolve_cb = native.PreSolveFn(
+                lambda a, aw, b, bw, m, ctx: int(bool(fn(a - 1, b - 1, m.contents))))
+        self.lib.f2d_world_set_pre_solve(self.id, self._presolve_cb, None)
+
     def sensor_events(self):
         """This step's sensor (begin, end) events as (sensor shape, visitor
         shape) rows of 0-based shape ids, in the order they were produced."""

@@ -329,6 +329,38 @@ F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int3
  * begin and end events of the last step, four ints each (sensor index1,
  * worldAndGeneration, visitor index1, worldAndGeneration); returns the begin
  * count, the end count in *endCount. */
+/* User callbacks (b2CustomFilterFcn / b2PreSolveFcn, types.h:1180-1195; forge2d
+ * passes them as NativeCallable.isolateLocal, raw_box2d_ffi.dart:2467-2527).
+ * Shape ids are (index1, worldAndGeneration) pairs. The custom filter sees
+ * every new pair that passed the shape and joint filters (broad_phase.c:
+ * 267-278) and every static candidate of continuous collision (solver.c:
+ * 270-280): zero keeps the pair apart. The pre-solve callback sees each
+ * awake touching contact with pre-solve events and its new manifold, anchors
+ * relative to the body origins (contact.c:504-517): zero disables the
+ * contact for this step. Both run on the thread that calls f2d_world_step,
+ * which then returns only after the step's last callback; the world steps
+ * without its CUDA graph while either is set. NULL removes a callback. */
+typedef struct f2d_manifold_point_view
+{
+	float pointX, pointY, anchorAX, anchorAY, anchorBX, anchorBY, separation;
+	int32_t id;
+} f2d_manifold_point_view;
+typedef struct f2d_manifold_view
+{
+	float normalX, normalY;
+	int32_t pointCount, pad0;
+	f2d_manifold_point_view points[2];
+} f2d_manifold_view;
+typedef int32_t ( *f2d_custom_filter_fn )( int32_t shapeAIndex1, int32_t shapeAWorldAndGeneration,
+										   int32_t shapeBIndex1, int32_t shapeBWorldAndGeneration, void* context );
+typedef int32_t ( *f2d_pre_solve_fn )( int32_t shapeAIndex1, int32_t shapeAWorldAndGeneration,
+									   int32_t shapeBIndex1, int32_t shapeBWorldAndGeneration,
+									   const f2d_manifold_view* manifold, void* context );
+/* RawBox2D.worldSetCustomFilterCallback / worldSetPreSolveCallback (raw_box2d.dart:1358, 1373;
+ * the Dart pre-solve callback takes the normal of this view) -> b2World_SetCustomFilterCallback /
+ * b2World_SetPreSolveCallback. */
+F2D_API void f2d_world_set_custom_filter( int32_t worldId, f2d_custom_filter_fn fn, void* context );
+F2D_API void f2d_world_set_pre_solve( int32_t worldId, f2d_pre_solve_fn fn, void* context );
 F2D_API int32_t f2d_world_get_sensor_events( int32_t worldId, int32_t* begin4, int32_t* end4, int32_t capacity,
 											 int32_t* endCount );
 F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* out4, int32_t capacity );

@@ -85,6 +85,21 @@ class RevoluteDef(C.Structure):
     ]
 
 
+class ManifoldPointView(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("pointX", "pointY", "anchorAX", "anchorAY", "anchorBX", "anchorBY",
+                                        "separation")] + [("id", C.c_int32)]
+
+
+class ManifoldView(C.Structure):
+    """f2d_manifold_view: the manifold a pre-solve callback sees."""
+    _fields_ = [("normalX", C.c_float), ("normalY", C.c_float), ("pointCount", C.c_int32), ("pad0", C.c_int32),
+                ("points", ManifoldPointView * 2)]
+
+
+FILTER_FN = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_void_p)
+PRESOLVE_FN = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.POINTER(ManifoldView), C.c_void_p)
+
+
 class JointDef(C.Structure):
     """f2d_joint_def: weld 2, distance 3, prismatic 4, wheel 5, motor 6,
     mouse 7 and filter 8 joints."""
@@ -149,6 +164,8 @@ def _bind(lib, prefix):
         "create_chain": (i, [i, i, _P(d), i, _P(d), i, C.c_longlong, C.c_longlong, i, i, i]),
         "chain_get_segments": (i, [i, i, _P(i), i]),
         "get_sensor_events": (i, [i, _P(i), _P(i), i, _P(i)]),
+        "set_custom_filter": (None, [i, FILTER_FN, C.c_void_p]),
+        "set_pre_solve": (None, [i, PRESOLVE_FN, C.c_void_p]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
         "create_revolute_joint": (i, [i, _P(RevoluteDef)]),
@@ -206,6 +223,16 @@ class _CpuWorld:
         self.w = self._fns["create_world"](C.byref(wd), int(workers))
         if self.w < 0:
             raise RuntimeError("world table full")
+
+    def set_custom_filter(self, fn):
+        """fn(shapeA, shapeB) -> bool, 0-based shape ids; None removes it."""
+        self._filter_cb = FILTER_FN(lambda a, b, ctx: int(bool(fn(a, b)))) if fn else FILTER_FN()
+        self._fns["set_custom_filter"](self.w, self._filter_cb, None)
+
+    def set_pre_solve(self, fn):
+        """fn(shapeA, shapeB, ManifoldView) -> bool; None removes it."""
+        self._presolve_cb = PRESOLVE_FN(lambda a, b, m, ctx: int(bool(fn(a, b, m.contents)))) if fn else PRESOLVE_FN()
+        self._fns["set_pre_solve"](self.w, self._presolve_cb, None)
 
     def close(self):
         if self.w is not None and self.w >= 0:

@@ -128,6 +128,27 @@ typedef struct f2d_joint_def
 	double targetX, targetY;
 } f2d_joint_def;
 
+// Callbacks (types.h b2CustomFilterFcn, b2PreSolveFcn) with 0-based shape ids:
+// nonzero lets the pair collide / keeps the contact touching this step. The
+// pre-solve view holds the new manifold before its anchors are shifted to
+// the centres of mass (contact.c:504-517).
+typedef struct f2d_manifold_point_view
+{
+	float pointX, pointY, anchorAX, anchorAY, anchorBX, anchorBY, separation;
+	int32_t id;
+} f2d_manifold_point_view;
+
+typedef struct f2d_manifold_view
+{
+	float normalX, normalY;
+	int32_t pointCount, pad0;
+	f2d_manifold_point_view points[2];
+} f2d_manifold_view;
+
+typedef int32_t ( *orc_custom_filter_fn )( int32_t shapeA, int32_t shapeB, void* context );
+typedef int32_t ( *orc_pre_solve_fn )( int32_t shapeA, int32_t shapeB, const f2d_manifold_view* manifold,
+									   void* context );
+
 // Dump strides used by the ref_get_* / orc_get_* state readers.
 #define F2D_BODY_DUMP_STRIDE 12
 #define F2D_CONTACT_DUMP_INTS 9

@@ -95,6 +95,9 @@ void p_solve_continuous( World* w, int bodyId )
 				continue;
 			if ( bodies_collide( w, bodyId, shape->bodyId ) == 0 )
 				continue;
+			// solver.c:270-280 the custom filter (static shape first)
+			if ( w->customFilter && w->customFilter( si, fs, w->customFilterContext ) == 0 )
+				continue;
 			// solver.c:283-304: no pausing on chain segment junctions (the fast
 			// shape starts behind, or crosses by less than a quarter of the
 			// body's minimum extent)

@@ -435,6 +435,11 @@ typedef struct World
 	struct PSensor* sensors;
 	int sensorCount, sensorCap;
 	IntArr sensorBegin, sensorEnd;
+	// user callbacks (world.c b2World_SetCustomFilterCallback / SetPreSolveCallback)
+	orc_custom_filter_fn customFilter;
+	void* customFilterContext;
+	orc_pre_solve_fn preSolve;
+	void* preSolveContext;
 } World;
 
 typedef struct PSensor

@@ -1280,6 +1280,16 @@ static void update_pairs( World* w )
 		if ( u == 0 || cands[u - 1].key != cands[i].key )
 			cands[u++] = cands[i];
 	nc = u;
+	// broad_phase.c:267-278: the custom filter is the last test of a new pair
+	// (A is the shape with the smaller proxy key)
+	if ( w->customFilter != NULL )
+	{
+		int v = 0;
+		for ( int i = 0; i < nc; ++i )
+			if ( w->customFilter( cands[i].a, cands[i].b, w->customFilterContext ) )
+				cands[v++] = cands[i];
+		nc = v;
+	}
 	// create contacts in native order (ascending pair key) or per plan. A
 	// plan's contacts are created in the order the reference's id pool handed
 	// their ids out (LIFO free list, then fresh ids), which is the order the
@@ -1399,6 +1409,34 @@ static void update_contact( World* w, Contact* c )
 	c->tangentSpeed = sa->tangentSpeed + sb->tangentSpeed;
 	int pointCount = c->m.pointCount;
 	int touching = pointCount > 0;
+	if ( touching && w->preSolve != NULL && ( c->simFlags & SIM_PRESOLVE ) )
+	{
+		// contact.c:504-517: the user may disable the contact for this step
+		f2d_manifold_view mv;
+		memset( &mv, 0, sizeof( mv ) );
+		mv.normalX = c->m.normal.x;
+		mv.normalY = c->m.normal.y;
+		mv.pointCount = pointCount;
+		for ( int i = 0; i < pointCount; ++i )
+		{
+			const ManifoldPoint* mp = c->m.points + i;
+			f2d_manifold_point_view* q = mv.points + i;
+			q->pointX = mp->point.x;
+			q->pointY = mp->point.y;
+			q->anchorAX = mp->anchorA.x;
+			q->anchorAY = mp->anchorA.y;
+			q->anchorBX = mp->anchorB.x;
+			q->anchorBY = mp->anchorB.y;
+			q->separation = mp->separation;
+			q->id = mp->id;
+		}
+		touching = w->preSolve( c->shapeA, c->shapeB, &mv, w->preSolveContext ) != 0;
+		if ( touching == 0 )
+		{
+			pointCount = 0;
+			c->m.pointCount = 0;
+		}
+	}
 	if ( touching && ( sa->enableHitEvents || sb->enableHitEvents ) )
 		c->simFlags |= SIM_HIT_EVENT;
 	else
@@ -1685,6 +1723,20 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	g_portPhase[2] += t3 - t2;
 	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
 	p_overlap_sensors( w );
+}
+
+void orc_set_custom_filter( int wi, orc_custom_filter_fn fn, void* context )
+{
+	World* w = p_world( wi );
+	w->customFilter = fn;
+	w->customFilterContext = context;
+}
+
+void orc_set_pre_solve( int wi, orc_pre_solve_fn fn, void* context )
+{
+	World* w = p_world( wi );
+	w->preSolve = fn;
+	w->preSolveContext = context;
 }
 
 // b2World_GetSensorEvents: begin and end (sensor shape, visitor shape) pairs

@@ -608,6 +608,61 @@ int ref_get_sensor_events( int w, int* begin, int* end, int cap, int* endCount )
 	return ev.beginCount;
 }
 
+// user callbacks: b2World_SetCustomFilterCallback / SetPreSolveCallback
+// with the 0-based shape ids and the manifold view of f2d_defs.h
+typedef struct RefCallbacks
+{
+	orc_custom_filter_fn filter;
+	void* filterContext;
+	orc_pre_solve_fn preSolve;
+	void* preSolveContext;
+} RefCallbacks;
+static RefCallbacks s_callbacks[REF_MAX_WORLDS];
+
+static bool ref_filter_trampoline( b2ShapeId a, b2ShapeId b, void* context )
+{
+	RefCallbacks* cb = (RefCallbacks*)context;
+	return cb->filter( a.index1 - 1, b.index1 - 1, cb->filterContext ) != 0;
+}
+
+static bool ref_pre_solve_trampoline( b2ShapeId a, b2ShapeId b, b2Manifold* m, void* context )
+{
+	RefCallbacks* cb = (RefCallbacks*)context;
+	f2d_manifold_view mv;
+	memset( &mv, 0, sizeof( mv ) );
+	mv.normalX = m->normal.x;
+	mv.normalY = m->normal.y;
+	mv.pointCount = m->pointCount;
+	for ( int i = 0; i < m->pointCount && i < 2; ++i )
+	{
+		const b2ManifoldPoint* mp = m->points + i;
+		f2d_manifold_point_view* q = mv.points + i;
+		q->pointX = mp->point.x;
+		q->pointY = mp->point.y;
+		q->anchorAX = mp->anchorA.x;
+		q->anchorAY = mp->anchorA.y;
+		q->anchorBX = mp->anchorB.x;
+		q->anchorBY = mp->anchorB.y;
+		q->separation = mp->separation;
+		q->id = mp->id;
+	}
+	return cb->preSolve( a.index1 - 1, b.index1 - 1, &mv, cb->preSolveContext ) != 0;
+}
+
+void ref_set_custom_filter( int w, orc_custom_filter_fn fn, void* context )
+{
+	s_callbacks[w].filter = fn;
+	s_callbacks[w].filterContext = context;
+	b2World_SetCustomFilterCallback( s_worlds[w], fn ? ref_filter_trampoline : NULL, s_callbacks + w );
+}
+
+void ref_set_pre_solve( int w, orc_pre_solve_fn fn, void* context )
+{
+	s_callbacks[w].preSolve = fn;
+	s_callbacks[w].preSolveContext = context;
+	b2World_SetPreSolveCallback( s_worlds[w], fn ? ref_pre_solve_trampoline : NULL, s_callbacks + w );
+}
+
 // ---------------------------------------------------------------------------
 // State dumps
 // ---------------------------------------------------------------------------

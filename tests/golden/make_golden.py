@@ -20,9 +20,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
 
 from forge2d_gb300 import scenes  # noqa: E402
 from oracle.oracle import RefWorld  # noqa: E402
+from parity import install_callbacks  # noqa: E402
 
 CASES = {
     "pyramid": dict(world=dict(enableSleep=0), scene=("pyramid", dict()), frames=256, checkpoints=[1, 8, 32, 64, 256]),
@@ -41,6 +43,10 @@ CASES = {
                              checkpoints=[1, 100, 200, 300]),
     "chain_terrain": dict(world=dict(enableSleep=0, enableContinuous=0), scene=("chain_terrain", dict(count=300)),
                           frames=256, checkpoints=[1, 64, 256]),
+    # custom filter and pre-solve callbacks (tests/parity.py rules)
+    "pile_callbacks": dict(world=dict(enableSleep=1, enableContinuous=1),
+                           scene=("pile", dict(count=400, seed=6, width=20.0, height=40.0, presolve=True)),
+                           frames=300, checkpoints=[1, 100, 200, 300], callbacks=True),
     # sensor events every frame (rows: frame, sensor shape, visitor shape)
     "sensor_field": dict(world=dict(enableSleep=1, enableContinuous=1), scene=("sensor_field", dict()), frames=300,
                          checkpoints=[1, 100, 300], sensors=True),
@@ -57,6 +63,8 @@ def record(name, spec):
     w = RefWorld(scenes.world_def(**spec["world"]))
     scene, kw = spec["scene"]
     scenes.build(w, scene, **kw)
+    if spec.get("callbacks"):
+        install_callbacks(w)
     prev = set()
     plan_rows = []
     out = {}

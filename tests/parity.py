@@ -45,3 +45,24 @@ def compare_contacts(a, b):
             if len(diffs) > 5:
                 break
     return diffs
+
+
+# User callbacks of the callback parity cases: pure functions of the shape
+# ids and the manifold, so every world that installs them decides alike.
+def filter_rule(a, b):
+    """Custom filter: pairs whose shape ids sum to a multiple of 5 never
+    collide."""
+    return (a + b) % 5 != 0
+
+
+def pre_solve_rule(a, b, m):
+    """Pre-solve: contacts whose shape ids sum to a multiple of 4 are one-way
+    (solved only while the normal does not point down)."""
+    if (a + b) % 4 == 0:
+        return m.normalY > -0.2
+    return True
+
+
+def install_callbacks(world):
+    world.set_custom_filter(filter_rule)
+    world.set_pre_solve(pre_solve_rule)

@@ -16,7 +16,7 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import compare_contacts
+from parity import compare_contacts, install_callbacks
 from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
                                 replay, sensor_rows)
 
@@ -96,6 +96,37 @@ def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, fra
     assert g.sync() == 0
     if name in ("pile_dense_overflow", "overflow_heap", "overflow_platforms", "overflow_long"):
         assert saw_overflow, "scene meant to exercise the overflow colour did not reach it"
+    g.close()
+    p.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_callbacks_match_port(gpu_lib, port_lib, sleep):
+    """Custom filter (new pairs on the host between pair finding and contact
+    creation; continuous candidates between a listing pass and the impact
+    pass) and pre-solve (host decision between the manifold listing and the
+    contact update): bit-identical to the oracle with the same callbacks."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (g, p):
+        scenes.build(w, "pile", count=600, seed=6, width=24.0, height=50.0, presolve=True)
+        install_callbacks(w)
+    for f in range(1, 241):
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
+        if f % 40 == 0:
+            assert compare_contacts(g, p) == [], "frame %d" % f
+    # removing the callbacks brings the CUDA graph back; results stay equal
+    for w in (g, p):
+        w.set_custom_filter(None)
+        w.set_pre_solve(None)
+    for f in range(241, 301):
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
+    assert g.sync() == 0
     g.close()
     p.close()
 

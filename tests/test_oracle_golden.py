@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from forge2d_gb300 import scenes
+from parity import install_callbacks
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -29,6 +30,8 @@ CASES = {
     "joint_rigs_sleep": (dict(enableSleep=1), "joint_rigs", dict()),
     "chain_terrain": (dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(count=300)),
     "sensor_field": (dict(enableSleep=1, enableContinuous=1), "sensor_field", dict()),
+    "pile_callbacks": (dict(enableSleep=1, enableContinuous=1), "pile",
+                       dict(count=400, seed=6, width=20.0, height=40.0, presolve=True)),
     "pyramid_sleep": (dict(enableSleep=1), "pyramid", dict(rows=12)),
     "pile_sleep": (dict(enableSleep=1, enableContinuous=1), "pile", dict(count=300, seed=3, width=20.0, height=30.0)),
 }
@@ -55,8 +58,11 @@ def frame_stats(world, mass):
 
 
 def replay(world, name, frames=None, on_frame=None):
-    """Steps ``world`` with the reference's contact ids from the fixture."""
+    """Steps ``world`` with the reference's contact ids from the fixture
+    (with the callback cases' user callbacks installed)."""
     gold = np.load(os.path.join(GOLD, name + "_ref.npz"))
+    if name in CALLBACK_CASES:
+        install_callbacks(world)
     plan = gold["plan"]
     last = int(gold["checkpoints"].max()) if frames is None else frames
     by_frame = {}
@@ -73,6 +79,7 @@ def replay(world, name, frames=None, on_frame=None):
 
 
 SENSOR_CASES = ("sensor_field",)
+CALLBACK_CASES = ("pile_callbacks",)
 
 
 def sensor_rows(world, f, rows):

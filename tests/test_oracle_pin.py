@@ -13,7 +13,7 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import compare_contacts, new_contacts
+from parity import compare_contacts, filter_rule, install_callbacks, new_contacts, pre_solve_rule
 
 
 def lockstep(ref, port, frames, each=None):
@@ -132,6 +132,36 @@ def test_port_sensor_events_with_reference(ref_lib, port_lib, sleep):
             assert np.array_equal(a, b), (f, k)
             totals[k] += len(a)
     assert totals[0] > 100 and totals[1] > 50, totals
+    ref.close()
+    port.close()
+
+
+def test_port_callbacks_with_reference(ref_lib, port_lib):
+    """Custom filter (new pairs and continuous candidates) and pre-solve
+    (one-way contacts) callbacks: bit-identical bodies, sets and contacts,
+    and both callbacks reject something."""
+    wkw = dict(enableSleep=1, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    seen = {"filter": 0, "pre": 0}
+
+    def counting_filter(a, b):
+        ok = filter_rule(a, b)
+        seen["filter"] += not ok
+        return ok
+
+    def counting_pre(a, b, m):
+        ok = pre_solve_rule(a, b, m)
+        seen["pre"] += not ok
+        return ok
+
+    for w in (ref, port):
+        scenes.build(w, "pile", count=400, seed=6, width=20.0, height=40.0, presolve=True)
+    ref.set_custom_filter(counting_filter)
+    ref.set_pre_solve(counting_pre)
+    install_callbacks(port)
+    lockstep_full(ref, port, 300)
+    assert seen["filter"] > 100 and seen["pre"] > 100, seen
     ref.close()
     port.close()
 
