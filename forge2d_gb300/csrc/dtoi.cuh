@@ -189,8 +189,11 @@ __device__ __forceinline__ void gjk_witness( const DSimplex& s, fv2& la, fv2& lb
 // distance, updates the cache (left alone when the shapes overlap) and, when
 // asked, gives the witness points in the world frame of A
 static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf xfA, fxf xfB, DCache& cache,
-									  fv2* pointA = nullptr, fv2* pointB = nullptr )
+									  fv2* pointA = nullptr, fv2* pointB = nullptr, fv2* normalOut = nullptr )
 {
+	fv2 nonUnitNormal = mk( 0.0f, 0.0f );
+	if ( normalOut != nullptr )
+		*normalOut = nonUnitNormal;
 	DProxy pb;
 	{
 		fxf t = xinvmul( xfA, xfB );
@@ -248,6 +251,7 @@ static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf 
 			}
 			return 0.0f;
 		}
+		nonUnitNormal = d;
 		DSimplexVertex& vx = s.v[s.count];
 		vx.indexA = support( pa, d );
 		vx.wA = pa.p[vx.indexA];
@@ -266,6 +270,8 @@ static __device__ float gjk_distance( const DProxy& pa, const DProxy& pbIn, fxf 
 			break;
 		s.count += 1;
 	}
+	if ( normalOut != nullptr )
+		*normalOut = rrot( xfA.q, vnormalize( nonUnitNormal ) );
 	fv2 la, lb;
 	gjk_witness( s, la, lb );
 	float dx = lb.x - la.x, dy = lb.y - la.y;

@@ -1178,6 +1178,21 @@ __global__ void k_isl_api( DWorld w, DIslands* Ip, int op, int body )
 	}
 }
 
+// Wakes the sleeping sets of the marked shapes' bodies in ascending shape id
+// (b2WakeBody per blast shape, world.c:2673).
+__global__ void k_isl_wake_marked( DWorld w, DIslands* Ip, const int* marks, int n )
+{
+	DIslands& I = *Ip;
+	for ( int s = 0; s < n; ++s )
+	{
+		if ( marks[s] == 0 )
+			continue;
+		int b = w.shapeBody[s];
+		if ( I.bSet[b] >= SET_FIRST_SLEEPING )
+			isl_wake_set( w, I, I.bSet[b] );
+	}
+}
+
 // Solver set per body for the state dump (0 static, 1 disabled, 2 awake, 3..).
 __global__ void k_isl_body_sets( DWorld w, DIslands* Ip, int* out, int n )
 {
@@ -1236,6 +1251,11 @@ void launch_isl_sleep( DWorld& w, cudaStream_t st, unsigned long long* scanState
 void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body )
 {
 	k_isl_api<<<1, 1, 0, st>>>( w, w.isl, op, body );
+}
+
+void launch_isl_wake_marked( DWorld& w, cudaStream_t st, const int* shapeMarks, int shapeCount )
+{
+	k_isl_wake_marked<<<1, 1, 0, st>>>( w, w.isl, shapeMarks, shapeCount );
 }
 
 void launch_isl_body_sets( DWorld& w, cudaStream_t st, int* out, int n )

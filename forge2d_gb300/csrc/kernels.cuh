@@ -66,6 +66,9 @@ void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long
 void launch_isl_split( DWorld& w, cudaStream_t st );
 void launch_isl_sleep( DWorld& w, cudaStream_t st, unsigned long long* scanState );
 void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body );
+void launch_isl_wake_marked( DWorld& w, cudaStream_t st, const int* shapeMarks, int shapeCount );
+void launch_explode( DWorld& w, cudaStream_t st, int* hit, unsigned long long mask, float x, float y, float radius,
+					 float falloff, float impulsePerLength );
 void launch_isl_fix_flags( DWorld& w, cudaStream_t st, int n );
 void launch_learned_warm_start( DWorld& w, cudaStream_t st );
 void launch_record_samples( DWorld& w, cudaStream_t st );

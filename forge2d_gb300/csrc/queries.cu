@@ -416,6 +416,120 @@ extern "C" F2D_API int32_t f2d_world_cast_ray_closest( int32_t worldId, double o
 	return 1;
 }
 
+// Every hit of the whole ray (callback form of b2World_CastRay): shape id
+// and point, normal, fraction in the world frame
+__global__ void k_ray_all( DWorld w, fv2 origin, fv2 translation, unsigned long long cat, unsigned long long msk,
+						   int* count, int* shapes, float* rows )
+{
+	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
+	{
+		int f = w.sflags[s];
+		if ( ( f & ( SF_USED | SF_PROXY ) ) != ( SF_USED | SF_PROXY ) )
+			continue;
+		if ( ( w.cat[s] & msk ) == 0ull || !query_collide( w, s, cat, msk ) )
+			continue;
+		if ( ray_box_enter( box_from4( w.fat[s] ), origin, translation ) > 1.0f )
+			continue;
+		int b = w.shapeBody[s];
+		float4 x4 = w.xf[b];
+		fxf xf;
+		xf.p = mk( x4.x, x4.y );
+		xf.q.c = x4.z;
+		xf.q.s = x4.w;
+		fv2 lo = rinvrot( xf.q, vsub( origin, xf.p ) );
+		fv2 lt = rinvrot( xf.q, translation );
+		const float4* g = w.geom + (size_t)s * GEOM_F4;
+		float4 g0 = g[0], g1 = g[1];
+		int type = shape_type( f );
+		RayHit h;
+		if ( type == ST_CIRCLE )
+			h = ray_circle( lo, lt, 1.0f, mk( g0.x, g0.y ), g1.x );
+		else if ( type == ST_CAPSULE )
+			h = ray_capsule( lo, lt, 1.0f, mk( g0.x, g0.y ), mk( g0.z, g0.w ), g1.x );
+		else if ( type == ST_SEGMENT || type == ST_CHAIN )
+			h = ray_segment_sided( lo, lt, mk( g0.x, g0.y ), mk( g0.z, g0.w ), type == ST_CHAIN );
+		else
+			h = ray_polygon( lo, lt, 1.0f, g );
+		if ( !h.hit )
+			continue;
+		int slot = atomicAdd( count, 1 );
+		fv2 p = xpoint( xf, h.point );
+		fv2 n = rrot( xf.q, h.normal );
+		shapes[slot] = s;
+		float* r = rows + 5 * (size_t)slot;
+		r[0] = p.x;
+		r[1] = p.y;
+		r[2] = n.x;
+		r[3] = n.y;
+		r[4] = h.fraction;
+	}
+}
+
+// RawBox2D.worldCastRay (raw_box2d.dart:1318 -> b2World_CastRay, world.c:
+// 2176-2251): the callback sees the ray's hits in ascending fraction (then
+// shape id), the order in which a ray clipped by every returned fraction
+// meets them; a hit past the current clip is not reported, 0 ends the cast,
+// -1 skips the hit, a fraction in [0, 1] clips. Returns the number of calls.
+extern "C" F2D_API int32_t f2d_world_cast_ray( int32_t worldId, double ox, double oy, double tx, double ty,
+											   int64_t categoryBits, int64_t maskBits, f2d_cast_result_fn fn,
+											   void* context )
+{
+	cudaStream_t st;
+	DWorld* w = f2d_internal_world( worldId, &st, nullptr, 0 );
+	if ( w == nullptr || fn == nullptr || w->shapeCount == 0 )
+		return 0;
+	int n = w->shapeCount;
+	int* dCount = nullptr;
+	int* dShapes = nullptr;
+	float* dRows = nullptr;
+	cudaMalloc( (void**)&dCount, sizeof( int ) );
+	cudaMalloc( (void**)&dShapes, sizeof( int ) * (size_t)n );
+	cudaMalloc( (void**)&dRows, sizeof( float ) * 5 * (size_t)n );
+	cudaMemsetAsync( dCount, 0, sizeof( int ), st );
+	fv2 o = mk( (float)ox, (float)oy ), t = mk( (float)tx, (float)ty );
+	k_ray_all<<<grid_for( n ), 256, 0, st>>>( *w, o, t, (unsigned long long)categoryBits, (unsigned long long)maskBits,
+											  dCount, dShapes, dRows );
+	int m = 0;
+	cudaMemcpyAsync( &m, dCount, sizeof( int ), cudaMemcpyDeviceToHost, st );
+	cudaStreamSynchronize( st );
+	m = std::min( m, n );
+	std::vector<int> shapes( (size_t)m );
+	std::vector<float> rows( 5 * (size_t)m );
+	if ( m > 0 )
+	{
+		cudaMemcpy( shapes.data(), dShapes, sizeof( int ) * m, cudaMemcpyDeviceToHost );
+		cudaMemcpy( rows.data(), dRows, sizeof( float ) * 5 * m, cudaMemcpyDeviceToHost );
+	}
+	cudaFree( dCount );
+	cudaFree( dShapes );
+	cudaFree( dRows );
+	std::vector<int> order( (size_t)m );
+	for ( int i = 0; i < m; ++i )
+		order[i] = i;
+	std::sort( order.begin(), order.end(), [&]( int a, int b ) {
+		float fa = rows[5 * (size_t)a + 4], fb = rows[5 * (size_t)b + 4];
+		return fa != fb ? fa < fb : shapes[a] < shapes[b];
+	} );
+	float clip = 1.0f;
+	int calls = 0;
+	int world0 = f2d_internal_world0( worldId );
+	for ( int k : order )
+	{
+		const float* r = rows.data() + 5 * (size_t)k;
+		if ( r[4] > clip )
+			break;
+		int s = shapes[k];
+		float v = fn( s + 1, world0 | ( (int)f2d_internal_shape_gen( worldId, s ) << 16 ), r[0], r[1], r[2], r[3], r[4],
+					  context );
+		calls += 1;
+		if ( v == 0.0f )
+			break;
+		if ( 0.0f <= v && v <= 1.0f )
+			clip = v;
+	}
+	return calls;
+}
+
 extern "C" F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lx, double ly, double ux, double uy,
 												   int64_t categoryBits, int64_t maskBits, int32_t* shapes2,
 												   int32_t capacity )

@@ -2490,6 +2490,19 @@ extern "C" F2D_API void f2d_body_set_awake( int32_t index1, int32_t wg, int32_t 
 	launch_isl_api( W->d, W->stream, awake ? 0 : 1, b );
 }
 
+// RawBox2D.worldExplode (raw_box2d.dart:1342 -> b2World_Explode, world.c:2718):
+// enqueued on the world's stream after the pending uploads
+extern "C" F2D_API void f2d_world_explode( int32_t worldId, int64_t maskBits, double positionX, double positionY,
+										   double radius, double falloff, double impulsePerLength )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || W->shapeCount == 0 )
+		return;
+	flush_uploads( W );
+	launch_explode( W->d, W->stream, W->s.tmpA, (unsigned long long)maskBits, (float)positionX, (float)positionY,
+					(float)radius, (float)falloff, (float)impulsePerLength );
+}
+
 // RawBox2D.bodyIsSleepEnabled / bodyEnableSleep (raw_box2d.dart:235-242;
 // b2Body_EnableSleep wakes the body when sleep is disabled)
 extern "C" F2D_API int32_t f2d_body_is_sleep_enabled( int32_t index1, int32_t wg )

@@ -110,6 +110,8 @@ class ManifoldView(C.Structure):
                 ("points", ManifoldPointView * 2)]
 
 
+CastResultFn = C.CFUNCTYPE(C.c_float, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                           C.c_void_p)
 CustomFilterFn = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p)
 PreSolveFn = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(ManifoldView),
                          C.c_void_p)
@@ -170,6 +172,8 @@ _SIGS = [
     ("f2d_world_get_sensor_events", _i, [_i, _P(_i), _P(_i), _i, _P(_i)]),
     ("f2d_world_set_custom_filter", None, [_i, CustomFilterFn, C.c_void_p]),
     ("f2d_world_set_pre_solve", None, [_i, PreSolveFn, C.c_void_p]),
+    ("f2d_world_explode", None, [_i, _i64, _d, _d, _d, _d, _d]),
+    ("f2d_world_cast_ray", _i, [_i, _d, _d, _d, _d, _i64, _i64, CastResultFn, C.c_void_p]),
     ("f2d_joint_is_valid", _i, [_i, _i]),
     ("f2d_world_get_event_counts", None, [_i, _P(_i)]),
     ("f2d_world_get_begin_events", _i, [_i, _P(_i), _i]),

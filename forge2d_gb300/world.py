@@ -159,6 +159,16 @@ class GpuWorld:
                                        C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def cast_ray(self, ox, oy, tx, ty, fn, cat=1, mask=-1):
+        """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float,
+        0-based shape ids, hits in ascending fraction."""
+        cb = native.CastResultFn(lambda s, sw, px, py, nx, ny, f, ctx: float(fn(s - 1, (px, py), (nx, ny), f)))
+        return self.lib.f2d_world_cast_ray(self.id, ox, oy, tx, ty, cat, mask, cb, None)
+
+    def explode(self, x, y, radius, falloff, impulse_per_length, mask=-1):
+        """b2World_Explode: radial impulse on the dynamic shapes near (x, y)."""
+        self.lib.f2d_world_explode(self.id, mask, x, y, radius, falloff, impulse_per_length)
+
     def set_custom_filter(self, fn):
         """fn(shapeA, shapeB) -> bool with 0-based shape ids (A has the smaller
         proxy key; for continuous collision A is the static shape); None

@@ -360,6 +360,20 @@ typedef int32_t ( *f2d_pre_solve_fn )( int32_t shapeAIndex1, int32_t shapeAWorld
  * the Dart pre-solve callback takes the normal of this view) -> b2World_SetCustomFilterCallback /
  * b2World_SetPreSolveCallback. */
 F2D_API void f2d_world_set_custom_filter( int32_t worldId, f2d_custom_filter_fn fn, void* context );
+/* RawBox2D.worldExplode (raw_box2d.dart:1342 -> b2World_Explode, world.c:2718):
+ * radial impulse on the dynamic shapes within radius + falloff of the
+ * position (category against maskBits), waking their bodies. */
+/* RawBox2D.worldCastRay (raw_box2d.dart:1318 -> b2World_CastRay, world.c:2222):
+ * the callback gets each hit (shape id pair, point, normal, fraction) in
+ * ascending fraction and returns -1 (ignore), 0 (stop), a fraction (clip)
+ * or 1 (go on). Returns the number of calls. */
+typedef float ( *f2d_cast_result_fn )( int32_t shapeIndex1, int32_t shapeWorldAndGeneration, float pointX, float pointY,
+									   float normalX, float normalY, float fraction, void* context );
+F2D_API int32_t f2d_world_cast_ray( int32_t worldId, double originX, double originY, double translationX,
+									double translationY, int64_t categoryBits, int64_t maskBits, f2d_cast_result_fn fn,
+									void* context );
+F2D_API void f2d_world_explode( int32_t worldId, int64_t maskBits, double positionX, double positionY, double radius,
+								double falloff, double impulsePerLength );
 F2D_API void f2d_world_set_pre_solve( int32_t worldId, f2d_pre_solve_fn fn, void* context );
 F2D_API int32_t f2d_world_get_sensor_events( int32_t worldId, int32_t* begin4, int32_t* end4, int32_t capacity,
 											 int32_t* endCount );

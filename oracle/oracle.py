@@ -97,6 +97,7 @@ class ManifoldView(C.Structure):
 
 
 FILTER_FN = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.c_void_p)
+CAST_FN = C.CFUNCTYPE(C.c_float, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p)
 PRESOLVE_FN = C.CFUNCTYPE(C.c_int32, C.c_int32, C.c_int32, C.POINTER(ManifoldView), C.c_void_p)
 
 
@@ -166,6 +167,8 @@ def _bind(lib, prefix):
         "get_sensor_events": (i, [i, _P(i), _P(i), i, _P(i)]),
         "set_custom_filter": (None, [i, FILTER_FN, C.c_void_p]),
         "set_pre_solve": (None, [i, PRESOLVE_FN, C.c_void_p]),
+        "world_explode": (None, [i, C.c_longlong, d, d, d, d, d]),
+        "world_cast_ray": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, CAST_FN, C.c_void_p]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
         "create_revolute_joint": (i, [i, _P(RevoluteDef)]),
@@ -223,6 +226,15 @@ class _CpuWorld:
         self.w = self._fns["create_world"](C.byref(wd), int(workers))
         if self.w < 0:
             raise RuntimeError("world table full")
+
+    def cast_ray(self, ox, oy, tx, ty, fn, cat=1, mask=-1):
+        """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float."""
+        cb = CAST_FN(lambda s, px, py, nx, ny, f, ctx: float(fn(s, (px, py), (nx, ny), f)))
+        return self._fns["world_cast_ray"](self.w, ox, oy, tx, ty, cat, mask, cb, None)
+
+    def explode(self, x, y, radius, falloff, impulse_per_length, mask=-1):
+        """b2World_Explode."""
+        self._fns["world_explode"](self.w, mask, x, y, radius, falloff, impulse_per_length)
 
     def set_custom_filter(self, fn):
         """fn(shapeA, shapeB) -> bool, 0-based shape ids; None removes it."""

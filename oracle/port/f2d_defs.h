@@ -149,6 +149,11 @@ typedef int32_t ( *orc_custom_filter_fn )( int32_t shapeA, int32_t shapeB, void*
 typedef int32_t ( *orc_pre_solve_fn )( int32_t shapeA, int32_t shapeB, const f2d_manifold_view* manifold,
 									   void* context );
 
+// b2CastResultFcn with a 0-based shape id: returns -1 to ignore the hit, 0 to
+// stop, a fraction to clip the ray, 1 to go on
+typedef float ( *orc_cast_fn )( int32_t shape, float pointX, float pointY, float normalX, float normalY,
+								float fraction, void* context );
+
 // Dump strides used by the ref_get_* / orc_get_* state readers.
 #define F2D_BODY_DUMP_STRIDE 12
 #define F2D_CONTACT_DUMP_INTS 9

@@ -238,8 +238,10 @@ static v2 solve3( Simplex* s )
 // the witness points in the world frame of A (optional) and the updated
 // cache (left alone when the shapes overlap)
 float p_shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform xfA, xform xfB, SimplexCache* cache,
-						v2* pointA, v2* pointB )
+						v2* pointA, v2* pointB, v2* normal )
 {
+	if ( normal != NULL )
+		*normal = V( 0.0f, 0.0f );
 	ShapeProxy pb;
 	{
 		xform t = invMulXf( xfA, xfB );
@@ -309,7 +311,8 @@ float p_shape_distance( const ShapeProxy* pa, const ShapeProxy* pbIn, xform xfA,
 			break;
 		simplex.count += 1;
 	}
-	(void)nonUnitNormal;
+	if ( normal != NULL )
+		*normal = rotate( xfA.q, normalize( nonUnitNormal ) );
 	v2 la, lb;
 	witness( &la, &lb, &simplex );
 	float dx = lb.x - la.x;
@@ -483,7 +486,7 @@ float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sw
 	{
 		xform xfA = sweep_xf( &sa, t1 );
 		xform xfB = sweep_xf( &sb, t1 );
-		float distance = p_shape_distance( pa, pb, xfA, xfB, &cache, NULL, NULL );
+		float distance = p_shape_distance( pa, pb, xfA, xfB, &cache, NULL, NULL, NULL );
 		distanceIterations += 1;
 		if ( distance <= 0.0f )
 		{

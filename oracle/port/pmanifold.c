@@ -802,7 +802,7 @@ static Manifold collide_chain_polygon( const Geometry* segA, xform xfA, const Po
 	ShapeProxy proxyB = p_make_proxy( vertices, count, 0.0f );
 	xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
 	v2 pointA = V( 0.0f, 0.0f ), pointB = V( 0.0f, 0.0f );
-	float distance = p_shape_distance( &proxyA, &proxyB, identity, identity, cache, &pointA, &pointB );
+	float distance = p_shape_distance( &proxyA, &proxyB, identity, identity, cache, &pointA, &pointB, 0 );
 	if ( distance > radiusB + P_SPECULATIVE )
 		return m;
 	v2 n0 = sp.convex1 ? sp.normal0 : normal1;

@@ -505,7 +505,7 @@ typedef struct Sweep
 	rot q1, q2;
 } Sweep;
 float p_shape_distance( const ShapeProxy* pa, const ShapeProxy* pb, xform xfA, xform xfB, SimplexCache* cache,
-						v2* pointA, v2* pointB );
+						v2* pointA, v2* pointB, v2* normal );
 ShapeProxy p_make_proxy( const v2* pts, int count, float radius );
 ShapeProxy p_shape_proxy( const Geometry* g );
 float p_time_of_impact( const ShapeProxy* pa, const ShapeProxy* pb, Sweep sa, Sweep sb, float maxFraction, int* state );

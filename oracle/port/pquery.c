@@ -15,6 +15,8 @@
 // found here by a linear scan. Equal fractions resolve to the lower shape id.
 #include "port.h"
 
+#include <stdlib.h>
+
 #include <stddef.h>
 
 World* p_world( int w ); // pworld.c
@@ -307,4 +309,169 @@ int orc_overlap_aabb( int wi, double lx, double ly, double ux, double uy, long l
 		n += 1;
 	}
 	return n;
+}
+
+// shape.c:655-703 b2GetShapeProjectedPerimeter
+static float projected_perimeter( const Shape* s, v2 line )
+{
+	const Geometry* g = &s->g;
+	switch ( g->type )
+	{
+		case SHAPE_CAPSULE:
+		{
+			v2 axis = sub( g->c2, g->c1 );
+			float projectedLength = fabsp( dot( axis, line ) );
+			return projectedLength + 2.0f * g->radius;
+		}
+		case SHAPE_CIRCLE:
+			return 2.0f * g->radius;
+		case SHAPE_POLYGON:
+		{
+			float value = dot( g->poly.vertices[0], line );
+			float lower = value, upper = value;
+			for ( int i = 1; i < g->poly.count; ++i )
+			{
+				value = dot( g->poly.vertices[i], line );
+				lower = fminp( lower, value );
+				upper = fmaxp( upper, value );
+			}
+			return ( upper - lower ) + 2.0f * g->poly.radius;
+		}
+		case SHAPE_SEGMENT:
+		case SHAPE_CHAIN_SEGMENT:
+		{
+			float value1 = dot( g->c1, line );
+			float value2 = dot( g->c2, line );
+			return fabsp( value2 - value1 );
+		}
+		default:
+			return 0.0f;
+	}
+}
+
+// world.c:2640-2735 b2World_Explode: every shape of a dynamic body whose fat
+// AABB meets the blast box (category against maskBits) and which lies within
+// radius + falloff of the centre (GJK with radii) wakes its body and gets an
+// impulse along the centre-to-closest-point direction, scaled by its
+// projected perimeter and the falloff. Shapes are visited in id order (the
+// reference visits its dynamic tree's order; the order only matters for a
+// body with several shapes in the blast or for the order sleeping sets wake).
+void orc_world_explode( int wi, long long maskBits, double px, double py, double radius, double falloff,
+						double impulsePerLength )
+{
+	World* w = p_world( wi );
+	if ( w == NULL )
+		return;
+	v2 position = V( (float)px, (float)py );
+	float r = (float)radius, fo = (float)falloff, ipl = (float)impulsePerLength;
+	box2 box;
+	box.lo = V( position.x - ( r + fo ), position.y - ( r + fo ) );
+	box.hi = V( position.x + ( r + fo ), position.y + ( r + fo ) );
+	for ( int id = 0; id < w->shapeCount; ++id )
+	{
+		const Shape* s = w->shapes + id;
+		if ( s->used == 0 || s->proxyKey == P_NULL || ( s->proxyKey & 3 ) != BODY_DYNAMIC )
+			continue;
+		if ( ( s->categoryBits & (uint64_t)maskBits ) == 0 || boxOverlaps( s->fatAABB, box ) == 0 )
+			continue;
+		Body* b = w->bodies + s->bodyId;
+		xform xf = b->xf;
+		ShapeProxy pa = p_shape_proxy( &s->g );
+		ShapeProxy pb = p_make_proxy( &position, 1, 0.0f );
+		xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+		SimplexCache cache = { 0 };
+		v2 pointA = V( 0.0f, 0.0f ), pointB = V( 0.0f, 0.0f ), normal = V( 0.0f, 0.0f );
+		float d = p_shape_distance( &pa, &pb, xf, identity, &cache, &pointA, &pointB, &normal );
+		// distance.c:592-603 useRadii
+		if ( d > 0.1f * P_LINEAR_SLOP )
+		{
+			d = fmaxp( 0.0f, d - pa.radius - pb.radius );
+			pointA = mulAdd( pointA, pa.radius, normal );
+		}
+		if ( d > r + fo )
+			continue;
+		if ( b->setIndex >= SET_FIRST_SLEEPING )
+			p_wake_solver_set( w, b->setIndex );
+		if ( b->setIndex != SET_AWAKE )
+			continue;
+		v2 closestPoint = pointA;
+		if ( d == 0.0f )
+			closestPoint = xfPoint( xf, p_shape_centroid( &s->g ) );
+		v2 direction = sub( closestPoint, position );
+		if ( lengthSq( direction ) > 100.0f * FLT_EPSILON * FLT_EPSILON )
+			direction = normalize( direction );
+		else
+			direction = V( 1.0f, 0.0f );
+		v2 localLine = invRotate( xf.q, leftPerp( direction ) );
+		float perimeter = projected_perimeter( s, localLine );
+		float scale = 1.0f;
+		if ( d > r && fo > 0.0f )
+			scale = fclampp( ( r + fo - d ) / fo, 0.0f, 1.0f );
+		float magnitude = ipl * perimeter * scale;
+		v2 impulse = mulSV( magnitude, direction );
+		b->v = mulAdd( b->v, b->invMass, impulse );
+		b->w += b->invInertia * cross( sub( closestPoint, b->center ), impulse );
+	}
+}
+
+typedef struct RayHitRow
+{
+	int shape;
+	CastOut o;
+} RayHitRow;
+
+static int cmp_ray_hit( const void* a, const void* b )
+{
+	const RayHitRow* x = (const RayHitRow*)a;
+	const RayHitRow* y = (const RayHitRow*)b;
+	if ( x->o.fraction != y->o.fraction )
+		return x->o.fraction < y->o.fraction ? -1 : 1;
+	return x->shape < y->shape ? -1 : ( x->shape > y->shape ? 1 : 0 );
+}
+
+// world.c:2176-2251 b2World_CastRay with a callback: the hits of the whole
+// ray are reported in ascending fraction (then shape id), the order in
+// which a ray clipped by each returned fraction meets them; a hit beyond the
+// current clip is not reported, 0 ends the cast, -1 skips the hit. (The
+// reference reports in its trees' order; closest-hit, any-hit and all-hit
+// callbacks end with the same answer.) Returns the number of calls.
+int orc_world_cast_ray( int wi, double ox, double oy, double tx, double ty, long long cat, long long mask,
+						orc_cast_fn fn, void* context )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || fn == NULL )
+		return 0;
+	v2 origin = V( (float)ox, (float)oy ), translation = V( (float)tx, (float)ty );
+	RayHitRow* rows = (RayHitRow*)malloc( sizeof( RayHitRow ) * (size_t)( w->shapeCount > 0 ? w->shapeCount : 1 ) );
+	int n = 0;
+	for ( int i = 0; i < w->shapeCount; ++i )
+	{
+		const Shape* s = w->shapes + i;
+		if ( s->used == 0 || s->proxyKey == P_NULL || query_collide( s, (uint64_t)cat, (uint64_t)mask ) == 0 )
+			continue;
+		CastOut o = ray_shape( s, w->bodies[s->bodyId].xf, origin, translation );
+		if ( o.hit )
+		{
+			rows[n].shape = i;
+			rows[n].o = o;
+			n += 1;
+		}
+	}
+	qsort( rows, (size_t)n, sizeof( RayHitRow ), cmp_ray_hit );
+	float clip = 1.0f;
+	int calls = 0;
+	for ( int k = 0; k < n; ++k )
+	{
+		const CastOut* o = &rows[k].o;
+		if ( o->fraction > clip )
+			break;
+		float r = fn( rows[k].shape, o->point.x, o->point.y, o->normal.x, o->normal.y, o->fraction, context );
+		calls += 1;
+		if ( r == 0.0f )
+			break;
+		if ( 0.0f <= r && r <= 1.0f )
+			clip = r;
+	}
+	free( rows );
+	return calls;
 }

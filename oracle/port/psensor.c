@@ -34,7 +34,7 @@ static float distance_with_radii( const Shape* a, xform xfA, const Shape* b, xfo
 	ShapeProxy pa = p_shape_proxy( &a->g );
 	ShapeProxy pb = p_shape_proxy( &b->g );
 	SimplexCache cache = { 0 };
-	float d = p_shape_distance( &pa, &pb, xfA, xfB, &cache, NULL, NULL );
+	float d = p_shape_distance( &pa, &pb, xfA, xfB, &cache, NULL, NULL, NULL );
 	if ( d > 0.1f * P_LINEAR_SLOP )
 	{
 		d = d - pa.radius - pb.radius;

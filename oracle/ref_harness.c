@@ -608,6 +608,41 @@ int ref_get_sensor_events( int w, int* begin, int* end, int cap, int* endCount )
 	return ev.beginCount;
 }
 
+typedef struct RefCast
+{
+	orc_cast_fn fn;
+	void* context;
+} RefCast;
+
+static float ref_cast_trampoline( b2ShapeId id, b2Vec2 point, b2Vec2 normal, float fraction, void* context )
+{
+	RefCast* c = (RefCast*)context;
+	return c->fn( id.index1 - 1, point.x, point.y, normal.x, normal.y, fraction, c->context );
+}
+
+// b2World_CastRay with the callback form (the reference's tree order)
+int ref_world_cast_ray( int w, double ox, double oy, double tx, double ty, long long cat, long long mask, orc_cast_fn fn,
+						void* context )
+{
+	RefCast c = { fn, context };
+	b2QueryFilter f = { (uint64_t)cat, (uint64_t)mask };
+	b2World_CastRay( s_worlds[w], ( b2Vec2 ){ (float)ox, (float)oy }, ( b2Vec2 ){ (float)tx, (float)ty }, f,
+					 ref_cast_trampoline, &c );
+	return 0;
+}
+
+void ref_world_explode( int w, long long maskBits, double px, double py, double radius, double falloff,
+						double impulsePerLength )
+{
+	b2ExplosionDef def = b2DefaultExplosionDef();
+	def.maskBits = (uint64_t)maskBits;
+	def.position = ( b2Vec2 ){ (float)px, (float)py };
+	def.radius = (float)radius;
+	def.falloff = (float)falloff;
+	def.impulsePerLength = (float)impulsePerLength;
+	b2World_Explode( s_worlds[w], &def );
+}
+
 // user callbacks: b2World_SetCustomFilterCallback / SetPreSolveCallback
 // with the 0-based shape ids and the manifold view of f2d_defs.h
 typedef struct RefCallbacks

@@ -63,6 +63,42 @@ def pre_solve_rule(a, b, m):
     return True
 
 
+BLASTS = {150: (-1.5, 2.0, 3.0, 2.0, 2.5, -1), 250: (-0.5, 2.0, 3.0, 2.0, 2.5, -1), 330: (0.3, 2.0, 3.0, 0.0, 4.0, 1)}
+
+
+def blast(world, f):
+    """The explosions of the explode parity cases (frame -> x, y, radius,
+    falloff, impulse per length, mask)."""
+    if f in BLASTS:
+        x, y, r, fo, ipl, mask = BLASTS[f]
+        world.explode(x, y, r, fo, ipl, mask=mask)
+
+
+def ray_answers(world, rays):
+    """Closest hit through a closest-hit callback, and every hit through an
+    all-hits callback (sorted), per ray."""
+    out = []
+    for o, t in rays:
+        best = {}
+
+        def closest(s, p, n, f):
+            if f == 0.0:
+                return -1.0
+            best["r"] = (s, tuple(np.float32(v).view(np.uint32).item() for v in (*p, *n, f)))
+            return f
+
+        hits = []
+
+        def every(s, p, n, f):
+            hits.append((s, np.float32(f).view(np.uint32).item()))
+            return 1.0
+
+        world.cast_ray(o[0], o[1], t[0], t[1], closest)
+        world.cast_ray(o[0], o[1], t[0], t[1], every)
+        out.append((best.get("r"), sorted(hits)))
+    return out
+
+
 def install_callbacks(world):
     world.set_custom_filter(filter_rule)
     world.set_pre_solve(pre_solve_rule)

@@ -16,7 +16,7 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import compare_contacts, install_callbacks
+from parity import blast, compare_contacts, install_callbacks, ray_answers
 from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
                                 replay, sensor_rows)
 
@@ -96,6 +96,44 @@ def test_gpu_matches_port_bit_exact(gpu_lib, port_lib, name, wkw, scene, kw, fra
     assert g.sync() == 0
     if name in ("pile_dense_overflow", "overflow_heap", "overflow_platforms", "overflow_long"):
         assert saw_overflow, "scene meant to exercise the overflow colour did not reach it"
+    g.close()
+    p.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_explode_matches_port(gpu_lib, port_lib, sleep):
+    """b2World_Explode between steps (waking sleeping sets, falloff, mask):
+    bit-identical to the oracle."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (g, p):
+        scenes.build(w, "pile", count=300, seed=3, width=20.0, height=30.0)
+    for f in range(1, 401):
+        blast(g, f)
+        blast(p, f)
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
+    assert g.sync() == 0
+    g.close()
+    p.close()
+
+
+def test_gpu_cast_ray_callback_matches_port(gpu_lib, port_lib):
+    """Callback ray casts (closest-hit and all-hits callbacks) on the chain
+    scene against the oracle."""
+    wkw = dict(enableSleep=0, enableContinuous=0)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (g, p):
+        scenes.build(w, "chain_terrain", count=150)
+    for _ in range(60):
+        g.step(1.0 / 60.0, 4)
+        p.step(1.0 / 60.0, 4)
+    rng = np.random.default_rng(1)
+    rays = [(rng.uniform(-20, 20, 2) + [0.0, 15.0], rng.uniform(-30, 30, 2)) for _ in range(150)]
+    assert ray_answers(g, rays) == ray_answers(p, rays)
     g.close()
     p.close()
 

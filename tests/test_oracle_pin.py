@@ -13,7 +13,8 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import compare_contacts, filter_rule, install_callbacks, new_contacts, pre_solve_rule
+from parity import (blast, compare_contacts, filter_rule, install_callbacks, new_contacts, pre_solve_rule,
+                    ray_answers)
 
 
 def lockstep(ref, port, frames, each=None):
@@ -162,6 +163,41 @@ def test_port_callbacks_with_reference(ref_lib, port_lib):
     install_callbacks(port)
     lockstep_full(ref, port, 300)
     assert seen["filter"] > 100 and seen["pre"] > 100, seen
+    ref.close()
+    port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_explode_with_reference(ref_lib, port_lib, sleep):
+    """b2World_Explode three times into a settling pile (falloff, no falloff,
+    a category mask), in lock step."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        scenes.build(w, "pile", count=300, seed=3, width=20.0, height=30.0)
+    for f in range(1, 401):
+        blast(ref, f)
+        blast(port, f)
+        lockstep_full(ref, port, 1, start=f)
+    ref.close()
+    port.close()
+
+
+def test_port_cast_ray_callback_with_reference(ref_lib, port_lib):
+    """b2World_CastRay's callback form: the closest-hit and all-hits
+    callbacks end with the reference's answers."""
+    wkw = dict(enableSleep=0, enableContinuous=0)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        scenes.build(w, "chain_terrain", count=150)
+    lockstep_full(ref, port, 60)
+    rng = np.random.default_rng(1)
+    rays = [(rng.uniform(-20, 20, 2) + [0.0, 15.0], rng.uniform(-30, 30, 2)) for _ in range(150)]
+    a, b = ray_answers(ref, rays), ray_answers(port, rays)
+    assert a == b
+    assert sum(len(x[1]) for x in a) > 100
     ref.close()
     port.close()
 
