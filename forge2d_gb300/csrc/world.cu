@@ -714,6 +714,7 @@ static void flush_uploads( HostWorld* W )
 		up( d.jdef1, W->jdef1, j, j + 1, W->stream );
 		up( d.jdef2, W->jdef2, j, j + 1, W->stream );
 		up( d.jdef3, W->jdef3, j, j + 1, W->stream );
+		up( d.jflags, W->jflags, j, j + 1, W->stream );
 	}
 	W->jointDirty.clear();
 	if ( W->sensorsDirty )
@@ -1616,6 +1617,52 @@ extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_de
 			break;
 	}
 	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
+}
+
+// Motor of a revolute, prismatic, wheel or distance joint (revolute_joint.c:
+// 129-168, prismatic_joint.c:111-150, wheel_joint.c:100-140, distance_joint.c:
+// 138-175): speed and the maximum torque (revolute, wheel) or force
+// (prismatic, distance); switching the motor clears its impulse. No wake.
+extern "C" F2D_API void f2d_joint_set_motor( int32_t index1, int32_t wg, int32_t enable, double speed, double maxMotor )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return;
+	int j = index1 - 1;
+	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) )
+		return;
+	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
+	float4& d2 = W->jdef2[j];
+	int impulseLane; // the motor impulse's component of the jimp row
+	if ( type == 0 || type == F2D_JOINT_PRISMATIC || type == F2D_JOINT_WHEEL )
+	{
+		d2.z = (float)maxMotor;
+		d2.w = (float)speed;
+		impulseLane = type == F2D_JOINT_WHEEL ? 2 : 3;
+	}
+	else if ( type == F2D_JOINT_DISTANCE )
+	{
+		d2.y = (float)maxMotor;
+		d2.z = (float)speed;
+		impulseLane = 3;
+	}
+	else
+		return;
+	bool on = ( W->jflags[j] & JF_MOTOR ) != 0;
+	if ( ( enable != 0 ) != on )
+	{
+		W->jflags[j] ^= JF_MOTOR;
+		if ( j < W->jointUploaded )
+		{
+			float zero = 0.0f;
+			cudaMemcpyAsync( (float*)( W->d.jimp + j ) + impulseLane, &zero, sizeof( float ), cudaMemcpyHostToDevice,
+							 W->stream );
+			cudaStreamSynchronize( W->stream );
+		}
+	}
+	if ( j < W->jointUploaded &&
+		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
+		W->jointDirty.push_back( j );
 }
 
 // b2MouseJoint_SetTarget (mouse_joint.c:14-19): no wake

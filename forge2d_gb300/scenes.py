@@ -415,13 +415,14 @@ def sensor_field(b, count=300, seed=8, width=30.0, height=40.0):
     return pile(b, count=count, seed=seed, width=width, height=height, sensor_visitors=True)
 
 
-def joint_rigs(b, copies=3):
+def joint_rigs(b, copies=3, motors=None):
     """Prismatic, wheel, motor, mouse and filter joints, ``copies`` times over
     a ground box: an elevator (vertical prismatic with limits and a motor)
     carrying a box, a horizontal prismatic spring, a two-wheeled cart on
     sprung, limited, motored wheel joints, a box led by a motor joint, a box
     held up by a mouse joint, and two overlapping boxes a filter joint keeps
-    from colliding. Returns the mouse joints' ids."""
+    from colliding. Returns the mouse joints' ids; the ids of the motorised
+    joints (lift, wheels) are appended to ``motors`` when given."""
     g = b.create_body(body_def(type=STATIC, positionY=-1.0))
     b.create_box(g, shape_def(), 30.0 * copies, 1.0)
     mice = []
@@ -431,10 +432,12 @@ def joint_rigs(b, copies=3):
         b.create_box(base, shape_def(), 0.2, 0.2)
         lift = b.create_body(body_def(type=DYNAMIC, positionX=x0, positionY=1.0))
         b.create_box(lift, shape_def(), 1.0, 0.1)
-        b.create_joint(joint_def(type=JOINT_PRISMATIC, bodyA=base, bodyB=lift, localAnchorAY=0.5,
-                                 localAxisAX=0.0, localAxisAY=1.0, enableLimit=1, lowerTranslation=0.0,
-                                 upperTranslation=3.0 + k, enableMotor=1, maxMotorForce=60.0,
-                                 motorSpeed=1.0 + 0.5 * k))
+        jid = b.create_joint(joint_def(type=JOINT_PRISMATIC, bodyA=base, bodyB=lift, localAnchorAY=0.5,
+                                       localAxisAX=0.0, localAxisAY=1.0, enableLimit=1, lowerTranslation=0.0,
+                                       upperTranslation=3.0 + k, enableMotor=1, maxMotorForce=60.0,
+                                       motorSpeed=1.0 + 0.5 * k))
+        if motors is not None:
+            motors.append(jid)
         cargo = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 0.2, positionY=1.5))
         b.create_box(cargo, shape_def(), 0.3, 0.3)
         slider = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 4.0, positionY=3.0))
@@ -448,11 +451,13 @@ def joint_rigs(b, copies=3):
         for side in (-1.0, 1.0):
             wheel = b.create_body(body_def(type=DYNAMIC, positionX=cx + 0.9 * side, positionY=cy - 0.6))
             b.create_circle(wheel, shape_def(friction=0.9), 0.0, 0.0, 0.35)
-            b.create_joint(joint_def(type=JOINT_WHEEL, bodyA=chassis, bodyB=wheel, localAnchorAX=0.9 * side,
-                                     localAnchorAY=-0.6, localAxisAX=0.0, localAxisAY=1.0, enableSpring=1,
-                                     hertz=4.0, dampingRatio=0.7, enableLimit=1, lowerTranslation=-0.25,
-                                     upperTranslation=0.25, enableMotor=1, maxMotorTorque=8.0,
-                                     motorSpeed=-2.0 - k))
+            jid = b.create_joint(joint_def(type=JOINT_WHEEL, bodyA=chassis, bodyB=wheel, localAnchorAX=0.9 * side,
+                                           localAnchorAY=-0.6, localAxisAX=0.0, localAxisAY=1.0, enableSpring=1,
+                                           hertz=4.0, dampingRatio=0.7, enableLimit=1, lowerTranslation=-0.25,
+                                           upperTranslation=0.25, enableMotor=1, maxMotorTorque=8.0,
+                                           motorSpeed=-2.0 - k))
+            if motors is not None:
+                motors.append(jid)
         led = b.create_body(body_def(type=DYNAMIC, positionX=x0 + 15.0, positionY=0.5))
         b.create_box(led, shape_def(), 0.5, 0.5)
         b.create_joint(joint_def(type=JOINT_MOTOR, bodyA=g, bodyB=led, linearOffsetX=x0 + 16.0,

@@ -216,6 +216,10 @@ class GpuWorld:
         ok = self.lib.f2d_create_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def set_motor(self, joint, enable, speed, max_motor):
+        """Motor of a revolute, prismatic, wheel or distance joint."""
+        self.lib.f2d_joint_set_motor(joint[0], joint[1], int(enable), speed, max_motor)
+
     def mouse_set_target(self, joint, x, y):
         self.lib.f2d_mouse_joint_set_target(joint[0], joint[1], x, y)
 

@@ -314,6 +314,13 @@ F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_def* def, int
 /* RawBox2D.mouseJointSetTarget (raw_box2d.dart:913 -> b2MouseJoint_SetTarget,
  * mouse_joint.c:14): takes effect at the next step; wakes nothing. */
 F2D_API void f2d_mouse_joint_set_target( int32_t index1, int32_t worldAndGeneration, double x, double y );
+/* RawBox2D.{revolute,prismatic,wheel,distance}JointEnableMotor / SetMotorSpeed /
+ * SetMaxMotorTorque|Force (raw_box2d.dart:823-850 and the revolute, prismatic
+ * and wheel sections): the motor's state, speed and maximum torque (revolute,
+ * wheel) or force (prismatic, distance) in one call; takes effect at the next
+ * step; wakes nothing. */
+F2D_API void f2d_joint_set_motor( int32_t index1, int32_t worldAndGeneration, int32_t enable, double speed,
+								  double maxMotor );
 F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
 										   int32_t* worldAndGeneration );
 F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );

@@ -168,6 +168,7 @@ def _bind(lib, prefix):
         "set_custom_filter": (None, [i, FILTER_FN, C.c_void_p]),
         "set_pre_solve": (None, [i, PRESOLVE_FN, C.c_void_p]),
         "world_explode": (None, [i, C.c_longlong, d, d, d, d, d]),
+        "joint_set_motor": (None, [i, i, i, d, d]),
         "world_cast_ray": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, CAST_FN, C.c_void_p]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
@@ -231,6 +232,10 @@ class _CpuWorld:
         """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float."""
         cb = CAST_FN(lambda s, px, py, nx, ny, f, ctx: float(fn(s, (px, py), (nx, ny), f)))
         return self._fns["world_cast_ray"](self.w, ox, oy, tx, ty, cat, mask, cb, None)
+
+    def set_motor(self, joint, enable, speed, max_motor):
+        """Motor of a revolute, prismatic, wheel or distance joint."""
+        self._fns["joint_set_motor"](self.w, joint, int(enable), speed, max_motor)
 
     def explode(self, x, y, radius, falloff, impulse_per_length, mask=-1):
         """b2World_Explode."""

@@ -856,6 +856,31 @@ int orc_create_joint( int wi, const f2d_joint_def* d )
 	return id;
 }
 
+// revolute_joint.c:129-168, prismatic_joint.c:111-150, wheel_joint.c:100-140,
+// distance_joint.c:138-175: motor setters of the motorised joint types (no
+// wake; switching the motor clears its impulse). `maxMotor` is the revolute
+// and wheel torque, the prismatic and distance force.
+void orc_joint_set_motor( int wi, int jid, int enable, double speed, double maxMotor )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || jid < 0 || jid >= w->jointCount )
+		return;
+	Joint* j = w->joints + jid;
+	if ( j->type != P_JOINT_REVOLUTE && j->type != P_JOINT_PRISMATIC && j->type != P_JOINT_WHEEL &&
+		 j->type != P_JOINT_DISTANCE )
+		return;
+	if ( ( enable != 0 ) != ( j->enableMotor != 0 ) )
+	{
+		j->enableMotor = enable != 0;
+		j->motorImpulse = 0.0f;
+	}
+	j->motorSpeed = (float)speed;
+	if ( j->type == P_JOINT_REVOLUTE || j->type == P_JOINT_WHEEL )
+		j->maxMotorTorque = (float)maxMotor;
+	else
+		j->maxMotorForce = (float)maxMotor;
+}
+
 // mouse_joint.c:14-19 b2MouseJoint_SetTarget (no wake)
 void orc_mouse_joint_set_target( int wi, int jid, double x, double y )
 {

@@ -608,6 +608,38 @@ int ref_get_sensor_events( int w, int* begin, int* end, int cap, int* endCount )
 	return ev.beginCount;
 }
 
+void ref_joint_set_motor( int w, int j, int enable, double speed, double maxMotor )
+{
+	b2World* world = ref_world( w );
+	b2Joint* joint = b2JointArray_Get( &world->joints, j );
+	b2JointId id = { j + 1, world->worldId, joint->generation };
+	switch ( b2Joint_GetType( id ) )
+	{
+		case b2_revoluteJoint:
+			b2RevoluteJoint_EnableMotor( id, enable != 0 );
+			b2RevoluteJoint_SetMotorSpeed( id, (float)speed );
+			b2RevoluteJoint_SetMaxMotorTorque( id, (float)maxMotor );
+			break;
+		case b2_prismaticJoint:
+			b2PrismaticJoint_EnableMotor( id, enable != 0 );
+			b2PrismaticJoint_SetMotorSpeed( id, (float)speed );
+			b2PrismaticJoint_SetMaxMotorForce( id, (float)maxMotor );
+			break;
+		case b2_wheelJoint:
+			b2WheelJoint_EnableMotor( id, enable != 0 );
+			b2WheelJoint_SetMotorSpeed( id, (float)speed );
+			b2WheelJoint_SetMaxMotorTorque( id, (float)maxMotor );
+			break;
+		case b2_distanceJoint:
+			b2DistanceJoint_EnableMotor( id, enable != 0 );
+			b2DistanceJoint_SetMotorSpeed( id, (float)speed );
+			b2DistanceJoint_SetMaxMotorForce( id, (float)maxMotor );
+			break;
+		default:
+			break;
+	}
+}
+
 typedef struct RefCast
 {
 	orc_cast_fn fn;

@@ -99,6 +99,17 @@ def ray_answers(world, rays):
     return out
 
 
+# frame -> (enable, speed, max) applied to every motorised joint of joint_rigs
+MOTOR_EDITS = {100: (1, 3.0, 40.0), 160: (0, 3.0, 40.0), 220: (1, -1.5, 15.0), 280: (1, 0.5, 90.0)}
+
+
+def edit_motors(world, motors, f):
+    if f in MOTOR_EDITS:
+        enable, speed, mx = MOTOR_EDITS[f]
+        for k, j in enumerate(motors):
+            world.set_motor(j, enable, speed * (1.0 + 0.25 * (k % 3)), mx)
+
+
 def install_callbacks(world):
     world.set_custom_filter(filter_rule)
     world.set_pre_solve(pre_solve_rule)

@@ -16,7 +16,7 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import blast, compare_contacts, install_callbacks, ray_answers
+from parity import blast, compare_contacts, edit_motors, install_callbacks, ray_answers
 from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
                                 replay, sensor_rows)
 
@@ -112,6 +112,27 @@ def test_gpu_explode_matches_port(gpu_lib, port_lib, sleep):
     for f in range(1, 401):
         blast(g, f)
         blast(p, f)
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
+    assert g.sync() == 0
+    g.close()
+    p.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_motor_edits_match_port(gpu_lib, port_lib, sleep):
+    """Joint motors switched and retuned between steps (uploaded with the
+    next step; switching clears the motor impulse on the device)."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    mg, mp = [], []
+    scenes.build(g, "joint_rigs", copies=3, motors=mg)
+    scenes.build(p, "joint_rigs", copies=3, motors=mp)
+    for f in range(1, 341):
+        edit_motors(g, mg, f)
+        edit_motors(p, mp, f)
         assert g.step(1.0 / 60.0, 4) == 0
         p.step(1.0 / 60.0, 4)
         assert_bodies_equal(g, p, f)

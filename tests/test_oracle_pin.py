@@ -13,8 +13,8 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import (blast, compare_contacts, filter_rule, install_callbacks, new_contacts, pre_solve_rule,
-                    ray_answers)
+from parity import (blast, compare_contacts, edit_motors, filter_rule, install_callbacks, new_contacts,
+                    pre_solve_rule, ray_answers)
 
 
 def lockstep(ref, port, frames, each=None):
@@ -179,6 +179,25 @@ def test_port_explode_with_reference(ref_lib, port_lib, sleep):
     for f in range(1, 401):
         blast(ref, f)
         blast(port, f)
+        lockstep_full(ref, port, 1, start=f)
+    ref.close()
+    port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_motor_edits_with_reference(ref_lib, port_lib, sleep):
+    """Motor speed, maximum and on/off of prismatic and wheel joints changed
+    between steps (b2*Joint_EnableMotor / SetMotorSpeed / SetMax*)."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    mr, mp = [], []
+    scenes.build(ref, "joint_rigs", copies=3, motors=mr)
+    scenes.build(port, "joint_rigs", copies=3, motors=mp)
+    assert mr == mp and len(mr) == 9
+    for f in range(1, 341):
+        edit_motors(ref, mr, f)
+        edit_motors(port, mp, f)
         lockstep_full(ref, port, 1, start=f)
     ref.close()
     port.close()
