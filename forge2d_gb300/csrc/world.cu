@@ -87,6 +87,7 @@ struct HostWorld
 	TreeIds trees[3];
 	std::vector<int> staticShapes;
 	std::vector<int> sensorShapes; // sensor shapes in creation order (sensor.c)
+	float invH = 0.0f; // inverse substep of the last step (world.c:745-755)
 	f2d_custom_filter_fn customFilter = nullptr;
 	void* customFilterContext = nullptr;
 	f2d_pre_solve_fn preSolve = nullptr;
@@ -1619,6 +1620,89 @@ extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_de
 	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
 }
 
+// b2Joint_GetConstraintForce / GetConstraintTorque (joint.c:1061-1135) with
+// the per-type b2Get*JointForce / Torque: the last step's impulses times its
+// inverse substep; out3 = force.x, force.y, torque
+extern "C" F2D_API void f2d_joint_get_constraint( int32_t index1, int32_t wg, float* out3 )
+{
+	out3[0] = out3[1] = out3[2] = 0.0f;
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return;
+	int j = index1 - 1;
+	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) || j >= W->jointUploaded )
+		return;
+	cudaStreamSynchronize( W->stream );
+	float4 imp, p3;
+	float2 imp2;
+	cudaMemcpy( &imp, W->d.jimp + j, sizeof( imp ), cudaMemcpyDeviceToHost );
+	cudaMemcpy( &imp2, W->d.jimp2 + j, sizeof( imp2 ), cudaMemcpyDeviceToHost );
+	cudaMemcpy( &p3, W->d.jprep3 + j, sizeof( p3 ), cudaMemcpyDeviceToHost );
+	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
+	int a = W->jbody[j].x, b = W->jbody[j].y;
+	float inv_h = W->invH;
+	fv2 f = mk( 0.0f, 0.0f );
+	float t = 0.0f;
+	auto xf_of = [&]( int body ) {
+		pull_body( W, body );
+		float4 x = W->xf[body];
+		fxf r;
+		r.p = mk( x.x, x.y );
+		r.q.c = x.z;
+		r.q.s = x.w;
+		return r;
+	};
+	switch ( type )
+	{
+		case 0: // revolute_joint.c:176-187
+			f = vscale( inv_h, mk( imp.x, imp.y ) );
+			t = inv_h * ( imp.w + imp2.x - imp2.y );
+			break;
+		case F2D_JOINT_WELD:  // weld_joint.c:66-75
+		case F2D_JOINT_MOTOR: // motor_joint.c:74-83
+		case F2D_JOINT_MOUSE: // mouse_joint.c:66-75
+			f = vscale( inv_h, mk( imp.x, imp.y ) );
+			t = inv_h * imp.z;
+			break;
+		case F2D_JOINT_DISTANCE: // distance_joint.c:185-198
+		{
+			float4 d0 = W->jdef0[j];
+			fv2 pA = xpoint( xf_of( a ), mk( d0.x, d0.y ) );
+			fv2 pB = xpoint( xf_of( b ), mk( d0.z, d0.w ) );
+			fv2 axis = vnormalize( vsub( pB, pA ) );
+			float force = ( imp.x + imp.y - imp.z + imp.w ) * inv_h;
+			f = vscale( force, axis );
+			break;
+		}
+		case F2D_JOINT_PRISMATIC: // prismatic_joint.c:211-232
+		{
+			float4 d1 = W->jdef1[j];
+			fv2 axisA = rrot( xf_of( a ).q, mk( d1.x, d1.y ) );
+			fv2 perpA = vleft( axisA );
+			float perpForce = inv_h * imp.x;
+			float axialForce = inv_h * ( imp.w + imp2.x - imp2.y );
+			f = vadd( vscale( perpForce, perpA ), vscale( axialForce, axisA ) );
+			t = inv_h * imp.y;
+			break;
+		}
+		case F2D_JOINT_WHEEL: // wheel_joint.c:147-165 (axis of the last step)
+		{
+			fv2 axisA = mk( p3.x, p3.y );
+			fv2 perpA = vleft( axisA );
+			float perpForce = inv_h * imp.x;
+			float axialForce = inv_h * ( imp.y + imp2.x - imp2.y );
+			f = vadd( vscale( perpForce, perpA ), vscale( axialForce, axisA ) );
+			t = inv_h * imp.z;
+			break;
+		}
+		default:
+			break;
+	}
+	out3[0] = f.x;
+	out3[1] = f.y;
+	out3[2] = t;
+}
+
 // Motor of a revolute, prismatic, wheel or distance joint (revolute_joint.c:
 // 129-168, prismatic_joint.c:111-150, wheel_joint.c:100-140, distance_joint.c:
 // 138-175): speed and the maximum torque (revolute, wheel) or force
@@ -1887,6 +1971,8 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	if ( dt == 0.0f )
 		return 0;
 	int subSteps = subStepCount < 1 ? 1 : subStepCount;
+	float inv_dt = 1.0f / dt;
+	W->invH = (float)subSteps * inv_dt;
 	// collect the status of earlier steps without blocking
 	if ( W->stepped && cudaEventQuery( W->evStop ) == cudaSuccess )
 		W->statusAccum |= *W->hostError;

@@ -216,6 +216,12 @@ class GpuWorld:
         ok = self.lib.f2d_create_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
         return self._ret(ok, i1, wg)
 
+    def joint_constraint(self, joint):
+        """(force.x, force.y, torque) of the last step."""
+        out = np.zeros(3, np.float32)
+        self.lib.f2d_joint_get_constraint(joint[0], joint[1], out.ctypes.data_as(C.POINTER(C.c_float)))
+        return out
+
     def set_motor(self, joint, enable, speed, max_motor):
         """Motor of a revolute, prismatic, wheel or distance joint."""
         self.lib.f2d_joint_set_motor(joint[0], joint[1], int(enable), speed, max_motor)

@@ -169,6 +169,7 @@ def _bind(lib, prefix):
         "set_pre_solve": (None, [i, PRESOLVE_FN, C.c_void_p]),
         "world_explode": (None, [i, C.c_longlong, d, d, d, d, d]),
         "joint_set_motor": (None, [i, i, i, d, d]),
+        "joint_get_constraint": (None, [i, i, _P(C.c_float)]),
         "world_cast_ray": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, CAST_FN, C.c_void_p]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
         "create_polygon_shape": (i, [i, i, _P(ShapeDef), _P(d), i, d]),
@@ -232,6 +233,12 @@ class _CpuWorld:
         """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float."""
         cb = CAST_FN(lambda s, px, py, nx, ny, f, ctx: float(fn(s, (px, py), (nx, ny), f)))
         return self._fns["world_cast_ray"](self.w, ox, oy, tx, ty, cat, mask, cb, None)
+
+    def joint_constraint(self, joint):
+        """(force.x, force.y, torque) of the last step."""
+        out = np.zeros(3, np.float32)
+        self._fns["joint_get_constraint"](self.w, joint, out.ctypes.data_as(_P(C.c_float)))
+        return out
 
     def set_motor(self, joint, enable, speed, max_motor):
         """Motor of a revolute, prismatic, wheel or distance joint."""

@@ -881,6 +881,70 @@ void orc_joint_set_motor( int wi, int jid, int enable, double speed, double maxM
 		j->maxMotorForce = (float)maxMotor;
 }
 
+// joint.c:1061-1135 b2Joint_GetConstraintForce / GetConstraintTorque with the
+// per-type b2Get*JointForce / Torque (the last step's impulses times inv_h);
+// out3 = force.x, force.y, torque
+void orc_joint_get_constraint( int wi, int jid, float* out3 )
+{
+	out3[0] = out3[1] = out3[2] = 0.0f;
+	World* w = p_world( wi );
+	if ( w == NULL || jid < 0 || jid >= w->jointCount )
+		return;
+	const Joint* j = w->joints + jid;
+	float inv_h = w->inv_h;
+	v2 f = V( 0.0f, 0.0f );
+	float t = 0.0f;
+	switch ( j->type )
+	{
+		case P_JOINT_REVOLUTE: // revolute_joint.c:176-187
+			f = mulSV( inv_h, j->linearImpulse );
+			t = inv_h * ( j->motorImpulse + j->lowerImpulse - j->upperImpulse );
+			break;
+		case P_JOINT_WELD: // weld_joint.c:66-75
+			f = mulSV( inv_h, j->linearImpulse );
+			t = inv_h * j->angularImpulse;
+			break;
+		case P_JOINT_MOTOR: // motor_joint.c:74-83
+		case P_JOINT_MOUSE: // mouse_joint.c:66-75
+			f = mulSV( inv_h, j->linearImpulse );
+			t = inv_h * j->angularImpulse;
+			break;
+		case P_JOINT_DISTANCE: // distance_joint.c:185-198
+		{
+			v2 pA = xfPoint( w->bodies[j->bodyA].xf, j->localOriginAnchorA );
+			v2 pB = xfPoint( w->bodies[j->bodyB].xf, j->localOriginAnchorB );
+			v2 axis = normalize( sub( pB, pA ) );
+			float force = ( j->impulse + j->lowerImpulse - j->upperImpulse + j->motorImpulse ) * inv_h;
+			f = mulSV( force, axis );
+			break;
+		}
+		case P_JOINT_PRISMATIC: // prismatic_joint.c:211-232
+		{
+			v2 axisA = rotate( w->bodies[j->bodyA].xf.q, j->localAxisA );
+			v2 perpA = leftPerp( axisA );
+			float perpForce = inv_h * j->prismaticImpulse.x;
+			float axialForce = inv_h * ( j->motorImpulse + j->lowerImpulse - j->upperImpulse );
+			f = add( mulSV( perpForce, perpA ), mulSV( axialForce, axisA ) );
+			t = inv_h * j->prismaticImpulse.y;
+			break;
+		}
+		case P_JOINT_WHEEL: // wheel_joint.c:147-165 (axis of the last step)
+		{
+			v2 perpA = leftPerp( j->axisA );
+			float perpForce = inv_h * j->perpImpulse;
+			float axialForce = inv_h * ( j->springImpulse + j->lowerImpulse - j->upperImpulse );
+			f = add( mulSV( perpForce, perpA ), mulSV( axialForce, j->axisA ) );
+			t = inv_h * j->motorImpulse;
+			break;
+		}
+		default:
+			break;
+	}
+	out3[0] = f.x;
+	out3[1] = f.y;
+	out3[2] = t;
+}
+
 // mouse_joint.c:14-19 b2MouseJoint_SetTarget (no wake)
 void orc_mouse_joint_set_target( int wi, int jid, double x, double y )
 {

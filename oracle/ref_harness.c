@@ -640,6 +640,20 @@ void ref_joint_set_motor( int w, int j, int enable, double speed, double maxMoto
 	}
 }
 
+void ref_joint_get_constraint( int w, int j, float* out3 )
+{
+	b2World* world = ref_world( w );
+	out3[0] = out3[1] = out3[2] = 0.0f;
+	if ( j < 0 || j >= world->joints.count || world->joints.data[j].jointId != j )
+		return;
+	b2Joint* joint = b2JointArray_Get( &world->joints, j );
+	b2JointId id = { j + 1, world->worldId, joint->generation };
+	b2Vec2 f = b2Joint_GetConstraintForce( id );
+	out3[0] = f.x;
+	out3[1] = f.y;
+	out3[2] = b2Joint_GetConstraintTorque( id );
+}
+
 typedef struct RefCast
 {
 	orc_cast_fn fn;

@@ -141,6 +141,31 @@ def test_gpu_motor_edits_match_port(gpu_lib, port_lib, sleep):
     p.close()
 
 
+@pytest.mark.parametrize("scene,kw", [("joint_gallery", dict(copies=2)), ("joint_zoo", dict(copies=2)),
+                                      ("joint_rigs", dict(copies=2))], ids=["revolute", "weld_distance", "rigs"])
+def test_gpu_joint_constraint_matches_port(gpu_lib, port_lib, scene, kw):
+    """Constraint force and torque of every joint (b2Joint_GetConstraint*)."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(g, scene, **kw)
+    scenes.build(p, scene, **kw)
+    world0 = g._body_ids[0][1] & 0xffff
+    nonzero = 0
+    for f in range(1, 201):
+        g.step(1.0 / 60.0, 4)
+        p.step(1.0 / 60.0, 4)
+        if f % 20 == 0:
+            for j in range(40):
+                a = g.joint_constraint((j + 1, world0 | (1 << 16)))
+                b = p.joint_constraint(j)
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (f, j, a, b)
+                nonzero += bool(np.any(a != 0))
+    assert nonzero > 50
+    g.close()
+    p.close()
+
+
 def test_gpu_cast_ray_callback_matches_port(gpu_lib, port_lib):
     """Callback ray casts (closest-hit and all-hits callbacks) on the chain
     scene against the oracle."""

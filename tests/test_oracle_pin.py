@@ -203,6 +203,28 @@ def test_port_motor_edits_with_reference(ref_lib, port_lib, sleep):
     port.close()
 
 
+@pytest.mark.parametrize("scene,kw", [("joint_gallery", dict(copies=2)), ("joint_zoo", dict(copies=2)),
+                                      ("joint_rigs", dict(copies=2))], ids=["revolute", "weld_distance", "rigs"])
+def test_port_joint_constraint_with_reference(ref_lib, port_lib, scene, kw):
+    """b2Joint_GetConstraintForce / Torque of every joint, every 20 frames."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, scene, **kw)
+    scenes.build(port, scene, **kw)
+    nonzero = 0
+    for f in range(1, 201):
+        lockstep_full(ref, port, 1, start=f)
+        if f % 20 == 0:
+            for j in range(60):
+                a, b = ref.joint_constraint(j), port.joint_constraint(j)
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (f, j, a, b)
+                nonzero += bool(np.any(a != 0))
+    assert nonzero > 50
+    ref.close()
+    port.close()
+
+
 def test_port_cast_ray_callback_with_reference(ref_lib, port_lib):
     """b2World_CastRay's callback form: the closest-hit and all-hits
     callbacks end with the reference's answers."""
