@@ -1620,6 +1620,45 @@ extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_de
 	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
 }
 
+// Limit of a revolute, prismatic or wheel joint (revolute_joint.c:84-127,
+// prismatic_joint.c:68-109, wheel_joint.c:57-98): EnableLimit then SetLimits;
+// a change clears the limit impulses (jimp2); bounds stored as min, max.
+extern "C" F2D_API void f2d_joint_set_limits( int32_t index1, int32_t wg, int32_t enable, double lower, double upper )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr )
+		return;
+	int j = index1 - 1;
+	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) )
+		return;
+	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
+	if ( type != 0 && type != F2D_JOINT_PRISMATIC && type != F2D_JOINT_WHEEL )
+		return;
+	bool clear = false;
+	if ( ( enable != 0 ) != ( ( W->jflags[j] & JF_LIMIT ) != 0 ) )
+	{
+		W->jflags[j] ^= JF_LIMIT;
+		clear = true;
+	}
+	float lo = (float)lower, hi = (float)upper;
+	float4& d2 = W->jdef2[j];
+	if ( lo != d2.x || hi != d2.y )
+	{
+		d2.x = fmin_s( lo, hi );
+		d2.y = fmax_s( lo, hi );
+		clear = true;
+	}
+	if ( clear && j < W->jointUploaded )
+	{
+		float2 zero = make_float2( 0.0f, 0.0f );
+		cudaMemcpyAsync( W->d.jimp2 + j, &zero, sizeof( zero ), cudaMemcpyHostToDevice, W->stream );
+		cudaStreamSynchronize( W->stream );
+	}
+	if ( j < W->jointUploaded &&
+		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
+		W->jointDirty.push_back( j );
+}
+
 // b2Joint_GetConstraintForce / GetConstraintTorque (joint.c:1061-1135) with
 // the per-type b2Get*JointForce / Torque: the last step's impulses times its
 // inverse substep; out3 = force.x, force.y, torque

@@ -168,6 +168,7 @@ _SIGS = [
     ("f2d_create_joint", _i, [_i, _P(JointDef), _P(_i), _P(_i)]),
     ("f2d_mouse_joint_set_target", None, [_i, _i, _d, _d]),
     ("f2d_joint_set_motor", None, [_i, _i, _i, _d, _d]),
+    ("f2d_joint_set_limits", None, [_i, _i, _i, _d, _d]),
     ("f2d_joint_get_constraint", None, [_i, _i, _P(_f)]),
     ("f2d_create_chain", _i, [_i, _i, _P(_d), _i, _P(_d), _i, _i64, _i64, _i, _i, _i, _P(_i), _P(_i)]),
     ("f2d_chain_get_segments", _i, [_i, _i, _P(_i), _i]),

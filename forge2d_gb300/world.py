@@ -222,6 +222,10 @@ class GpuWorld:
         self.lib.f2d_joint_get_constraint(joint[0], joint[1], out.ctypes.data_as(C.POINTER(C.c_float)))
         return out
 
+    def set_limits(self, joint, enable, lower, upper):
+        """Limit of a revolute, prismatic or wheel joint."""
+        self.lib.f2d_joint_set_limits(joint[0], joint[1], int(enable), lower, upper)
+
     def set_motor(self, joint, enable, speed, max_motor):
         """Motor of a revolute, prismatic, wheel or distance joint."""
         self.lib.f2d_joint_set_motor(joint[0], joint[1], int(enable), speed, max_motor)

@@ -325,6 +325,11 @@ F2D_API void f2d_joint_set_motor( int32_t index1, int32_t worldAndGeneration, in
  * 748-751 -> b2Joint_GetConstraintForce / Torque, joint.c:1061): the last
  * step's constraint force and torque; out3 = force.x, force.y, torque. */
 F2D_API void f2d_joint_get_constraint( int32_t index1, int32_t worldAndGeneration, float* out3 );
+/* RawBox2D.{revolute,prismatic,wheel}JointEnableLimit / SetLimits: the limit's
+ * state and bounds (angles for the revolute joint, translations otherwise)
+ * in one call; takes effect at the next step; wakes nothing. */
+F2D_API void f2d_joint_set_limits( int32_t index1, int32_t worldAndGeneration, int32_t enable, double lower,
+								   double upper );
 F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
 										   int32_t* worldAndGeneration );
 F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );

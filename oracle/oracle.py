@@ -169,6 +169,7 @@ def _bind(lib, prefix):
         "set_pre_solve": (None, [i, PRESOLVE_FN, C.c_void_p]),
         "world_explode": (None, [i, C.c_longlong, d, d, d, d, d]),
         "joint_set_motor": (None, [i, i, i, d, d]),
+        "joint_set_limits": (None, [i, i, i, d, d]),
         "joint_get_constraint": (None, [i, i, _P(C.c_float)]),
         "world_cast_ray": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, CAST_FN, C.c_void_p]),
         "create_box_shape": (i, [i, i, _P(ShapeDef), d, d, d, d, d, d, d]),
@@ -239,6 +240,10 @@ class _CpuWorld:
         out = np.zeros(3, np.float32)
         self._fns["joint_get_constraint"](self.w, joint, out.ctypes.data_as(_P(C.c_float)))
         return out
+
+    def set_limits(self, joint, enable, lower, upper):
+        """Limit of a revolute, prismatic or wheel joint."""
+        self._fns["joint_set_limits"](self.w, joint, int(enable), lower, upper)
 
     def set_motor(self, joint, enable, speed, max_motor):
         """Motor of a revolute, prismatic, wheel or distance joint."""

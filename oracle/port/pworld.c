@@ -881,6 +881,35 @@ void orc_joint_set_motor( int wi, int jid, int enable, double speed, double maxM
 		j->maxMotorForce = (float)maxMotor;
 }
 
+// revolute_joint.c:84-127, prismatic_joint.c:68-109, wheel_joint.c:57-98:
+// b2*Joint_EnableLimit then b2*Joint_SetLimits (a change clears the limit
+// impulses; the bounds are stored as min, max)
+void orc_joint_set_limits( int wi, int jid, int enable, double lower, double upper )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || jid < 0 || jid >= w->jointCount )
+		return;
+	Joint* j = w->joints + jid;
+	if ( j->type != P_JOINT_REVOLUTE && j->type != P_JOINT_PRISMATIC && j->type != P_JOINT_WHEEL )
+		return;
+	if ( ( enable != 0 ) != ( j->enableLimit != 0 ) )
+	{
+		j->enableLimit = enable != 0;
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+	}
+	float lo = (float)lower, hi = (float)upper;
+	float* cl = j->type == P_JOINT_REVOLUTE ? &j->lowerAngle : &j->lowerTranslation;
+	float* cu = j->type == P_JOINT_REVOLUTE ? &j->upperAngle : &j->upperTranslation;
+	if ( lo != *cl || hi != *cu )
+	{
+		*cl = fminp( lo, hi );
+		*cu = fmaxp( lo, hi );
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+	}
+}
+
 // joint.c:1061-1135 b2Joint_GetConstraintForce / GetConstraintTorque with the
 // per-type b2Get*JointForce / Torque (the last step's impulses times inv_h);
 // out3 = force.x, force.y, torque

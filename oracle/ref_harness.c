@@ -640,6 +640,30 @@ void ref_joint_set_motor( int w, int j, int enable, double speed, double maxMoto
 	}
 }
 
+void ref_joint_set_limits( int w, int j, int enable, double lower, double upper )
+{
+	b2World* world = ref_world( w );
+	b2Joint* joint = b2JointArray_Get( &world->joints, j );
+	b2JointId id = { j + 1, world->worldId, joint->generation };
+	switch ( b2Joint_GetType( id ) )
+	{
+		case b2_revoluteJoint:
+			b2RevoluteJoint_EnableLimit( id, enable != 0 );
+			b2RevoluteJoint_SetLimits( id, (float)lower, (float)upper );
+			break;
+		case b2_prismaticJoint:
+			b2PrismaticJoint_EnableLimit( id, enable != 0 );
+			b2PrismaticJoint_SetLimits( id, (float)lower, (float)upper );
+			break;
+		case b2_wheelJoint:
+			b2WheelJoint_EnableLimit( id, enable != 0 );
+			b2WheelJoint_SetLimits( id, (float)lower, (float)upper );
+			break;
+		default:
+			break;
+	}
+}
+
 void ref_joint_get_constraint( int w, int j, float* out3 )
 {
 	b2World* world = ref_world( w );

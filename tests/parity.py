@@ -103,7 +103,15 @@ def ray_answers(world, rays):
 MOTOR_EDITS = {100: (1, 3.0, 40.0), 160: (0, 3.0, 40.0), 220: (1, -1.5, 15.0), 280: (1, 0.5, 90.0)}
 
 
+# frame -> (enable, lower, upper) for the same joints' limits
+LIMIT_EDITS = {120: (1, -0.5, 0.8), 190: (0, -0.5, 0.8), 240: (1, 0.6, -0.2), 300: (1, -0.1, 0.1)}
+
+
 def edit_motors(world, motors, f):
+    if f in LIMIT_EDITS:
+        enable, lo, hi = LIMIT_EDITS[f]
+        for j in motors:
+            world.set_limits(j, enable, lo, hi)
     if f in MOTOR_EDITS:
         enable, speed, mx = MOTOR_EDITS[f]
         for k, j in enumerate(motors):
