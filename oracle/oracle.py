@@ -197,6 +197,8 @@ def _bind(lib, prefix):
         "create_joint": (i, [i, _P(JointDef)]),
         "mouse_joint_set_target": (None, [i, i, d, d]),
         "world_enable_sleeping": (None, [i, i]),
+        "tree_order": (i, [i, i, _P(i), i]),
+        "tree_stats": (None, [i, i, _P(i)]),
     }
     out = {}
     for name, (res, args) in sig.items():
@@ -262,6 +264,19 @@ class _CpuWorld:
         """fn(shapeA, shapeB, ManifoldView) -> bool; None removes it."""
         self._presolve_cb = PRESOLVE_FN(lambda a, b, m, ctx: int(bool(fn(a, b, m.contents)))) if fn else PRESOLVE_FN()
         self._fns["set_pre_solve"](self.w, self._presolve_cb, None)
+
+    def tree_order(self, body_type):
+        """Leaf shape ids of the broadphase tree of ``body_type`` (0 static,
+        1 kinematic, 2 dynamic) in depth-first visiting order."""
+        out = np.zeros(self._fns["shape_capacity"](self.w) + 1, np.int32)
+        n = self._fns["tree_order"](self.w, body_type, out.ctypes.data_as(_P(C.c_int)), len(out))
+        return out[:n].copy()
+
+    def tree_stats(self, body_type):
+        """(nodeCount, nodeCapacity, proxyCount, height, root, freeList)."""
+        out = np.zeros(6, np.int32)
+        self._fns["tree_stats"](self.w, body_type, out.ctypes.data_as(_P(C.c_int)))
+        return out
 
     def close(self):
         if self.w is not None and self.w >= 0:

@@ -1,9 +1,10 @@
 // Continuous collision of fast non-bullet bodies against static shapes.
 // TEST INFRASTRUCTURE (oracle). Restates solver.c:196-388
 // (b2ContinuousQueryCallback) and :390-541 (b2SolveContinuous) of
-// packages/forge2d/third_party/box2d/src. The reference visits candidate
-// static shapes in static-tree order and narrows the running fraction with
-// each hit; this port visits them in shape-id order.
+// packages/forge2d/third_party/box2d/src. Candidate static shapes are
+// visited in the static tree's depth-first order (p_static_order), as the
+// reference's query meets them: the running fraction narrows with each hit,
+// so the order shows in the last bits of the result.
 #include "port.h"
 
 static int should_collide_filters( const Shape* a, const Shape* b )
@@ -78,9 +79,9 @@ void p_solve_continuous( World* w, int bodyId )
 			continue;
 		v2 centroid1 = xfPoint( xf1, fastShape->localCentroid );
 		v2 centroid2 = xfPoint( xf2, fastShape->localCentroid );
-		for ( int k = 0; k < w->staticShapeCount; ++k )
+		for ( int k = 0; k < w->staticOrderCount; ++k )
 		{
-			int si = w->staticShapes[k];
+			int si = w->staticOrder[k];
 			Shape* shape = w->shapes + si;
 			if ( shape->used == 0 || shape->proxyKey == P_NULL || ( shape->proxyKey & 3 ) != BODY_STATIC )
 				continue;

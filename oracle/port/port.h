@@ -7,6 +7,7 @@
 
 #include "f2d_defs.h"
 #include "pmath.h"
+#include "ptree.h"
 
 enum
 {
@@ -314,15 +315,6 @@ typedef struct Island
 	int constraintRemoveCount;
 } Island;
 
-typedef struct TreeIds
-{
-	int* freeStack;
-	int freeCount;
-	int freeCap;
-	int nodeCount;
-	int proxyCount;
-} TreeIds;
-
 typedef struct PairSet
 {
 	uint64_t* keys; // 0 = empty, key+1 stored
@@ -373,7 +365,8 @@ typedef struct World
 	int* chainFree;
 	int chainFreeCount;
 
-	TreeIds trees[3];
+	// the reference's three broadphase trees (static, kinematic, dynamic)
+	RTree trees[3];
 	PairSet pairs;
 
 	// move buffer in deterministic order (shape ids)
@@ -410,8 +403,10 @@ typedef struct World
 	// gravity; shapes of different sub-worlds never interact
 	int subCount; // 0 = no sub-worlds (one world, world gravity)
 	v2 subGravity;
-	int* staticShapes; // static-body shapes with a proxy, ascending id
-	int staticShapeCount, staticShapeCap;
+	// static shapes in the static tree's depth-first visiting order (the
+	// order continuous collision meets them), rebuilt when that tree changes
+	int* staticOrder;
+	int staticOrderCount, staticOrderCap, staticOrderDirty;
 	int* constraintOrder; // contact id per constraint slot
 	int constraintOrderCap;
 	int* jointOrder; // graph-colour joints grouped by colour
@@ -468,6 +463,7 @@ void p_try_sleep_island( World* w, int islandId );
 void p_wake_solver_set( World* w, int setId );
 void p_sleep_islands( World* w, const unsigned char* awakeIslandBits, int splitCandidate );
 int p_body_awake( const World* w, int bodyId );
+void p_static_order( World* w );
 int p_new_sleeping_set( World* w );
 void p_set_joint_add( World* w, int setId, int jid );
 void p_merge_solver_sets( World* w, int setId1, int setId2 );

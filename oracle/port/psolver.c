@@ -683,6 +683,8 @@ void p_solve( World* w, float dt, int subStepCount )
 
 	// world.c:709: the step's move events start empty
 	w->moveEventCount = 0;
+	// continuous collision walks the static tree's order (finalize is parallel)
+	p_static_order( w );
 	// solver.c:1194-1220: merge islands linked this step; nothing to solve
 	// without awake bodies
 	p_merge_awake_islands( w );
@@ -926,20 +928,26 @@ void p_solve( World* w, float dt, int subStepCount )
 		}
 	}
 
-	// enlarge proxies / build the move buffer in body order (solver.c:1820-1913)
-	for ( int b = 0; b < w->bodyCount; ++b )
+	// solver.c:1842-1905: enlarge the tree proxies of the flagged bodies and
+	// build the move array, in awake-set order (the enlarged-body bitset is
+	// indexed by awake-set position), each body's shapes in list order
 	{
-		Body* body = w->bodies + b;
-		if ( !body_awake( body ) || body->enlargeAABB == 0 )
-			continue;
-		body->enlargeAABB = 0;
-		for ( int s = body->headShape; s != P_NULL; s = w->shapes[s].nextShape )
+		const IntArr* awake = &w->sets[SET_AWAKE].bodies;
+		for ( int k = 0; k < awake->count; ++k )
 		{
-			Shape* sh = w->shapes + s;
-			if ( sh->enlarged )
+			Body* body = w->bodies + awake->data[k];
+			if ( body->enlargeAABB == 0 )
+				continue;
+			body->enlargeAABB = 0;
+			for ( int s = body->headShape; s != P_NULL; s = w->shapes[s].nextShape )
 			{
-				sh->enlarged = 0;
-				p_push_move( w, s );
+				Shape* sh = w->shapes + s;
+				if ( sh->enlarged )
+				{
+					sh->enlarged = 0;
+					rt_enlarge_proxy( w->trees + ( sh->proxyKey & 3 ), sh->proxyKey >> 2, sh->fatAABB );
+					p_push_move( w, s );
+				}
 			}
 		}
 	}

@@ -5,14 +5,11 @@
 // constraint_graph.c, id_pool.c.
 //
 // Contact creation order. The reference creates new contacts in broadphase
-// move-array order x dynamic-tree traversal order (broad_phase.c:376-474),
-// which only its incremental tree can reproduce. This port orders the pairs
-// found in a step by their 64-bit shape-pair key instead ("native order", the
-// same rule the CUDA path uses), and offers a parity mode (orc_set_contact_plan)
-// in which the caller dictates the contact id of each pair created in the next
-// step, e.g. the ids the reference itself assigned. Everything downstream of
-// the ids -- colour assignment, overflow order, events -- then follows the
-// reference's own rules.
+// move-array order x tree order (broad_phase.c:311-474); this port keeps the
+// reference's trees operation by operation (ptree.c), so its contacts are
+// created in the reference's order and take the reference's ids. A parity
+// mode (orc_set_contact_plan) remains, in which the caller dictates the
+// contact id of each pair created in the next step.
 #include "port.h"
 
 #include <stdlib.h>
@@ -146,28 +143,6 @@ static void pairset_rehash( PairSet* s, int ncap )
 }
 
 // ---------------------------------------------------------------------------
-// dynamic-tree node ids (dynamic_tree.c:122-167, :625-800): a proxy takes a
-// leaf node, and a parent node when the tree already holds a proxy. Tree
-// rebuilds free and re-allocate the same number of internal nodes LIFO, so
-// they leave the free list unchanged and need no emulation.
-// ---------------------------------------------------------------------------
-static int tree_alloc( TreeIds* t )
-{
-	if ( t->freeCount > 0 )
-		return t->freeStack[--t->freeCount];
-	return t->nodeCount++;
-}
-
-static int tree_create_proxy( TreeIds* t )
-{
-	int leaf = tree_alloc( t );
-	if ( t->proxyCount > 0 )
-		(void)tree_alloc( t );
-	t->proxyCount += 1;
-	return leaf;
-}
-
-// ---------------------------------------------------------------------------
 // world lifecycle (world.c:100-340)
 // ---------------------------------------------------------------------------
 int orc_create_world( const f2d_world_def* d, int workerCount )
@@ -196,6 +171,8 @@ int orc_create_world( const f2d_world_def* d, int workerCount )
 	w->enableSleep = d->enableSleep != 0;
 	w->enableContinuous = d->enableContinuous != 0;
 	w->enableWarmStarting = 1;
+	for ( int i = 0; i < 3; ++i )
+		rt_init( w->trees + i );
 	p_sets_init( w );
 	return slot;
 }
@@ -226,7 +203,7 @@ void orc_destroy_world( int wi )
 	ia_free( &w->sensorBegin );
 	ia_free( &w->sensorEnd );
 	for ( int i = 0; i < 3; ++i )
-		free( w->trees[i].freeStack );
+		rt_release_all( w->trees + i );
 	free( w->pairs.keys );
 	free( w->moveArray );
 	free( w->overflowContacts );
@@ -240,10 +217,34 @@ void orc_destroy_world( int wi )
 	free( w->moveEventBodies );
 	free( w->moveEventXf );
 	free( w->constraintOrder );
-	free( w->staticShapes );
+	free( w->staticOrder );
 	free( w->jointOrder );
 	p_sets_free( w );
 	memset( w, 0, sizeof( *w ) );
+}
+
+// The static tree's leaves in its depth-first visiting order (categories of
+// zero never visited), rebuilt after the tree changed. Continuous collision
+// walks this list with its box test: a query visits the overlapping leaves
+// in exactly this relative order (dynamic_tree.c:1114-1170).
+static int static_visit( int proxyId, int shape, void* context )
+{
+	(void)proxyId;
+	World* w = context;
+	w->staticOrder = grow( w->staticOrder, &w->staticOrderCap, w->staticOrderCount + 1, sizeof( int ) );
+	w->staticOrder[w->staticOrderCount++] = shape;
+	return 1;
+}
+
+void p_static_order( World* w )
+{
+	if ( w->staticOrderDirty == 0 )
+		return;
+	w->staticOrderDirty = 0;
+	w->staticOrderCount = 0;
+	const RTree* t = w->trees + BODY_STATIC;
+	if ( t->root != P_NULL )
+		rt_query( t, t->nodes[t->root].aabb, ~0ull, static_visit, w );
 }
 
 // id_pool.c:19-38: LIFO free list
@@ -447,20 +448,11 @@ static int create_shape( World* w, int bodyId, const f2d_shape_def* d, const Geo
 		s->fatAABB.lo.y = aabb.lo.y - margin;
 		s->fatAABB.hi.x = aabb.hi.x + margin;
 		s->fatAABB.hi.y = aabb.hi.y + margin;
-		int proxyId = tree_create_proxy( w->trees + proxyType );
+		// shape.c:901-911 b2CreateShapeProxy -> broad_phase.c:91-103
+		int proxyId = rt_create_proxy( w->trees + proxyType, s->fatAABB, s->categoryBits, id );
 		s->proxyKey = ( proxyId << 2 ) | proxyType;
 		if ( proxyType == BODY_STATIC )
-		{
-			// candidates of continuous collision, kept in shape-id order
-			w->staticShapes = grow( w->staticShapes, &w->staticShapeCap, w->staticShapeCount + 1, sizeof( int ) );
-			int k = w->staticShapeCount++;
-			while ( k > 0 && w->staticShapes[k - 1] > id )
-			{
-				w->staticShapes[k] = w->staticShapes[k - 1];
-				k -= 1;
-			}
-			w->staticShapes[k] = id;
-		}
+			w->staticOrderDirty = 1;
 		int force = d->invokeContactCreation != 0 || d->isSensor != 0;
 		if ( proxyType != BODY_STATIC || force )
 			push_move( w, id );
@@ -1157,12 +1149,13 @@ void orc_set_contact_plan( int wi, const int* rows, int count )
 }
 
 // ---------------------------------------------------------------------------
-// broadphase pair finding (broad_phase.c:160-474). The reference queries its
-// dynamic trees with each moved proxy; the pair SET it produces is every
-// filter-passing pair with overlapping fat AABBs, at least one dynamic
-// proxy and at least one moved proxy, that has no contact yet. This port
-// finds the same set with a uniform grid (small proxies) plus a brute-force
-// list (large proxies).
+// broadphase pair finding (broad_phase.c:160-474 b2PairQueryCallback,
+// b2FindPairsTask, b2UpdateBroadPhasePairs). Every moved proxy, in move-array
+// order, queries the kinematic and static trees (dynamic proxies only) and
+// then the dynamic tree; each pair the callback keeps is PREPENDED to the
+// proxy's list, so a proxy's pairs come out dynamic-tree first, each tree's
+// leaves left to right (the reverse of the depth-first visit). Contacts are
+// created proxy by proxy in that order.
 // ---------------------------------------------------------------------------
 typedef struct Cand
 {
@@ -1170,93 +1163,57 @@ typedef struct Cand
 	int a, b; // ordered by proxy key: a has the smaller proxy key
 } Cand;
 
-static int cmp_cand( const void* x, const void* y )
+typedef struct PairQuery
 {
-	const Cand* a = x;
-	const Cand* b = y;
-	return a->key < b->key ? -1 : ( a->key > b->key ? 1 : 0 );
-}
+	World* w;
+	int queryShape, queryProxyKey, treeType;
+	Cand* list;
+	int n, cap;
+} PairQuery;
 
-typedef struct GridEntry
+// broad_phase.c:160-266 b2PairQueryCallback (the custom filter, its last
+// test, runs after the queries: see update_pairs)
+static int pair_visit( int proxyId, int shape, void* context )
 {
-	int64_t cell;
-	int shape;
-} GridEntry;
-
-// Stable LSD radix sort by cell key (16-bit digits, passes whose digit is
-// the same for every entry skipped). Entries are inserted in shape order, so
-// the result is ordered by (cell, shape).
-static void sort_grid( GridEntry* a, int n )
-{
-	if ( n < 2 )
-		return;
-	GridEntry* tmp = malloc( sizeof( GridEntry ) * (size_t)n );
-	int* hist = malloc( sizeof( int ) * 65536 );
-	for ( int pass = 0; pass < 4; ++pass )
+	PairQuery* q = context;
+	World* w = q->w;
+	int proxyKey = ( proxyId << 2 ) | q->treeType;
+	if ( proxyKey == q->queryProxyKey )
+		return 1;
+	Shape* other = w->shapes + shape;
+	if ( ( q->queryProxyKey & 3 ) == BODY_DYNAMIC )
 	{
-		int shift = 16 * pass;
-		memset( hist, 0, sizeof( int ) * 65536 );
-		for ( int i = 0; i < n; ++i )
-			hist[( (uint64_t)a[i].cell >> shift ) & 0xffff] += 1;
-		if ( hist[( (uint64_t)a[0].cell >> shift ) & 0xffff] == n )
-			continue;
-		int sum = 0;
-		for ( int d = 0; d < 65536; ++d )
-		{
-			int c = hist[d];
-			hist[d] = sum;
-			sum += c;
-		}
-		for ( int i = 0; i < n; ++i )
-			tmp[hist[( (uint64_t)a[i].cell >> shift ) & 0xffff]++] = a[i];
-		memcpy( a, tmp, sizeof( GridEntry ) * (size_t)n );
+		// both moving: the pair belongs to the smaller proxy key's query
+		if ( q->treeType == BODY_DYNAMIC && proxyKey < q->queryProxyKey && other->moved )
+			return 1;
 	}
-	free( hist );
-	free( tmp );
-}
-
-static int shape_active( World* w, int s )
-{
-	Shape* sh = w->shapes + s;
-	return sh->used && sh->proxyKey != P_NULL;
-}
-
-static void consider_pair( World* w, int s1, int s2, Cand** cands, int* n, int* cap )
-{
-	Shape* a = w->shapes + s1;
-	Shape* b = w->shapes + s2;
-	if ( a->moved == 0 && b->moved == 0 )
-		return;
-	int ta = a->proxyKey & 3, tb = b->proxyKey & 3;
-	if ( ta != BODY_DYNAMIC && tb != BODY_DYNAMIC )
-		return;
-	if ( boxOverlaps( a->fatAABB, b->fatAABB ) == 0 )
-		return;
-	uint64_t key = pair_key( s1, s2 );
+	else if ( other->moved )
+		return 1;
+	uint64_t key = pair_key( shape, q->queryShape );
 	if ( pairset_contains( &w->pairs, key ) )
-		return;
-	if ( a->bodyId == b->bodyId || a->sub != b->sub )
-		return;
-	if ( a->isSensor || b->isSensor )
-		return;
-	if ( should_shapes_collide( a, b ) == 0 )
-		return;
-	if ( should_bodies_collide( w, a->bodyId, b->bodyId ) == 0 )
-		return;
-	*cands = grow( *cands, cap, *n + 1, sizeof( Cand ) );
-	Cand* c = *cands + *n;
+		return 1;
+	int a = proxyKey < q->queryProxyKey ? shape : q->queryShape;
+	int b = proxyKey < q->queryProxyKey ? q->queryShape : shape;
+	Shape* sa = w->shapes + a;
+	Shape* sb = w->shapes + b;
+	if ( sa->bodyId == sb->bodyId )
+		return 1;
+	if ( sa->sensorIndex != P_NULL || sb->sensorIndex != P_NULL )
+		return 1;
+	if ( should_shapes_collide( sa, sb ) == 0 )
+		return 1;
+	if ( should_bodies_collide( w, sa->bodyId, sb->bodyId ) == 0 )
+		return 1;
+	// sub-worlds of the batched form never meet (each is a world of its own)
+	if ( sa->sub != sb->sub )
+		return 1;
+	q->list = grow( q->list, &q->cap, q->n + 1, sizeof( Cand ) );
+	Cand* c = q->list + q->n;
 	c->key = key;
-	if ( a->proxyKey < b->proxyKey )
-	{
-		c->a = s1;
-		c->b = s2;
-	}
-	else
-	{
-		c->a = s2;
-		c->b = s1;
-	}
-	*n += 1;
+	c->a = a;
+	c->b = b;
+	q->n += 1;
+	return 1;
 }
 
 static void update_pairs( World* w )
@@ -1266,138 +1223,67 @@ static void update_pairs( World* w )
 		w->planCount = 0;
 		return;
 	}
-	int ns = w->shapeCount;
-	// cell size: largest fat extent of non-static proxies, clamped
-	float cell = 0.0f;
-	for ( int s = 0; s < ns; ++s )
-	{
-		if ( !shape_active( w, s ) || ( w->shapes[s].proxyKey & 3 ) == BODY_STATIC )
-			continue;
-		box2 f = w->shapes[s].fatAABB;
-		cell = fmaxp( cell, fmaxp( f.hi.x - f.lo.x, f.hi.y - f.lo.y ) );
-	}
-	if ( cell < 0.5f )
-		cell = 0.5f;
-	float inv = 1.0f / cell;
-	int* large = NULL;
-	int nl = 0, capl = 0;
-	// shapes no larger than a cell go into every cell their fat AABB
-	// touches (at most 4); larger ones are paired against all shapes
-	int* gcount = malloc( sizeof( int ) * (size_t)( ns + 1 ) );
-#pragma omp parallel for schedule( static )
-	for ( int s = 0; s < ns; ++s )
-	{
-		gcount[s] = 0;
-		if ( !shape_active( w, s ) )
-			continue;
-		box2 f = w->shapes[s].fatAABB;
-		if ( f.hi.x - f.lo.x > cell || f.hi.y - f.lo.y > cell )
-			continue;
-		int64_t x0 = (int64_t)floorf( f.lo.x * inv ), x1 = (int64_t)floorf( f.hi.x * inv );
-		int64_t y0 = (int64_t)floorf( f.lo.y * inv ), y1 = (int64_t)floorf( f.hi.y * inv );
-		gcount[s] = (int)( ( x1 - x0 + 1 ) * ( y1 - y0 + 1 ) );
-	}
-	int ng = 0;
-	for ( int s = 0; s < ns; ++s )
-	{
-		int c = gcount[s];
-		gcount[s] = ng;
-		ng += c;
-		if ( c == 0 && shape_active( w, s ) )
-		{
-			large = grow( large, &capl, nl + 1, sizeof( int ) );
-			large[nl++] = s;
-		}
-	}
-	GridEntry* grid = malloc( sizeof( GridEntry ) * (size_t)( ng > 0 ? ng : 1 ) );
-#pragma omp parallel for schedule( static )
-	for ( int s = 0; s < ns; ++s )
-	{
-		if ( !shape_active( w, s ) )
-			continue;
-		box2 f = w->shapes[s].fatAABB;
-		if ( f.hi.x - f.lo.x > cell || f.hi.y - f.lo.y > cell )
-			continue;
-		int64_t x0 = (int64_t)floorf( f.lo.x * inv ), x1 = (int64_t)floorf( f.hi.x * inv );
-		int64_t y0 = (int64_t)floorf( f.lo.y * inv ), y1 = (int64_t)floorf( f.hi.y * inv );
-		int k = gcount[s];
-		for ( int64_t x = x0; x <= x1; ++x )
-			for ( int64_t y = y0; y <= y1; ++y )
-			{
-				grid[k].cell = (int64_t)( ( (uint64_t)(uint32_t)x << 32 ) | (uint64_t)(uint32_t)y );
-				grid[k].shape = s;
-				k += 1;
-			}
-	}
-	free( gcount );
-	sort_grid( grid, ng );
-	// cell boundaries, then every cell and every large shape is examined in
-	// parallel into per-thread candidate lists (their order does not matter:
-	// the candidates are sorted by key below)
-	int* cellStart = NULL;
-	int ncell = 0, capcell = 0;
-	for ( int i = 0; i < ng; ++i )
-		if ( i == 0 || grid[i].cell != grid[i - 1].cell )
-		{
-			cellStart = grow( cellStart, &capcell, ncell + 2, sizeof( int ) );
-			cellStart[ncell++] = i;
-		}
-	if ( cellStart )
-		cellStart[ncell] = ng;
+	int nm = w->moveCount;
 	int nthreads = 1;
 #ifdef _OPENMP
 	nthreads = omp_get_max_threads();
 #endif
-	Cand** tc = calloc( (size_t)nthreads, sizeof( Cand* ) );
-	int* tn = calloc( (size_t)nthreads, sizeof( int ) );
-	int* tcap = calloc( (size_t)nthreads, sizeof( int ) );
+	// broad_phase.c:311-372: each thread takes one contiguous run of the move
+	// array (schedule static), so the threads' lists concatenated in thread
+	// order are the move-array order
+	PairQuery* tq = calloc( (size_t)nthreads, sizeof( PairQuery ) );
 #pragma omp parallel
 	{
 		int t = 0;
 #ifdef _OPENMP
 		t = omp_get_thread_num();
 #endif
-#pragma omp for schedule( dynamic, 64 )
-		for ( int ci = 0; ci < ncell; ++ci )
+		PairQuery* q = tq + t;
+		q->w = w;
+#pragma omp for schedule( static )
+		for ( int i = 0; i < nm; ++i )
 		{
-			int i = cellStart[ci], j = cellStart[ci + 1];
-			for ( int p = i; p < j; ++p )
-				for ( int q = p + 1; q < j; ++q )
-					consider_pair( w, grid[p].shape, grid[q].shape, tc + t, tn + t, tcap + t );
-		}
-		// large-large pairs are visited twice; the sort+unique below drops repeats
-#pragma omp for schedule( dynamic, 1024 )
-		for ( int s = 0; s < ns; ++s )
-		{
-			if ( !shape_active( w, s ) )
+			int shapeId = w->moveArray[i];
+			Shape* s = w->shapes + shapeId;
+			if ( s->used == 0 || s->proxyKey == P_NULL )
 				continue;
-			for ( int i = 0; i < nl; ++i )
-				if ( s != large[i] )
-					consider_pair( w, large[i], s, tc + t, tn + t, tcap + t );
+			int type = s->proxyKey & 3;
+			const RTree* base = w->trees + type;
+			box2 fat = base->nodes[s->proxyKey >> 2].aabb;
+			q->queryShape = shapeId;
+			q->queryProxyKey = s->proxyKey;
+			int first = q->n;
+			if ( type == BODY_DYNAMIC )
+			{
+				q->treeType = BODY_KINEMATIC;
+				rt_query( w->trees + BODY_KINEMATIC, fat, ~0ull, pair_visit, q );
+				q->treeType = BODY_STATIC;
+				rt_query( w->trees + BODY_STATIC, fat, ~0ull, pair_visit, q );
+			}
+			q->treeType = BODY_DYNAMIC;
+			rt_query( w->trees + BODY_DYNAMIC, fat, ~0ull, pair_visit, q );
+			// prepend order: this proxy's pairs in reverse visiting order
+			for ( int lo = first, hi = q->n - 1; lo < hi; ++lo, --hi )
+			{
+				Cand tmp = q->list[lo];
+				q->list[lo] = q->list[hi];
+				q->list[hi] = tmp;
+			}
 		}
 	}
 	Cand* cands = NULL;
 	int nc = 0, capc = 0;
 	for ( int t = 0; t < nthreads; ++t )
 	{
-		if ( tn[t] > 0 )
+		if ( tq[t].n > 0 )
 		{
-			cands = grow( cands, &capc, nc + tn[t], sizeof( Cand ) );
-			memcpy( cands + nc, tc[t], sizeof( Cand ) * (size_t)tn[t] );
-			nc += tn[t];
+			cands = grow( cands, &capc, nc + tq[t].n, sizeof( Cand ) );
+			memcpy( cands + nc, tq[t].list, sizeof( Cand ) * (size_t)tq[t].n );
+			nc += tq[t].n;
 		}
-		free( tc[t] );
+		free( tq[t].list );
 	}
-	free( tc );
-	free( tn );
-	free( tcap );
-	free( cellStart );
-	qsort( cands, (size_t)nc, sizeof( Cand ), cmp_cand );
-	int u = 0;
-	for ( int i = 0; i < nc; ++i )
-		if ( u == 0 || cands[u - 1].key != cands[i].key )
-			cands[u++] = cands[i];
-	nc = u;
+	free( tq );
 	// broad_phase.c:267-278: the custom filter is the last test of a new pair
 	// (A is the shape with the smaller proxy key)
 	if ( w->customFilter != NULL )
@@ -1408,7 +1294,7 @@ static void update_pairs( World* w )
 				cands[v++] = cands[i];
 		nc = v;
 	}
-	// create contacts in native order (ascending pair key) or per plan. A
+	// create contacts in the reference's order or per plan. A
 	// plan's contacts are created in the order the reference's id pool handed
 	// their ids out (LIFO free list, then fresh ids), which is the order the
 	// reference created them in; that order is visible in the bodies'
@@ -1482,8 +1368,6 @@ static void update_pairs( World* w )
 	w->moveCount = 0;
 	w->planCount = 0;
 	free( cands );
-	free( grid );
-	free( large );
 }
 
 // ---------------------------------------------------------------------------
@@ -1827,6 +1711,12 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 		return;
 	double t0 = p_now();
 	update_pairs( w );
+	// world.c:488-502 b2Collide -> broad_phase.c:488-492: the dynamic and
+	// kinematic trees are rebuilt over their enlarged nodes every step (the
+	// reference runs this beside the narrowphase; nothing reads the trees
+	// before the finalize that follows)
+	rt_rebuild( w->trees + BODY_DYNAMIC, 0 );
+	rt_rebuild( w->trees + BODY_KINEMATIC, 0 );
 	double t1 = p_now();
 	int nc = w->contactCount;
 #pragma omp parallel for schedule( dynamic, 256 )
@@ -2145,4 +2035,43 @@ int orc_get_move_events( int wi, int* ints, float* floats, int cap )
 void p_push_move( World* w, int shapeId )
 {
 	push_move( w, shapeId );
+}
+
+// The restated tree of one body type: leaf shape ids in depth-first visiting
+// order, and the node pool's counters (as ref_tree_order / ref_tree_stats)
+typedef struct TreeOrderCtx
+{
+	int* out;
+	int cap;
+	int n;
+} TreeOrderCtx;
+
+static int tree_order_visit( int proxyId, int shape, void* context )
+{
+	(void)proxyId;
+	TreeOrderCtx* c = context;
+	if ( c->n < c->cap )
+		c->out[c->n] = shape;
+	c->n += 1;
+	return 1;
+}
+
+int orc_tree_order( int wi, int type, int* out, int cap )
+{
+	const RTree* t = p_world( wi )->trees + type;
+	TreeOrderCtx c = { out, cap, 0 };
+	if ( t->root != P_NULL )
+		rt_query( t, t->nodes[t->root].aabb, ~0ull, tree_order_visit, &c );
+	return c.n;
+}
+
+void orc_tree_stats( int wi, int type, int* out6 )
+{
+	const RTree* t = p_world( wi )->trees + type;
+	out6[0] = t->count;
+	out6[1] = t->cap;
+	out6[2] = t->proxyCount;
+	out6[3] = t->root == P_NULL ? 0 : t->nodes[t->root].height;
+	out6[4] = t->root;
+	out6[5] = t->freeList;
 }

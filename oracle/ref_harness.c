@@ -1091,3 +1091,47 @@ int ref_joint_color( int w, int joint )
 	b2World* world = ref_world( w );
 	return world->joints.data[joint].colorIndex;
 }
+
+// ---------------------------------------------------------------------------
+// Broadphase tree of one body type (0 static, 1 kinematic, 2 dynamic): the
+// shape ids of its leaves in the order b2DynamicTree_Query visits them (the
+// whole tree, every category), and the node pool's counters. These pin the
+// restatement's tree topology and proxy ids.
+// ---------------------------------------------------------------------------
+typedef struct TreeOrderCtx
+{
+	int* out;
+	int cap;
+	int n;
+} TreeOrderCtx;
+
+static bool ref_tree_visit( int proxyId, uint64_t userData, void* context )
+{
+	(void)proxyId;
+	TreeOrderCtx* c = context;
+	if ( c->n < c->cap )
+		c->out[c->n] = (int)userData;
+	c->n += 1;
+	return true;
+}
+
+int ref_tree_order( int w, int type, int* out, int cap )
+{
+	const b2DynamicTree* t = ref_world( w )->broadPhase.trees + type;
+	TreeOrderCtx c = { out, cap, 0 };
+	if ( t->root != B2_NULL_INDEX )
+		b2DynamicTree_Query( t, b2DynamicTree_GetRootBounds( t ), B2_DEFAULT_MASK_BITS, ref_tree_visit, &c );
+	return c.n;
+}
+
+// nodeCount, nodeCapacity, proxyCount, height, root, freeList
+void ref_tree_stats( int w, int type, int* out6 )
+{
+	const b2DynamicTree* t = ref_world( w )->broadPhase.trees + type;
+	out6[0] = t->nodeCount;
+	out6[1] = t->nodeCapacity;
+	out6[2] = t->proxyCount;
+	out6[3] = b2DynamicTree_GetHeight( t );
+	out6[4] = t->root;
+	out6[5] = t->freeList;
+}

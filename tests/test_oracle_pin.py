@@ -1,10 +1,13 @@
 """Pins the CPU restatement to the live reference (needs the reference
 checkout; skipped elsewhere, where the committed fixtures stand in).
 
-The reference world and the port are stepped in lock step; before each port
-step the port is handed the contact ids the reference created in that step
-(parity mode). Bodies, manifolds, colours, events and query answers must then
-agree bit for bit.
+The reference world and the port are stepped in lock step with nothing
+passed between them: the port keeps the reference's broadphase trees, so it
+creates contacts in the reference's order with the reference's ids. Bodies,
+manifolds, colours, events, tree orders and query answers must agree bit for
+bit. One case also drives the port in parity mode (the reference's contact
+ids handed over before each step), which the GPU replays of recorded
+fixtures use.
 """
 from __future__ import annotations
 
@@ -17,14 +20,21 @@ from parity import (blast, compare_contacts, edit_motors, filter_rule, install_c
                     pre_solve_rule, ray_answers)
 
 
-def lockstep(ref, port, frames, each=None):
+def trees_equal(ref, port):
+    for t in range(3):
+        assert np.array_equal(ref.tree_order(t), port.tree_order(t)), t
+        assert np.array_equal(ref.tree_stats(t), port.tree_stats(t)), (t, ref.tree_stats(t), port.tree_stats(t))
+
+
+def lockstep(ref, port, frames, each=None, plan=False):
     prev = set()
     for f in range(1, frames + 1):
         ref.step(1.0 / 60.0, 4)
-        ints, _ = ref.contacts()
-        prev, created = new_contacts(prev, ints)
-        if created:
-            port.set_contact_plan(np.array(created, np.int32))
+        if plan:
+            ints, _ = ref.contacts()
+            prev, created = new_contacts(prev, ints)
+            if created:
+                port.set_contact_plan(np.array(created, np.int32))
         port.step(1.0 / 60.0, 4)
         rb, pb = ref.bodies()[:, :9], port.bodies()[:, :9]
         bad = np.argwhere(rb.view(np.uint32) != pb.view(np.uint32))
@@ -44,10 +54,11 @@ SCENES = [
     ("joint_gallery", dict(enableSleep=0), "joint_gallery", dict(copies=6), 400),
     ("joint_zoo", dict(enableSleep=0), "joint_zoo", dict(copies=4), 400),
     ("joint_rigs", dict(enableSleep=0), "joint_rigs", dict(copies=4), 400),
-    # chain shapes: one-sided segments with ghost vertices (continuous off:
-    # with it on, a fast body meeting several segments at once visits them in
-    # the reference's static-tree order, the restatement in shape-id order)
+    # chain shapes: one-sided segments with ghost vertices, continuous
+    # collision on and off (a fast body meeting several segments at once
+    # visits them in the static tree's order)
     ("chain_terrain", dict(enableSleep=0, enableContinuous=0), "chain_terrain", dict(), 300),
+    ("chain_terrain_ccd", dict(enableSleep=0, enableContinuous=1), "chain_terrain", dict(), 300),
 ]
 
 
@@ -62,8 +73,27 @@ def test_port_lockstep_with_reference(ref_lib, port_lib, name, wkw, scene, kw, f
         if f % 25 == 0 or f == frames:
             assert compare_contacts(ref, port) == []
             assert np.array_equal(ref.color_counts(), port.color_counts())
+            trees_equal(ref, port)
 
     lockstep(ref, port, frames, each)
+    ref.close()
+    port.close()
+
+
+def test_port_parity_mode_with_reference(ref_lib, port_lib):
+    """Parity mode: the reference's new contact ids handed to the port before
+    each step give the same world as the port's own order."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    scenes.build(ref, "pile", count=300, seed=5, width=20.0, height=40.0)
+    scenes.build(port, "pile", count=300, seed=5, width=20.0, height=40.0)
+
+    def each(f):
+        if f % 30 == 0:
+            assert compare_contacts(ref, port) == []
+
+    lockstep(ref, port, 120, each, plan=True)
     ref.close()
     port.close()
 
@@ -76,19 +106,15 @@ SLEEP_SCENES = [
     ("joint_zoo_sleep", dict(enableSleep=1), "joint_zoo", dict(copies=3), 400),
     ("joint_rigs_sleep", dict(enableSleep=1), "joint_rigs", dict(copies=3), 400),
     ("chain_terrain_sleep", dict(enableSleep=1, enableContinuous=0), "chain_terrain", dict(count=200), 500),
+    ("chain_terrain_ccd_sleep", dict(enableSleep=1, enableContinuous=1), "chain_terrain", dict(count=200), 500),
 ]
 
 
 def lockstep_full(ref, port, frames, start=1):
     """Lock step comparing every body row: transform, velocity, centre,
     solver set (awake, sleeping set id) and sleep time."""
-    prev = set(tuple(r) for r in ref.contacts()[0][:, :3].tolist()) if start > 1 else set()
     for f in range(start, start + frames):
         ref.step(1.0 / 60.0, 4)
-        ints, _ = ref.contacts()
-        prev, created = new_contacts(prev, ints)
-        if created:
-            port.set_contact_plan(np.array(created, np.int32))
         port.step(1.0 / 60.0, 4)
         rb, pb = ref.bodies(), port.bodies()
         bad = np.argwhere(rb.view(np.uint32) != pb.view(np.uint32))
@@ -98,7 +124,7 @@ def lockstep_full(ref, port, frames, start=1):
         if f % 25 == 0:
             assert compare_contacts(ref, port) == [], f
             assert np.array_equal(ref.color_counts(), port.color_counts()), f
-    return prev
+            trees_equal(ref, port)
 
 
 @pytest.mark.parametrize("name,wkw,scene,kw,frames", SLEEP_SCENES, ids=[s[0] for s in SLEEP_SCENES])
