@@ -37,18 +37,31 @@ METRIC = "body-steps/s on 1 GB300: plain vs batched/learned-warm-start at equal 
 HBM_FALLBACK = 6800.0
 
 WORKLOADS = {
-    "pile100k": dict(scene="pile", kw=dict(count=100_000, seed=1234),
+    "pile100k": dict(scene="pile", kw=dict(count=100_000, seed=1234), frames=600,
                      desc="100k mixed circles/capsules/polygons (40/30/30), spawn 400x800 above a static U container, "
                           "density 1, friction 0.6, restitution U[0,0.3], dt=1/60, 4 substeps, 600 frames"),
-    "pile25k": dict(scene="pile", kw=dict(count=25_000, seed=1234, width=200.0, height=400.0),
+    "pile25k": dict(scene="pile", kw=dict(count=25_000, seed=1234, width=200.0, height=400.0), frames=600,
                     desc="25k-body variant of pile100k (same mix and seed, 200x400 spawn region); the ncu "
                          "capture case of the solver kernel"),
-    "pyramid": dict(scene="pyramid", kw=dict(),
+    "pyramid": dict(scene="pyramid", kw=dict(), frames=256,
                     desc="40-row pyramid of 820 unit boxes on a 100x2 static box, dt=1/60, 4 substeps, 256 frames"),
-    "pyramids_chains": dict(scene="pyramids_chains", kw=dict(),
+    "pyramids_chains": dict(scene="pyramids_chains", kw=dict(), frames=512,
                             desc="64 pyramids (52,480 boxes) + 200 revolute chains of 50 capsules (10k joints), "
                                  "dt=1/60, 4 substeps, 512 frames"),
 }
+
+
+def timed_frames(total, warmup, steps):
+    """The K timed frames, spread evenly over frames warmup..total-1 of the
+    scene (every frame when K covers them), so that a short run samples the
+    sparse early frames and the dense late ones alike. Frames are numbered
+    from 0; the other frames are stepped untimed."""
+    span = total - warmup
+    if steps >= span:
+        return list(range(warmup, warmup + steps))
+    if steps == 1:
+        return [warmup + span // 2]
+    return sorted(set(warmup + round(k * (span - 1) / (steps - 1)) for k in range(steps)))
 
 
 def measured_peaks():
@@ -183,6 +196,7 @@ def run_gpu(args, rank, world):
     g = GpuWorld(wd)
     scenes.build(g, spec["scene"], **spec["kw"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    frames = timed_frames(spec["frames"], args.warmup, args.steps)
     for _ in range(args.warmup):
         st = g.step(1.0 / 60.0, 4)
     st = g.sync()
@@ -200,11 +214,21 @@ def run_gpu(args, rank, world):
     launches = 0
     t0 = time.perf_counter()
     torch.cuda.nvtx.range_push("timed_steps")
-    for _ in range(args.steps):
+    frame = args.warmup
+    untimed_s = 0.0
+    for target in frames:
+        if frame < target:
+            u0 = time.perf_counter()
+            while frame < target:   # untimed frames between two timed ones
+                status |= g.step(1.0 / 60.0, 4)
+                frame += 1
+            status |= g.sync()
+            untimed_s += time.perf_counter() - u0
         flush.fill_(1.0)
         torch.cuda.synchronize()
         status |= g.step(1.0 / 60.0, 4)
         status |= g.sync()
+        frame += 1
         total_ms += g.last_step_ms()
         launches += g.last_step_launches()
     torch.cuda.synchronize()
@@ -231,16 +255,23 @@ def run_gpu(args, rank, world):
     n = g2.lib.f2d_world_body_capacity(g2.id)
     host = torch.empty((max(n, 1), 12), dtype=torch.float32, pin_memory=True)
     ptr = C.cast(host.data_ptr(), C.POINTER(C.c_float))
-    e2e_steps = args.steps
+    e2e_steps = len(frames)
     rows = 0
     if world is not None:
         world.barrier()
     torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for _ in range(e2e_steps):
+    e2e_s = 0.0
+    frame = args.warmup
+    for target in frames:
+        while frame < target:
+            status |= g2.lib.f2d_world_step(g2.id, 1.0 / 60.0, 4)
+            frame += 1
+        status |= g2.sync()
+        t1 = time.perf_counter()
         status |= g2.lib.f2d_world_step(g2.id, 1.0 / 60.0, 4)
         rows = g2.lib.f2d_world_get_bodies(g2.id, ptr, n)
-    e2e_s = time.perf_counter() - t1
+        e2e_s += time.perf_counter() - t1
+        frame += 1
     status |= g2.sync()
     e2e_s = reduce_seconds_over_ranks(e2e_s, world)
     g2.close()
@@ -272,23 +303,25 @@ def run_gpu(args, rank, world):
 
     # ---- reduce over ranks -------------------------------------------
     ms_total, nranks = reduce_over_ranks(total_ms, world, "cuda")
-    value = job_throughput(nranks, bodies, args.steps, ms_total)
+    value = job_throughput(nranks, bodies, len(frames), ms_total)
     e2e_value = nranks * bodies * e2e_steps / e2e_s
     result = {
         "metric": METRIC,
         "value": value,
         "unit": "body-steps/s",
         "n_gpus": nranks,
-        "steps": args.steps,
+        "steps": len(frames),
         "warmup": args.warmup,
-        "ms_per_step": ms_total / args.steps,
+        "ms_per_step": ms_total / len(frames),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded scene generator, forge2d_gb300/scenes.py)",
         "config": {"workload": args.workload, "description": spec["desc"], "bodies_per_gpu": bodies,
-                   "frames": "timed frames %d..%d of the scene" % (args.warmup, args.warmup + args.steps - 1),
+                   "frames": "%d timed frames spread over frames %d..%d of the scene's %d (first %d, last %d), "
+                             "the others stepped untimed" % (len(frames), args.warmup, spec["frames"] - 1,
+                                                             spec["frames"], frames[0], frames[-1]),
                    "sleep": False, "continuous": True, "substeps": 4,
                    "l2": "flushed before every timed step (512 MB write, untimed)",
                    "parallelism": "replicas" if nranks > 1 else "single world",
@@ -298,7 +331,7 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": int(rows * 12 * 4),
                 "what": "f2d_world_step + f2d_world_get_bodies (every body row: transform, velocities, "
                         "to a pinned host buffer) on a second copy of the scene over the same frames, host clock",
-                "steps": e2e_steps},
+                "steps": len(frames)},
         "roofline": {"kernel": "k_solve (persistent cooperative solver)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
@@ -549,7 +582,9 @@ def run_learned(args, torch):
 
 
 def cpu_baseline(args, bodies_hint=None, budget_s=None):
-    """Bounded sample of the CPU restatement on this host's cores."""
+    """The CPU restatement on this host's cores, timed on the same frames as
+    the GPU arm (the frames between them stepped untimed), stopping early
+    if the whole run passes the wall-clock budget."""
     from forge2d_gb300 import scenes
     from oracle.oracle import PortWorld
 
@@ -557,20 +592,29 @@ def cpu_baseline(args, bodies_hint=None, budget_s=None):
     wd = scenes.world_def(enableSleep=0, enableContinuous=1)
     p = PortWorld(wd)
     scenes.build(p, spec["scene"], **spec["kw"])
+    frames = timed_frames(spec["frames"], args.warmup, args.steps)
+    budget = args.cpu_budget if budget_s is None else budget_s
+    t_start = time.perf_counter()
     for _ in range(args.warmup):
         p.step(1.0 / 60.0, 4)
-    budget = args.cpu_budget if budget_s is None else budget_s
-    frames, spent = 0, 0.0
-    while spent < budget and frames < args.steps:
+    frame, spent, done = args.warmup, 0.0, []
+    for target in frames:
+        while frame < target:
+            p.step(1.0 / 60.0, 4)
+            frame += 1
+        if time.perf_counter() - t_start > budget:
+            break
         spent += p.step_timed(1.0 / 60.0, 4, 1)
-        frames += 1
+        frame += 1
+        done.append(target)
     bodies = p.awake_body_count()
     threads = int(os.environ.get("OMP_NUM_THREADS", "0")) or (os.cpu_count() or 1)
-    value = bodies * frames / spent
+    value = bodies * len(done) / spent
     p.close()
     return {"value": value, "unit": "body-steps/s", "cores": port_threads(threads), "kind": "port",
-            "sample": "frames %d..%d of the %s scene (%d frames, %.1f s of CPU step time)" % (
-                args.warmup, args.warmup + frames - 1, args.workload, frames, spent)}
+            "sample": "%d timed frames (first %d, last %d) of the %s scene's %d, the frames between them "
+                      "stepped untimed; %.1f s of timed CPU step time" % (
+                          len(done), done[0], done[-1], args.workload, spec["frames"], spent)}
 
 
 def port_threads(default):
@@ -591,7 +635,8 @@ def run_reference(args, rank):
     if rank != 0:
         return None
     base = cpu_baseline(args, budget_s=args.cpu_budget)
-    line = {"metric": METRIC, "value": base["value"], "unit": "body-steps/s", "n_gpus": 0, "steps": args.steps,
+    line = {"metric": METRIC, "value": base["value"], "unit": "body-steps/s", "n_gpus": 0,
+            "steps": len(timed_frames(WORKLOADS[args.workload]["frames"], args.warmup, args.steps)),
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded scene generator, forge2d_gb300/scenes.py)",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"]},
@@ -608,7 +653,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="pile100k", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="wall-clock seconds after which the CPU arm stops taking timed frames")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the batched form (4096 sub-worlds) beside the headline workload")

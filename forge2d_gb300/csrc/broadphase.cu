@@ -1,22 +1,25 @@
-// Broadphase of the world step: the set of new contact pairs.
+// Broadphase of the world step: the new contact pairs, in the reference's
+// creation order.
 //
 // Box2D v3.1.1 keeps three incremental dynamic trees and queries them with
-// every proxy whose fat AABB grew last step (broad_phase.c:160-474,
-// dynamic_tree.c:1114). The pair set that produces is: every pair of shapes
-// with overlapping fat AABBs, at least one of them a dynamic proxy and at
-// least one of them moved, that passes the filters and has no contact yet.
-// This file computes the same set GPU-first:
-//   1. an implicit 32-ary bounding-volume tree over all proxies' fat AABBs,
-//      rebuilt each step: leaves in the order of their 30-bit Morton codes
-//      (one-launch radix sort), node k of level l bounding children
-//      32k..32k+31 of level l-1, so no topology is stored and a refit is one
-//      launch whose longest dependency chain is the tree height (4 levels
-//      at 1e6 proxies);
-//   2. one thread per moved proxy walks it depth first (leaves in Morton
-//      order, so neighbouring threads walk neighbouring subtrees; the 32
-//      children of a node are contiguous);
-//   3. new pairs are sorted by their 64-bit shape-pair key, the order in
-//      which contact ids are then drawn from the LIFO id pool.
+// every moved proxy (broad_phase.c:160-474, dynamic_tree.c:1114). The pair
+// SET that produces is: every pair of shapes with overlapping fat AABBs, at
+// least one of them a dynamic proxy and at least one of them moved, that
+// passes the filters and has no contact yet. This file finds that set
+// GPU-first:
+//   1. an implicit 32-ary bounding-volume tree over all proxies' fat AABBs:
+//      leaves in the order of their 30-bit Morton codes (one-launch radix
+//      sort), node k of level l bounding children 32k..32k+31 of level l-1,
+//      so no topology is stored and a refit is one launch whose longest
+//      dependency chain is the tree height (4 levels at 1e6 proxies);
+//   2. one warp per moved proxy walks it depth first, the 32 children of a
+//      node tested by the 32 lanes at once;
+//   3. each pair is kept by the proxy whose query creates it in the
+//      reference, with the key (that proxy's move-array position, tree of
+//      the other proxy, that proxy's rank in the reference's tree), which
+//      the reference's trees kept in proxytree.cu provide; sorting the keys
+//      gives the reference's creation order, in which contact ids are then
+//      drawn from the LIFO id pool.
 #include "dscan.cuh"
 #include "dsort.cuh"
 #include "dtree.cuh"
@@ -343,20 +346,28 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 	return false;
 }
 
-// One thread per moved proxy. A pair found by both of its moved proxies is
-// reported by the one with the smaller shape id.
 // Candidate pair (si moved, sj its overlapping leaf): the filters of
-// b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup.
+// b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup. A
+// pair whose proxies both moved belongs to one query in the reference: the
+// smaller proxy key's when both are dynamic, else the dynamic proxy's (a
+// static or kinematic proxy queries the dynamic tree only and skips moved
+// proxies there).
 __device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int typeI, int bi, int sj )
 {
 	if ( sj == si || ( w.subCount > 0 && w.shapeSub[si] != w.shapeSub[sj] ) )
 		return;
 	int fj = w.sflags[sj];
-	int typeJ = w.proxyKey[sj] & 3;
-	bool movedJ = ( fj & SF_MOVED ) != 0;
-	if ( movedJ && sj < si )
-		return; // reported by sj
+	int keyI = w.proxyKey[si], keyJ = w.proxyKey[sj];
+	int typeJ = keyJ & 3;
 	if ( typeI != 2 && typeJ != 2 )
+		return;
+	if ( fj & SF_MOVED )
+	{
+		if ( typeI == 2 && typeJ == 2 ? keyJ < keyI : typeI != 2 )
+			return; // created by sj's query
+	}
+	// dynamic_tree.c:1140: a leaf of category zero is never visited
+	if ( w.cat[sj] == 0ull )
 		return;
 	bool primaryUnused;
 	if ( !registered( shape_type( fi ), shape_type( fj ), &primaryUnused ) )
@@ -371,8 +382,12 @@ __device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int 
 	int slot = atomicAdd( &w.sc->newPairCount, 1 );
 	if ( slot < w.pairCap )
 	{
-		int lo = si < sj ? si : sj, hi = si < sj ? sj : si;
-		w.pairKeys[slot] = ( (unsigned long long)lo << w.pairKeyBits ) | (unsigned)hi;
+		// tree order of a query's pairs after the prepends: dynamic, static,
+		// kinematic, each left to right
+		int rb = w.pairKeyBits;
+		unsigned long long tord = typeJ == 2 ? 0ull : ( typeJ == 0 ? 1ull : 2ull );
+		unsigned long long rank = (unsigned)w.pt[typeJ].rank[keyJ >> 2];
+		w.pairKeys[slot] = ( (unsigned long long)w.shapeMove[si] << ( rb + 2 ) ) | ( tord << rb ) | rank;
 	}
 	else
 		atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
@@ -382,7 +397,7 @@ __device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int 
 // lanes at once (one coalesced load), overlapping inner children are pushed
 // on a per-warp stack in shared memory, overlapping leaves are tested by
 // their lanes in parallel. The visiting order does not matter: new pairs are
-// sorted by key afterwards.
+// sorted by their keys afterwards.
 #define FIND_WARPS ( BP_THREADS / 32 )
 #define FIND_STACK ( WIDE * WIDE_MAX_LEVELS )
 
@@ -458,8 +473,26 @@ __global__ void k_clamp_pairs( DWorld w )
 }
 
 // ---------------------------------------------------------------------------
-// contact creation (contact.c:186-330) in pair-key order
+// contact creation (contact.c:186-330) in the reference's order: row r of the
+// sorted keys, decoded into (creating proxy's shape, other shape)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int plan_lookup( const DWorld& w, unsigned long long key )
+{
+	int lo = 0, hi = w.sc->planCount - 1;
+	while ( lo <= hi )
+	{
+		int mid = ( lo + hi ) >> 1;
+		unsigned long long k = w.planKeys[mid];
+		if ( k == key )
+			return w.planIds[mid];
+		if ( k < key )
+			lo = mid + 1;
+		else
+			hi = mid - 1;
+	}
+	return -1;
+}
+
 __global__ void k_create_contacts( DWorld w, int planMode )
 {
 	int n = w.sc->newPairCount;
@@ -467,9 +500,7 @@ __global__ void k_create_contacts( DWorld w, int planMode )
 	int base = w.sc->contactIdCount;
 	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
 	{
-		unsigned long long sortKey = w.pairKeys[r];
-		int s1 = (int)( sortKey >> w.pairKeyBits );
-		int s2 = (int)( sortKey & ( ( 1ull << w.pairKeyBits ) - 1ull ) );
+		int s1 = w.pairVal[r], s2 = w.pairValAlt[r];
 		unsigned long long key = pair_key( s1, s2 );
 		// A is the shape with the smaller proxy key (broad_phase.c:258-267)
 		int a = s1, b = s2;
@@ -483,7 +514,9 @@ __global__ void k_create_contacts( DWorld w, int planMode )
 		int id;
 		if ( planMode )
 		{
-			id = r < w.sc->planCount && w.planKeys[r] == key ? w.planIds[r] : -1;
+			// parity mode: the plan names each pair's contact id
+			id = plan_lookup( w, key );
+			w.newPairId[r] = id;
 			if ( id < 0 )
 			{
 				atomicOr( &w.sc->error, ERR_PLAN_MISMATCH );
@@ -542,8 +575,8 @@ __global__ void k_after_create( DWorld w, int planMode )
 			// plan ids are explicit; raise the high-water mark and drop used
 			// ids from the free stack (order of the remaining ids is kept)
 			int hi = w.sc->contactIdCount;
-			for ( int r = 0; r < n && r < w.sc->planCount; ++r )
-				hi = max( hi, w.planIds[r] + 1 );
+			for ( int r = 0; r < n && r < w.pairCap; ++r )
+				hi = max( hi, w.newPairId[r] + 1 );
 			int F = w.sc->contactFreeCount;
 			int keep = 0;
 			for ( int k = 0; k < F; ++k )
@@ -573,6 +606,7 @@ __global__ void k_after_create( DWorld w, int planMode )
 		}
 		w.sc->newPairCount = 0;
 		w.sc->planCount = 0;
+		w.sc->moveArrayCount = 0; // broad_phase.c:456-458: the move buffer is reset
 	}
 	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
 		w.sflags[s] &= ~SF_MOVED;
@@ -585,6 +619,7 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 						void* hookContext )
 {
 	int gridS = grid_for( w.shapeCount );
+	launch_pt_host_moves( w, s, st );
 	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, st>>>( w );
 	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, st>>>( w );
 	k_leaf_flags<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA );
@@ -599,10 +634,11 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_wide_refit<<<( ( w.shapeCap + WIDE - 1 ) / WIDE + 7 ) / 8, BP_THREADS, 0, st>>>( w );
 	k_find_pairs<<<( w.shapeCap + FIND_WARPS - 1 ) / FIND_WARPS, BP_THREADS, 0, st>>>( w );
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );
-	int bits = 2 * w.pairKeyBits;
-	// new pair keys are unique, so the key order alone fixes the result
+	// keys are unique (one per pair), so the key order alone fixes the result
+	int bits = 2 * w.pairKeyBits + 2;
 	sort_coop<unsigned long long>( w.pairKeys, nullptr, w.pairKeysAlt, nullptr, &w.sc->newPairCount, bits, w.sortHist,
 								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
+	launch_pt_decode( w, st );
 	// broad_phase.c:267-278: the custom filter sees the new pairs last
 	if ( pairHook )
 		pairHook( hookContext );
@@ -610,4 +646,7 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	if ( w.isl )
 		launch_isl_new_contacts( w, st, planMode );
 	k_after_create<<<gridS, BP_THREADS, 0, st>>>( w, planMode );
+	// world.c:488-502: the dynamic and kinematic trees are rebuilt over their
+	// enlarged nodes every step
+	launch_pt_rebuild( w, s, st );
 }

@@ -126,6 +126,70 @@ struct DScalars
 	int sensorCur, sensorPrev;	   // sensor overlaps this step / last step
 	int sensorBegin, sensorEnd;	   // sensor events of this step
 	int cbList, cbReject;		   // user callbacks: listed candidates, rejected keys
+	// the reference's broadphase trees (static, kinematic, dynamic) and the
+	// move array: root node, proxies; proxies in the move array, proxies the
+	// host buffered since the last step
+	int treeRoot[3];
+	int treeProxies[3];
+	int moveArrayCount;
+	int hostMoveCount;
+	// partial rebuild of one tree: active, gathered nodes, large segments
+	// per level (two levels in flight), small segments
+	int rbActive, rbCount, rbLarge[2], rbSmall;
+};
+
+// node flags of the broadphase trees (dynamic_tree.c b2TreeNodeFlags)
+#define PT_ALLOCATED 1
+#define PT_ENLARGED 2
+#define PT_LEAF 4
+
+// ---------------------------------------------------------------------------
+// The reference's broadphase trees (dynamic_tree.c), one per body type, kept
+// node for node: ids, topology, boxes, heights, categories and flags (bits
+// PT_ALLOCATED, PT_ENLARGED, PT_LEAF of htree.h). The host inserts and
+// removes proxies (htree.cpp); the device enlarges proxies and rebuilds the
+// enlarged part every step (proxytree.cu). `leaves` counts the leaves of a
+// subtree; `rank` is a leaf's left-to-right position and `rankShape` its
+// inverse, from which the order of new contacts is made.
+// ---------------------------------------------------------------------------
+struct DProxyTree
+{
+	int cap;
+	int* child1;
+	int* child2;
+	int* parent;
+	int* height;
+	int* flags;
+	int* shape;
+	int* leaves;
+	float4* box; // lower.x lower.y upper.x upper.y
+	unsigned long long* cat;
+	int* rank;
+	int* rankShape;
+};
+
+// Scratch of the partial rebuild (sized by the largest tree capacity).
+// Segments are (start, end, child1 edges above, -) ranges of the gathered
+// nodes; a chunk is PT_CHUNK consecutive gathered nodes of one segment.
+struct DRebuild
+{
+	int cap, segCap, chunkCap;
+	int* doomed;   // internal node being rebuilt
+	int* cnt;	   // arrival counters of the bottom-up passes
+	int* rlc;	   // gathered nodes below a doomed node
+	int* gIdx;	   // gathered nodes, left to right, then partitioned
+	float2* gCen;  // their box centres
+	int* freed;	   // doomed nodes in pre-order (the reference's free order)
+	int* bl;	   // per segment: positions of left-side nodes that belong right
+	int* br;	   // and of right-side nodes that belong left, from the end
+	int4* segA;
+	int4* segB;
+	int4* segSmall;
+	int* chunkBase; // per large segment: first chunk (and the total at [count])
+	int* chunkStat; // per chunk: below pivot, bad left, bad right, left offset, right offset
+	int* segBounds; // per large segment: centre bounds as ordered ints
+	int* segBelow;	// per large segment: centres below the pivot
+	int* pairBase;	// per large segment: first swap pair
 };
 
 // ---------------------------------------------------------------------------
@@ -323,8 +387,9 @@ struct DWorld
 	unsigned long long* pairKeysAlt;
 	int* pairVal;
 	int* pairValAlt;
-	int* planIds; // parity plan: contact id for the k-th new pair in key order
+	int* planIds; // parity plan: contact ids by ascending pair key
 	unsigned long long* planKeys;
+	int* newPairId; // parity mode: the contact id given to each new pair (creation order)
 
 	// ---------------- state-change ops ----------------
 	int* opContact; // contact id
@@ -407,6 +472,13 @@ struct DWorld
 	float* cbManifold; // 22 per listed pre-solve contact: f2d_manifold_view, shape A, shape B
 	unsigned long long* cbReject;
 	int staticCount;
+
+	// the reference's broadphase trees and the move array (proxytree.cu)
+	DProxyTree pt[3];
+	DRebuild rb;
+	int* shapeMove; // per shape: position in the move array
+	int* moveShape; // move array: shape ids
+	int* hostMoves; // shapes the host buffered since the last step, in call order
 
 	DScalars* sc;
 	int* sortTemp;

@@ -295,7 +295,8 @@ __global__ void k_continuous( DWorld w, int listOnly )
 				int sfs = w.sflags[ss];
 				if ( ( sfs & SF_USED ) == 0 )
 					return;
-				if ( !box_overlaps( box_from4( w.fat[ss] ), box ) )
+				// the static tree's query skips categories of zero
+				if ( w.cat[ss] == 0ull || !box_overlaps( box_from4( w.fat[ss] ), box ) )
 					return;
 				int sb = w.shapeBody[ss];
 				if ( ss == fs || sb == b || ( sfs & SF_SENSOR ) ||
@@ -378,8 +379,10 @@ __global__ void k_continuous( DWorld w, int listOnly )
 						fraction = f;
 				}
 			};
-			// candidates in shape-id order: the static list when it is short,
-			// else the tree's static leaves overlapping the sweep box
+			// candidates in the static tree's depth-first order (descending
+			// left-to-right rank), as the reference's query meets them: the
+			// static list (kept in that order) when it is short, else the
+			// static leaves of the pair tree overlapping the sweep box
 			bool scanList = w.staticCount <= CCD_LIST_MAX;
 			int cand[CCD_CANDIDATES];
 			int nc = 0;
@@ -396,7 +399,8 @@ __global__ void k_continuous( DWorld w, int listOnly )
 						return;
 					}
 					int k = nc++;
-					while ( k > 0 && cand[k - 1] > ss )
+					int rs = w.pt[0].rank[w.proxyKey[ss] >> 2];
+					while ( k > 0 && w.pt[0].rank[w.proxyKey[cand[k - 1]] >> 2] < rs )
 					{
 						cand[k] = cand[k - 1];
 						k -= 1;
@@ -458,19 +462,6 @@ __global__ void k_continuous( DWorld w, int listOnly )
 			}
 		}
 	}
-}
-
-// enlarged shapes enter the move buffer of the next step
-__global__ void k_moved_flags( DWorld w )
-{
-	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
-	{
-		int f = w.sflags[s];
-		if ( f & SF_ENLARGED )
-			w.sflags[s] = ( f & ~SF_ENLARGED ) | SF_MOVED;
-	}
-	if ( blockIdx.x == 0 && threadIdx.x == 0 )
-		w.sc->fastCount = 0;
 }
 
 // solver.c:1758-1818 hit events
@@ -547,7 +538,9 @@ void launch_finalize( DWorld& w, StepScratch& s, cudaStream_t st, float dt, Host
 	}
 	k_continuous<<<grid_for( w.bodyCount ), 64, 0, st>>>( w, 0 );
 	k_hit_events<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
-	k_moved_flags<<<grid_for( w.shapeCount ), 256, 0, st>>>( w );
+	// solver.c:1842-1905: enlarged proxies enter the move array of the next
+	// step in awake order and grow their tree leaves
+	launch_pt_moves( w, s, st );
 	if ( w.isl )
 		launch_isl_sleep( w, st, s.scanState );
 }

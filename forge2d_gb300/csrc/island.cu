@@ -930,7 +930,7 @@ __global__ void k_isl_new_contacts( DWorld w, DIslands* Ip, int planMode )
 	{
 		int id;
 		if ( planMode )
-			id = r < w.sc->planCount ? w.planIds[r] : -1;
+			id = w.newPairId[r];
 		else
 			id = r < F ? w.contactFree[F - 1 - r] : base + ( r - F );
 		if ( id < 0 || id >= w.contactCap || ( w.cflags[id] & CF_USED ) == 0 )

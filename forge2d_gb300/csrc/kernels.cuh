@@ -36,6 +36,7 @@ struct StepScratch
 	int clusterCapacity; // bodies the cluster solver takes (0: cooperative solver only)
 	int solverBlocks256; // grid of the 256-thread variant of the grid-wide solver
 	int solverVariant;	 // SOLVER_* (the autotuner's choice; results never depend on it)
+	int ptBlocks;		 // co-resident grid of the tree rebuild's cooperative levels
 	cudaEvent_t evSolveStart; // recorded right before the cooperative solver launch when non-null
 };
 
@@ -73,3 +74,10 @@ void launch_isl_fix_flags( DWorld& w, cudaStream_t st, int n );
 void launch_learned_warm_start( DWorld& w, cudaStream_t st );
 void launch_record_samples( DWorld& w, cudaStream_t st );
 int solver_cluster_capacity();
+// the reference's broadphase trees and the move array (proxytree.cu)
+int pt_large_blocks();
+void launch_pt_host_moves( DWorld& w, StepScratch& s, cudaStream_t st );
+void launch_pt_decode( DWorld& w, cudaStream_t st );
+void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st );
+void launch_pt_moves( DWorld& w, StepScratch& s, cudaStream_t st );
+void launch_pt_ranks( DWorld& w, cudaStream_t st, int t );

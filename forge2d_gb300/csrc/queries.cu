@@ -16,6 +16,7 @@
 #include "../../include/forge2d_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 struct RayHit
@@ -590,22 +591,26 @@ struct OverlapScratch
 
 static __device__ __align__( 256 ) OverlapScratch g_overlapScratch;
 
-// device address of g_overlapScratch per device ordinal, resolved on first use
-static OverlapScratch* s_overlapScratch[NOALLOC_MAX_DEVICES];
+// device address of g_overlapScratch per device ordinal, resolved on first
+// use; host threads may race to resolve it, so the cache entries are atomic
+// (every thread stores the same address)
+static std::atomic<OverlapScratch*> s_overlapScratch[NOALLOC_MAX_DEVICES];
 
 static OverlapScratch* overlap_scratch()
 {
 	int dev = 0;
 	if ( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES )
 		return nullptr;
-	if ( s_overlapScratch[dev] == nullptr )
+	OverlapScratch* cached = s_overlapScratch[dev].load( std::memory_order_acquire );
+	if ( cached == nullptr )
 	{
 		void* p = nullptr;
 		if ( cudaGetSymbolAddress( &p, g_overlapScratch ) != cudaSuccess )
 			return nullptr;
-		s_overlapScratch[dev] = (OverlapScratch*)p;
+		cached = (OverlapScratch*)p;
+		s_overlapScratch[dev].store( cached, std::memory_order_release );
 	}
-	return s_overlapScratch[dev];
+	return cached;
 }
 
 __device__ __forceinline__ bool overlap_hit( const DWorld& w, int s, fbox box, unsigned long long cat,

@@ -13,6 +13,7 @@
 #include "dsort.cuh"
 #include "dworld.cuh"
 #include "hgeom.h"
+#include "htree.h"
 #include "joint.cuh"
 #include "kernels.cuh"
 
@@ -28,13 +29,6 @@ void launch_reset_counters( DWorld& w, cudaStream_t st );
 
 
 #define MAX_WORLDS 128
-
-struct TreeIds
-{
-	std::vector<int> freeStack;
-	int nodeCount = 0;
-	int proxyCount = 0;
-};
 
 struct HostWorld
 {
@@ -84,8 +78,20 @@ struct HostWorld
 	std::vector<int> shapeFree;
 	int shapeCount = 0, shapeUploaded = 0;
 	std::vector<int> shapeDirty;
-	TreeIds trees[3];
-	std::vector<int> staticShapes;
+	// the reference's broadphase trees (static, kinematic, dynamic): the
+	// host inserts and removes; the device enlarges and rebuilds the
+	// kinematic and dynamic trees every step, so those are read back before
+	// a host edit (treeStale) and sent after it (treeDirty)
+	HTree trees[3];
+	bool treeDirty[3] = { true, true, true };
+	bool treeStale[3] = { false, false, false };
+	// proxies buffered for the next step's pair search since the last step
+	// (creation, transforms), in call order, each once
+	std::vector<int> hostMoves;
+	std::vector<uint8_t> hostMoved;
+	std::vector<int> staticShapes; // static shapes in the static tree's query order
+	int treeScalars[6] = {};	   // staging of the trees' roots and proxy counts
+	int hostMoveCount = 0;		   // staging of the buffered proxy count
 	std::vector<int> sensorShapes; // sensor shapes in creation order (sensor.c)
 	float invH = 0.0f; // inverse substep of the last step (world.c:745-755)
 	f2d_custom_filter_fn customFilter = nullptr;
@@ -103,6 +109,7 @@ struct HostWorld
 	std::vector<int> jflags, jcolor, jnext;
 	std::vector<float4> jdef0, jdef1, jdef2, jdef3;
 	std::vector<int> jointDirty; // uploaded joints whose definition rows changed on the host
+	std::vector<uint8_t> jointIsDirty;
 	std::vector<uint16_t> jgen;
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
@@ -210,6 +217,7 @@ static void alloc_scratch( HostWorld* W )
 	s.solverBlocks = solver_max_blocks( 512 );
 	s.solverBlocks256 = solver_max_blocks( 256 );
 	s.clusterCapacity = W->gridSolverOnly ? 0 : solver_cluster_capacity();
+	s.ptBlocks = pt_large_blocks();
 }
 
 static void grow_bodies( HostWorld* W, int cap )
@@ -305,6 +313,9 @@ static void grow_shapes( HostWorld* W, int cap )
 	dgrow( d.proxyKey, o, cap );
 	dgrow( d.nextShape, o, cap );
 	dgrow( d.staticShapes, 0, cap );
+	dgrow( d.shapeMove, o, cap );
+	dgrow( d.moveShape, 0, cap );
+	dgrow( d.hostMoves, 0, cap );
 	// broadphase scratch
 	dgrow( d.mortonKeys, 0, cap );
 	dgrow( d.mortonKeysAlt, 0, cap );
@@ -323,6 +334,7 @@ static void grow_shapes( HostWorld* W, int cap )
 	dgrow( d.pairValAlt, 0, pc );
 	dgrow( d.planKeys, 0, pc );
 	dgrow( d.planIds, 0, pc );
+	dgrow( d.newPairId, 0, pc );
 	d.pairCap = pc;
 	if ( d.contactCap < 8 * cap )
 		grow_contacts( W, 8 * cap );
@@ -676,6 +688,172 @@ static void mark_shape( HostWorld* W, int s )
 		W->shapeDirty.push_back( s );
 }
 
+// ---------------------------------------------------------------------------
+// the broadphase trees between the host copy and the device
+// ---------------------------------------------------------------------------
+static void pt_free( DProxyTree& T )
+{
+	dfree( T.child1 );
+	dfree( T.child2 );
+	dfree( T.parent );
+	dfree( T.height );
+	dfree( T.flags );
+	dfree( T.shape );
+	dfree( T.leaves );
+	dfree( T.box );
+	dfree( T.cat );
+	dfree( T.rank );
+	dfree( T.rankShape );
+	T.cap = 0;
+}
+
+static void rb_free( DRebuild& R )
+{
+	dfree( R.doomed );
+	dfree( R.cnt );
+	dfree( R.rlc );
+	dfree( R.gIdx );
+	dfree( R.gCen );
+	dfree( R.freed );
+	dfree( R.bl );
+	dfree( R.br );
+	dfree( R.segA );
+	dfree( R.segB );
+	dfree( R.segSmall );
+	dfree( R.chunkBase );
+	dfree( R.chunkStat );
+	dfree( R.segBounds );
+	dfree( R.segBelow );
+	dfree( R.pairBase );
+	R.cap = 0;
+}
+
+// rebuild scratch for trees of up to `cap` nodes (segments of more than
+// 1024 nodes are at most cap / 1024; chunks of 1024 nodes at most
+// cap / 1024 plus one per segment)
+static void rb_ensure( HostWorld* W, int cap )
+{
+	DRebuild& R = W->d.rb;
+	if ( cap <= R.cap )
+		return;
+	rb_free( R );
+	size_t n = (size_t)cap;
+	dgrow( R.doomed, 0, n );
+	dgrow( R.cnt, 0, n );
+	dgrow( R.rlc, 0, n );
+	dgrow( R.gIdx, 0, n );
+	dgrow( R.gCen, 0, n );
+	dgrow( R.freed, 0, n );
+	dgrow( R.bl, 0, n );
+	dgrow( R.br, 0, n );
+	R.segCap = cap / 512 + 8;
+	R.chunkCap = cap / 512 + R.segCap + 8;
+	dgrow( R.segA, 0, (size_t)R.segCap );
+	dgrow( R.segB, 0, (size_t)R.segCap );
+	dgrow( R.segSmall, 0, n / 2 + 8 );
+	dgrow( R.chunkBase, 0, (size_t)R.segCap + 1 );
+	dgrow( R.chunkStat, 0, 5 * (size_t)R.chunkCap );
+	dgrow( R.segBounds, 0, 4 * (size_t)R.segCap );
+	dgrow( R.segBelow, 0, (size_t)R.segCap );
+	dgrow( R.pairBase, 0, (size_t)R.segCap + 1 );
+	R.cap = cap;
+	W->graphDirty = true;
+}
+
+// host copy -> device (after host inserts and removes), then the ranks
+static void tree_upload( HostWorld* W, int t )
+{
+	DWorld& d = W->d;
+	HTree& h = W->trees[t];
+	DProxyTree& T = d.pt[t];
+	if ( h.cap > T.cap )
+	{
+		pt_free( T );
+		size_t n = (size_t)h.cap;
+		dgrow( T.child1, 0, n );
+		dgrow( T.child2, 0, n );
+		dgrow( T.parent, 0, n );
+		dgrow( T.height, 0, n );
+		dgrow( T.flags, 0, n );
+		dgrow( T.shape, 0, n );
+		dgrow( T.leaves, 0, n );
+		dgrow( T.box, 0, n );
+		dgrow( T.cat, 0, n );
+		dgrow( T.rank, 0, n );
+		dgrow( T.rankShape, 0, n );
+		T.cap = h.cap;
+		W->graphDirty = true;
+	}
+	int n = h.cap;
+	up( T.child1, h.child1, 0, n, W->stream );
+	up( T.child2, h.child2, 0, n, W->stream );
+	up( T.parent, h.parent, 0, n, W->stream );
+	up( T.height, h.height, 0, n, W->stream );
+	up( T.flags, h.flags, 0, n, W->stream );
+	up( T.shape, h.shape, 0, n, W->stream );
+	up( T.leaves, h.leaves, 0, n, W->stream );
+	up( T.box, h.box, 0, n, W->stream );
+	up( T.cat, h.cat, 0, n, W->stream );
+	W->treeScalars[t] = h.root;
+	W->treeScalars[3 + t] = h.proxyCount;
+	cudaMemcpyAsync( &d.sc->treeRoot[t], &W->treeScalars[t], sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+	cudaMemcpyAsync( &d.sc->treeProxies[t], &W->treeScalars[3 + t], sizeof( int ), cudaMemcpyHostToDevice,
+					 W->stream );
+	launch_pt_ranks( d, W->stream, t );
+	rb_ensure( W, std::max( d.pt[1].cap, d.pt[2].cap ) );
+	cudaStreamSynchronize( W->stream );
+	W->treeDirty[t] = false;
+}
+
+// device -> host copy, before a host edit of a tree the steps have changed
+static void tree_pull( HostWorld* W, int t )
+{
+	if ( !W->treeStale[t] )
+		return;
+	HTree& h = W->trees[t];
+	const DProxyTree& T = W->d.pt[t];
+	cudaStreamSynchronize( W->stream );
+	int n = h.cap;
+	down( h.child1, T.child1, 0, n );
+	down( h.child2, T.child2, 0, n );
+	down( h.parent, T.parent, 0, n );
+	down( h.height, T.height, 0, n );
+	down( h.flags, T.flags, 0, n );
+	down( h.shape, T.shape, 0, n );
+	down( h.leaves, T.leaves, 0, n );
+	down( h.box, T.box, 0, n );
+	down( h.cat, T.cat, 0, n );
+	cudaMemcpy( &h.root, &W->d.sc->treeRoot[t], sizeof( int ), cudaMemcpyDeviceToHost );
+	W->treeStale[t] = false;
+}
+
+// b2BufferMove (broad_phase.c): a proxy joins the next step's move array once
+static void host_move( HostWorld* W, int s )
+{
+	if ( (int)W->hostMoved.size() <= s )
+		W->hostMoved.resize( (size_t)s + 1, 0 );
+	if ( W->hostMoved[s] )
+		return;
+	W->hostMoved[s] = 1;
+	W->hostMoves.push_back( s );
+}
+
+// the buffered proxies go to the device for the step about to be enqueued
+static void upload_host_moves( HostWorld* W )
+{
+	int n = (int)W->hostMoves.size();
+	if ( n == 0 )
+		return;
+	cudaMemcpyAsync( W->d.hostMoves, W->hostMoves.data(), sizeof( int ) * (size_t)n, cudaMemcpyHostToDevice,
+					 W->stream );
+	W->hostMoveCount = n;
+	cudaMemcpyAsync( &W->d.sc->hostMoveCount, &W->hostMoveCount, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+	cudaStreamSynchronize( W->stream );
+	for ( int sh : W->hostMoves )
+		W->hostMoved[sh] = 0;
+	W->hostMoves.clear();
+}
+
 static void flush_uploads( HostWorld* W )
 {
 	ensure_capacity( W );
@@ -716,6 +894,7 @@ static void flush_uploads( HostWorld* W )
 		up( d.jdef2, W->jdef2, j, j + 1, W->stream );
 		up( d.jdef3, W->jdef3, j, j + 1, W->stream );
 		up( d.jflags, W->jflags, j, j + 1, W->stream );
+		W->jointIsDirty[j] = 0;
 	}
 	W->jointDirty.clear();
 	if ( W->sensorsDirty )
@@ -745,6 +924,7 @@ static void flush_uploads( HostWorld* W )
 	}
 	if ( W->staticDirty )
 	{
+		W->trees[0].visit_order( W->staticShapes );
 		if ( !W->staticShapes.empty() )
 			cudaMemcpyAsync( W->d.staticShapes, W->staticShapes.data(), sizeof( int ) * W->staticShapes.size(),
 							 cudaMemcpyHostToDevice, W->stream );
@@ -779,6 +959,9 @@ static void flush_uploads( HostWorld* W )
 		W->pendingJoints.clear();
 		W->graphDirty = true;
 	}
+	for ( int t = 0; t < 3; ++t )
+		if ( W->treeDirty[t] )
+			tree_upload( W, t );
 	// counts are kernel parameters of the captured step: a change re-captures
 	if ( W->d.bodyCount != W->bodyCount || W->d.shapeCount != W->shapeCount || W->d.jointCount != W->jointCount )
 		W->graphDirty = true;
@@ -868,7 +1051,11 @@ static void free_world( HostWorld* W )
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
 	F( sensorBeginEv ); F( sensorEndEv ); F( cbList ); F( cbReject ); F( cbManifold ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
+	F( shapeMove ); F( moveShape ); F( hostMoves ); F( newPairId );
 #undef F
+	for ( int t = 0; t < 3; ++t )
+		pt_free( d.pt[t] );
+	rb_free( d.rb );
 	dfree( W->s.tmpA );
 	dfree( W->s.tmpB );
 	dfree( W->s.scanTmp );
@@ -1084,24 +1271,6 @@ static void update_mass( HostWorld* W, int b )
 	W->massv[b] = make_float4( invMass, invInertia, minExtent, maxExtent );
 }
 
-static int tree_create_proxy( TreeIds& t )
-{
-	auto alloc = [&]() {
-		if ( !t.freeStack.empty() )
-		{
-			int v = t.freeStack.back();
-			t.freeStack.pop_back();
-			return v;
-		}
-		return t.nodeCount++;
-	};
-	int leaf = alloc();
-	if ( t.proxyCount > 0 )
-		(void)alloc();
-	t.proxyCount += 1;
-	return leaf;
-}
-
 static void pack_geom( const HShapeGeom& g, float4* out )
 {
 	for ( int i = 0; i < GEOM_F4; ++i )
@@ -1190,17 +1359,19 @@ static int create_shape( HostWorld* W, int b, const f2d_shape_def* def, const HS
 		aabb = box_grow( h_shape_aabb( g, xf ), F2D_SPECULATIVE );
 		float margin = proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN;
 		fat = box_grow( aabb, margin );
-		int proxyId = tree_create_proxy( W->trees[proxyType] );
+		// shape.c:901-911 b2CreateShapeProxy -> broad_phase.c:91-103: the
+		// proxy id is the tree node id; non-static (or forced) proxies join
+		// the move buffer
+		tree_pull( W, proxyType );
+		int proxyId = W->trees[proxyType].create_proxy( box_to4( fat ), (unsigned long long)def->categoryBits, id );
+		W->treeDirty[proxyType] = true;
 		pkey = ( proxyId << 2 ) | proxyType;
 		flags |= SF_PROXY;
 		bool force = def->invokeContactCreation != 0 || def->isSensor != 0;
 		if ( proxyType != 0 || force )
-			flags |= SF_MOVED;
-		if ( proxyType == 0 && !def->isSensor )
-		{
-			W->staticShapes.push_back( id );
+			host_move( W, id );
+		if ( proxyType == 0 )
 			W->staticDirty = true;
-		}
 	}
 	vset( W->sflags, id, flags );
 	vset( W->proxyKey, id, pkey );
@@ -1620,6 +1791,20 @@ extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_de
 	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
 }
 
+// an uploaded joint whose definition rows changed on the host (sent with the
+// next step)
+static void mark_joint_dirty( HostWorld* W, int j )
+{
+	if ( j >= W->jointUploaded )
+		return;
+	if ( (int)W->jointIsDirty.size() <= j )
+		W->jointIsDirty.resize( (size_t)j + 1, 0 );
+	if ( W->jointIsDirty[j] )
+		return;
+	W->jointIsDirty[j] = 1;
+	W->jointDirty.push_back( j );
+}
+
 // Limit of a revolute, prismatic or wheel joint (revolute_joint.c:84-127,
 // prismatic_joint.c:68-109, wheel_joint.c:57-98): EnableLimit then SetLimits;
 // a change clears the limit impulses (jimp2); bounds stored as min, max.
@@ -1648,15 +1833,11 @@ extern "C" F2D_API void f2d_joint_set_limits( int32_t index1, int32_t wg, int32_
 		d2.y = fmax_s( lo, hi );
 		clear = true;
 	}
+	// stream-ordered clear: after any step in flight, before the next one,
+	// without blocking the caller
 	if ( clear && j < W->jointUploaded )
-	{
-		float2 zero = make_float2( 0.0f, 0.0f );
-		cudaMemcpyAsync( W->d.jimp2 + j, &zero, sizeof( zero ), cudaMemcpyHostToDevice, W->stream );
-		cudaStreamSynchronize( W->stream );
-	}
-	if ( j < W->jointUploaded &&
-		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
-		W->jointDirty.push_back( j );
+		cudaMemsetAsync( W->d.jimp2 + j, 0, sizeof( float2 ), W->stream );
+	mark_joint_dirty( W, j );
 }
 
 // b2Joint_GetConstraintForce / GetConstraintTorque (joint.c:1061-1135) with
@@ -1775,17 +1956,11 @@ extern "C" F2D_API void f2d_joint_set_motor( int32_t index1, int32_t wg, int32_t
 	if ( ( enable != 0 ) != on )
 	{
 		W->jflags[j] ^= JF_MOTOR;
+		// stream-ordered clear, as in f2d_joint_set_limits
 		if ( j < W->jointUploaded )
-		{
-			float zero = 0.0f;
-			cudaMemcpyAsync( (float*)( W->d.jimp + j ) + impulseLane, &zero, sizeof( float ), cudaMemcpyHostToDevice,
-							 W->stream );
-			cudaStreamSynchronize( W->stream );
-		}
+			cudaMemsetAsync( (float*)( W->d.jimp + j ) + impulseLane, 0, sizeof( float ), W->stream );
 	}
-	if ( j < W->jointUploaded &&
-		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
-		W->jointDirty.push_back( j );
+	mark_joint_dirty( W, j );
 }
 
 // b2MouseJoint_SetTarget (mouse_joint.c:14-19): no wake
@@ -1800,9 +1975,7 @@ extern "C" F2D_API void f2d_mouse_joint_set_target( int32_t index1, int32_t wg, 
 		return;
 	W->jdef1[j].x = (float)x;
 	W->jdef1[j].y = (float)y;
-	if ( j < W->jointUploaded &&
-		 std::find( W->jointDirty.begin(), W->jointDirty.end(), j ) == W->jointDirty.end() )
-		W->jointDirty.push_back( j );
+	mark_joint_dirty( W, j );
 }
 
 extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )
@@ -1864,23 +2037,31 @@ static void pair_filter_hook( void* context )
 	n = std::min( n, d.pairCap );
 	if ( n <= 0 )
 		return;
-	std::vector<unsigned long long> keys( (size_t)n );
-	cudaMemcpy( keys.data(), d.pairKeys, sizeof( unsigned long long ) * n, cudaMemcpyDeviceToHost );
-	const unsigned long long low = ( 1ull << d.pairKeyBits ) - 1ull;
+	// the sorted pairs, decoded: (creating proxy's shape, other shape)
+	std::vector<int> s1( (size_t)n ), s2( (size_t)n );
+	cudaMemcpy( s1.data(), d.pairVal, sizeof( int ) * n, cudaMemcpyDeviceToHost );
+	cudaMemcpy( s2.data(), d.pairValAlt, sizeof( int ) * n, cudaMemcpyDeviceToHost );
 	int kept = 0;
 	for ( int i = 0; i < n; ++i )
 	{
-		int a = (int)( keys[i] >> d.pairKeyBits ), b = (int)( keys[i] & low );
+		int a = s1[i], b = s2[i];
 		if ( W->proxyKey[b] < W->proxyKey[a] )
 			std::swap( a, b );
 		if ( W->customFilter( a + 1, pack_wg( W, W->sgen[a] ), b + 1, pack_wg( W, W->sgen[b] ),
 							  W->customFilterContext ) )
-			keys[kept++] = keys[i];
+		{
+			s1[kept] = s1[i];
+			s2[kept] = s2[i];
+			kept += 1;
+		}
 	}
 	if ( kept == n )
 		return;
 	if ( kept > 0 )
-		cudaMemcpy( d.pairKeys, keys.data(), sizeof( unsigned long long ) * kept, cudaMemcpyHostToDevice );
+	{
+		cudaMemcpy( d.pairVal, s1.data(), sizeof( int ) * kept, cudaMemcpyHostToDevice );
+		cudaMemcpy( d.pairValAlt, s2.data(), sizeof( int ) * kept, cudaMemcpyHostToDevice );
+	}
 	cudaMemcpy( &d.sc->newPairCount, &kept, sizeof( int ), cudaMemcpyHostToDevice );
 }
 
@@ -2016,6 +2197,7 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	if ( W->stepped && cudaEventQuery( W->evStop ) == cudaSuccess )
 		W->statusAccum |= *W->hostError;
 	flush_uploads( W );
+	upload_host_moves( W );
 	int planMode = 0;
 	if ( W->planPending )
 	{
@@ -2079,6 +2261,9 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	cudaEventRecord( W->evStop, W->stream );
 	cudaMemcpyAsync( W->hostError, &W->d.sc->error, sizeof( int ), cudaMemcpyDeviceToHost, W->stream );
 	W->stepped = true;
+	// the step enlarged and rebuilt the kinematic and dynamic trees
+	W->treeStale[1] = true;
+	W->treeStale[2] = true;
 	cudaError_t e = cudaGetLastError();
 	if ( e != cudaSuccess )
 		W->statusAccum |= F2D_STATUS_CUDA;
@@ -2442,7 +2627,17 @@ extern "C" F2D_API void f2d_body_set_transform( int32_t index1, int32_t wg, doub
 		float margin = proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN;
 		W->aabb[sh] = box_to4( aabb );
 		W->fat[sh] = box_to4( box_grow( aabb, margin ) );
-		W->sflags[sh] |= SF_MOVED;
+		// broad_phase.c:116-123 b2BroadPhase_MoveProxy: re-insert, then buffer
+		int pk = W->proxyKey[sh];
+		if ( pk != F2D_NULL )
+		{
+			tree_pull( W, pk & 3 );
+			W->trees[pk & 3].move_proxy( pk >> 2, W->fat[sh] );
+			W->treeDirty[pk & 3] = true;
+			host_move( W, sh );
+			if ( ( pk & 3 ) == 0 )
+				W->staticDirty = true;
+		}
 		mark_shape( W, sh );
 	}
 	mark_body( W, b );
@@ -3239,7 +3434,15 @@ DWorld* f2d_internal_world_noalloc( int32_t worldId, cudaStream_t* st, int maxSh
 		return nullptr;
 	}
 	const DWorld& d = W->d;
-	if ( W->bodyCount > d.bodyCap || W->shapeCount > d.shapeCap || W->jointCount > d.jointCap )
+	// every path of flush_uploads that would allocate device memory: grown
+	// body, shape or joint rows, a changed sensor list (its buffers are
+	// reallocated), a broadphase tree whose node pool grew, rebuild scratch
+	bool grows = W->bodyCount > d.bodyCap || W->shapeCount > d.shapeCap || W->jointCount > d.jointCap;
+	grows = grows || W->sensorsDirty;
+	for ( int t = 0; t < 3; ++t )
+		grows = grows || ( W->treeDirty[t] && W->trees[t].cap > d.pt[t].cap );
+	grows = grows || std::max( W->trees[1].cap, W->trees[2].cap ) > d.rb.cap;
+	if ( grows )
 	{
 		*code = F2D_NOALLOC_NEEDS_GROWTH;
 		return nullptr;

@@ -423,10 +423,12 @@ F2D_API int32_t f2d_world_overlap_aabb( int32_t worldId, double lowerX, double l
  * before capturing any stream. Calls that overlap in time on one device
  * share the array and race; serialise them.
  * Returns F2D_NOALLOC_TOO_MANY_SHAPES when the world holds more shapes than
- * the array can take, F2D_NOALLOC_NEEDS_GROWTH when bodies or shapes were
- * created past the world's device capacities since the last step (step the
- * world or call f2d_world_reserve first), F2D_NOALLOC_DEVICE_SETUP when the
- * array's address cannot be resolved. No output is written in those cases. */
+ * the array can take, F2D_NOALLOC_NEEDS_GROWTH when the world's pending
+ * uploads would allocate (bodies or shapes created past its device
+ * capacities, a sensor shape created, a broadphase tree whose node pool
+ * grew, since the last step: step the world, or call f2d_world_reserve
+ * first), F2D_NOALLOC_DEVICE_SETUP when the array's address cannot be
+ * resolved. No output is written in those cases. */
 #define F2D_OVERLAP_NOALLOC_MAX_SHAPES 262144
 #define F2D_NOALLOC_TOO_MANY_SHAPES ( -1 )
 #define F2D_NOALLOC_NEEDS_GROWTH ( -2 )

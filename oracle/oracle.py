@@ -22,7 +22,25 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SO = os.path.join(HERE, "_ref", "libbox2d_ref.so")
 PORT_SO = os.path.join(HERE, "_build", "libf2d_port.so")
-REF_B2 = "/root/reference/packages/forge2d/third_party/box2d"
+
+
+def reference_box2d_dir() -> str:
+    """The reference's vendored Box2D tree: $F2D_REF_B2 when set, else the
+    default of the build recipe (``REF_B2 ?=`` in oracle/Makefile)."""
+    env = os.environ.get("F2D_REF_B2")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                if line.startswith("REF_B2 ?="):
+                    return line.split("?=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+REF_B2 = reference_box2d_dir()
 
 BODY_STRIDE = 12
 CONTACT_INTS = 9
@@ -134,7 +152,7 @@ def build_ref(quiet=True) -> bool:
     """Compile the reference library in place (needs the reference tree)."""
     if not os.path.isdir(REF_B2):
         return os.path.exists(REF_SO)
-    r = subprocess.run(["make", "-C", HERE, "ref", "-j8"], capture_output=quiet)
+    r = subprocess.run(["make", "-C", HERE, "ref", "-j8", "REF_B2=" + REF_B2], capture_output=quiet)
     return r.returncode == 0 and os.path.exists(REF_SO)
 
 
@@ -199,6 +217,7 @@ def _bind(lib, prefix):
         "world_enable_sleeping": (None, [i, i]),
         "tree_order": (i, [i, i, _P(i), i]),
         "tree_stats": (None, [i, i, _P(i)]),
+        "tree_nodes": (i, [i, i, _P(i), _P(C.c_float), i]),
     }
     out = {}
     for name, (res, args) in sig.items():
@@ -271,6 +290,15 @@ class _CpuWorld:
         out = np.zeros(self._fns["shape_capacity"](self.w) + 1, np.int32)
         n = self._fns["tree_order"](self.w, body_type, out.ctypes.data_as(_P(C.c_int)), len(out))
         return out[:n].copy()
+
+    def tree_nodes(self, body_type):
+        """Port only: every node of a tree as ints (child1, child2, parent,
+        height, flags, shape) and boxes (lower, upper), by node id."""
+        cap = self._fns["tree_nodes"](self.w, body_type, None, None, 0)
+        ints = np.zeros((cap, 6), np.int32)
+        boxes = np.zeros((cap, 4), np.float32)
+        self._fns["tree_nodes"](self.w, body_type, _iptr(ints), _fptr(boxes), cap)
+        return ints, boxes
 
     def tree_stats(self, body_type):
         """(nodeCount, nodeCapacity, proxyCount, height, root, freeList)."""

@@ -930,9 +930,11 @@ void p_solve( World* w, float dt, int subStepCount )
 
 	// solver.c:1842-1905: enlarge the tree proxies of the flagged bodies and
 	// build the move array, in awake-set order (the enlarged-body bitset is
-	// indexed by awake-set position), each body's shapes in list order
+	// indexed by awake-set position), each body's shapes in list order; the
+	// tree enlargements themselves commute and run in parallel
 	{
 		const IntArr* awake = &w->sets[SET_AWAKE].bodies;
+		int first = w->moveCount;
 		for ( int k = 0; k < awake->count; ++k )
 		{
 			Body* body = w->bodies + awake->data[k];
@@ -945,10 +947,34 @@ void p_solve( World* w, float dt, int subStepCount )
 				if ( sh->enlarged )
 				{
 					sh->enlarged = 0;
-					rt_enlarge_proxy( w->trees + ( sh->proxyKey & 3 ), sh->proxyKey >> 2, sh->fatAABB );
 					p_push_move( w, s );
 				}
 			}
+		}
+		int n = w->moveCount - first;
+		int* proxies[3] = { NULL, NULL, NULL };
+		box2* boxes[3] = { NULL, NULL, NULL };
+		int counts[3] = { 0, 0, 0 };
+		for ( int t = 1; t < 3; ++t )
+		{
+			proxies[t] = malloc( sizeof( int ) * (size_t)( n + 1 ) );
+			boxes[t] = malloc( sizeof( box2 ) * (size_t)( n + 1 ) );
+		}
+		for ( int i = first; i < w->moveCount; ++i )
+		{
+			Shape* sh = w->shapes + w->moveArray[i];
+			int t = sh->proxyKey & 3;
+			if ( t == BODY_STATIC )
+				continue;
+			proxies[t][counts[t]] = sh->proxyKey >> 2;
+			boxes[t][counts[t]] = sh->fatAABB;
+			counts[t] += 1;
+		}
+		for ( int t = 1; t < 3; ++t )
+		{
+			rt_enlarge_many( w->trees + t, proxies[t], boxes[t], counts[t] );
+			free( proxies[t] );
+			free( boxes[t] );
 		}
 	}
 	// island sleeping, last (solver.c:1995-2048)

@@ -469,13 +469,15 @@ void rt_set_category( RTree* t, int proxyId, uint64_t category )
 }
 
 // :1114-1170 b2DynamicTree_Query: explicit stack, child1 pushed before child2
-// (so child2's subtree is visited first)
+// (so child2's subtree is visited first); the stack lives on the C stack
+// and moves to the heap only for trees deeper than it holds
 void rt_query( const RTree* t, box2 aabb, uint64_t maskBits, rt_visit_fn fn, void* context )
 {
 	if ( t->count == 0 || t->root == P_NULL )
 		return;
+	int local[256];
+	int* stack = local;
 	int stackCap = 256, sp = 0;
-	int* stack = malloc( sizeof( int ) * (size_t)stackCap );
 	stack[sp++] = t->root;
 	while ( sp > 0 )
 	{
@@ -492,15 +494,86 @@ void rt_query( const RTree* t, box2 aabb, uint64_t maskBits, rt_visit_fn fn, voi
 			{
 				if ( sp + 2 > stackCap )
 				{
+					int* bigger = malloc( sizeof( int ) * (size_t)stackCap * 2 );
+					memcpy( bigger, stack, sizeof( int ) * (size_t)sp );
+					if ( stack != local )
+						free( stack );
+					stack = bigger;
 					stackCap *= 2;
-					stack = realloc( stack, sizeof( int ) * (size_t)stackCap );
 				}
 				stack[sp++] = n->child1;
 				stack[sp++] = n->child2;
 			}
 		}
 	}
-	free( stack );
+	if ( stack != local )
+		free( stack );
+}
+
+static int cas_lower( float* addr, float v )
+{
+	int* ia = (int*)addr;
+	int old = __atomic_load_n( ia, __ATOMIC_RELAXED );
+	for ( ;; )
+	{
+		float cur;
+		memcpy( &cur, &old, sizeof( cur ) );
+		if ( !( v < cur ) )
+			return 0;
+		int nv;
+		memcpy( &nv, &v, sizeof( nv ) );
+		if ( __atomic_compare_exchange_n( ia, &old, nv, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED ) )
+			return 1;
+	}
+}
+
+static int cas_upper( float* addr, float v )
+{
+	int* ia = (int*)addr;
+	int old = __atomic_load_n( ia, __ATOMIC_RELAXED );
+	for ( ;; )
+	{
+		float cur;
+		memcpy( &cur, &old, sizeof( cur ) );
+		if ( !( cur < v ) )
+			return 0;
+		int nv;
+		memcpy( &nv, &v, sizeof( nv ) );
+		if ( __atomic_compare_exchange_n( ia, &old, nv, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED ) )
+			return 1;
+	}
+}
+
+// Many b2DynamicTree_EnlargeProxy calls at once (proxy ids and boxes in
+// `count` rows). The serial calls leave every ancestor of an enlarged leaf
+// marked, with its old box joined with the new boxes of the leaves below it,
+// whatever their order; here each leaf climbs with compare-and-swap unions
+// and stops at an ancestor that already held its box and was already
+// marked (the thread that marked it carries the climb on), which gives the
+// same boxes and marks.
+void rt_enlarge_many( RTree* t, const int* proxies, const box2* boxes, int count )
+{
+	RNode* nodes = t->nodes;
+#pragma omp parallel for schedule( dynamic, 256 )
+	for ( int k = 0; k < count; ++k )
+	{
+		int leaf = proxies[k];
+		box2 b = boxes[k];
+		nodes[leaf].aabb = b;
+		int p = nodes[leaf].parent;
+		while ( p != P_NULL )
+		{
+			box2* pb = &nodes[p].aabb;
+			int changed = cas_lower( &pb->lo.x, b.lo.x );
+			changed |= cas_lower( &pb->lo.y, b.lo.y );
+			changed |= cas_upper( &pb->hi.x, b.hi.x );
+			changed |= cas_upper( &pb->hi.y, b.hi.y );
+			int old = __atomic_fetch_or( &nodes[p].flags, RN_ENLARGED, __ATOMIC_RELAXED );
+			if ( !changed && ( old & RN_ENLARGED ) )
+				break;
+			p = nodes[p].parent;
+		}
+	}
 }
 
 // :1426-1552 b2PartitionMid: Hoare partition of the centres about the middle

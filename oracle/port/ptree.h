@@ -54,6 +54,9 @@ int rt_create_proxy( RTree* t, box2 aabb, uint64_t category, int shape );
 void rt_destroy_proxy( RTree* t, int proxyId );
 void rt_move_proxy( RTree* t, int proxyId, box2 aabb );
 void rt_enlarge_proxy( RTree* t, int proxyId, box2 aabb );
+// rt_enlarge_proxy of `count` proxies at once (same result as the calls in
+// any order)
+void rt_enlarge_many( RTree* t, const int* proxies, const box2* boxes, int count );
 void rt_set_category( RTree* t, int proxyId, uint64_t category );
 int rt_rebuild( RTree* t, int fullBuild );
 

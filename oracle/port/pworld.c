@@ -2075,3 +2075,29 @@ void orc_tree_stats( int wi, int type, int* out6 )
 	out6[4] = t->root;
 	out6[5] = t->freeList;
 }
+
+// Every node of the restated tree of one body type: ints (child1, child2,
+// parent, height, flags, shape) and box (lower, upper) per node id; returns
+// the node capacity
+int orc_tree_nodes( int wi, int type, int* ints, float* boxes, int cap )
+{
+	const RTree* t = p_world( wi )->trees + type;
+	int n = t->cap < cap ? t->cap : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		const RNode* nd = t->nodes + i;
+		int* k = ints + 6 * i;
+		k[0] = nd->child1;
+		k[1] = nd->child2;
+		k[2] = nd->parent;
+		k[3] = nd->height;
+		k[4] = nd->flags;
+		k[5] = nd->shape;
+		float* b = boxes + 4 * i;
+		b[0] = nd->aabb.lo.x;
+		b[1] = nd->aabb.lo.y;
+		b[2] = nd->aabb.hi.x;
+		b[3] = nd->aabb.hi.y;
+	}
+	return t->cap;
+}

@@ -1135,3 +1135,11 @@ void ref_tree_stats( int w, int type, int* out6 )
 	out6[4] = t->root;
 	out6[5] = t->freeList;
 }
+
+// b2World_GetProfile of the last step (milliseconds): step, pairs, collide,
+// solve, then the solver's stages in the struct's order (22 floats)
+void ref_world_profile( int w, float* out22 )
+{
+	b2Profile p = b2World_GetProfile( s_worlds[w] );
+	memcpy( out22, &p, sizeof( float ) * 22 );
+}

@@ -5,12 +5,14 @@ oracle/_ref/libbox2d_ref.so by oracle/Makefile) on seeded scenes from
 forge2d_gb300/scenes.py and records, per frame, the contact ids the
 reference created (so a candidate can reproduce its contact order) and,
 at checkpoint frames, every body's position, rotation, linear and angular
-velocity and centre of mass, the colour occupancy and a contact dump.
+velocity and centre of mass, the colour occupancy and a contact dump; for
+the full-size workloads, a digest of the bodies and colours of every frame.
 
 Usage: python tests/golden/make_golden.py   (needs the reference checkout)
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import sys
@@ -57,6 +59,43 @@ CASES = {
                        scene=("pile", dict(count=300, seed=3, width=20.0, height=30.0)), frames=360,
                        checkpoints=[1, 100, 250, 300, 360]),
 }
+
+
+# Full-size workloads, recorded as per-frame digests (the states themselves
+# would be hundreds of megabytes): the 100k-body mixed pile (its first 60
+# frames: free fall, first contacts, the first dense frames) and the 64
+# pyramids plus 200 fifty-link chains (10k revolute joints, deep overflow
+# colours). The reference runs with a thread pool (its results do not depend
+# on the worker count with sleeping off).
+DIGEST_CASES = {
+    "pile100k": dict(world=dict(enableSleep=0, enableContinuous=1), scene=("pile", dict(count=100_000, seed=1234)),
+                     frames=60),
+    "stack_chains": dict(world=dict(enableSleep=0), scene=("pyramids_chains", dict()), frames=64),
+}
+
+
+def frame_digest(world):
+    """SHA-256 (first 128 bits) of every body row (position, rotation,
+    linear and angular velocity, centre of mass) and the colour counts."""
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(world.bodies()[:, :9], np.float32).tobytes())
+    h.update(np.ascontiguousarray(world.color_counts(), np.int32).tobytes())
+    return h.hexdigest()[:32]
+
+
+def record_digests(name, spec, workers=8):
+    w = RefWorld(scenes.world_def(**spec["world"]), workers=workers)
+    scene, kw = spec["scene"]
+    scenes.build(w, scene, **kw)
+    digests, contacts = [], []
+    for _ in range(spec["frames"]):
+        w.step(1.0 / 60.0, 4)
+        digests.append(frame_digest(w))
+        contacts.append(int(len(w.contacts()[0])))
+    with open(os.path.join(HERE, name + "_digests_ref.json"), "w") as f:
+        json.dump({"world": spec["world"], "scene": scene, "kw": kw, "digests": digests, "contacts": contacts}, f,
+                  indent=0)
+    w.close()
 
 
 def record(name, spec):
@@ -186,6 +225,9 @@ if __name__ == "__main__":
     for name, spec in CASES.items():
         if not only or name in only:
             record(name, spec)
+    for name, spec in DIGEST_CASES.items():
+        if not only or name in only:
+            record_digests(name, spec)
     if only:
         sys.exit(0)
     record_stats("pyramid", dict(enableSleep=0), "pyramid", dict(), 256)

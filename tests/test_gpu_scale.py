@@ -1,7 +1,10 @@
-"""The full-size workload (100k-body mixed pile) on the GPU.
+"""The full-size workloads on the GPU.
 
-Bit-exact against the oracle over the scene's whole 600 frames (the
-multithreaded restatement steps them in about ten seconds), and
+Bit-exact against the reference's own per-frame digests at the workloads'
+sizes (the 100k-body mixed pile, the 64 pyramids plus 200 chains), with no
+reference contact ids handed over; bit-exact against the oracle over the
+pile's whole 600 frames (the multithreaded restatement steps them in about
+ten seconds); and
 size-independent properties over a run: every step ends with status 0,
 states stay finite, the run is deterministic, every colour 0..10 holds at
 most one constraint per dynamic body, and the contact table holds one
@@ -15,6 +18,7 @@ import pytest
 from forge2d_gb300 import scenes
 
 from parity import compare_contacts
+from test_oracle_fullsize import DIGEST_CASES, load_digests, step_and_compare
 
 pytestmark = pytest.mark.gpu
 
@@ -27,6 +31,19 @@ def make_gpu():
     g = GpuWorld(scenes.world_def(**WKW))
     scenes.build(g, "pile", **PILE)
     return g
+
+
+@pytest.mark.parametrize("name", DIGEST_CASES)
+def test_gpu_full_size_digests_match_reference(gpu_lib, name):
+    """Every frame's body rows and colour counts equal the reference's
+    (digests recorded from the unmodified reference)."""
+    from forge2d_gb300.world import GpuWorld
+    gold = load_digests(name)
+    g = GpuWorld(scenes.world_def(**gold["world"]))
+    scenes.build(g, gold["scene"], **gold["kw"])
+    step_and_compare(g, gold)
+    assert g.sync() == 0
+    g.close()
 
 
 def test_pile100k_first_frames_bit_exact(gpu_lib, port_lib):

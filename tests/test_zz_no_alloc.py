@@ -4,7 +4,9 @@ The allocation-free variant keeps its scratch in a file-scope device array
 (at most F2D_OVERLAP_NOALLOC_MAX_SHAPES shapes) instead of allocating per
 call. Two calls in a row must each return exactly what the allocating entry
 point returns -- count, order and ids, with a roomy and with a short output
-buffer -- and a world past the array's size must be rejected without output.
+buffer -- and a world past the array's size, or one whose pending uploads
+would allocate (grown rows, a changed sensor list), must be rejected without
+output.
 Collected last so that it also runs after every other test in one process.
 """
 from __future__ import annotations
@@ -87,6 +89,28 @@ def test_noalloc_overlap_rejects_oversize_and_pending_growth(gpu_lib):
     n, _ = g.overlap_aabb_noalloc(-1000.0, -1000.0, 1000.0, 1000.0)
     assert n == 4098
     g.close()
+
+    # a sensor shape created after a step makes the next upload reallocate
+    # the sensor buffers: the call is refused instead of allocating, and
+    # answers again once a step has done the upload
+    import torch
+    sw = GpuWorld(scenes.world_def(enableSleep=0))
+    base = sw.create_body(scenes.body_def(type=0))
+    sw.create_box(base, scenes.shape_def(), 5.0, 1.0)
+    sw.step(1.0 / 60.0, 4)
+    n, _ = sw.overlap_aabb_noalloc(-10.0, -10.0, 10.0, 10.0)
+    assert n == 1
+    holder = sw.create_body(scenes.body_def(type=2, positionY=4.0))
+    sw.create_circle(holder, scenes.shape_def(isSensor=1, enableSensorEvents=1), 0.0, 0.0, 0.5)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    n, rows = sw.overlap_aabb_noalloc(-10.0, -10.0, 10.0, 10.0)
+    assert n == NEEDS_GROWTH and len(rows) == 0
+    assert torch.cuda.mem_get_info()[0] == free_before
+    sw.step(1.0 / 60.0, 4)
+    n, _ = sw.overlap_aabb_noalloc(-10.0, -10.0, 10.0, 10.0)
+    assert n >= 1
+    sw.close()
 
     # a world holding more shapes than the static scratch takes is refused
     big = GpuWorld(scenes.world_def(enableSleep=0))
