@@ -9,6 +9,8 @@
 #include "pmath.h"
 #include "ptree.h"
 
+#include <pthread.h>
+
 enum
 {
 	SHAPE_CIRCLE = 0,
@@ -369,9 +371,12 @@ typedef struct World
 	RTree trees[3];
 	PairSet pairs;
 
-	// move buffer in deterministic order (shape ids)
+	// move buffer in deterministic order (shape ids), and a compact copy of
+	// the shapes' moved flags (the pair queries test it for every leaf)
 	int* moveArray;
 	int moveCount, moveCap;
+	unsigned char* movedFlag;
+	int movedFlagCap;
 
 	// overflow colour order (contact ids / joint ids) as the reference's
 	// colour-11 arrays keep them: append on add, swap-remove on remove
@@ -413,6 +418,11 @@ typedef struct World
 	int jointOrderCap;
 
 	int stepIndex;
+	// the step's tree rebuild runs beside the narrowphase and solver, as the
+	// reference's task does (world.c:488-502, solver.c:1824-1830)
+	pthread_t treeThread;
+	int treeThreadActive;
+	int treeThreadsSaved; // OpenMP threads to restore when it is joined
 
 	// islands and solver sets
 	Island* islands;
@@ -464,6 +474,7 @@ void p_wake_solver_set( World* w, int setId );
 void p_sleep_islands( World* w, const unsigned char* awakeIslandBits, int splitCandidate );
 int p_body_awake( const World* w, int bodyId );
 void p_static_order( World* w );
+void p_finish_tree_rebuild( World* w );
 int p_new_sleeping_set( World* w );
 void p_set_joint_add( World* w, int setId, int jid );
 void p_merge_solver_sets( World* w, int setId1, int setId2 );

@@ -928,6 +928,7 @@ void p_solve( World* w, float dt, int subStepCount )
 		}
 	}
 
+	p_finish_tree_rebuild( w );
 	// solver.c:1842-1905: enlarge the tree proxies of the flagged bodies and
 	// build the move array, in awake-set order (the enlarged-body bitset is
 	// indexed by awake-set position), each body's shapes in list order; the

@@ -85,8 +85,8 @@ static void node_free( RTree* t, int id )
 	t->count -= 1;
 }
 
-// refresh an internal node from its children: box, category, height, the
-// enlarged bit and the leaf count
+// refresh an internal node from its children: box, category, height and
+// the enlarged bit
 static void refresh( RTree* t, int id, int keepEnlarged )
 {
 	RNode* n = t->nodes + id;
@@ -97,7 +97,6 @@ static void refresh( RTree* t, int id, int keepEnlarged )
 	n->height = 1 + max_int( c1->height, c2->height );
 	if ( keepEnlarged )
 		n->flags |= ( c1->flags | c2->flags ) & RN_ENLARGED;
-	n->leaves = c1->leaves + c2->leaves;
 }
 
 // :187-328 b2FindBestSibling: one greedy descent, choosing between making a
@@ -216,7 +215,6 @@ static void swap_nodes( RTree* t, int a, int top, int low, int g, int keep, int 
 	nodes[a].category = nodes[low].category | nodes[g].category;
 	nodes[low].flags |= ( nodes[top].flags | nodes[keep].flags ) & RN_ENLARGED;
 	nodes[a].flags |= ( nodes[low].flags | nodes[g].flags ) & RN_ENLARGED;
-	nodes[low].leaves = nodes[top].leaves + nodes[keep].leaves;
 }
 
 // :338-623 b2RotateNodes: with A = (B, C), try swapping B or C with a
@@ -332,7 +330,6 @@ static void insert_leaf( RTree* t, int leaf, int shouldRotate )
 	nodes[np].height = nodes[sibling].height + 1;
 	nodes[np].child1 = sibling;
 	nodes[np].child2 = leaf;
-	nodes[np].leaves = nodes[sibling].leaves + nodes[leaf].leaves;
 	if ( oldParent != P_NULL )
 	{
 		if ( nodes[oldParent].child1 == sibling )
@@ -394,7 +391,6 @@ int rt_create_proxy( RTree* t, box2 aabb, uint64_t category, int shape )
 	n->category = category;
 	n->height = 0;
 	n->flags = RN_ALLOCATED | RN_LEAF;
-	n->leaves = 1;
 	insert_leaf( t, id, 1 );
 	t->proxyCount += 1;
 	return id;

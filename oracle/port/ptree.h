@@ -26,16 +26,23 @@ enum
 	RN_LEAF = 4,
 };
 
+// 40 bytes, as the reference's node: children and the leaf's user data
+// share their space
 typedef struct RNode
 {
 	box2 aabb;
 	uint64_t category;
-	int child1, child2; // internal nodes
-	int shape;          // leaves: the shape id (the reference's user data)
-	int parent;         // allocated: parent; free: next node of the free list
-	int height;         // 0 for leaves
-	int flags;
-	int leaves;         // leaves in the subtree (not in the reference; ranks)
+	union
+	{
+		struct
+		{
+			int child1, child2; // internal nodes
+		};
+		int shape; // leaves: the shape id (the reference's user data)
+	};
+	int parent; // allocated: parent; free: next node of the free list
+	uint16_t height; // 0 for leaves
+	uint16_t flags;
 } RNode;
 
 typedef struct RTree

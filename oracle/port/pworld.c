@@ -206,6 +206,7 @@ void orc_destroy_world( int wi )
 		rt_release_all( w->trees + i );
 	free( w->pairs.keys );
 	free( w->moveArray );
+	free( w->movedFlag );
 	free( w->overflowContacts );
 	free( w->overflowJoints );
 	free( w->plan );
@@ -399,6 +400,8 @@ static void push_move( World* w, int shapeId )
 	if ( s->moved )
 		return;
 	s->moved = 1;
+	w->movedFlag = grow( w->movedFlag, &w->movedFlagCap, w->shapeCount + 1, 1 );
+	w->movedFlag[shapeId] = 1;
 	w->moveArray = grow( w->moveArray, &w->moveCap, w->moveCount + 1, sizeof( int ) );
 	w->moveArray[w->moveCount++] = shapeId;
 }
@@ -1180,14 +1183,14 @@ static int pair_visit( int proxyId, int shape, void* context )
 	int proxyKey = ( proxyId << 2 ) | q->treeType;
 	if ( proxyKey == q->queryProxyKey )
 		return 1;
-	Shape* other = w->shapes + shape;
+	const unsigned char* moved = w->movedFlag;
 	if ( ( q->queryProxyKey & 3 ) == BODY_DYNAMIC )
 	{
 		// both moving: the pair belongs to the smaller proxy key's query
-		if ( q->treeType == BODY_DYNAMIC && proxyKey < q->queryProxyKey && other->moved )
+		if ( q->treeType == BODY_DYNAMIC && proxyKey < q->queryProxyKey && moved[shape] )
 			return 1;
 	}
-	else if ( other->moved )
+	else if ( moved[shape] )
 		return 1;
 	uint64_t key = pair_key( shape, q->queryShape );
 	if ( pairset_contains( &w->pairs, key ) )
@@ -1364,7 +1367,10 @@ static void update_pairs( World* w )
 	free( createOrder );
 	// reset move buffer
 	for ( int i = 0; i < w->moveCount; ++i )
+	{
 		w->shapes[w->moveArray[i]].moved = 0;
+		w->movedFlag[w->moveArray[i]] = 0;
+	}
 	w->moveCount = 0;
 	w->planCount = 0;
 	free( cands );
@@ -1695,6 +1701,45 @@ void orc_reset_phase_seconds( void )
 		g_portPhase[i] = 0.0;
 }
 
+static void* tree_rebuild_thread( void* context )
+{
+	World* w = context;
+	rt_rebuild( w->trees + BODY_DYNAMIC, 0 );
+	rt_rebuild( w->trees + BODY_KINEMATIC, 0 );
+	return NULL;
+}
+
+static void start_tree_rebuild( World* w )
+{
+	int threads = 1;
+#ifdef _OPENMP
+	threads = omp_get_max_threads();
+#endif
+	if ( threads > 1 && pthread_create( &w->treeThread, NULL, tree_rebuild_thread, w ) == 0 )
+	{
+		w->treeThreadActive = 1;
+		w->treeThreadsSaved = threads;
+#ifdef _OPENMP
+		omp_set_num_threads( threads - 1 );
+#endif
+		return;
+	}
+	tree_rebuild_thread( w );
+}
+
+// solver.c:1824-1830: the rebuild is finished before the broadphase is
+// touched again
+void p_finish_tree_rebuild( World* w )
+{
+	if ( w->treeThreadActive == 0 )
+		return;
+	pthread_join( w->treeThread, NULL );
+	w->treeThreadActive = 0;
+#ifdef _OPENMP
+	omp_set_num_threads( w->treeThreadsSaved );
+#endif
+}
+
 void orc_world_step( int wi, double timeStep, int subStepCount )
 {
 	World* w = p_world( wi );
@@ -1712,11 +1757,12 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	double t0 = p_now();
 	update_pairs( w );
 	// world.c:488-502 b2Collide -> broad_phase.c:488-492: the dynamic and
-	// kinematic trees are rebuilt over their enlarged nodes every step (the
-	// reference runs this beside the narrowphase; nothing reads the trees
-	// before the finalize that follows)
-	rt_rebuild( w->trees + BODY_DYNAMIC, 0 );
-	rt_rebuild( w->trees + BODY_KINEMATIC, 0 );
+	// kinematic trees are rebuilt over their enlarged nodes every step, on a
+	// thread of their own as the reference's task does, while the step's
+	// parallel loops use one thread fewer (their results do not depend on
+	// the thread count); nothing reads those trees before the finalize waits
+	// for the rebuild (p_finish_tree_rebuild)
+	start_tree_rebuild( w );
 	double t1 = p_now();
 	int nc = w->contactCount;
 #pragma omp parallel for schedule( dynamic, 256 )
@@ -1730,6 +1776,7 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	g_portPhase[1] += t2 - t1;
 	g_portPhase[2] += t3 - t2;
 	p_solve( w, dt, subStepCount < 1 ? 1 : subStepCount );
+	p_finish_tree_rebuild( w );
 	p_overlap_sensors( w );
 }
 
