@@ -16,10 +16,11 @@
 //      node tested by the 32 lanes at once;
 //   3. each pair is kept by the proxy whose query creates it in the
 //      reference, with the key (that proxy's move-array position, tree of
-//      the other proxy, that proxy's rank in the reference's tree), which
-//      the reference's trees kept in proxytree.cu provide; sorting the keys
-//      gives the reference's creation order, in which contact ids are then
-//      drawn from the LIFO id pool.
+//      the other proxy, the other proxy's left-to-right rank in the
+//      reference's tree, found by a walk to the root) and the other shape as
+//      the sorted value; the reference's trees are kept in proxytree.cu.
+//      Sorting the keys gives the reference's creation order, in which
+//      contact ids are then drawn from the LIFO id pool.
 #include "dscan.cuh"
 #include "dsort.cuh"
 #include "dtree.cuh"
@@ -346,6 +347,23 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 	return false;
 }
 
+// Left-to-right position of a leaf in one of the reference's trees: the
+// leaves of every child1 subtree passed on the way up from the leaf
+__device__ __forceinline__ int tree_leaf_rank( const DProxyTree& T, int leaf )
+{
+	int r = 0, c = leaf;
+	for ( int guard = 0; guard < ( 1 << 16 ); ++guard )
+	{
+		int p = T.parent[c];
+		if ( p < 0 || p >= T.cap )
+			break;
+		if ( T.child2[p] == c )
+			r += T.leaves[T.child1[p]];
+		c = p;
+	}
+	return r;
+}
+
 // Candidate pair (si moved, sj its overlapping leaf): the filters of
 // b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup. A
 // pair whose proxies both moved belongs to one query in the reference: the
@@ -386,8 +404,9 @@ __device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int 
 		// kinematic, each left to right
 		int rb = w.pairKeyBits;
 		unsigned long long tord = typeJ == 2 ? 0ull : ( typeJ == 0 ? 1ull : 2ull );
-		unsigned long long rank = (unsigned)w.pt[typeJ].rank[keyJ >> 2];
+		unsigned long long rank = (unsigned)tree_leaf_rank( w.pt[typeJ], keyJ >> 2 );
 		w.pairKeys[slot] = ( (unsigned long long)w.shapeMove[si] << ( rb + 2 ) ) | ( tord << rb ) | rank;
+		w.pairVal[slot] = sj;
 	}
 	else
 		atomicOr( &w.sc->error, ERR_PAIR_CAPACITY );
@@ -500,7 +519,7 @@ __global__ void k_create_contacts( DWorld w, int planMode )
 	int base = w.sc->contactIdCount;
 	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
 	{
-		int s1 = w.pairVal[r], s2 = w.pairValAlt[r];
+		int s1 = w.pairValAlt[r], s2 = w.pairVal[r];
 		unsigned long long key = pair_key( s1, s2 );
 		// A is the shape with the smaller proxy key (broad_phase.c:258-267)
 		int a = s1, b = s2;
@@ -636,8 +655,8 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );
 	// keys are unique (one per pair), so the key order alone fixes the result
 	int bits = 2 * w.pairKeyBits + 2;
-	sort_coop<unsigned long long>( w.pairKeys, nullptr, w.pairKeysAlt, nullptr, &w.sc->newPairCount, bits, w.sortHist,
-								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
+	sort_coop<unsigned long long>( w.pairKeys, w.pairVal, w.pairKeysAlt, w.pairValAlt, &w.sc->newPairCount, bits,
+								   w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
 	launch_pt_decode( w, st );
 	// broad_phase.c:267-278: the custom filter sees the new pairs last
 	if ( pairHook )

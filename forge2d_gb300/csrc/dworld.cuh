@@ -450,6 +450,7 @@ struct DWorld
 	// ---------------- finalize / events ----------------
 	int* fastBodies;
 	int* beginEv; // [2*i] shapeA shapeB
+	float* beginEvF; // [9*i] manifold: normal.xy pointCount, per point point.xy separation
 	int* endEv;
 	int* hitEvI;
 	float* hitEvF; // [5*i] point normal approachSpeed
@@ -475,6 +476,7 @@ struct DWorld
 
 	// the reference's broadphase trees and the move array (proxytree.cu)
 	DProxyTree pt[3];
+	int ptProxies[3]; // proxies per tree as of the last upload (host count)
 	DRebuild rb;
 	int* shapeMove; // per shape: position in the move array
 	int* moveShape; // move array: shape ids

@@ -337,6 +337,20 @@ __global__ void __launch_bounds__( OPS_TILE ) k_op_outputs( DWorld w, const int*
 			{
 				w.beginEv[2 * e] = sh.x;
 				w.beginEv[2 * e + 1] = sh.y;
+				// world.c:630-640: the event carries this step's manifold
+				float4 mn = w.mnorm[c];
+				int count = __float_as_int( mn.w );
+				float* o = w.beginEvF + 9 * (size_t)e;
+				o[0] = mn.x;
+				o[1] = mn.y;
+				o[2] = (float)count;
+				for ( int k = 0; k < 2; ++k )
+				{
+					float4 pb = w.mpB[2 * c + k];
+					o[3 + 3 * k] = k < count ? pb.x : 0.0f;
+					o[4 + 3 * k] = k < count ? pb.y : 0.0f;
+					o[5 + 3 * k] = k < count ? pb.z : 0.0f;
+				}
 			}
 		}
 		if ( isEnd )

@@ -30,8 +30,11 @@
 //     segment [s, e) reached through c child1 edges is freed[F - 1 - s - c]
 //     (F internal nodes; s + c is its pre-order index);
 //   * ranks: a leaf's left-to-right position is the sum of the child1 leaf
-//     counts along its path; a new pair's key is (move index of the proxy
-//     whose query creates it, tree, rank of the other proxy).
+//     counts along its path (found per new pair in broadphase.cu); a new
+//     pair's key is (move index of the proxy whose query creates it, tree,
+//     rank of the other proxy). Every leaf's rank is kept only for the
+//     static tree (continuous collision visits static shapes in its order),
+//     recomputed when the host uploads a tree.
 #include "dscan.cuh"
 #include "dsort.cuh"
 #include "dsync.cuh"
@@ -212,23 +215,15 @@ __global__ void k_pt_host_done( DWorld w, const int* flag, const int* pos )
 }
 
 // ---------------------------------------------------------------------------
-// new-pair keys -> (creating proxy's shape, other shape)
+// new-pair keys -> the creating proxy's shape (the other shape is the
+// sorted value)
 // ---------------------------------------------------------------------------
 __global__ void k_pt_decode( DWorld w )
 {
 	int n = min( w.sc->newPairCount, w.pairCap );
 	int rb = w.pairKeyBits;
-	unsigned long long low = ( 1ull << rb ) - 1ull;
 	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
-	{
-		unsigned long long k = w.pairKeys[r];
-		int move = (int)( k >> ( rb + 2 ) );
-		int tord = (int)( k >> rb ) & 3;
-		int rank = (int)( k & low );
-		int type = tord == 0 ? 2 : ( tord == 1 ? 0 : 1 );
-		w.pairVal[r] = w.moveShape[move];
-		w.pairValAlt[r] = w.pt[type].rankShape[rank];
-	}
+		w.pairValAlt[r] = w.moveShape[(int)( w.pairKeys[r] >> ( rb + 2 ) )];
 }
 
 // ---------------------------------------------------------------------------
@@ -974,13 +969,13 @@ void launch_pt_decode( DWorld& w, cudaStream_t st )
 }
 
 // collide phase: partial rebuild of the dynamic and kinematic trees
-// (broad_phase.c:488-492), then their ranks
+// (broad_phase.c:488-492)
 void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 {
 	for ( int t = 2; t >= 1; --t )
 	{
 		const DProxyTree& T = w.pt[t];
-		if ( T.cap == 0 )
+		if ( T.cap == 0 || w.ptProxies[t] == 0 )
 			continue;
 		int g = grid_for( T.cap );
 		k_pt_mark<<<g, 256, 0, st>>>( w, t );
@@ -995,7 +990,6 @@ void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 		}
 		k_pt_small<<<F2D_SMS * 4, PT_THREADS, 0, st>>>( w, t );
 		k_pt_refresh<<<g, 256, 0, st>>>( w, t );
-		k_pt_ranks<<<g, 256, 0, st>>>( w, t, 1 );
 	}
 }
 

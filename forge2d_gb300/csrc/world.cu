@@ -137,6 +137,9 @@ struct HostWorld
 	// thread-block cluster (F2D_NO_CLUSTER_SOLVER set at world creation)
 	bool gridSolverOnly = false;
 
+	// state of the host mirror of device-changed body rows (MIRROR_*)
+	int bodyMirror = 0;
+
 	// device staging of the bulk body reader (12 floats per body)
 	float* packedBodies = nullptr;
 	int packedCap = 0;
@@ -284,6 +287,7 @@ static void grow_contacts( HostWorld* W, int cap )
 	dgrow( d.kImp, 0, cap );
 	dgrow( d.kTot, 0, cap );
 	dgrow( d.beginEv, 0, 2 * (size_t)cap );
+	dgrow( d.beginEvF, 0, 9 * (size_t)cap );
 	dgrow( d.endEv, 0, 2 * (size_t)cap );
 	dgrow( d.hitEvI, 0, 2 * (size_t)cap );
 	dgrow( d.hitEvF, 0, 5 * (size_t)cap );
@@ -652,21 +656,79 @@ static void upload_joint_rows( HostWorld* W, int lo, int hi )
 }
 
 // bring one existing body's device-updated fields into the host mirror
+// The host mirror of the body rows the device changes. After a step or an
+// explosion every row may have changed: the first read refreshes the whole
+// mirror with one copy per array and later reads are free. After a
+// device-side wake or sleep of single bodies, rows are read back one at a
+// time until the next step. Rows created or edited on the host since the
+// last upload stay authoritative on the host throughout.
+enum
+{
+	MIRROR_FRESH = 0,
+	MIRROR_ROWS_STALE = 1,
+	MIRROR_ALL_STALE = 2,
+};
+
+static void body_rows_changed( HostWorld* W, bool all )
+{
+	if ( all )
+		W->bodyMirror = MIRROR_ALL_STALE;
+	else if ( W->bodyMirror == MIRROR_FRESH )
+		W->bodyMirror = MIRROR_ROWS_STALE;
+}
+
+static void pull_body_rows( HostWorld* W, int lo, int hi )
+{
+	DWorld& d = W->d;
+	down( W->xf, d.xf, lo, hi );
+	down( W->vel, d.vel, lo, hi );
+	down( W->delta, d.delta, lo, hi );
+	down( W->center, d.center, lo, hi );
+	down( W->sweep0, d.sweep0, lo, hi );
+	down( W->force, d.force, lo, hi );
+	down( W->bflags, d.bflags, lo, hi );
+}
+
 static void pull_body( HostWorld* W, int b )
 {
-	// rows not yet uploaded, or edited on the host since the last upload, are
-	// authoritative on the host
 	if ( b >= W->bodyUploaded || ( b < (int)W->bodyIsDirty.size() && W->bodyIsDirty[b] ) )
 		return;
+	if ( W->bodyMirror == MIRROR_FRESH )
+		return;
 	cudaStreamSynchronize( W->stream );
-	DWorld& d = W->d;
-	down( W->xf, d.xf, b, b + 1 );
-	down( W->vel, d.vel, b, b + 1 );
-	down( W->delta, d.delta, b, b + 1 );
-	down( W->center, d.center, b, b + 1 );
-	down( W->sweep0, d.sweep0, b, b + 1 );
-	down( W->force, d.force, b, b + 1 );
-	down( W->bflags, d.bflags, b, b + 1 );
+	if ( W->bodyMirror == MIRROR_ROWS_STALE )
+	{
+		pull_body_rows( W, b, b + 1 );
+		return;
+	}
+	// whole mirror; host-edited rows are kept
+	std::vector<int> keep = W->bodyDirty;
+	std::vector<float4> kx, kv, kd, ks, kf;
+	std::vector<float2> kc;
+	std::vector<int> kb;
+	for ( int r : keep )
+	{
+		kx.push_back( W->xf[r] );
+		kv.push_back( W->vel[r] );
+		kd.push_back( W->delta[r] );
+		ks.push_back( W->sweep0[r] );
+		kf.push_back( W->force[r] );
+		kc.push_back( W->center[r] );
+		kb.push_back( W->bflags[r] );
+	}
+	pull_body_rows( W, 0, W->bodyUploaded );
+	for ( size_t k = 0; k < keep.size(); ++k )
+	{
+		int r = keep[k];
+		W->xf[r] = kx[k];
+		W->vel[r] = kv[k];
+		W->delta[r] = kd[k];
+		W->sweep0[r] = ks[k];
+		W->force[r] = kf[k];
+		W->center[r] = kc[k];
+		W->bflags[r] = kb[k];
+	}
+	W->bodyMirror = MIRROR_FRESH;
 }
 
 static void mark_body( HostWorld* W, int b )
@@ -796,6 +858,9 @@ static void tree_upload( HostWorld* W, int t )
 	up( T.cat, h.cat, 0, n, W->stream );
 	W->treeScalars[t] = h.root;
 	W->treeScalars[3 + t] = h.proxyCount;
+	if ( ( d.ptProxies[t] == 0 ) != ( h.proxyCount == 0 ) )
+		W->graphDirty = true; // the step launches a tree's rebuild only when it has proxies
+	d.ptProxies[t] = h.proxyCount;
 	cudaMemcpyAsync( &d.sc->treeRoot[t], &W->treeScalars[t], sizeof( int ), cudaMemcpyHostToDevice, W->stream );
 	cudaMemcpyAsync( &d.sc->treeProxies[t], &W->treeScalars[3 + t], sizeof( int ), cudaMemcpyHostToDevice,
 					 W->stream );
@@ -935,7 +1000,10 @@ static void flush_uploads( HostWorld* W )
 	if ( W->islOn && W->d.isl )
 	{
 		if ( W->islBodiesUploaded )
+		{
 			launch_isl_fix_flags( W->d, W->stream, W->bodyCount );
+			body_rows_changed( W, false );
+		}
 		W->islBodiesUploaded = false;
 		if ( !W->islLog.empty() )
 		{
@@ -945,6 +1013,7 @@ static void flush_uploads( HostWorld* W )
 			cudaMemcpyAsync( &W->islDev->logCount, &W->islLogCount, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
 			cudaStreamSynchronize( W->stream );
 			launch_isl_create( W->d, W->stream );
+			body_rows_changed( W, false );
 			W->islLog.clear();
 			W->graphDirty = true;
 		}
@@ -1048,7 +1117,7 @@ static void free_world( HostWorld* W )
 	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
 	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 ); F( jdef3 );
 	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprep3 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
-	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
+	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( beginEvF ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
 	F( sensorBeginEv ); F( sensorEndEv ); F( cbList ); F( cbReject ); F( cbManifold ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
 	F( shapeMove ); F( moveShape ); F( hostMoves ); F( newPairId );
@@ -2261,9 +2330,11 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	cudaEventRecord( W->evStop, W->stream );
 	cudaMemcpyAsync( W->hostError, &W->d.sc->error, sizeof( int ), cudaMemcpyDeviceToHost, W->stream );
 	W->stepped = true;
-	// the step enlarged and rebuilt the kinematic and dynamic trees
+	// the step enlarged and rebuilt the kinematic and dynamic trees and
+	// changed every awake body row
 	W->treeStale[1] = true;
 	W->treeStale[2] = true;
+	body_rows_changed( W, true );
 	cudaError_t e = cudaGetLastError();
 	if ( e != cudaSuccess )
 		W->statusAccum |= F2D_STATUS_CUDA;
@@ -2540,6 +2611,7 @@ extern "C" F2D_API void f2d_world_enable_sleeping( int32_t worldId, int32_t enab
 	{
 		flush_uploads( W );
 		launch_isl_api( W->d, W->stream, 2, 0 );
+		body_rows_changed( W, false );
 	}
 }
 
@@ -2672,7 +2744,10 @@ static bool isl_edit( HostWorld* W, int b, bool wake )
 		return true;
 	flush_uploads( W );
 	if ( wake )
+	{
 		launch_isl_api( W->d, W->stream, 0, b );
+		body_rows_changed( W, false );
+	}
 	return isl_set_of( W, b ) == SET_AWAKE;
 }
 
@@ -2855,6 +2930,7 @@ extern "C" F2D_API void f2d_body_set_awake( int32_t index1, int32_t wg, int32_t 
 		return;
 	flush_uploads( W );
 	launch_isl_api( W->d, W->stream, awake ? 0 : 1, b );
+	body_rows_changed( W, false );
 }
 
 // RawBox2D.worldExplode (raw_box2d.dart:1342 -> b2World_Explode, world.c:2718):
@@ -2868,6 +2944,7 @@ extern "C" F2D_API void f2d_world_explode( int32_t worldId, int64_t maskBits, do
 	flush_uploads( W );
 	launch_explode( W->d, W->stream, W->s.tmpA, (unsigned long long)maskBits, (float)positionX, (float)positionY,
 					(float)radius, (float)falloff, (float)impulsePerLength );
+	body_rows_changed( W, true );
 }
 
 // RawBox2D.bodyIsSleepEnabled / bodyEnableSleep (raw_box2d.dart:235-242;
@@ -2889,6 +2966,7 @@ extern "C" F2D_API void f2d_body_enable_sleep( int32_t index1, int32_t wg, int32
 	{
 		flush_uploads( W );
 		launch_isl_api( W->d, W->stream, 0, b );
+		body_rows_changed( W, false );
 	}
 	pull_body( W, b );
 	if ( enabled )
@@ -3261,6 +3339,22 @@ extern "C" F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t*
 	int c[4];
 	f2d_world_get_event_counts( worldId, c );
 	return read_pairs( W, W->d.beginEv, c[0], out4, cap );
+}
+
+// The manifolds of the begin events (RawContactBeginEvent's normal and
+// points, raw_box2d_ffi.dart:2205-2228, from b2ContactBeginTouchEvent.
+// manifold): 9 floats per event in the order of f2d_world_get_begin_events.
+extern "C" F2D_API int32_t f2d_world_get_begin_manifolds( int32_t worldId, float* out9, int32_t cap )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	int c[4];
+	f2d_world_get_event_counts( worldId, c );
+	int n = std::min( c[0], cap );
+	if ( n > 0 )
+		cudaMemcpy( out9, W->d.beginEvF, sizeof( float ) * 9 * (size_t)n, cudaMemcpyDeviceToHost );
+	return n;
 }
 
 extern "C" F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* out4, int32_t cap )

@@ -180,6 +180,7 @@ _SIGS = [
     ("f2d_joint_is_valid", _i, [_i, _i]),
     ("f2d_world_get_event_counts", None, [_i, _P(_i)]),
     ("f2d_world_get_begin_events", _i, [_i, _P(_i), _i]),
+    ("f2d_world_get_begin_manifolds", _i, [_i, _P(_f), _i]),
     ("f2d_world_get_end_events", _i, [_i, _P(_i), _i]),
     ("f2d_world_get_hit_events", _i, [_i, _P(_i), _P(_f), _i]),
     ("f2d_world_get_body_events", _i, [_i, _P(_i), _P(_f), _i]),

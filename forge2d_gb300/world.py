@@ -337,6 +337,14 @@ class GpuWorld:
         m = self.lib.f2d_world_get_begin_events(self.id, _iptr(out), n)
         return out[:m][:, [0, 2]] - 1
 
+    def begin_manifolds(self):
+        """Per begin event: normal (2), point count, then per point the world
+        point (2) and separation (9 floats)."""
+        n = int(self.event_counts()[0])
+        out = np.zeros((max(n, 1), 9), np.float32)
+        m = self.lib.f2d_world_get_begin_manifolds(self.id, out.ctypes.data_as(C.POINTER(C.c_float)), n)
+        return out[:m]
+
     def end_events(self):
         n = int(self.event_counts()[1])
         out = np.zeros((max(n, 1), 4), np.int32)

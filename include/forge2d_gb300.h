@@ -341,6 +341,13 @@ F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* counts4 );
 /* Begin / end touch events as shape id pairs (index1, worldAndGeneration) x 2
  * = 4 ints per event. Return the number written. */
 F2D_API int32_t f2d_world_get_begin_events( int32_t worldId, int32_t* out4, int32_t capacity );
+/* The manifold each begin event carries (RawContactBeginEvent normal and
+ * points, raw_box2d_ffi.dart:2205-2228; b2ContactBeginTouchEvent.manifold,
+ * world.c:630-640), in the order of f2d_world_get_begin_events: 9 floats per
+ * event -- normal x, y, point count, then per point (two slots, zero past
+ * the count) the world point x, y and the separation. Returns the number
+ * written. */
+F2D_API int32_t f2d_world_get_begin_manifolds( int32_t worldId, float* out9, int32_t capacity );
 /* RawBox2D.worldGetSensorEvents (raw_box2d.dart:1295 -> b2World_GetSensorEvents, world.c:1505):
  * begin and end events of the last step, four ints each (sensor index1,
  * worldAndGeneration, visitor index1, worldAndGeneration); returns the begin

@@ -206,6 +206,7 @@ def _bind(lib, prefix):
         "event_counts": (None, [i, _P(i)]),
         "get_begin_events": (i, [i, _P(i), i]),
         "get_end_events": (i, [i, _P(i), i]),
+        "get_begin_manifolds": (i, [i, _P(C.c_float), i]),
         "get_hit_events": (i, [i, _P(i), _P(C.c_float), i]),
         "get_move_events": (i, [i, _P(i), _P(C.c_float), i]),
         "cast_ray_closest": (i, [i, d, d, d, d, C.c_longlong, C.c_longlong, _P(i), _P(C.c_float)]),
@@ -421,6 +422,14 @@ class _CpuWorld:
         n = int(self.event_counts()[0])
         out = np.zeros((max(n, 1), 2), np.int32)
         m = self._fns["get_begin_events"](self.w, _iptr(out), n)
+        return out[:m]
+
+    def begin_manifolds(self):
+        """Per begin event: normal (2), point count, then per point the world
+        point (2) and separation (9 floats)."""
+        n = int(self.event_counts()[0])
+        out = np.zeros((max(n, 1), 9), np.float32)
+        m = self._fns["get_begin_manifolds"](self.w, _fptr(out), n)
         return out[:m]
 
     def end_events(self):

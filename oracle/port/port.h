@@ -396,6 +396,10 @@ typedef struct World
 	// events of the last step
 	int* beginEvents; // pairs shapeA shapeB
 	int beginCount, beginCap;
+	// the manifold of each begin event (types.h b2ContactBeginTouchEvent):
+	// normal, point count, then per point the world point and separation
+	float* beginManifolds;
+	int beginManifoldCap;
 	int* endEvents;
 	int endCount, endCap;
 	int* hitShapes;

@@ -212,6 +212,7 @@ void orc_destroy_world( int wi )
 	free( w->plan );
 	free( w->constraints );
 	free( w->beginEvents );
+	free( w->beginManifolds );
 	free( w->endEvents );
 	free( w->hitShapes );
 	free( w->hitData );
@@ -1636,7 +1637,24 @@ static void process_state_changes( World* w )
 		else if ( f & SIM_STARTED )
 		{
 			if ( c->enableContactEvents )
+			{
+				// world.c:630-640: the event carries the manifold of this
+				// step's collide phase
+				w->beginManifolds =
+					grow( w->beginManifolds, &w->beginManifoldCap, 9 * ( w->beginCount + 1 ), sizeof( float ) );
+				float* m = w->beginManifolds + 9 * w->beginCount;
+				m[0] = c->m.normal.x;
+				m[1] = c->m.normal.y;
+				m[2] = (float)c->m.pointCount;
+				for ( int k = 0; k < 2; ++k )
+				{
+					int on = k < c->m.pointCount;
+					m[3 + 3 * k] = on ? c->m.points[k].point.x : 0.0f;
+					m[4 + 3 * k] = on ? c->m.points[k].point.y : 0.0f;
+					m[5 + 3 * k] = on ? c->m.points[k].separation : 0.0f;
+				}
 				push_pair( &w->beginEvents, &w->beginCount, &w->beginCap, c->shapeA, c->shapeB );
+			}
 			// link first: this wakes a sleeping set the contact touches
 			c->touchingFlag = 1;
 			p_link_contact( w, id );
@@ -2045,6 +2063,17 @@ int orc_get_begin_events( int wi, int* pairs, int cap )
 	World* w = p_world( wi );
 	int n = w->beginCount < cap ? w->beginCount : cap;
 	memcpy( pairs, w->beginEvents, sizeof( int ) * 2 * (size_t)n );
+	return n;
+}
+
+// the begin events' manifolds, 9 floats per event (as
+// f2d_world_get_begin_manifolds)
+int orc_get_begin_manifolds( int wi, float* out9, int cap )
+{
+	World* w = p_world( wi );
+	int n = w->beginCount < cap ? w->beginCount : cap;
+	if ( n > 0 )
+		memcpy( out9, w->beginManifolds, sizeof( float ) * 9 * (size_t)n );
 	return n;
 }
 

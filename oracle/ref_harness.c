@@ -995,6 +995,30 @@ int ref_get_begin_events( int w, int* pairs, int cap )
 	return n;
 }
 
+// The begin events' manifolds (b2ContactBeginTouchEvent.manifold), 9 floats
+// per event: normal, point count, per point the world point and separation
+int ref_get_begin_manifolds( int w, float* out9, int cap )
+{
+	b2ContactEvents e = b2World_GetContactEvents( s_worlds[w] );
+	int n = e.beginCount < cap ? e.beginCount : cap;
+	for ( int i = 0; i < n; ++i )
+	{
+		const b2Manifold* m = &e.beginEvents[i].manifold;
+		float* o = out9 + 9 * i;
+		o[0] = m->normal.x;
+		o[1] = m->normal.y;
+		o[2] = (float)m->pointCount;
+		for ( int k = 0; k < 2; ++k )
+		{
+			int on = k < m->pointCount;
+			o[3 + 3 * k] = on ? m->points[k].point.x : 0.0f;
+			o[4 + 3 * k] = on ? m->points[k].point.y : 0.0f;
+			o[5 + 3 * k] = on ? m->points[k].separation : 0.0f;
+		}
+	}
+	return n;
+}
+
 int ref_get_end_events( int w, int* pairs, int cap )
 {
 	b2ContactEvents e = b2World_GetContactEvents( s_worlds[w] );

@@ -254,6 +254,9 @@ def test_gpu_events_match_port(gpu_lib, port_lib):
         assert np.array_equal(g.event_counts(), p.event_counts()), f
         for a, b in ((g.begin_events(), p.begin_events()), (g.end_events(), p.end_events())):
             assert sorted(map(tuple, a.tolist())) == sorted(map(tuple, b.tolist())), f
+        # begin events in contact-id order with their manifolds, bit for bit
+        assert np.array_equal(g.begin_events(), p.begin_events()), f
+        assert np.array_equal(g.begin_manifolds().view(np.uint32), p.begin_manifolds().view(np.uint32)), f
         gi, gf = g.hit_events()
         pi, pf = p.hit_events()
         assert sorted(tuple(i) + tuple(x) for i, x in zip(gi.tolist(), gf.view(np.uint32).tolist())) == \

@@ -368,7 +368,10 @@ def test_port_events_match_reference(ref_lib, port_lib):
     def each(f):
         assert np.array_equal(ref.event_counts(), port.event_counts()), f
         for a, b in ((ref.begin_events(), port.begin_events()), (ref.end_events(), port.end_events())):
-            assert sorted(map(tuple, a.tolist())) == sorted(map(tuple, b.tolist())), f
+            assert np.array_equal(a, b), f
+        # begin events carry the manifold of the collide phase, bit for bit
+        rm, pm = ref.begin_manifolds(), port.begin_manifolds()
+        assert np.array_equal(rm.view(np.uint32), pm.view(np.uint32)), f
         # hit events: same multiset; the order inside one colour follows the
         # reference's colour arrays, which the port does not keep
         assert hit_rows(ref) == hit_rows(port), f
