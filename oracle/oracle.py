@@ -217,6 +217,10 @@ def _bind(lib, prefix):
         "mouse_joint_set_target": (None, [i, i, d, d]),
         "world_enable_sleeping": (None, [i, i]),
         "tree_order": (i, [i, i, _P(i), i]),
+        "destroy_body": (None, [i, i]),
+        "destroy_shape": (None, [i, i, i]),
+        "destroy_joint": (None, [i, i]),
+        "destroy_chain": (None, [i, i]),
         "tree_stats": (None, [i, i, _P(i)]),
         "tree_nodes": (i, [i, i, _P(i), _P(C.c_float), i]),
     }
@@ -284,6 +288,19 @@ class _CpuWorld:
         """fn(shapeA, shapeB, ManifoldView) -> bool; None removes it."""
         self._presolve_cb = PRESOLVE_FN(lambda a, b, m, ctx: int(bool(fn(a, b, m.contents)))) if fn else PRESOLVE_FN()
         self._fns["set_pre_solve"](self.w, self._presolve_cb, None)
+
+    # destroy path -----------------------------------------------------
+    def destroy_body(self, body):
+        self._fns["destroy_body"](self.w, body)
+
+    def destroy_shape(self, shape, update_mass=True):
+        self._fns["destroy_shape"](self.w, shape, int(update_mass))
+
+    def destroy_joint(self, joint):
+        self._fns["destroy_joint"](self.w, joint)
+
+    def destroy_chain(self, chain):
+        self._fns["destroy_chain"](self.w, chain)
 
     def tree_order(self, body_type):
         """Leaf shape ids of the broadphase tree of ``body_type`` (0 static,

@@ -743,3 +743,101 @@ void p_merge_solver_sets( World* w, int setId1, int setId2 )
 	}
 	set_destroy( w, setId2 );
 }
+
+// ---------------------------------------------------------------------------
+// removal (the destroy path, pdestroy.c)
+// ---------------------------------------------------------------------------
+// island.c:384-424 b2UnlinkJoint
+void p_unlink_joint( World* w, int jid )
+{
+	Joint* j = w->joints + jid;
+	Island* isl = island_get( w, j->islandId );
+	if ( j->islandPrev != P_NULL )
+		w->joints[j->islandPrev].islandNext = j->islandNext;
+	if ( j->islandNext != P_NULL )
+		w->joints[j->islandNext].islandPrev = j->islandPrev;
+	if ( isl->headJoint == jid )
+		isl->headJoint = j->islandNext;
+	if ( isl->tailJoint == jid )
+		isl->tailJoint = j->islandPrev;
+	isl->jointCount -= 1;
+	isl->constraintRemoveCount += 1;
+	j->islandId = j->islandPrev = j->islandNext = P_NULL;
+}
+
+// body.c:99-157 b2RemoveBodyFromIsland: an island left without bodies is
+// destroyed
+void p_remove_body_from_island( World* w, int bodyId )
+{
+	Body* b = w->bodies + bodyId;
+	if ( b->islandId == P_NULL )
+		return;
+	int id = b->islandId;
+	Island* isl = island_get( w, id );
+	if ( b->islandPrev != P_NULL )
+		w->bodies[b->islandPrev].islandNext = b->islandNext;
+	if ( b->islandNext != P_NULL )
+		w->bodies[b->islandNext].islandPrev = b->islandPrev;
+	isl->bodyCount -= 1;
+	if ( isl->headBody == bodyId )
+	{
+		isl->headBody = b->islandNext;
+		if ( isl->headBody == P_NULL )
+			island_destroy( w, id );
+	}
+	else if ( isl->tailBody == bodyId )
+		isl->tailBody = b->islandPrev;
+	b->islandId = b->islandPrev = b->islandNext = P_NULL;
+}
+
+// body.c:412-432: swap-remove from the owning set; a sleeping set left
+// without bodies is destroyed (solver_set.c:18-29)
+void p_set_remove_body( World* w, int bodyId )
+{
+	Body* b = w->bodies + bodyId;
+	int setId = b->setIndex;
+	if ( setId == P_NULL )
+		return;
+	set_body_remove( w, setId, bodyId );
+	if ( setId >= SET_FIRST_SLEEPING && set_get( w, setId )->bodies.count == 0 )
+		set_destroy( w, setId );
+	b->setIndex = P_NULL;
+}
+
+static void remove_swap_value( IntArr* a, int v )
+{
+	for ( int i = 0; i < a->count; ++i )
+		if ( a->data[i] == v )
+		{
+			ia_remove_swap( a, i );
+			return;
+		}
+}
+
+// contact.c:428-440 / joint.c:774-787: a constraint outside the constraint
+// graph leaves its set's array by swap-remove
+void p_set_remove_contact( World* w, int cid )
+{
+	int setId = w->contacts[cid].setIndex;
+	if ( setId != P_NULL && setId != SET_AWAKE && setId < w->setCap )
+		remove_swap_value( &set_get( w, setId )->contacts, cid );
+}
+
+void p_set_remove_joint( World* w, int jid )
+{
+	int setId = w->joints[jid].setIndex;
+	if ( setId != P_NULL && setId != SET_AWAKE && setId < w->setCap )
+		remove_swap_value( &set_get( w, setId )->joints, jid );
+}
+
+// body.c:331-340 b2WakeBody
+int p_wake_body( World* w, int bodyId )
+{
+	int setId = w->bodies[bodyId].setIndex;
+	if ( setId >= SET_FIRST_SLEEPING )
+	{
+		p_wake_solver_set( w, setId );
+		return 1;
+	}
+	return 0;
+}

@@ -113,6 +113,7 @@ typedef struct Body
 	// topology
 	int headShape;
 	int shapeCount;
+	int headChain; // chains on the body, newest first (body.h headChainId)
 	int headJoint; // joint key list: (jointId << 1) | edge
 	int jointCount;
 	float sleepThreshold, sleepTime;
@@ -327,6 +328,7 @@ typedef struct PairSet
 typedef struct PChain
 {
 	int used, generation, bodyId;
+	int nextChain;
 	int count;
 	int* shapeIds;
 } PChain;
@@ -444,6 +446,10 @@ typedef struct World
 	struct PSensor* sensors;
 	int sensorCount, sensorCap;
 	IntArr sensorBegin, sensorEnd;
+	// end events made between steps (destroyed contacts and sensors): the
+	// reference reports them with the next step's end events, first
+	// (world.c:808-810 double buffer)
+	IntArr pendingEnd, pendingSensorEnd;
 	// user callbacks (world.c b2World_SetCustomFilterCallback / SetPreSolveCallback)
 	orc_custom_filter_fn customFilter;
 	void* customFilterContext;
@@ -482,6 +488,13 @@ void p_finish_tree_rebuild( World* w );
 int p_new_sleeping_set( World* w );
 void p_set_joint_add( World* w, int setId, int jid );
 void p_merge_solver_sets( World* w, int setId1, int setId2 );
+void p_unlink_joint( World* w, int jid );
+void p_remove_body_from_island( World* w, int bodyId );
+void p_set_remove_body( World* w, int bodyId );
+void p_set_remove_contact( World* w, int cid );
+void p_set_remove_joint( World* w, int jid );
+int p_wake_body( World* w, int bodyId );
+void p_joint_created( World* w, int jid );
 // constraint graph (pworld.c)
 void p_add_contact_to_graph( World* w, int cid );
 void p_remove_contact_from_graph( World* w, int cid );

@@ -212,6 +212,8 @@ void orc_destroy_world( int wi )
 	free( w->plan );
 	free( w->constraints );
 	free( w->beginEvents );
+	ia_free( &w->pendingEnd );
+	ia_free( &w->pendingSensorEnd );
 	free( w->beginManifolds );
 	free( w->endEvents );
 	free( w->hitShapes );
@@ -303,6 +305,7 @@ int orc_create_body( int wi, const f2d_body_def* d )
 	b->dq.c = 1.0f;
 	b->dq.s = 0.0f;
 	b->headShape = P_NULL;
+	b->headChain = P_NULL;
 	b->headJoint = P_NULL;
 	b->sleepThreshold = (float)d->sleepThreshold;
 	b->enableSleep = d->enableSleep != 0;
@@ -536,6 +539,9 @@ int orc_create_chain( int wi, int body, const double* points, int count, const d
 	ch->generation = gen + 1;
 	ch->used = 1;
 	ch->bodyId = body;
+	// shape.c:369-387: chains on a body form a list, newest first
+	ch->nextChain = w->bodies[body].headChain;
+	w->bodies[body].headChain = id;
 	ch->count = isLoop ? count : count - 3;
 	ch->shapeIds = (int*)malloc( sizeof( int ) * (size_t)ch->count );
 	f2d_shape_def d = { 0 };
@@ -761,6 +767,8 @@ int orc_create_revolute_joint( int wi, const f2d_revolute_def* d )
 	j->enableMotor = d->enableMotor != 0;
 	j->drawSize = (float)d->drawSize;
 	joint_finish( w, id );
+	// joint.c:549-553: a joint that blocks collision ends its bodies' contacts
+	p_joint_created( w, id );
 	return id;
 }
 
@@ -849,6 +857,10 @@ int orc_create_joint( int wi, const f2d_joint_def* d )
 		j->enableMotor = d->enableMotor != 0;
 	}
 	joint_finish( w, id );
+	// joint.c:396-400 (and the other constructors but the mouse and filter
+	// joints): a joint that blocks collision ends its bodies' contacts
+	if ( d->type != P_JOINT_MOUSE && d->type != P_JOINT_FILTER )
+		p_joint_created( w, id );
 	return id;
 }
 
@@ -1605,20 +1617,44 @@ static void push_pair( int** arr, int* count, int* cap, int a, int b )
 	*count += 1;
 }
 
-// contact.c:340-440 b2DestroyContact (no wake)
-static void destroy_contact( World* w, int cid )
+// contact.c:337-453 b2DestroyContact. During a step the end event joins this
+// step's events; between steps (`between`) it waits for the next step's.
+static void destroy_contact_ex( World* w, int cid, int wakeBodies, int between )
 {
 	Contact* c = w->contacts + cid;
 	pairset_remove( &w->pairs, pair_key( c->shapeA, c->shapeB ) );
-	if ( c->touchingFlag && c->enableContactEvents )
-		push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
+	int touching = c->touchingFlag;
+	if ( touching && c->enableContactEvents )
+	{
+		if ( between )
+		{
+			ia_push( &w->pendingEnd, c->shapeA );
+			ia_push( &w->pendingEnd, c->shapeB );
+		}
+		else
+			push_pair( &w->endEvents, &w->endCount, &w->endCap, c->shapeA, c->shapeB );
+	}
 	p_contact_edges_unlink( w, cid );
 	if ( c->islandId != P_NULL )
 		p_unlink_contact( w, cid );
 	if ( c->color != P_NULL )
 		p_remove_contact_from_graph( w, cid );
+	else
+		p_set_remove_contact( w, cid );
+	int bodyA = c->bodyA, bodyB = c->bodyB;
 	c->used = 0;
+	c->setIndex = P_NULL;
 	free_contact_id( w, cid );
+	if ( wakeBodies && touching )
+	{
+		p_wake_body( w, bodyA );
+		p_wake_body( w, bodyB );
+	}
+}
+
+static void destroy_contact( World* w, int cid )
+{
+	destroy_contact_ex( w, cid, 0, 0 );
 }
 
 // world.c:586-686: serial state changes in contact-id order
@@ -1765,10 +1801,17 @@ void orc_world_step( int wi, double timeStep, int subStepCount )
 	w->hitCount = 0;
 	w->moveEventCount = 0;
 	// end events are double-buffered in the reference and reported for the
-	// step that produced them; this port clears them at step start
+	// step that produced them; those made between steps (destroyed contacts
+	// and sensors) come first
 	w->endCount = 0;
+	for ( int i = 0; i + 1 < w->pendingEnd.count; i += 2 )
+		push_pair( &w->endEvents, &w->endCount, &w->endCap, w->pendingEnd.data[i], w->pendingEnd.data[i + 1] );
+	w->pendingEnd.count = 0;
 	w->sensorBegin.count = 0;
 	w->sensorEnd.count = 0;
+	for ( int i = 0; i < w->pendingSensorEnd.count; ++i )
+		ia_push( &w->sensorEnd, w->pendingSensorEnd.data[i] );
+	w->pendingSensorEnd.count = 0;
 	float dt = (float)timeStep;
 	if ( dt == 0.0f )
 		return;
@@ -2176,4 +2219,265 @@ int orc_tree_nodes( int wi, int type, int* ints, float* boxes, int cap )
 		b[3] = nd->aabb.hi.y;
 	}
 	return t->cap;
+}
+
+// ---------------------------------------------------------------------------
+// destroy path (body.c:343-440, shape.c:230-338, :488-540, joint.c:313-351,
+// :702-822, sensor.c:353-380, broad_phase.c:70-114)
+// ---------------------------------------------------------------------------
+static void free_id( int** freeList, int* freeCount, int id )
+{
+	*freeList = realloc( *freeList, sizeof( int ) * (size_t)( *freeCount + 1 ) );
+	( *freeList )[( *freeCount )++] = id;
+}
+
+// broad_phase.c:105-114 b2BroadPhase_DestroyProxy: out of the move array
+// (b2UnBufferMove, swap-remove) and out of its tree
+static void destroy_proxy( World* w, int sid )
+{
+	Shape* s = w->shapes + sid;
+	if ( s->proxyKey == P_NULL )
+		return;
+	if ( s->moved )
+	{
+		for ( int i = 0; i < w->moveCount; ++i )
+			if ( w->moveArray[i] == sid )
+			{
+				w->moveArray[i] = w->moveArray[w->moveCount - 1];
+				w->moveCount -= 1;
+				break;
+			}
+		s->moved = 0;
+		w->movedFlag[sid] = 0;
+	}
+	int t = s->proxyKey & 3;
+	rt_destroy_proxy( w->trees + t, s->proxyKey >> 2 );
+	if ( t == BODY_STATIC )
+		w->staticOrderDirty = 1;
+	s->proxyKey = P_NULL;
+}
+
+// sensor.c:353-380 b2DestroySensor: an end event per current visitor, then
+// the sensor leaves the sensor array by swap-remove
+static void destroy_sensor( World* w, int sid )
+{
+	Shape* s = w->shapes + sid;
+	int idx = s->sensorIndex;
+	PSensor* sn = w->sensors + idx;
+	for ( int i = 0; i < sn->overlaps2.count; ++i )
+	{
+		ia_push( &w->pendingSensorEnd, sid );
+		ia_push( &w->pendingSensorEnd, sn->overlaps2.data[i] );
+	}
+	ia_free( &sn->overlaps1 );
+	ia_free( &sn->overlaps2 );
+	int last = w->sensorCount - 1;
+	if ( idx != last )
+	{
+		w->sensors[idx] = w->sensors[last];
+		w->shapes[w->sensors[idx].shapeId].sensorIndex = idx;
+	}
+	memset( w->sensors + last, 0, sizeof( PSensor ) );
+	w->sensorCount = last;
+	s->sensorIndex = P_NULL;
+}
+
+// shape.c:230-316 b2DestroyShapeInternal
+static void destroy_shape_internal( World* w, int sid, int wakeBodies )
+{
+	Shape* s = w->shapes + sid;
+	Body* b = w->bodies + s->bodyId;
+	if ( s->prevShape != P_NULL )
+		w->shapes[s->prevShape].nextShape = s->nextShape;
+	if ( s->nextShape != P_NULL )
+		w->shapes[s->nextShape].prevShape = s->prevShape;
+	if ( sid == b->headShape )
+		b->headShape = s->nextShape;
+	b->shapeCount -= 1;
+	destroy_proxy( w, sid );
+	for ( int key = b->headContactKey; key != P_NULL; )
+	{
+		Contact* c = w->contacts + ( key >> 1 );
+		int cid = key >> 1;
+		key = c->edgeNext[key & 1];
+		if ( c->shapeA == sid || c->shapeB == sid )
+			destroy_contact_ex( w, cid, wakeBodies, 1 );
+	}
+	if ( s->sensorIndex != P_NULL )
+		destroy_sensor( w, sid );
+	free_id( &w->shapeFree, &w->shapeFreeCount, sid );
+	s->used = 0;
+}
+
+// joint.c:702-806 b2DestroyJointInternal
+static void destroy_joint_internal( World* w, int jid, int wakeBodies )
+{
+	Joint* j = w->joints + jid;
+	int ids[2] = { j->bodyA, j->bodyB };
+	for ( int e = 0; e < 2; ++e )
+	{
+		Body* b = w->bodies + ids[e];
+		int prev = e == 0 ? j->prevA : j->prevB;
+		int next = e == 0 ? j->nextA : j->nextB;
+		if ( prev != P_NULL )
+		{
+			Joint* pj = w->joints + ( prev >> 1 );
+			if ( prev & 1 )
+				pj->nextB = next;
+			else
+				pj->nextA = next;
+		}
+		if ( next != P_NULL )
+		{
+			Joint* nj = w->joints + ( next >> 1 );
+			if ( next & 1 )
+				nj->prevB = prev;
+			else
+				nj->prevA = prev;
+		}
+		if ( b->headJoint == ( ( jid << 1 ) | e ) )
+			b->headJoint = next;
+		b->jointCount -= 1;
+	}
+	if ( j->islandId != P_NULL )
+		p_unlink_joint( w, jid );
+	if ( j->setIndex == SET_AWAKE )
+		p_remove_joint_from_graph( w, jid );
+	else
+		p_set_remove_joint( w, jid );
+	j->setIndex = P_NULL;
+	j->color = P_NULL;
+	j->used = 0;
+	free_id( &w->jointFree, &w->jointFreeCount, jid );
+	if ( wakeBodies )
+	{
+		p_wake_body( w, ids[0] );
+		p_wake_body( w, ids[1] );
+	}
+}
+
+// joint.c:313-351 b2DestroyContactsBetweenBodies: the smaller contact list
+// is walked (body B's on a tie), no wake
+static void destroy_contacts_between( World* w, int bodyA, int bodyB )
+{
+	Body* a = w->bodies + bodyA;
+	Body* b = w->bodies + bodyB;
+	int key, other;
+	if ( a->contactCount < b->contactCount )
+	{
+		key = a->headContactKey;
+		other = bodyB;
+	}
+	else
+	{
+		key = b->headContactKey;
+		other = bodyA;
+	}
+	while ( key != P_NULL )
+	{
+		int cid = key >> 1, e = key & 1;
+		Contact* c = w->contacts + cid;
+		key = c->edgeNext[e];
+		int otherBody = ( e ^ 1 ) == 0 ? c->bodyA : c->bodyB;
+		if ( otherBody == other )
+			destroy_contact_ex( w, cid, 0, 1 );
+	}
+}
+
+void p_joint_created( World* w, int jid )
+{
+	Joint* j = w->joints + jid;
+	if ( j->collideConnected == 0 )
+		destroy_contacts_between( w, j->bodyA, j->bodyB );
+}
+
+void orc_destroy_joint( int wi, int jid )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || jid < 0 || jid >= w->jointCount || w->joints[jid].used == 0 )
+		return;
+	destroy_joint_internal( w, jid, 1 );
+}
+
+// shape.c:318-338 b2DestroyShape
+void orc_destroy_shape( int wi, int sid, int updateBodyMass )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || sid < 0 || sid >= w->shapeCount || w->shapes[sid].used == 0 )
+		return;
+	int bodyId = w->shapes[sid].bodyId;
+	destroy_shape_internal( w, sid, 1 );
+	if ( updateBodyMass )
+		update_mass( w, w->bodies + bodyId );
+}
+
+// shape.c:488-540 b2DestroyChain
+void orc_destroy_chain( int wi, int chainId )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || chainId < 0 || chainId >= w->chainCount || w->chains[chainId].used == 0 )
+		return;
+	PChain* ch = w->chains + chainId;
+	for ( int* link = &w->bodies[ch->bodyId].headChain; *link != P_NULL; link = &w->chains[*link].nextChain )
+		if ( *link == chainId )
+		{
+			*link = ch->nextChain;
+			break;
+		}
+	for ( int i = 0; i < ch->count; ++i )
+		destroy_shape_internal( w, ch->shapeIds[i], 1 );
+	free( ch->shapeIds );
+	ch->shapeIds = NULL;
+	ch->count = 0;
+	ch->used = 0;
+	free_id( &w->chainFree, &w->chainFreeCount, chainId );
+}
+
+// body.c:343-440 b2DestroyBody: joints, contacts, shapes (with their
+// sensors and proxies), chains, island, solver set, id
+void orc_destroy_body( int wi, int bodyId )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || bodyId < 0 || bodyId >= w->bodyCount || w->bodies[bodyId].used == 0 )
+		return;
+	Body* b = w->bodies + bodyId;
+	for ( int key = b->headJoint; key != P_NULL; )
+	{
+		Joint* j = w->joints + ( key >> 1 );
+		int jid = key >> 1;
+		key = ( key & 1 ) ? j->nextB : j->nextA;
+		destroy_joint_internal( w, jid, 1 );
+	}
+	for ( int key = b->headContactKey; key != P_NULL; )
+	{
+		int cid = key >> 1;
+		Contact* c = w->contacts + cid;
+		key = c->edgeNext[key & 1];
+		destroy_contact_ex( w, cid, 1, 1 );
+	}
+	for ( int sid = b->headShape; sid != P_NULL; sid = w->shapes[sid].nextShape )
+	{
+		Shape* s = w->shapes + sid;
+		if ( s->sensorIndex != P_NULL )
+			destroy_sensor( w, sid );
+		destroy_proxy( w, sid );
+		free_id( &w->shapeFree, &w->shapeFreeCount, sid );
+		s->used = 0;
+	}
+	for ( int c = b->headChain; c != P_NULL; c = w->chains[c].nextChain )
+	{
+		free( w->chains[c].shapeIds );
+		w->chains[c].shapeIds = NULL;
+		w->chains[c].count = 0;
+		w->chains[c].used = 0;
+		free_id( &w->chainFree, &w->chainFreeCount, c );
+	}
+	b->headChain = P_NULL;
+	p_remove_body_from_island( w, bodyId );
+	p_set_remove_body( w, bodyId );
+	b->used = 0;
+	b->headShape = P_NULL;
+	b->headJoint = P_NULL;
+	b->headContactKey = P_NULL;
+	free_id( &w->bodyFree, &w->bodyFreeCount, bodyId );
 }

@@ -1167,3 +1167,35 @@ void ref_world_profile( int w, float* out22 )
 	b2Profile p = b2World_GetProfile( s_worlds[w] );
 	memcpy( out22, &p, sizeof( float ) * 22 );
 }
+
+// ---------------------------------------------------------------------------
+// destroy path: b2DestroyBody, b2DestroyShape, b2DestroyJoint, b2DestroyChain
+// ---------------------------------------------------------------------------
+void ref_destroy_body( int w, int body )
+{
+	b2DestroyBody( ref_body_id( w, body ) );
+}
+
+void ref_destroy_shape( int w, int shape, int updateBodyMass )
+{
+	b2World* world = ref_world( w );
+	b2Shape* s = b2ShapeArray_Get( &world->shapes, shape );
+	b2ShapeId id = { shape + 1, world->worldId, s->generation };
+	b2DestroyShape( id, updateBodyMass != 0 );
+}
+
+void ref_destroy_joint( int w, int joint )
+{
+	b2World* world = ref_world( w );
+	b2Joint* j = b2JointArray_Get( &world->joints, joint );
+	b2JointId id = { joint + 1, world->worldId, j->generation };
+	b2DestroyJoint( id );
+}
+
+void ref_destroy_chain( int w, int chain )
+{
+	b2World* world = ref_world( w );
+	b2ChainShape* c = b2ChainShapeArray_Get( &world->chainShapes, chain );
+	b2ChainId id = { chain + 1, world->worldId, c->generation };
+	b2DestroyChain( id );
+}

@@ -121,3 +121,44 @@ def edit_motors(world, motors, f):
 def install_callbacks(world):
     world.set_custom_filter(filter_rule)
     world.set_pre_solve(pre_solve_rule)
+
+
+def touching_pair(world):
+    """Body ids of the first touching contact between two dynamic bodies."""
+    ints, _ = world.contacts()
+    _, sh = world.shapes()
+    mass = world.mass()
+    for r in ints:
+        if r[4] > 0 and ( r[5] & 1 ):
+            a, b = int(sh[r[1], 1]), int(sh[r[2], 1])
+            if a != b and mass[a, 2] > 0 and mass[b, 2] > 0:
+                return a, b
+    return None
+
+
+def destroy_script(world, f, ids):
+    """Destroys and re-creates between steps, the same calls on every world
+    (bodies, shapes, joints and chains picked by id from the scene built by
+    scenes.build(..., "pyramids_chains", pyramids=2, rows=8, chains=4,
+    links=10) plus two chain shapes): ``ids`` holds the picks."""
+    from forge2d_gb300 import scenes
+    if f == 30:
+        world.destroy_body(ids["box"])          # a box inside a pyramid
+        world.destroy_body(ids["link"])         # a chain link: two joints go
+    elif f == 50:
+        world.destroy_shape(ids["shape"], True)  # one of two shapes of a body
+        world.destroy_joint(ids["joint"])
+    elif f == 70:
+        world.destroy_chain(ids["chain"])
+        # new bodies take the freed ids; the proxies take freed tree nodes
+        for k in range(3):
+            b = world.create_body(scenes.body_def(type=2, positionX=-3.0 + 1.1 * k, positionY=12.0 + k))
+            world.create_circle(b, scenes.shape_def(enableContactEvents=1), 0.0, 0.0, 0.35)
+    elif f == 90:
+        pair = ids.get("touch")
+        if pair is not None:
+            # a joint between touching bodies ends their contacts
+            world.create_revolute(scenes.revolute_def(bodyA=pair[0], bodyB=pair[1], collideConnected=0))
+    elif f == 110:
+        world.destroy_body(ids["last"])
+        world.destroy_shape(ids["twin_box"], False)

@@ -152,3 +152,49 @@ def test_body_accessors_and_impulses(gpu_lib):
     assert w.gravity == (0.0, -5.0)
     assert b.is_valid and b.type == 2
     w.destroy()
+
+
+def test_per_body_reads_after_a_step_are_cheap(gpu_lib):
+    """forge2d reads each body's position through bodyGetPosition
+    (raw_box2d.dart); after a step the first read refreshes the host mirror
+    of every body row at once (under 50 ms for 100k bodies) and later reads
+    copy nothing; the reads return the device state (checked against the
+    bulk reader)."""
+    import ctypes as C
+    import time
+    from forge2d_gb300.world import GpuWorld
+    g = GpuWorld(scenes.world_def(enableSleep=0, enableContinuous=1))
+    scenes.build(g, "pile", count=100_000, seed=1234)
+    for _ in range(3):
+        assert g.step(1.0 / 60.0, 4) == 0
+    assert g.sync() == 0
+    ids = g._body_ids
+    fn = g.lib.f2d_body_get_position
+    x, y = C.c_double(0.0), C.c_double(0.0)
+    px, py = C.byref(x), C.byref(y)
+    got = np.zeros((len(ids), 2))
+    t0 = time.perf_counter()
+    fn(ids[0][0], ids[0][1], px, py)     # refreshes the whole mirror
+    first_ms = 1000.0 * (time.perf_counter() - t0)
+    t1 = time.perf_counter()
+    for k, (i1, wg) in enumerate(ids):
+        fn(i1, wg, px, py)
+        got[k, 0] = x.value
+        got[k, 1] = y.value
+    per_call_us = 1e6 * (time.perf_counter() - t1) / len(ids)
+    rows = g.bodies()
+    assert np.array_equal(got.astype(np.float32), rows[:len(ids), :2])
+    assert len(ids) > 100_000
+    # one bulk refresh; afterwards a read costs the ctypes call (a device
+    # synchronisation and seven copies per read cost tens of microseconds)
+    assert first_ms < 50.0, first_ms
+    assert per_call_us < 8.0, per_call_us
+    # a body moved on the host stays authoritative until the next step
+    i1, wg = ids[5]
+    g.lib.f2d_body_set_transform(i1, wg, 1.5, 900.0, 1.0, 0.0)
+    fn(i1, wg, px, py)
+    assert (x.value, y.value) == (1.5, 900.0)
+    assert g.step(1.0 / 60.0, 4) == 0
+    fn(i1, wg, px, py)
+    assert abs(y.value - 900.0) < 1.0
+    g.close()

@@ -16,7 +16,8 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import (blast, compare_contacts, edit_motors, filter_rule, install_callbacks, new_contacts,
+from parity import (blast, compare_contacts, destroy_script, edit_motors, filter_rule, install_callbacks,
+                    new_contacts, touching_pair,
                     pre_solve_rule, ray_answers)
 
 
@@ -417,5 +418,50 @@ def test_port_queries_on_moving_scene(ref_lib, port_lib):
 
     lockstep(ref, port, 60, each)
     assert hits[0] > 20
+    ref.close()
+    port.close()
+
+
+def build_destroy_scene(w):
+    """pyramids with chains, one body with two shapes, two chain shapes on a
+    static body; returns the ids the destroy script picks."""
+    scenes.build(w, "pyramids_chains", pyramids=2, rows=8, chains=4, links=10, gap=3.0)
+    twin = w.create_body(scenes.body_def(type=2, positionX=-2.0, positionY=9.0))
+    twin_box = w.create_box(twin, scenes.shape_def(enableContactEvents=1), 0.5, 0.3)
+    second = w.create_circle(twin, scenes.shape_def(density=2.0), 0.6, 0.0, 0.3)
+    ground = w.create_body(scenes.body_def(type=0, positionY=-6.0))
+    w.create_chain(ground, [(-40.0, 0.0), (-20.0, -1.0), (0.0, 0.0), (20.0, -1.0), (40.0, 0.0)])
+    w.create_chain(ground, [(-40.0, -3.0), (-20.0, -4.0), (0.0, -3.0), (20.0, -4.0), (40.0, -3.0)])
+    nb = len(w.bodies())
+    return {"box": 12, "link": nb // 2, "shape": second, "joint": 5, "chain": 1, "last": nb - 3,
+            "twin_box": twin_box}
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_destroy_path_with_reference(ref_lib, port_lib, sleep):
+    """b2DestroyBody / b2DestroyShape / b2DestroyJoint / b2DestroyChain
+    between steps, ids reused by bodies created after them, and a joint
+    created between touching bodies (its bodies' contacts end): bodies,
+    solver sets, contacts, colours, trees and end events in lock step."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    ids = build_destroy_scene(ref)
+    assert build_destroy_scene(port) == ids
+    ends = 0
+    for f in range(1, 141):
+        if f == 90:
+            ids["touch"] = touching_pair(ref)
+            assert ids["touch"] == touching_pair(port) and ids["touch"] is not None
+        destroy_script(ref, f, ids)
+        destroy_script(port, f, ids)
+        lockstep_full(ref, port, 1, start=f)
+        assert np.array_equal(ref.end_events(), port.end_events()), f
+        ends += len(ref.end_events())
+        if f % 10 == 0:
+            assert compare_contacts(ref, port) == [], f
+            assert np.array_equal(ref.color_counts(), port.color_counts()), f
+            trees_equal(ref, port)
+    assert ends > 0
     ref.close()
     port.close()
