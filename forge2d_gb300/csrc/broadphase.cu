@@ -568,6 +568,7 @@ __global__ void k_create_contacts( DWorld w, int planMode )
 		w.cflags[id] = flags;
 		w.ccolor[id] = F2D_NULL;
 		w.coverflowIndex[id] = F2D_NULL;
+		w.cstamp[id] = w.sc->stampBase + (unsigned long long)r;
 		float4 ma = w.mat[a], mb = w.mat[b];
 		// world.c:88-98 default mixing
 		w.cmat[id] = make_float4( sqrtf( ma.x * mb.x ), ma.y > mb.y ? ma.y : mb.y, 0.0f, 0.0f );
@@ -623,6 +624,7 @@ __global__ void k_after_create( DWorld w, int planMode )
 				w.sc->contactIdCount = min( w.sc->contactIdCount + ( n - F ), w.contactCap );
 			}
 		}
+		w.sc->stampBase += (unsigned long long)n;
 		w.sc->newPairCount = 0;
 		w.sc->planCount = 0;
 		w.sc->moveArrayCount = 0; // broad_phase.c:456-458: the move buffer is reset

@@ -136,6 +136,12 @@ struct DScalars
 	// partial rebuild of one tree: active, gathered nodes, large segments
 	// per level (two levels in flight), small segments
 	int rbActive, rbCount, rbLarge[2], rbSmall;
+	// creation stamp of the next new contact (the bodies' contact lists are
+	// newest first); non-static bodies in the awake set (worlds without
+	// island records); destroy calls: collected contacts, end events
+	unsigned long long stampBase;
+	int awakeOrderCount;
+	int apiCount, apiEndCount;
 };
 
 // node flags of the broadphase trees (dynamic_tree.c b2TreeNodeFlags)
@@ -481,6 +487,12 @@ struct DWorld
 	int* shapeMove; // per shape: position in the move array
 	int* moveShape; // move array: shape ids
 	int* hostMoves; // shapes the host buffered since the last step, in call order
+
+	// destroy path: creation stamp per contact, the awake set's body order
+	// (worlds without island records), end events of destroyed contacts
+	unsigned long long* cstamp;
+	int* awakeOrder;
+	int* apiEndEv; // [2*i] shapeA shapeB
 
 	DScalars* sc;
 	int* sortTemp;

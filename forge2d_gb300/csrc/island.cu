@@ -1281,3 +1281,369 @@ void launch_isl_fix_flags( DWorld& w, cudaStream_t st, int n )
 {
 	k_isl_fix_flags<<<grid_for( n ), 256, 0, st>>>( w, w.isl, n );
 }
+
+// ---------------------------------------------------------------------------
+// Destroy path, serial (between steps; one thread, the reference's order):
+// contact.c:337-453 b2DestroyContact, joint.c:702-806
+// b2DestroyJointInternal, body.c:99-157 b2RemoveBodyFromIsland, :412-432
+// (the body leaves its solver set), island.c:58-84, :384-424. Worlds without
+// sleeping keep no island records (Ip null): contacts and joints then only
+// leave the constraint graph.
+// ---------------------------------------------------------------------------
+// The reference's set arrays lose an element by moving their last element
+// into the hole; a sleeping set here is a singly linked list in array order,
+// so the same move is made on the list.
+template <typename Next>
+__device__ void isl_list_swap_remove( int& head, int& tail, int& count, Next next, int x )
+{
+	bool found = false;
+	int prevX = ISL_NULL, prevT = ISL_NULL;
+	for ( int k = head, p = ISL_NULL, g = 0; k != ISL_NULL && g < ( 1 << 26 ); p = k, k = next( k ), ++g )
+	{
+		if ( k == x )
+		{
+			found = true;
+			prevX = p;
+		}
+		if ( k == tail )
+			prevT = p;
+	}
+	if ( !found )
+		return;
+	count -= 1;
+	int t = tail;
+	if ( x == t )
+	{
+		if ( prevX == ISL_NULL )
+			head = ISL_NULL;
+		else
+			next( prevX ) = ISL_NULL;
+		tail = prevX;
+		return;
+	}
+	if ( prevT == x )
+	{
+		// x, then the last element: x simply leaves
+		if ( prevX == ISL_NULL )
+			head = t;
+		else
+			next( prevX ) = t;
+		return;
+	}
+	next( prevT ) = ISL_NULL;
+	tail = prevT;
+	next( t ) = next( x );
+	if ( prevX == ISL_NULL )
+		head = t;
+	else
+		next( prevX ) = t;
+}
+
+// island.c:58-84 for an island of any set
+__device__ void isl_island_destroy_any( DIslands& I, int id )
+{
+	int setId = I.islands[id].setIndex;
+	if ( setId == SET_AWAKE )
+	{
+		isl_island_destroy( I, id );
+		return;
+	}
+	if ( I.splitIslandId == id )
+		I.splitIslandId = ISL_NULL;
+	if ( setId >= SET_FIRST_SLEEPING )
+	{
+		DSet& s = I.sets[setId];
+		int moved = s.tailIsland;
+		isl_list_swap_remove( s.headIsland, s.tailIsland, s.islandCount,
+							  [&]( int k ) -> int& { return I.islands[k].setNext; }, id );
+		if ( moved != id && moved != ISL_NULL )
+			I.islands[moved].localIndex = I.islands[id].localIndex;
+	}
+	I.islands[id].setIndex = ISL_NULL;
+	I.islands[id].localIndex = ISL_NULL;
+	I.islandFree[I.islandFreeCount++] = id;
+}
+
+// island.c:384-424 b2UnlinkJoint
+__device__ void isl_unlink_joint( DIslands& I, int j )
+{
+	int id = I.jIsland[j];
+	if ( id == ISL_NULL )
+		return;
+	DIsland& isl = I.islands[id];
+	int prev = I.jIslandPrev[j], next = I.jIslandNext[j];
+	if ( prev != ISL_NULL )
+		I.jIslandNext[prev] = next;
+	if ( next != ISL_NULL )
+		I.jIslandPrev[next] = prev;
+	if ( isl.headJoint == j )
+		isl.headJoint = next;
+	if ( isl.tailJoint == j )
+		isl.tailJoint = prev;
+	isl.jointCount -= 1;
+	isl.removeCount += 1;
+	I.jIsland[j] = I.jIslandPrev[j] = I.jIslandNext[j] = ISL_NULL;
+}
+
+// body.c:331-340 b2WakeBody
+__device__ void isl_wake_body( const DWorld& w, DIslands& I, int b )
+{
+	if ( I.bSet[b] >= SET_FIRST_SLEEPING )
+		isl_wake_set( w, I, I.bSet[b] );
+}
+
+// constraint_graph.c:290-318 without island records: the overflow index of
+// a joint is its position in the overflow array
+__device__ void plain_graph_remove_joint( const DWorld& w, int j )
+{
+	int color = w.jcolor[j];
+	if ( color == F2D_NULL )
+		return;
+	int2 jb = w.jbody[j];
+	if ( color != F2D_OVERFLOW )
+	{
+		unsigned bit = 1u << color;
+		if ( !isl_static( w, jb.x ) )
+			w.colorMask[jb.x] &= ~bit;
+		if ( !isl_static( w, jb.y ) )
+			w.colorMask[jb.y] &= ~bit;
+	}
+	else
+	{
+		int last = w.sc->overflowJointCount - 1;
+		for ( int idx = 0; idx <= last; ++idx )
+			if ( w.overflowJoints[idx] == j )
+			{
+				w.overflowJoints[idx] = w.overflowJoints[last];
+				w.sc->overflowJointCount = last;
+				break;
+			}
+	}
+	w.jcolor[j] = F2D_NULL;
+}
+
+// contact.c:337-453; the end event of a touching contact with events goes to
+// the destroy buffer (reported with the next step's end events)
+__device__ void dev_destroy_contact( const DWorld& w, DIslands* Ip, int c, bool wake )
+{
+	int f = w.cflags[c];
+	if ( ( f & CF_USED ) == 0 )
+		return;
+	bool touching = ( f & CF_TOUCHING ) != 0;
+	if ( touching && ( f & CF_EVENTS ) )
+	{
+		int e = w.sc->apiEndCount++;
+		if ( e < w.contactCap )
+		{
+			int2 sh = w.cshape[c];
+			w.apiEndEv[2 * e] = sh.x;
+			w.apiEndEv[2 * e + 1] = sh.y;
+		}
+	}
+	int2 bd = w.cbody[c];
+	if ( Ip )
+	{
+		DIslands& I = *Ip;
+		isl_edges_unlink( w, I, c );
+		isl_unlink_contact( I, c );
+		if ( w.ccolor[c] != F2D_NULL )
+			isl_graph_remove_contact( w, c );
+		else
+		{
+			int s = I.cSet[c];
+			if ( s >= SET_FIRST_SLEEPING )
+				isl_list_swap_remove( I.sets[s].headContact, I.sets[s].tailContact, I.sets[s].contactCount,
+									  [&]( int k ) -> int& { return I.cSetNext[k]; }, c );
+		}
+		I.cSet[c] = ISL_NULL;
+	}
+	else if ( w.ccolor[c] != F2D_NULL )
+		isl_graph_remove_contact( w, c );
+	w.cflags[c] = 0;
+	w.ccolor[c] = F2D_NULL;
+	w.contactFree[w.sc->contactFreeCount++] = c;
+	if ( Ip && wake && touching )
+	{
+		isl_wake_body( w, *Ip, bd.x );
+		isl_wake_body( w, *Ip, bd.y );
+	}
+}
+
+// Contacts of body b in the order of its contact list (newest first): the
+// island records keep the list; without them the collected contacts are
+// ordered by creation stamp. Filters: only contacts with shape `shape`
+// (>= 0), or only those whose other body is `other` (>= 0).
+__global__ void k_collect_body_contacts( DWorld w, int b, int* out )
+{
+	int n = w.sc->contactIdCount;
+	for ( int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x )
+	{
+		if ( ( w.cflags[c] & CF_USED ) == 0 )
+			continue;
+		int2 bd = w.cbody[c];
+		if ( bd.x == b || bd.y == b )
+		{
+			int k = atomicAdd( &w.sc->apiCount, 1 );
+			if ( k < w.contactCap )
+				out[k] = c;
+		}
+	}
+}
+
+__global__ void k_destroy_body_contacts( DWorld w, DIslands* Ip, int b, int shape, int other, int wake, int* list )
+{
+	int n = 0;
+	if ( Ip )
+	{
+		DIslands& I = *Ip;
+		for ( int key = I.bHeadContact[b], g = 0; key != ISL_NULL && g < I.contactCap; ++g )
+		{
+			int c = key >> 1;
+			int4 e = I.cEdge[c];
+			list[n++] = c;
+			key = ( key & 1 ) ? e.w : e.y;
+		}
+	}
+	else
+	{
+		n = min( w.sc->apiCount, w.contactCap );
+		// newest first
+		for ( int i = 1; i < n; ++i )
+		{
+			int v = list[i];
+			unsigned long long sv = w.cstamp[v];
+			int j = i - 1;
+			while ( j >= 0 && w.cstamp[list[j]] < sv )
+			{
+				list[j + 1] = list[j];
+				j -= 1;
+			}
+			list[j + 1] = v;
+		}
+	}
+	for ( int i = 0; i < n; ++i )
+	{
+		int c = list[i];
+		int2 sh = w.cshape[c];
+		int2 bd = w.cbody[c];
+		if ( shape >= 0 && sh.x != shape && sh.y != shape )
+			continue;
+		if ( other >= 0 && ( bd.x == b ? bd.y : bd.x ) != other )
+			continue;
+		dev_destroy_contact( w, Ip, c, wake != 0 );
+	}
+	w.sc->apiCount = 0;
+}
+
+// joint.c:702-806 on the device records (the body joint lists live on the
+// host and are uploaded with the body rows)
+__global__ void k_destroy_joint( DWorld w, DIslands* Ip, int j, int wake )
+{
+	int2 jb = w.jbody[j];
+	if ( Ip )
+	{
+		DIslands& I = *Ip;
+		isl_unlink_joint( I, j );
+		int s = I.jSet[j];
+		if ( s == SET_AWAKE )
+			isl_graph_remove_joint( w, I, j );
+		else if ( s >= SET_FIRST_SLEEPING )
+			isl_list_swap_remove( I.sets[s].headJoint, I.sets[s].tailJoint, I.sets[s].jointCount,
+								  [&]( int k ) -> int& { return I.jSetNext[k]; }, j );
+		I.jSet[j] = ISL_NULL;
+	}
+	else
+		plain_graph_remove_joint( w, j );
+	w.jflags[j] = 0;
+	w.jimp[j] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	w.jimp2[j] = make_float2( 0.0f, 0.0f );
+	if ( Ip && wake )
+	{
+		isl_wake_body( w, *Ip, jb.x );
+		isl_wake_body( w, *Ip, jb.y );
+	}
+}
+
+// body.c:99-157 and :412-432: out of its island and its solver set
+__global__ void k_destroy_body_records( DWorld w, DIslands* Ip, int b )
+{
+	if ( Ip )
+	{
+		DIslands& I = *Ip;
+		int id = I.bIsland[b];
+		if ( id != ISL_NULL )
+		{
+			DIsland& isl = I.islands[id];
+			int prev = I.bIslandPrev[b], next = I.bIslandNext[b];
+			if ( prev != ISL_NULL )
+				I.bIslandNext[prev] = next;
+			if ( next != ISL_NULL )
+				I.bIslandPrev[next] = prev;
+			isl.bodyCount -= 1;
+			if ( isl.headBody == b )
+			{
+				isl.headBody = next;
+				if ( next == ISL_NULL )
+					isl_island_destroy_any( I, id );
+			}
+			else if ( isl.tailBody == b )
+				isl.tailBody = prev;
+			I.bIsland[b] = I.bIslandPrev[b] = I.bIslandNext[b] = ISL_NULL;
+		}
+		int s = I.bSet[b];
+		if ( s == SET_AWAKE )
+			isl_awake_remove_body( I, b );
+		else if ( s >= SET_FIRST_SLEEPING )
+		{
+			DSet& set = I.sets[s];
+			isl_list_swap_remove( set.headBody, set.tailBody, set.bodyCount,
+								  [&]( int k ) -> int& { return I.bSetNext[k]; }, b );
+			if ( set.bodyCount == 0 )
+				isl_set_destroy( I, s );
+		}
+		I.bSet[b] = ISL_NULL;
+		I.bHeadContact[b] = ISL_NULL;
+	}
+	w.bflags[b] = 0;
+}
+
+// broad_phase.c:70-88 b2UnBufferMove: the proxy leaves the move array by
+// swap-remove
+__global__ void k_unbuffer_move( DWorld w, int s )
+{
+	int f = w.sflags[s];
+	if ( ( f & SF_MOVED ) == 0 )
+		return;
+	int idx = w.shapeMove[s];
+	int last = w.sc->moveArrayCount - 1;
+	if ( idx != last )
+	{
+		int m = w.moveShape[last];
+		w.moveShape[idx] = m;
+		w.shapeMove[m] = idx;
+	}
+	w.sc->moveArrayCount = last;
+	w.sflags[s] = f & ~SF_MOVED;
+}
+
+void launch_destroy_contacts_of( DWorld& w, cudaStream_t st, int body, int shape, int other, int wake, int* list )
+{
+	if ( !w.isl )
+		k_collect_body_contacts<<<grid_for( w.contactCap ), 256, 0, st>>>( w, body, list );
+	k_destroy_body_contacts<<<1, 1, 0, st>>>( w, w.isl, body, shape, other, wake, list );
+}
+
+void launch_destroy_joint( DWorld& w, cudaStream_t st, int joint, int wake )
+{
+	k_destroy_joint<<<1, 1, 0, st>>>( w, w.isl, joint, wake );
+}
+
+void launch_destroy_body_records( DWorld& w, cudaStream_t st, int body )
+{
+	k_destroy_body_records<<<1, 1, 0, st>>>( w, w.isl, body );
+}
+
+void launch_unbuffer_move( DWorld& w, cudaStream_t st, int shape )
+{
+	k_unbuffer_move<<<1, 1, 0, st>>>( w, shape );
+}

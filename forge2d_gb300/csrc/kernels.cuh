@@ -67,6 +67,14 @@ void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long
 void launch_isl_split( DWorld& w, cudaStream_t st );
 void launch_isl_sleep( DWorld& w, cudaStream_t st, unsigned long long* scanState );
 void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body );
+// destroy path (island.cu), serial launches between steps: the contacts of a
+// body in its contact-list order (only those of `shape` / with body `other`
+// when >= 0; `list` holds contactCap ints), one joint, a body's island and
+// solver-set records, one proxy out of the move array
+void launch_destroy_contacts_of( DWorld& w, cudaStream_t st, int body, int shape, int other, int wake, int* list );
+void launch_destroy_joint( DWorld& w, cudaStream_t st, int joint, int wake );
+void launch_destroy_body_records( DWorld& w, cudaStream_t st, int body );
+void launch_unbuffer_move( DWorld& w, cudaStream_t st, int shape );
 void launch_isl_wake_marked( DWorld& w, cudaStream_t st, const int* shapeMarks, int shapeCount );
 void launch_explode( DWorld& w, cudaStream_t st, int* hit, unsigned long long mask, float x, float y, float radius,
 					 float falloff, float impulsePerLength );

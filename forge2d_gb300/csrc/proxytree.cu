@@ -139,12 +139,12 @@ __device__ __forceinline__ bool body_awake_plain( int f )
 // per awake-set position: the body's enlarged shapes
 __global__ void k_pt_move_count( DWorld w, int* cnt )
 {
-	int n = w.isl ? w.isl->awakeBodyCount : w.bodyCount;
+	int n = w.isl ? w.isl->awakeBodyCount : w.sc->awakeOrderCount;
 	if ( blockIdx.x == 0 && threadIdx.x == 0 )
 		w.sc->fastCount = 0;
 	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x )
 	{
-		int b = w.isl ? w.isl->awakeBodies[k] : k;
+		int b = w.isl ? w.isl->awakeBodies[k] : w.awakeOrder[k];
 		int c = 0;
 		if ( w.isl || body_awake_plain( w.bflags[b] ) )
 			for ( int s = w.headShape[b], guard = 0; s != F2D_NULL && guard < ( 1 << 20 ); s = w.nextShape[s], ++guard )
@@ -156,10 +156,10 @@ __global__ void k_pt_move_count( DWorld w, int* cnt )
 // move-array slots in awake order; the proxies' tree leaves are enlarged
 __global__ void k_pt_move_assign( DWorld w, const int* pos )
 {
-	int n = w.isl ? w.isl->awakeBodyCount : w.bodyCount;
+	int n = w.isl ? w.isl->awakeBodyCount : w.sc->awakeOrderCount;
 	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x )
 	{
-		int b = w.isl ? w.isl->awakeBodies[k] : k;
+		int b = w.isl ? w.isl->awakeBodies[k] : w.awakeOrder[k];
 		if ( !w.isl && !body_awake_plain( w.bflags[b] ) )
 			continue;
 		int slot = pos[k];
@@ -996,7 +996,7 @@ void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 // finalize: the move array in awake order, proxies enlarged
 void launch_pt_moves( DWorld& w, StepScratch& s, cudaStream_t st )
 {
-	int* count = w.isl ? (int*)( (char*)w.isl + offsetof( DIslands, awakeBodyCount ) ) : nullptr;
+	int* count = w.isl ? (int*)( (char*)w.isl + offsetof( DIslands, awakeBodyCount ) ) : &w.sc->awakeOrderCount;
 	k_pt_move_count<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, s.tmpA );
 	scan_lookback( s.tmpA, s.tmpB, count, w.bodyCount, w.bodyCap, &w.sc->moveArrayCount, s.scanState, &w.sc->error, st );
 	k_pt_move_assign<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, s.tmpB );

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -103,7 +104,22 @@ struct HostWorld
 	std::vector<std::vector<int>> chainSegments;
 	std::vector<uint16_t> chainGen;
 	std::vector<int> chainFree;
+	// chains per body (the reference's body chain list, newest first)
+	std::vector<int> chainBody, chainNext, headChain;
 	bool staticDirty = false;
+	// the awake set's non-static bodies in the reference's array order
+	// (appended at creation, swap-removed at destruction), for worlds without
+	// island records; awakeSlot is a body's position, -1 when absent
+	std::vector<int> awakeOrder, awakeSlot;
+	bool awakeOrderDirty = true;
+	int awakeOrderCount = 0; // staging of the device count
+	// end events of contacts and sensors destroyed between steps (four ints
+	// per event, ids packed at destruction): `Next` collects them, the next
+	// step reports them ahead of its own (`Prefix`), as the reference's
+	// double-buffered end event arrays do (world.c:808-810)
+	std::vector<int32_t> endNext, endPrefix, sensorEndNext, sensorEndPrefix;
+	// a zero time step cleared the step events (world.c:717-725)
+	bool eventsCleared = false;
 
 	std::vector<int2> jbody;
 	std::vector<int> jflags, jcolor, jnext;
@@ -113,6 +129,8 @@ struct HostWorld
 	std::vector<uint16_t> jgen;
 	int jointCount = 0, jointUploaded = 0;
 	std::vector<int> pendingJoints;
+	std::vector<int> jointFree; // LIFO id pool (id_pool.c)
+	std::vector<int> jointRows; // reused joint ids whose whole rows go up at the next upload
 
 	// islands and solver sets (worlds with sleeping enabled): host copy of the
 	// device record's pointers and capacities, the device record, and the
@@ -245,6 +263,7 @@ static void grow_bodies( HostWorld* W, int cap )
 	dgrow( d.colorLock, o, cap );
 	dgrow( d.fastBodies, o, cap );
 	dgrow( d.moveEvXf, o, cap );
+	dgrow( d.awakeOrder, o, cap );
 	d.bodyCap = cap;
 }
 
@@ -265,6 +284,8 @@ static void grow_contacts( HostWorld* W, int cap )
 	dgrow( d.mpB, 2 * o, 2 * (size_t)cap );
 	dgrow( d.mpI, 2 * o, 2 * (size_t)cap );
 	dgrow( d.contactFree, o, cap );
+	dgrow( d.cstamp, o, cap );
+	dgrow( d.apiEndEv, 0, 2 * (size_t)cap );
 	// step scratch sized by contacts (content not preserved)
 	dgrow( d.opContact, 0, cap );
 	dgrow( d.opKind, 0, cap );
@@ -951,6 +972,21 @@ static void flush_uploads( HostWorld* W )
 		upload_joint_rows( W, W->jointUploaded, W->jointCount );
 		W->jointUploaded = W->jointCount;
 	}
+	for ( int j : W->jointRows )
+		upload_joint_rows( W, j, j + 1 );
+	W->jointRows.clear();
+	if ( !W->islOn && W->awakeOrderDirty )
+	{
+		int n = (int)W->awakeOrder.size();
+		if ( n > 0 )
+			cudaMemcpyAsync( W->d.awakeOrder, W->awakeOrder.data(), sizeof( int ) * (size_t)n, cudaMemcpyHostToDevice,
+							 W->stream );
+		W->awakeOrderCount = n;
+		cudaMemcpyAsync( &W->d.sc->awakeOrderCount, &W->awakeOrderCount, sizeof( int ), cudaMemcpyHostToDevice,
+						 W->stream );
+		cudaStreamSynchronize( W->stream );
+		W->awakeOrderDirty = false;
+	}
 	for ( int j : W->jointDirty )
 	{
 		DWorld& d = W->d;
@@ -1120,7 +1156,7 @@ static void free_world( HostWorld* W )
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( beginEvF ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
 	F( sensorBeginEv ); F( sensorEndEv ); F( cbList ); F( cbReject ); F( cbManifold ); F( sc ); F( sortTemp ); F( newPoint ); F( newFeat ); F( samples );
-	F( shapeMove ); F( moveShape ); F( hostMoves ); F( newPairId );
+	F( shapeMove ); F( moveShape ); F( hostMoves ); F( newPairId ); F( cstamp ); F( awakeOrder ); F( apiEndEv );
 #undef F
 	for ( int t = 0; t < 3; ++t )
 		pt_free( d.pt[t] );
@@ -1189,6 +1225,32 @@ template <typename T> static void vset( std::vector<T>& v, int i, const T& x )
 	v[i] = x;
 }
 
+// The reference's creation asserts (body.c:180-187, shape.c:166-170, :379-382,
+// math_functions.c:10-59) as refusals: a definition they would stop on
+// creates nothing and the call returns 0.
+static bool valid_float( double v )
+{
+	return std::isfinite( (float)v );
+}
+
+static bool valid_body_def( const f2d_body_def* d )
+{
+	float c = (float)d->rotationCos, s = (float)d->rotationSin;
+	float qq = s * s + c * c;
+	return valid_float( d->positionX ) && valid_float( d->positionY ) && valid_float( c ) && valid_float( s ) &&
+		   1.0f - 0.0006f < qq && qq < 1.0f + 0.0006f && valid_float( d->linearVelocityX ) &&
+		   valid_float( d->linearVelocityY ) && valid_float( d->angularVelocity ) && valid_float( d->linearDamping ) &&
+		   d->linearDamping >= 0.0 && valid_float( d->angularDamping ) && d->angularDamping >= 0.0 &&
+		   valid_float( d->sleepThreshold ) && d->sleepThreshold >= 0.0 && valid_float( d->gravityScale ) &&
+		   d->type >= 0 && d->type <= 2;
+}
+
+static bool valid_material( double friction, double restitution, double rolling, double tangentSpeed )
+{
+	return valid_float( friction ) && friction >= 0.0 && valid_float( restitution ) && restitution >= 0.0 &&
+		   valid_float( rolling ) && rolling >= 0.0 && valid_float( tangentSpeed );
+}
+
 extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def* def, int32_t* index1,
 											int32_t* worldAndGeneration )
 {
@@ -1197,7 +1259,7 @@ extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def*
 	if ( worldAndGeneration )
 		*worldAndGeneration = 0;
 	HostWorld* W = world_from_id( worldId );
-	if ( W == nullptr || def == nullptr )
+	if ( W == nullptr || def == nullptr || !valid_body_def( def ) )
 		return 0;
 	int id;
 	if ( !W->bodyFree.empty() )
@@ -1252,7 +1314,16 @@ extern "C" F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def*
 	vset( W->bflags, id, flags );
 	vset( W->headShape, id, F2D_NULL );
 	vset( W->headJoint, id, F2D_NULL );
+	vset( W->headChain, id, F2D_NULL );
 	vset( W->jointCountB, id, 0 );
+	vset( W->awakeSlot, id, -1 );
+	if ( !W->islOn && type != 0 && def->isEnabled )
+	{
+		// body.c:225-260: a new non-static body joins the awake set's arrays
+		W->awakeSlot[id] = (int)W->awakeOrder.size();
+		W->awakeOrder.push_back( id );
+		W->awakeOrderDirty = true;
+	}
 	vset( W->bmass, id, 0.0f );
 	vset( W->binertia, id, 0.0f );
 	mark_body( W, id );
@@ -1372,6 +1443,9 @@ static int create_shape( HostWorld* W, int b, const f2d_shape_def* def, const HS
 		*index1 = 0;
 	if ( wg )
 		*wg = 0;
+	if ( def == nullptr || !valid_float( def->density ) || def->density < 0.0 ||
+		 !valid_material( def->friction, def->restitution, def->rollingResistance, def->tangentSpeed ) )
+		return 0;
 	pull_body( W, b );
 	int id;
 	if ( !W->shapeFree.empty() )
@@ -1524,6 +1598,12 @@ extern "C" F2D_API int32_t f2d_create_chain( int32_t bi, int32_t bwg, const doub
 	if ( b < 0 || points == nullptr || materials == nullptr || count < 4 || count > ( 1 << 20 ) ||
 		 ( materialCount != 1 && materialCount != count ) )
 		return 0;
+	for ( int i = 0; i < materialCount; ++i )
+	{
+		const double* m = materials + 6 * i;
+		if ( !valid_material( m[0], m[1], m[2], m[3] ) )
+			return 0;
+	}
 	int id;
 	if ( !W->chainFree.empty() )
 	{
@@ -1537,6 +1617,9 @@ extern "C" F2D_API int32_t f2d_create_chain( int32_t bi, int32_t bwg, const doub
 		W->chainGen.push_back( 0 );
 	}
 	W->chainGen[id] = (uint16_t)( W->chainGen[id] + 1 );
+	vset( W->chainBody, id, b );
+	vset( W->chainNext, id, W->headChain[b] );
+	W->headChain[b] = id;
 	std::vector<int>& segs = W->chainSegments[id];
 	segs.clear();
 	int n = isLoop ? count : count - 3;
@@ -1617,7 +1700,7 @@ extern "C" F2D_API int32_t f2d_create_box_shape( int32_t bi, int32_t bwg, const 
 {
 	HostWorld* W;
 	int b = body_from( bi, bwg, &W );
-	if ( b < 0 || def == nullptr )
+	if ( b < 0 || def == nullptr || !valid_float( radius ) || radius < 0.0 ) // shape.c:213
 		return 0;
 	HShapeGeom g = {};
 	g.type = ST_POLYGON;
@@ -1638,7 +1721,8 @@ extern "C" F2D_API int32_t f2d_create_polygon_shape( int32_t bi, int32_t bwg, co
 		*wg = 0;
 	HostWorld* W;
 	int b = body_from( bi, bwg, &W );
-	if ( b < 0 || def == nullptr || points == nullptr || count < 3 || count > F2D_MAX_POLY )
+	if ( b < 0 || def == nullptr || points == nullptr || count < 3 || count > F2D_MAX_POLY || !valid_float( radius ) ||
+		 radius < 0.0 ) // shape.c:213
 		return 0;
 	fv2 pts[F2D_MAX_POLY], hull[F2D_MAX_POLY];
 	for ( int i = 0; i < count; ++i )
@@ -1672,10 +1756,21 @@ extern "C" F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t wg )
 // ---------------------------------------------------------------------------
 // Shared tail of the joint constructors (joint.c:146-330): slot, generation,
 // body joint lists, definition rows, then the graph / island log.
+static void destroy_contacts_between( HostWorld* W, int a, int b );
+
 static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0, float4 d1, float4 d2,
 								int32_t* index1, int32_t* wg, float4 d3 = make_float4( 0.0f, 0.0f, 0.0f, 0.0f ) )
 {
-	int j = W->jointCount++;
+	int j;
+	if ( !W->jointFree.empty() )
+	{
+		j = W->jointFree.back();
+		W->jointFree.pop_back();
+		if ( j < W->jointUploaded )
+			W->jointRows.push_back( j );
+	}
+	else
+		j = W->jointCount++;
 	uint16_t gen = (uint16_t)( ( j < (int)W->jgen.size() ? W->jgen[j] : 0 ) + 1 );
 	vset( W->jgen, j, gen );
 	vset( W->jbody, j, make_int2( a, b ) );
@@ -1703,6 +1798,11 @@ static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0
 		W->islLog.push_back( ( 1 << 30 ) | j ); // set, colour and island at the next upload
 	else if ( !( staticA && staticB ) )
 		W->pendingJoints.push_back( j );
+	// joint.c:396-400 and the other constructors but the mouse and filter
+	// joints: contacts between bodies that may no longer collide go
+	int type = ( flags >> JF_TYPE_SHIFT ) & 0xf;
+	if ( ( flags & JF_COLLIDE ) == 0 && type != F2D_JOINT_MOUSE && type != F2D_JOINT_FILTER )
+		destroy_contacts_between( W, a, b );
 	if ( index1 )
 		*index1 = j + 1;
 	if ( wg )
@@ -1860,6 +1960,12 @@ extern "C" F2D_API int32_t f2d_create_joint( int32_t worldId, const f2d_joint_de
 	return create_joint_common( W, a, b, flags, d0, d1, d2, index1, wg, d3 );
 }
 
+// a live joint of generation wg (j below the joint count)
+static bool joint_live( const HostWorld* W, int j, int32_t wg )
+{
+	return ( W->jflags[j] & JF_USED ) != 0 && W->jgen[j] == ( ( wg >> 16 ) & 0xffff );
+}
+
 // an uploaded joint whose definition rows changed on the host (sent with the
 // next step)
 static void mark_joint_dirty( HostWorld* W, int j )
@@ -1883,7 +1989,7 @@ extern "C" F2D_API void f2d_joint_set_limits( int32_t index1, int32_t wg, int32_
 	if ( W == nullptr )
 		return;
 	int j = index1 - 1;
-	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) )
+	if ( j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
 		return;
 	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
 	if ( type != 0 && type != F2D_JOINT_PRISMATIC && type != F2D_JOINT_WHEEL )
@@ -1919,7 +2025,7 @@ extern "C" F2D_API void f2d_joint_get_constraint( int32_t index1, int32_t wg, fl
 	if ( W == nullptr )
 		return;
 	int j = index1 - 1;
-	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) || j >= W->jointUploaded )
+	if ( j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) || j >= W->jointUploaded )
 		return;
 	cudaStreamSynchronize( W->stream );
 	float4 imp, p3;
@@ -2002,7 +2108,7 @@ extern "C" F2D_API void f2d_joint_set_motor( int32_t index1, int32_t wg, int32_t
 	if ( W == nullptr )
 		return;
 	int j = index1 - 1;
-	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) )
+	if ( j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
 		return;
 	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
 	float4& d2 = W->jdef2[j];
@@ -2039,7 +2145,7 @@ extern "C" F2D_API void f2d_mouse_joint_set_target( int32_t index1, int32_t wg, 
 	if ( W == nullptr )
 		return;
 	int j = index1 - 1;
-	if ( j < 0 || j >= W->jointCount || W->jgen[j] != ( ( wg >> 16 ) & 0xffff ) ||
+	if ( j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) ||
 		 ( ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf ) != F2D_JOINT_MOUSE )
 		return;
 	W->jdef1[j].x = (float)x;
@@ -2053,7 +2159,373 @@ extern "C" F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t wg )
 	if ( W == nullptr )
 		return 0;
 	int j = index1 - 1;
-	return j >= 0 && j < W->jointCount && W->jgen[j] == ( ( wg >> 16 ) & 0xffff );
+	return j >= 0 && j < W->jointCount && ( W->jflags[j] & JF_USED ) && W->jgen[j] == ( ( wg >> 16 ) & 0xffff );
+}
+
+// ---------------------------------------------------------------------------
+// destroy path: b2DestroyBody (body.c:343-440), b2DestroyShape and
+// b2DestroyShapeInternal (shape.c:230-338), b2DestroyChain (:488-540),
+// b2DestroyJoint and b2DestroyJointInternal (joint.c:702-822),
+// b2DestroyContactsBetweenBodies (:313-351), b2DestroySensor
+// (sensor.c:353-380), b2BroadPhase_DestroyProxy (broad_phase.c:70-114).
+// The host keeps the id pools, the body shape, joint and chain lists, the
+// trees and the sensor list; the device takes contacts, joints and bodies out
+// of the constraint graph, the islands and the solver sets in the
+// reference's order (island.cu). Single fields go up as they change, so
+// device-side state (positions, sleep timers) is never overwritten.
+// ---------------------------------------------------------------------------
+static bool chain_live( const HostWorld* W, int c, int32_t wg )
+{
+	return c >= 0 && c < (int)W->chainSegments.size() && W->chainBody[c] >= 0 &&
+		   W->chainGen[c] == ( ( wg >> 16 ) & 0xffff );
+}
+
+// creations reach the device and the proxies buffered since the last step
+// join the move array (after the finalize moves, as b2BufferMove appends)
+static void destroy_begin( HostWorld* W )
+{
+	flush_uploads( W );
+	if ( !W->hostMoves.empty() )
+	{
+		upload_host_moves( W );
+		launch_pt_host_moves( W->d, W->s, W->stream );
+	}
+	cudaMemsetAsync( &W->d.sc->apiEndCount, 0, sizeof( int ), W->stream );
+	cudaMemsetAsync( &W->d.sc->apiCount, 0, sizeof( int ), W->stream );
+}
+
+// end events of the contacts destroyed since destroy_begin, with the shape
+// ids as they are now, for the next step's events
+static void destroy_end( HostWorld* W )
+{
+	cudaStreamSynchronize( W->stream );
+	int n = 0;
+	cudaMemcpy( &n, &W->d.sc->apiEndCount, sizeof( int ), cudaMemcpyDeviceToHost );
+	n = std::min( n, W->d.contactCap );
+	if ( n > 0 )
+	{
+		std::vector<int> ev( 2 * (size_t)n );
+		cudaMemcpy( ev.data(), W->d.apiEndEv, sizeof( int ) * 2 * (size_t)n, cudaMemcpyDeviceToHost );
+		for ( int i = 0; i < n; ++i )
+		{
+			int a = ev[2 * i], b = ev[2 * i + 1];
+			W->endNext.insert( W->endNext.end(),
+							   { a + 1, pack_wg( W, W->sgen[a] ), b + 1, pack_wg( W, W->sgen[b] ) } );
+		}
+	}
+	if ( W->islOn )
+		body_rows_changed( W, false ); // woken sets
+	W->forceRebuild = true;
+}
+
+// the joint key leaves body b's joint list (singly linked here)
+static void unlink_joint_key( HostWorld* W, int b, int key, int next )
+{
+	if ( W->headJoint[b] == key )
+	{
+		W->headJoint[b] = next;
+		up( W->d.headJoint, W->headJoint, b, b + 1, W->stream );
+		return;
+	}
+	for ( int cur = W->headJoint[b], g = 0; cur != F2D_NULL && g <= W->jointCount; ++g )
+	{
+		int slot = 2 * ( cur >> 1 ) + ( cur & 1 );
+		if ( W->jnext[slot] == key )
+		{
+			W->jnext[slot] = next;
+			up( W->d.jnext, W->jnext, slot, slot + 1, W->stream );
+			return;
+		}
+		cur = W->jnext[slot];
+	}
+}
+
+static void destroy_joint_host( HostWorld* W, int j, int wake )
+{
+	int2 jb = W->jbody[j];
+	int ids[2] = { jb.x, jb.y };
+	for ( int e = 0; e < 2; ++e )
+	{
+		int b = ids[e];
+		unlink_joint_key( W, b, ( j << 1 ) | e, W->jnext[2 * j + e] );
+		W->jointCountB[b] -= 1;
+		up( W->d.jointCountB, W->jointCountB, b, b + 1, W->stream );
+	}
+	launch_destroy_joint( W->d, W->stream, j, wake );
+	W->jflags[j] = 0;
+	W->jcolor[j] = F2D_NULL;
+	W->jointFree.push_back( j );
+}
+
+// broad_phase.c:105-114: out of the move array, then out of its tree
+static void destroy_proxy_host( HostWorld* W, int s )
+{
+	int pk = W->proxyKey[s];
+	if ( pk == F2D_NULL )
+		return;
+	launch_unbuffer_move( W->d, W->stream, s );
+	int t = pk & 3;
+	tree_pull( W, t );
+	W->trees[t].destroy_proxy( pk >> 2 );
+	W->treeDirty[t] = true;
+	if ( t == 0 )
+		W->staticDirty = true;
+	W->proxyKey[s] = F2D_NULL;
+	up( W->d.proxyKey, W->proxyKey, s, s + 1, W->stream );
+}
+
+// sensor.c:353-380: an end event per current visitor (the last step's
+// overlaps, visitor order), then the sensor leaves the sensor array by
+// swap-remove and the overlaps of the moved sensor follow it
+static void destroy_sensor_host( HostWorld* W, int s )
+{
+	std::vector<int>& S = W->sensorShapes;
+	int idx = -1;
+	for ( int i = 0; i < (int)S.size(); ++i )
+		if ( S[i] == s )
+			idx = i;
+	if ( idx < 0 )
+		return;
+	int last = (int)S.size() - 1;
+	DWorld& d = W->d;
+	if ( W->stepped && d.sensorCount > 0 && d.sensorPrevKeys )
+	{
+		cudaStreamSynchronize( W->stream );
+		int n = 0;
+		cudaMemcpy( &n, &d.sc->sensorPrev, sizeof( int ), cudaMemcpyDeviceToHost );
+		n = std::max( 0, std::min( n, d.sensorPairCap ) );
+		std::vector<unsigned long long> keys( (size_t)n ), kept;
+		if ( n > 0 )
+			cudaMemcpy( keys.data(), d.sensorPrevKeys, sizeof( unsigned long long ) * (size_t)n, cudaMemcpyDeviceToHost );
+		for ( unsigned long long k : keys )
+		{
+			int si = (int)( k >> 32 );
+			int v = (int)( k & 0xffffffffull );
+			if ( si == idx )
+			{
+				W->sensorEndNext.insert( W->sensorEndNext.end(),
+										 { s + 1, pack_wg( W, W->sgen[s] ), v + 1, pack_wg( W, W->sgen[v] ) } );
+				continue;
+			}
+			if ( si == last )
+				k = ( (unsigned long long)idx << 32 ) | (unsigned long long)(unsigned)v;
+			kept.push_back( k );
+		}
+		std::sort( kept.begin(), kept.end() );
+		if ( !kept.empty() )
+			cudaMemcpyAsync( d.sensorPrevKeys, kept.data(), sizeof( unsigned long long ) * kept.size(),
+							 cudaMemcpyHostToDevice, W->stream );
+		int m = (int)kept.size();
+		cudaMemcpyAsync( &d.sc->sensorPrev, &m, sizeof( int ), cudaMemcpyHostToDevice, W->stream );
+		cudaStreamSynchronize( W->stream );
+	}
+	S[idx] = S[last];
+	S.pop_back();
+	W->sensorsDirty = true;
+}
+
+static void free_shape_host( HostWorld* W, int s )
+{
+	W->sflags[s] = 0;
+	up( W->d.sflags, W->sflags, s, s + 1, W->stream );
+	W->shapeFree.push_back( s );
+}
+
+// shape.c:230-316: out of the body's shape list, proxy, contacts (the body's
+// contact list order), sensor, id
+static void destroy_shape_host( HostWorld* W, int s, int wake )
+{
+	int b = W->shapeBody[s];
+	if ( W->headShape[b] == s )
+	{
+		W->headShape[b] = W->nextShape[s];
+		up( W->d.headShape, W->headShape, b, b + 1, W->stream );
+	}
+	else
+		for ( int k = W->headShape[b]; k != F2D_NULL; k = W->nextShape[k] )
+			if ( W->nextShape[k] == s )
+			{
+				W->nextShape[k] = W->nextShape[s];
+				up( W->d.nextShape, W->nextShape, k, k + 1, W->stream );
+				break;
+			}
+	destroy_proxy_host( W, s );
+	launch_destroy_contacts_of( W->d, W->stream, b, s, -1, wake, W->s.tmpA );
+	if ( W->sflags[s] & SF_SENSOR )
+		destroy_sensor_host( W, s );
+	free_shape_host( W, s );
+}
+
+static void destroy_chain_host( HostWorld* W, int c )
+{
+	int b = W->chainBody[c];
+	if ( W->headChain[b] == c )
+		W->headChain[b] = W->chainNext[c];
+	else
+		for ( int k = W->headChain[b]; k != F2D_NULL; k = W->chainNext[k] )
+			if ( W->chainNext[k] == c )
+			{
+				W->chainNext[k] = W->chainNext[c];
+				break;
+			}
+	for ( int s : W->chainSegments[c] )
+		destroy_shape_host( W, s, 1 );
+	W->chainSegments[c].clear();
+	W->chainBody[c] = -1;
+	W->chainFree.push_back( c );
+}
+
+// body.c:343-440: joints, contacts, shapes (sensors, proxies, ids), chains,
+// island, solver set, id
+static void destroy_body_host( HostWorld* W, int b )
+{
+	for ( int key = W->headJoint[b], g = 0; key != F2D_NULL && g <= W->jointCount; ++g )
+	{
+		int j = key >> 1;
+		key = W->jnext[2 * j + ( key & 1 )];
+		destroy_joint_host( W, j, 1 );
+	}
+	launch_destroy_contacts_of( W->d, W->stream, b, -1, -1, 1, W->s.tmpA );
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		if ( W->sflags[s] & SF_SENSOR )
+			destroy_sensor_host( W, s );
+		destroy_proxy_host( W, s );
+		free_shape_host( W, s );
+	}
+	for ( int c = W->headChain[b]; c != F2D_NULL; c = W->chainNext[c] )
+	{
+		W->chainSegments[c].clear();
+		W->chainBody[c] = -1;
+		W->chainFree.push_back( c );
+	}
+	W->headChain[b] = F2D_NULL;
+	launch_destroy_body_records( W->d, W->stream, b );
+	if ( !W->islOn && W->awakeSlot[b] >= 0 )
+	{
+		int k = W->awakeSlot[b];
+		int m = W->awakeOrder.back();
+		W->awakeOrder[k] = m;
+		W->awakeSlot[m] = k;
+		W->awakeOrder.pop_back();
+		W->awakeSlot[b] = -1;
+		W->awakeOrderDirty = true;
+	}
+	W->bflags[b] = 0;
+	W->headShape[b] = F2D_NULL;
+	W->headJoint[b] = F2D_NULL;
+	W->jointCountB[b] = 0;
+	up( W->d.headShape, W->headShape, b, b + 1, W->stream );
+	up( W->d.headJoint, W->headJoint, b, b + 1, W->stream );
+	up( W->d.jointCountB, W->jointCountB, b, b + 1, W->stream );
+	W->bodyFree.push_back( b );
+}
+
+// RawBox2D.destroyBody (raw_box2d.dart:96) -> b2DestroyBody (body.c:343)
+extern "C" F2D_API void f2d_destroy_body( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	destroy_begin( W );
+	destroy_body_host( W, b );
+	destroy_end( W );
+}
+
+// RawBox2D.destroyShape (raw_box2d.dart:390) -> b2DestroyShape (shape.c:318)
+extern "C" F2D_API void f2d_destroy_shape( int32_t index1, int32_t wg, int32_t updateBodyMass )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return;
+	int b = W->shapeBody[s];
+	destroy_begin( W );
+	destroy_shape_host( W, s, 1 );
+	destroy_end( W );
+	if ( updateBodyMass )
+	{
+		pull_body( W, b );
+		update_mass( W, b );
+		mark_body( W, b );
+	}
+}
+
+// RawBox2D.destroyChain (raw_box2d.dart:550) -> b2DestroyChain (shape.c:488)
+extern "C" F2D_API void f2d_destroy_chain( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr || !chain_live( W, index1 - 1, wg ) )
+		return;
+	destroy_begin( W );
+	destroy_chain_host( W, index1 - 1 );
+	destroy_end( W );
+}
+
+// RawBox2D.destroyJoint (raw_box2d.dart:714) -> b2DestroyJoint (joint.c:808)
+extern "C" F2D_API void f2d_destroy_joint( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return;
+	destroy_begin( W );
+	destroy_joint_host( W, j, 1 );
+	destroy_end( W );
+}
+
+// joint.c:313-351 after a joint that keeps its bodies from colliding joined
+// the graph: their contacts go, without waking (both contact lists hold the
+// shared contacts in the same relative order, newest first)
+static void destroy_contacts_between( HostWorld* W, int a, int b )
+{
+	if ( !W->stepped )
+		return; // contacts exist only after a step
+	destroy_begin( W );
+	launch_destroy_contacts_of( W->d, W->stream, a, -1, b, 0, W->s.tmpA );
+	destroy_end( W );
+}
+
+// RawBox2D.jointSetCollideConnected (b2Joint_SetCollideConnected,
+// joint.c:980-1022): allowing collision buffers the proxies of the body with
+// fewer shapes; forbidding it destroys the contacts between the bodies
+extern "C" F2D_API void f2d_joint_set_collide_connected( int32_t index1, int32_t wg, int32_t flag )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return;
+	bool on = flag != 0;
+	if ( ( ( W->jflags[j] & JF_COLLIDE ) != 0 ) == on )
+		return;
+	W->jflags[j] = on ? ( W->jflags[j] | JF_COLLIDE ) : ( W->jflags[j] & ~JF_COLLIDE );
+	mark_joint_dirty( W, j );
+	int2 jb = W->jbody[j];
+	if ( on )
+	{
+		auto count = [&]( int body ) {
+			int n = 0;
+			for ( int s = W->headShape[body]; s != F2D_NULL; s = W->nextShape[s] )
+				n += 1;
+			return n;
+		};
+		int body = count( jb.x ) < count( jb.y ) ? jb.x : jb.y;
+		for ( int s = W->headShape[body]; s != F2D_NULL; s = W->nextShape[s] )
+			if ( W->proxyKey[s] != F2D_NULL )
+				host_move( W, s );
+	}
+	else
+		destroy_contacts_between( W, jb.x, jb.y );
+}
+
+extern "C" F2D_API int32_t f2d_joint_get_collide_connected( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return 0;
+	return ( W->jflags[j] & JF_COLLIDE ) != 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -2257,8 +2729,18 @@ extern "C" F2D_API int32_t f2d_world_step( int32_t worldId, double timeStep, int
 	if ( W == nullptr )
 		return F2D_STATUS_INVALID;
 	float dt = (float)timeStep;
+	// world.c:717-725, :808-810: the end events of destroys since the last
+	// step are reported with this one; a zero step reports only those
+	W->endPrefix.swap( W->endNext );
+	W->endNext.clear();
+	W->sensorEndPrefix.swap( W->sensorEndNext );
+	W->sensorEndNext.clear();
 	if ( dt == 0.0f )
+	{
+		W->eventsCleared = true;
 		return 0;
+	}
+	W->eventsCleared = false;
 	int subSteps = subStepCount < 1 ? 1 : subStepCount;
 	float inv_dt = 1.0f / dt;
 	W->invH = (float)subSteps * inv_dt;
@@ -3276,19 +3758,20 @@ extern "C" F2D_API void f2d_world_get_event_counts( int32_t worldId, int32_t* co
 	cudaStreamSynchronize( W->stream );
 	DScalars sc;
 	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
+	int prefix = (int)W->endPrefix.size() / 4;
+	if ( W->eventsCleared )
+	{
+		counts4[1] = prefix;
+		return;
+	}
 	counts4[0] = sc.beginCount;
-	counts4[1] = sc.endCount;
+	counts4[1] = prefix + sc.endCount;
 	counts4[2] = std::min( sc.hitCount, W->d.eventCap );
 	int moved = 0;
 	if ( W->islOn && W->islDev )
 		cudaMemcpy( &moved, &W->islDev->moveCount, sizeof( int ), cudaMemcpyDeviceToHost );
 	else
-		for ( int b = 0; b < W->bodyCount; ++b )
-		{
-			int f = W->bflags[b];
-			if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
-				moved += 1;
-		}
+		moved = (int)W->awakeOrder.size();
 	counts4[3] = moved;
 }
 
@@ -3319,15 +3802,22 @@ extern "C" F2D_API int32_t f2d_world_get_sensor_events( int32_t worldId, int32_t
 	if ( endCount )
 		*endCount = 0;
 	HostWorld* W = world_from_id( worldId );
-	if ( W == nullptr || !W->stepped || W->d.sensorCount == 0 )
+	if ( W == nullptr || !W->stepped )
+		return 0;
+	// end events of sensors destroyed before the step come first
+	int prefix = std::min( (int)W->sensorEndPrefix.size() / 4, (int)cap );
+	std::copy( W->sensorEndPrefix.begin(), W->sensorEndPrefix.begin() + 4 * (size_t)prefix, end4 );
+	if ( endCount )
+		*endCount = prefix;
+	if ( W->d.sensorCount == 0 || W->eventsCleared )
 		return 0;
 	cudaStreamSynchronize( W->stream );
 	DScalars sc;
 	cudaMemcpy( &sc, W->d.sc, sizeof( sc ), cudaMemcpyDeviceToHost );
 	int nb = read_pairs( W, (const int*)W->d.sensorBeginEv, sc.sensorBegin, begin4, cap );
-	int ne = read_pairs( W, (const int*)W->d.sensorEndEv, sc.sensorEnd, end4, cap );
+	int ne = read_pairs( W, (const int*)W->d.sensorEndEv, sc.sensorEnd, end4 + 4 * (size_t)prefix, cap - prefix );
 	if ( endCount )
-		*endCount = ne;
+		*endCount = prefix + ne;
 	return nb;
 }
 
@@ -3364,7 +3854,10 @@ extern "C" F2D_API int32_t f2d_world_get_end_events( int32_t worldId, int32_t* o
 		return 0;
 	int c[4];
 	f2d_world_get_event_counts( worldId, c );
-	return read_pairs( W, W->d.endEv, c[1], out4, cap );
+	int prefix = std::min( (int)W->endPrefix.size() / 4, (int)cap );
+	std::copy( W->endPrefix.begin(), W->endPrefix.begin() + 4 * (size_t)prefix, out4 );
+	return prefix + read_pairs( W, W->d.endEv, c[1] - (int)W->endPrefix.size() / 4, out4 + 4 * (size_t)prefix,
+								cap - prefix );
 }
 
 extern "C" F2D_API int32_t f2d_world_get_hit_events( int32_t worldId, int32_t* ints4, float* floats5, int32_t cap )
@@ -3383,7 +3876,7 @@ extern "C" F2D_API int32_t f2d_world_get_hit_events( int32_t worldId, int32_t* i
 extern "C" F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* ints3, float* floats4, int32_t cap )
 {
 	HostWorld* W = world_from_id( worldId );
-	if ( W == nullptr || !W->stepped )
+	if ( W == nullptr || !W->stepped || W->eventsCleared )
 		return 0;
 	cudaStreamSynchronize( W->stream );
 	int n = W->bodyCount;
@@ -3415,12 +3908,12 @@ extern "C" F2D_API int32_t f2d_world_get_body_events( int32_t worldId, int32_t* 
 		}
 		return count;
 	}
+	// the awake set's order (solver.c:603-611)
 	int m = 0;
-	for ( int b = 0; b < n && m < cap; ++b )
+	for ( int b : W->awakeOrder )
 	{
-		int f = W->bflags[b];
-		if ( !( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 ) )
-			continue;
+		if ( m >= cap )
+			break;
 		ints3[3 * m + 0] = b + 1;
 		ints3[3 * m + 1] = pack_wg( W, W->bgen[b] );
 		ints3[3 * m + 2] = 0;
@@ -3477,12 +3970,7 @@ extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )
 	if ( W->islOn && W->islDev )
 		cudaMemcpy( &awake, &W->islDev->awakeBodyCount, sizeof( int ), cudaMemcpyDeviceToHost );
 	else
-		for ( int b = 0; b < W->bodyCount; ++b )
-		{
-			int f = W->bflags[b];
-			if ( ( f & BF_USED ) && ( f & BF_ENABLED ) && body_type( f ) != 0 )
-				awake += 1;
-		}
+		awake = (int)W->awakeOrder.size();
 	int active = 0;
 	for ( int c = 0; c < 11; ++c )
 		active += sc.colorCount[c] > 0 ? 1 : 0;
@@ -3492,8 +3980,8 @@ extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )
 	out8[3] = sc.overflowCount;
 	out8[4] = active;
 	out8[5] = sc.colorRounds;
-	out8[6] = W->shapeCount;
-	out8[7] = W->jointCount;
+	out8[6] = W->shapeCount - (int)W->shapeFree.size();
+	out8[7] = W->jointCount - (int)W->jointFree.size();
 }
 
 // ---------------------------------------------------------------------------

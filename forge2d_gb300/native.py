@@ -135,6 +135,12 @@ _SIGS = [
     ("f2d_world_is_continuous_enabled", _i, [_i]),
     ("f2d_create_body", _i, [_i, _P(BodyDef), _P(_i), _P(_i)]),
     ("f2d_body_is_valid", _i, [_i, _i]),
+    ("f2d_destroy_body", None, [_i, _i]),
+    ("f2d_destroy_shape", None, [_i, _i, _i]),
+    ("f2d_destroy_chain", None, [_i, _i]),
+    ("f2d_destroy_joint", None, [_i, _i]),
+    ("f2d_joint_set_collide_connected", None, [_i, _i, _i]),
+    ("f2d_joint_get_collide_connected", _i, [_i, _i]),
     ("f2d_body_get_position", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_get_rotation", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_set_transform", None, [_i, _i, _d, _d, _d, _d]),

@@ -47,7 +47,8 @@ class GpuWorld:
         wd = dict(WORLD_DEFAULTS)
         if world_def:
             wd.update(world_def)
-        self._body_ids = []
+        # current generation per index of each id kind (ids are reused)
+        self._wg = {"body": {}, "shape": {}, "joint": {}, "chain": {}}
         self.id = self.lib.f2d_create_world(C.byref(_fill(native.WorldDef(), wd)))
         if self.id == 0:
             raise RuntimeError("f2d_create_world failed (no CUDA device?)")
@@ -74,11 +75,38 @@ class GpuWorld:
         i1, wg = C.c_int32(0), C.c_int32(0)
         if not self.lib.f2d_create_body(self.id, C.byref(_fill(native.BodyDef(), bd)), C.byref(i1), C.byref(wg)):
             raise RuntimeError("createBody failed")
-        self._body_ids.append((i1.value, wg.value))
+        self._wg["body"][i1.value - 1] = wg.value
         return (i1.value, wg.value)
 
+    def _id(self, kind, x):
+        """(index1, worldAndGeneration) of a handle or of a 0-based index."""
+        if isinstance(x, (int, np.integer)):
+            return (int(x) + 1, self._wg[kind][int(x)])
+        return x
+
     def _body(self, body):
-        return self._body_ids[body] if isinstance(body, int) else body
+        return self._id("body", body)
+
+    # destroy path ------------------------------------------------------
+    def destroy_body(self, body):
+        b = self._body(body)
+        self.lib.f2d_destroy_body(b[0], b[1])
+
+    def destroy_shape(self, shape, update_mass=True):
+        s = self._id("shape", shape)
+        self.lib.f2d_destroy_shape(s[0], s[1], int(update_mass))
+
+    def destroy_joint(self, joint):
+        j = self._id("joint", joint)
+        self.lib.f2d_destroy_joint(j[0], j[1])
+
+    def destroy_chain(self, chain):
+        c = self._id("chain", chain)
+        self.lib.f2d_destroy_chain(c[0], c[1])
+
+    def set_collide_connected(self, joint, flag):
+        j = self._id("joint", joint)
+        self.lib.f2d_joint_set_collide_connected(j[0], j[1], int(flag))
 
     # sleeping ---------------------------------------------------------
     def set_awake(self, body, awake):
@@ -101,8 +129,11 @@ class GpuWorld:
         d.update(sd)
         return C.byref(_fill(native.ShapeDef(), d))
 
-    def _ret(self, ok, i1, wg):
-        return (i1.value, wg.value) if ok else -1
+    def _ret(self, ok, i1, wg, kind="shape"):
+        if not ok:
+            return -1
+        self._wg[kind][i1.value - 1] = wg.value
+        return (i1.value, wg.value)
 
     def create_circle(self, body, sd, cx, cy, r):
         i1, wg = C.c_int32(0), C.c_int32(0)
@@ -138,13 +169,13 @@ class GpuWorld:
     def create_revolute(self, jd: dict):
         d = dict(REVOLUTE_DEFAULTS)
         d.update(jd)
-        a, b = d.pop("bodyA"), d.pop("bodyB")
+        a, b = self._body(d.pop("bodyA")), self._body(d.pop("bodyB"))
         rd = _fill(native.RevoluteDef(), d)
         rd.bodyAIndex1, rd.bodyAWorldAndGeneration = a
         rd.bodyBIndex1, rd.bodyBWorldAndGeneration = b
         i1, wg = C.c_int32(0), C.c_int32(0)
         ok = self.lib.f2d_create_revolute_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
-        return self._ret(ok, i1, wg)
+        return self._ret(ok, i1, wg, "joint")
 
     def create_chain(self, body, points, materials=((0.6, 0.0, 0.0, 0.0, 0, 0),), categoryBits=1, maskBits=-1,
                      groupIndex=0, isLoop=False, enableSensorEvents=False):
@@ -157,7 +188,7 @@ class GpuWorld:
                                        mats.ctypes.data_as(C.POINTER(C.c_double)), len(mats) // 6, categoryBits,
                                        maskBits, groupIndex, int(isLoop), int(enableSensorEvents),
                                        C.byref(i1), C.byref(wg))
-        return self._ret(ok, i1, wg)
+        return self._ret(ok, i1, wg, "chain")
 
     def cast_ray(self, ox, oy, tx, ty, fn, cat=1, mask=-1):
         """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float,
@@ -208,13 +239,13 @@ class GpuWorld:
         """Weld (type 2) or distance (type 3) joint from an f2d_joint_def dict."""
         d = dict(JOINT_DEFAULTS)
         d.update(jd)
-        a, b = d.pop("bodyA"), d.pop("bodyB")
+        a, b = self._body(d.pop("bodyA")), self._body(d.pop("bodyB"))
         rd = _fill(native.JointDef(), d)
         rd.bodyAIndex1, rd.bodyAWorldAndGeneration = a
         rd.bodyBIndex1, rd.bodyBWorldAndGeneration = b
         i1, wg = C.c_int32(0), C.c_int32(0)
         ok = self.lib.f2d_create_joint(self.id, C.byref(rd), C.byref(i1), C.byref(wg))
-        return self._ret(ok, i1, wg)
+        return self._ret(ok, i1, wg, "joint")
 
     def joint_constraint(self, joint):
         """(force.x, force.y, torque) of the last step."""

@@ -212,6 +212,13 @@ F2D_API int32_t f2d_world_subworld_count( int32_t worldId );
 /* RawBox2D.createBody (raw_box2d.dart:71; raw_box2d_ffi.dart:135 -> b2CreateBody). */
 F2D_API int32_t f2d_create_body( int32_t worldId, const f2d_body_def* def, int32_t* index1,
 								 int32_t* worldAndGeneration );
+/* RawBox2D.destroyBody (raw_box2d.dart:96 -> b2DestroyBody, body.c:343):
+ * its joints (waking their bodies), its contacts (waking touching pairs),
+ * its shapes with their sensors and proxies, its chains, its island and
+ * solver-set records; ids go back to LIFO pools and keep their generation.
+ * End events of destroyed touching contacts (and of destroyed sensors'
+ * visitors) are reported with the next step's, ahead of its own. */
+F2D_API void f2d_destroy_body( int32_t index1, int32_t worldAndGeneration );
 /* RawBox2D.bodyIsValid (raw_box2d.dart:99 -> b2Body_IsValid). */
 F2D_API int32_t f2d_body_is_valid( int32_t index1, int32_t worldAndGeneration );
 /* RawBox2D.bodyGetPosition / bodyGetRotation (raw_box2d.dart:102-106). */
@@ -300,6 +307,13 @@ F2D_API int32_t f2d_create_chain( int32_t bodyIndex1, int32_t bodyWorldAndGenera
  * (index1, worldAndGeneration) in creation order; returns the count. */
 F2D_API int32_t f2d_chain_get_segments( int32_t index1, int32_t worldAndGeneration, int32_t* out2,
 										int32_t capacity );
+/* RawBox2D.destroyShape (raw_box2d.dart:390 -> b2DestroyShape, shape.c:318):
+ * proxy, contacts (waking), sensor; the body's mass is recomputed when
+ * updateBodyMass is non-zero. */
+F2D_API void f2d_destroy_shape( int32_t index1, int32_t worldAndGeneration, int32_t updateBodyMass );
+/* RawBox2D.destroyChain (raw_box2d.dart:550 -> b2DestroyChain, shape.c:488):
+ * every segment shape in creation order, then the chain id. */
+F2D_API void f2d_destroy_chain( int32_t index1, int32_t worldAndGeneration );
 /* RawBox2D.shapeIsValid / shapeGetType (raw_box2d.dart:397-400). */
 F2D_API int32_t f2d_shape_is_valid( int32_t index1, int32_t worldAndGeneration );
 F2D_API int32_t f2d_shape_get_type( int32_t index1, int32_t worldAndGeneration );
@@ -333,6 +347,17 @@ F2D_API void f2d_joint_set_limits( int32_t index1, int32_t worldAndGeneration, i
 F2D_API int32_t f2d_create_revolute_joint( int32_t worldId, const f2d_revolute_def* def, int32_t* index1,
 										   int32_t* worldAndGeneration );
 F2D_API int32_t f2d_joint_is_valid( int32_t index1, int32_t worldAndGeneration );
+/* RawBox2D.destroyJoint (raw_box2d.dart:714 -> b2DestroyJoint, joint.c:808):
+ * out of the graph, island and solver set; wakes its bodies. A joint created
+ * with collideConnected false (all types but mouse and filter) destroys the
+ * contacts between its bodies, without waking (joint.c:313-351). */
+F2D_API void f2d_destroy_joint( int32_t index1, int32_t worldAndGeneration );
+/* RawBox2D.jointSetCollideConnected / jointGetCollideConnected
+ * (raw_box2d.dart:738 / :735 -> b2Joint_SetCollideConnected, joint.c:980-1022): allowing collision
+ * buffers the proxies of the body with fewer shapes for the next pair
+ * search; forbidding it destroys the contacts between the bodies. */
+F2D_API void f2d_joint_set_collide_connected( int32_t index1, int32_t worldAndGeneration, int32_t flag );
+F2D_API int32_t f2d_joint_get_collide_connected( int32_t index1, int32_t worldAndGeneration );
 
 /* ---- events (RawBox2D.worldGetContactEvents / worldGetBodyEvents,
  *      raw_box2d_ffi.dart:2172 and :2259) ----------------------------------
