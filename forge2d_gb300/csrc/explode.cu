@@ -214,3 +214,55 @@ void launch_explode( DWorld& w, cudaStream_t st, int* hit, unsigned long long ma
 		launch_isl_wake_marked( w, st, hit, w.shapeCount );
 	k_explode_apply<<<grid_for( w.bodyCount ), 128, 0, st>>>( w, bl, hit );
 }
+
+// b2Shape_TestPoint (shape.c:979-1001, geometry.c:456-502): the point in the
+// body frame against the circle, the capsule's segment or, by GJK distance
+// without radii, the polygon's core within its radius
+__global__ void k_shape_test_point( DWorld w, int s, fv2 point, int* out )
+{
+	int type = shape_type( w.sflags[s] );
+	fxf xf = body_xform( w, w.shapeBody[s] );
+	fv2 lp = rinvrot( xf.q, vsub( point, xf.p ) );
+	const float4* g = w.geom + (size_t)s * GEOM_F4;
+	float4 g0 = g[0], g1 = g[1];
+	int r = 0;
+	if ( type == ST_CIRCLE )
+		r = vdist2( lp, mk( g0.x, g0.y ) ) <= g1.x * g1.x;
+	else if ( type == ST_CAPSULE )
+	{
+		float rr = g1.x * g1.x;
+		fv2 p1 = mk( g0.x, g0.y ), p2 = mk( g0.z, g0.w );
+		fv2 d = vsub( p2, p1 );
+		float dd = vdot( d, d );
+		if ( dd == 0.0f )
+			r = vdist2( lp, p1 ) <= rr;
+		else
+		{
+			float t = fclamp_s( vdot( vsub( lp, p1 ), d ) / dd, 0.0f, 1.0f );
+			r = vdist2( lp, vmuladd( p1, t, d ) ) <= rr;
+		}
+	}
+	else if ( type == ST_POLYGON )
+	{
+		DProxy pa = blast_proxy( g, ST_POLYGON );
+		pa.radius = 0.0f;
+		DProxy pb;
+		pb.p[0] = lp;
+		pb.count = 1;
+		pb.radius = 0.0f;
+		fxf identity;
+		identity.p = mk( 0.0f, 0.0f );
+		identity.q.c = 1.0f;
+		identity.q.s = 0.0f;
+		DCache cache;
+		cache.count = 0;
+		fv2 pA, pB, n;
+		r = gjk_distance( pa, pb, identity, identity, cache, &pA, &pB, &n ) <= g1.x;
+	}
+	*out = r;
+}
+
+void launch_shape_test_point( DWorld& w, cudaStream_t st, int shape, float x, float y, int* out )
+{
+	k_shape_test_point<<<1, 1, 0, st>>>( w, shape, mk( x, y ), out );
+}

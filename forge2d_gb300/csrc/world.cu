@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 void launch_reset_counters( DWorld& w, cudaStream_t st );
@@ -66,6 +67,7 @@ struct HostWorld
 	std::vector<uint16_t> bgen;
 	std::vector<float> bmass, binertia;
 	std::vector<int> bodyFree;
+	std::vector<std::string> bname; // b2Body_SetName (host only)
 	int bodyCount = 0, bodyUploaded = 0;
 	std::vector<int> bodyDirty;
 	std::vector<uint8_t> bodyIsDirty; // host row newer than the device row
@@ -2526,6 +2528,847 @@ extern "C" F2D_API int32_t f2d_joint_get_collide_connected( int32_t index1, int3
 	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
 		return 0;
 	return ( W->jflags[j] & JF_COLLIDE ) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// properties: the RawBox2D getters and setters without a call of their own
+// (bodies raw_box2d.dart:198-319, shapes :403-527, chains :553-569, joints
+// :717-1285). Values the device changes (flags with dynamic bits, joint
+// impulses) are edited in place on the stream; host-owned rows go up as
+// single fields, so nothing the device keeps is overwritten.
+// ---------------------------------------------------------------------------
+__global__ void k_edit_bits( int* a, int i, int set, int clear )
+{
+	a[i] = ( a[i] & ~clear ) | set;
+}
+
+static void edit_body_bits( HostWorld* W, int b, int set, int clear )
+{
+	W->bflags[b] = ( W->bflags[b] & ~clear ) | set;
+	if ( b < W->bodyUploaded )
+		k_edit_bits<<<1, 1, 0, W->stream>>>( W->d.bflags, b, set, clear );
+}
+
+static void edit_shape_bits( HostWorld* W, int s, int set, int clear )
+{
+	W->sflags[s] = ( W->sflags[s] & ~clear ) | set;
+	if ( s < W->shapeUploaded )
+		k_edit_bits<<<1, 1, 0, W->stream>>>( W->d.sflags, s, set, clear );
+}
+
+static fxf body_xf( HostWorld* W, int b )
+{
+	pull_body( W, b );
+	float4 x = W->xf[b];
+	fxf t;
+	t.p = mk( x.x, x.y );
+	t.q.c = x.z;
+	t.q.s = x.w;
+	return t;
+}
+
+extern "C" F2D_API double f2d_body_get_param( int32_t index1, int32_t wg, int32_t code )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return 0.0;
+	pull_body( W, b );
+	int f = W->bflags[b];
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING:
+			return W->damp[b].x;
+		case F2D_BODY_ANGULAR_DAMPING:
+			return W->damp[b].y;
+		case F2D_BODY_GRAVITY_SCALE:
+			return W->damp[b].z;
+		case F2D_BODY_BULLET:
+			return ( f & BF_BULLET ) != 0;
+		case F2D_BODY_FIXED_ROTATION:
+			return ( f & BF_FIXED_ROT ) != 0;
+		case F2D_BODY_ENABLED:
+			return ( f & BF_ENABLED ) != 0;
+		case F2D_BODY_TYPE:
+			return body_type( f );
+		case F2D_BODY_LOCAL_CENTER_X:
+			return W->localCenter[b].x;
+		case F2D_BODY_LOCAL_CENTER_Y:
+			return W->localCenter[b].y;
+		case F2D_BODY_WORLD_CENTER_X:
+			return W->center[b].x;
+		case F2D_BODY_WORLD_CENTER_Y:
+			return W->center[b].y;
+		default:
+			return 0.0;
+	}
+}
+
+// body.c:1412-1480 (damping, gravity scale: the value only), :1560-1580
+// (bullet), :1536-1558 (fixed rotation: angular velocity cleared, mass
+// recomputed)
+extern "C" F2D_API void f2d_body_set_param( int32_t index1, int32_t wg, int32_t code, double value )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	float v = (float)value;
+	auto damp = [&]( int k ) {
+		float4& d = W->damp[b];
+		( k == 0 ? d.x : k == 1 ? d.y : d.z ) = v;
+		if ( b < W->bodyUploaded )
+			up( W->d.damp, W->damp, b, b + 1, W->stream );
+	};
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING:
+			if ( valid_float( value ) && value >= 0.0 )
+				damp( 0 );
+			break;
+		case F2D_BODY_ANGULAR_DAMPING:
+			if ( valid_float( value ) && value >= 0.0 )
+				damp( 1 );
+			break;
+		case F2D_BODY_GRAVITY_SCALE:
+			if ( valid_float( value ) )
+				damp( 2 );
+			break;
+		case F2D_BODY_BULLET:
+			edit_body_bits( W, b, value != 0.0 ? BF_BULLET : 0, value != 0.0 ? 0 : BF_BULLET );
+			break;
+		case F2D_BODY_FIXED_ROTATION:
+		{
+			bool on = value != 0.0;
+			if ( ( ( W->bflags[b] & BF_FIXED_ROT ) != 0 ) == on )
+				break;
+			pull_body( W, b );
+			W->bflags[b] = on ? ( W->bflags[b] | BF_FIXED_ROT ) : ( W->bflags[b] & ~BF_FIXED_ROT );
+			W->vel[b].z = 0.0f;
+			update_mass( W, b );
+			mark_body( W, b );
+			break;
+		}
+		default:
+			break;
+	}
+}
+
+extern "C" F2D_API void f2d_body_get_world_point( int32_t index1, int32_t wg, double x, double y, double* ox,
+												  double* oy )
+{
+	*ox = *oy = 0.0;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	fv2 p = xpoint( body_xf( W, b ), mk( (float)x, (float)y ) );
+	*ox = p.x;
+	*oy = p.y;
+}
+
+extern "C" F2D_API void f2d_body_get_local_point( int32_t index1, int32_t wg, double x, double y, double* ox,
+												  double* oy )
+{
+	*ox = *oy = 0.0;
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	fxf t = body_xf( W, b );
+	fv2 p = rinvrot( t.q, vsub( mk( (float)x, (float)y ), t.p ) );
+	*ox = p.x;
+	*oy = p.y;
+}
+
+// body.c:1357-1381: mass, inertia and local centre as given (extents kept)
+extern "C" F2D_API void f2d_body_set_mass_data( int32_t index1, int32_t wg, double mass, double rotationalInertia,
+												double centerX, double centerY )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || !valid_float( mass ) || mass < 0.0 || !valid_float( rotationalInertia ) || rotationalInertia < 0.0 ||
+		 !valid_float( centerX ) || !valid_float( centerY ) )
+		return;
+	fxf t = body_xf( W, b );
+	float m = (float)mass, I = (float)rotationalInertia;
+	fv2 lc = mk( (float)centerX, (float)centerY );
+	fv2 c = xpoint( t, lc );
+	W->bmass[b] = m;
+	W->binertia[b] = I;
+	W->localCenter[b] = make_float2( lc.x, lc.y );
+	W->center[b] = make_float2( c.x, c.y );
+	float4 s0 = W->sweep0[b];
+	W->sweep0[b] = make_float4( c.x, c.y, s0.z, s0.w );
+	float4 mv = W->massv[b];
+	W->massv[b] = make_float4( m > 0.0f ? 1.0f / m : 0.0f, I > 0.0f ? 1.0f / I : 0.0f, mv.z, mv.w );
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_apply_mass_from_shapes( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	update_mass( W, b );
+	mark_body( W, b );
+}
+
+extern "C" F2D_API void f2d_body_set_name( int32_t index1, int32_t wg, const char* name )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	if ( (int)W->bname.size() <= b )
+		W->bname.resize( (size_t)b + 1 );
+	std::string& n = W->bname[b];
+	n.clear();
+	if ( name != nullptr )
+		for ( int i = 0; i < 31 && name[i] != 0; ++i )
+			n.push_back( name[i] );
+}
+
+extern "C" F2D_API int32_t f2d_body_get_name( int32_t index1, int32_t wg, char* out, int32_t capacity )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( out && capacity > 0 )
+		out[0] = 0;
+	if ( b < 0 || b >= (int)W->bname.size() )
+		return 0;
+	const std::string& n = W->bname[b];
+	if ( out && capacity > 0 )
+	{
+		int k = std::min( (int)n.size(), capacity - 1 );
+		memcpy( out, n.data(), (size_t)k );
+		out[k] = 0;
+	}
+	return (int32_t)n.size();
+}
+
+extern "C" F2D_API int32_t f2d_body_get_shapes( int32_t index1, int32_t wg, int32_t* out2, int32_t capacity )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return 0;
+	int n = 0;
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s], ++n )
+		if ( out2 && n < capacity )
+		{
+			out2[2 * n] = s + 1;
+			out2[2 * n + 1] = pack_wg( W, W->sgen[s] );
+		}
+	return n;
+}
+
+extern "C" F2D_API int32_t f2d_body_get_joints( int32_t index1, int32_t wg, int32_t* out2, int32_t capacity )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return 0;
+	int n = 0;
+	for ( int key = W->headJoint[b]; key != F2D_NULL && n <= W->jointCount; key = W->jnext[2 * ( key >> 1 ) + ( key & 1 )], ++n )
+		if ( out2 && n < capacity )
+		{
+			int j = key >> 1;
+			out2[2 * n] = j + 1;
+			out2[2 * n + 1] = pack_wg( W, W->jgen[j] );
+		}
+	return n;
+}
+
+extern "C" F2D_API double f2d_shape_get_param( int32_t index1, int32_t wg, int32_t code )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return 0.0;
+	int f = W->sflags[s];
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY:
+			return W->density[s];
+		case F2D_SHAPE_FRICTION:
+			return W->mat[s].x;
+		case F2D_SHAPE_RESTITUTION:
+			return W->mat[s].y;
+		case F2D_SHAPE_SENSOR:
+			return ( f & SF_SENSOR ) != 0;
+		case F2D_SHAPE_SENSOR_EVENTS:
+			return ( f & SF_SENSOR_EVENTS ) != 0;
+		case F2D_SHAPE_CONTACT_EVENTS:
+			return ( f & SF_CONTACT_EVENTS ) != 0;
+		case F2D_SHAPE_HIT_EVENTS:
+			return ( f & SF_HIT_EVENTS ) != 0;
+		case F2D_SHAPE_PRESOLVE_EVENTS:
+			return ( f & SF_PRESOLVE ) != 0;
+		case F2D_SHAPE_CATEGORY:
+			return (double)(int64_t)W->cat[s];
+		case F2D_SHAPE_MASK:
+			return (double)(int64_t)W->mask[s];
+		case F2D_SHAPE_GROUP:
+			return W->group[s];
+		default:
+			return 0.0;
+	}
+}
+
+// shape.c:1057-1183: density (mass recomputed on request), friction and
+// restitution (mixed into the contacts at their next update), event flags
+// (read when contacts are created, hit and sensor flags every step)
+static void shape_set( HostWorld* W, int s, int code, double value, int flag )
+{
+	float v = (float)value;
+	int bit = code == F2D_SHAPE_SENSOR_EVENTS	 ? SF_SENSOR_EVENTS
+			  : code == F2D_SHAPE_CONTACT_EVENTS ? SF_CONTACT_EVENTS
+			  : code == F2D_SHAPE_HIT_EVENTS	 ? SF_HIT_EVENTS
+			  : code == F2D_SHAPE_PRESOLVE_EVENTS ? SF_PRESOLVE
+												  : 0;
+	if ( bit )
+	{
+		edit_shape_bits( W, s, value != 0.0 ? bit : 0, value != 0.0 ? 0 : bit );
+		return;
+	}
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY:
+		{
+			if ( !valid_float( value ) || value < 0.0 || v == W->density[s] )
+				return;
+			W->density[s] = v;
+			if ( flag )
+			{
+				int b = W->shapeBody[s];
+				pull_body( W, b );
+				update_mass( W, b );
+				mark_body( W, b );
+			}
+			return;
+		}
+		case F2D_SHAPE_FRICTION:
+		case F2D_SHAPE_RESTITUTION:
+			if ( !valid_float( value ) || value < 0.0 )
+				return;
+			( code == F2D_SHAPE_FRICTION ? W->mat[s].x : W->mat[s].y ) = v;
+			if ( s < W->shapeUploaded )
+				up( W->d.mat, W->mat, s, s + 1, W->stream );
+			return;
+		default:
+			return;
+	}
+}
+
+extern "C" F2D_API void f2d_shape_set_param( int32_t index1, int32_t wg, int32_t code, double value, int32_t flag )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s >= 0 )
+		shape_set( W, s, code, value, flag );
+}
+
+extern "C" F2D_API int32_t f2d_shape_get_body( int32_t index1, int32_t wg, int32_t* bodyIndex1, int32_t* bodyWg )
+{
+	*bodyIndex1 = *bodyWg = 0;
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return 0;
+	int b = W->shapeBody[s];
+	*bodyIndex1 = b + 1;
+	*bodyWg = pack_wg( W, W->bgen[b] );
+	return 1;
+}
+
+// shape.c:1185-1262 b2Shape_SetFilter / b2ResetProxy: the shape's contacts
+// end (waking), its boxes are recomputed; a new category re-creates the
+// proxy (new node, forced pair search), otherwise the proxy moves
+extern "C" F2D_API void f2d_shape_set_filter( int32_t index1, int32_t wg, int64_t categoryBits, int64_t maskBits,
+											  int32_t groupIndex )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return;
+	unsigned long long cat = (unsigned long long)categoryBits, mask = (unsigned long long)maskBits;
+	if ( cat == W->cat[s] && mask == W->mask[s] && groupIndex == W->group[s] )
+		return;
+	bool destroyProxy = cat != W->cat[s];
+	W->cat[s] = cat;
+	W->mask[s] = mask;
+	W->group[s] = groupIndex;
+	int b = W->shapeBody[s];
+	destroy_begin( W );
+	launch_destroy_contacts_of( W->d, W->stream, b, s, -1, 1, W->s.tmpA );
+	if ( s < W->shapeUploaded )
+	{
+		up( W->d.cat, W->cat, s, s + 1, W->stream );
+		up( W->d.mask, W->mask, s, s + 1, W->stream );
+		up( W->d.group, W->group, s, s + 1, W->stream );
+	}
+	fxf xf = body_xf( W, b );
+	int pk = W->proxyKey[s];
+	int proxyType = pk != F2D_NULL ? ( pk & 3 ) : body_type( W->bflags[b] );
+	fbox aabb = box_grow( h_shape_aabb( W->hgeomv[s], xf ), F2D_SPECULATIVE );
+	fbox fat = box_grow( aabb, proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN );
+	W->aabb[s] = box_to4( aabb );
+	W->fat[s] = box_to4( fat );
+	if ( pk != F2D_NULL )
+	{
+		int t = pk & 3;
+		tree_pull( W, t );
+		if ( destroyProxy )
+		{
+			launch_unbuffer_move( W->d, W->stream, s );
+			W->trees[t].destroy_proxy( pk >> 2 );
+			int proxyId = W->trees[t].create_proxy( W->fat[s], cat, s );
+			W->proxyKey[s] = ( proxyId << 2 ) | t;
+			if ( s < W->shapeUploaded )
+				up( W->d.proxyKey, W->proxyKey, s, s + 1, W->stream );
+		}
+		else
+			W->trees[t].move_proxy( pk >> 2, W->fat[s] );
+		W->treeDirty[t] = true;
+		if ( t == 0 )
+			W->staticDirty = true;
+		host_move( W, s );
+	}
+	if ( s < W->shapeUploaded )
+	{
+		up( W->d.aabb, W->aabb, s, s + 1, W->stream );
+		up( W->d.fat, W->fat, s, s + 1, W->stream );
+	}
+	destroy_end( W );
+}
+
+extern "C" F2D_API int32_t f2d_shape_test_point( int32_t index1, int32_t wg, double x, double y )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return 0;
+	flush_uploads( W );
+	int* dOut = W->s.tmpA;
+	launch_shape_test_point( W->d, W->stream, s, (float)x, (float)y, dOut );
+	int r = 0;
+	cudaMemcpyAsync( &r, dOut, sizeof( int ), cudaMemcpyDeviceToHost, W->stream );
+	cudaStreamSynchronize( W->stream );
+	return r;
+}
+
+extern "C" F2D_API int32_t f2d_shape_get_geometry( int32_t index1, int32_t wg, int32_t type, double* out,
+												   int32_t capacity )
+{
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return 0;
+	const HShapeGeom& g = W->hgeomv[s];
+	if ( g.type != type )
+		return 0;
+	double v[2 * F2D_MAX_POLY + 1];
+	int n = 0;
+	switch ( g.type )
+	{
+		case ST_CIRCLE:
+			v[n++] = g.c1.x, v[n++] = g.c1.y, v[n++] = g.radius;
+			break;
+		case ST_CAPSULE:
+			v[n++] = g.c1.x, v[n++] = g.c1.y, v[n++] = g.c2.x, v[n++] = g.c2.y, v[n++] = g.radius;
+			break;
+		case ST_SEGMENT:
+		case ST_CHAIN:
+			v[n++] = g.c1.x, v[n++] = g.c1.y, v[n++] = g.c2.x, v[n++] = g.c2.y;
+			break;
+		case ST_POLYGON:
+			for ( int i = 0; i < g.poly.count; ++i )
+				v[n++] = g.poly.v[i].x, v[n++] = g.poly.v[i].y;
+			v[n++] = g.poly.radius;
+			break;
+		default:
+			return 0;
+	}
+	for ( int i = 0; i < n && i < capacity; ++i )
+		out[i] = v[i];
+	return n;
+}
+
+extern "C" F2D_API void f2d_shape_get_aabb( int32_t index1, int32_t wg, double* out4 )
+{
+	out4[0] = out4[1] = out4[2] = out4[3] = 0.0;
+	HostWorld* W;
+	int s = shape_from( index1, wg, &W );
+	if ( s < 0 )
+		return;
+	flush_uploads( W );
+	cudaStreamSynchronize( W->stream );
+	float4 a;
+	cudaMemcpy( &a, W->d.aabb + s, sizeof( float4 ), cudaMemcpyDeviceToHost );
+	out4[0] = a.x;
+	out4[1] = a.y;
+	out4[2] = a.z;
+	out4[3] = a.w;
+}
+
+extern "C" F2D_API int32_t f2d_chain_is_valid( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	return W != nullptr && chain_live( W, index1 - 1, wg );
+}
+
+// shape.c:1476-1530: the chain's materials and every segment
+extern "C" F2D_API double f2d_chain_get_param( int32_t index1, int32_t wg, int32_t code )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr || !chain_live( W, index1 - 1, wg ) )
+		return 0.0;
+	int s = W->chainSegments[index1 - 1].front();
+	return code == F2D_SHAPE_FRICTION ? W->mat[s].x : code == F2D_SHAPE_RESTITUTION ? W->mat[s].y : 0.0;
+}
+
+extern "C" F2D_API void f2d_chain_set_param( int32_t index1, int32_t wg, int32_t code, double value )
+{
+	HostWorld* W = world_from_wg( wg );
+	if ( W == nullptr || !chain_live( W, index1 - 1, wg ) )
+		return;
+	if ( code != F2D_SHAPE_FRICTION && code != F2D_SHAPE_RESTITUTION )
+		return;
+	for ( int s : W->chainSegments[index1 - 1] )
+		shape_set( W, s, code, value, 0 );
+}
+
+// joint rows by type (the layouts beside the solvers in joint.cuh)
+static float* joint_field( HostWorld* W, int j, int type, int code )
+{
+	float4& d0 = W->jdef0[j];
+	float4& d1 = W->jdef1[j];
+	float4& d2 = W->jdef2[j];
+	float4& d3 = W->jdef3[j];
+	switch ( code )
+	{
+		case F2D_JP_LOCAL_ANCHOR_AX:
+			return &d0.x;
+		case F2D_JP_LOCAL_ANCHOR_AY:
+			return &d0.y;
+		case F2D_JP_LOCAL_ANCHOR_BX:
+			return &d0.z;
+		case F2D_JP_LOCAL_ANCHOR_BY:
+			return &d0.w;
+		default:
+			break;
+	}
+	switch ( type )
+	{
+		case 0: // revolute
+			switch ( code )
+			{
+				case F2D_JP_SPRING_HERTZ: return &d1.z;
+				case F2D_JP_SPRING_DAMPING: return &d1.w;
+				case F2D_JP_TARGET: return &d1.y;
+				case F2D_JP_LOWER: return &d2.x;
+				case F2D_JP_UPPER: return &d2.y;
+				case F2D_JP_MAX_MOTOR: return &d2.z;
+				case F2D_JP_MOTOR_SPEED: return &d2.w;
+			}
+			break;
+		case F2D_JOINT_PRISMATIC:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_HERTZ: return &d3.x;
+				case F2D_JP_SPRING_DAMPING: return &d3.y;
+				case F2D_JP_TARGET: return &d1.w;
+				case F2D_JP_LOWER: return &d2.x;
+				case F2D_JP_UPPER: return &d2.y;
+				case F2D_JP_MAX_MOTOR: return &d2.z;
+				case F2D_JP_MOTOR_SPEED: return &d2.w;
+			}
+			break;
+		case F2D_JOINT_WHEEL:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_HERTZ: return &d1.z;
+				case F2D_JP_SPRING_DAMPING: return &d1.w;
+				case F2D_JP_LOWER: return &d2.x;
+				case F2D_JP_UPPER: return &d2.y;
+				case F2D_JP_MAX_MOTOR: return &d2.z;
+				case F2D_JP_MOTOR_SPEED: return &d2.w;
+			}
+			break;
+		case F2D_JOINT_DISTANCE:
+			switch ( code )
+			{
+				case F2D_JP_LENGTH: return &d1.x;
+				case F2D_JP_MIN_LENGTH: return &d1.y;
+				case F2D_JP_MAX_LENGTH: return &d1.z;
+				case F2D_JP_SPRING_HERTZ: return &d1.w;
+				case F2D_JP_SPRING_DAMPING: return &d2.x;
+				case F2D_JP_MAX_MOTOR: return &d2.y;
+				case F2D_JP_MOTOR_SPEED: return &d2.z;
+			}
+			break;
+		case F2D_JOINT_WELD:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_HERTZ: return &d1.y;
+				case F2D_JP_LINEAR_DAMPING: return &d1.z;
+				case F2D_JP_ANGULAR_HERTZ: return &d1.w;
+				case F2D_JP_ANGULAR_DAMPING: return &d2.x;
+			}
+			break;
+		case F2D_JOINT_MOTOR:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_OFFSET_X: return &d1.x;
+				case F2D_JP_LINEAR_OFFSET_Y: return &d1.y;
+				case F2D_JP_ANGULAR_OFFSET: return &d1.z;
+				case F2D_JP_MAX_FORCE: return &d1.w;
+				case F2D_JP_MAX_TORQUE: return &d2.x;
+				case F2D_JP_CORRECTION: return &d2.y;
+			}
+			break;
+		case F2D_JOINT_MOUSE:
+			switch ( code )
+			{
+				case F2D_JP_TARGET_X: return &d1.x;
+				case F2D_JP_TARGET_Y: return &d1.y;
+				case F2D_JP_SPRING_HERTZ: return &d1.z;
+				case F2D_JP_SPRING_DAMPING: return &d1.w;
+				case F2D_JP_MAX_FORCE: return &d2.x;
+			}
+			break;
+	}
+	return nullptr;
+}
+
+// the flag bit a code switches, for the types that have it
+static int joint_bit( int type, int code )
+{
+	bool sprung = type == 0 || type == F2D_JOINT_PRISMATIC || type == F2D_JOINT_WHEEL || type == F2D_JOINT_DISTANCE;
+	if ( !sprung )
+		return 0;
+	return code == F2D_JP_SPRING_ENABLED ? JF_SPRING
+		   : code == F2D_JP_LIMIT_ENABLED ? JF_LIMIT
+		   : code == F2D_JP_MOTOR_ENABLED ? JF_MOTOR
+										  : 0;
+}
+
+// b2JointType values (types.h:630-640) of the library's joint types
+static int reference_joint_type( int type )
+{
+	switch ( type )
+	{
+		case F2D_JOINT_DISTANCE: return 0;
+		case F2D_JOINT_FILTER: return 1;
+		case F2D_JOINT_MOTOR: return 2;
+		case F2D_JOINT_MOUSE: return 3;
+		case F2D_JOINT_PRISMATIC: return 4;
+		case 0: return 5;
+		case F2D_JOINT_WELD: return 6;
+		case F2D_JOINT_WHEEL: return 7;
+		default: return -1;
+	}
+}
+
+static float4 joint_impulses( HostWorld* W, int j, float2* imp2 )
+{
+	float4 imp = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	*imp2 = make_float2( 0.0f, 0.0f );
+	if ( j < W->jointUploaded )
+	{
+		cudaStreamSynchronize( W->stream );
+		cudaMemcpy( &imp, W->d.jimp + j, sizeof( imp ), cudaMemcpyDeviceToHost );
+		cudaMemcpy( imp2, W->d.jimp2 + j, sizeof( float2 ), cudaMemcpyDeviceToHost );
+	}
+	return imp;
+}
+
+extern "C" F2D_API double f2d_joint_get_param( int32_t index1, int32_t wg, int32_t code )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return 0.0;
+	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
+	if ( code == F2D_JP_TYPE )
+		return reference_joint_type( type );
+	if ( int bit = joint_bit( type, code ) )
+		return ( W->jflags[j] & bit ) != 0;
+	int a = W->jbody[j].x, b = W->jbody[j].y;
+	float4 d0 = W->jdef0[j];
+	if ( code == F2D_JP_MOTOR_EFFORT )
+	{
+		float2 imp2;
+		float4 imp = joint_impulses( W, j, &imp2 );
+		// revolute_joint.c:157, prismatic_joint.c:152, distance_joint.c:175
+		// (motor impulse in w), wheel_joint.c:142 (in z)
+		if ( type == 0 || type == F2D_JOINT_PRISMATIC || type == F2D_JOINT_DISTANCE )
+			return W->invH * imp.w;
+		if ( type == F2D_JOINT_WHEEL )
+			return W->invH * imp.z;
+		return 0.0;
+	}
+	if ( code == F2D_JP_CURRENT )
+	{
+		fxf ta = body_xf( W, a ), tb = body_xf( W, b );
+		if ( type == 0 ) // revolute_joint.c:72-82
+			return remainderf( relative_angle( tb.q, ta.q ) - W->jdef1[j].x, 2.0f * F2D_PI );
+		if ( type == F2D_JOINT_DISTANCE ) // distance_joint.c:79-98
+			return vlen( vsub( xpoint( tb, mk( d0.z, d0.w ) ), xpoint( ta, mk( d0.x, d0.y ) ) ) );
+		if ( type == F2D_JOINT_PRISMATIC ) // prismatic_joint.c:158-172
+		{
+			fv2 axisA = rrot( ta.q, mk( W->jdef1[j].x, W->jdef1[j].y ) );
+			fv2 d = vsub( xpoint( tb, mk( d0.z, d0.w ) ), xpoint( ta, mk( d0.x, d0.y ) ) );
+			return vdot( d, axisA );
+		}
+		return 0.0;
+	}
+	if ( code == F2D_JP_SPEED && type == F2D_JOINT_PRISMATIC ) // prismatic_joint.c:174-209
+	{
+		fxf ta = body_xf( W, a ), tb = body_xf( W, b );
+		fv2 axisA = rrot( ta.q, mk( W->jdef1[j].x, W->jdef1[j].y ) );
+		fv2 cA = mk( W->center[a].x, W->center[a].y ), cB = mk( W->center[b].x, W->center[b].y );
+		fv2 rA = rrot( ta.q, vsub( mk( d0.x, d0.y ), mk( W->localCenter[a].x, W->localCenter[a].y ) ) );
+		fv2 rB = rrot( tb.q, vsub( mk( d0.z, d0.w ), mk( W->localCenter[b].x, W->localCenter[b].y ) ) );
+		fv2 d = vadd( vsub( cB, cA ), vsub( rB, rA ) );
+		// a body outside the awake set has no state: zero velocity
+		auto moving = [&]( int body ) {
+			int f = W->bflags[body];
+			return body_type( f ) != 0 && ( f & BF_ENABLED ) && ( f & BF_ASLEEP ) == 0;
+		};
+		fv2 vA = moving( a ) ? mk( W->vel[a].x, W->vel[a].y ) : mk( 0.0f, 0.0f );
+		fv2 vB = moving( b ) ? mk( W->vel[b].x, W->vel[b].y ) : mk( 0.0f, 0.0f );
+		float wA = moving( a ) ? W->vel[a].z : 0.0f;
+		float wB = moving( b ) ? W->vel[b].z : 0.0f;
+		fv2 vRel = vsub( vadd( vB, vcrossSV( wB, rB ) ), vadd( vA, vcrossSV( wA, rA ) ) );
+		return vdot( d, vcrossSV( wA, axisA ) ) + vdot( axisA, vRel );
+	}
+	float* f = joint_field( W, j, type, code );
+	return f ? *f : 0.0;
+}
+
+// zero impulse components of joint j on the device (stream-ordered): mask
+// bits 0-3 the jimp components, 4-5 the jimp2 components
+static void clear_joint_impulses( HostWorld* W, int j, int mask )
+{
+	if ( j >= W->jointUploaded )
+		return;
+	for ( int k = 0; k < 4; ++k )
+		if ( mask & ( 1 << k ) )
+			cudaMemsetAsync( (float*)( W->d.jimp + j ) + k, 0, sizeof( float ), W->stream );
+	for ( int k = 0; k < 2; ++k )
+		if ( mask & ( 16 << k ) )
+			cudaMemsetAsync( (float*)( W->d.jimp2 + j ) + k, 0, sizeof( float ), W->stream );
+}
+
+// revolute_joint.c:29-168, prismatic_joint.c:27-156, wheel_joint.c:27-145,
+// distance_joint.c:27-178, weld_joint.c:19-63, motor_joint.c:19-73,
+// mouse_joint.c:20-63: the value (clamped where the setter clamps); the
+// impulses the setter clears
+extern "C" F2D_API void f2d_joint_set_param( int32_t index1, int32_t wg, int32_t code, double value, double value2 )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return;
+	int type = ( W->jflags[j] >> JF_TYPE_SHIFT ) & 0xf;
+	float v = (float)value, v2 = (float)value2;
+	// components of jimp (bits 0-3) and jimp2 (bits 4-5) per impulse kind
+	int springImp = type == F2D_JOINT_WHEEL ? 2 : 4;
+	int motorImp = type == F2D_JOINT_WHEEL ? 4 : 8;
+	int limitImp = type == F2D_JOINT_DISTANCE ? 0 : 48;
+	if ( int bit = joint_bit( type, code ) )
+	{
+		bool on = value != 0.0;
+		if ( ( ( W->jflags[j] & bit ) != 0 ) == on )
+			return;
+		W->jflags[j] ^= bit;
+		if ( bit == JF_SPRING && type != F2D_JOINT_DISTANCE )
+			clear_joint_impulses( W, j, springImp );
+		else if ( bit == JF_LIMIT )
+			clear_joint_impulses( W, j, limitImp );
+		else if ( bit == JF_MOTOR )
+			clear_joint_impulses( W, j, motorImp );
+		mark_joint_dirty( W, j );
+		return;
+	}
+	if ( code == F2D_JP_LOWER && ( type == 0 || type == F2D_JOINT_PRISMATIC || type == F2D_JOINT_WHEEL ) )
+	{
+		float4& d2 = W->jdef2[j];
+		if ( v != d2.x || v2 != d2.y )
+		{
+			d2.x = fmin_s( v, v2 );
+			d2.y = fmax_s( v, v2 );
+			clear_joint_impulses( W, j, 48 );
+			mark_joint_dirty( W, j );
+		}
+		return;
+	}
+	if ( type == F2D_JOINT_DISTANCE && ( code == F2D_JP_LENGTH || code == F2D_JP_MIN_LENGTH ) )
+	{
+		float4& d1 = W->jdef1[j];
+		if ( code == F2D_JP_LENGTH )
+			d1.x = fclamp_s( v, F2D_LINEAR_SLOP, F2D_HUGE );
+		else
+		{
+			float lo = fclamp_s( v, F2D_LINEAR_SLOP, F2D_HUGE ), hi = fclamp_s( v2, F2D_LINEAR_SLOP, F2D_HUGE );
+			d1.y = fmin_s( lo, hi );
+			d1.z = fmax_s( lo, hi );
+		}
+		clear_joint_impulses( W, j, 7 ); // impulse, lower, upper
+		mark_joint_dirty( W, j );
+		return;
+	}
+	if ( type == F2D_JOINT_MOTOR && code == F2D_JP_LINEAR_OFFSET_X )
+	{
+		W->jdef1[j].x = v;
+		W->jdef1[j].y = v2;
+		mark_joint_dirty( W, j );
+		return;
+	}
+	if ( code == F2D_JP_UPPER || code == F2D_JP_MAX_LENGTH || code == F2D_JP_LINEAR_OFFSET_Y || code == F2D_JP_TYPE ||
+		 code == F2D_JP_CURRENT || code == F2D_JP_SPEED || code == F2D_JP_MOTOR_EFFORT || code == F2D_JP_TARGET_X ||
+		 code == F2D_JP_TARGET_Y || ( code >= F2D_JP_LOCAL_ANCHOR_AX && code <= F2D_JP_LOCAL_ANCHOR_BY ) )
+		return; // read-only, or set through another code or call
+	float* f = joint_field( W, j, type, code );
+	if ( f == nullptr )
+		return;
+	if ( type == F2D_JOINT_MOTOR && ( code == F2D_JP_MAX_FORCE || code == F2D_JP_MAX_TORQUE ) )
+		v = fmax_s( 0.0f, v );
+	else if ( type == F2D_JOINT_MOTOR && code == F2D_JP_CORRECTION )
+		v = fclamp_s( v, 0.0f, 1.0f );
+	*f = v;
+	mark_joint_dirty( W, j );
+}
+
+extern "C" F2D_API int32_t f2d_joint_get_body( int32_t index1, int32_t wg, int32_t edge, int32_t* bodyIndex1,
+											   int32_t* bodyWg )
+{
+	*bodyIndex1 = *bodyWg = 0;
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return 0;
+	int b = edge == 0 ? W->jbody[j].x : W->jbody[j].y;
+	*bodyIndex1 = b + 1;
+	*bodyWg = pack_wg( W, W->bgen[b] );
+	return 1;
+}
+
+extern "C" F2D_API void f2d_joint_wake_bodies( int32_t index1, int32_t wg )
+{
+	HostWorld* W = world_from_wg( wg );
+	int j = index1 - 1;
+	if ( W == nullptr || j < 0 || j >= W->jointCount || !joint_live( W, j, wg ) )
+		return;
+	for ( int e = 0; e < 2; ++e )
+	{
+		int b = e == 0 ? W->jbody[j].x : W->jbody[j].y;
+		f2d_body_set_awake( b + 1, pack_wg( W, W->bgen[b] ), 1 );
+	}
 }
 
 // ---------------------------------------------------------------------------

@@ -11,6 +11,21 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libforge2d_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "forge2d_gb300.h")
+
+
+def _codes():
+    """The property codes of the generic get/set calls, read from the C
+    header (F2D_BODY_*, F2D_SHAPE_*, F2D_JP_*)."""
+    import re
+    out = {}
+    with open(HEADER) as f:
+        for m in re.finditer(r"^#define (F2D_(?:BODY|SHAPE|JP)_[A-Z_]+) (\d+)", f.read(), re.M):
+            out[m.group(1)] = int(m.group(2))
+    return out
+
+
+CODES = _codes()
 
 _P = C.POINTER
 _lib = None
@@ -141,6 +156,30 @@ _SIGS = [
     ("f2d_destroy_joint", None, [_i, _i]),
     ("f2d_joint_set_collide_connected", None, [_i, _i, _i]),
     ("f2d_joint_get_collide_connected", _i, [_i, _i]),
+    ("f2d_body_get_param", _d, [_i, _i, _i]),
+    ("f2d_body_set_param", None, [_i, _i, _i, _d]),
+    ("f2d_body_get_world_point", None, [_i, _i, _d, _d, _P(_d), _P(_d)]),
+    ("f2d_body_get_local_point", None, [_i, _i, _d, _d, _P(_d), _P(_d)]),
+    ("f2d_body_set_mass_data", None, [_i, _i, _d, _d, _d, _d]),
+    ("f2d_body_apply_mass_from_shapes", None, [_i, _i]),
+    ("f2d_body_set_name", None, [_i, _i, C.c_char_p]),
+    ("f2d_body_get_name", _i, [_i, _i, C.c_char_p, _i]),
+    ("f2d_body_get_shapes", _i, [_i, _i, _P(_i), _i]),
+    ("f2d_body_get_joints", _i, [_i, _i, _P(_i), _i]),
+    ("f2d_shape_get_param", _d, [_i, _i, _i]),
+    ("f2d_shape_set_param", None, [_i, _i, _i, _d, _i]),
+    ("f2d_shape_get_body", _i, [_i, _i, _P(_i), _P(_i)]),
+    ("f2d_shape_set_filter", None, [_i, _i, _i64, _i64, _i]),
+    ("f2d_shape_test_point", _i, [_i, _i, _d, _d]),
+    ("f2d_shape_get_geometry", _i, [_i, _i, _i, _P(_d), _i]),
+    ("f2d_shape_get_aabb", None, [_i, _i, _P(_d)]),
+    ("f2d_chain_is_valid", _i, [_i, _i]),
+    ("f2d_chain_get_param", _d, [_i, _i, _i]),
+    ("f2d_chain_set_param", None, [_i, _i, _i, _d]),
+    ("f2d_joint_get_param", _d, [_i, _i, _i]),
+    ("f2d_joint_set_param", None, [_i, _i, _i, _d, _d]),
+    ("f2d_joint_get_body", _i, [_i, _i, _i, _P(_i), _P(_i)]),
+    ("f2d_joint_wake_bodies", None, [_i, _i]),
     ("f2d_body_get_position", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_get_rotation", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_set_transform", None, [_i, _i, _d, _d, _d, _d]),

@@ -104,6 +104,53 @@ class GpuWorld:
         c = self._id("chain", chain)
         self.lib.f2d_destroy_chain(c[0], c[1])
 
+    # properties (generic get/set codes, native.CODES) ----------------
+    def body_get(self, body, code):
+        b = self._body(body)
+        return self.lib.f2d_body_get_param(b[0], b[1], native.CODES[code] if isinstance(code, str) else code)
+
+    def body_set(self, body, code, value):
+        b = self._body(body)
+        self.lib.f2d_body_set_param(b[0], b[1], native.CODES[code] if isinstance(code, str) else code, value)
+
+    def body_set_mass_data(self, body, mass, inertia, cx, cy):
+        b = self._body(body)
+        self.lib.f2d_body_set_mass_data(b[0], b[1], mass, inertia, cx, cy)
+
+    def body_apply_mass_from_shapes(self, body):
+        b = self._body(body)
+        self.lib.f2d_body_apply_mass_from_shapes(b[0], b[1])
+
+    def shape_get(self, shape, code):
+        s = self._id("shape", shape)
+        return self.lib.f2d_shape_get_param(s[0], s[1], native.CODES[code] if isinstance(code, str) else code)
+
+    def shape_set(self, shape, code, value, flag=0):
+        s = self._id("shape", shape)
+        self.lib.f2d_shape_set_param(s[0], s[1], native.CODES[code] if isinstance(code, str) else code, value,
+                                     int(flag))
+
+    def shape_set_filter(self, shape, category, mask, group):
+        s = self._id("shape", shape)
+        self.lib.f2d_shape_set_filter(s[0], s[1], category, mask, group)
+
+    def shape_test_point(self, shape, x, y):
+        s = self._id("shape", shape)
+        return bool(self.lib.f2d_shape_test_point(s[0], s[1], x, y))
+
+    def chain_set(self, chain, code, value):
+        c = self._id("chain", chain)
+        self.lib.f2d_chain_set_param(c[0], c[1], native.CODES[code] if isinstance(code, str) else code, value)
+
+    def joint_get(self, joint, code):
+        j = self._id("joint", joint)
+        return self.lib.f2d_joint_get_param(j[0], j[1], native.CODES[code] if isinstance(code, str) else code)
+
+    def joint_set(self, joint, code, value, value2=0.0):
+        j = self._id("joint", joint)
+        self.lib.f2d_joint_set_param(j[0], j[1], native.CODES[code] if isinstance(code, str) else code, value,
+                                     value2)
+
     def set_collide_connected(self, joint, flag):
         j = self._id("joint", joint)
         self.lib.f2d_joint_set_collide_connected(j[0], j[1], int(flag))

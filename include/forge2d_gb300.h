@@ -359,6 +359,139 @@ F2D_API void f2d_destroy_joint( int32_t index1, int32_t worldAndGeneration );
 F2D_API void f2d_joint_set_collide_connected( int32_t index1, int32_t worldAndGeneration, int32_t flag );
 F2D_API int32_t f2d_joint_get_collide_connected( int32_t index1, int32_t worldAndGeneration );
 
+/* ---- properties ---------------------------------------------------------
+ * The RawBox2D getters and setters without a call of their own go through
+ * one get and one set per kind, the property chosen by a code named for the
+ * RawBox2D method pair (raw_box2d.dart line beside each). Gets return 0 for
+ * an invalid id or a code the object does not have; sets ignore them, and
+ * ignore values the reference's setter asserts against (negative damping,
+ * NaN, ...). Pairs (limits, length range, linear offset) are set with both
+ * values at once: value = first, value2 = second. */
+
+/* bodies: f2d_body_get_param / f2d_body_set_param */
+#define F2D_BODY_LINEAR_DAMPING 1	/* bodyGet/SetLinearDamping :282-291 */
+#define F2D_BODY_ANGULAR_DAMPING 2	/* bodyGet/SetAngularDamping :288-291 */
+#define F2D_BODY_GRAVITY_SCALE 3	/* bodyGet/SetGravityScale :276-279 */
+#define F2D_BODY_BULLET 4			/* bodyIsBullet / bodySetBullet :270-273 */
+#define F2D_BODY_FIXED_ROTATION 5	/* bodyIsFixedRotation / bodySetFixedRotation :260-263 */
+#define F2D_BODY_ENABLED 6			/* bodyIsEnabled / bodyEnable / bodyDisable :251-257 */
+#define F2D_BODY_TYPE 7				/* bodyGetType / bodySetType :217-220 */
+#define F2D_BODY_LOCAL_CENTER_X 8	/* bodyGetLocalCenterOfMass :198 */
+#define F2D_BODY_LOCAL_CENTER_Y 9
+#define F2D_BODY_WORLD_CENTER_X 10	/* bodyGetWorldCenterOfMass :201 */
+#define F2D_BODY_WORLD_CENTER_Y 11
+F2D_API double f2d_body_get_param( int32_t index1, int32_t worldAndGeneration, int32_t code );
+F2D_API void f2d_body_set_param( int32_t index1, int32_t worldAndGeneration, int32_t code, double value );
+/* RawBox2D.bodyGetWorldPoint / bodyGetLocalPoint (raw_box2d.dart:298-311). */
+F2D_API void f2d_body_get_world_point( int32_t index1, int32_t worldAndGeneration, double x, double y, double* ox,
+									   double* oy );
+F2D_API void f2d_body_get_local_point( int32_t index1, int32_t worldAndGeneration, double x, double y, double* ox,
+									   double* oy );
+/* RawBox2D.bodySetMassData / bodyApplyMassFromShapes (raw_box2d.dart:204-214
+ * -> b2Body_SetMassData, body.c:917; b2Body_ApplyMassFromShapes). */
+F2D_API void f2d_body_set_mass_data( int32_t index1, int32_t worldAndGeneration, double mass,
+									 double rotationalInertia, double centerX, double centerY );
+F2D_API void f2d_body_apply_mass_from_shapes( int32_t index1, int32_t worldAndGeneration );
+/* RawBox2D.bodyGetName / bodySetName (raw_box2d.dart:223-226): up to 31
+ * bytes kept (b2Body_SetName, body.c:1160); null or "" clears it. get copies
+ * the name, zero-terminated, into out (capacity bytes) and returns its
+ * length. */
+F2D_API void f2d_body_set_name( int32_t index1, int32_t worldAndGeneration, const char* name );
+F2D_API int32_t f2d_body_get_name( int32_t index1, int32_t worldAndGeneration, char* out, int32_t capacity );
+/* RawBox2D.bodyGetShapes / bodyGetJoints (raw_box2d.dart:315-319): id pairs
+ * in the body's list order (newest first); returns the count. */
+F2D_API int32_t f2d_body_get_shapes( int32_t index1, int32_t worldAndGeneration, int32_t* out2, int32_t capacity );
+F2D_API int32_t f2d_body_get_joints( int32_t index1, int32_t worldAndGeneration, int32_t* out2, int32_t capacity );
+
+/* shapes: f2d_shape_get_param / f2d_shape_set_param (flag = updateBodyMass
+ * for the density) */
+#define F2D_SHAPE_DENSITY 1			/* shapeGetDensity / shapeSetDensity :409-417 */
+#define F2D_SHAPE_FRICTION 2		/* shapeGet/SetFriction :420-423 */
+#define F2D_SHAPE_RESTITUTION 3		/* shapeGet/SetRestitution :426-433 */
+#define F2D_SHAPE_SENSOR 4			/* shapeIsSensor :406 (get) */
+#define F2D_SHAPE_SENSOR_EVENTS 5	/* shapeAreSensorEventsEnabled / shapeEnableSensorEvents :448-455 */
+#define F2D_SHAPE_CONTACT_EVENTS 6	/* :458-465 */
+#define F2D_SHAPE_HIT_EVENTS 7		/* :468-475 */
+#define F2D_SHAPE_PRESOLVE_EVENTS 8 /* :478-485 */
+#define F2D_SHAPE_CATEGORY 9		/* shapeGetFilter :436 (get) */
+#define F2D_SHAPE_MASK 10
+#define F2D_SHAPE_GROUP 11
+F2D_API double f2d_shape_get_param( int32_t index1, int32_t worldAndGeneration, int32_t code );
+F2D_API void f2d_shape_set_param( int32_t index1, int32_t worldAndGeneration, int32_t code, double value,
+								  int32_t flag );
+/* RawBox2D.shapeGetBody (raw_box2d.dart:403). */
+F2D_API int32_t f2d_shape_get_body( int32_t index1, int32_t worldAndGeneration, int32_t* bodyIndex1,
+									int32_t* bodyWorldAndGeneration );
+/* RawBox2D.shapeSetFilter (raw_box2d.dart:439 -> b2Shape_SetFilter,
+ * shape.c:1197): a change of category or mask re-creates the proxy (its
+ * contacts end, the bodies wake); a group change alone keeps it. */
+F2D_API void f2d_shape_set_filter( int32_t index1, int32_t worldAndGeneration, int64_t categoryBits, int64_t maskBits,
+								   int32_t groupIndex );
+/* RawBox2D.shapeTestPoint (raw_box2d.dart:488 -> b2Shape_TestPoint). */
+F2D_API int32_t f2d_shape_test_point( int32_t index1, int32_t worldAndGeneration, double x, double y );
+/* RawBox2D.shapeGetCircle / GetCapsule / GetSegment / GetChainSegment /
+ * GetPolygon (raw_box2d.dart:491-520): the shape's local geometry; returns
+ * the number of floats written to out (circle 3: center, radius; capsule 5:
+ * center1, center2, radius; segment and chain segment 4: point1, point2;
+ * polygon 2 * count + 1: vertices, then the radius), 0 for another type. */
+F2D_API int32_t f2d_shape_get_geometry( int32_t index1, int32_t worldAndGeneration, int32_t type, double* out,
+										int32_t capacity );
+/* RawBox2D.shapeGetAabb (raw_box2d.dart:524 -> b2Shape_GetAABB): the
+ * shape's current box (lower.xy, upper.xy). */
+F2D_API void f2d_shape_get_aabb( int32_t index1, int32_t worldAndGeneration, double* out4 );
+
+/* chains: RawBox2D.chainIsValid / chainSet/GetFriction / Restitution
+ * (raw_box2d.dart:553-569); the set reaches every segment (shape.c:1476). */
+F2D_API int32_t f2d_chain_is_valid( int32_t index1, int32_t worldAndGeneration );
+F2D_API double f2d_chain_get_param( int32_t index1, int32_t worldAndGeneration, int32_t code );
+F2D_API void f2d_chain_set_param( int32_t index1, int32_t worldAndGeneration, int32_t code, double value );
+
+/* joints: f2d_joint_get_param / f2d_joint_set_param. The codes that belong
+ * to each type follow the type's RawBox2D methods; setters clear the
+ * impulses the reference's setters clear and wake nothing. */
+#define F2D_JP_TYPE 1				/* jointGetType :720 (b2JointType values) */
+#define F2D_JP_LOCAL_ANCHOR_AX 2	/* jointGetLocalAnchorA / B :729-732 */
+#define F2D_JP_LOCAL_ANCHOR_AY 3
+#define F2D_JP_LOCAL_ANCHOR_BX 4
+#define F2D_JP_LOCAL_ANCHOR_BY 5
+#define F2D_JP_SPRING_ENABLED 6		/* {distance,prismatic,revolute,wheel}JointIsSpringEnabled / EnableSpring */
+#define F2D_JP_SPRING_HERTZ 7		/* ...Get/SetSpringHertz (and mouse) */
+#define F2D_JP_SPRING_DAMPING 8		/* ...Get/SetSpringDampingRatio (and mouse) */
+#define F2D_JP_TARGET 9				/* revoluteJointGet/SetTargetAngle, prismaticJointGet/SetTargetTranslation */
+#define F2D_JP_LIMIT_ENABLED 10		/* {distance,prismatic,revolute,wheel}JointIsLimitEnabled / EnableLimit */
+#define F2D_JP_LOWER 11				/* ...GetLowerLimit; set: SetLimits(value, value2) */
+#define F2D_JP_UPPER 12				/* ...GetUpperLimit */
+#define F2D_JP_MOTOR_ENABLED 13		/* ...IsMotorEnabled / EnableMotor */
+#define F2D_JP_MOTOR_SPEED 14		/* ...Get/SetMotorSpeed */
+#define F2D_JP_MAX_MOTOR 15			/* ...Get/SetMaxMotorTorque (revolute, wheel) / Force (prismatic, distance) */
+#define F2D_JP_MOTOR_EFFORT 16		/* ...GetMotorTorque / GetMotorForce (get) */
+#define F2D_JP_LENGTH 17			/* distanceJointGet/SetLength */
+#define F2D_JP_MIN_LENGTH 18		/* distanceJointGetMinLength; set: SetLengthRange(value, value2) */
+#define F2D_JP_MAX_LENGTH 19		/* distanceJointGetMaxLength */
+#define F2D_JP_CURRENT 20			/* distanceJointGetCurrentLength, revoluteJointGetAngle, prismaticJointGetTranslation */
+#define F2D_JP_SPEED 21				/* prismaticJointGetSpeed */
+#define F2D_JP_LINEAR_HERTZ 22		/* weldJointGet/SetLinearHertz */
+#define F2D_JP_LINEAR_DAMPING 23	/* weldJointGet/SetLinearDampingRatio */
+#define F2D_JP_ANGULAR_HERTZ 24		/* weldJointGet/SetAngularHertz */
+#define F2D_JP_ANGULAR_DAMPING 25	/* weldJointGet/SetAngularDampingRatio */
+#define F2D_JP_LINEAR_OFFSET_X 26	/* motorJointGetLinearOffset; set: SetLinearOffset(value, value2) */
+#define F2D_JP_LINEAR_OFFSET_Y 27
+#define F2D_JP_ANGULAR_OFFSET 28	/* motorJointGet/SetAngularOffset */
+#define F2D_JP_MAX_FORCE 29			/* motorJointGet/SetMaxForce, mouseJointGet/SetMaxForce */
+#define F2D_JP_MAX_TORQUE 30		/* motorJointGet/SetMaxTorque */
+#define F2D_JP_CORRECTION 31		/* motorJointGet/SetCorrectionFactor */
+#define F2D_JP_TARGET_X 32			/* mouseJointGetTarget (set: f2d_mouse_joint_set_target) */
+#define F2D_JP_TARGET_Y 33
+F2D_API double f2d_joint_get_param( int32_t index1, int32_t worldAndGeneration, int32_t code );
+F2D_API void f2d_joint_set_param( int32_t index1, int32_t worldAndGeneration, int32_t code, double value,
+								  double value2 );
+/* RawBox2D.jointGetBodyA / jointGetBodyB (raw_box2d.dart:723-726): edge 0
+ * or 1. */
+F2D_API int32_t f2d_joint_get_body( int32_t index1, int32_t worldAndGeneration, int32_t edge, int32_t* bodyIndex1,
+									int32_t* bodyWorldAndGeneration );
+/* RawBox2D.jointWakeBodies (raw_box2d.dart:745 -> b2Joint_WakeBodies). */
+F2D_API void f2d_joint_wake_bodies( int32_t index1, int32_t worldAndGeneration );
+
 /* ---- events (RawBox2D.worldGetContactEvents / worldGetBodyEvents,
  *      raw_box2d_ffi.dart:2172 and :2259) ----------------------------------
  * Counts of the last step's events: begin, end, hit, body move. */

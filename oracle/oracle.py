@@ -223,6 +223,17 @@ def _bind(lib, prefix):
         "destroy_chain": (None, [i, i]),
         "tree_stats": (None, [i, i, _P(i)]),
         "tree_nodes": (i, [i, i, _P(i), _P(C.c_float), i]),
+        "body_get_param": (d, [i, i, i]),
+        "body_set_param": (None, [i, i, i, d]),
+        "body_set_mass_data": (None, [i, i, d, d, d, d]),
+        "body_apply_mass_from_shapes": (None, [i, i]),
+        "shape_get_param": (d, [i, i, i]),
+        "shape_set_param": (None, [i, i, i, d, i]),
+        "shape_set_filter": (None, [i, i, C.c_longlong, C.c_longlong, i]),
+        "shape_test_point": (i, [i, i, d, d]),
+        "chain_set_param": (None, [i, i, i, d]),
+        "joint_get_param": (d, [i, i, i]),
+        "joint_set_param": (None, [i, i, i, d, d]),
     }
     out = {}
     for name, (res, args) in sig.items():
@@ -288,6 +299,47 @@ class _CpuWorld:
         """fn(shapeA, shapeB, ManifoldView) -> bool; None removes it."""
         self._presolve_cb = PRESOLVE_FN(lambda a, b, m, ctx: int(bool(fn(a, b, m.contents)))) if fn else PRESOLVE_FN()
         self._fns["set_pre_solve"](self.w, self._presolve_cb, None)
+
+    # properties (the product header's generic get/set codes) ----------
+    @staticmethod
+    def _code(code):
+        if isinstance(code, str):
+            from forge2d_gb300.native import CODES
+            return CODES[code]
+        return code
+
+    def body_get(self, body, code):
+        return self._fns["body_get_param"](self.w, body, self._code(code))
+
+    def body_set(self, body, code, value):
+        self._fns["body_set_param"](self.w, body, self._code(code), value)
+
+    def body_set_mass_data(self, body, mass, inertia, cx, cy):
+        self._fns["body_set_mass_data"](self.w, body, mass, inertia, cx, cy)
+
+    def body_apply_mass_from_shapes(self, body):
+        self._fns["body_apply_mass_from_shapes"](self.w, body)
+
+    def shape_get(self, shape, code):
+        return self._fns["shape_get_param"](self.w, shape, self._code(code))
+
+    def shape_set(self, shape, code, value, flag=0):
+        self._fns["shape_set_param"](self.w, shape, self._code(code), value, int(flag))
+
+    def shape_set_filter(self, shape, category, mask, group):
+        self._fns["shape_set_filter"](self.w, shape, category, mask, group)
+
+    def shape_test_point(self, shape, x, y):
+        return bool(self._fns["shape_test_point"](self.w, shape, x, y))
+
+    def chain_set(self, chain, code, value):
+        self._fns["chain_set_param"](self.w, chain, self._code(code), value)
+
+    def joint_get(self, joint, code):
+        return self._fns["joint_get_param"](self.w, joint, self._code(code))
+
+    def joint_set(self, joint, code, value, value2=0.0):
+        self._fns["joint_set_param"](self.w, joint, self._code(code), value, value2)
 
     # destroy path -----------------------------------------------------
     def destroy_body(self, body):

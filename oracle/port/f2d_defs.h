@@ -158,3 +158,61 @@ typedef float ( *orc_cast_fn )( int32_t shape, float pointX, float pointY, float
 #define F2D_BODY_DUMP_STRIDE 12
 #define F2D_CONTACT_DUMP_INTS 9
 #define F2D_CONTACT_DUMP_FLOATS 25
+
+// property codes of the generic get/set calls (the same values as the
+// product header's; a CPU test compares the two lists)
+#define F2D_BODY_LINEAR_DAMPING 1
+#define F2D_BODY_ANGULAR_DAMPING 2
+#define F2D_BODY_GRAVITY_SCALE 3
+#define F2D_BODY_BULLET 4
+#define F2D_BODY_FIXED_ROTATION 5
+#define F2D_BODY_ENABLED 6
+#define F2D_BODY_TYPE 7
+#define F2D_BODY_LOCAL_CENTER_X 8
+#define F2D_BODY_LOCAL_CENTER_Y 9
+#define F2D_BODY_WORLD_CENTER_X 10
+#define F2D_BODY_WORLD_CENTER_Y 11
+#define F2D_SHAPE_DENSITY 1
+#define F2D_SHAPE_FRICTION 2
+#define F2D_SHAPE_RESTITUTION 3
+#define F2D_SHAPE_SENSOR 4
+#define F2D_SHAPE_SENSOR_EVENTS 5
+#define F2D_SHAPE_CONTACT_EVENTS 6
+#define F2D_SHAPE_HIT_EVENTS 7
+#define F2D_SHAPE_PRESOLVE_EVENTS 8
+#define F2D_SHAPE_CATEGORY 9
+#define F2D_SHAPE_MASK 10
+#define F2D_SHAPE_GROUP 11
+#define F2D_JP_TYPE 1
+#define F2D_JP_LOCAL_ANCHOR_AX 2
+#define F2D_JP_LOCAL_ANCHOR_AY 3
+#define F2D_JP_LOCAL_ANCHOR_BX 4
+#define F2D_JP_LOCAL_ANCHOR_BY 5
+#define F2D_JP_SPRING_ENABLED 6
+#define F2D_JP_SPRING_HERTZ 7
+#define F2D_JP_SPRING_DAMPING 8
+#define F2D_JP_TARGET 9
+#define F2D_JP_LIMIT_ENABLED 10
+#define F2D_JP_LOWER 11
+#define F2D_JP_UPPER 12
+#define F2D_JP_MOTOR_ENABLED 13
+#define F2D_JP_MOTOR_SPEED 14
+#define F2D_JP_MAX_MOTOR 15
+#define F2D_JP_MOTOR_EFFORT 16
+#define F2D_JP_LENGTH 17
+#define F2D_JP_MIN_LENGTH 18
+#define F2D_JP_MAX_LENGTH 19
+#define F2D_JP_CURRENT 20
+#define F2D_JP_SPEED 21
+#define F2D_JP_LINEAR_HERTZ 22
+#define F2D_JP_LINEAR_DAMPING 23
+#define F2D_JP_ANGULAR_HERTZ 24
+#define F2D_JP_ANGULAR_DAMPING 25
+#define F2D_JP_LINEAR_OFFSET_X 26
+#define F2D_JP_LINEAR_OFFSET_Y 27
+#define F2D_JP_ANGULAR_OFFSET 28
+#define F2D_JP_MAX_FORCE 29
+#define F2D_JP_MAX_TORQUE 30
+#define F2D_JP_CORRECTION 31
+#define F2D_JP_TARGET_X 32
+#define F2D_JP_TARGET_Y 33

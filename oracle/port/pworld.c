@@ -2481,3 +2481,452 @@ void orc_destroy_body( int wi, int bodyId )
 	b->headContactKey = P_NULL;
 	free_id( &w->bodyFree, &w->bodyFreeCount, bodyId );
 }
+
+// ---------------------------------------------------------------------------
+// properties (body.c:1357-1580, shape.c:979-1262, :1476-1530 and the
+// setters and getters of revolute_joint.c, prismatic_joint.c,
+// wheel_joint.c, distance_joint.c, weld_joint.c, motor_joint.c,
+// mouse_joint.c), one get and one set per kind selected by an F2D_*_ code
+// ---------------------------------------------------------------------------
+static Body* live_body( World* w, int bid )
+{
+	return ( w != NULL && bid >= 0 && bid < w->bodyCount && w->bodies[bid].used ) ? w->bodies + bid : NULL;
+}
+
+static Shape* live_shape( World* w, int sid )
+{
+	return ( w != NULL && sid >= 0 && sid < w->shapeCount && w->shapes[sid].used ) ? w->shapes + sid : NULL;
+}
+
+static Joint* live_joint( World* w, int jid )
+{
+	return ( w != NULL && jid >= 0 && jid < w->jointCount && w->joints[jid].used ) ? w->joints + jid : NULL;
+}
+
+static int valid_f( double v )
+{
+	float f = (float)v;
+	return !isnan( f ) && !isinf( f );
+}
+
+double orc_body_get_param( int wi, int bid, int code )
+{
+	Body* b = live_body( p_world( wi ), bid );
+	if ( b == NULL )
+		return 0.0;
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING: return b->linearDamping;
+		case F2D_BODY_ANGULAR_DAMPING: return b->angularDamping;
+		case F2D_BODY_GRAVITY_SCALE: return b->gravityScale;
+		case F2D_BODY_BULLET: return b->isBullet;
+		case F2D_BODY_FIXED_ROTATION: return b->fixedRotation;
+		case F2D_BODY_ENABLED: return b->enabled;
+		case F2D_BODY_TYPE: return b->type;
+		case F2D_BODY_LOCAL_CENTER_X: return b->localCenter.x;
+		case F2D_BODY_LOCAL_CENTER_Y: return b->localCenter.y;
+		case F2D_BODY_WORLD_CENTER_X: return b->center.x;
+		case F2D_BODY_WORLD_CENTER_Y: return b->center.y;
+		default: return 0.0;
+	}
+}
+
+void orc_body_set_param( int wi, int bid, int code, double value )
+{
+	World* w = p_world( wi );
+	Body* b = live_body( w, bid );
+	if ( b == NULL )
+		return;
+	float v = (float)value;
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING:
+			if ( valid_f( value ) && value >= 0.0 )
+				b->linearDamping = v;
+			break;
+		case F2D_BODY_ANGULAR_DAMPING:
+			if ( valid_f( value ) && value >= 0.0 )
+				b->angularDamping = v;
+			break;
+		case F2D_BODY_GRAVITY_SCALE:
+			if ( valid_f( value ) )
+				b->gravityScale = v;
+			break;
+		case F2D_BODY_BULLET:
+			b->isBullet = value != 0.0;
+			break;
+		case F2D_BODY_FIXED_ROTATION:
+			// body.c:1536-1558: the awake state's angular velocity is cleared
+			if ( b->fixedRotation != ( value != 0.0 ) )
+			{
+				b->fixedRotation = value != 0.0;
+				if ( b->setIndex == SET_AWAKE )
+					b->w = 0.0f;
+				update_mass( w, b );
+			}
+			break;
+		default:
+			break;
+	}
+}
+
+void orc_body_set_mass_data( int wi, int bid, double mass, double inertia, double cx, double cy )
+{
+	Body* b = live_body( p_world( wi ), bid );
+	if ( b == NULL )
+		return;
+	b->mass = (float)mass;
+	b->inertia = (float)inertia;
+	b->localCenter = V( (float)cx, (float)cy );
+	v2 c = xfPoint( b->xf, b->localCenter );
+	b->center = c;
+	b->center0 = c;
+	b->invMass = b->mass > 0.0f ? 1.0f / b->mass : 0.0f;
+	b->invInertia = b->inertia > 0.0f ? 1.0f / b->inertia : 0.0f;
+}
+
+void orc_body_apply_mass_from_shapes( int wi, int bid )
+{
+	World* w = p_world( wi );
+	Body* b = live_body( w, bid );
+	if ( b != NULL )
+		update_mass( w, b );
+}
+
+double orc_shape_get_param( int wi, int sid, int code )
+{
+	Shape* s = live_shape( p_world( wi ), sid );
+	if ( s == NULL )
+		return 0.0;
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY: return s->density;
+		case F2D_SHAPE_FRICTION: return s->friction;
+		case F2D_SHAPE_RESTITUTION: return s->restitution;
+		case F2D_SHAPE_SENSOR: return s->isSensor;
+		case F2D_SHAPE_SENSOR_EVENTS: return s->enableSensorEvents;
+		case F2D_SHAPE_CONTACT_EVENTS: return s->enableContactEvents;
+		case F2D_SHAPE_HIT_EVENTS: return s->enableHitEvents;
+		case F2D_SHAPE_PRESOLVE_EVENTS: return s->enablePreSolveEvents;
+		case F2D_SHAPE_CATEGORY: return (double)(int64_t)s->categoryBits;
+		case F2D_SHAPE_MASK: return (double)(int64_t)s->maskBits;
+		case F2D_SHAPE_GROUP: return s->groupIndex;
+		default: return 0.0;
+	}
+}
+
+void orc_shape_set_param( int wi, int sid, int code, double value, int flag )
+{
+	World* w = p_world( wi );
+	Shape* s = live_shape( w, sid );
+	if ( s == NULL )
+		return;
+	float v = (float)value;
+	int on = value != 0.0;
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY:
+			// shape.c:1057-1075
+			if ( !valid_f( value ) || value < 0.0 || v == s->density )
+				return;
+			s->density = v;
+			if ( flag )
+				update_mass( w, w->bodies + s->bodyId );
+			break;
+		case F2D_SHAPE_FRICTION:
+			if ( valid_f( value ) && value >= 0.0 )
+				s->friction = v;
+			break;
+		case F2D_SHAPE_RESTITUTION:
+			if ( valid_f( value ) && value >= 0.0 )
+				s->restitution = v;
+			break;
+		case F2D_SHAPE_SENSOR_EVENTS: s->enableSensorEvents = on; break;
+		case F2D_SHAPE_CONTACT_EVENTS: s->enableContactEvents = on; break;
+		case F2D_SHAPE_HIT_EVENTS: s->enableHitEvents = on; break;
+		case F2D_SHAPE_PRESOLVE_EVENTS: s->enablePreSolveEvents = on; break;
+		default: break;
+	}
+}
+
+// shape.c:1185-1262 b2Shape_SetFilter / b2ResetProxy
+void orc_shape_set_filter( int wi, int sid, long long categoryBits, long long maskBits, int groupIndex )
+{
+	World* w = p_world( wi );
+	Shape* s = live_shape( w, sid );
+	if ( s == NULL )
+		return;
+	uint64_t cat = (uint64_t)categoryBits, mask = (uint64_t)maskBits;
+	if ( cat == s->categoryBits && mask == s->maskBits && groupIndex == s->groupIndex )
+		return;
+	int destroyProxyFlag = cat != s->categoryBits;
+	s->categoryBits = cat;
+	s->maskBits = mask;
+	s->groupIndex = groupIndex;
+	Body* b = w->bodies + s->bodyId;
+	for ( int key = b->headContactKey; key != P_NULL; )
+	{
+		int cid = key >> 1;
+		Contact* c = w->contacts + cid;
+		key = c->edgeNext[key & 1];
+		if ( c->shapeA == sid || c->shapeB == sid )
+			destroy_contact_ex( w, cid, 1, 1 );
+	}
+	int proxyType = s->proxyKey != P_NULL ? ( s->proxyKey & 3 ) : b->type;
+	box2 aabb = p_shape_aabb( &s->g, b->xf );
+	aabb.lo.x -= P_SPECULATIVE;
+	aabb.lo.y -= P_SPECULATIVE;
+	aabb.hi.x += P_SPECULATIVE;
+	aabb.hi.y += P_SPECULATIVE;
+	s->aabb = aabb;
+	float margin = proxyType == BODY_STATIC ? P_SPECULATIVE : P_AABB_MARGIN;
+	s->fatAABB.lo.x = aabb.lo.x - margin;
+	s->fatAABB.lo.y = aabb.lo.y - margin;
+	s->fatAABB.hi.x = aabb.hi.x + margin;
+	s->fatAABB.hi.y = aabb.hi.y + margin;
+	if ( s->proxyKey == P_NULL )
+		return;
+	if ( destroyProxyFlag )
+	{
+		destroy_proxy( w, sid );
+		int proxyId = rt_create_proxy( w->trees + proxyType, s->fatAABB, s->categoryBits, sid );
+		s->proxyKey = ( proxyId << 2 ) | proxyType;
+	}
+	else
+		rt_move_proxy( w->trees + proxyType, s->proxyKey >> 2, s->fatAABB );
+	if ( proxyType == BODY_STATIC )
+		w->staticOrderDirty = 1;
+	push_move( w, sid );
+}
+
+// shape.c:979-1001, geometry.c:456-502
+int orc_shape_test_point( int wi, int sid, double x, double y )
+{
+	World* w = p_world( wi );
+	Shape* s = live_shape( w, sid );
+	if ( s == NULL )
+		return 0;
+	v2 lp = invXfPoint( w->bodies[s->bodyId].xf, V( (float)x, (float)y ) );
+	const Geometry* g = &s->g;
+	if ( g->type == SHAPE_CIRCLE )
+	{
+		v2 d = sub( lp, g->c1 );
+		return dot( d, d ) <= g->radius * g->radius;
+	}
+	if ( g->type == SHAPE_CAPSULE )
+	{
+		float rr = g->radius * g->radius;
+		v2 d = sub( g->c2, g->c1 );
+		float dd = dot( d, d );
+		if ( dd == 0.0f )
+		{
+			v2 e = sub( lp, g->c1 );
+			return dot( e, e ) <= rr;
+		}
+		float t = fclampp( dot( sub( lp, g->c1 ), d ) / dd, 0.0f, 1.0f );
+		v2 e = sub( lp, mulAdd( g->c1, t, d ) );
+		return dot( e, e ) <= rr;
+	}
+	if ( g->type == SHAPE_POLYGON )
+	{
+		ShapeProxy pa = p_make_proxy( g->poly.vertices, g->poly.count, 0.0f );
+		ShapeProxy pb = p_make_proxy( &lp, 1, 0.0f );
+		xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+		SimplexCache cache = { 0 };
+		v2 pA, pB, n;
+		return p_shape_distance( &pa, &pb, identity, identity, &cache, &pA, &pB, &n ) <= g->poly.radius;
+	}
+	return 0;
+}
+
+void orc_chain_set_param( int wi, int chainId, int code, double value )
+{
+	World* w = p_world( wi );
+	if ( w == NULL || chainId < 0 || chainId >= w->chainCount || w->chains[chainId].used == 0 )
+		return;
+	PChain* ch = w->chains + chainId;
+	for ( int i = 0; i < ch->count; ++i )
+		orc_shape_set_param( wi, ch->shapeIds[i], code, value, 0 );
+}
+
+static float* joint_param_field( Joint* j, int code )
+{
+	int t = j->type;
+	switch ( code )
+	{
+		case F2D_JP_LOCAL_ANCHOR_AX: return &j->localOriginAnchorA.x;
+		case F2D_JP_LOCAL_ANCHOR_AY: return &j->localOriginAnchorA.y;
+		case F2D_JP_LOCAL_ANCHOR_BX: return &j->localOriginAnchorB.x;
+		case F2D_JP_LOCAL_ANCHOR_BY: return &j->localOriginAnchorB.y;
+		case F2D_JP_SPRING_HERTZ:
+			return ( t == P_JOINT_REVOLUTE || t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL || t == P_JOINT_DISTANCE ||
+					 t == P_JOINT_MOUSE )
+					   ? &j->hertz
+					   : NULL;
+		case F2D_JP_SPRING_DAMPING:
+			return ( t == P_JOINT_REVOLUTE || t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL || t == P_JOINT_DISTANCE ||
+					 t == P_JOINT_MOUSE )
+					   ? &j->dampingRatio
+					   : NULL;
+		case F2D_JP_TARGET:
+			return t == P_JOINT_REVOLUTE ? &j->targetAngle : t == P_JOINT_PRISMATIC ? &j->targetTranslation : NULL;
+		case F2D_JP_LOWER:
+			return t == P_JOINT_REVOLUTE ? &j->lowerAngle
+				   : ( t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL ) ? &j->lowerTranslation
+																		: NULL;
+		case F2D_JP_UPPER:
+			return t == P_JOINT_REVOLUTE ? &j->upperAngle
+				   : ( t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL ) ? &j->upperTranslation
+																		: NULL;
+		case F2D_JP_MOTOR_SPEED:
+			return ( t == P_JOINT_REVOLUTE || t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL || t == P_JOINT_DISTANCE )
+					   ? &j->motorSpeed
+					   : NULL;
+		case F2D_JP_MAX_MOTOR:
+			return ( t == P_JOINT_REVOLUTE || t == P_JOINT_WHEEL )		   ? &j->maxMotorTorque
+				   : ( t == P_JOINT_PRISMATIC || t == P_JOINT_DISTANCE ) ? &j->maxMotorForce
+																		   : NULL;
+		case F2D_JP_LENGTH: return t == P_JOINT_DISTANCE ? &j->length : NULL;
+		case F2D_JP_MIN_LENGTH: return t == P_JOINT_DISTANCE ? &j->minLength : NULL;
+		case F2D_JP_MAX_LENGTH: return t == P_JOINT_DISTANCE ? &j->maxLength : NULL;
+		case F2D_JP_LINEAR_HERTZ: return t == P_JOINT_WELD ? &j->linearHertz : NULL;
+		case F2D_JP_LINEAR_DAMPING: return t == P_JOINT_WELD ? &j->linearDampingRatio : NULL;
+		case F2D_JP_ANGULAR_HERTZ: return t == P_JOINT_WELD ? &j->angularHertz : NULL;
+		case F2D_JP_ANGULAR_DAMPING: return t == P_JOINT_WELD ? &j->angularDampingRatio : NULL;
+		case F2D_JP_LINEAR_OFFSET_X: return t == P_JOINT_MOTOR ? &j->linearOffset.x : NULL;
+		case F2D_JP_LINEAR_OFFSET_Y: return t == P_JOINT_MOTOR ? &j->linearOffset.y : NULL;
+		case F2D_JP_ANGULAR_OFFSET: return t == P_JOINT_MOTOR ? &j->angularOffset : NULL;
+		case F2D_JP_MAX_FORCE: return ( t == P_JOINT_MOTOR || t == P_JOINT_MOUSE ) ? &j->maxForce : NULL;
+		case F2D_JP_MAX_TORQUE: return t == P_JOINT_MOTOR ? &j->maxTorque : NULL;
+		case F2D_JP_CORRECTION: return t == P_JOINT_MOTOR ? &j->correctionFactor : NULL;
+		case F2D_JP_TARGET_X: return t == P_JOINT_MOUSE ? &j->targetA.x : NULL;
+		case F2D_JP_TARGET_Y: return t == P_JOINT_MOUSE ? &j->targetA.y : NULL;
+		default: return NULL;
+	}
+}
+
+static int* joint_param_flag( Joint* j, int code )
+{
+	int t = j->type;
+	if ( t != P_JOINT_REVOLUTE && t != P_JOINT_PRISMATIC && t != P_JOINT_WHEEL && t != P_JOINT_DISTANCE )
+		return NULL;
+	return code == F2D_JP_SPRING_ENABLED ? &j->enableSpring
+		   : code == F2D_JP_LIMIT_ENABLED ? &j->enableLimit
+		   : code == F2D_JP_MOTOR_ENABLED ? &j->enableMotor
+										  : NULL;
+}
+
+double orc_joint_get_param( int wi, int jid, int code )
+{
+	World* w = p_world( wi );
+	Joint* j = live_joint( w, jid );
+	if ( j == NULL )
+		return 0.0;
+	int t = j->type;
+	if ( code == F2D_JP_TYPE )
+	{
+		// b2JointType values (types.h)
+		static const int map[] = { -1, 5, 6, 0, 4, 7, 2, 3, 1 };
+		return t >= 0 && t <= 8 ? map[t] : -1;
+	}
+	int* flag = joint_param_flag( j, code );
+	if ( flag )
+		return *flag;
+	Body* a = w->bodies + j->bodyA;
+	Body* b = w->bodies + j->bodyB;
+	if ( code == F2D_JP_MOTOR_EFFORT )
+		return ( t == P_JOINT_REVOLUTE || t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL || t == P_JOINT_DISTANCE )
+				   ? w->inv_h * j->motorImpulse
+				   : 0.0;
+	if ( code == F2D_JP_CURRENT )
+	{
+		if ( t == P_JOINT_REVOLUTE )
+			return unwindAngle( relativeAngle( b->xf.q, a->xf.q ) - j->referenceAngle );
+		v2 pA = xfPoint( a->xf, j->localOriginAnchorA ), pB = xfPoint( b->xf, j->localOriginAnchorB );
+		if ( t == P_JOINT_DISTANCE )
+			return length( sub( pB, pA ) );
+		if ( t == P_JOINT_PRISMATIC )
+			return dot( sub( pB, pA ), rotate( a->xf.q, j->localAxisA ) );
+		return 0.0;
+	}
+	if ( code == F2D_JP_SPEED && t == P_JOINT_PRISMATIC )
+	{
+		v2 axisA = rotate( a->xf.q, j->localAxisA );
+		v2 rA = rotate( a->xf.q, sub( j->localOriginAnchorA, a->localCenter ) );
+		v2 rB = rotate( b->xf.q, sub( j->localOriginAnchorB, b->localCenter ) );
+		v2 d = add( sub( b->center, a->center ), sub( rB, rA ) );
+		int awakeA = a->setIndex == SET_AWAKE, awakeB = b->setIndex == SET_AWAKE;
+		v2 vA = awakeA ? a->v : V( 0.0f, 0.0f ), vB = awakeB ? b->v : V( 0.0f, 0.0f );
+		float wA = awakeA ? a->w : 0.0f, wB = awakeB ? b->w : 0.0f;
+		v2 vRel = sub( add( vB, crossSV( wB, rB ) ), add( vA, crossSV( wA, rA ) ) );
+		return dot( d, crossSV( wA, axisA ) ) + dot( axisA, vRel );
+	}
+	float* f = joint_param_field( j, code );
+	return f ? *f : 0.0;
+}
+
+void orc_joint_set_param( int wi, int jid, int code, double value, double value2 )
+{
+	World* w = p_world( wi );
+	Joint* j = live_joint( w, jid );
+	if ( j == NULL )
+		return;
+	int t = j->type;
+	float v = (float)value, v2 = (float)value2;
+	int* flag = joint_param_flag( j, code );
+	if ( flag )
+	{
+		int on = value != 0.0;
+		if ( *flag == on )
+			return;
+		*flag = on;
+		if ( code == F2D_JP_SPRING_ENABLED && t != P_JOINT_DISTANCE )
+			j->springImpulse = 0.0f;
+		else if ( code == F2D_JP_LIMIT_ENABLED && t != P_JOINT_DISTANCE )
+			j->lowerImpulse = j->upperImpulse = 0.0f;
+		else if ( code == F2D_JP_MOTOR_ENABLED )
+			j->motorImpulse = 0.0f;
+		return;
+	}
+	if ( code == F2D_JP_LOWER && ( t == P_JOINT_REVOLUTE || t == P_JOINT_PRISMATIC || t == P_JOINT_WHEEL ) )
+	{
+		float* lo = joint_param_field( j, F2D_JP_LOWER );
+		float* hi = joint_param_field( j, F2D_JP_UPPER );
+		if ( v != *lo || v2 != *hi )
+		{
+			*lo = fminp( v, v2 );
+			*hi = fmaxp( v, v2 );
+			j->lowerImpulse = j->upperImpulse = 0.0f;
+		}
+		return;
+	}
+	if ( t == P_JOINT_DISTANCE && ( code == F2D_JP_LENGTH || code == F2D_JP_MIN_LENGTH ) )
+	{
+		if ( code == F2D_JP_LENGTH )
+			j->length = fclampp( v, P_LINEAR_SLOP, P_HUGE );
+		else
+		{
+			float lo = fclampp( v, P_LINEAR_SLOP, P_HUGE ), hi = fclampp( v2, P_LINEAR_SLOP, P_HUGE );
+			j->minLength = fminp( lo, hi );
+			j->maxLength = fmaxp( lo, hi );
+		}
+		j->impulse = j->lowerImpulse = j->upperImpulse = 0.0f;
+		return;
+	}
+	if ( t == P_JOINT_MOTOR && code == F2D_JP_LINEAR_OFFSET_X )
+	{
+		j->linearOffset = V( v, v2 );
+		return;
+	}
+	if ( code == F2D_JP_UPPER || code == F2D_JP_MAX_LENGTH || code == F2D_JP_LINEAR_OFFSET_Y || code == F2D_JP_TARGET_X ||
+		 code == F2D_JP_TARGET_Y || ( code >= F2D_JP_LOCAL_ANCHOR_AX && code <= F2D_JP_LOCAL_ANCHOR_BY ) )
+		return;
+	float* f = joint_param_field( j, code );
+	if ( f == NULL )
+		return;
+	if ( t == P_JOINT_MOTOR && ( code == F2D_JP_MAX_FORCE || code == F2D_JP_MAX_TORQUE ) )
+		v = fmaxp( 0.0f, v );
+	else if ( t == P_JOINT_MOTOR && code == F2D_JP_CORRECTION )
+		v = fclampp( v, 0.0f, 1.0f );
+	*f = v;
+}

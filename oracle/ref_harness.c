@@ -1199,3 +1199,346 @@ void ref_destroy_chain( int w, int chain )
 	b2ChainId id = { chain + 1, world->worldId, c->generation };
 	b2DestroyChain( id );
 }
+
+// ---------------------------------------------------------------------------
+// properties: the generic get/set codes of the product's C ABI, through the
+// library's own b2Body_* / b2Shape_* / b2Chain_* / b2*Joint_* calls
+// ---------------------------------------------------------------------------
+static b2ShapeId ref_shape_id( int w, int shape )
+{
+	b2World* world = ref_world( w );
+	b2Shape* s = b2ShapeArray_Get( &world->shapes, shape );
+	b2ShapeId id = { shape + 1, world->worldId, s->generation };
+	return id;
+}
+
+static b2JointId ref_joint_id( int w, int joint )
+{
+	b2World* world = ref_world( w );
+	b2Joint* j = b2JointArray_Get( &world->joints, joint );
+	b2JointId id = { joint + 1, world->worldId, j->generation };
+	return id;
+}
+
+double ref_body_get_param( int w, int body, int code )
+{
+	b2BodyId id = ref_body_id( w, body );
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING: return b2Body_GetLinearDamping( id );
+		case F2D_BODY_ANGULAR_DAMPING: return b2Body_GetAngularDamping( id );
+		case F2D_BODY_GRAVITY_SCALE: return b2Body_GetGravityScale( id );
+		case F2D_BODY_BULLET: return b2Body_IsBullet( id );
+		case F2D_BODY_FIXED_ROTATION: return b2Body_IsFixedRotation( id );
+		case F2D_BODY_ENABLED: return b2Body_IsEnabled( id );
+		case F2D_BODY_TYPE: return (int)b2Body_GetType( id );
+		case F2D_BODY_LOCAL_CENTER_X: return b2Body_GetLocalCenterOfMass( id ).x;
+		case F2D_BODY_LOCAL_CENTER_Y: return b2Body_GetLocalCenterOfMass( id ).y;
+		case F2D_BODY_WORLD_CENTER_X: return b2Body_GetWorldCenterOfMass( id ).x;
+		case F2D_BODY_WORLD_CENTER_Y: return b2Body_GetWorldCenterOfMass( id ).y;
+		default: return 0.0;
+	}
+}
+
+void ref_body_set_param( int w, int body, int code, double value )
+{
+	b2BodyId id = ref_body_id( w, body );
+	float v = (float)value;
+	switch ( code )
+	{
+		case F2D_BODY_LINEAR_DAMPING: b2Body_SetLinearDamping( id, v ); break;
+		case F2D_BODY_ANGULAR_DAMPING: b2Body_SetAngularDamping( id, v ); break;
+		case F2D_BODY_GRAVITY_SCALE: b2Body_SetGravityScale( id, v ); break;
+		case F2D_BODY_BULLET: b2Body_SetBullet( id, value != 0.0 ); break;
+		case F2D_BODY_FIXED_ROTATION: b2Body_SetFixedRotation( id, value != 0.0 ); break;
+		default: break;
+	}
+}
+
+void ref_body_set_mass_data( int w, int body, double mass, double inertia, double cx, double cy )
+{
+	b2MassData md = { (float)mass, { (float)cx, (float)cy }, (float)inertia };
+	b2Body_SetMassData( ref_body_id( w, body ), md );
+}
+
+void ref_body_apply_mass_from_shapes( int w, int body )
+{
+	b2Body_ApplyMassFromShapes( ref_body_id( w, body ) );
+}
+
+double ref_shape_get_param( int w, int shape, int code )
+{
+	b2ShapeId id = ref_shape_id( w, shape );
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY: return b2Shape_GetDensity( id );
+		case F2D_SHAPE_FRICTION: return b2Shape_GetFriction( id );
+		case F2D_SHAPE_RESTITUTION: return b2Shape_GetRestitution( id );
+		case F2D_SHAPE_SENSOR: return b2Shape_IsSensor( id );
+		case F2D_SHAPE_SENSOR_EVENTS: return b2Shape_AreSensorEventsEnabled( id );
+		case F2D_SHAPE_CONTACT_EVENTS: return b2Shape_AreContactEventsEnabled( id );
+		case F2D_SHAPE_HIT_EVENTS: return b2Shape_AreHitEventsEnabled( id );
+		case F2D_SHAPE_PRESOLVE_EVENTS: return b2Shape_ArePreSolveEventsEnabled( id );
+		case F2D_SHAPE_CATEGORY: return (double)(int64_t)b2Shape_GetFilter( id ).categoryBits;
+		case F2D_SHAPE_MASK: return (double)(int64_t)b2Shape_GetFilter( id ).maskBits;
+		case F2D_SHAPE_GROUP: return b2Shape_GetFilter( id ).groupIndex;
+		default: return 0.0;
+	}
+}
+
+void ref_shape_set_param( int w, int shape, int code, double value, int flag )
+{
+	b2ShapeId id = ref_shape_id( w, shape );
+	float v = (float)value;
+	bool on = value != 0.0;
+	switch ( code )
+	{
+		case F2D_SHAPE_DENSITY: b2Shape_SetDensity( id, v, flag != 0 ); break;
+		case F2D_SHAPE_FRICTION: b2Shape_SetFriction( id, v ); break;
+		case F2D_SHAPE_RESTITUTION: b2Shape_SetRestitution( id, v ); break;
+		case F2D_SHAPE_SENSOR_EVENTS: b2Shape_EnableSensorEvents( id, on ); break;
+		case F2D_SHAPE_CONTACT_EVENTS: b2Shape_EnableContactEvents( id, on ); break;
+		case F2D_SHAPE_HIT_EVENTS: b2Shape_EnableHitEvents( id, on ); break;
+		case F2D_SHAPE_PRESOLVE_EVENTS: b2Shape_EnablePreSolveEvents( id, on ); break;
+		default: break;
+	}
+}
+
+void ref_shape_set_filter( int w, int shape, long long categoryBits, long long maskBits, int groupIndex )
+{
+	b2Filter f = b2DefaultFilter();
+	f.categoryBits = (uint64_t)categoryBits;
+	f.maskBits = (uint64_t)maskBits;
+	f.groupIndex = groupIndex;
+	b2Shape_SetFilter( ref_shape_id( w, shape ), f );
+}
+
+int ref_shape_test_point( int w, int shape, double x, double y )
+{
+	b2Vec2 p = { (float)x, (float)y };
+	return b2Shape_TestPoint( ref_shape_id( w, shape ), p );
+}
+
+void ref_chain_set_param( int w, int chain, int code, double value )
+{
+	b2World* world = ref_world( w );
+	b2ChainShape* c = b2ChainShapeArray_Get( &world->chainShapes, chain );
+	b2ChainId id = { chain + 1, world->worldId, c->generation };
+	if ( code == F2D_SHAPE_FRICTION )
+		b2Chain_SetFriction( id, (float)value );
+	else if ( code == F2D_SHAPE_RESTITUTION )
+		b2Chain_SetRestitution( id, (float)value );
+}
+
+double ref_joint_get_param( int w, int joint, int code )
+{
+	b2JointId id = ref_joint_id( w, joint );
+	b2JointType t = b2Joint_GetType( id );
+	switch ( code )
+	{
+		case F2D_JP_TYPE: return (int)t;
+		case F2D_JP_LOCAL_ANCHOR_AX: return b2Joint_GetLocalAnchorA( id ).x;
+		case F2D_JP_LOCAL_ANCHOR_AY: return b2Joint_GetLocalAnchorA( id ).y;
+		case F2D_JP_LOCAL_ANCHOR_BX: return b2Joint_GetLocalAnchorB( id ).x;
+		case F2D_JP_LOCAL_ANCHOR_BY: return b2Joint_GetLocalAnchorB( id ).y;
+		default: break;
+	}
+	switch ( t )
+	{
+		case b2_revoluteJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: return b2RevoluteJoint_IsSpringEnabled( id );
+				case F2D_JP_SPRING_HERTZ: return b2RevoluteJoint_GetSpringHertz( id );
+				case F2D_JP_SPRING_DAMPING: return b2RevoluteJoint_GetSpringDampingRatio( id );
+				case F2D_JP_TARGET: return b2RevoluteJoint_GetTargetAngle( id );
+				case F2D_JP_LIMIT_ENABLED: return b2RevoluteJoint_IsLimitEnabled( id );
+				case F2D_JP_LOWER: return b2RevoluteJoint_GetLowerLimit( id );
+				case F2D_JP_UPPER: return b2RevoluteJoint_GetUpperLimit( id );
+				case F2D_JP_MOTOR_ENABLED: return b2RevoluteJoint_IsMotorEnabled( id );
+				case F2D_JP_MOTOR_SPEED: return b2RevoluteJoint_GetMotorSpeed( id );
+				case F2D_JP_MAX_MOTOR: return b2RevoluteJoint_GetMaxMotorTorque( id );
+				case F2D_JP_MOTOR_EFFORT: return b2RevoluteJoint_GetMotorTorque( id );
+				case F2D_JP_CURRENT: return b2RevoluteJoint_GetAngle( id );
+			}
+			break;
+		case b2_prismaticJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: return b2PrismaticJoint_IsSpringEnabled( id );
+				case F2D_JP_SPRING_HERTZ: return b2PrismaticJoint_GetSpringHertz( id );
+				case F2D_JP_SPRING_DAMPING: return b2PrismaticJoint_GetSpringDampingRatio( id );
+				case F2D_JP_TARGET: return b2PrismaticJoint_GetTargetTranslation( id );
+				case F2D_JP_LIMIT_ENABLED: return b2PrismaticJoint_IsLimitEnabled( id );
+				case F2D_JP_LOWER: return b2PrismaticJoint_GetLowerLimit( id );
+				case F2D_JP_UPPER: return b2PrismaticJoint_GetUpperLimit( id );
+				case F2D_JP_MOTOR_ENABLED: return b2PrismaticJoint_IsMotorEnabled( id );
+				case F2D_JP_MOTOR_SPEED: return b2PrismaticJoint_GetMotorSpeed( id );
+				case F2D_JP_MAX_MOTOR: return b2PrismaticJoint_GetMaxMotorForce( id );
+				case F2D_JP_MOTOR_EFFORT: return b2PrismaticJoint_GetMotorForce( id );
+				case F2D_JP_CURRENT: return b2PrismaticJoint_GetTranslation( id );
+				case F2D_JP_SPEED: return b2PrismaticJoint_GetSpeed( id );
+			}
+			break;
+		case b2_wheelJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: return b2WheelJoint_IsSpringEnabled( id );
+				case F2D_JP_SPRING_HERTZ: return b2WheelJoint_GetSpringHertz( id );
+				case F2D_JP_SPRING_DAMPING: return b2WheelJoint_GetSpringDampingRatio( id );
+				case F2D_JP_LIMIT_ENABLED: return b2WheelJoint_IsLimitEnabled( id );
+				case F2D_JP_LOWER: return b2WheelJoint_GetLowerLimit( id );
+				case F2D_JP_UPPER: return b2WheelJoint_GetUpperLimit( id );
+				case F2D_JP_MOTOR_ENABLED: return b2WheelJoint_IsMotorEnabled( id );
+				case F2D_JP_MOTOR_SPEED: return b2WheelJoint_GetMotorSpeed( id );
+				case F2D_JP_MAX_MOTOR: return b2WheelJoint_GetMaxMotorTorque( id );
+				case F2D_JP_MOTOR_EFFORT: return b2WheelJoint_GetMotorTorque( id );
+			}
+			break;
+		case b2_distanceJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: return b2DistanceJoint_IsSpringEnabled( id );
+				case F2D_JP_SPRING_HERTZ: return b2DistanceJoint_GetSpringHertz( id );
+				case F2D_JP_SPRING_DAMPING: return b2DistanceJoint_GetSpringDampingRatio( id );
+				case F2D_JP_LIMIT_ENABLED: return b2DistanceJoint_IsLimitEnabled( id );
+				case F2D_JP_MOTOR_ENABLED: return b2DistanceJoint_IsMotorEnabled( id );
+				case F2D_JP_MOTOR_SPEED: return b2DistanceJoint_GetMotorSpeed( id );
+				case F2D_JP_MAX_MOTOR: return b2DistanceJoint_GetMaxMotorForce( id );
+				case F2D_JP_MOTOR_EFFORT: return b2DistanceJoint_GetMotorForce( id );
+				case F2D_JP_LENGTH: return b2DistanceJoint_GetLength( id );
+				case F2D_JP_MIN_LENGTH: return b2DistanceJoint_GetMinLength( id );
+				case F2D_JP_MAX_LENGTH: return b2DistanceJoint_GetMaxLength( id );
+				case F2D_JP_CURRENT: return b2DistanceJoint_GetCurrentLength( id );
+			}
+			break;
+		case b2_weldJoint:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_HERTZ: return b2WeldJoint_GetLinearHertz( id );
+				case F2D_JP_LINEAR_DAMPING: return b2WeldJoint_GetLinearDampingRatio( id );
+				case F2D_JP_ANGULAR_HERTZ: return b2WeldJoint_GetAngularHertz( id );
+				case F2D_JP_ANGULAR_DAMPING: return b2WeldJoint_GetAngularDampingRatio( id );
+			}
+			break;
+		case b2_motorJoint:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_OFFSET_X: return b2MotorJoint_GetLinearOffset( id ).x;
+				case F2D_JP_LINEAR_OFFSET_Y: return b2MotorJoint_GetLinearOffset( id ).y;
+				case F2D_JP_ANGULAR_OFFSET: return b2MotorJoint_GetAngularOffset( id );
+				case F2D_JP_MAX_FORCE: return b2MotorJoint_GetMaxForce( id );
+				case F2D_JP_MAX_TORQUE: return b2MotorJoint_GetMaxTorque( id );
+				case F2D_JP_CORRECTION: return b2MotorJoint_GetCorrectionFactor( id );
+			}
+			break;
+		case b2_mouseJoint:
+			switch ( code )
+			{
+				case F2D_JP_TARGET_X: return b2MouseJoint_GetTarget( id ).x;
+				case F2D_JP_TARGET_Y: return b2MouseJoint_GetTarget( id ).y;
+				case F2D_JP_SPRING_HERTZ: return b2MouseJoint_GetSpringHertz( id );
+				case F2D_JP_SPRING_DAMPING: return b2MouseJoint_GetSpringDampingRatio( id );
+				case F2D_JP_MAX_FORCE: return b2MouseJoint_GetMaxForce( id );
+			}
+			break;
+		default:
+			break;
+	}
+	return 0.0;
+}
+
+void ref_joint_set_param( int w, int joint, int code, double value, double value2 )
+{
+	b2JointId id = ref_joint_id( w, joint );
+	b2JointType t = b2Joint_GetType( id );
+	float v = (float)value, v2 = (float)value2;
+	bool on = value != 0.0;
+	switch ( t )
+	{
+		case b2_revoluteJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: b2RevoluteJoint_EnableSpring( id, on ); break;
+				case F2D_JP_SPRING_HERTZ: b2RevoluteJoint_SetSpringHertz( id, v ); break;
+				case F2D_JP_SPRING_DAMPING: b2RevoluteJoint_SetSpringDampingRatio( id, v ); break;
+				case F2D_JP_TARGET: b2RevoluteJoint_SetTargetAngle( id, v ); break;
+				case F2D_JP_LIMIT_ENABLED: b2RevoluteJoint_EnableLimit( id, on ); break;
+				case F2D_JP_LOWER: b2RevoluteJoint_SetLimits( id, v, v2 ); break;
+				case F2D_JP_MOTOR_ENABLED: b2RevoluteJoint_EnableMotor( id, on ); break;
+				case F2D_JP_MOTOR_SPEED: b2RevoluteJoint_SetMotorSpeed( id, v ); break;
+				case F2D_JP_MAX_MOTOR: b2RevoluteJoint_SetMaxMotorTorque( id, v ); break;
+			}
+			break;
+		case b2_prismaticJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: b2PrismaticJoint_EnableSpring( id, on ); break;
+				case F2D_JP_SPRING_HERTZ: b2PrismaticJoint_SetSpringHertz( id, v ); break;
+				case F2D_JP_SPRING_DAMPING: b2PrismaticJoint_SetSpringDampingRatio( id, v ); break;
+				case F2D_JP_TARGET: b2PrismaticJoint_SetTargetTranslation( id, v ); break;
+				case F2D_JP_LIMIT_ENABLED: b2PrismaticJoint_EnableLimit( id, on ); break;
+				case F2D_JP_LOWER: b2PrismaticJoint_SetLimits( id, v, v2 ); break;
+				case F2D_JP_MOTOR_ENABLED: b2PrismaticJoint_EnableMotor( id, on ); break;
+				case F2D_JP_MOTOR_SPEED: b2PrismaticJoint_SetMotorSpeed( id, v ); break;
+				case F2D_JP_MAX_MOTOR: b2PrismaticJoint_SetMaxMotorForce( id, v ); break;
+			}
+			break;
+		case b2_wheelJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: b2WheelJoint_EnableSpring( id, on ); break;
+				case F2D_JP_SPRING_HERTZ: b2WheelJoint_SetSpringHertz( id, v ); break;
+				case F2D_JP_SPRING_DAMPING: b2WheelJoint_SetSpringDampingRatio( id, v ); break;
+				case F2D_JP_LIMIT_ENABLED: b2WheelJoint_EnableLimit( id, on ); break;
+				case F2D_JP_LOWER: b2WheelJoint_SetLimits( id, v, v2 ); break;
+				case F2D_JP_MOTOR_ENABLED: b2WheelJoint_EnableMotor( id, on ); break;
+				case F2D_JP_MOTOR_SPEED: b2WheelJoint_SetMotorSpeed( id, v ); break;
+				case F2D_JP_MAX_MOTOR: b2WheelJoint_SetMaxMotorTorque( id, v ); break;
+			}
+			break;
+		case b2_distanceJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_ENABLED: b2DistanceJoint_EnableSpring( id, on ); break;
+				case F2D_JP_SPRING_HERTZ: b2DistanceJoint_SetSpringHertz( id, v ); break;
+				case F2D_JP_SPRING_DAMPING: b2DistanceJoint_SetSpringDampingRatio( id, v ); break;
+				case F2D_JP_LIMIT_ENABLED: b2DistanceJoint_EnableLimit( id, on ); break;
+				case F2D_JP_MOTOR_ENABLED: b2DistanceJoint_EnableMotor( id, on ); break;
+				case F2D_JP_MOTOR_SPEED: b2DistanceJoint_SetMotorSpeed( id, v ); break;
+				case F2D_JP_MAX_MOTOR: b2DistanceJoint_SetMaxMotorForce( id, v ); break;
+				case F2D_JP_LENGTH: b2DistanceJoint_SetLength( id, v ); break;
+				case F2D_JP_MIN_LENGTH: b2DistanceJoint_SetLengthRange( id, v, v2 ); break;
+			}
+			break;
+		case b2_weldJoint:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_HERTZ: b2WeldJoint_SetLinearHertz( id, v ); break;
+				case F2D_JP_LINEAR_DAMPING: b2WeldJoint_SetLinearDampingRatio( id, v ); break;
+				case F2D_JP_ANGULAR_HERTZ: b2WeldJoint_SetAngularHertz( id, v ); break;
+				case F2D_JP_ANGULAR_DAMPING: b2WeldJoint_SetAngularDampingRatio( id, v ); break;
+			}
+			break;
+		case b2_motorJoint:
+			switch ( code )
+			{
+				case F2D_JP_LINEAR_OFFSET_X: b2MotorJoint_SetLinearOffset( id, ( b2Vec2 ){ v, v2 } ); break;
+				case F2D_JP_ANGULAR_OFFSET: b2MotorJoint_SetAngularOffset( id, v ); break;
+				case F2D_JP_MAX_FORCE: b2MotorJoint_SetMaxForce( id, v ); break;
+				case F2D_JP_MAX_TORQUE: b2MotorJoint_SetMaxTorque( id, v ); break;
+				case F2D_JP_CORRECTION: b2MotorJoint_SetCorrectionFactor( id, v ); break;
+			}
+			break;
+		case b2_mouseJoint:
+			switch ( code )
+			{
+				case F2D_JP_SPRING_HERTZ: b2MouseJoint_SetSpringHertz( id, v ); break;
+				case F2D_JP_SPRING_DAMPING: b2MouseJoint_SetSpringDampingRatio( id, v ); break;
+				case F2D_JP_MAX_FORCE: b2MouseJoint_SetMaxForce( id, v ); break;
+			}
+			break;
+		default:
+			break;
+	}
+}

@@ -162,3 +162,173 @@ def destroy_script(world, f, ids):
     elif f == 110:
         world.destroy_body(ids["last"])
         world.destroy_shape(ids["twin_box"], False)
+
+
+class _JointCounter:
+    """Builder proxy that counts the joints created through it."""
+
+    def __init__(self, b):
+        self.b, self.joints = b, 0
+
+    def create_joint(self, d):
+        self.joints += 1
+        return self.b.create_joint(d)
+
+    def create_revolute(self, d):
+        self.joints += 1
+        return self.b.create_revolute(d)
+
+    def __getattr__(self, name):
+        return getattr(self.b, name)
+
+
+def build_property_scene(w):
+    """Every joint type (weld and distance rigs, prismatic / wheel / motor /
+    mouse / filter rigs, revolute gallery) side by side over one ground, a
+    small mixed pile and a chain strip, for the property script. Returns
+    (bodies, joints)."""
+    from forge2d_gb300 import scenes
+    c = _JointCounter(w)
+    scenes.joint_zoo(c, copies=2)
+    scenes.joint_rigs(scenes._PileOffset(c, 0.0, 40.0), copies=2)
+    scenes.joint_gallery(scenes._PileOffset(c, 0.0, 80.0), copies=2)
+    scenes.pile(scenes._PileOffset(c, 150.0, 0.0), count=120, seed=11, width=20.0, height=30.0)
+    ground = w.create_body(scenes.body_def(type=0, positionX=-120.0, positionY=-3.0))
+    w.create_chain(ground, [(-20.0, 0.0), (-10.0, -1.0), (0.0, 0.0), (10.0, -1.0), (20.0, 0.0)])
+    return len(w.bodies()), c.joints
+
+
+# codes read back from every joint after the script's edits
+JOINT_READS = ("F2D_JP_TYPE", "F2D_JP_LOCAL_ANCHOR_AX", "F2D_JP_LOCAL_ANCHOR_BY", "F2D_JP_SPRING_ENABLED",
+               "F2D_JP_SPRING_HERTZ", "F2D_JP_SPRING_DAMPING", "F2D_JP_TARGET", "F2D_JP_LIMIT_ENABLED",
+               "F2D_JP_LOWER", "F2D_JP_UPPER", "F2D_JP_MOTOR_ENABLED", "F2D_JP_MOTOR_SPEED", "F2D_JP_MAX_MOTOR",
+               "F2D_JP_MOTOR_EFFORT", "F2D_JP_LENGTH", "F2D_JP_MIN_LENGTH", "F2D_JP_MAX_LENGTH", "F2D_JP_CURRENT",
+               "F2D_JP_SPEED", "F2D_JP_LINEAR_HERTZ", "F2D_JP_LINEAR_DAMPING", "F2D_JP_ANGULAR_HERTZ",
+               "F2D_JP_ANGULAR_DAMPING", "F2D_JP_LINEAR_OFFSET_X", "F2D_JP_LINEAR_OFFSET_Y",
+               "F2D_JP_ANGULAR_OFFSET", "F2D_JP_MAX_FORCE", "F2D_JP_MAX_TORQUE", "F2D_JP_CORRECTION",
+               "F2D_JP_TARGET_X", "F2D_JP_TARGET_Y")
+BODY_READS = ("F2D_BODY_LINEAR_DAMPING", "F2D_BODY_ANGULAR_DAMPING", "F2D_BODY_GRAVITY_SCALE", "F2D_BODY_BULLET",
+              "F2D_BODY_FIXED_ROTATION", "F2D_BODY_ENABLED", "F2D_BODY_TYPE", "F2D_BODY_LOCAL_CENTER_X",
+              "F2D_BODY_LOCAL_CENTER_Y", "F2D_BODY_WORLD_CENTER_X", "F2D_BODY_WORLD_CENTER_Y")
+SHAPE_READS = ("F2D_SHAPE_DENSITY", "F2D_SHAPE_FRICTION", "F2D_SHAPE_RESTITUTION", "F2D_SHAPE_SENSOR",
+               "F2D_SHAPE_SENSOR_EVENTS", "F2D_SHAPE_CONTACT_EVENTS", "F2D_SHAPE_HIT_EVENTS",
+               "F2D_SHAPE_PRESOLVE_EVENTS", "F2D_SHAPE_CATEGORY", "F2D_SHAPE_MASK", "F2D_SHAPE_GROUP")
+
+
+def property_reads(world, nb, ns, nj):
+    """Every getter code of every body, shape and joint (a flat list)."""
+    out = []
+    for b in range(nb):
+        out += [world.body_get(b, c) for c in BODY_READS]
+    for s in range(ns):
+        out += [world.shape_get(s, c) for c in SHAPE_READS]
+    for j in range(nj):
+        out += [world.joint_get(j, c) for c in JOINT_READS]
+    return out
+
+
+def property_script(world, f, nb, nj):
+    """Setters of every kind between steps, the same calls on every world:
+    joint springs, limits, motors, targets, lengths, offsets and stiffness
+    by type; body damping, gravity scale, bullet, fixed rotation and mass
+    data; shape friction, restitution, density, event flags and filters;
+    chain friction. Bodies are picked among the dynamic ones by index."""
+    if f == 20:
+        for j in range(nj):
+            t = int(world.joint_get(j, "F2D_JP_TYPE"))
+            if t == 5:  # revolute
+                world.joint_set(j, "F2D_JP_SPRING_ENABLED", 1)
+                world.joint_set(j, "F2D_JP_SPRING_HERTZ", 2.5)
+                world.joint_set(j, "F2D_JP_SPRING_DAMPING", 0.4)
+                world.joint_set(j, "F2D_JP_TARGET", 0.3)
+                world.joint_set(j, "F2D_JP_LIMIT_ENABLED", 1)
+                world.joint_set(j, "F2D_JP_LOWER", 0.6, -0.4)
+            elif t == 4:  # prismatic
+                world.joint_set(j, "F2D_JP_SPRING_ENABLED", 1 - world.joint_get(j, "F2D_JP_SPRING_ENABLED"))
+                world.joint_set(j, "F2D_JP_SPRING_HERTZ", 2.0)
+                world.joint_set(j, "F2D_JP_TARGET", 0.5)
+                world.joint_set(j, "F2D_JP_LOWER", -1.0, 2.0)
+                world.joint_set(j, "F2D_JP_MOTOR_SPEED", -0.5)
+                world.joint_set(j, "F2D_JP_MAX_MOTOR", 40.0)
+            elif t == 7:  # wheel
+                world.joint_set(j, "F2D_JP_SPRING_HERTZ", 6.0)
+                world.joint_set(j, "F2D_JP_SPRING_DAMPING", 0.9)
+                world.joint_set(j, "F2D_JP_LOWER", -0.3, 0.2)
+                world.joint_set(j, "F2D_JP_MOTOR_SPEED", 3.0)
+                world.joint_set(j, "F2D_JP_MAX_MOTOR", 12.0)
+            elif t == 0:  # distance
+                world.joint_set(j, "F2D_JP_LENGTH", 2.5)
+                world.joint_set(j, "F2D_JP_MIN_LENGTH", 3.2, 1.2)
+                world.joint_set(j, "F2D_JP_SPRING_ENABLED", 1 - world.joint_get(j, "F2D_JP_SPRING_ENABLED"))
+                world.joint_set(j, "F2D_JP_SPRING_HERTZ", 3.0)
+                world.joint_set(j, "F2D_JP_MOTOR_SPEED", -1.0)
+            elif t == 6:  # weld
+                world.joint_set(j, "F2D_JP_LINEAR_HERTZ", 4.0)
+                world.joint_set(j, "F2D_JP_LINEAR_DAMPING", 0.3)
+                world.joint_set(j, "F2D_JP_ANGULAR_HERTZ", 2.0)
+                world.joint_set(j, "F2D_JP_ANGULAR_DAMPING", 0.8)
+            elif t == 2:  # motor
+                world.joint_set(j, "F2D_JP_LINEAR_OFFSET_X", world.joint_get(j, "F2D_JP_LINEAR_OFFSET_X") - 2.0, 3.0)
+                world.joint_set(j, "F2D_JP_ANGULAR_OFFSET", -0.4)
+                world.joint_set(j, "F2D_JP_MAX_FORCE", 50.0)
+                world.joint_set(j, "F2D_JP_MAX_TORQUE", -5.0)  # clamped to 0
+                world.joint_set(j, "F2D_JP_CORRECTION", 1.5)  # clamped to 1
+            elif t == 3:  # mouse
+                world.joint_set(j, "F2D_JP_SPRING_HERTZ", 3.0)
+                world.joint_set(j, "F2D_JP_SPRING_DAMPING", 0.5)
+                world.joint_set(j, "F2D_JP_MAX_FORCE", 150.0)
+    dyn = [b for b in range(nb) if int(world.body_get(b, "F2D_BODY_TYPE")) == 2]
+    if f == 30:
+        for j in range(nj):
+            t = int(world.joint_get(j, "F2D_JP_TYPE"))
+            if t in (4, 5, 7, 0):
+                world.joint_set(j, "F2D_JP_MOTOR_ENABLED", 1 - world.joint_get(j, "F2D_JP_MOTOR_ENABLED"))
+            if t in (4, 7):
+                world.joint_set(j, "F2D_JP_LIMIT_ENABLED", 1 - world.joint_get(j, "F2D_JP_LIMIT_ENABLED"))
+        world.body_set(dyn[3], "F2D_BODY_LINEAR_DAMPING", 0.5)
+        world.body_set(dyn[4], "F2D_BODY_ANGULAR_DAMPING", 0.3)
+        world.body_set(dyn[5], "F2D_BODY_GRAVITY_SCALE", -0.5)
+        world.body_set(dyn[6], "F2D_BODY_BULLET", 1)
+        world.body_set(dyn[-7], "F2D_BODY_FIXED_ROTATION", 1)
+        world.body_set_mass_data(dyn[-9], 4.0, 1.5, 0.1, -0.05)
+    if f == 40:
+        ns = len(world.shapes()[1])
+        pile_shapes = range(ns - 130, ns - 10)
+        for k, s in enumerate(pile_shapes):
+            if k % 7 == 0:
+                world.shape_set(s, "F2D_SHAPE_FRICTION", 0.1)
+            if k % 7 == 1:
+                world.shape_set(s, "F2D_SHAPE_RESTITUTION", 0.7)
+            if k % 7 == 2:
+                world.shape_set(s, "F2D_SHAPE_DENSITY", 3.0, 1)
+            if k % 7 == 3:
+                world.shape_set(s, "F2D_SHAPE_CONTACT_EVENTS", 1)
+                world.shape_set(s, "F2D_SHAPE_HIT_EVENTS", 1)
+            if k % 7 == 4:
+                world.shape_set_filter(s, 2, -1, 0)  # new category: proxy re-created
+            if k % 7 == 5:
+                world.shape_set_filter(s, 1, ~2, 0)  # mask only: proxy moves
+            if k % 7 == 6:
+                world.shape_set(s, "F2D_SHAPE_DENSITY", 0.5, 0)
+        world.chain_set(0, "F2D_SHAPE_FRICTION", 0.05)
+    if f == 60:
+        world.body_set(dyn[-7], "F2D_BODY_FIXED_ROTATION", 0)
+        world.body_apply_mass_from_shapes(dyn[-9])
+        for j in range(nj):
+            if int(world.joint_get(j, "F2D_JP_TYPE")) == 5:
+                world.joint_set(j, "F2D_JP_LOWER", -0.4, 0.6)  # the same bounds: no change
+                world.joint_set(j, "F2D_JP_LIMIT_ENABLED", 0)
+
+
+def point_answers(world):
+    """b2Shape_TestPoint of every third shape at a point near its body's
+    origin (the answers, in shape order)."""
+    bodies = world.bodies()
+    _, sh = world.shapes()
+    out = []
+    for s in range(0, len(sh), 3):
+        b = int(sh[s, 1])
+        if b < 0:
+            continue
+        out.append(world.shape_test_point(s, float(bodies[b, 0]) + 0.25, float(bodies[b, 1]) - 0.1))
+    return out

@@ -16,9 +16,9 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import (blast, compare_contacts, destroy_script, edit_motors, filter_rule, install_callbacks,
-                    new_contacts, touching_pair,
-                    pre_solve_rule, ray_answers)
+from parity import (blast, build_property_scene, compare_contacts, destroy_script, edit_motors, filter_rule,
+                    install_callbacks, new_contacts, pre_solve_rule, property_reads, property_script, ray_answers,
+                    point_answers, touching_pair)
 
 
 def trees_equal(ref, port):
@@ -465,3 +465,36 @@ def test_port_destroy_path_with_reference(ref_lib, port_lib, sleep):
     assert ends > 0
     ref.close()
     port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_properties_with_reference(ref_lib, port_lib, sleep):
+    """The generic property calls: joint setters of every type (springs,
+    limits, motors, targets, lengths, offsets, stiffness; impulses cleared
+    as the reference clears them), body damping / gravity scale / bullet /
+    fixed rotation / mass data, shape friction / restitution / density /
+    event flags / filters (proxies re-created or moved), chain friction.
+    Bodies, contacts, colours, every getter and shape point tests agree bit
+    for bit in lock step."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    nb, nj = build_property_scene(ref)
+    assert build_property_scene(port) == (nb, nj)
+    ns = len(ref.shapes()[1])
+    for f in range(1, 101):
+        property_script(ref, f, nb, nj)
+        property_script(port, f, nb, nj)
+        lockstep_full(ref, port, 1, start=f)
+        assert np.array_equal(ref.end_events(), port.end_events()), f
+        if f % 10 == 0:
+            assert compare_contacts(ref, port) == [], f
+            assert np.array_equal(ref.color_counts(), port.color_counts()), f
+            a = np.array(property_reads(ref, nb, ns, nj), np.float64)
+            b = np.array(property_reads(port, nb, ns, nj), np.float64)
+            bad = np.flatnonzero(a.view(np.uint64) != b.view(np.uint64))
+            assert len(bad) == 0, (f, bad[:5], a[bad[:5]], b[bad[:5]])
+            assert point_answers(ref) == point_answers(port), f
+    ref.close()
+    port.close()
+
