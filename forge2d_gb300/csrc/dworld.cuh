@@ -288,6 +288,11 @@ struct DIslands
 	int moveCount;
 	int splitCandidate;
 	int error;
+	// state changes: 1 when a contact that began touching wakes a sleeping
+	// set (the step's changes then run serially), and the per-contact marks
+	// of the parallel unlink (bit 0 island list, bit 1 body edge lists)
+	int serialOps;
+	unsigned char* cRemoved;
 };
 
 // Solver view of one body: velocity and the substep position/rotation

@@ -311,7 +311,8 @@ __global__ void __launch_bounds__( OPS_TILE ) k_op_outputs( DWorld w, const int*
 		isBegin = kind == 1 && ( f & CF_EVENTS );
 		isEnd = ( kind == 2 || ( kind == 0 && ( f & CF_TOUCHING ) ) ) && ( f & CF_EVENTS );
 		// the serial island path maintains the overflow array itself
-		isOvf = !serialGraph && gkind[k] != OP_NONE && w.opColor[k] == F2D_OVERFLOW;
+		bool serial = serialGraph || ( w.isl && w.isl->serialOps );
+		isOvf = !serial && gkind[k] != OP_NONE && w.opColor[k] == F2D_OVERFLOW;
 	}
 	// per-tile counts stay below 2^16: two counters per scanned int
 	int t01, t23;
@@ -586,16 +587,11 @@ void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st )
 	int* ovOps = s.tmpA + cap; // reuses the pending flags once the rounds are done
 	int g = grid_for( w.opCap );
 	k_op_prepare<<<g, 256, 0, st>>>( w, gkind );
+	// sleeping worlds: island links and unlinks (island.cu); a step whose
+	// changes wake a sleeping set applies them serially there, colours
+	// included, and leaves no op for the rounds below
 	if ( w.isl )
-	{
-		// sleeping worlds: the state changes run serially with their island
-		// links and the wakes they cause (island.cu)
 		launch_isl_ops( w, st, gkind, s.scanState );
-		cudaMemsetAsync( w.opScan, 0, sizeof( unsigned long long ) * (size_t)OPS_SCAN_WORDS( w.opCap ), st );
-		k_op_outputs<<<( w.opCap + OPS_TILE - 1 ) / OPS_TILE, OPS_TILE, 0, st>>>( w, gkind, ovOps, 1 );
-		k_overflow_ops<<<1, GRAPH_THREADS, 0, st>>>( w, gkind, ovOps );
-		return;
-	}
 	k_op_lock<<<g, 256, 0, st>>>( w );
 	k_op_round<<<g, 256, 0, st>>>( w, gkind, pending );
 	scan_lookback( pending, pos, &w.sc->opCount, 0, w.opCap, &w.sc->pendingOps, s.scanState, &w.sc->error, st );

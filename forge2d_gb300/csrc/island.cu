@@ -988,14 +988,38 @@ __global__ void k_isl_new_contacts( DWorld w, DIslands* Ip, int planMode )
 // The step's contact state changes in contact-id order (world.c:586-686)
 // with island links, unlinks and the wakes they cause, then the island
 // merge that opens b2Solve (solver.c:1194-1199).
+// A contact that begins touching between an awake and a sleeping body wakes
+// the sleeping set inside the serial loop (island.c:116-130), and the woken
+// contacts enter the colour graph between the step's own changes: such a
+// step keeps the whole serial form below. Any other step colours in
+// parallel (graph.cu) and takes the island changes apart: unlinks as one
+// set removal (their order does not change the lists: removing and
+// prepending commute), links serially.
+__global__ void k_isl_op_check( DWorld w, DIslands* Ip )
+{
+	const DIslands& I = *Ip;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		if ( w.opKind[k] != 1 )
+			continue;
+		int2 bd = w.cbody[w.opContact[k]];
+		if ( I.bSet[bd.x] >= SET_FIRST_SLEEPING || I.bSet[bd.y] >= SET_FIRST_SLEEPING )
+			atomicOr( &Ip->serialOps, 1 );
+	}
+}
+
 __global__ void k_isl_ops( DWorld w, DIslands* Ip, const int* gkind )
 {
 	DIslands& I = *Ip;
+	if ( I.serialOps == 0 )
+		return;
 	int nOps = w.sc->opCount;
 	if ( nOps > w.opCap )
 		nOps = w.opCap;
 	for ( int k = 0; k < nOps; ++k )
 	{
+		w.opDone[k] = 1; // nothing left for the parallel colouring
 		int c = w.opContact[k];
 		int kind = w.opKind[k];
 		if ( kind == 0 )
@@ -1226,9 +1250,139 @@ static void isl_list( DWorld& w, unsigned long long* scanState, cudaStream_t st 
 	k_isl_list<<<grid_for( w.bodyCap ), 256, 0, st>>>( w.isl, count );
 }
 
+// parallel form, step 1: mark the contacts that leave an island list (end
+// of touching, destroy) and the body edge lists (destroy)
+__global__ void k_isl_unlink_mark( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		int kind = w.opKind[k];
+		if ( kind == 1 )
+			continue;
+		int c = w.opContact[k];
+		int m = ( I.cIsland[c] != ISL_NULL ? 1 : 0 ) | ( kind == 0 ? 2 : 0 );
+		I.cRemoved[c] = (unsigned char)m;
+	}
+}
+
+// step 2: every maximal run of marked nodes is cut out by the thread of its
+// first node (the one whose predecessor stays): predecessor and successor
+// are joined, or the list's head / tail moves. Each boundary field has one
+// writer; the marked nodes keep their links until step 3.
+__global__ void k_isl_unlink_runs( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		int kind = w.opKind[k];
+		if ( kind == 1 )
+			continue;
+		int c = w.opContact[k];
+		int m = I.cRemoved[c];
+		if ( m & 1 )
+		{
+			int prev = I.cIslandPrev[c];
+			if ( prev == ISL_NULL || ( I.cRemoved[prev] & 1 ) == 0 )
+			{
+				int next = I.cIslandNext[c];
+				for ( int g = 0; next != ISL_NULL && ( I.cRemoved[next] & 1 ) && g < I.contactCap; ++g )
+					next = I.cIslandNext[next];
+				DIsland& isl = I.islands[I.cIsland[c]];
+				if ( prev != ISL_NULL )
+					I.cIslandNext[prev] = next;
+				else
+					isl.headContact = next;
+				if ( next != ISL_NULL )
+					I.cIslandPrev[next] = prev;
+				else
+					isl.tailContact = prev;
+			}
+		}
+		if ( m & 2 )
+		{
+			int2 bd = w.cbody[c];
+			for ( int edge = 0; edge < 2; ++edge )
+			{
+				int4 e = I.cEdge[c];
+				int prev = edge == 0 ? e.x : e.z;
+				if ( prev != ISL_NULL && ( I.cRemoved[prev >> 1] & 2 ) )
+					continue;
+				int next = edge == 0 ? e.y : e.w;
+				for ( int g = 0; next != ISL_NULL && ( I.cRemoved[next >> 1] & 2 ) && g < 2 * I.contactCap; ++g )
+				{
+					int4 ne = I.cEdge[next >> 1];
+					next = ( next & 1 ) ? ne.w : ne.y;
+				}
+				if ( prev != ISL_NULL )
+					( (int*)( I.cEdge + ( prev >> 1 ) ) )[( prev & 1 ) ? 3 : 1] = next;
+				else
+					I.bHeadContact[edge == 0 ? bd.x : bd.y] = next;
+				if ( next != ISL_NULL )
+					( (int*)( I.cEdge + ( next >> 1 ) ) )[( next & 1 ) ? 2 : 0] = prev;
+			}
+		}
+	}
+}
+
+// step 3: the marked nodes leave (island counts: island.c:221-261)
+__global__ void k_isl_unlink_clear( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		if ( w.opKind[k] == 1 )
+			continue;
+		int c = w.opContact[k];
+		int m = I.cRemoved[c];
+		if ( m & 1 )
+		{
+			DIsland* isl = I.islands + I.cIsland[c];
+			atomicSub( &isl->contactCount, 1 );
+			atomicAdd( &isl->removeCount, 1 );
+			I.cIsland[c] = I.cIslandPrev[c] = I.cIslandNext[c] = ISL_NULL;
+		}
+		if ( m & 2 )
+			I.cEdge[c] = make_int4( ISL_NULL, ISL_NULL, ISL_NULL, ISL_NULL );
+		I.cRemoved[c] = 0;
+	}
+}
+
+// step 4: the contacts that began touching link their islands in op order
+__global__ void k_isl_link_serial( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = 0; k < nOps; ++k )
+		if ( w.opKind[k] == 1 )
+		{
+			int c = w.opContact[k];
+			w.cflags[c] |= CF_TOUCHING;
+			isl_link_contact( w, I, c );
+		}
+}
+
 void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long long* scanState )
 {
+	int g = grid_for( w.opCap );
+	cudaMemsetAsync( (char*)w.isl + offsetof( DIslands, serialOps ), 0, sizeof( int ), st );
+	k_isl_op_check<<<g, 256, 0, st>>>( w, w.isl );
 	k_isl_ops<<<1, 1, 0, st>>>( w, w.isl, gkind );
+	k_isl_unlink_mark<<<g, 256, 0, st>>>( w, w.isl );
+	k_isl_unlink_runs<<<g, 256, 0, st>>>( w, w.isl );
+	k_isl_unlink_clear<<<g, 256, 0, st>>>( w, w.isl );
+	k_isl_link_serial<<<1, 1, 0, st>>>( w, w.isl );
 	k_isl_merge_roots<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, w.isl );
 	isl_list( w, scanState, st );
 	k_isl_merge_apply<<<1, 1, 0, st>>>( w.isl );

@@ -459,6 +459,7 @@ static void isl_ensure( HostWorld* W )
 		dgrow( h.cMark, oc, nc );
 		dgrow( h.cEdge, oc, nc );
 		dgrow( h.order, 0, nc );
+		dgrow( h.cRemoved, 0, nc );
 		h.contactCap = (int)nc;
 	}
 	if ( oj != nj )
@@ -506,6 +507,8 @@ static void isl_free( HostWorld* W )
 			cudaFree( h.cEdge );
 		if ( h.islandBits )
 			cudaFree( h.islandBits );
+		if ( h.cRemoved )
+			cudaFree( h.cRemoved );
 		cudaFree( W->islDev );
 	}
 	W->islDev = nullptr;
