@@ -293,6 +293,10 @@ struct DIslands
 	// of the parallel unlink (bit 0 island list, bit 1 body edge lists)
 	int serialOps;
 	unsigned char* cRemoved;
+	// new contacts' body edges sorted by (body, creation rank): keys and
+	// their capacity (2 x the new-pair capacity)
+	unsigned long long *ncKeys, *ncKeysAlt;
+	int ncCap, ncCount;
 };
 
 // Solver view of one body: velocity and the substep position/rotation
@@ -452,6 +456,7 @@ struct DWorld
 	DIslands* isl;  // islands and solver sets (sleeping worlds only, else null)
 	int* islFlag;	// device copies of isl->flag and isl->pos (scan arguments)
 	int* islPos;
+	unsigned long long *islNcKeys, *islNcKeysAlt; // copies of isl->ncKeys, ncKeysAlt (sort arguments)
 	int* ovfOwner; // bodyCap
 	int* ovfLevel; // contactCap + jointCap
 	int* ovfOrder; // contactCap + jointCap

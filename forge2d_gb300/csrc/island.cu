@@ -1232,9 +1232,122 @@ void launch_isl_create( DWorld& w, cudaStream_t st )
 	k_isl_create<<<1, 1, 0, st>>>( w, w.isl );
 }
 
-void launch_isl_new_contacts( DWorld& w, cudaStream_t st, int planMode )
+// Native order in parallel: the new contacts are the first newPairCount ids
+// the pool hands out (LIFO free ids, then fresh ones), those created in
+// creation order; their set records start in parallel and their body edges,
+// sorted by (body, creation rank), are prepended in rank order per body --
+// the list the serial prepends (contact.c:227-262) give.
+__global__ void k_isl_nc_flags( DWorld w, int* ids, int* flag )
 {
-	k_isl_new_contacts<<<1, 1, 0, st>>>( w, w.isl, planMode );
+	int n = min( w.sc->newPairCount, w.pairCap );
+	int F = w.sc->contactFreeCount;
+	int base = w.sc->contactIdCount;
+	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
+	{
+		int id = r < F ? w.contactFree[F - 1 - r] : base + ( r - F );
+		bool ok = id >= 0 && id < w.contactCap && ( w.cflags[id] & CF_USED ) != 0;
+		ids[r] = id;
+		flag[r] = ok ? 1 : 0;
+	}
+}
+
+__global__ void k_isl_nc_init( DWorld w, DIslands* Ip, const int* ids, const int* flag, const int* pos )
+{
+	DIslands& I = *Ip;
+	int n = min( w.sc->newPairCount, w.pairCap );
+	for ( int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x )
+	{
+		if ( !flag[r] )
+			continue;
+		int i = pos[r];
+		int c = ids[r];
+		I.order[i] = c;
+		int2 bd = w.cbody[c];
+		bool awake = I.bSet[bd.x] == SET_AWAKE || I.bSet[bd.y] == SET_AWAKE;
+		I.cSet[c] = awake ? SET_AWAKE : SET_DISABLED;
+		I.cIsland[c] = I.cIslandPrev[c] = I.cIslandNext[c] = ISL_NULL;
+		I.cMark[c] = 0;
+		if ( !awake )
+			w.cflags[c] |= CF_INACTIVE;
+		I.ncKeys[2 * i] = ( (unsigned long long)(unsigned)bd.x << 32 ) | (unsigned)( 2 * i );
+		I.ncKeys[2 * i + 1] = ( (unsigned long long)(unsigned)bd.y << 32 ) | (unsigned)( 2 * i + 1 );
+	}
+	if ( blockIdx.x == 0 && threadIdx.x == 0 )
+		I.ncCount = 2 * ( n > 0 ? pos[n - 1] + flag[n - 1] : 0 );
+}
+
+// edge key of sorted row p: (contact << 1) | edge
+__device__ __forceinline__ int nc_edge_key( const DIslands& I, unsigned long long k )
+{
+	int idx = (int)( k & 0xffffffffull );
+	return ( I.order[idx >> 1] << 1 ) | ( idx & 1 );
+}
+
+__global__ void k_isl_nc_chain( DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.ncCount;
+	for ( int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+	{
+		unsigned long long k = I.ncKeys[p];
+		unsigned b = (unsigned)( k >> 32 );
+		int key = nc_edge_key( I, k );
+		bool first = p == 0 || (unsigned)( I.ncKeys[p - 1] >> 32 ) != b;
+		bool last = p + 1 == n || (unsigned)( I.ncKeys[p + 1] >> 32 ) != b;
+		int next, prev = last ? ISL_NULL : nc_edge_key( I, I.ncKeys[p + 1] );
+		if ( first )
+		{
+			next = I.bHeadContact[b];
+			if ( next != ISL_NULL )
+				( (int*)( I.cEdge + ( next >> 1 ) ) )[( next & 1 ) ? 2 : 0] = key;
+		}
+		else
+			next = nc_edge_key( I, I.ncKeys[p - 1] );
+		int* e = (int*)( I.cEdge + ( key >> 1 ) );
+		e[( key & 1 ) ? 3 : 1] = next;
+		e[( key & 1 ) ? 2 : 0] = prev;
+	}
+}
+
+__global__ void k_isl_nc_heads( DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	int n = I.ncCount;
+	for ( int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+	{
+		unsigned long long k = I.ncKeys[p];
+		unsigned b = (unsigned)( k >> 32 );
+		if ( p + 1 == n || (unsigned)( I.ncKeys[p + 1] >> 32 ) != b )
+			I.bHeadContact[b] = nc_edge_key( I, k );
+	}
+}
+
+void launch_isl_new_contacts( DWorld& w, StepScratch& s, cudaStream_t st, int planMode )
+{
+	if ( planMode )
+	{
+		k_isl_new_contacts<<<1, 1, 0, st>>>( w, w.isl, planMode );
+		return;
+	}
+	DIslands* I = w.isl;
+	int* ids = s.tmpA;
+	int* flag = s.tmpA + w.pairCap;
+	int* pos = s.tmpB;
+	int g = grid_for( w.pairCap );
+	k_isl_nc_flags<<<g, 256, 0, st>>>( w, ids, flag );
+	scan_lookback( flag, pos, &w.sc->newPairCount, 0, w.pairCap, nullptr, s.scanState, &w.sc->error, st );
+	k_isl_nc_init<<<g, 256, 0, st>>>( w, I, ids, flag, pos );
+	int bodyBits = 1;
+	while ( ( 1 << bodyBits ) < w.bodyCap )
+		bodyBits += 1;
+	int* count = (int*)( (char*)I + offsetof( DIslands, ncCount ) );
+	unsigned long long* k0 = w.islNcKeys;
+	unsigned long long* k1 = w.islNcKeysAlt;
+	sort_coop<unsigned long long>( k0, nullptr, k1, nullptr, count, 32 + bodyBits, w.sortHist, &w.sc->barrierCount,
+								   &w.sc->error, s.sortBlocks64, st );
+	int g2 = grid_for( 2 * w.pairCap );
+	k_isl_nc_chain<<<g2, 256, 0, st>>>( I );
+	k_isl_nc_heads<<<g2, 256, 0, st>>>( I );
 }
 
 static int* isl_field( DIslands* I, size_t offset )

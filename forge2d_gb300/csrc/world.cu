@@ -402,7 +402,7 @@ static void isl_ensure( HostWorld* W )
 	DIslands& h = W->islHost;
 	bool fresh = W->islDev == nullptr;
 	if ( !fresh && h.bodyCap == d.bodyCap && h.contactCap == d.contactCap && h.jointCap == d.jointCap &&
-		 h.logCap >= d.bodyCap + d.jointCap )
+		 h.logCap >= d.bodyCap + d.jointCap && h.ncCap >= 2 * d.pairCap )
 		return;
 	cudaStreamSynchronize( W->stream );
 	if ( fresh )
@@ -473,6 +473,14 @@ static void isl_ensure( HostWorld* W )
 		dgrow( h.jOverflowIndex, oj, nj );
 		h.jointCap = (int)nj;
 	}
+	if ( h.ncCap < 2 * d.pairCap )
+	{
+		dfree( h.ncKeys );
+		dfree( h.ncKeysAlt );
+		dgrow( h.ncKeys, 0, 2 * (size_t)d.pairCap );
+		dgrow( h.ncKeysAlt, 0, 2 * (size_t)d.pairCap );
+		h.ncCap = 2 * d.pairCap;
+	}
 	if ( h.logCap < d.bodyCap + d.jointCap )
 	{
 		dfree( h.log );
@@ -483,6 +491,8 @@ static void isl_ensure( HostWorld* W )
 	d.isl = W->islDev;
 	d.islFlag = h.flag;
 	d.islPos = h.pos;
+	d.islNcKeys = h.ncKeys;
+	d.islNcKeysAlt = h.ncKeysAlt;
 	W->graphDirty = true;
 }
 
@@ -509,11 +519,16 @@ static void isl_free( HostWorld* W )
 			cudaFree( h.islandBits );
 		if ( h.cRemoved )
 			cudaFree( h.cRemoved );
+		if ( h.ncKeys )
+			cudaFree( h.ncKeys );
+		if ( h.ncKeysAlt )
+			cudaFree( h.ncKeysAlt );
 		cudaFree( W->islDev );
 	}
 	W->islDev = nullptr;
 	W->d.isl = nullptr;
 	W->d.islFlag = W->d.islPos = nullptr;
+	W->d.islNcKeys = W->d.islNcKeysAlt = nullptr;
 	memset( &h, 0, sizeof( h ) );
 }
 
