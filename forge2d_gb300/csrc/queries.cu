@@ -7,9 +7,10 @@
 // per shape over the device rows: every candidate is tested against the full
 // ray and the closest hit is picked with one 64-bit atomicMin on
 // (fraction bits, shape id), so ties resolve to the lower shape id.
-// Shape ray casts follow geometry.c:506-760 (circle, capsule, segment,
-// polygon with zero radius).
+// Shape ray casts follow geometry.c:506-888 (circle, capsule, segment,
+// polygon; a rounded polygon by the shape cast of distance.c:608-697).
 #include "dmath.cuh"
+#include "dtoi.cuh"
 #include "dworld.cuh"
 #include "kernels.cuh"
 
@@ -181,8 +182,71 @@ __device__ RayHit ray_segment_sided( fv2 origin, fv2 translation, fv2 p1, fv2 p2
 	return ray_segment( origin, translation, 1.0f, p1, p2 );
 }
 
+// geometry.c:879-888 + distance.c:608-697 b2ShapeCast: the ray's origin
+// advances conservatively on the GJK distance (radii off) to the rounded
+// polygon until it is within the radius; an initial overlap reports the
+// midpoint of the two closest points at fraction 0
+__device__ RayHit ray_rounded_polygon( fv2 origin, fv2 d, float maxFraction, const float4* g )
+{
+	RayHit out;
+	out.hit = false;
+	out.fraction = 0.0f;
+	out.point = out.normal = mk( 0.0f, 0.0f );
+	DProxy pa;
+	for ( int i = 0; i < 4; ++i )
+	{
+		float4 a = g[2 + i];
+		pa.p[2 * i] = mk( a.x, a.y );
+		pa.p[2 * i + 1] = mk( a.z, a.w );
+	}
+	pa.count = __float_as_int( g[1].y );
+	pa.radius = g[1].x;
+	DProxy pb;
+	pb.p[0] = origin;
+	pb.count = 1;
+	pb.radius = 0.0f;
+	float target = fmax_s( F2D_LINEAR_SLOP, pa.radius + pb.radius - F2D_LINEAR_SLOP );
+	float tolerance = 0.25f * F2D_LINEAR_SLOP;
+	DCache cache;
+	cache.count = 0;
+	fxf xfA;
+	xfA.p = mk( 0.0f, 0.0f );
+	xfA.q.c = 1.0f;
+	xfA.q.s = 0.0f;
+	fxf xfB = xfA;
+	float fraction = 0.0f;
+	for ( int iteration = 0; iteration < 20; ++iteration )
+	{
+		fv2 pA = mk( 0.0f, 0.0f ), pB = mk( 0.0f, 0.0f ), n = mk( 0.0f, 0.0f );
+		float dist = gjk_distance( pa, pb, xfA, xfB, cache, &pA, &pB, &n );
+		if ( dist < target + tolerance )
+		{
+			out.hit = true;
+			if ( iteration == 0 )
+			{
+				out.point = vlerp( vmuladd( pA, pa.radius, n ), vmuladd( pB, -pb.radius, n ), 0.5f );
+				return out;
+			}
+			out.fraction = fraction;
+			out.point = vmuladd( pA, pa.radius, n );
+			out.normal = n;
+			return out;
+		}
+		float den = vdot( d, n );
+		if ( den >= 0.0f )
+			return out;
+		fraction += ( target - dist ) / den;
+		if ( fraction >= maxFraction )
+			return out;
+		xfB.p = vmuladd( mk( 0.0f, 0.0f ), fraction, d );
+	}
+	return out;
+}
+
 __device__ RayHit ray_polygon( fv2 origin, fv2 d, float maxFraction, const float4* g )
 {
+	if ( g[1].x != 0.0f )
+		return ray_rounded_polygon( origin, d, maxFraction, g );
 	RayHit out;
 	out.hit = false;
 	out.fraction = 0.0f;

@@ -208,6 +208,51 @@ static CastOut ray_polygon( v2 origin, v2 d, float maxFraction, const Polygon* p
 	return o;
 }
 
+// geometry.c:879-888 + distance.c:608-697 b2ShapeCast: a ray against a
+// rounded polygon advances the origin conservatively on the GJK distance
+// (radii off) until it is within the radius
+static CastOut ray_rounded_polygon( v2 origin, v2 d, float maxFraction, const Polygon* poly )
+{
+	CastOut o = cast_none();
+	ShapeProxy pa = p_make_proxy( poly->vertices, poly->count, poly->radius );
+	ShapeProxy pb = p_make_proxy( &origin, 1, 0.0f );
+	float target = fmaxp( P_LINEAR_SLOP, pa.radius + pb.radius - P_LINEAR_SLOP );
+	float tolerance = 0.25f * P_LINEAR_SLOP;
+	SimplexCache cache = { 0 };
+	xform xfA = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+	xform xfB = xfA;
+	float fraction = 0.0f;
+	for ( int iteration = 0; iteration < 20; ++iteration )
+	{
+		v2 pA = V( 0.0f, 0.0f ), pB = V( 0.0f, 0.0f ), n = V( 0.0f, 0.0f );
+		float dist = p_shape_distance( &pa, &pb, xfA, xfB, &cache, &pA, &pB, &n );
+		if ( dist < target + tolerance )
+		{
+			o.hit = 1;
+			if ( iteration == 0 )
+			{
+				// initial overlap: a common point
+				v2 c1 = mulAdd( pA, pa.radius, n );
+				v2 c2 = mulAdd( pB, -pb.radius, n );
+				o.point = lerp( c1, c2, 0.5f );
+				return o;
+			}
+			o.fraction = fraction;
+			o.point = mulAdd( pA, pa.radius, n );
+			o.normal = n;
+			return o;
+		}
+		float den = dot( d, n );
+		if ( den >= 0.0f )
+			return o;
+		fraction += ( target - dist ) / den;
+		if ( fraction >= maxFraction )
+			return o;
+		xfB.p = mulAdd( V( 0.0f, 0.0f ), fraction, d );
+	}
+	return o;
+}
+
 static int query_collide( const Shape* s, uint64_t cat, uint64_t mask )
 {
 	return ( s->categoryBits & mask ) != 0 && ( s->maskBits & cat ) != 0;
@@ -238,8 +283,9 @@ static CastOut ray_shape( const Shape* s, xform xf, v2 origin, v2 translation )
 			break;
 		case SHAPE_POLYGON:
 			if ( s->g.poly.radius != 0.0f )
-				return cast_none(); // rounded polygons take the shape-cast path, not restated
-			o = ray_polygon( lo, lt, 1.0f, &s->g.poly );
+				o = ray_rounded_polygon( lo, lt, 1.0f, &s->g.poly );
+			else
+				o = ray_polygon( lo, lt, 1.0f, &s->g.poly );
 			break;
 		default:
 			return cast_none();

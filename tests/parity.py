@@ -332,3 +332,27 @@ def point_answers(world):
             continue
         out.append(world.shape_test_point(s, float(bodies[b, 0]) + 0.25, float(bodies[b, 1]) - 0.1))
     return out
+
+
+def rounded_scene(w):
+    """Rounded boxes and rounded polygons over a rounded ground, for ray
+    casts that take the shape-cast path (geometry.c:879-888)."""
+    from forge2d_gb300 import scenes
+    rng = np.random.default_rng(21)
+    ground = w.create_body(scenes.body_def(type=0, positionY=-1.0))
+    w.create_box(ground, scenes.shape_def(), 20.0, 0.5, radius=0.25)
+    for k in range(48):
+        b = w.create_body(scenes.body_def(type=2, positionX=float(rng.uniform(-15, 15)),
+                                          positionY=float(rng.uniform(1, 12))))
+        r = float(rng.uniform(0.05, 0.3))
+        if k % 2 == 0:
+            w.create_box(b, scenes.shape_def(), float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.2, 0.6)), radius=r)
+        else:
+            ang = np.sort(rng.uniform(0, 2 * np.pi, 5))
+            pts = [(0.5 * np.cos(a), 0.5 * np.sin(a)) for a in ang]
+            w.create_polygon(b, scenes.shape_def(), pts, radius=r)
+
+
+def rounded_rays(n=200, seed=4):
+    rng = np.random.default_rng(seed)
+    return [(rng.uniform(-18, 18, 2) + [0.0, 6.0], rng.uniform(-20, 20, 2)) for _ in range(n)]

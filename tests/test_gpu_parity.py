@@ -18,7 +18,7 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import blast, compare_contacts, edit_motors, install_callbacks, ray_answers
+from parity import blast, compare_contacts, edit_motors, install_callbacks, ray_answers, rounded_rays, rounded_scene
 from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
                                 replay, sensor_rows)
 
@@ -181,6 +181,23 @@ def test_gpu_cast_ray_callback_matches_port(gpu_lib, port_lib):
         p.step(1.0 / 60.0, 4)
     rng = np.random.default_rng(1)
     rays = [(rng.uniform(-20, 20, 2) + [0.0, 15.0], rng.uniform(-30, 30, 2)) for _ in range(150)]
+    assert ray_answers(g, rays) == ray_answers(p, rays)
+    g.close()
+    p.close()
+
+
+def test_gpu_rounded_polygon_rays_match_port(gpu_lib, port_lib):
+    """Rays against rounded boxes and polygons (the shape-cast path) on the
+    GPU against the oracle."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (g, p):
+        rounded_scene(w)
+    for _ in range(40):
+        g.step(1.0 / 60.0, 4)
+        p.step(1.0 / 60.0, 4)
+    rays = rounded_rays()
     assert ray_answers(g, rays) == ray_answers(p, rays)
     g.close()
     p.close()

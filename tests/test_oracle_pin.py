@@ -18,7 +18,7 @@ from forge2d_gb300 import scenes
 
 from parity import (blast, build_property_scene, compare_contacts, destroy_script, edit_motors, filter_rule,
                     install_callbacks, new_contacts, pre_solve_rule, property_reads, property_script, ray_answers,
-                    point_answers, touching_pair)
+                    point_answers, rounded_rays, rounded_scene, touching_pair)
 
 
 def trees_equal(ref, port):
@@ -498,3 +498,21 @@ def test_port_properties_with_reference(ref_lib, port_lib, sleep):
     ref.close()
     port.close()
 
+
+
+def test_port_rounded_polygon_rays_with_reference(ref_lib, port_lib):
+    """Rays against rounded boxes and polygons take the reference's shape
+    cast (conservative advancement on GJK distance): closest and all hits,
+    points, normals and fractions bit for bit."""
+    wkw = dict(enableSleep=0, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        rounded_scene(w)
+    lockstep_full(ref, port, 40)
+    rays = rounded_rays()
+    a, b = ray_answers(ref, rays), ray_answers(port, rays)
+    assert a == b
+    assert sum(len(x[1]) for x in a) > 100
+    ref.close()
+    port.close()
