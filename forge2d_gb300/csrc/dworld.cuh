@@ -135,7 +135,7 @@ struct DScalars
 	int hostMoveCount;
 	// partial rebuild of one tree: active, gathered nodes, large segments
 	// per level (two levels in flight), small segments
-	int rbActive, rbCount, rbLarge[2], rbSmall;
+	int rbActive, rbCount, rbLarge[2], rbSmall, rbRefresh;
 	// creation stamp of the next new contact (the bodies' contact lists are
 	// newest first); non-static bodies in the awake set (worlds without
 	// island records); destroy calls: collected contacts, end events
@@ -196,6 +196,7 @@ struct DRebuild
 	int* segBounds; // per large segment: centre bounds as ordered ints
 	int* segBelow;	// per large segment: centres below the pivot
 	int* pairBase;	// per large segment: first swap pair
+	int* rfStart;	// children of the large levels the bottom-up pass starts from
 };
 
 // ---------------------------------------------------------------------------

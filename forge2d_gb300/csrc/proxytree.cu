@@ -250,6 +250,7 @@ __global__ void k_pt_mark( DWorld w, int t )
 		w.sc->rbLarge[0] = 0;
 		w.sc->rbLarge[1] = 0;
 		w.sc->rbSmall = 0;
+		w.sc->rbRefresh = 0;
 	}
 }
 
@@ -695,6 +696,12 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 			T.child2[node] = right;
 			T.parent[left] = node;
 			T.parent[right] = node;
+			// children the bottom-up pass starts from: single gathered nodes and
+			// the roots of small segments (their inner nodes are done in k_pt_small)
+			if ( le - ls <= PT_SMALL )
+				__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), left );
+			if ( re - le <= PT_SMALL )
+				__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), right );
 			if ( le - ls >= 2 )
 			{
 				int4 v = make_int4( ls, le, c1 + 1, 0 );
@@ -718,15 +725,51 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 }
 
 // Segments of at most PT_SMALL nodes: one block each, in shared memory,
-// level by level with one warp per sub-segment.
+// level by level: one warp partitions each sub-segment, then one thread per
+// sub-segment links its node. The internal nodes of a segment of n gathered
+// nodes entered with c1 child1 edges above take the n - 1 freed slots from
+// position start + c1 on (each sub-segment (s, c1) takes s + c1, its left
+// part from s + c1 + 1, its right part from its split + c1), so those ids
+// are staged in shared memory first.
+// shared memory of k_pt_small (dynamic: more than the static 48 KB)
+#define PT_SMALL_LEVELS 64
+struct PtSmall
+{
+	int idx[PT_SMALL];
+	float2 cen[PT_SMALL];
+	int bl[PT_SMALL];
+	int br[PT_SMALL];
+	int freed[PT_SMALL];
+	int4 item[2][PT_SMALL / 2];
+	int split[PT_SMALL / 2];
+	int4 kid[PT_SMALL]; // (node, child1, child2, -) in creation order
+	int levelStart[PT_SMALL_LEVELS + 1];
+	int count[2];
+	int kidCount;
+};
+
+// a new internal node from its two children (dynamic_tree.c:1990-2010)
+__device__ __forceinline__ void pt_refresh_node( const DProxyTree& T, int p, int a, int b )
+{
+	T.box[p] = pt_union( __ldcg( T.box + a ), __ldcg( T.box + b ) );
+	T.height[p] = 1 + max( __ldcg( T.height + a ), __ldcg( T.height + b ) );
+	T.cat[p] = __ldcg( T.cat + a ) | __ldcg( T.cat + b );
+	T.leaves[p] = __ldcg( T.leaves + a ) + __ldcg( T.leaves + b );
+	T.flags[p] = PT_ALLOCATED;
+}
+
 __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 {
-	__shared__ int sIdx[PT_SMALL];
-	__shared__ float2 sCen[PT_SMALL];
-	__shared__ int sBL[PT_SMALL];
-	__shared__ int sBR[PT_SMALL];
-	__shared__ int4 sItem[2][PT_SMALL / 2];
-	__shared__ int sCount[2];
+	extern __shared__ __align__( 16 ) unsigned char ptSmem[];
+	PtSmall& sm = *reinterpret_cast<PtSmall*>( ptSmem );
+	int* sIdx = sm.idx;
+	float2* sCen = sm.cen;
+	int* sBL = sm.bl;
+	int* sBR = sm.br;
+	int* sFreed = sm.freed;
+	int4( *sItem )[PT_SMALL / 2] = sm.item;
+	int* sSplit = sm.split;
+	int* sCount = sm.count;
 	DScalars* sc = w.sc;
 	if ( sc->rbActive == 0 )
 		return;
@@ -739,29 +782,36 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 	for ( int q = blockIdx.x; q < S; q += gridDim.x )
 	{
 		int4 sg = R.segSmall[q];
-		int gs = sg.x, n = sg.y - sg.x;
+		int gs = sg.x, n = sg.y - sg.x, z = sg.z;
 		for ( int i = threadIdx.x; i < n; i += blockDim.x )
 		{
 			sIdx[i] = R.gIdx[gs + i];
 			sCen[i] = R.gCen[gs + i];
+			if ( i < n - 1 )
+				sFreed[i] = R.freed[F - 1 - ( gs + z + i )];
 		}
 		if ( threadIdx.x == 0 )
 		{
-			sItem[0][0] = make_int4( 0, n, sg.z, 0 );
+			sItem[0][0] = make_int4( 0, n, z, 0 );
 			sCount[0] = 1;
 			sCount[1] = 0;
+			sm.kidCount = 0;
 		}
 		__syncthreads();
-		for ( int level = 0; level < 64; ++level )
+		int levels = 0;
+		for ( int level = 0; level < PT_SMALL_LEVELS; ++level )
 		{
 			int cur = level & 1;
 			int m = sCount[cur];
 			if ( m == 0 )
 				break;
+			if ( threadIdx.x == 0 )
+				sm.levelStart[level] = sm.kidCount;
+			levels = level + 1;
 			for ( int it = wid; it < m; it += PT_WARPS )
 			{
 				int4 item = sItem[cur][it];
-				int s = item.x, e = item.y, c1 = item.z, cnt = e - s;
+				int s = item.x, e = item.y, cnt = e - s;
 				int split = 1;
 				if ( cnt > 2 )
 				{
@@ -834,33 +884,57 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 					}
 				}
 				if ( lane == 0 )
+					sSplit[it] = split;
+			}
+			__syncthreads();
+			// link the level's nodes, queue the parts of two or more
+			for ( int it = threadIdx.x; it < m; it += blockDim.x )
+			{
+				int4 item = sItem[cur][it];
+				int s = item.x, e = item.y, c1 = item.z;
+				int le = s + sSplit[it];
+				int kn = s + c1 - z, kl = s + c1 + 1 - z, kr = le + c1 - z;
+				if ( kn < 0 || kn >= n - 1 || ( le - s > 1 && ( kl < 0 || kl >= n - 1 ) ) ||
+					 ( e - le > 1 && ( kr < 0 || kr >= n - 1 ) ) || le <= s || le >= e )
 				{
-					int node = R.freed[F - 1 - ( gs + s + c1 )];
-					int le = s + split;
-					int left = le - s == 1 ? sIdx[s] : R.freed[F - 1 - ( gs + s + c1 + 1 )];
-					int right = e - le == 1 ? sIdx[le] : R.freed[F - 1 - ( gs + le + c1 )];
-					T.child1[node] = left;
-					T.child2[node] = right;
-					T.parent[left] = node;
-					T.parent[right] = node;
-					if ( le - s >= 2 )
-						sItem[cur ^ 1][atomicAdd( &sCount[cur ^ 1], 1 )] = make_int4( s, le, c1 + 1, 0 );
-					if ( e - le >= 2 )
-						sItem[cur ^ 1][atomicAdd( &sCount[cur ^ 1], 1 )] = make_int4( le, e, c1, 0 );
+					atomicOr( &sc->error, ERR_TREE );
+					continue;
 				}
-				__syncwarp();
+				int node = sFreed[kn];
+				int left = le - s == 1 ? sIdx[s] : sFreed[kl];
+				int right = e - le == 1 ? sIdx[le] : sFreed[kr];
+				T.child1[node] = left;
+				T.child2[node] = right;
+				T.parent[left] = node;
+				T.parent[right] = node;
+				sm.kid[atomicAdd( &sm.kidCount, 1 )] = make_int4( node, left, right, 0 );
+				if ( le - s >= 2 )
+					sItem[cur ^ 1][atomicAdd( &sCount[cur ^ 1], 1 )] = make_int4( s, le, c1 + 1, 0 );
+				if ( e - le >= 2 )
+					sItem[cur ^ 1][atomicAdd( &sCount[cur ^ 1], 1 )] = make_int4( le, e, c1, 0 );
 			}
 			__syncthreads();
 			if ( threadIdx.x == 0 )
 				sCount[cur] = 0;
 			__syncthreads();
 		}
+		if ( threadIdx.x == 0 )
+			sm.levelStart[levels] = sm.kidCount;
 		__syncthreads();
+		// boxes, heights, categories and leaf counts bottom up, a level at a
+		// time (the children of a level were written before the barrier)
+		for ( int level = levels - 1; level >= 0; --level )
+		{
+			int k0 = sm.levelStart[level], k1 = sm.levelStart[level + 1];
+			for ( int k = k0 + threadIdx.x; k < k1; k += blockDim.x )
+				pt_refresh_node( T, sm.kid[k].x, sm.kid[k].y, sm.kid[k].z );
+			__syncthreads();
+		}
 	}
 }
 
-// boxes, categories, heights and leaf counts of the new internal nodes,
-// bottom up (the second child to arrive computes its parent)
+// boxes, categories, heights and leaf counts of the large levels' new
+// internal nodes, bottom up (the second child to arrive computes its parent)
 __global__ void k_pt_refresh( DWorld w, int t )
 {
 	if ( w.sc->rbActive == 0 )
@@ -874,9 +948,11 @@ __global__ void k_pt_refresh( DWorld w, int t )
 		T.parent[root] = -1;
 		w.sc->treeRoot[t] = root;
 	}
-	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+	// the large levels' nodes only: k_pt_small did the nodes below them
+	int starts = w.sc->rbRefresh;
+	for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < starts; i += gridDim.x * blockDim.x )
 	{
-		int c = R.gIdx[i];
+		int c = R.rfStart[i];
 		for ( int guard = 0;; ++guard )
 		{
 			if ( guard > PT_GUARD )
@@ -892,12 +968,7 @@ __global__ void k_pt_refresh( DWorld w, int t )
 			}
 			if ( pt_atom_add( R.cnt + p, 1 ) == 0 )
 				break;
-			int a = T.child1[p], b = T.child2[p];
-			T.box[p] = pt_union( __ldcg( T.box + a ), __ldcg( T.box + b ) );
-			T.height[p] = 1 + max( __ldcg( T.height + a ), __ldcg( T.height + b ) );
-			T.cat[p] = __ldcg( T.cat + a ) | __ldcg( T.cat + b );
-			T.leaves[p] = __ldcg( T.leaves + a ) + __ldcg( T.leaves + b );
-			T.flags[p] = PT_ALLOCATED;
+			pt_refresh_node( T, p, T.child1[p], T.child2[p] );
 			__threadfence();
 			if ( p == root )
 				break;
@@ -944,6 +1015,7 @@ __global__ void k_pt_ranks( DWorld w, int t, int onlyAfterRebuild )
 // ---------------------------------------------------------------------------
 int pt_large_blocks()
 {
+	cudaFuncSetAttribute( k_pt_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof( PtSmall ) );
 	int perSM = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_pt_large, PT_THREADS, 0 );
 	int dev = 0, sms = 0;
@@ -988,7 +1060,7 @@ void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 			void* args[] = { &w, &t, &counter };
 			cudaLaunchCooperativeKernel( (void*)k_pt_large, dim3( s.ptBlocks ), dim3( PT_THREADS ), args, 0, st );
 		}
-		k_pt_small<<<F2D_SMS * 4, PT_THREADS, 0, st>>>( w, t );
+		k_pt_small<<<F2D_SMS * 2, PT_THREADS, sizeof( PtSmall ), st>>>( w, t );
 		k_pt_refresh<<<g, 256, 0, st>>>( w, t );
 	}
 }

@@ -828,6 +828,7 @@ static void rb_free( DRebuild& R )
 	dfree( R.segBounds );
 	dfree( R.segBelow );
 	dfree( R.pairBase );
+	dfree( R.rfStart );
 	R.cap = 0;
 }
 
@@ -859,6 +860,7 @@ static void rb_ensure( HostWorld* W, int cap )
 	dgrow( R.segBounds, 0, 4 * (size_t)R.segCap );
 	dgrow( R.segBelow, 0, (size_t)R.segCap );
 	dgrow( R.pairBase, 0, (size_t)R.segCap + 1 );
+	dgrow( R.rfStart, 0, n / 2 + 8 );
 	R.cap = cap;
 	W->graphDirty = true;
 }
