@@ -371,6 +371,9 @@ __global__ void k_pt_gather( DWorld w, int t )
 		else
 		{
 			R.segA[0] = make_int4( 0, n, 0, 0 );
+			R.segBounds[0] = R.segBounds[1] = INT_MAX;
+			R.segBounds[2] = R.segBounds[3] = INT_MIN;
+			R.segBelow[0] = 0;
 			w.sc->rbLarge[0] = 1;
 		}
 	}
@@ -383,6 +386,21 @@ __device__ __forceinline__ int pt_find( const int* base, int count, int x )
 	{
 		int mid = ( lo + hi + 1 ) >> 1;
 		if ( __ldcg( base + mid ) <= x )
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+// the same search over a shared-memory array
+__device__ __forceinline__ int pt_find_s( const int* base, int count, int x )
+{
+	int lo = 0, hi = count - 1;
+	while ( lo < hi )
+	{
+		int mid = ( lo + hi + 1 ) >> 1;
+		if ( base[mid] <= x )
 			lo = mid;
 		else
 			hi = mid - 1;
@@ -448,10 +466,59 @@ __device__ __forceinline__ int block_excl( int v, int* red, int* total )
 }
 
 // Median-split levels of the segments larger than PT_SMALL: one cooperative
-// launch, the whole grid on each level (see the file comment).
+// launch, the whole grid on each level, four grid barriers a level:
+//   A  every block derives the level's segments from the last level's
+//      splits (deterministic, in shared memory), links the last level's
+//      nodes (its share of them), and accumulates the centre bounds;
+//   B  centres below each pivot, per chunk;
+//   C  each misplaced centre's rank: left of the split and not below from
+//      the left, right of it and below from the right (chunk offsets follow
+//      from the per-chunk counts, as only the chunk holding the split mixes
+//      both sides);
+//   D  the k-th misplaced left centre swaps with the k-th misplaced right one
+//      (b2PartitionMid's swaps in closed form).
+// Accumulators are double-buffered by level parity; a level resets the next
+// level's after its last reader has passed a barrier.
+#define PT_LMAX 2048
+struct PtLarge
+{
+	int4 seg[2][PT_LMAX];
+	int chunkBase[PT_LMAX + 1];
+	int pairBase[PT_LMAX + 1];
+	int red[4 * PT_WARPS];
+	int count[2];
+};
+
+// exclusive prefix of vals[0..L) into out[0..L] (out[L] = total), whole block
+template <typename F>
+__device__ __forceinline__ void pt_block_prefix( int L, F value, int* out, int* red )
+{
+	int carry = 0;
+	for ( int base = 0; base < L; base += PT_THREADS )
+	{
+		int j = base + threadIdx.x;
+		int v = j < L ? value( j ) : 0;
+		int total;
+		int ex = block_excl( v, red, &total );
+		if ( j < L )
+			out[j] = carry + ex;
+		carry += total;
+		__syncthreads();
+	}
+	if ( threadIdx.x == 0 )
+		out[L] = carry;
+	__syncthreads();
+}
+
+__device__ __forceinline__ int pt_split( int n, int below )
+{
+	return ( below == 0 || below == n ) ? n / 2 : below;
+}
+
 __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, unsigned* counter )
 {
-	__shared__ int red[4 * PT_WARPS];
+	extern __shared__ __align__( 16 ) unsigned char ptSmemL[];
+	PtLarge& sm = *reinterpret_cast<PtLarge*>( ptSmemL );
 	DScalars* sc = w.sc;
 	if ( __ldcg( &sc->rbActive ) == 0 || __ldcg( &sc->rbLarge[0] ) == 0 )
 		return;
@@ -459,50 +526,93 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 	const DRebuild R = w.rb;
 	const int tid = threadIdx.x;
 	const int F = __ldcg( &sc->rbCount ) - 1;
+	const int SC = R.segCap;
 	unsigned epoch = 0;
+	if ( tid == 0 )
+	{
+		sm.seg[0][0] = __ldcg( R.segA );
+		sm.count[0] = 1;
+	}
+	__syncthreads();
 	for ( int level = 0; level < 64; ++level )
 	{
-		const int cur = level & 1;
-		const int L = __ldcg( &sc->rbLarge[cur] );
-		if ( L == 0 )
-			break;
-		int4* seg = cur ? R.segB : R.segA;
-		int4* nxt = cur ? R.segA : R.segB;
-		// chunks of each segment, accumulators cleared
-		if ( blockIdx.x == 0 )
+		const int cur = level & 1, prv = cur ^ 1;
+		int* bounds = R.segBounds + 4 * SC * cur;
+		int* belowAcc = R.segBelow + SC * cur;
+		// ---- A: this level's segments, the last level's links, bounds ----
+		if ( level > 0 )
 		{
-			for ( int j = tid; j < L; j += blockDim.x )
+			const int Lp = sm.count[prv];
+			const int* belowPrev = R.segBelow + SC * prv;
+			pt_block_prefix(
+				Lp,
+				[&]( int j ) {
+					int4 sg = sm.seg[prv][j];
+					int n = sg.y - sg.x, split = pt_split( n, __ldcg( belowPrev + j ) );
+					return ( split > PT_SMALL ? 1 : 0 ) + ( n - split > PT_SMALL ? 1 : 0 );
+				},
+				sm.pairBase, sm.red );
+			for ( int j = tid; j < Lp; j += PT_THREADS )
 			{
-				__stcg( R.segBounds + 4 * j + 0, INT_MAX );
-				__stcg( R.segBounds + 4 * j + 1, INT_MAX );
-				__stcg( R.segBounds + 4 * j + 2, INT_MIN );
-				__stcg( R.segBounds + 4 * j + 3, INT_MIN );
-				__stcg( R.segBelow + j, 0 );
+				int4 sg = sm.seg[prv][j];
+				int n = sg.y - sg.x, split = pt_split( n, __ldcg( belowPrev + j ) );
+				int o = sm.pairBase[j];
+				if ( o + 2 > PT_LMAX )
+					continue;
+				if ( split > PT_SMALL )
+					sm.seg[cur][o++] = make_int4( sg.x, sg.x + split, sg.z + 1, 0 );
+				if ( n - split > PT_SMALL )
+					sm.seg[cur][o] = make_int4( sg.x + split, sg.y, sg.z, 0 );
 			}
 			if ( tid == 0 )
+				sm.count[cur] = sm.pairBase[Lp];
+			// link the last level's nodes (this block's share)
+			for ( int j = blockIdx.x * PT_THREADS + tid; j < Lp; j += gridDim.x * PT_THREADS )
 			{
-				int base = 0;
-				for ( int j = 0; j < L; ++j )
-				{
-					int4 s = __ldcg( seg + j );
-					__stcg( R.chunkBase + j, base );
-					base += ( s.y - s.x + PT_CHUNK - 1 ) / PT_CHUNK;
-				}
-				__stcg( R.chunkBase + L, base );
-				__stcg( &sc->rbLarge[cur ^ 1], 0 );
+				int4 sg = sm.seg[prv][j];
+				int n = sg.y - sg.x, split = pt_split( n, __ldcg( belowPrev + j ) );
+				int c1 = sg.z;
+				int node = R.freed[F - 1 - ( sg.x + c1 )];
+				int ls = sg.x, le = sg.x + split, re = sg.y;
+				int left = le - ls == 1 ? __ldcg( R.gIdx + ls ) : R.freed[F - 1 - ( ls + c1 + 1 )];
+				int right = re - le == 1 ? __ldcg( R.gIdx + le ) : R.freed[F - 1 - ( le + c1 )];
+				T.child1[node] = left;
+				T.child2[node] = right;
+				T.parent[left] = node;
+				T.parent[right] = node;
+				// children the bottom-up pass starts from: single gathered nodes
+				// and the roots of small segments (k_pt_small does their inside)
+				if ( le - ls <= PT_SMALL )
+					__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), left );
+				if ( re - le <= PT_SMALL )
+					__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), right );
+				if ( le - ls >= 2 && le - ls <= PT_SMALL )
+					__stcg( R.segSmall + atomicAdd( &sc->rbSmall, 1 ), make_int4( ls, le, c1 + 1, 0 ) );
+				if ( re - le >= 2 && re - le <= PT_SMALL )
+					__stcg( R.segSmall + atomicAdd( &sc->rbSmall, 1 ), make_int4( le, re, c1, 0 ) );
+			}
+			__syncthreads();
+			if ( sm.pairBase[Lp] > PT_LMAX )
+			{
+				if ( blockIdx.x == 0 && tid == 0 )
+					atomicOr( &sc->error, ERR_TREE );
+				return;
 			}
 		}
-		if ( !grid_barrier( counter, &sc->error, epoch ) )
-			return;
-		const int C = __ldcg( R.chunkBase + L );
-		// centre bounds per segment
+		const int L = sm.count[cur];
+		if ( L == 0 )
+			return; // all blocks see the same count
+		pt_block_prefix(
+			L, [&]( int j ) { return ( sm.seg[cur][j].y - sm.seg[cur][j].x + PT_CHUNK - 1 ) / PT_CHUNK; },
+			sm.chunkBase, sm.red );
+		const int C = sm.chunkBase[L];
 		for ( int c = blockIdx.x; c < C; c += gridDim.x )
 		{
-			int j = pt_find( R.chunkBase, L, c );
-			int4 s = __ldcg( seg + j );
-			int lo = s.x + ( c - __ldcg( R.chunkBase + j ) ) * PT_CHUNK, hi = min( s.y, lo + PT_CHUNK );
+			int j = pt_find_s( sm.chunkBase, L, c );
+			int4 sg = sm.seg[cur][j];
+			int lo = sg.x + ( c - sm.chunkBase[j] ) * PT_CHUNK, hi = min( sg.y, lo + PT_CHUNK );
 			int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN;
-			for ( int i = lo + tid; i < hi; i += blockDim.x )
+			for ( int i = lo + tid; i < hi; i += PT_THREADS )
 			{
 				float2 cc = __ldcg( R.gCen + i );
 				mnx = min( mnx, f2o( cc.x ) );
@@ -520,108 +630,73 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 			}
 			if ( ( tid & 31 ) == 0 )
 			{
-				atomicMin( R.segBounds + 4 * j + 0, mnx );
-				atomicMin( R.segBounds + 4 * j + 1, mny );
-				atomicMax( R.segBounds + 4 * j + 2, mxx );
-				atomicMax( R.segBounds + 4 * j + 3, mxy );
+				atomicMin( bounds + 4 * j + 0, mnx );
+				atomicMin( bounds + 4 * j + 1, mny );
+				atomicMax( bounds + 4 * j + 2, mxx );
+				atomicMax( bounds + 4 * j + 3, mxy );
 			}
 		}
 		if ( !grid_barrier( counter, &sc->error, epoch ) )
 			return;
-		// centres below the pivot
-		for ( int c = blockIdx.x; c < C; c += gridDim.x )
-		{
-			int j = pt_find( R.chunkBase, L, c );
-			int4 s = __ldcg( seg + j );
-			int lo = s.x + ( c - __ldcg( R.chunkBase + j ) ) * PT_CHUNK, hi = min( s.y, lo + PT_CHUNK );
-			bool axisY;
-			float pivot = pt_pivot( R.segBounds + 4 * j, &axisY );
-			int below = 0;
-			for ( int i = lo + tid; i < hi; i += blockDim.x )
-				below += pt_axis( __ldcg( R.gCen + i ), axisY ) < pivot ? 1 : 0;
-			below = block_sum( below, red );
-			if ( tid == 0 )
-			{
-				__stcg( R.chunkStat + 5 * c + 0, below );
-				atomicAdd( R.segBelow + j, below );
-			}
-		}
-		if ( !grid_barrier( counter, &sc->error, epoch ) )
-			return;
-		// misplaced centres per chunk: left of the split and not below, or
-		// right of it and below
-		for ( int c = blockIdx.x; c < C; c += gridDim.x )
-		{
-			int j = pt_find( R.chunkBase, L, c );
-			int4 s = __ldcg( seg + j );
-			int lo = s.x + ( c - __ldcg( R.chunkBase + j ) ) * PT_CHUNK, hi = min( s.y, lo + PT_CHUNK );
-			bool axisY;
-			float pivot = pt_pivot( R.segBounds + 4 * j, &axisY );
-			int m = s.x + __ldcg( R.segBelow + j );
-			int bl = 0, br = 0;
-			for ( int i = lo + tid; i < hi; i += blockDim.x )
-			{
-				bool below = pt_axis( __ldcg( R.gCen + i ), axisY ) < pivot;
-				bl += ( i < m && !below ) ? 1 : 0;
-				br += ( i >= m && below ) ? 1 : 0;
-			}
-			bl = block_sum( bl, red );
-			br = block_sum( br, red + PT_WARPS );
-			if ( tid == 0 )
-			{
-				__stcg( R.chunkStat + 5 * c + 1, bl );
-				__stcg( R.chunkStat + 5 * c + 2, br );
-			}
-		}
-		if ( !grid_barrier( counter, &sc->error, epoch ) )
-			return;
-		// offsets of each chunk's misplaced centres inside its segment: from
-		// the left for the left side, from the right for the right side
+		// ---- B: centres below the pivot per chunk; next level's accumulators ----
 		if ( blockIdx.x == 0 )
 		{
-			for ( int j = tid; j < L; j += blockDim.x )
+			int* nb = R.segBounds + 4 * SC * prv;
+			int* nbl = R.segBelow + SC * prv;
+			int lim = min( 2 * L, SC );
+			for ( int j = tid; j < lim; j += PT_THREADS )
 			{
-				int c0 = __ldcg( R.chunkBase + j ), c1 = __ldcg( R.chunkBase + j + 1 );
-				int off = 0;
-				for ( int c = c0; c < c1; ++c )
-				{
-					__stcg( R.chunkStat + 5 * c + 3, off );
-					off += __ldcg( R.chunkStat + 5 * c + 1 );
-				}
-				int offR = 0;
-				for ( int c = c1 - 1; c >= c0; --c )
-				{
-					__stcg( R.chunkStat + 5 * c + 4, offR );
-					offR += __ldcg( R.chunkStat + 5 * c + 2 );
-				}
-				__stcg( R.pairBase + j, off );
+				__stcg( nb + 4 * j + 0, INT_MAX );
+				__stcg( nb + 4 * j + 1, INT_MAX );
+				__stcg( nb + 4 * j + 2, INT_MIN );
+				__stcg( nb + 4 * j + 3, INT_MIN );
+				__stcg( nbl + j, 0 );
 			}
-			__syncthreads();
+		}
+		for ( int c = blockIdx.x; c < C; c += gridDim.x )
+		{
+			int j = pt_find_s( sm.chunkBase, L, c );
+			int4 sg = sm.seg[cur][j];
+			int lo = sg.x + ( c - sm.chunkBase[j] ) * PT_CHUNK, hi = min( sg.y, lo + PT_CHUNK );
+			bool axisY;
+			float pivot = pt_pivot( bounds + 4 * j, &axisY );
+			int below = 0;
+			for ( int i = lo + tid; i < hi; i += PT_THREADS )
+				below += pt_axis( __ldcg( R.gCen + i ), axisY ) < pivot ? 1 : 0;
+			below = block_sum( below, sm.red );
 			if ( tid == 0 )
 			{
-				int run = 0;
-				for ( int j = 0; j < L; ++j )
-				{
-					int v = __ldcg( R.pairBase + j );
-					__stcg( R.pairBase + j, run );
-					run += v;
-				}
-				__stcg( R.pairBase + L, run );
+				__stcg( R.chunkStat + c, below );
+				atomicAdd( belowAcc + j, below );
 			}
 		}
 		if ( !grid_barrier( counter, &sc->error, epoch ) )
 			return;
-		// positions of the misplaced centres, ranked
+		// ---- C: ranks of the misplaced centres ----
 		for ( int c = blockIdx.x; c < C; c += gridDim.x )
 		{
-			int j = pt_find( R.chunkBase, L, c );
-			int4 s = __ldcg( seg + j );
-			int lo = s.x + ( c - __ldcg( R.chunkBase + j ) ) * PT_CHUNK, hi = min( s.y, lo + PT_CHUNK );
+			int j = pt_find_s( sm.chunkBase, L, c );
+			int4 sg = sm.seg[cur][j];
+			int c0 = sm.chunkBase[j], cEnd = sm.chunkBase[j + 1];
+			int lo = sg.x + ( c - c0 ) * PT_CHUNK, hi = min( sg.y, lo + PT_CHUNK );
 			bool axisY;
-			float pivot = pt_pivot( R.segBounds + 4 * j, &axisY );
-			int m = s.x + __ldcg( R.segBelow + j );
-			int offL = __ldcg( R.chunkStat + 5 * c + 3 ), offR = __ldcg( R.chunkStat + 5 * c + 4 );
-			int chunkBR = __ldcg( R.chunkStat + 5 * c + 2 );
+			float pivot = pt_pivot( bounds + 4 * j, &axisY );
+			int m = sg.x + __ldcg( belowAcc + j );
+			// every chunk before this one lies left of the split when this one
+			// holds misplaced left centres; every later one right of it when
+			// this one holds misplaced right centres
+			int offL = 0, offR = 0;
+			if ( lo < m )
+				for ( int k = c0 + tid; k < c; k += PT_THREADS )
+				{
+					int klo = sg.x + ( k - c0 ) * PT_CHUNK, khi = min( sg.y, klo + PT_CHUNK );
+					offL += ( khi - klo ) - __ldcg( R.chunkStat + k );
+				}
+			if ( hi > m )
+				for ( int k = c + 1 + tid; k < cEnd; k += PT_THREADS )
+					offR += __ldcg( R.chunkStat + k );
+			offL = block_sum( offL, sm.red );
+			offR = block_sum( offR, sm.red + PT_WARPS );
 			int first = lo + tid * PT_ITEMS;
 			int fl = 0, fr = 0;
 			int kind[PT_ITEMS];
@@ -642,35 +717,41 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 				fr += kind[k] == 2;
 			}
 			int totL, totR;
-			int exL = block_excl( fl, red, &totL );
-			int exR = block_excl( fr, red + PT_WARPS, &totR );
+			int exL = block_excl( fl, sm.red, &totL );
+			int exR = block_excl( fr, sm.red + PT_WARPS, &totR );
 #pragma unroll
 			for ( int k = 0; k < PT_ITEMS; ++k )
 			{
 				int i = first + k;
 				if ( kind[k] == 1 )
 				{
-					__stcg( R.bl + s.x + offL + exL, i );
+					__stcg( R.bl + sg.x + offL + exL, i );
 					exL += 1;
 				}
 				else if ( kind[k] == 2 )
 				{
-					__stcg( R.br + s.x + offR + ( chunkBR - 1 - exR ), i );
+					__stcg( R.br + sg.x + offR + ( totR - 1 - exR ), i );
 					exR += 1;
 				}
 			}
+			// the swap count: the chunk holding the split's last left centre
+			// (or the first chunk when nothing is below the pivot)
+			if ( tid == 0 && ( m > sg.x ? ( lo <= m - 1 && m - 1 < hi ) : c == c0 ) )
+				__stcg( R.pairBase + j, m > sg.x ? offL + totL : 0 );
+			__syncthreads();
 		}
 		if ( !grid_barrier( counter, &sc->error, epoch ) )
 			return;
-		// the swaps
+		// ---- D: the swaps ----
+		pt_block_prefix( L, [&]( int j ) { return __ldcg( R.pairBase + j ); }, sm.pairBase, sm.red );
 		{
-			int P = __ldcg( R.pairBase + L );
-			for ( int p = blockIdx.x * blockDim.x + tid; p < P; p += gridDim.x * blockDim.x )
+			int P = sm.pairBase[L];
+			for ( int p = blockIdx.x * PT_THREADS + tid; p < P; p += gridDim.x * PT_THREADS )
 			{
-				int j = pt_find( R.pairBase, L, p );
-				int4 s = __ldcg( seg + j );
-				int k = p - __ldcg( R.pairBase + j );
-				int a = __ldcg( R.bl + s.x + k ), b = __ldcg( R.br + s.x + k );
+				int j = pt_find_s( sm.pairBase, L, p );
+				int4 sg = sm.seg[cur][j];
+				int k = p - sm.pairBase[j];
+				int a = __ldcg( R.bl + sg.x + k ), b = __ldcg( R.br + sg.x + k );
 				int ia = __ldcg( R.gIdx + a ), ib = __ldcg( R.gIdx + b );
 				float2 ca = __ldcg( R.gCen + a ), cb = __ldcg( R.gCen + b );
 				__stcg( R.gIdx + a, ib );
@@ -681,56 +762,9 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 		}
 		if ( !grid_barrier( counter, &sc->error, epoch ) )
 			return;
-		// split, link the segment's node to its two children, queue them
-		for ( int j = blockIdx.x * blockDim.x + tid; j < L; j += gridDim.x * blockDim.x )
-		{
-			int4 s = __ldcg( seg + j );
-			int n = s.y - s.x, below = __ldcg( R.segBelow + j );
-			int split = ( below == 0 || below == n ) ? n / 2 : below;
-			int c1 = s.z;
-			int node = R.freed[F - 1 - ( s.x + c1 )];
-			int ls = s.x, le = s.x + split, re = s.y;
-			int left = le - ls == 1 ? __ldcg( R.gIdx + ls ) : R.freed[F - 1 - ( ls + c1 + 1 )];
-			int right = re - le == 1 ? __ldcg( R.gIdx + le ) : R.freed[F - 1 - ( le + c1 )];
-			T.child1[node] = left;
-			T.child2[node] = right;
-			T.parent[left] = node;
-			T.parent[right] = node;
-			// children the bottom-up pass starts from: single gathered nodes and
-			// the roots of small segments (their inner nodes are done in k_pt_small)
-			if ( le - ls <= PT_SMALL )
-				__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), left );
-			if ( re - le <= PT_SMALL )
-				__stcg( R.rfStart + atomicAdd( &sc->rbRefresh, 1 ), right );
-			if ( le - ls >= 2 )
-			{
-				int4 v = make_int4( ls, le, c1 + 1, 0 );
-				if ( le - ls > PT_SMALL )
-					__stcg( nxt + atomicAdd( &sc->rbLarge[cur ^ 1], 1 ), v );
-				else
-					__stcg( R.segSmall + atomicAdd( &sc->rbSmall, 1 ), v );
-			}
-			if ( re - le >= 2 )
-			{
-				int4 v = make_int4( le, re, c1, 0 );
-				if ( re - le > PT_SMALL )
-					__stcg( nxt + atomicAdd( &sc->rbLarge[cur ^ 1], 1 ), v );
-				else
-					__stcg( R.segSmall + atomicAdd( &sc->rbSmall, 1 ), v );
-			}
-		}
-		if ( !grid_barrier( counter, &sc->error, epoch ) )
-			return;
 	}
 }
 
-// Segments of at most PT_SMALL nodes: one block each, in shared memory,
-// level by level: one warp partitions each sub-segment, then one thread per
-// sub-segment links its node. The internal nodes of a segment of n gathered
-// nodes entered with c1 child1 edges above take the n - 1 freed slots from
-// position start + c1 on (each sub-segment (s, c1) takes s + c1, its left
-// part from s + c1 + 1, its right part from its split + c1), so those ids
-// are staged in shared memory first.
 // shared memory of k_pt_small (dynamic: more than the static 48 KB)
 #define PT_SMALL_LEVELS 64
 struct PtSmall
@@ -1016,8 +1050,9 @@ __global__ void k_pt_ranks( DWorld w, int t, int onlyAfterRebuild )
 int pt_large_blocks()
 {
 	cudaFuncSetAttribute( k_pt_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof( PtSmall ) );
+	cudaFuncSetAttribute( k_pt_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof( PtLarge ) );
 	int perSM = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_pt_large, PT_THREADS, 0 );
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM, k_pt_large, PT_THREADS, sizeof( PtLarge ) );
 	int dev = 0, sms = 0;
 	cudaGetDevice( &dev );
 	cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
@@ -1058,7 +1093,8 @@ void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 			unsigned* counter = &w.sc->barrierCount;
 			cudaMemsetAsync( counter, 0, sizeof( unsigned ), st );
 			void* args[] = { &w, &t, &counter };
-			cudaLaunchCooperativeKernel( (void*)k_pt_large, dim3( s.ptBlocks ), dim3( PT_THREADS ), args, 0, st );
+			cudaLaunchCooperativeKernel( (void*)k_pt_large, dim3( s.ptBlocks ), dim3( PT_THREADS ), args,
+										 sizeof( PtLarge ), st );
 		}
 		k_pt_small<<<F2D_SMS * 2, PT_THREADS, sizeof( PtSmall ), st>>>( w, t );
 		k_pt_refresh<<<g, 256, 0, st>>>( w, t );

@@ -857,8 +857,8 @@ static void rb_ensure( HostWorld* W, int cap )
 	dgrow( R.segSmall, 0, n / 2 + 8 );
 	dgrow( R.chunkBase, 0, (size_t)R.segCap + 1 );
 	dgrow( R.chunkStat, 0, 5 * (size_t)R.chunkCap );
-	dgrow( R.segBounds, 0, 4 * (size_t)R.segCap );
-	dgrow( R.segBelow, 0, (size_t)R.segCap );
+	dgrow( R.segBounds, 0, 8 * (size_t)R.segCap ); // two level parities
+	dgrow( R.segBelow, 0, 2 * (size_t)R.segCap );
 	dgrow( R.pairBase, 0, (size_t)R.segCap + 1 );
 	dgrow( R.rfStart, 0, n / 2 + 8 );
 	R.cap = cap;
