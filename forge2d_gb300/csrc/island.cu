@@ -454,17 +454,22 @@ __device__ void isl_link_joint( const DWorld& w, DIslands& I, int j, bool merge 
 }
 
 // island.c:429-528
-__device__ void isl_merge_one( DIslands& I, int id )
+// remap: move the members' island ids too (the step's merge has done that
+// for all islands at once, k_isl_merge_remap)
+__device__ void isl_merge_one( DIslands& I, int id, bool remap = true )
 {
 	DIsland& isl = I.islands[id];
 	int rootId = isl.parent;
 	DIsland& root = I.islands[rootId];
-	for ( int b = isl.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; b = I.bIslandNext[b], ++g )
-		I.bIsland[b] = rootId;
-	for ( int c = isl.headContact, g = 0; c != ISL_NULL && g < I.contactCap; c = I.cIslandNext[c], ++g )
-		I.cIsland[c] = rootId;
-	for ( int j = isl.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; j = I.jIslandNext[j], ++g )
-		I.jIsland[j] = rootId;
+	if ( remap )
+	{
+		for ( int b = isl.headBody, g = 0; b != ISL_NULL && g < I.bodyCap; b = I.bIslandNext[b], ++g )
+			I.bIsland[b] = rootId;
+		for ( int c = isl.headContact, g = 0; c != ISL_NULL && g < I.contactCap; c = I.cIslandNext[c], ++g )
+			I.cIsland[c] = rootId;
+		for ( int j = isl.headJoint, g = 0; j != ISL_NULL && g < I.jointCap; j = I.jIslandNext[j], ++g )
+			I.jIsland[j] = rootId;
+	}
 	I.bIslandNext[root.tailBody] = isl.headBody;
 	I.bIslandPrev[isl.headBody] = root.tailBody;
 	root.tailBody = isl.tailBody;
@@ -1078,13 +1083,35 @@ __global__ void k_isl_list( DIslands* Ip, const int* count )
 			I.list[I.pos[i]] = I.awakeIslands[i];
 }
 
+// island.c:539-600 members of merged islands: every body, contact and joint
+// of an island that has a parent (a root, after k_isl_merge_roots) takes the
+// root's id, all at once
+__global__ void k_isl_merge_remap( DWorld w, DIslands* Ip )
+{
+	const DIslands& I = *Ip;
+	if ( I.listCount == 0 )
+		return;
+	int nb = min( I.bodyKnown, I.bodyCap ), nc = w.sc->contactIdCount, nj = w.jointCount;
+	int total = nb + nc + nj;
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x )
+	{
+		int* slot = k < nb ? I.bIsland + k : k < nb + nc ? I.cIsland + ( k - nb ) : I.jIsland + ( k - nb - nc );
+		int id = *slot;
+		if ( id == ISL_NULL )
+			continue;
+		int p = I.islands[id].parent;
+		if ( p != ISL_NULL )
+			*slot = p;
+	}
+}
+
 __global__ void k_isl_merge_apply( DIslands* Ip )
 {
 	DIslands& I = *Ip;
 	for ( int k = I.listCount - 1; k >= 0; --k )
 	{
 		int id = I.list[k];
-		isl_merge_one( I, id );
+		isl_merge_one( I, id, false );
 		isl_island_destroy( I, id );
 	}
 }
@@ -1498,6 +1525,7 @@ void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long
 	k_isl_link_serial<<<1, 1, 0, st>>>( w, w.isl );
 	k_isl_merge_roots<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, w.isl );
 	isl_list( w, scanState, st );
+	k_isl_merge_remap<<<grid_for( w.bodyCap + w.contactCap + w.jointCap ), 256, 0, st>>>( w, w.isl );
 	k_isl_merge_apply<<<1, 1, 0, st>>>( w.isl );
 }
 
