@@ -294,6 +294,8 @@ def run_gpu(args, rank, world):
         alg_bytes.append(solver_bytes(g.counters()))
     g.set_profiling(False)
     phases /= reps
+    # latency floor of the solver: its grid barriers x the measured cost of one
+    barriers, us_per_barrier = g.solver_latency(2000)
     solve_avg = sum(solve_ms) / len(solve_ms)
     alg = sum(alg_bytes) / len(alg_bytes)
     peak, peak_kind = measured_peaks()
@@ -340,7 +342,14 @@ def run_gpu(args, rank, world):
                      "traffic_source": "ncu dram bytes per algorithmic byte of a captured pile25k launch "
                                        "(profiles/k_solve_pile25k.md) x this run's algorithmic bytes",
                      "profiled_steps": [{"solve_ms": a, "algorithmic_bytes": b}
-                                        for a, b in zip(solve_ms, alg_bytes)]},
+                                        for a, b in zip(solve_ms, alg_bytes)],
+                     "latency": {"barriers_per_launch": barriers, "us_per_barrier": us_per_barrier,
+                                 "floor_ms": barriers * us_per_barrier * 1e-3,
+                                 "floor_frac_of_launch": (barriers * us_per_barrier * 1e-3 / solve_avg)
+                                 if solve_avg > 0 else None,
+                                 "what": "the solver's stages are separated by grid-wide barriers; the floor is "
+                                         "their count in the last launch times the cost of one barrier measured "
+                                         "by a launch of 2000 bare barriers on the same grid"}},
         "phases_ms": {"broadphase": phases[0], "narrowphase": phases[1], "colouring": phases[2],
                       "solver_setup": phases[3], "solver_kernel": phases[4], "finalize": phases[5]},
         "gpu_launches": launches,

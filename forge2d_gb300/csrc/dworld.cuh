@@ -139,6 +139,7 @@ struct DScalars
 	// creation stamp of the next new contact (the bodies' contact lists are
 	// newest first); non-static bodies in the awake set (worlds without
 	// island records); destroy calls: collected contacts, end events
+	int solveBarriers; // grid barriers the last grid-wide solver launch passed
 	unsigned long long stampBase;
 	int awakeOrderCount;
 	int apiCount, apiEndCount;

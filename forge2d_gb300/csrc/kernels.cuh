@@ -75,6 +75,8 @@ void launch_destroy_contacts_of( DWorld& w, cudaStream_t st, int body, int shape
 void launch_destroy_joint( DWorld& w, cudaStream_t st, int joint, int wake );
 void launch_destroy_body_records( DWorld& w, cudaStream_t st, int body );
 void launch_unbuffer_move( DWorld& w, cudaStream_t st, int shape );
+// microseconds per grid barrier on the grid-wide solver's grid (n barriers timed)
+float solver_barrier_probe( StepScratch& s, cudaStream_t st, unsigned* counter, int* err, int n );
 // b2Shape_TestPoint on the device row of one shape; *out (device) = 0 or 1
 void launch_shape_test_point( DWorld& w, cudaStream_t st, int shape, float x, float y, int* out );
 void launch_isl_wake_marked( DWorld& w, cudaStream_t st, const int* shapeMarks, int shapeCount );

@@ -1261,6 +1261,36 @@ __global__ void __launch_bounds__( THREADS ) k_solve( DWorld w, SolveParams p, c
 	// tail constraints below the extras' range had no register lane
 	for ( int k = tailSlot + gtid; k < min( novf + gstride, novf + nColour ); k += gstride )
 		store_manifold_global( w, k, true );
+	if ( blockIdx.x == 0 && threadIdx.x == 0 )
+		w.sc->solveBarriers = (int)epoch; // grid barriers this launch passed
+}
+
+// A launch of nothing but grid barriers on the solver's grid: the per-barrier
+// latency that bounds the stages of k_solve from below.
+__global__ void __launch_bounds__( 512 ) k_barrier_probe( unsigned* counter, int* err, int n )
+{
+	unsigned epoch = 0;
+	for ( int i = 0; i < n; ++i )
+		if ( !grid_barrier( counter, err, epoch ) )
+			return;
+}
+
+float solver_barrier_probe( StepScratch& s, cudaStream_t st, unsigned* counter, int* err, int n )
+{
+	cudaEvent_t a, b;
+	cudaEventCreate( &a );
+	cudaEventCreate( &b );
+	cudaMemsetAsync( counter, 0, sizeof( unsigned ), st );
+	void* args[] = { &counter, &err, &n };
+	cudaEventRecord( a, st );
+	cudaLaunchCooperativeKernel( (void*)k_barrier_probe, dim3( s.solverBlocks ), dim3( 512 ), args, 0, st );
+	cudaEventRecord( b, st );
+	cudaEventSynchronize( b );
+	float ms = 0.0f;
+	cudaEventElapsedTime( &ms, a, b );
+	cudaEventDestroy( a );
+	cudaEventDestroy( b );
+	return n > 0 ? 1000.0f * ms / (float)n : 0.0f;
 }
 
 // ---------------------------------------------------------------------------

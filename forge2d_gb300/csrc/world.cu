@@ -4847,6 +4847,27 @@ extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )
 	out8[7] = W->jointCount - (int)W->jointFree.size();
 }
 
+// Latency side of the solver's roofline: the grid barriers the last
+// grid-wide solver launch passed (0 after a cluster-solver step) and the
+// measured cost of one barrier on its grid (n barriers timed by events).
+extern "C" F2D_API void f2d_world_get_solver_latency( int32_t worldId, int32_t probeBarriers, double* out2 )
+{
+	out2[0] = out2[1] = 0.0;
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr )
+		return;
+	cudaStreamSynchronize( W->stream );
+	int barriers = 0;
+	cudaMemcpy( &barriers, &W->d.sc->solveBarriers, sizeof( int ), cudaMemcpyDeviceToHost );
+	out2[0] = barriers;
+	if ( probeBarriers > 0 && W->s.solverBlocks > 0 )
+	{
+		int* err = W->s.tmpB;
+		cudaMemsetAsync( err, 0, sizeof( int ), W->stream );
+		out2[1] = solver_barrier_probe( W->s, W->stream, (unsigned*)W->s.tmpA, err, probeBarriers );
+	}
+}
+
 // ---------------------------------------------------------------------------
 // accessors for queries.cu
 // ---------------------------------------------------------------------------

@@ -180,6 +180,7 @@ _SIGS = [
     ("f2d_joint_set_param", None, [_i, _i, _i, _d, _d]),
     ("f2d_joint_get_body", _i, [_i, _i, _i, _P(_i), _P(_i)]),
     ("f2d_joint_wake_bodies", None, [_i, _i]),
+    ("f2d_world_get_solver_latency", None, [_i, _i, _P(_d)]),
     ("f2d_body_get_position", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_get_rotation", None, [_i, _i, _P(_d), _P(_d)]),
     ("f2d_body_set_transform", None, [_i, _i, _d, _d, _d, _d]),

@@ -361,6 +361,13 @@ class GpuWorld:
         self.lib.f2d_world_get_phase_ms(self.id, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
+    def solver_latency(self, probe_barriers=2000):
+        """(grid barriers of the last grid-wide solver launch, measured
+        microseconds per grid barrier on its grid)."""
+        out = np.zeros(2, np.float64)
+        self.lib.f2d_world_get_solver_latency(self.id, probe_barriers, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return int(out[0]), float(out[1])
+
     def counters(self) -> dict:
         out = np.zeros(8, np.int32)
         self.lib.f2d_world_get_counters(self.id, _iptr(out))

@@ -636,6 +636,11 @@ F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 );
 /* awake bodies, live contacts, touching contacts, overflow contacts, active
  * colours, colouring rounds, shapes, joints (b2Counters, types.h:493-506). */
 F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 );
+/* The grid barriers the last grid-wide solver launch passed (out2[0]; 0 after
+ * a step on the cluster solver) and, when probeBarriers > 0, the measured
+ * microseconds per grid barrier on that solver's grid (out2[1]): the latency
+ * floor of the solver kernel is their product. */
+F2D_API void f2d_world_get_solver_latency( int32_t worldId, int32_t probeBarriers, double* out2 );
 /* ---- learned warm start (no reference counterpart) ----------------------
  * A small MLP [12 -> 64 -> 64 -> 2] (BF16 weights, FP32 accumulation,
  * tensor-core MMA) predicts the normal and tangent impulses of manifold

@@ -168,7 +168,7 @@ def test_per_body_reads_after_a_step_are_cheap(gpu_lib):
     for _ in range(3):
         assert g.step(1.0 / 60.0, 4) == 0
     assert g.sync() == 0
-    ids = g._body_ids
+    ids = [g._body(b) for b in sorted(g._wg["body"])]
     fn = g.lib.f2d_body_get_position
     x, y = C.c_double(0.0), C.c_double(0.0)
     px, py = C.byref(x), C.byref(y)

@@ -152,7 +152,7 @@ def test_gpu_joint_constraint_matches_port(gpu_lib, port_lib, scene, kw):
     p = port_lib.PortWorld(scenes.world_def(**wkw))
     scenes.build(g, scene, **kw)
     scenes.build(p, scene, **kw)
-    world0 = g._body_ids[0][1] & 0xffff
+    world0 = g._body(0)[1] & 0xffff
     nonzero = 0
     for f in range(1, 201):
         g.step(1.0 / 60.0, 4)
