@@ -299,6 +299,7 @@ struct DIslands
 	// their capacity (2 x the new-pair capacity)
 	unsigned long long *ncKeys, *ncKeysAlt;
 	int ncCap, ncCount;
+	int linkCount; // contacts that began touching this step (parallel links)
 };
 
 // Solver view of one body: velocity and the substep position/rotation

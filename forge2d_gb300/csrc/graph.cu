@@ -591,7 +591,7 @@ void launch_graph( DWorld& w, StepScratch& s, cudaStream_t st )
 	// changes wake a sleeping set applies them serially there, colours
 	// included, and leaves no op for the rounds below
 	if ( w.isl )
-		launch_isl_ops( w, st, gkind, s.scanState );
+		launch_isl_ops( w, s, st, gkind );
 	k_op_lock<<<g, 256, 0, st>>>( w );
 	k_op_round<<<g, 256, 0, st>>>( w, gkind, pending );
 	scan_lookback( pending, pos, &w.sc->opCount, 0, w.opCap, &w.sc->pendingOps, s.scanState, &w.sc->error, st );

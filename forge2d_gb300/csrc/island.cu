@@ -1019,6 +1019,7 @@ __global__ void k_isl_ops( DWorld w, DIslands* Ip, const int* gkind )
 	DIslands& I = *Ip;
 	if ( I.serialOps == 0 )
 		return;
+	I.linkCount = 0; // nothing for the parallel link kernels to sort
 	int nOps = w.sc->opCount;
 	if ( nOps > w.opCap )
 		nOps = w.opCap;
@@ -1497,24 +1498,134 @@ __global__ void k_isl_unlink_clear( DWorld w, DIslands* Ip )
 	}
 }
 
-// step 4: the contacts that began touching link their islands in op order
-__global__ void k_isl_link_serial( DWorld w, DIslands* Ip )
+// step 4: links of the contacts that began touching (island.c:116-219). The
+// island a link prepends to is the body's island when both bodies share one
+// (decided in parallel), else the union-find root at that point of the op
+// order, which a serial pass over those ops alone finds (making the B root a
+// child of the A root as it goes). The prepends themselves then run in
+// parallel: sorted by (island, op), each island's new contacts chain in op
+// order in front of its old head.
+__global__ void k_isl_link_flags( DWorld w, DIslands* Ip, int* flag )
+{
+	const DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		int target = ISL_NULL;
+		bool link = w.opKind[k] == 1;
+		if ( link )
+		{
+			int2 bd = w.cbody[w.opContact[k]];
+			int idA = I.bIsland[bd.x], idB = I.bIsland[bd.y];
+			if ( idA == idB )
+				target = idA;
+		}
+		I.order[k] = target;
+		flag[k] = link ? 1 : 0;
+	}
+}
+
+__global__ void k_isl_link_roots( DWorld w, DIslands* Ip )
 {
 	DIslands& I = *Ip;
 	if ( I.serialOps )
 		return;
 	int nOps = min( w.sc->opCount, w.opCap );
 	for ( int k = 0; k < nOps; ++k )
-		if ( w.opKind[k] == 1 )
-		{
-			int c = w.opContact[k];
-			w.cflags[c] |= CF_TOUCHING;
-			isl_link_contact( w, I, c );
-		}
+	{
+		if ( w.opKind[k] != 1 || I.order[k] != ISL_NULL )
+			continue;
+		int2 bd = w.cbody[w.opContact[k]];
+		int idA = I.bIsland[bd.x], idB = I.bIsland[bd.y];
+		int rootA = idA != ISL_NULL ? isl_root( I, idA ) : ISL_NULL;
+		int rootB = idB != ISL_NULL ? isl_root( I, idB ) : ISL_NULL;
+		if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
+			I.islands[rootB].parent = rootA;
+		I.order[k] = rootA != ISL_NULL ? rootA : rootB;
+	}
 }
 
-void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long long* scanState )
+__global__ void k_isl_link_keys( DWorld w, DIslands* Ip, const int* flag, const int* pos )
 {
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int nOps = min( w.sc->opCount, w.opCap );
+	for ( int k = blockIdx.x * blockDim.x + threadIdx.x; k < nOps; k += gridDim.x * blockDim.x )
+	{
+		if ( !flag[k] )
+			continue;
+		int c = w.opContact[k];
+		w.cflags[c] |= CF_TOUCHING;
+		I.ncKeys[pos[k]] = ( (unsigned long long)(unsigned)I.order[k] << 32 ) | (unsigned)k;
+	}
+	if ( blockIdx.x == 0 && threadIdx.x == 0 )
+		Ip->linkCount = nOps > 0 ? pos[nOps - 1] + flag[nOps - 1] : 0;
+}
+
+__global__ void k_isl_link_chain( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int n = I.linkCount;
+	for ( int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+	{
+		unsigned long long key = I.ncKeys[p];
+		int id = (int)( key >> 32 );
+		int c = w.opContact[(int)( key & 0xffffffffull )];
+		bool first = p == 0 || (int)( I.ncKeys[p - 1] >> 32 ) != id;
+		bool last = p + 1 == n || (int)( I.ncKeys[p + 1] >> 32 ) != id;
+		DIsland& isl = I.islands[id];
+		int next;
+		if ( first )
+		{
+			// the island's old head and tail (written below only by the
+			// segment's last / first thread, after these reads by the same
+			// or an earlier thread of the segment: read them here)
+			next = isl.headContact;
+			if ( next != ISL_NULL )
+				I.cIslandPrev[next] = c;
+		}
+		else
+			next = w.opContact[(int)( I.ncKeys[p - 1] & 0xffffffffull )];
+		I.cIslandNext[c] = next;
+		I.cIslandPrev[c] = last ? ISL_NULL : w.opContact[(int)( I.ncKeys[p + 1] & 0xffffffffull )];
+		I.cIsland[c] = id;
+	}
+}
+
+// heads, tails and counts of the islands that gained contacts
+__global__ void k_isl_link_heads( DWorld w, DIslands* Ip )
+{
+	DIslands& I = *Ip;
+	if ( I.serialOps )
+		return;
+	int n = I.linkCount;
+	for ( int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+	{
+		unsigned long long key = I.ncKeys[p];
+		int id = (int)( key >> 32 );
+		bool last = p + 1 == n || (int)( I.ncKeys[p + 1] >> 32 ) != id;
+		if ( !last )
+			continue;
+		int q = p;
+		while ( q > 0 && (int)( I.ncKeys[q - 1] >> 32 ) == id )
+			q -= 1;
+		DIsland& isl = I.islands[id];
+		int c = w.opContact[(int)( key & 0xffffffffull )];
+		if ( isl.tailContact == ISL_NULL )
+			isl.tailContact = w.opContact[(int)( I.ncKeys[q] & 0xffffffffull )];
+		isl.headContact = c;
+		isl.contactCount += p - q + 1;
+	}
+}
+
+void launch_isl_ops( DWorld& w, StepScratch& s, cudaStream_t st, const int* gkind )
+{
+	unsigned long long* scanState = s.scanState;
 	int g = grid_for( w.opCap );
 	cudaMemsetAsync( (char*)w.isl + offsetof( DIslands, serialOps ), 0, sizeof( int ), st );
 	k_isl_op_check<<<g, 256, 0, st>>>( w, w.isl );
@@ -1522,7 +1633,22 @@ void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long
 	k_isl_unlink_mark<<<g, 256, 0, st>>>( w, w.isl );
 	k_isl_unlink_runs<<<g, 256, 0, st>>>( w, w.isl );
 	k_isl_unlink_clear<<<g, 256, 0, st>>>( w, w.isl );
-	k_isl_link_serial<<<1, 1, 0, st>>>( w, w.isl );
+	// links: flags and same-island targets, the serial unions, then the
+	// prepends sorted by (island, op) (scratch past the op kinds in tmpA)
+	int* flag = s.tmpA + w.opCap;
+	int* pos = s.tmpB;
+	k_isl_link_flags<<<g, 256, 0, st>>>( w, w.isl, flag );
+	k_isl_link_roots<<<1, 1, 0, st>>>( w, w.isl );
+	scan_lookback( flag, pos, &w.sc->opCount, 0, w.opCap, nullptr, scanState, &w.sc->error, st );
+	k_isl_link_keys<<<g, 256, 0, st>>>( w, w.isl, flag, pos );
+	int islandBits = 1;
+	while ( ( 1 << islandBits ) < w.bodyCap + 1 )
+		islandBits += 1;
+	sort_coop<unsigned long long>( w.islNcKeys, nullptr, w.islNcKeysAlt, nullptr,
+								   (int*)( (char*)w.isl + offsetof( DIslands, linkCount ) ), 32 + islandBits, w.sortHist,
+								   &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
+	k_isl_link_chain<<<g, 256, 0, st>>>( w, w.isl );
+	k_isl_link_heads<<<g, 256, 0, st>>>( w, w.isl );
 	k_isl_merge_roots<<<grid_for( w.bodyCap ), 256, 0, st>>>( w, w.isl );
 	isl_list( w, scanState, st );
 	k_isl_merge_remap<<<grid_for( w.bodyCap + w.contactCap + w.jointCap ), 256, 0, st>>>( w, w.isl );

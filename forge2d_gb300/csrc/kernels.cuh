@@ -63,7 +63,7 @@ int solver_max_blocks( int threads );
 // islands and sleeping (island.cu; worlds with sleeping enabled)
 void launch_isl_create( DWorld& w, cudaStream_t st );
 void launch_isl_new_contacts( DWorld& w, StepScratch& s, cudaStream_t st, int planMode );
-void launch_isl_ops( DWorld& w, cudaStream_t st, const int* gkind, unsigned long long* scanState );
+void launch_isl_ops( DWorld& w, StepScratch& s, cudaStream_t st, const int* gkind );
 void launch_isl_split( DWorld& w, cudaStream_t st );
 void launch_isl_sleep( DWorld& w, cudaStream_t st, unsigned long long* scanState );
 void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body );

@@ -235,7 +235,11 @@ class GpuWorld:
                                        mats.ctypes.data_as(C.POINTER(C.c_double)), len(mats) // 6, categoryBits,
                                        maskBits, groupIndex, int(isLoop), int(enableSensorEvents),
                                        C.byref(i1), C.byref(wg))
-        return self._ret(ok, i1, wg, "chain")
+        chain = self._ret(ok, i1, wg, "chain")
+        if ok:
+            for s in self.chain_segments(chain):
+                self._wg["shape"][s[0] - 1] = s[1]
+        return chain
 
     def cast_ray(self, ox, oy, tx, ty, fn, cat=1, mask=-1):
         """b2World_CastRay: fn(shape, point(2), normal(2), fraction) -> float,
