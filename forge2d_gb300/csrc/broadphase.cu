@@ -347,23 +347,6 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 	return false;
 }
 
-// Left-to-right position of a leaf in one of the reference's trees: the
-// leaves of every child1 subtree passed on the way up from the leaf
-__device__ __forceinline__ int tree_leaf_rank( const DProxyTree& T, int leaf )
-{
-	int r = 0, c = leaf;
-	for ( int guard = 0; guard < ( 1 << 16 ); ++guard )
-	{
-		int p = T.parent[c];
-		if ( p < 0 || p >= T.cap )
-			break;
-		if ( T.child2[p] == c )
-			r += T.leaves[T.child1[p]];
-		c = p;
-	}
-	return r;
-}
-
 // Candidate pair (si moved, sj its overlapping leaf): the filters of
 // b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup. A
 // pair whose proxies both moved belongs to one query in the reference: the

@@ -511,6 +511,26 @@ struct DWorld
 	int* sortTemp;
 };
 
+#ifdef __CUDACC__
+// Left-to-right position of a leaf in one of the reference's trees: the
+// leaves of every child1 subtree passed on the way up from the leaf (a
+// depth-first query visits overlapping leaves in descending position)
+__device__ __forceinline__ int tree_leaf_rank( const DProxyTree& T, int leaf )
+{
+	int r = 0, c = leaf;
+	for ( int guard = 0; guard < ( 1 << 16 ); ++guard )
+	{
+		int p = T.parent[c];
+		if ( p < 0 || p >= T.cap )
+			break;
+		if ( T.child2[p] == c )
+			r += T.leaves[T.child1[p]];
+		c = p;
+	}
+	return r;
+}
+#endif
+
 __host__ __device__ __forceinline__ int body_type( int f )
 {
 	return ( f >> BF_TYPE_SHIFT ) & 3;

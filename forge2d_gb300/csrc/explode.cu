@@ -11,6 +11,8 @@
 #include "dworld.cuh"
 #include "kernels.cuh"
 
+#include <climits>
+
 struct Blast
 {
 	fv2 position;
@@ -98,7 +100,10 @@ __device__ __forceinline__ bool blast_candidate( const DWorld& w, int s, const B
 	return box_overlaps( box_from4( w.fat[s] ), box );
 }
 
-__global__ void k_explode_mark( DWorld w, Blast bl, int* hit )
+// hit[s] = 1 + the shape's left-to-right position in the dynamic tree for
+// the shapes the blast reaches (the reference's query visits them in
+// descending position, world.c:2746), else 0; byRank[position] = s
+__global__ void k_explode_mark( DWorld w, Blast bl, int* hit, int* byRank )
 {
 	for ( int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.shapeCount; s += gridDim.x * blockDim.x )
 	{
@@ -106,7 +111,15 @@ __global__ void k_explode_mark( DWorld w, Blast bl, int* hit )
 		if ( blast_candidate( w, s, bl ) )
 		{
 			fv2 pA;
-			h = blast_distance( w, s, body_xform( w, w.shapeBody[s] ), bl, pA ) <= bl.radius + bl.falloff;
+			if ( blast_distance( w, s, body_xform( w, w.shapeBody[s] ), bl, pA ) <= bl.radius + bl.falloff )
+			{
+				int r = tree_leaf_rank( w.pt[2], w.proxyKey[s] >> 2 );
+				if ( r >= 0 && r < w.shapeCap )
+				{
+					h = r + 1;
+					byRank[r] = s;
+				}
+			}
 		}
 		hit[s] = h;
 	}
@@ -142,7 +155,8 @@ __device__ __forceinline__ float projected_perimeter( const float4* g, int type,
 	return fabs_s( value2 - value1 );
 }
 
-// one thread per body: its hit shapes in ascending id order
+// one thread per body: its hit shapes in the query's order (descending
+// tree position), so the impulses add up as the reference's do
 __global__ void k_explode_apply( DWorld w, Blast bl, const int* hit )
 {
 	for ( int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.bodyCount; b += gridDim.x * blockDim.x )
@@ -155,17 +169,20 @@ __global__ void k_explode_apply( DWorld w, Blast bl, const int* hit )
 		float4 mv = w.massv[b];
 		float2 c = w.center[b];
 		bool touched = false;
-		int last = -1;
+		int last = INT_MAX;
 		for ( int guard = 0; guard < 4096; ++guard )
 		{
-			// next hit shape of this body above `last`
-			int next = -1;
+			// next hit shape of this body below position `last`
+			int next = -1, nextPos = 0;
 			for ( int s = w.headShape[b], g2 = 0; s != F2D_NULL && g2 < 4096; s = w.nextShape[s], ++g2 )
-				if ( s > last && hit[s] && ( next < 0 || s < next ) )
+				if ( hit[s] && hit[s] < last && hit[s] > nextPos )
+				{
 					next = s;
+					nextPos = hit[s];
+				}
 			if ( next < 0 )
 				break;
-			last = next;
+			last = nextPos;
 			int s = next;
 			fv2 pointA;
 			float d = blast_distance( w, s, xf, bl, pointA );
@@ -209,9 +226,11 @@ void launch_explode( DWorld& w, cudaStream_t st, int* hit, unsigned long long ma
 	bl.falloff = falloff;
 	bl.impulsePerLength = impulsePerLength;
 	bl.mask = mask;
-	k_explode_mark<<<grid_for( w.shapeCount ), 256, 0, st>>>( w, bl, hit );
+	int* byRank = hit + w.shapeCap;
+	cudaMemsetAsync( byRank, 0xff, sizeof( int ) * (size_t)w.shapeCap, st );
+	k_explode_mark<<<grid_for( w.shapeCount ), 256, 0, st>>>( w, bl, hit, byRank );
 	if ( w.isl )
-		launch_isl_wake_marked( w, st, hit, w.shapeCount );
+		launch_isl_wake_marked( w, st, byRank, w.shapeCap );
 	k_explode_apply<<<grid_for( w.bodyCount ), 128, 0, st>>>( w, bl, hit );
 }
 

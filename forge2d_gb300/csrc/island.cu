@@ -1230,14 +1230,17 @@ __global__ void k_isl_api( DWorld w, DIslands* Ip, int op, int body )
 	}
 }
 
-// Wakes the sleeping sets of the marked shapes' bodies in ascending shape id
-// (b2WakeBody per blast shape, world.c:2673).
-__global__ void k_isl_wake_marked( DWorld w, DIslands* Ip, const int* marks, int n )
+// Wakes the sleeping sets of the blast's shapes' bodies in the order the
+// reference's query visits them (b2WakeBody per blast shape, world.c:2673):
+// byRank[r] is the shape at left-to-right tree position r (or -1), visited
+// from the last position down.
+__global__ void k_isl_wake_marked( DWorld w, DIslands* Ip, const int* byRank, int n )
 {
 	DIslands& I = *Ip;
-	for ( int s = 0; s < n; ++s )
+	for ( int r = n - 1; r >= 0; --r )
 	{
-		if ( marks[s] == 0 )
+		int s = byRank[r];
+		if ( s < 0 || s >= w.shapeCount )
 			continue;
 		int b = w.shapeBody[s];
 		if ( I.bSet[b] >= SET_FIRST_SLEEPING )

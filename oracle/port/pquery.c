@@ -402,62 +402,77 @@ static float projected_perimeter( const Shape* s, v2 line )
 // projected perimeter and the falloff. Shapes are visited in id order (the
 // reference visits its dynamic tree's order; the order only matters for a
 // body with several shapes in the blast or for the order sleeping sets wake).
+typedef struct ExplodeCtx
+{
+	World* w;
+	v2 position;
+	float r, fo, ipl;
+} ExplodeCtx;
+
+// world.c:2640-2716 ExplosionCallback, per shape in the dynamic tree's
+// query order
+static int explode_visit( int proxyId, int id, void* context )
+{
+	(void)proxyId;
+	ExplodeCtx* e = context;
+	World* w = e->w;
+	const Shape* s = w->shapes + id;
+	float r = e->r, fo = e->fo;
+	v2 position = e->position;
+	Body* b = w->bodies + s->bodyId;
+	xform xf = b->xf;
+	ShapeProxy pa = p_shape_proxy( &s->g );
+	ShapeProxy pb = p_make_proxy( &position, 1, 0.0f );
+	xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+	SimplexCache cache = { 0 };
+	v2 pointA = V( 0.0f, 0.0f ), pointB = V( 0.0f, 0.0f ), normal = V( 0.0f, 0.0f );
+	float d = p_shape_distance( &pa, &pb, xf, identity, &cache, &pointA, &pointB, &normal );
+	// distance.c:592-603 useRadii
+	if ( d > 0.1f * P_LINEAR_SLOP )
+	{
+		d = fmaxp( 0.0f, d - pa.radius - pb.radius );
+		pointA = mulAdd( pointA, pa.radius, normal );
+	}
+	if ( d > r + fo )
+		return 1;
+	if ( b->setIndex >= SET_FIRST_SLEEPING )
+		p_wake_solver_set( w, b->setIndex );
+	if ( b->setIndex != SET_AWAKE )
+		return 1;
+	v2 closestPoint = pointA;
+	if ( d == 0.0f )
+		closestPoint = xfPoint( xf, p_shape_centroid( &s->g ) );
+	v2 direction = sub( closestPoint, position );
+	if ( lengthSq( direction ) > 100.0f * FLT_EPSILON * FLT_EPSILON )
+		direction = normalize( direction );
+	else
+		direction = V( 1.0f, 0.0f );
+	v2 localLine = invRotate( xf.q, leftPerp( direction ) );
+	float perimeter = projected_perimeter( s, localLine );
+	float scale = 1.0f;
+	if ( d > r && fo > 0.0f )
+		scale = fclampp( ( r + fo - d ) / fo, 0.0f, 1.0f );
+	float magnitude = e->ipl * perimeter * scale;
+	v2 impulse = mulSV( magnitude, direction );
+	b->v = mulAdd( b->v, b->invMass, impulse );
+	b->w += b->invInertia * cross( sub( closestPoint, b->center ), impulse );
+	return 1;
+}
+
+// world.c:2718-2747 b2World_Explode: the dynamic tree's query over the
+// blast box
 void orc_world_explode( int wi, long long maskBits, double px, double py, double radius, double falloff,
 						double impulsePerLength )
 {
 	World* w = p_world( wi );
 	if ( w == NULL )
 		return;
-	v2 position = V( (float)px, (float)py );
-	float r = (float)radius, fo = (float)falloff, ipl = (float)impulsePerLength;
+	ExplodeCtx e = { w, V( (float)px, (float)py ), (float)radius, (float)falloff, (float)impulsePerLength };
 	box2 box;
-	box.lo = V( position.x - ( r + fo ), position.y - ( r + fo ) );
-	box.hi = V( position.x + ( r + fo ), position.y + ( r + fo ) );
-	for ( int id = 0; id < w->shapeCount; ++id )
-	{
-		const Shape* s = w->shapes + id;
-		if ( s->used == 0 || s->proxyKey == P_NULL || ( s->proxyKey & 3 ) != BODY_DYNAMIC )
-			continue;
-		if ( ( s->categoryBits & (uint64_t)maskBits ) == 0 || boxOverlaps( s->fatAABB, box ) == 0 )
-			continue;
-		Body* b = w->bodies + s->bodyId;
-		xform xf = b->xf;
-		ShapeProxy pa = p_shape_proxy( &s->g );
-		ShapeProxy pb = p_make_proxy( &position, 1, 0.0f );
-		xform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
-		SimplexCache cache = { 0 };
-		v2 pointA = V( 0.0f, 0.0f ), pointB = V( 0.0f, 0.0f ), normal = V( 0.0f, 0.0f );
-		float d = p_shape_distance( &pa, &pb, xf, identity, &cache, &pointA, &pointB, &normal );
-		// distance.c:592-603 useRadii
-		if ( d > 0.1f * P_LINEAR_SLOP )
-		{
-			d = fmaxp( 0.0f, d - pa.radius - pb.radius );
-			pointA = mulAdd( pointA, pa.radius, normal );
-		}
-		if ( d > r + fo )
-			continue;
-		if ( b->setIndex >= SET_FIRST_SLEEPING )
-			p_wake_solver_set( w, b->setIndex );
-		if ( b->setIndex != SET_AWAKE )
-			continue;
-		v2 closestPoint = pointA;
-		if ( d == 0.0f )
-			closestPoint = xfPoint( xf, p_shape_centroid( &s->g ) );
-		v2 direction = sub( closestPoint, position );
-		if ( lengthSq( direction ) > 100.0f * FLT_EPSILON * FLT_EPSILON )
-			direction = normalize( direction );
-		else
-			direction = V( 1.0f, 0.0f );
-		v2 localLine = invRotate( xf.q, leftPerp( direction ) );
-		float perimeter = projected_perimeter( s, localLine );
-		float scale = 1.0f;
-		if ( d > r && fo > 0.0f )
-			scale = fclampp( ( r + fo - d ) / fo, 0.0f, 1.0f );
-		float magnitude = ipl * perimeter * scale;
-		v2 impulse = mulSV( magnitude, direction );
-		b->v = mulAdd( b->v, b->invMass, impulse );
-		b->w += b->invInertia * cross( sub( closestPoint, b->center ), impulse );
-	}
+	box.lo = V( e.position.x - ( e.r + e.fo ), e.position.y - ( e.r + e.fo ) );
+	box.hi = V( e.position.x + ( e.r + e.fo ), e.position.y + ( e.r + e.fo ) );
+	p_finish_tree_rebuild( w );
+	rt_query( w->trees + BODY_DYNAMIC, box, (uint64_t)maskBits, explode_visit, &e );
 }
 
 typedef struct RayHitRow

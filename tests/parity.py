@@ -356,3 +356,26 @@ def rounded_scene(w):
 def rounded_rays(n=200, seed=4):
     rng = np.random.default_rng(seed)
     return [(rng.uniform(-18, 18, 2) + [0.0, 6.0], rng.uniform(-20, 20, 2)) for _ in range(n)]
+
+
+def multishape_scene(w):
+    """Bodies of two or three shapes each over a ground, for explosions whose
+    impulses on one body add up over several shapes (the order of the
+    dynamic tree's query fixes the sum's last bits)."""
+    from forge2d_gb300 import scenes
+    rng = np.random.default_rng(12)
+    ground = w.create_body(scenes.body_def(type=0, positionY=-1.0))
+    w.create_box(ground, scenes.shape_def(), 30.0, 1.0)
+    for k in range(90):
+        b = w.create_body(scenes.body_def(type=2, positionX=float(rng.uniform(-12, 12)),
+                                          positionY=float(rng.uniform(1, 14))))
+        w.create_box(b, scenes.shape_def(), 0.35, 0.25)
+        w.create_circle(b, scenes.shape_def(density=2.0), 0.4, 0.1, 0.2)
+        if k % 2:
+            w.create_capsule(b, scenes.shape_def(), -0.3, -0.2, 0.0, -0.4, 0.12)
+
+
+# frame -> blasts (x, y, radius, falloff, impulse per length, mask) into the
+# multi-shape scene: through sleeping sets late, with and without falloff
+MULTI_BLASTS = {60: (0.0, 2.0, 4.0, 2.0, 3.0, -1), 150: (5.0, 1.0, 3.0, 0.0, 6.0, -1),
+                260: (-4.0, 1.5, 5.0, 3.0, 4.0, 0x1)}

@@ -18,7 +18,8 @@ import pytest
 
 from forge2d_gb300 import scenes
 
-from parity import blast, compare_contacts, edit_motors, install_callbacks, ray_answers, rounded_rays, rounded_scene
+from parity import (MULTI_BLASTS, blast, compare_contacts, edit_motors, install_callbacks, multishape_scene, ray_answers,
+                    rounded_rays, rounded_scene)
 from test_oracle_golden import (CASES, GOLD, SENSOR_CASES, STATS_CASES, check_sensor_rows, check_sets, frame_stats,
                                 replay, sensor_rows)
 
@@ -118,6 +119,27 @@ def test_gpu_explode_matches_port(gpu_lib, port_lib, sleep):
         p.step(1.0 / 60.0, 4)
         assert_bodies_equal(g, p, f)
     assert g.sync() == 0
+    g.close()
+    p.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_gpu_explode_multishape_matches_port(gpu_lib, port_lib, sleep):
+    """Explosions over bodies of several shapes through sleeping sets: shapes
+    in the dynamic tree's query order (wake order, impulse sums)."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    g = gpu_world(gpu_lib, wkw)
+    p = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (g, p):
+        multishape_scene(w)
+    for f in range(1, 321):
+        if f in MULTI_BLASTS:
+            x, y, r, fo, ipl, mask = MULTI_BLASTS[f]
+            for w in (g, p):
+                w.explode(x, y, r, fo, ipl, mask=mask)
+        assert g.step(1.0 / 60.0, 4) == 0
+        p.step(1.0 / 60.0, 4)
+        assert_bodies_equal(g, p, f)
     g.close()
     p.close()
 

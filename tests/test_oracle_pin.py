@@ -18,7 +18,7 @@ from forge2d_gb300 import scenes
 
 from parity import (blast, build_property_scene, compare_contacts, destroy_script, edit_motors, filter_rule,
                     install_callbacks, new_contacts, pre_solve_rule, property_reads, property_script, ray_answers,
-                    point_answers, rounded_rays, rounded_scene, touching_pair)
+                    point_answers, rounded_rays, rounded_scene, touching_pair, multishape_scene, MULTI_BLASTS)
 
 
 def trees_equal(ref, port):
@@ -514,5 +514,25 @@ def test_port_rounded_polygon_rays_with_reference(ref_lib, port_lib):
     a, b = ray_answers(ref, rays), ray_answers(port, rays)
     assert a == b
     assert sum(len(x[1]) for x in a) > 100
+    ref.close()
+    port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_explode_multishape_with_reference(ref_lib, port_lib, sleep):
+    """Explosions over bodies of several shapes each, through sleeping sets:
+    the shapes are visited in the dynamic tree's query order, which fixes
+    the order sets wake in and the order a body's impulses add up."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    for w in (ref, port):
+        multishape_scene(w)
+    for f in range(1, 321):
+        if f in MULTI_BLASTS:
+            x, y, r, fo, ipl, mask = MULTI_BLASTS[f]
+            for w in (ref, port):
+                w.explode(x, y, r, fo, ipl, mask=mask)
+        lockstep_full(ref, port, 1, start=f)
     ref.close()
     port.close()
