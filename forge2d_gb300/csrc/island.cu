@@ -1584,6 +1584,8 @@ __global__ void k_isl_link_chain( DWorld w, DIslands* Ip )
 		DIsland& isl = I.islands[id];
 		int next;
 		if ( first )
+			I.pos[id] = p; // the segment's first position, for k_isl_link_heads
+		if ( first )
 		{
 			// the island's old head and tail (written below only by the
 			// segment's last / first thread, after these reads by the same
@@ -1614,9 +1616,7 @@ __global__ void k_isl_link_heads( DWorld w, DIslands* Ip )
 		bool last = p + 1 == n || (int)( I.ncKeys[p + 1] >> 32 ) != id;
 		if ( !last )
 			continue;
-		int q = p;
-		while ( q > 0 && (int)( I.ncKeys[q - 1] >> 32 ) == id )
-			q -= 1;
+		int q = I.pos[id];
 		DIsland& isl = I.islands[id];
 		int c = w.opContact[(int)( key & 0xffffffffull )];
 		if ( isl.tailContact == ISL_NULL )
