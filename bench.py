@@ -358,6 +358,8 @@ def run_gpu(args, rank, world):
         "wall_s_timed_region": wall,
     }
     forms = {}
+    if args.sleep_form:
+        forms["sleep_on"] = run_sleep_on(args, torch, frames, flush, bodies)
     if args.batched:
         forms["batched"] = run_batched(args, torch)
     if args.learned:
@@ -367,6 +369,36 @@ def run_gpu(args, rank, world):
     if rank == 0 and args.cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, bodies_hint=bodies)
     return result, rank
+
+
+def run_sleep_on(args, torch, frames, flush, bodies):
+    """The same workload and frames with sleeping on, forge2d's default
+    (islands, sleeping sets and their bookkeeping kept every step): device
+    time of the same timed frames, L2 flushed before each."""
+    from forge2d_gb300 import scenes
+    from forge2d_gb300.world import GpuWorld
+    spec = WORKLOADS[args.workload]
+    g = GpuWorld(scenes.world_def(enableSleep=1, enableContinuous=1))
+    scenes.build(g, spec["scene"], **spec["kw"])
+    frame, total_ms, status = 0, 0.0, 0
+    for target in frames:
+        while frame < target:
+            status |= g.step(1.0 / 60.0, 4)
+            frame += 1
+        status |= g.sync()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        status |= g.step(1.0 / 60.0, 4)
+        status |= g.sync()
+        frame += 1
+        total_ms += g.last_step_ms()
+    c = g.counters()
+    g.close()
+    ms = total_ms / len(frames)
+    return {"what": "the main workload with sleeping on (islands and sleeping sets kept on the device), "
+                    "the same timed frames; value counts the main line's bodies", "ms_per_step": ms,
+            "value": bodies * 1e3 / ms if ms > 0 else None, "unit": "body-steps/s",
+            "awake_end": c["awake_bodies"], "status": status}
 
 
 class _SubRecorder:
@@ -667,6 +699,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="wall-clock seconds after which the CPU arm stops taking timed frames")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-sleep-form", dest="sleep_form", action="store_false",
+                    help="skip the sleeping-on measurement of the main workload")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the batched form (4096 sub-worlds) beside the headline workload")
     ap.add_argument("--batch-worlds", type=int, default=4096)
