@@ -192,7 +192,7 @@ def run_gpu(args, rank, world):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     spec = WORKLOADS[args.workload]
-    wd = scenes.world_def(enableSleep=0, enableContinuous=1)
+    wd = scenes.world_def(enableSleep=1 if args.sleep else 0, enableContinuous=1)
     g = GpuWorld(wd)
     scenes.build(g, spec["scene"], **spec["kw"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -324,7 +324,7 @@ def run_gpu(args, rank, world):
                    "frames": "%d timed frames spread over frames %d..%d of the scene's %d (first %d, last %d), "
                              "the others stepped untimed" % (len(frames), args.warmup, spec["frames"] - 1,
                                                              spec["frames"], frames[0], frames[-1]),
-                   "sleep": False, "continuous": True, "substeps": 4,
+                   "sleep": bool(args.sleep), "continuous": True, "substeps": 4,
                    "l2": "flushed before every timed step (512 MB write, untimed)",
                    "parallelism": "replicas" if nranks > 1 else "single world",
                    "contacts_live_end": counters_after["contacts"],
@@ -699,6 +699,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="wall-clock seconds after which the CPU arm stops taking timed frames")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--sleep", action="store_true",
+                    help="create the main workload's worlds with sleeping on (profiling of the island path)")
     ap.add_argument("--no-sleep-form", dest="sleep_form", action="store_false",
                     help="skip the sleeping-on measurement of the main workload")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
