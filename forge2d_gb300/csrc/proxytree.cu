@@ -770,16 +770,29 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_large( DWorld w, int t, uns
 struct PtSmall
 {
 	int idx[PT_SMALL];
-	float2 cen[PT_SMALL];
-	int bl[PT_SMALL];
-	int br[PT_SMALL];
 	int freed[PT_SMALL];
-	int4 item[2][PT_SMALL / 2];
-	int split[PT_SMALL / 2];
-	int4 kid[PT_SMALL]; // (node, child1, child2, -) in creation order
+	int4 kid[PT_SMALL]; // (freed position, child1, child2, -) in creation order
 	int levelStart[PT_SMALL_LEVELS + 1];
 	int count[2];
 	int kidCount;
+	union
+	{
+		struct // the median-split levels
+		{
+			float2 cen[PT_SMALL];
+			int bl[PT_SMALL];
+			int br[PT_SMALL];
+			int4 item[2][PT_SMALL / 2];
+			int split[PT_SMALL / 2];
+		} b;
+		struct // the bottom-up pass: gathered nodes at their positions, then
+			   // the new internal nodes at PT_SMALL + freed position
+		{
+			float4 box[2 * PT_SMALL];
+			unsigned long long cat[2 * PT_SMALL];
+			int2 hl[2 * PT_SMALL]; // height, leaves
+		} r;
+	} u;
 };
 
 // a new internal node from its two children (dynamic_tree.c:1990-2010)
@@ -792,17 +805,67 @@ __device__ __forceinline__ void pt_refresh_node( const DProxyTree& T, int p, int
 	T.flags[p] = PT_ALLOCATED;
 }
 
+// b2PartitionMid (dynamic_tree.c:1426) on one thread: the centre bounds,
+// the pivot on the longer axis, then the Hoare partition itself (the k-th
+// centre of [s, s + below) that is not below the pivot swaps with the k-th
+// centre of [s + below, e) that is, counted from the end), the same pairs as
+// the warp form. Returns the split (nodes on the left).
+#define PT_SERIAL 32
+__device__ __forceinline__ int pt_partition_serial( int* idx, float2* cen, int s, int e )
+{
+	int cnt = e - s;
+	if ( cnt <= 2 )
+		return 1;
+	float lx = FLT_MAX, ly = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX;
+	for ( int i = s; i < e; ++i )
+	{
+		float2 c = cen[i];
+		lx = c.x < lx ? c.x : lx;
+		ly = c.y < ly ? c.y : ly;
+		hx = c.x > hx ? c.x : hx;
+		hy = c.y > hy ? c.y : hy;
+	}
+	float dx = hx - lx, dy = hy - ly;
+	bool axisY = !( dx > dy );
+	float pivot = axisY ? 0.5f * ( ly + hy ) : 0.5f * ( lx + hx );
+	int below = 0;
+	for ( int i = s; i < e; ++i )
+		below += pt_axis( cen[i], axisY ) < pivot ? 1 : 0;
+	if ( below == 0 || below == cnt )
+		return cnt / 2;
+	int mid = s + below, i = s, j = e - 1;
+	for ( ;; )
+	{
+		while ( i < mid && pt_axis( cen[i], axisY ) < pivot )
+			++i;
+		while ( j >= mid && !( pt_axis( cen[j], axisY ) < pivot ) )
+			--j;
+		// as many misplaced on each side, so both run out together
+		if ( i >= mid || j < mid )
+			break;
+		int ti = idx[i];
+		idx[i] = idx[j];
+		idx[j] = ti;
+		float2 tc = cen[i];
+		cen[i] = cen[j];
+		cen[j] = tc;
+		++i;
+		--j;
+	}
+	return below;
+}
+
 __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 {
 	extern __shared__ __align__( 16 ) unsigned char ptSmem[];
 	PtSmall& sm = *reinterpret_cast<PtSmall*>( ptSmem );
 	int* sIdx = sm.idx;
-	float2* sCen = sm.cen;
-	int* sBL = sm.bl;
-	int* sBR = sm.br;
+	float2* sCen = sm.u.b.cen;
+	int* sBL = sm.u.b.bl;
+	int* sBR = sm.u.b.br;
 	int* sFreed = sm.freed;
-	int4( *sItem )[PT_SMALL / 2] = sm.item;
-	int* sSplit = sm.split;
+	int4( *sItem )[PT_SMALL / 2] = sm.u.b.item;
+	int* sSplit = sm.u.b.split;
 	int* sCount = sm.count;
 	DScalars* sc = w.sc;
 	if ( sc->rbActive == 0 )
@@ -842,12 +905,21 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 			if ( threadIdx.x == 0 )
 				sm.levelStart[level] = sm.kidCount;
 			levels = level + 1;
+			// items of at most PT_SERIAL nodes: a thread each
+			for ( int it = threadIdx.x; it < m; it += blockDim.x )
+			{
+				int4 item = sItem[cur][it];
+				if ( item.y - item.x <= PT_SERIAL )
+					sSplit[it] = pt_partition_serial( sIdx, sCen, item.x, item.y );
+			}
+			// larger items: a warp each
 			for ( int it = wid; it < m; it += PT_WARPS )
 			{
 				int4 item = sItem[cur][it];
 				int s = item.x, e = item.y, cnt = e - s;
+				if ( cnt <= PT_SERIAL )
+					continue;
 				int split = 1;
-				if ( cnt > 2 )
 				{
 					float lx = FLT_MAX, ly = FLT_MAX, hx = -FLT_MAX, hy = -FLT_MAX;
 					for ( int i = s + lane; i < e; i += 32 )
@@ -941,7 +1013,10 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 				T.child2[node] = right;
 				T.parent[left] = node;
 				T.parent[right] = node;
-				sm.kid[atomicAdd( &sm.kidCount, 1 )] = make_int4( node, left, right, 0 );
+				// children by local slot: a gathered node by its position,
+				// a new internal node by PT_SMALL + its freed position
+				sm.kid[atomicAdd( &sm.kidCount, 1 )] =
+					make_int4( kn, le - s == 1 ? s : PT_SMALL + kl, e - le == 1 ? le : PT_SMALL + kr, 0 );
 				if ( le - s >= 2 )
 					sItem[cur ^ 1][atomicAdd( &sCount[cur ^ 1], 1 )] = make_int4( s, le, c1 + 1, 0 );
 				if ( e - le >= 2 )
@@ -956,12 +1031,37 @@ __global__ void __launch_bounds__( PT_THREADS ) k_pt_small( DWorld w, int t )
 			sm.levelStart[levels] = sm.kidCount;
 		__syncthreads();
 		// boxes, heights, categories and leaf counts bottom up, a level at a
-		// time (the children of a level were written before the barrier)
+		// time in shared memory (dynamic_tree.c:1990-2010), each new node
+		// written out once; the gathered nodes' values are read first
+		for ( int i = threadIdx.x; i < n; i += blockDim.x )
+		{
+			int g = sIdx[i];
+			sm.u.r.box[i] = T.box[g];
+			sm.u.r.cat[i] = T.cat[g];
+			sm.u.r.hl[i] = make_int2( T.height[g], T.leaves[g] );
+		}
+		__syncthreads();
 		for ( int level = levels - 1; level >= 0; --level )
 		{
 			int k0 = sm.levelStart[level], k1 = sm.levelStart[level + 1];
 			for ( int k = k0 + threadIdx.x; k < k1; k += blockDim.x )
-				pt_refresh_node( T, sm.kid[k].x, sm.kid[k].y, sm.kid[k].z );
+			{
+				int4 kd = sm.kid[k];
+				float4 bx = pt_union( sm.u.r.box[kd.y], sm.u.r.box[kd.z] );
+				unsigned long long ct = sm.u.r.cat[kd.y] | sm.u.r.cat[kd.z];
+				int2 ha = sm.u.r.hl[kd.y], hb = sm.u.r.hl[kd.z];
+				int2 hl = make_int2( 1 + max( ha.x, hb.x ), ha.y + hb.y );
+				int slot = PT_SMALL + kd.x;
+				sm.u.r.box[slot] = bx;
+				sm.u.r.cat[slot] = ct;
+				sm.u.r.hl[slot] = hl;
+				int node = sFreed[kd.x];
+				T.box[node] = bx;
+				T.cat[node] = ct;
+				T.height[node] = hl.x;
+				T.leaves[node] = hl.y;
+				T.flags[node] = PT_ALLOCATED;
+			}
 			__syncthreads();
 		}
 	}
