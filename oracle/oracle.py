@@ -218,6 +218,9 @@ def _bind(lib, prefix):
         "world_enable_sleeping": (None, [i, i]),
         "tree_order": (i, [i, i, _P(i), i]),
         "destroy_body": (None, [i, i]),
+        "body_set_type": (None, [i, i, i]),
+        "body_disable": (None, [i, i]),
+        "body_enable": (None, [i, i]),
         "destroy_shape": (None, [i, i, i]),
         "destroy_joint": (None, [i, i]),
         "destroy_chain": (None, [i, i]),
@@ -342,6 +345,15 @@ class _CpuWorld:
         self._fns["joint_set_param"](self.w, joint, self._code(code), value, value2)
 
     # destroy path -----------------------------------------------------
+    def body_set_type(self, body, body_type):
+        self._fns["body_set_type"](self.w, body, body_type)
+
+    def body_disable(self, body):
+        self._fns["body_disable"](self.w, body)
+
+    def body_enable(self, body):
+        self._fns["body_enable"](self.w, body)
+
     def destroy_body(self, body):
         self._fns["destroy_body"](self.w, body)
 

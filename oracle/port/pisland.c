@@ -804,6 +804,25 @@ void p_set_remove_body( World* w, int bodyId )
 	b->setIndex = P_NULL;
 }
 
+// solver_set.c:521-556 b2TransferBody: the body joins the target set's
+// array and leaves the source set's by swap-remove; a body entering the awake
+// set gets the identity state and one leaving it loses its state (velocity)
+void p_transfer_body( World* w, int targetSet, int bodyId )
+{
+	Body* b = w->bodies + bodyId;
+	int src = b->setIndex;
+	set_body_remove( w, src, bodyId );
+	p_set_body_add( w, targetSet, bodyId );
+	if ( src == SET_AWAKE || targetSet == SET_AWAKE )
+	{
+		b->v = V( 0.0f, 0.0f );
+		b->w = 0.0f;
+		b->dp = V( 0.0f, 0.0f );
+		b->dq.c = 1.0f;
+		b->dq.s = 0.0f;
+	}
+}
+
 static void remove_swap_value( IntArr* a, int v )
 {
 	for ( int i = 0; i < a->count; ++i )
@@ -840,4 +859,23 @@ int p_wake_body( World* w, int bodyId )
 		return 1;
 	}
 	return 0;
+}
+
+// solver_set.c:558-613 b2TransferJoint: out of the constraint graph (awake)
+// or the source set's array (swap-remove), into the graph (awake) or the
+// target set's array (appended)
+void p_transfer_joint( World* w, int targetSet, int jid )
+{
+	Joint* j = w->joints + jid;
+	if ( j->setIndex == SET_AWAKE )
+		p_remove_joint_from_graph( w, jid );
+	else
+		p_set_remove_joint( w, jid );
+	if ( targetSet == SET_AWAKE )
+	{
+		j->setIndex = SET_AWAKE;
+		p_add_joint_to_graph( w, jid );
+	}
+	else
+		p_set_joint_add( w, targetSet, jid );
 }

@@ -231,6 +231,7 @@ typedef struct Joint
 	int type; // P_JOINT_*
 	int bodyA, bodyB;
 	int color;
+	int colorBodies; // bit 0 / 1: body A / B took the colour's bit when coloured
 	int overflowIndex;
 	int collideConnected;
 	int nextA, prevA, nextB, prevB; // body joint lists (joint keys)
@@ -489,6 +490,8 @@ int p_new_sleeping_set( World* w );
 void p_set_joint_add( World* w, int setId, int jid );
 void p_merge_solver_sets( World* w, int setId1, int setId2 );
 void p_unlink_joint( World* w, int jid );
+void p_transfer_body( World* w, int targetSet, int bodyId );
+void p_transfer_joint( World* w, int targetSet, int jid );
 void p_remove_body_from_island( World* w, int bodyId );
 void p_set_remove_body( World* w, int bodyId );
 void p_set_remove_contact( World* w, int cid );

@@ -996,6 +996,7 @@ void p_add_joint_to_graph( World* w, int jid )
 {
 	Joint* j = w->joints + jid;
 	j->color = assign_joint_color( w, j->bodyA, j->bodyB );
+	j->colorBodies = ( w->bodies[j->bodyA].type != BODY_STATIC ? 1 : 0 ) | ( w->bodies[j->bodyB].type != BODY_STATIC ? 2 : 0 );
 	if ( j->color == P_OVERFLOW )
 	{
 		w->overflowJoints = grow( w->overflowJoints, &w->overflowJointCap, w->overflowJointCount + 1, sizeof( int ) );
@@ -1013,9 +1014,15 @@ void p_remove_joint_from_graph( World* w, int jid )
 		return;
 	if ( j->color != P_OVERFLOW )
 	{
+		// the bits its colouring set: the reference clears both bodies' bits
+		// (constraint_graph.c:303-308), which differs only for a body that was
+		// static when the joint was coloured and is not any more (a type
+		// change), where it would free a bit another joint of that body holds
 		uint16_t bit = (uint16_t)( 1u << j->color );
-		w->bodies[j->bodyA].colorMask &= (uint16_t)~bit;
-		w->bodies[j->bodyB].colorMask &= (uint16_t)~bit;
+		if ( j->colorBodies & 1 )
+			w->bodies[j->bodyA].colorMask &= (uint16_t)~bit;
+		if ( j->colorBodies & 2 )
+			w->bodies[j->bodyB].colorMask &= (uint16_t)~bit;
 	}
 	else
 	{
@@ -2480,6 +2487,202 @@ void orc_destroy_body( int wi, int bodyId )
 	b->headJoint = P_NULL;
 	b->headContactKey = P_NULL;
 	free_id( &w->bodyFree, &w->bodyFreeCount, bodyId );
+}
+
+// ---------------------------------------------------------------------------
+// type changes, disable and enable (body.c:1036-1282, 1557-1700)
+// ---------------------------------------------------------------------------
+static Body* live_body( World* w, int bid );
+
+// shape.c:585-601 b2CreateShapeProxy with forcePairCreation: boxes for the
+// proxy's type, a leaf of that tree, the proxy buffered as moved
+static void create_proxy_forced( World* w, int sid, int proxyType )
+{
+	Shape* s = w->shapes + sid;
+	Body* b = w->bodies + s->bodyId;
+	box2 aabb = p_shape_aabb( &s->g, b->xf );
+	aabb.lo.x -= P_SPECULATIVE;
+	aabb.lo.y -= P_SPECULATIVE;
+	aabb.hi.x += P_SPECULATIVE;
+	aabb.hi.y += P_SPECULATIVE;
+	s->aabb = aabb;
+	float margin = proxyType == BODY_STATIC ? P_SPECULATIVE : P_AABB_MARGIN;
+	s->fatAABB.lo.x = aabb.lo.x - margin;
+	s->fatAABB.lo.y = aabb.lo.y - margin;
+	s->fatAABB.hi.x = aabb.hi.x + margin;
+	s->fatAABB.hi.y = aabb.hi.y + margin;
+	int proxyId = rt_create_proxy( w->trees + proxyType, s->fatAABB, s->categoryBits, sid );
+	s->proxyKey = ( proxyId << 2 ) | proxyType;
+	if ( proxyType == BODY_STATIC )
+		w->staticOrderDirty = 1;
+	push_move( w, sid );
+}
+
+static void recreate_proxies( World* w, Body* b, int proxyType )
+{
+	for ( int sid = b->headShape; sid != P_NULL; sid = w->shapes[sid].nextShape )
+	{
+		destroy_proxy( w, sid );
+		create_proxy_forced( w, sid, proxyType );
+	}
+}
+
+// body.c:1036-1282 b2Body_SetType
+void orc_body_set_type( int wi, int bodyId, int type )
+{
+	World* w = p_world( wi );
+	Body* b = live_body( w, bodyId );
+	if ( b == NULL || type < BODY_STATIC || type > BODY_DYNAMIC || b->type == type )
+		return;
+	int original = b->type;
+	if ( b->setIndex == SET_DISABLED )
+	{
+		b->type = type;
+		update_mass( w, b );
+		return;
+	}
+	// contacts go without waking the bodies they touched
+	for ( int key = b->headContactKey; key != P_NULL; )
+	{
+		int cid = key >> 1;
+		key = w->contacts[cid].edgeNext[key & 1];
+		destroy_contact_ex( w, cid, 0, 1 );
+	}
+	p_wake_body( w, bodyId );
+	for ( int key = b->headJoint; key != P_NULL; )
+	{
+		Joint* j = w->joints + ( key >> 1 );
+		key = ( key & 1 ) ? j->nextB : j->nextA;
+		if ( j->islandId != P_NULL )
+			p_unlink_joint( w, (int)( j - w->joints ) );
+		p_wake_body( w, j->bodyA );
+		p_wake_body( w, j->bodyB );
+	}
+	b->type = type;
+	if ( original == BODY_STATIC )
+	{
+		p_transfer_body( w, SET_AWAKE, bodyId );
+		p_create_island_for_body( w, SET_AWAKE, bodyId );
+		for ( int key = b->headJoint; key != P_NULL; )
+		{
+			int jid = key >> 1;
+			Joint* j = w->joints + jid;
+			key = ( key & 1 ) ? j->nextB : j->nextA;
+			if ( j->setIndex == SET_STATIC )
+				p_transfer_joint( w, SET_AWAKE, jid );
+			else if ( j->setIndex == SET_AWAKE )
+			{
+				// back into the graph for its colour
+				p_transfer_joint( w, SET_STATIC, jid );
+				p_transfer_joint( w, SET_AWAKE, jid );
+			}
+		}
+		recreate_proxies( w, b, type );
+	}
+	else if ( type == BODY_STATIC )
+	{
+		p_transfer_body( w, SET_STATIC, bodyId );
+		p_remove_body_from_island( w, bodyId );
+		b->isFast = 0;
+		for ( int key = b->headJoint; key != P_NULL; )
+		{
+			int jid = key >> 1;
+			Joint* j = w->joints + jid;
+			int other = ( key & 1 ) ? j->bodyA : j->bodyB;
+			key = ( key & 1 ) ? j->nextB : j->nextA;
+			if ( j->setIndex == SET_DISABLED )
+				continue;
+			p_transfer_joint( w, SET_STATIC, jid );
+			if ( w->bodies[other].setIndex != SET_STATIC )
+				p_transfer_joint( w, SET_AWAKE, jid );
+		}
+		recreate_proxies( w, b, BODY_STATIC );
+	}
+	else
+		recreate_proxies( w, b, type );
+	for ( int key = b->headJoint; key != P_NULL; )
+	{
+		int jid = key >> 1;
+		Joint* j = w->joints + jid;
+		int other = ( key & 1 ) ? j->bodyA : j->bodyB;
+		key = ( key & 1 ) ? j->nextB : j->nextA;
+		Body* o = w->bodies + other;
+		if ( o->setIndex == SET_DISABLED )
+			continue;
+		if ( b->type == BODY_STATIC && o->type == BODY_STATIC )
+			continue;
+		p_link_joint( w, jid, 0 );
+	}
+	p_merge_awake_islands( w );
+	update_mass( w, b );
+}
+
+// body.c:1557-1626 b2Body_Disable
+void orc_body_disable( int wi, int bodyId )
+{
+	World* w = p_world( wi );
+	Body* b = live_body( w, bodyId );
+	if ( b == NULL || b->setIndex == SET_DISABLED )
+		return;
+	for ( int key = b->headContactKey; key != P_NULL; )
+	{
+		int cid = key >> 1;
+		key = w->contacts[cid].edgeNext[key & 1];
+		destroy_contact_ex( w, cid, 1, 1 );
+	}
+	p_remove_body_from_island( w, bodyId );
+	for ( int sid = b->headShape; sid != P_NULL; sid = w->shapes[sid].nextShape )
+		destroy_proxy( w, sid );
+	p_transfer_body( w, SET_DISABLED, bodyId );
+	b->enabled = 0;
+	for ( int key = b->headJoint; key != P_NULL; )
+	{
+		int jid = key >> 1;
+		Joint* j = w->joints + jid;
+		key = ( key & 1 ) ? j->nextB : j->nextA;
+		if ( j->setIndex == SET_DISABLED )
+			continue;
+		if ( j->islandId != P_NULL )
+			p_unlink_joint( w, jid );
+		p_transfer_joint( w, SET_DISABLED, jid );
+	}
+}
+
+// body.c:1628-1700 b2Body_Enable
+void orc_body_enable( int wi, int bodyId )
+{
+	World* w = p_world( wi );
+	Body* b = live_body( w, bodyId );
+	if ( b == NULL || b->setIndex != SET_DISABLED )
+		return;
+	int setId = b->type == BODY_STATIC ? SET_STATIC : SET_AWAKE;
+	p_transfer_body( w, setId, bodyId );
+	b->enabled = 1;
+	for ( int sid = b->headShape; sid != P_NULL; sid = w->shapes[sid].nextShape )
+		create_proxy_forced( w, sid, b->type );
+	if ( setId != SET_STATIC )
+		p_create_island_for_body( w, setId, bodyId );
+	for ( int key = b->headJoint; key != P_NULL; )
+	{
+		int jid = key >> 1;
+		Joint* j = w->joints + jid;
+		key = ( key & 1 ) ? j->nextB : j->nextA;
+		Body* ba = w->bodies + j->bodyA;
+		Body* bb = w->bodies + j->bodyB;
+		if ( ba->setIndex == SET_DISABLED || bb->setIndex == SET_DISABLED )
+			continue;
+		int jointSet;
+		if ( ba->setIndex == SET_STATIC && bb->setIndex == SET_STATIC )
+			jointSet = SET_STATIC;
+		else if ( ba->setIndex == SET_STATIC )
+			jointSet = bb->setIndex;
+		else
+			jointSet = ba->setIndex;
+		p_transfer_joint( w, jointSet, jid );
+		if ( jointSet != SET_STATIC )
+			p_link_joint( w, jid, 0 );
+	}
+	p_merge_awake_islands( w );
 }
 
 // ---------------------------------------------------------------------------

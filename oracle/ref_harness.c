@@ -1176,6 +1176,21 @@ void ref_destroy_body( int w, int body )
 	b2DestroyBody( ref_body_id( w, body ) );
 }
 
+void ref_body_set_type( int w, int body, int type )
+{
+	b2Body_SetType( ref_body_id( w, body ), (b2BodyType)type );
+}
+
+void ref_body_disable( int w, int body )
+{
+	b2Body_Disable( ref_body_id( w, body ) );
+}
+
+void ref_body_enable( int w, int body )
+{
+	b2Body_Enable( ref_body_id( w, body ) );
+}
+
 void ref_destroy_shape( int w, int shape, int updateBodyMass )
 {
 	b2World* world = ref_world( w );

@@ -164,6 +164,37 @@ def destroy_script(world, f, ids):
         world.destroy_shape(ids["twin_box"], False)
 
 
+def type_script(world, f):
+    """Body type changes, disables and enables between steps, the same calls
+    on every world, on the scene of build_destroy_scene (ground 0, pyramid
+    boxes 1-72, chains of an anchor and ten links at 73, 84, 95 and 106, the
+    two-shape body 117): dynamic <-> static <-> kinematic with and without
+    joints, static anchors made dynamic, disabled bodies with joints, a type
+    change while disabled. No call turns a static body holding two joints of
+    the constraint graph non-static (the one colour deviation, see
+    test_port_type_change_colour_deviation)."""
+    calls = {
+        15: [("body_set_type", 12, 0)],      # a pyramid box becomes static
+        20: [("body_set_type", 78, 1)],      # a chain link (two joints) kinematic
+        25: [("body_set_type", 117, 1)],     # the two-shape body kinematic
+        35: [("body_set_type", 84, 2)],      # a static anchor (joint, no shapes) dynamic
+        40: [("body_set_type", 78, 2), ("body_set_type", 12, 2)],
+        50: [("body_disable", 89), ("body_disable", 30)],
+        55: [("body_set_type", 30, 1)],      # type change while disabled
+        65: [("body_set_type", 117, 2)],
+        70: [("body_enable", 89), ("body_enable", 30)],
+        80: [("body_set_type", 100, 0)],     # static between two dynamic links
+        85: [("body_set_type", 101, 0)],     # its neighbour too: a joint between statics
+        95: [("body_set_type", 101, 2)],     # static -> dynamic: one joint re-coloured, one from the static set
+        110: [("body_disable", 106)],        # a static anchor with a joint
+        120: [("body_enable", 106), ("body_set_type", 30, 2)],
+        130: [("body_disable", 40), ("body_set_type", 60, 0)],
+        135: [("body_enable", 40), ("body_set_type", 60, 2)],
+    }
+    for call in calls.get(f, ()):
+        getattr(world, call[0])(*call[1:])
+
+
 class _JointCounter:
     """Builder proxy that counts the joints created through it."""
 

@@ -18,7 +18,7 @@ from forge2d_gb300 import scenes
 
 from parity import (blast, build_property_scene, compare_contacts, destroy_script, edit_motors, filter_rule,
                     install_callbacks, new_contacts, pre_solve_rule, property_reads, property_script, ray_answers,
-                    point_answers, rounded_rays, rounded_scene, touching_pair, multishape_scene, MULTI_BLASTS)
+                    point_answers, rounded_rays, rounded_scene, touching_pair, multishape_scene, MULTI_BLASTS, type_script)
 
 
 def trees_equal(ref, port):
@@ -465,6 +465,61 @@ def test_port_destroy_path_with_reference(ref_lib, port_lib, sleep):
     assert ends > 0
     ref.close()
     port.close()
+
+
+@pytest.mark.parametrize("sleep", [0, 1])
+def test_port_type_changes_with_reference(ref_lib, port_lib, sleep):
+    """b2Body_SetType / b2Body_Disable / b2Body_Enable between steps (type
+    script of parity.py): bodies with their solver sets, contacts, colours,
+    trees and end events in lock step, with and without sleeping."""
+    wkw = dict(enableSleep=sleep, enableContinuous=1)
+    ref = ref_lib.RefWorld(scenes.world_def(**wkw))
+    port = port_lib.PortWorld(scenes.world_def(**wkw))
+    assert build_destroy_scene(ref) == build_destroy_scene(port)
+    events = 0
+    for f in range(1, 141):
+        type_script(ref, f)
+        type_script(port, f)
+        lockstep_full(ref, port, 1, start=f)
+        assert np.array_equal(ref.end_events(), port.end_events()), f
+        assert np.array_equal(ref.begin_events(), port.begin_events()), f
+        events += len(ref.end_events()) + len(ref.begin_events())
+        if f % 5 == 0:
+            assert compare_contacts(ref, port) == [], f
+            assert np.array_equal(ref.color_counts(), port.color_counts()), f
+            trees_equal(ref, port)
+    assert events > 0
+    ref.close()
+    port.close()
+
+
+def test_port_type_change_colour_deviation(ref_lib, port_lib):
+    """The one deviation of the type change: a static chain link holding two
+    joints of the constraint graph turned dynamic. The reference re-colours
+    its joints one by one and each graph removal clears both bodies' colour
+    bits (constraint_graph.c:303-308), including the bit the previous joint
+    of this (no longer static) body just took, so two joints of one dynamic
+    body end in one colour. Here a removal clears only the bits its colouring
+    set: the joints get different colours and the bodies agree up to that
+    step only."""
+    calls = {30: (5, 0), 35: (6, 0), 45: (5, 2)}
+    ws = [ref_lib.RefWorld(scenes.world_def(enableSleep=0)), port_lib.PortWorld(scenes.world_def(enableSleep=0))]
+    for w in ws:
+        scenes.chain(w, 0.0, 5.0, links=10)
+    for f in range(1, 46):
+        for w in ws:
+            if f in calls:
+                w.body_set_type(*calls[f])
+        if f < 45:
+            for w in ws:
+                w.step(1.0 / 60.0, 4)
+            assert np.array_equal(ws[0].bodies().view(np.uint32), ws[1].bodies().view(np.uint32)), f
+    ref_colors = [ws[0].joint_color(j) for j in (4, 5)]
+    port_colors = [ws[1].joint_color(j) for j in (4, 5)]
+    assert ref_colors[0] == ref_colors[1]       # joints 4-5 and 5-6 share body 5 and a colour
+    assert port_colors[0] != port_colors[1]
+    for w in ws:
+        w.close()
 
 
 @pytest.mark.parametrize("sleep", [0, 1])
