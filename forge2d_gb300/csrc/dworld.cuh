@@ -436,6 +436,7 @@ struct DWorld
 	int2* jbody;
 	int* jflags; // used, enableSpring, enableLimit, enableMotor, collideConnected; type in bits 8-11
 	int* jcolor;
+	int* jcolorSet; // bit 0 / 1: body A / B took the colour's bit when the joint was coloured
 	int* jnext;	 // [2*id+edge] next joint key in the body list
 	// definition, impulse and prepared rows; the revolute layout is given,
 	// the other types' layouts sit beside their solvers

@@ -569,6 +569,7 @@ __global__ void k_joint_ops( DWorld w, int count )
 				w.colorMask[d] |= 1u << color;
 		}
 		w.jcolor[j] = color;
+		w.jcolorSet[j] = color == F2D_OVERFLOW ? 0 : ( a >= 0 ? 1 : 0 ) | ( b >= 0 ? 2 : 0 );
 		if ( color == F2D_OVERFLOW )
 		{
 			w.overflowJoints[w.sc->overflowJointCount] = j;

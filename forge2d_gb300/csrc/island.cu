@@ -140,6 +140,7 @@ __device__ void isl_graph_add_joint( const DWorld& w, DIslands& I, int j )
 			w.colorMask[d] |= 1u << color;
 	}
 	w.jcolor[j] = color;
+	w.jcolorSet[j] = color == F2D_OVERFLOW ? 0 : ( a >= 0 ? 1 : 0 ) | ( b >= 0 ? 2 : 0 );
 	if ( color == F2D_OVERFLOW )
 	{
 		int idx = w.sc->overflowJointCount;
@@ -157,10 +158,14 @@ __device__ void isl_graph_remove_joint( const DWorld& w, DIslands& I, int j )
 	int2 jb = w.jbody[j];
 	if ( color != F2D_OVERFLOW )
 	{
+		// the bits its colouring set (the reference clears both bodies'
+		// bits, constraint_graph.c:303-308, which differs only for a body
+		// that was static when the joint was coloured and is not any more)
 		unsigned bit = 1u << color;
-		if ( !isl_static( w, jb.x ) )
+		int set = w.jcolorSet[j];
+		if ( set & 1 )
 			w.colorMask[jb.x] &= ~bit;
-		if ( !isl_static( w, jb.y ) )
+		if ( set & 2 )
 			w.colorMask[jb.y] &= ~bit;
 	}
 	else
@@ -1826,10 +1831,14 @@ __device__ void plain_graph_remove_joint( const DWorld& w, int j )
 	int2 jb = w.jbody[j];
 	if ( color != F2D_OVERFLOW )
 	{
+		// the bits its colouring set (the reference clears both bodies'
+		// bits, constraint_graph.c:303-308, which differs only for a body
+		// that was static when the joint was coloured and is not any more)
 		unsigned bit = 1u << color;
-		if ( !isl_static( w, jb.x ) )
+		int set = w.jcolorSet[j];
+		if ( set & 1 )
 			w.colorMask[jb.x] &= ~bit;
-		if ( !isl_static( w, jb.y ) )
+		if ( set & 2 )
 			w.colorMask[jb.y] &= ~bit;
 	}
 	else
@@ -1988,32 +1997,47 @@ __global__ void k_destroy_joint( DWorld w, DIslands* Ip, int j, int wake )
 	}
 }
 
+// body.c:99-157 b2RemoveBodyFromIsland: an island left without bodies goes
+__device__ void isl_remove_body_from_island( DIslands& I, int b )
+{
+	int id = I.bIsland[b];
+	if ( id == ISL_NULL )
+		return;
+	DIsland& isl = I.islands[id];
+	int prev = I.bIslandPrev[b], next = I.bIslandNext[b];
+	if ( prev != ISL_NULL )
+		I.bIslandNext[prev] = next;
+	if ( next != ISL_NULL )
+		I.bIslandPrev[next] = prev;
+	isl.bodyCount -= 1;
+	if ( isl.headBody == b )
+	{
+		isl.headBody = next;
+		if ( next == ISL_NULL )
+			isl_island_destroy_any( I, id );
+	}
+	else if ( isl.tailBody == b )
+		isl.tailBody = prev;
+	I.bIsland[b] = I.bIslandPrev[b] = I.bIslandNext[b] = ISL_NULL;
+}
+
+// body.c:84-96 b2CreateIslandForBody
+__device__ void isl_create_island_for_body( DIslands& I, int setId, int b )
+{
+	int isl = isl_island_create( I, setId );
+	I.bIsland[b] = isl;
+	I.bIslandPrev[b] = I.bIslandNext[b] = ISL_NULL;
+	I.islands[isl].headBody = I.islands[isl].tailBody = b;
+	I.islands[isl].bodyCount = 1;
+}
+
 // body.c:99-157 and :412-432: out of its island and its solver set
 __global__ void k_destroy_body_records( DWorld w, DIslands* Ip, int b )
 {
 	if ( Ip )
 	{
 		DIslands& I = *Ip;
-		int id = I.bIsland[b];
-		if ( id != ISL_NULL )
-		{
-			DIsland& isl = I.islands[id];
-			int prev = I.bIslandPrev[b], next = I.bIslandNext[b];
-			if ( prev != ISL_NULL )
-				I.bIslandNext[prev] = next;
-			if ( next != ISL_NULL )
-				I.bIslandPrev[next] = prev;
-			isl.bodyCount -= 1;
-			if ( isl.headBody == b )
-			{
-				isl.headBody = next;
-				if ( next == ISL_NULL )
-					isl_island_destroy_any( I, id );
-			}
-			else if ( isl.tailBody == b )
-				isl.tailBody = prev;
-			I.bIsland[b] = I.bIslandPrev[b] = I.bIslandNext[b] = ISL_NULL;
-		}
+		isl_remove_body_from_island( I, b );
 		int s = I.bSet[b];
 		if ( s == SET_AWAKE )
 			isl_awake_remove_body( I, b );
@@ -2029,6 +2053,264 @@ __global__ void k_destroy_body_records( DWorld w, DIslands* Ip, int b )
 		I.bHeadContact[b] = ISL_NULL;
 	}
 	w.bflags[b] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// type changes, disable and enable (body.c:1036-1282, 1557-1700) on the
+// device records, one thread; the host destroys the body's contacts before
+// (launch_destroy_contacts_of) and re-creates its proxies after. Worlds
+// without islands keep no set records: there a joint is in the awake set
+// when it holds a colour, in the disabled set when a body is disabled and in
+// the static set otherwise.
+// ---------------------------------------------------------------------------
+__device__ int joint_set_of( const DWorld& w, DIslands* Ip, int j )
+{
+	if ( Ip )
+		return Ip->jSet[j];
+	if ( w.jcolor[j] != F2D_NULL )
+		return SET_AWAKE;
+	int2 jb = w.jbody[j];
+	if ( ( w.bflags[jb.x] & BF_ENABLED ) == 0 || ( w.bflags[jb.y] & BF_ENABLED ) == 0 )
+		return SET_DISABLED;
+	return SET_STATIC;
+}
+
+// k_joint_ops' colouring for a world without islands (overflow joints keep
+// no index there)
+__device__ void plain_graph_add_joint( const DWorld& w, int j )
+{
+	int2 jb = w.jbody[j];
+	int a = isl_static( w, jb.x ) ? -1 : jb.x, b = isl_static( w, jb.y ) ? -1 : jb.y;
+	int color = F2D_OVERFLOW;
+	for ( int c = 0; c < F2D_OVERFLOW && ( a >= 0 || b >= 0 ); ++c )
+	{
+		unsigned used = ( a >= 0 ? w.colorMask[a] : 0u ) | ( b >= 0 ? w.colorMask[b] : 0u );
+		if ( ( used & ( 1u << c ) ) == 0 )
+		{
+			color = c;
+			break;
+		}
+	}
+	if ( color != F2D_OVERFLOW )
+	{
+		if ( a >= 0 )
+			w.colorMask[a] |= 1u << color;
+		if ( b >= 0 )
+			w.colorMask[b] |= 1u << color;
+	}
+	w.jcolor[j] = color;
+	w.jcolorSet[j] = color == F2D_OVERFLOW ? 0 : ( a >= 0 ? 1 : 0 ) | ( b >= 0 ? 2 : 0 );
+	if ( color == F2D_OVERFLOW )
+	{
+		w.overflowJoints[w.sc->overflowJointCount] = j;
+		w.sc->overflowJointCount += 1;
+	}
+}
+
+// solver_set.c:558-613 b2TransferJoint: out of the graph (awake) or the
+// source set's list, into the graph (awake) or the target set's list
+__device__ void transfer_joint( const DWorld& w, DIslands* Ip, int j, int target )
+{
+	int src = joint_set_of( w, Ip, j );
+	if ( src == SET_AWAKE )
+	{
+		if ( Ip )
+			isl_graph_remove_joint( w, *Ip, j );
+		else
+			plain_graph_remove_joint( w, j );
+	}
+	else if ( Ip && src >= SET_FIRST_SLEEPING )
+		isl_list_swap_remove( Ip->sets[src].headJoint, Ip->sets[src].tailJoint, Ip->sets[src].jointCount,
+							  [&]( int k ) -> int& { return Ip->jSetNext[k]; }, j );
+	if ( target == SET_AWAKE )
+	{
+		if ( Ip )
+		{
+			Ip->jSet[j] = SET_AWAKE;
+			isl_graph_add_joint( w, *Ip, j );
+		}
+		else
+			plain_graph_add_joint( w, j );
+	}
+	else if ( Ip && target >= SET_FIRST_SLEEPING )
+		isl_set_push_joint( *Ip, target, j );
+	else if ( Ip )
+		Ip->jSet[j] = target;
+}
+
+// b2_identityBodyState: a body entering or leaving the awake set
+__device__ void identity_state( const DWorld& w, int b )
+{
+	w.vel[b] = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	w.delta[b] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+}
+
+#define JOINT_KEYS( w, b, key, j )                                                                                      \
+	for ( int key = ( w ).headJoint[b], j = key >> 1, guard_ = 0; key != F2D_NULL && guard_ <= ( w ).jointCount;     \
+		  key = ( w ).jnext[2 * j + ( key & 1 )], j = key >> 1, ++guard_ )
+
+// body.c:1036-1282 b2Body_SetType
+__global__ void k_body_set_type( DWorld w, DIslands* Ip, int b, int type )
+{
+	int orig = body_type( w.bflags[b] );
+	if ( Ip )
+	{
+		isl_wake_body( w, *Ip, b );
+		JOINT_KEYS( w, b, key, j )
+		{
+			int2 jb = w.jbody[j];
+			if ( Ip->jIsland[j] != ISL_NULL )
+				isl_unlink_joint( *Ip, j );
+			isl_wake_body( w, *Ip, jb.x );
+			isl_wake_body( w, *Ip, jb.y );
+		}
+	}
+	// the joints' sets before the type changes
+	w.bflags[b] = ( w.bflags[b] & ~( 3 << BF_TYPE_SHIFT ) ) | ( type << BF_TYPE_SHIFT );
+	if ( orig == 0 )
+	{
+		if ( Ip )
+		{
+			isl_awake_add_body( w, *Ip, b );
+			isl_create_island_for_body( *Ip, SET_AWAKE, b );
+		}
+		identity_state( w, b );
+		JOINT_KEYS( w, b, key, j )
+		{
+			int s = joint_set_of( w, Ip, j );
+			if ( s == SET_STATIC )
+				transfer_joint( w, Ip, j, SET_AWAKE );
+			else if ( s == SET_AWAKE )
+			{
+				// back into the graph for its colour
+				transfer_joint( w, Ip, j, SET_STATIC );
+				transfer_joint( w, Ip, j, SET_AWAKE );
+			}
+		}
+	}
+	else if ( type == 0 )
+	{
+		if ( Ip )
+		{
+			isl_awake_remove_body( *Ip, b );
+			Ip->bSet[b] = SET_STATIC;
+			isl_remove_body_from_island( *Ip, b );
+		}
+		identity_state( w, b );
+		w.bflags[b] &= ~BF_IS_FAST;
+		JOINT_KEYS( w, b, key, j )
+		{
+			int2 jb = w.jbody[j];
+			int other = ( key & 1 ) ? jb.x : jb.y;
+			int s = joint_set_of( w, Ip, j );
+			if ( s == SET_DISABLED )
+				continue;
+			transfer_joint( w, Ip, j, SET_STATIC );
+			if ( body_type( w.bflags[other] ) != 0 )
+				transfer_joint( w, Ip, j, SET_AWAKE );
+		}
+	}
+	if ( Ip )
+	{
+		JOINT_KEYS( w, b, key, j )
+		{
+			int2 jb = w.jbody[j];
+			int other = ( key & 1 ) ? jb.x : jb.y;
+			if ( Ip->bSet[other] == SET_DISABLED )
+				continue;
+			if ( type == 0 && body_type( w.bflags[other] ) == 0 )
+				continue;
+			isl_link_joint( w, *Ip, j, false );
+		}
+		isl_merge_awake( *Ip );
+	}
+}
+
+// body.c:1557-1626 b2Body_Disable (contacts destroyed and proxies removed by
+// the host)
+__global__ void k_body_disable( DWorld w, DIslands* Ip, int b )
+{
+	int f = w.bflags[b];
+	int src = body_type( f ) == 0 ? SET_STATIC : SET_AWAKE;
+	if ( Ip )
+	{
+		DIslands& I = *Ip;
+		isl_remove_body_from_island( I, b );
+		src = I.bSet[b];
+		if ( src == SET_AWAKE )
+			isl_awake_remove_body( I, b );
+		else if ( src >= SET_FIRST_SLEEPING )
+			isl_list_swap_remove( I.sets[src].headBody, I.sets[src].tailBody, I.sets[src].bodyCount,
+								  [&]( int k ) -> int& { return I.bSetNext[k]; }, b );
+		I.bSet[b] = SET_DISABLED;
+	}
+	if ( src == SET_AWAKE )
+		identity_state( w, b );
+	JOINT_KEYS( w, b, key, j )
+	{
+		int s = joint_set_of( w, Ip, j );
+		if ( s == SET_DISABLED )
+			continue;
+		if ( Ip && Ip->jIsland[j] != ISL_NULL )
+			isl_unlink_joint( *Ip, j );
+		transfer_joint( w, Ip, j, SET_DISABLED );
+	}
+	w.bflags[b] = f & ~BF_ENABLED;
+}
+
+// body.c:1628-1700 b2Body_Enable (proxies re-created by the host)
+__global__ void k_body_enable( DWorld w, DIslands* Ip, int b )
+{
+	int setId = body_type( w.bflags[b] ) == 0 ? SET_STATIC : SET_AWAKE;
+	w.bflags[b] |= BF_ENABLED;
+	if ( Ip )
+	{
+		if ( setId == SET_AWAKE )
+			isl_awake_add_body( w, *Ip, b );
+		else
+			Ip->bSet[b] = SET_STATIC;
+	}
+	if ( setId == SET_AWAKE )
+		identity_state( w, b );
+	if ( Ip && setId != SET_STATIC )
+		isl_create_island_for_body( *Ip, setId, b );
+	JOINT_KEYS( w, b, key, j )
+	{
+		int2 jb = w.jbody[j];
+		if ( ( w.bflags[jb.x] & BF_ENABLED ) == 0 || ( w.bflags[jb.y] & BF_ENABLED ) == 0 )
+			continue;
+		bool sa = body_type( w.bflags[jb.x] ) == 0, sb = body_type( w.bflags[jb.y] ) == 0;
+		int jointSet = SET_STATIC;
+		if ( Ip )
+		{
+			int ba = Ip->bSet[jb.x], bb = Ip->bSet[jb.y];
+			jointSet = ( sa && sb ) ? SET_STATIC : ( ba == SET_STATIC ? bb : ba );
+			// from the disabled set
+			Ip->jSet[j] = SET_DISABLED;
+		}
+		else if ( !( sa && sb ) )
+			jointSet = SET_AWAKE;
+		transfer_joint( w, Ip, j, jointSet );
+		if ( Ip && jointSet != SET_STATIC )
+			isl_link_joint( w, *Ip, j, false );
+	}
+	if ( Ip )
+		isl_merge_awake( *Ip );
+}
+
+void launch_body_set_type( DWorld& w, cudaStream_t st, int body, int type )
+{
+	k_body_set_type<<<1, 1, 0, st>>>( w, w.isl, body, type );
+}
+
+void launch_body_disable( DWorld& w, cudaStream_t st, int body )
+{
+	k_body_disable<<<1, 1, 0, st>>>( w, w.isl, body );
+}
+
+void launch_body_enable( DWorld& w, cudaStream_t st, int body )
+{
+	k_body_enable<<<1, 1, 0, st>>>( w, w.isl, body );
 }
 
 // broad_phase.c:70-88 b2UnBufferMove: the proxy leaves the move array by

@@ -74,6 +74,10 @@ void launch_isl_api( DWorld& w, cudaStream_t st, int op, int body );
 void launch_destroy_contacts_of( DWorld& w, cudaStream_t st, int body, int shape, int other, int wake, int* list );
 void launch_destroy_joint( DWorld& w, cudaStream_t st, int joint, int wake );
 void launch_destroy_body_records( DWorld& w, cudaStream_t st, int body );
+// type changes, disable and enable (island.cu), serial launches between steps
+void launch_body_set_type( DWorld& w, cudaStream_t st, int body, int type );
+void launch_body_disable( DWorld& w, cudaStream_t st, int body );
+void launch_body_enable( DWorld& w, cudaStream_t st, int body );
 void launch_unbuffer_move( DWorld& w, cudaStream_t st, int shape );
 // microseconds per grid barrier on the grid-wide solver's grid (n barriers timed)
 float solver_barrier_probe( StepScratch& s, cudaStream_t st, unsigned* counter, int* err, int n );

@@ -374,6 +374,7 @@ static void grow_joints( HostWorld* W, int cap )
 	dgrow( d.jbody, o, cap );
 	dgrow( d.jflags, o, cap );
 	dgrow( d.jcolor, o, cap );
+	dgrow( d.jcolorSet, o, cap );
 	dgrow( d.jnext, 2 * o, 2 * (size_t)cap );
 	dgrow( d.jdef0, o, cap );
 	dgrow( d.jdef1, o, cap );
@@ -1173,7 +1174,7 @@ static void free_world( HostWorld* W )
 	F( nodeVisit ); F( sortHist ); F( pairKeys ); F( pairKeysAlt ); F( pairVal ); F( pairValAlt ); F( planIds );
 	F( planKeys ); F( opContact ); F( opKind ); F( opColor ); F( opDone ); F( opBodies ); F( opScan ); F( slotContact ); F( overflowList );
 	F( kIndex ); F( kMass ); F( kNormal ); F( kMisc ); F( kSoft ); F( kAnch1 ); F( kAnch2 ); F( kP1 ); F( kP2 );
-	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 ); F( jdef3 );
+	F( kImp ); F( kTot ); F( jbody ); F( jflags ); F( jcolor ); F( jcolorSet ); F( jnext ); F( jdef0 ); F( jdef1 ); F( jdef2 ); F( jdef3 );
 	F( jimp ); F( jimp2 ); F( jprep0 ); F( jprep1 ); F( jprep2 ); F( jprep3 ); F( jprepM ); F( jindex ); F( overflowJoints ); F( npBucket ); F( ovfOwner ); F( ovfLevel ); F( ovfOrder );
 	F( pendingJointOps ); F( fastBodies ); F( beginEv ); F( beginEvF ); F( endEv ); F( hitEvI ); F( hitEvF ); F( moveEvBody );
 	F( moveEvXf ); F( staticShapes ); F( sensorShapes ); F( sensorKeys ); F( sensorKeysAlt ); F( sensorPrevKeys );
@@ -2585,6 +2586,154 @@ static fxf body_xf( HostWorld* W, int b )
 	t.q.c = x.z;
 	t.q.s = x.w;
 	return t;
+}
+
+// ---------------------------------------------------------------------------
+// body type, disable and enable (body.c:1036-1282, 1557-1700): contacts and
+// proxies on the host side of the boundary as the destroy path does them,
+// solver sets, islands and graph colours in one device launch each
+// ---------------------------------------------------------------------------
+// the awake set's body array of a world without islands
+static void awake_order_add( HostWorld* W, int b )
+{
+	if ( W->islOn || W->awakeSlot[b] >= 0 )
+		return;
+	W->awakeSlot[b] = (int)W->awakeOrder.size();
+	W->awakeOrder.push_back( b );
+	W->awakeOrderDirty = true;
+}
+
+static void awake_order_remove( HostWorld* W, int b )
+{
+	if ( W->islOn || W->awakeSlot[b] < 0 )
+		return;
+	int k = W->awakeSlot[b];
+	int m = W->awakeOrder.back();
+	W->awakeOrder[k] = m;
+	W->awakeSlot[m] = k;
+	W->awakeOrder.pop_back();
+	W->awakeSlot[b] = -1;
+	W->awakeOrderDirty = true;
+}
+
+// shape.c:585-601 b2CreateShapeProxy with forcePairCreation: the boxes for
+// the proxy's type, a leaf of that tree, the proxy buffered as moved
+static void create_proxy_forced( HostWorld* W, int s, int proxyType )
+{
+	int b = W->shapeBody[s];
+	fxf xf = body_xf( W, b );
+	fbox aabb = box_grow( h_shape_aabb( W->hgeomv[s], xf ), F2D_SPECULATIVE );
+	fbox fat = box_grow( aabb, proxyType == 0 ? F2D_SPECULATIVE : F2D_AABB_MARGIN );
+	W->aabb[s] = box_to4( aabb );
+	W->fat[s] = box_to4( fat );
+	tree_pull( W, proxyType );
+	int proxyId = W->trees[proxyType].create_proxy( W->fat[s], W->cat[s], s );
+	W->treeDirty[proxyType] = true;
+	if ( proxyType == 0 )
+		W->staticDirty = true;
+	W->proxyKey[s] = ( proxyId << 2 ) | proxyType;
+	if ( s < W->shapeUploaded )
+	{
+		up( W->d.proxyKey, W->proxyKey, s, s + 1, W->stream );
+		up( W->d.aabb, W->aabb, s, s + 1, W->stream );
+		up( W->d.fat, W->fat, s, s + 1, W->stream );
+	}
+	host_move( W, s );
+}
+
+// after the device launch: the body's rows (type, state, flags) come back
+// to the host mirror, then its mass data (b2UpdateBodyMassData)
+static void type_change_end( HostWorld* W, int b )
+{
+	destroy_end( W );
+	body_rows_changed( W, false );
+	pull_body( W, b );
+	update_mass( W, b );
+	mark_body( W, b );
+}
+
+// RawBox2D.bodySetType (raw_box2d.dart:220) -> b2Body_SetType (body.c:1036)
+extern "C" F2D_API void f2d_body_set_type( int32_t index1, int32_t wg, int32_t type )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 || type < 0 || type > 2 )
+		return;
+	pull_body( W, b );
+	int f = W->bflags[b];
+	int orig = body_type( f );
+	if ( orig == type )
+		return;
+	if ( ( f & BF_ENABLED ) == 0 )
+	{
+		// a disabled body changes no set, island or proxy
+		edit_body_bits( W, b, type << BF_TYPE_SHIFT, 3 << BF_TYPE_SHIFT );
+		update_mass( W, b );
+		mark_body( W, b );
+		return;
+	}
+	destroy_begin( W );
+	launch_destroy_contacts_of( W->d, W->stream, b, -1, -1, 0, W->s.tmpA );
+	launch_body_set_type( W->d, W->stream, b, type );
+	W->bflags[b] = ( f & ~( 3 << BF_TYPE_SHIFT ) ) | ( type << BF_TYPE_SHIFT );
+	if ( orig == 0 )
+		awake_order_add( W, b );
+	else if ( type == 0 )
+		awake_order_remove( W, b );
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		destroy_proxy_host( W, s );
+		create_proxy_forced( W, s, type );
+	}
+	type_change_end( W, b );
+}
+
+// RawBox2D.bodyDisable (raw_box2d.dart:254) -> b2Body_Disable (body.c:1557)
+extern "C" F2D_API void f2d_body_disable( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	if ( ( W->bflags[b] & BF_ENABLED ) == 0 )
+		return;
+	destroy_begin( W );
+	launch_destroy_contacts_of( W->d, W->stream, b, -1, -1, 1, W->s.tmpA );
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		destroy_proxy_host( W, s );
+		edit_shape_bits( W, s, 0, SF_PROXY );
+	}
+	launch_body_disable( W->d, W->stream, b );
+	W->bflags[b] &= ~( BF_ENABLED | BF_ASLEEP );
+	awake_order_remove( W, b );
+	type_change_end( W, b );
+}
+
+// RawBox2D.bodyEnable (raw_box2d.dart:258) -> b2Body_Enable (body.c:1628)
+extern "C" F2D_API void f2d_body_enable( int32_t index1, int32_t wg )
+{
+	HostWorld* W;
+	int b = body_from( index1, wg, &W );
+	if ( b < 0 )
+		return;
+	pull_body( W, b );
+	int f = W->bflags[b];
+	if ( f & BF_ENABLED )
+		return;
+	destroy_begin( W );
+	launch_body_enable( W->d, W->stream, b );
+	W->bflags[b] = f | BF_ENABLED;
+	int type = body_type( f );
+	if ( type != 0 )
+		awake_order_add( W, b );
+	for ( int s = W->headShape[b]; s != F2D_NULL; s = W->nextShape[s] )
+	{
+		create_proxy_forced( W, s, type );
+		edit_shape_bits( W, s, SF_PROXY, 0 );
+	}
+	type_change_end( W, b );
 }
 
 extern "C" F2D_API double f2d_body_get_param( int32_t index1, int32_t wg, int32_t code )

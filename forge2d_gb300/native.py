@@ -199,6 +199,9 @@ _SIGS = [
     ("f2d_body_get_type", _i, [_i, _i]),
     ("f2d_body_is_awake", _i, [_i, _i]),
     ("f2d_body_set_awake", None, [_i, _i, _i]),
+    ("f2d_body_set_type", None, [_i, _i, _i]),
+    ("f2d_body_disable", None, [_i, _i]),
+    ("f2d_body_enable", None, [_i, _i]),
     ("f2d_body_is_sleep_enabled", _i, [_i, _i]),
     ("f2d_body_enable_sleep", None, [_i, _i, _i]),
     ("f2d_body_get_sleep_threshold", _d, [_i, _i]),

@@ -92,6 +92,19 @@ class GpuWorld:
         b = self._body(body)
         self.lib.f2d_destroy_body(b[0], b[1])
 
+    def body_set_type(self, body, body_type):
+        """b2Body_SetType; ``body`` is a creation handle or a body index."""
+        b = self._body(body)
+        self.lib.f2d_body_set_type(b[0], b[1], int(body_type))
+
+    def body_disable(self, body):
+        b = self._body(body)
+        self.lib.f2d_body_disable(b[0], b[1])
+
+    def body_enable(self, body):
+        b = self._body(body)
+        self.lib.f2d_body_enable(b[0], b[1])
+
     def destroy_shape(self, shape, update_mass=True):
         s = self._id("shape", shape)
         self.lib.f2d_destroy_shape(s[0], s[1], int(update_mass))
@@ -670,6 +683,18 @@ class Body:
     @property
     def type(self):
         return self.lib.f2d_body_get_type(*self.id)
+
+    @type.setter
+    def type(self, value):
+        self.lib.f2d_body_set_type(self.id[0], self.id[1], int(value))
+
+    @property
+    def is_enabled(self):
+        return bool(self.lib.f2d_body_get_param(self.id[0], self.id[1], native.CODES["F2D_BODY_ENABLED"]))
+
+    def set_enabled(self, flag):
+        """Body.setEnabled: b2Body_Enable / b2Body_Disable."""
+        (self.lib.f2d_body_enable if flag else self.lib.f2d_body_disable)(self.id[0], self.id[1])
 
     @property
     def is_valid(self):

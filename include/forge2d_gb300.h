@@ -258,6 +258,24 @@ F2D_API int32_t f2d_body_is_awake( int32_t index1, int32_t worldAndGeneration );
  * constraints were removed). Worlds created with sleeping off keep every body
  * awake and ignore it. */
 F2D_API void f2d_body_set_awake( int32_t index1, int32_t worldAndGeneration, int32_t awake );
+/* RawBox2D.bodySetType (raw_box2d.dart:220 -> b2Body_SetType, body.c:1036):
+ * type 0 static, 1 kinematic, 2 dynamic. The body's contacts end without
+ * waking anything, its joints move between the static and awake sets (and
+ * re-take graph colours), its proxies move to the new type's tree (forced
+ * pair search) and its mass data is recomputed. A disabled body only changes
+ * type and mass. One deviation: a removal from the constraint graph clears
+ * only the colour bits the joint's colouring set, so when a static body
+ * holding two or more joints of the graph turns non-static its joints take
+ * distinct colours where the reference can give two of them one colour. */
+F2D_API void f2d_body_set_type( int32_t index1, int32_t worldAndGeneration, int32_t type );
+/* RawBox2D.bodyDisable / bodyEnable (raw_box2d.dart:254-257 -> b2Body_Disable
+ * / b2Body_Enable, body.c:1557-1700): disabling ends the body's contacts
+ * (waking the bodies they touched), removes its proxies and moves it and its
+ * joints to the disabled set; enabling puts it back in the static or awake
+ * set with new proxies (forced pair search) and re-links its joints whose
+ * other body is enabled. */
+F2D_API void f2d_body_disable( int32_t index1, int32_t worldAndGeneration );
+F2D_API void f2d_body_enable( int32_t index1, int32_t worldAndGeneration );
 /* RawBox2D.bodyIsSleepEnabled / bodyEnableSleep (raw_box2d.dart:235-242 ->
  * b2Body_IsSleepEnabled / b2Body_EnableSleep; disabling wakes the body). */
 F2D_API int32_t f2d_body_is_sleep_enabled( int32_t index1, int32_t worldAndGeneration );
