@@ -650,7 +650,4 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	if ( w.isl )
 		launch_isl_new_contacts( w, s, st, planMode );
 	k_after_create<<<gridS, BP_THREADS, 0, st>>>( w, planMode );
-	// world.c:488-502: the dynamic and kinematic trees are rebuilt over their
-	// enlarged nodes every step
-	launch_pt_rebuild( w, s, st );
 }

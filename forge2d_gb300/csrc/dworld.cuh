@@ -106,6 +106,7 @@ struct DScalars
 	int error;
 	int colorRounds;
 	unsigned barrierCount;
+	unsigned ptBarrier; // the tree rebuild's grid barrier (it runs beside other kernels)
 	unsigned barrierGen;
 	int planCount;
 	int awakeCount;

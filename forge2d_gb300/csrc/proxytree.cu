@@ -1190,7 +1190,7 @@ void launch_pt_rebuild( DWorld& w, StepScratch& s, cudaStream_t st )
 		k_pt_gather<<<g, 256, 0, st>>>( w, t );
 		if ( s.ptBlocks > 0 )
 		{
-			unsigned* counter = &w.sc->barrierCount;
+			unsigned* counter = &w.sc->ptBarrier;
 			cudaMemsetAsync( counter, 0, sizeof( unsigned ), st );
 			void* args[] = { &w, &t, &counter };
 			cudaLaunchCooperativeKernel( (void*)k_pt_large, dim3( s.ptBlocks ), dim3( PT_THREADS ), args,

@@ -41,6 +41,9 @@ struct HostWorld
 	StepScratch s;
 	cudaStream_t stream = nullptr;
 	cudaEvent_t evStart = nullptr, evStop = nullptr;
+	// the tree rebuild's stream and its fork / join events
+	cudaStream_t stream2 = nullptr;
+	cudaEvent_t evFork = nullptr, evJoin = nullptr;
 	int* hostError = nullptr; // pinned
 	int statusAccum = 0;
 	bool stepped = false;
@@ -1138,8 +1141,11 @@ extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
 	d.enableContinuous = def->enableContinuous != 0;
 	d.enableWarmStarting = 1;
 	cudaStreamCreateWithFlags( &W->stream, cudaStreamNonBlocking );
+	cudaStreamCreateWithFlags( &W->stream2, cudaStreamNonBlocking );
 	cudaEventCreate( &W->evStart );
 	cudaEventCreate( &W->evStop );
+	cudaEventCreateWithFlags( &W->evFork, cudaEventDisableTiming );
+	cudaEventCreateWithFlags( &W->evJoin, cudaEventDisableTiming );
 	cudaMallocHost( (void**)&W->hostError, sizeof( int ) );
 	*W->hostError = 0;
 	cudaMalloc( (void**)&d.sc, sizeof( DScalars ) );
@@ -1196,6 +1202,9 @@ static void free_world( HostWorld* W )
 	cudaFreeHost( W->hostError );
 	cudaEventDestroy( W->evStart );
 	cudaEventDestroy( W->evStop );
+	cudaEventDestroy( W->evFork );
+	cudaEventDestroy( W->evJoin );
+	cudaStreamDestroy( W->stream2 );
 	cudaStreamDestroy( W->stream );
 }
 
@@ -1815,11 +1824,13 @@ static int create_joint_common( HostWorld* W, int a, int b, int flags, float4 d0
 	vset( W->jdef1, j, d1 );
 	vset( W->jdef2, j, d2 );
 	vset( W->jdef3, j, d3 );
-	// joints between two static bodies never enter the graph
+	// joints between two static bodies or with a disabled body never enter
+	// the graph
 	bool staticA = body_type( W->bflags[a] ) == 0, staticB = body_type( W->bflags[b] ) == 0;
+	bool enabled = ( W->bflags[a] & BF_ENABLED ) && ( W->bflags[b] & BF_ENABLED );
 	if ( W->islOn )
 		W->islLog.push_back( ( 1 << 30 ) | j ); // set, colour and island at the next upload
-	else if ( !( staticA && staticB ) )
+	else if ( !( staticA && staticB ) && enabled )
 		W->pendingJoints.push_back( j );
 	// joint.c:396-400 and the other constructors but the mouse and filter
 	// joints: contacts between bodies that may no longer collide go
@@ -3696,12 +3707,22 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 		cudaEventRecord( W->ph[0], W->stream );
 	bool filter = W->customFilter != nullptr, pre = W->preSolve != nullptr;
 	launch_broadphase( d, W->s, W->stream, planMode, filter ? pair_filter_hook : nullptr, W );
+	// world.c:488-502: the dynamic and kinematic trees are rebuilt over
+	// their enlarged nodes every step, beside the collide phase as the
+	// reference's rebuild task runs beside the collide tasks; nothing until
+	// the solver reads or writes them. The join comes before the solver: its
+	// persistent cooperative kernel needs the whole GPU.
+	cudaEventRecord( W->evFork, W->stream );
+	cudaStreamWaitEvent( W->stream2, W->evFork, 0 );
+	launch_pt_rebuild( d, W->s, W->stream2 );
+	cudaEventRecord( W->evJoin, W->stream2 );
 	if ( prof )
 		cudaEventRecord( W->ph[1], W->stream );
 	launch_narrowphase( d, W->s, W->stream, pre ? pre_solve_hook : nullptr, W );
 	if ( prof )
 		cudaEventRecord( W->ph[2], W->stream );
 	launch_graph( d, W->s, W->stream );
+	cudaStreamWaitEvent( W->stream, W->evJoin, 0 );
 	if ( prof )
 		cudaEventRecord( W->ph[3], W->stream );
 	launch_solver( d, W->s, W->stream, dt, subSteps );

@@ -27,7 +27,8 @@ def test_gpu_type_changes_match_port(gpu_lib, port_lib, sleep):
     wkw = dict(enableSleep=sleep, enableContinuous=1)
     gpu = GpuWorld(scenes.world_def(**wkw))
     port = port_lib.PortWorld(scenes.world_def(**wkw))
-    assert build_destroy_scene(gpu) == build_destroy_scene(port)
+    gids, pids = build_destroy_scene(gpu), build_destroy_scene(port)
+    assert gids["box"] == pids["box"] and gids["last"] == pids["last"]
     cols = 12 if sleep else 9
     for f in range(1, 141):
         type_script(gpu, f)
