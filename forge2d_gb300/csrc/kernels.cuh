@@ -38,6 +38,10 @@ struct StepScratch
 	int solverVariant;	 // SOLVER_* (the autotuner's choice; results never depend on it)
 	int ptBlocks;		 // co-resident grid of the tree rebuild's cooperative levels
 	cudaEvent_t evSolveStart; // recorded right before the cooperative solver launch when non-null
+	// streams beside the world's own for independent launches of one phase
+	// (the manifold classes), with their fork and join events
+	cudaStream_t side[4];
+	cudaEvent_t sideFork, sideJoin[4];
 };
 
 // solver variants: same arithmetic, different launch shapes

@@ -352,11 +352,29 @@ void launch_narrowphase( DWorld& w, StepScratch& s, cudaStream_t st, HostHook pr
 		preSolveHook( hookContext );
 	}
 	k_np_classify<<<grid_for( w.contactCap ), 256, 0, st>>>( w );
-	k_narrowphase<0><<<g, NP_THREADS, 0, st>>>( w );
-	k_narrowphase<1><<<g, NP_THREADS, 0, st>>>( w );
-	k_narrowphase<2><<<g, NP_THREADS, 0, st>>>( w );
-	k_narrowphase<3><<<g, NP_THREADS, 0, st>>>( w );
-	k_narrowphase<4><<<g, NP_THREADS, 0, st>>>( w );
+	// the classes update disjoint contacts: the polygon clipper and three
+	// short classes run beside the first class, each on its own stream
+	cudaStream_t cs[5] = { st, st, st, st, st };
+	if ( s.side[0] )
+	{
+		cudaEventRecord( s.sideFork, st );
+		for ( int k = 0; k < 4; ++k )
+		{
+			cudaStreamWaitEvent( s.side[k], s.sideFork, 0 );
+			cs[4 - k] = s.side[k];
+		}
+	}
+	k_narrowphase<4><<<g, NP_THREADS, 0, cs[4]>>>( w );
+	k_narrowphase<3><<<g, NP_THREADS, 0, cs[3]>>>( w );
+	k_narrowphase<2><<<g, NP_THREADS, 0, cs[2]>>>( w );
+	k_narrowphase<1><<<g, NP_THREADS, 0, cs[1]>>>( w );
+	k_narrowphase<0><<<g, NP_THREADS, 0, cs[0]>>>( w );
+	if ( s.side[0] )
+		for ( int k = 0; k < 4; ++k )
+		{
+			cudaEventRecord( s.sideJoin[k], s.side[k] );
+			cudaStreamWaitEvent( st, s.sideJoin[k], 0 );
+		}
 	k_op_flags<<<grid_for( w.contactCap ), 256, 0, st>>>( w, s.tmpA );
 	scan_lookback( s.tmpA, s.tmpB, &w.sc->contactIdCount, 0, w.contactCap, &w.sc->opCount, s.scanState, &w.sc->error,
 				   st );

@@ -1146,6 +1146,12 @@ extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
 	cudaEventCreate( &W->evStop );
 	cudaEventCreateWithFlags( &W->evFork, cudaEventDisableTiming );
 	cudaEventCreateWithFlags( &W->evJoin, cudaEventDisableTiming );
+	cudaEventCreateWithFlags( &W->s.sideFork, cudaEventDisableTiming );
+	for ( int k = 0; k < 4; ++k )
+	{
+		cudaStreamCreateWithFlags( &W->s.side[k], cudaStreamNonBlocking );
+		cudaEventCreateWithFlags( &W->s.sideJoin[k], cudaEventDisableTiming );
+	}
 	cudaMallocHost( (void**)&W->hostError, sizeof( int ) );
 	*W->hostError = 0;
 	cudaMalloc( (void**)&d.sc, sizeof( DScalars ) );
@@ -1204,6 +1210,12 @@ static void free_world( HostWorld* W )
 	cudaEventDestroy( W->evStop );
 	cudaEventDestroy( W->evFork );
 	cudaEventDestroy( W->evJoin );
+	cudaEventDestroy( W->s.sideFork );
+	for ( int k = 0; k < 4; ++k )
+	{
+		cudaEventDestroy( W->s.sideJoin[k] );
+		cudaStreamDestroy( W->s.side[k] );
+	}
 	cudaStreamDestroy( W->stream2 );
 	cudaStreamDestroy( W->stream );
 }
