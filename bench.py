@@ -283,6 +283,7 @@ def run_gpu(args, rank, world):
     reps = 3
     solve_ms, alg_bytes = [], []
     phases = np.zeros(6)
+    rebuild = 0.0
     for _ in range(reps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -290,6 +291,7 @@ def run_gpu(args, rank, world):
         g.sync()
         p = g.phase_ms()
         phases += p
+        rebuild += g.rebuild_ms() / reps
         solve_ms.append(p[4])
         alg_bytes.append(solver_bytes(g.counters()))
     g.set_profiling(False)
@@ -351,7 +353,8 @@ def run_gpu(args, rank, world):
                                          "their count in the last launch times the cost of one barrier measured "
                                          "by a launch of 2000 bare barriers on the same grid"}},
         "phases_ms": {"broadphase": phases[0], "narrowphase": phases[1], "colouring": phases[2],
-                      "solver_setup": phases[3], "solver_kernel": phases[4], "finalize": phases[5]},
+                      "solver_setup": phases[3], "solver_kernel": phases[4], "finalize": phases[5],
+                      "tree_rebuild_beside": rebuild},
         "gpu_launches": launches,
         "clocks": clk,
         "status": status,
@@ -489,6 +492,10 @@ def run_batched(args, torch):
         g.step(1.0 / 60.0, 4)
     st, chosen, taken = g.autotune(1.0 / 60.0, 4, 2)
     frames = 3 + taken
+    # untimed frames up to the config's last ones, then the timed steps
+    while frames < args.batch_frames - args.batch_steps:
+        st |= g.step(1.0 / 60.0, 4)
+        frames += 1
     torch.cuda.synchronize()
     ms = []
     for _ in range(args.batch_steps):
@@ -707,6 +714,8 @@ def main():
                     help="skip the batched form (4096 sub-worlds) beside the headline workload")
     ap.add_argument("--batch-worlds", type=int, default=4096)
     ap.add_argument("--batch-steps", type=int, default=30)
+    ap.add_argument("--batch-frames", type=int, default=1000,
+                    help="frames the batched form runs (its last batch-steps timed)")
     ap.add_argument("--batch-sample", type=int, default=16)
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned warm start (200k pile) beside the headline workload")

@@ -52,7 +52,7 @@ struct HostWorld
 
 	// phase timing (profiling mode: no graph, events between phases)
 	bool profiling = false;
-	cudaEvent_t ph[7] = {};
+	cudaEvent_t ph[9] = {}; // [7], [8]: the tree rebuild on its own stream
 
 	// graph replay
 	cudaGraphExec_t graphExec = nullptr;
@@ -3711,7 +3711,7 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	DWorld& d = W->d;
 	bool prof = W->profiling;
 	if ( prof && W->ph[0] == nullptr )
-		for ( int i = 0; i < 7; ++i )
+		for ( int i = 0; i < 9; ++i )
 			cudaEventCreate( W->ph + i );
 	W->s.evSolveStart = prof ? W->ph[4] : nullptr;
 	launch_reset_counters( d, W->stream );
@@ -3726,7 +3726,11 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	// persistent cooperative kernel needs the whole GPU.
 	cudaEventRecord( W->evFork, W->stream );
 	cudaStreamWaitEvent( W->stream2, W->evFork, 0 );
+	if ( prof )
+		cudaEventRecord( W->ph[7], W->stream2 );
 	launch_pt_rebuild( d, W->s, W->stream2 );
+	if ( prof )
+		cudaEventRecord( W->ph[8], W->stream2 );
 	cudaEventRecord( W->evJoin, W->stream2 );
 	if ( prof )
 		cudaEventRecord( W->ph[1], W->stream );
@@ -4999,6 +5003,18 @@ extern "C" F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 )
 		if ( cudaEventElapsedTime( &ms, W->ph[a[i]], W->ph[b[i]] ) == cudaSuccess )
 			out6[i] = ms;
 	}
+}
+
+extern "C" F2D_API double f2d_world_get_rebuild_ms( int32_t worldId )
+{
+	HostWorld* W = world_from_id( worldId );
+	if ( W == nullptr || W->ph[7] == nullptr )
+		return 0.0;
+	cudaStreamSynchronize( W->stream );
+	float ms = 0.0f;
+	if ( cudaEventElapsedTime( &ms, W->ph[7], W->ph[8] ) != cudaSuccess )
+		return 0.0;
+	return ms;
 }
 
 extern "C" F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 )

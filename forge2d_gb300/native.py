@@ -265,6 +265,7 @@ _SIGS = [
     ("f2d_world_get_tuning", None, [_i, _P(_i)]),
     ("f2d_world_set_profiling", None, [_i, _i]),
     ("f2d_world_get_phase_ms", None, [_i, _P(_d)]),
+    ("f2d_world_get_rebuild_ms", _d, [_i]),
     ("f2d_world_get_counters", None, [_i, _P(_i)]),
 ]
 

@@ -378,6 +378,10 @@ class GpuWorld:
         self.lib.f2d_world_get_phase_ms(self.id, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
+    def rebuild_ms(self) -> float:
+        """Profiling mode: the tree rebuild's time on its own stream."""
+        return float(self.lib.f2d_world_get_rebuild_ms(self.id))
+
     def solver_latency(self, probe_barriers=2000):
         """(grid barriers of the last grid-wide solver launch, measured
         microseconds per grid barrier on its grid)."""

@@ -651,6 +651,10 @@ F2D_API void f2d_world_set_profiling( int32_t worldId, int32_t enabled );
 /* Last profiled step, ms: broadphase, narrowphase, colouring, solver set-up,
  * solver kernel, finalize. */
 F2D_API void f2d_world_get_phase_ms( int32_t worldId, double* out6 );
+/* Last profiled step, ms: the partial rebuild of the dynamic and kinematic
+ * trees, which runs on a second stream beside the narrowphase and the
+ * colouring (world.c:488-502). */
+F2D_API double f2d_world_get_rebuild_ms( int32_t worldId );
 /* awake bodies, live contacts, touching contacts, overflow contacts, active
  * colours, colouring rounds, shapes, joints (b2Counters, types.h:493-506). */
 F2D_API void f2d_world_get_counters( int32_t worldId, int32_t* out8 );
