@@ -624,8 +624,18 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 {
 	int gridS = grid_for( w.shapeCount );
 	launch_pt_host_moves( w, s, st );
-	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, st>>>( w );
-	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, st>>>( w );
+	// the pair hash of the live contacts is built beside the leaf ordering,
+	// which does not touch it; both meet before the refit
+	cudaStream_t hs = s.side[0] ? s.side[0] : st;
+	if ( hs != st )
+	{
+		cudaEventRecord( s.sideFork, st );
+		cudaStreamWaitEvent( hs, s.sideFork, 0 );
+	}
+	k_hash_clear<<<grid_for( w.hashCap ), BP_THREADS, 0, hs>>>( w );
+	k_hash_insert<<<grid_for( w.contactCap ), BP_THREADS, 0, hs>>>( w );
+	if ( hs != st )
+		cudaEventRecord( s.sideJoin[0], hs );
 	k_leaf_flags<<<gridS, BP_THREADS, 0, st>>>( w, s.tmpA );
 	scan_lookback( s.tmpA, s.tmpB, nullptr, w.shapeCount, w.shapeCap, &w.sc->treeLeafCount, s.scanState, &w.sc->error,
 				   st, &w.sc->rebuildOrder );
@@ -635,6 +645,8 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	k_morton<<<gridS, BP_THREADS, 0, st>>>( w, s.bounds );
 	sort_coop<unsigned>( w.mortonKeys, w.leafShape, w.mortonKeysAlt, w.leafShapeAlt, &w.sc->treeLeafCount, 30,
 						 w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks32, st, &w.sc->rebuildOrder );
+	if ( hs != st )
+		cudaStreamWaitEvent( st, s.sideJoin[0], 0 );
 	k_wide_refit<<<( ( w.shapeCap + WIDE - 1 ) / WIDE + 7 ) / 8, BP_THREADS, 0, st>>>( w );
 	k_find_pairs<<<( w.shapeCap + FIND_WARPS - 1 ) / FIND_WARPS, BP_THREADS, 0, st>>>( w );
 	k_clamp_pairs<<<1, 1, 0, st>>>( w );
