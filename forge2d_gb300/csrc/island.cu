@@ -1535,23 +1535,45 @@ __global__ void k_isl_link_flags( DWorld w, DIslands* Ip, int* flag )
 	}
 }
 
+// The unions of the links between two islands, in op order (island.c:251-
+// 289: the root choice depends on it). One warp: the lanes read 32 ops and
+// their bodies' islands at once, lane 0 then walks the roots of the ones
+// that link two islands, one after another.
 __global__ void k_isl_link_roots( DWorld w, DIslands* Ip )
 {
 	DIslands& I = *Ip;
 	if ( I.serialOps )
 		return;
+	const int lane = threadIdx.x & 31;
 	int nOps = min( w.sc->opCount, w.opCap );
-	for ( int k = 0; k < nOps; ++k )
+	for ( int base = 0; base < nOps; base += 32 )
 	{
-		if ( w.opKind[k] != 1 || I.order[k] != ISL_NULL )
-			continue;
-		int2 bd = w.cbody[w.opContact[k]];
-		int idA = I.bIsland[bd.x], idB = I.bIsland[bd.y];
-		int rootA = idA != ISL_NULL ? isl_root( I, idA ) : ISL_NULL;
-		int rootB = idB != ISL_NULL ? isl_root( I, idB ) : ISL_NULL;
-		if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
-			I.islands[rootB].parent = rootA;
-		I.order[k] = rootA != ISL_NULL ? rootA : rootB;
+		int k = base + lane;
+		bool need = false;
+		int idA = ISL_NULL, idB = ISL_NULL;
+		if ( k < nOps && w.opKind[k] == 1 && I.order[k] == ISL_NULL )
+		{
+			int2 bd = w.cbody[w.opContact[k]];
+			idA = I.bIsland[bd.x];
+			idB = I.bIsland[bd.y];
+			need = true;
+		}
+		unsigned m = __ballot_sync( 0xffffffffu, need );
+		while ( m )
+		{
+			int src = __ffs( m ) - 1;
+			m &= m - 1;
+			int a = __shfl_sync( 0xffffffffu, idA, src ), b = __shfl_sync( 0xffffffffu, idB, src );
+			if ( lane == 0 )
+			{
+				int rootA = a != ISL_NULL ? isl_root( I, a ) : ISL_NULL;
+				int rootB = b != ISL_NULL ? isl_root( I, b ) : ISL_NULL;
+				if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
+					I.islands[rootB].parent = rootA;
+				I.order[base + src] = rootA != ISL_NULL ? rootA : rootB;
+			}
+			__syncwarp();
+		}
 	}
 }
 
@@ -1646,7 +1668,7 @@ void launch_isl_ops( DWorld& w, StepScratch& s, cudaStream_t st, const int* gkin
 	int* flag = s.tmpA + w.opCap;
 	int* pos = s.tmpB;
 	k_isl_link_flags<<<g, 256, 0, st>>>( w, w.isl, flag );
-	k_isl_link_roots<<<1, 1, 0, st>>>( w, w.isl );
+	k_isl_link_roots<<<1, 32, 0, st>>>( w, w.isl );
 	scan_lookback( flag, pos, &w.sc->opCount, 0, w.opCap, nullptr, scanState, &w.sc->error, st );
 	k_isl_link_keys<<<g, 256, 0, st>>>( w, w.isl, flag, pos );
 	int islandBits = 1;
