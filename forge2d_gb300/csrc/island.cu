@@ -1536,19 +1536,23 @@ __global__ void k_isl_link_flags( DWorld w, DIslands* Ip, int* flag )
 }
 
 // The unions of the links between two islands, in op order (island.c:251-
-// 289: the root choice depends on it). One warp: the lanes read 32 ops and
-// their bodies' islands at once, lane 0 then walks the roots of the ones
-// that link two islands, one after another.
-__global__ void k_isl_link_roots( DWorld w, DIslands* Ip )
+// 289: the root choice depends on it). One block: its threads read 1024 ops
+// and their bodies' islands at once and list the ones that link two
+// islands in op order (warp ballots, then the warps' offsets); thread 0
+// then walks their roots one after another.
+#define LINK_ROOTS_THREADS 1024
+__global__ void __launch_bounds__( LINK_ROOTS_THREADS ) k_isl_link_roots( DWorld w, DIslands* Ip )
 {
+	__shared__ int sK[LINK_ROOTS_THREADS], sA[LINK_ROOTS_THREADS], sB[LINK_ROOTS_THREADS];
+	__shared__ int sWarp[LINK_ROOTS_THREADS / 32 + 1];
 	DIslands& I = *Ip;
 	if ( I.serialOps )
 		return;
-	const int lane = threadIdx.x & 31;
+	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 	int nOps = min( w.sc->opCount, w.opCap );
-	for ( int base = 0; base < nOps; base += 32 )
+	for ( int base = 0; base < nOps; base += LINK_ROOTS_THREADS )
 	{
-		int k = base + lane;
+		int k = base + tid;
 		bool need = false;
 		int idA = ISL_NULL, idB = ISL_NULL;
 		if ( k < nOps && w.opKind[k] == 1 && I.order[k] == ISL_NULL )
@@ -1559,21 +1563,43 @@ __global__ void k_isl_link_roots( DWorld w, DIslands* Ip )
 			need = true;
 		}
 		unsigned m = __ballot_sync( 0xffffffffu, need );
-		while ( m )
+		if ( lane == 0 )
+			sWarp[wid] = __popc( m );
+		__syncthreads();
+		if ( tid == 0 )
 		{
-			int src = __ffs( m ) - 1;
-			m &= m - 1;
-			int a = __shfl_sync( 0xffffffffu, idA, src ), b = __shfl_sync( 0xffffffffu, idB, src );
-			if ( lane == 0 )
+			int total = 0;
+			for ( int i = 0; i < LINK_ROOTS_THREADS / 32; ++i )
 			{
+				int c = sWarp[i];
+				sWarp[i] = total;
+				total += c;
+			}
+			sWarp[LINK_ROOTS_THREADS / 32] = total;
+		}
+		__syncthreads();
+		if ( need )
+		{
+			int pos = sWarp[wid] + __popc( m & ( ( 1u << lane ) - 1u ) );
+			sK[pos] = k;
+			sA[pos] = idA;
+			sB[pos] = idB;
+		}
+		__syncthreads();
+		if ( tid == 0 )
+		{
+			int cnt = sWarp[LINK_ROOTS_THREADS / 32];
+			for ( int i = 0; i < cnt; ++i )
+			{
+				int a = sA[i], b = sB[i];
 				int rootA = a != ISL_NULL ? isl_root( I, a ) : ISL_NULL;
 				int rootB = b != ISL_NULL ? isl_root( I, b ) : ISL_NULL;
 				if ( rootA != rootB && rootA != ISL_NULL && rootB != ISL_NULL )
 					I.islands[rootB].parent = rootA;
-				I.order[base + src] = rootA != ISL_NULL ? rootA : rootB;
+				I.order[sK[i]] = rootA != ISL_NULL ? rootA : rootB;
 			}
-			__syncwarp();
 		}
+		__syncthreads();
 	}
 }
 
@@ -1668,7 +1694,7 @@ void launch_isl_ops( DWorld& w, StepScratch& s, cudaStream_t st, const int* gkin
 	int* flag = s.tmpA + w.opCap;
 	int* pos = s.tmpB;
 	k_isl_link_flags<<<g, 256, 0, st>>>( w, w.isl, flag );
-	k_isl_link_roots<<<1, 32, 0, st>>>( w, w.isl );
+	k_isl_link_roots<<<1, LINK_ROOTS_THREADS, 0, st>>>( w, w.isl );
 	scan_lookback( flag, pos, &w.sc->opCount, 0, w.opCap, nullptr, scanState, &w.sc->error, st );
 	k_isl_link_keys<<<g, 256, 0, st>>>( w, w.isl, flag, pos );
 	int islandBits = 1;
