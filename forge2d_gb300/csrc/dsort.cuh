@@ -116,13 +116,85 @@ __global__ void __launch_bounds__( CSORT_THREADS )
 	const int lo = min( n, blockIdx.x * per ), hi = min( n, lo + per );
 	const int lane = tid & 31, warp = tid >> 5;
 	const int passes = ( bits + 7 ) / 8;
+	// A digit every row shares needs no pass (a stable pass over it keeps
+	// the order): the OR and the AND of all keys, one word pair per block in
+	// the histogram buffer's last rows, which the histograms of at most
+	// CSORT_MAX_BLOCKS - 4 blocks never reach.
+	unsigned long long diff = ~0ull;
+	if ( G <= CSORT_MAX_BLOCKS - 4 )
+	{
+		__shared__ unsigned long long sOr, sAnd;
+		unsigned long long o = 0ull, a = ~0ull;
+		for ( int i = lo + tid; i < hi; i += CSORT_THREADS )
+		{
+			unsigned long long k = (unsigned long long)__ldcg( keys + i );
+			o |= k;
+			a &= k;
+		}
+#pragma unroll
+		for ( int off = 16; off > 0; off >>= 1 )
+		{
+			o |= __shfl_xor_sync( 0xffffffffu, o, off );
+			a &= __shfl_xor_sync( 0xffffffffu, a, off );
+		}
+		if ( tid == 0 )
+		{
+			sOr = 0ull;
+			sAnd = ~0ull;
+		}
+		__syncthreads();
+		if ( lane == 0 )
+		{
+			atomicOr( &sOr, o );
+			atomicAnd( &sAnd, a );
+		}
+		__syncthreads();
+		unsigned long long* part = (unsigned long long*)( hist + 256 * ( CSORT_MAX_BLOCKS - 4 ) );
+		if ( tid == 0 )
+		{
+			__stcg( part + 2 * blockIdx.x, sOr );
+			__stcg( part + 2 * blockIdx.x + 1, sAnd );
+		}
+		if ( !grid_barrier( counter, err, epoch ) )
+			return;
+		if ( tid == 0 )
+		{
+			sOr = 0ull;
+			sAnd = ~0ull;
+		}
+		__syncthreads();
+		o = 0ull;
+		a = ~0ull;
+		for ( int b = tid; b < G; b += CSORT_THREADS )
+		{
+			o |= __ldcg( part + 2 * b );
+			a &= __ldcg( part + 2 * b + 1 );
+		}
+#pragma unroll
+		for ( int off = 16; off > 0; off >>= 1 )
+		{
+			o |= __shfl_xor_sync( 0xffffffffu, o, off );
+			a &= __shfl_xor_sync( 0xffffffffu, a, off );
+		}
+		if ( lane == 0 )
+		{
+			atomicOr( &sOr, o );
+			atomicAnd( &sAnd, a );
+		}
+		__syncthreads();
+		diff = sOr ^ sAnd;
+	}
 	K* kin = keys;
 	int* vin = vals;
 	K* kout = keysAlt;
 	int* vout = valsAlt;
+	int done = 0;
 	for ( int p = 0; p < passes; ++p )
 	{
 		const int shift = 8 * p;
+		if ( ( ( diff >> shift ) & 0xffull ) == 0ull )
+			continue;
+		done += 1;
 		// 1. digit histogram of this block's rows
 		if ( tid < 256 )
 			sm.radix.base[tid] = 0;
@@ -211,7 +283,7 @@ __global__ void __launch_bounds__( CSORT_THREADS )
 		vin = vout;
 		vout = tv;
 	}
-	if ( passes & 1 )
+	if ( done & 1 )
 	{
 		// the rows ended in the alternate buffers: copy this block's range back
 		for ( int i = lo + tid; i < hi; i += CSORT_THREADS )
