@@ -347,122 +347,39 @@ __device__ __forceinline__ bool registered( int ta, int tb, bool* primary )
 	return false;
 }
 
-// The querying proxy's rows a candidate test reads, loaded once per query.
-struct PairQuery
-{
-	int si, fi, typeI, keyI, bi, groupI, subI, bflagsI, jointsI, headJointI;
-	unsigned long long catI, maskI;
-};
-
-__device__ __forceinline__ PairQuery pair_query( const DWorld& w, int si, int fi )
-{
-	PairQuery q;
-	q.si = si;
-	q.fi = fi;
-	q.keyI = w.proxyKey[si];
-	q.typeI = q.keyI & 3;
-	q.bi = w.shapeBody[si];
-	q.groupI = w.group[si];
-	q.catI = w.cat[si];
-	q.maskI = w.mask[si];
-	q.subI = w.subCount > 0 ? w.shapeSub[si] : 0;
-	q.bflagsI = w.bflags[q.bi];
-	q.jointsI = w.jointCountB[q.bi];
-	q.headJointI = w.headJoint[q.bi];
-	return q;
-}
-
 // Candidate pair (si moved, sj its overlapping leaf): the filters of
 // b2PairQueryCallback (broad_phase.c:160-266) and the pair-set lookup. A
 // pair whose proxies both moved belongs to one query in the reference: the
 // smaller proxy key's when both are dynamic, else the dynamic proxy's (a
 // static or kinematic proxy queries the dynamic tree only and skips moved
-// proxies there). The candidate's rows and the first probe of the pair hash
-// are loaded together before the filters read them (the same tests in the
-// same order; only the loads move ahead).
-__device__ __forceinline__ void test_pair( const DWorld& w, const PairQuery& q, int sj )
+// proxies there).
+__device__ __forceinline__ void test_pair( const DWorld& w, int si, int fi, int typeI, int bi, int sj )
 {
-	const int si = q.si, fi = q.fi, typeI = q.typeI, bi = q.bi;
-	if ( sj == si )
+	if ( sj == si || ( w.subCount > 0 && w.shapeSub[si] != w.shapeSub[sj] ) )
 		return;
-	const unsigned long long pk = pair_key( si, sj );
-	const unsigned hm = (unsigned)w.hashCap - 1u;
-	unsigned h = hash64( pk ) & hm;
-	const unsigned long long probe0 = w.pairHash[h];
-	const int fj = w.sflags[sj];
-	const int keyJ = w.proxyKey[sj];
-	const unsigned long long catJ = w.cat[sj], maskJ = w.mask[sj];
-	const int groupJ = w.group[sj];
-	const int bj = w.shapeBody[sj];
-	const int subJ = w.subCount > 0 ? w.shapeSub[sj] : 0;
-	const int bflagsJ = w.bflags[bj];
-	if ( w.subCount > 0 && q.subI != subJ )
-		return;
+	int fj = w.sflags[sj];
+	int keyI = w.proxyKey[si], keyJ = w.proxyKey[sj];
 	int typeJ = keyJ & 3;
 	if ( typeI != 2 && typeJ != 2 )
 		return;
 	if ( fj & SF_MOVED )
 	{
-		if ( typeI == 2 && typeJ == 2 ? keyJ < q.keyI : typeI != 2 )
+		if ( typeI == 2 && typeJ == 2 ? keyJ < keyI : typeI != 2 )
 			return; // created by sj's query
 	}
 	// dynamic_tree.c:1140: a leaf of category zero is never visited
-	if ( catJ == 0ull )
+	if ( w.cat[sj] == 0ull )
 		return;
 	bool primaryUnused;
 	if ( !registered( shape_type( fi ), shape_type( fj ), &primaryUnused ) )
 		return; // no manifold function: b2CreateContact makes no contact
+	int bj = w.shapeBody[sj];
 	if ( bj == bi || ( fi & SF_SENSOR ) || ( fj & SF_SENSOR ) )
 		return;
-	// shape.h:122-130 b2ShouldShapesCollide
-	if ( q.groupI == groupJ && q.groupI != 0 )
-	{
-		if ( q.groupI <= 0 )
-			return;
-	}
-	else if ( ( q.maskI & catJ ) == 0ull || ( q.catI & maskJ ) == 0ull )
+	if ( !shapes_collide( w, si, sj ) || !bodies_collide( w, bi, bj ) )
 		return;
-	// body.c:1861-1897 b2ShouldBodiesCollide
-	if ( body_type( q.bflagsI ) != 2 && body_type( bflagsJ ) != 2 )
+	if ( hash_contains( w, pair_key( si, sj ) ) )
 		return;
-	{
-		int jointsJ = w.jointCountB[bj];
-		int key, other;
-		if ( q.jointsI < jointsJ )
-		{
-			key = q.headJointI;
-			other = bj;
-		}
-		else
-		{
-			key = w.headJoint[bj];
-			other = bi;
-		}
-		for ( int guard = 0; key != F2D_NULL && guard < ( 1 << 20 ); ++guard )
-		{
-			int jid = key >> 1;
-			int edge = key & 1;
-			int2 jb = w.jbody[jid];
-			int otherBody = edge == 0 ? jb.y : jb.x;
-			if ( ( w.jflags[jid] & 0x10 ) == 0 && otherBody == other )
-				return;
-			key = w.jnext[2 * jid + edge];
-		}
-	}
-	// the pair set (hash_contains, its first probe already loaded)
-	{
-		const unsigned long long k1 = pk + 1ull;
-		unsigned long long v = probe0;
-		for ( int probe = 0; probe < w.hashCap; ++probe )
-		{
-			if ( v == 0ull )
-				break;
-			if ( v == k1 )
-				return;
-			h = ( h + 1u ) & hm;
-			v = w.pairHash[h];
-		}
-	}
 	int slot = atomicAdd( &w.sc->newPairCount, 1 );
 	if ( slot < w.pairCap )
 	{
@@ -503,8 +420,9 @@ __global__ void __launch_bounds__( BP_THREADS ) k_find_pairs( DWorld w )
 		int fi = w.sflags[si];
 		if ( ( fi & SF_MOVED ) == 0 )
 			continue;
-		const PairQuery pq = pair_query( w, si, fi );
+		int typeI = w.proxyKey[si] & 3;
 		fbox q = box_from4( w.fat[si] );
+		int bi = w.shapeBody[si];
 		// stack entries: level << 26 | node
 		int sp = 1;
 		if ( lane == 0 )
@@ -529,7 +447,7 @@ __global__ void __launch_bounds__( BP_THREADS ) k_find_pairs( DWorld w )
 			if ( level == 1 )
 			{
 				if ( ov )
-					test_pair( w, pq, w.leafShape[child] );
+					test_pair( w, si, fi, typeI, bi, w.leafShape[child] );
 			}
 			else
 			{
