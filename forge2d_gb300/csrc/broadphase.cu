@@ -655,6 +655,25 @@ void launch_broadphase( DWorld& w, StepScratch& s, cudaStream_t st, int planMode
 	sort_coop<unsigned long long>( w.pairKeys, w.pairVal, w.pairKeysAlt, w.pairValAlt, &w.sc->newPairCount, bits,
 								   w.sortHist, &w.sc->barrierCount, &w.sc->error, s.sortBlocks64, st );
 	launch_pt_decode( w, st );
+	// world.c:488-502: the dynamic and kinematic trees are rebuilt over
+	// their enlarged nodes every step, once the new pairs have their tree
+	// ranks, beside the rest of the collide phase (as the reference's rebuild
+	// task runs beside its collide tasks); nothing until the solver reads or
+	// writes them, and the world joins the rebuild's stream before its
+	// persistent cooperative solver, which needs the whole GPU
+	if ( s.rebuild )
+	{
+		cudaEventRecord( s.rebuildFork, st );
+		cudaStreamWaitEvent( s.rebuild, s.rebuildFork, 0 );
+		if ( s.rebuildT0 )
+			cudaEventRecord( s.rebuildT0, s.rebuild );
+		launch_pt_rebuild( w, s, s.rebuild );
+		if ( s.rebuildT1 )
+			cudaEventRecord( s.rebuildT1, s.rebuild );
+		cudaEventRecord( s.rebuildJoin, s.rebuild );
+	}
+	else
+		launch_pt_rebuild( w, s, st );
 	// broad_phase.c:267-278: the custom filter sees the new pairs last
 	if ( pairHook )
 		pairHook( hookContext );

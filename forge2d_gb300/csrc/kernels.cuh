@@ -42,6 +42,10 @@ struct StepScratch
 	// (the manifold classes), with their fork and join events
 	cudaStream_t side[4];
 	cudaEvent_t sideFork, sideJoin[4];
+	// the tree rebuild's stream, its fork and join, and (profiling only,
+	// else null) the events around it
+	cudaStream_t rebuild;
+	cudaEvent_t rebuildFork, rebuildJoin, rebuildT0, rebuildT1;
 };
 
 // solver variants: same arithmetic, different launch shapes

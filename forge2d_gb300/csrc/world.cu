@@ -1146,6 +1146,10 @@ extern "C" F2D_API int32_t f2d_create_world( const f2d_world_def* def )
 	cudaEventCreate( &W->evStop );
 	cudaEventCreateWithFlags( &W->evFork, cudaEventDisableTiming );
 	cudaEventCreateWithFlags( &W->evJoin, cudaEventDisableTiming );
+	W->s.rebuild = W->stream2;
+	W->s.rebuildFork = W->evFork;
+	W->s.rebuildJoin = W->evJoin;
+	W->s.rebuildT0 = W->s.rebuildT1 = nullptr;
 	cudaEventCreateWithFlags( &W->s.sideFork, cudaEventDisableTiming );
 	for ( int k = 0; k < 4; ++k )
 	{
@@ -3718,27 +3722,17 @@ static void enqueue_step( HostWorld* W, float dt, int subSteps, int planMode )
 	if ( prof )
 		cudaEventRecord( W->ph[0], W->stream );
 	bool filter = W->customFilter != nullptr, pre = W->preSolve != nullptr;
+	W->s.rebuildT0 = prof ? W->ph[7] : nullptr;
+	W->s.rebuildT1 = prof ? W->ph[8] : nullptr;
+	// the tree rebuild forks onto its own stream inside the broadphase
 	launch_broadphase( d, W->s, W->stream, planMode, filter ? pair_filter_hook : nullptr, W );
-	// world.c:488-502: the dynamic and kinematic trees are rebuilt over
-	// their enlarged nodes every step, beside the collide phase as the
-	// reference's rebuild task runs beside the collide tasks; nothing until
-	// the solver reads or writes them. The join comes before the solver: its
-	// persistent cooperative kernel needs the whole GPU.
-	cudaEventRecord( W->evFork, W->stream );
-	cudaStreamWaitEvent( W->stream2, W->evFork, 0 );
-	if ( prof )
-		cudaEventRecord( W->ph[7], W->stream2 );
-	launch_pt_rebuild( d, W->s, W->stream2 );
-	if ( prof )
-		cudaEventRecord( W->ph[8], W->stream2 );
-	cudaEventRecord( W->evJoin, W->stream2 );
 	if ( prof )
 		cudaEventRecord( W->ph[1], W->stream );
 	launch_narrowphase( d, W->s, W->stream, pre ? pre_solve_hook : nullptr, W );
 	if ( prof )
 		cudaEventRecord( W->ph[2], W->stream );
 	launch_graph( d, W->s, W->stream );
-	cudaStreamWaitEvent( W->stream, W->evJoin, 0 );
+	cudaStreamWaitEvent( W->stream, W->s.rebuildJoin, 0 );
 	if ( prof )
 		cudaEventRecord( W->ph[3], W->stream );
 	launch_solver( d, W->s, W->stream, dt, subSteps );
