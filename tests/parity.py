@@ -186,7 +186,10 @@ def type_script(world, f):
         80: [("body_set_type", 100, 0)],     # static between two dynamic links
         85: [("body_set_type", 101, 0)],     # its neighbour too: a joint between statics
         95: [("body_set_type", 101, 2)],     # static -> dynamic: one joint re-coloured, one from the static set
+        100: [("body_set_type", 20, 1)],     # a box of a sleeping pyramid (with sleeping on) turns kinematic
+        105: [("body_disable", 50)],         # a box of the other sleeping pyramid is disabled
         110: [("body_disable", 106)],        # a static anchor with a joint
+        112: [("body_enable", 50), ("body_set_type", 20, 2)],
         120: [("body_enable", 106), ("body_set_type", 30, 2)],
         130: [("body_disable", 40), ("body_set_type", 60, 0)],
         135: [("body_enable", 40), ("body_set_type", 60, 2)],
